@@ -1,0 +1,93 @@
+"""Generate asm-free copies of two reference translation units for the Linux
+build of the reference pipeline core (oracle/_ref).  TEST INFRASTRUCTURE ONLY.
+
+The reference's interp.cpp and fbo.cpp each contain MSVC 32-bit ``__asm{}``
+blocks, which GCC cannot compile.  This script reads the two files from the
+read-only reference tree and writes copies into the build output directory
+(never into the repository) in which each ``__asm{...}`` block is replaced by
+SSE intrinsics issuing the same operations:
+
+* interp.cpp ``interpolateStartAndStep`` (reference interp.cpp:55-66): two
+  haddps reductions of the left/right corrected contributions; lane 0 of the
+  left and lane 2 of the right are stored to ``temp``.
+* fbo.cpp ``clear16`` / ``clearToZero`` (reference fbo.cpp:348-393): fill
+  m_bytes/16 16-byte slots of m_buffer with the given vector / zero.
+
+Everything else in both files is left byte-for-byte unchanged.  Each block is
+matched by its own instruction text so that a different reference revision
+fails loudly instead of silently compiling something else.
+
+Usage: python patch_asm.py <reference src/puresoft3d dir> <output dir>
+"""
+import os
+import re
+import sys
+
+INTERP_REPL = """{
+\t\t__m128 l = _mm_loadu_ps(correctedContributesForLeft);
+\t\tl = _mm_hadd_ps(l, l);
+\t\tl = _mm_hadd_ps(l, l);
+\t\t__m128 r = _mm_loadu_ps(correctedContributesForLeft + 4);
+\t\tr = _mm_hadd_ps(r, r);
+\t\tr = _mm_hadd_ps(r, r);
+\t\t_mm_storeu_ps(temp, _mm_move_ss(r, l));
+\t}"""
+
+CLEAR16_REPL = """{
+\t\t__m128 v = _mm_loadu_ps((const float*)dataAligned16Bytes);
+\t\tchar* d = (char*)m_buffer;
+\t\tfor(size_t i = 0; i < m_bytes / 16; i++) _mm_storeu_ps((float*)(d + 16 * i), v);
+\t}"""
+
+CLEARZERO_REPL = """{
+\t\t__m128 v = _mm_setzero_ps();
+\t\tchar* d = (char*)m_buffer;
+\t\tfor(size_t i = 0; i < m_bytes / 16; i++) _mm_storeu_ps((float*)(d + 16 * i), v);
+\t}"""
+
+
+def _asm_blocks(text):
+    """Yield (start, end) spans of every ``__asm{ ... }`` block (no nesting)."""
+    for m in re.finditer(r"__asm\s*\{", text):
+        end = text.index("}", m.end())
+        yield m.start(), end + 1
+
+
+def _patch(text, expect):
+    """Replace asm blocks in order; ``expect`` is a list of (needles, repl)."""
+    spans = list(_asm_blocks(text))
+    if len(spans) != len(expect):
+        raise SystemExit("unexpected number of __asm blocks: %d" % len(spans))
+    out, pos = [], 0
+    for (s, e), (needles, repl) in zip(spans, expect):
+        body = text[s:e]
+        for n in needles:
+            if n not in body:
+                raise SystemExit("asm block does not contain %r" % n)
+        out.append(text[pos:s])
+        out.append(repl)
+        pos = e
+    out.append(text[pos:])
+    return "".join(out)
+
+
+def main(src_dir, out_dir):
+    os.makedirs(out_dir, exist_ok=True)
+    with open(os.path.join(src_dir, "interp.cpp"), encoding="latin-1") as f:
+        interp = f.read()
+    interp = _patch(interp, [(["haddps", "movss\txmm1,\txmm0", "[eax + 16]"], INTERP_REPL)])
+    interp = "#include <pmmintrin.h>\n" + interp
+    with open(os.path.join(out_dir, "interp.cpp"), "w", encoding="latin-1") as f:
+        f.write(interp)
+
+    with open(os.path.join(src_dir, "fbo.cpp"), encoding="latin-1") as f:
+        fbo = f.read()
+    fbo = _patch(fbo, [(["movaps\txmm0,\t[eax]", "loop\tlup"], CLEAR16_REPL),
+                       (["xorps\txmm0, xmm0", "loop\tlup"], CLEARZERO_REPL)])
+    fbo = "#include <pmmintrin.h>\n" + fbo
+    with open(os.path.join(out_dir, "fbo.cpp"), "w", encoding="latin-1") as f:
+        f.write(fbo)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1], sys.argv[2])

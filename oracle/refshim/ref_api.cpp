@@ -1,0 +1,254 @@
+/*
+ * ref_api.cpp -- a C entry surface over the reference's own PuresoftPipeline
+ * (compiled unmodified from the reference sources), so that Python test code
+ * can replay a scene on it and read back colour and depth.  TEST
+ * INFRASTRUCTURE ONLY: it builds into oracle/_ref/libps3dref.so, which exists
+ * only where the reference sources are present, and is used to generate and
+ * check golden fixtures.
+ *
+ * Every ps3dr_* call forwards to the PuresoftPipeline method of the same
+ * meaning (reference pipeline.h:26-69).  C++ exceptions are turned into the
+ * status codes the product's C ABI uses: -1 std::out_of_range,
+ * -2 std::invalid_argument, -3 std::bad_alloc.
+ *
+ * Colour: the pipeline draws into a headless renderer's buffer (a stand-in for
+ * the GDI back buffer, reference rndrgdi.cpp).  Its memory layout is the
+ * reference display FBO's: BGRA8, top-down (memory row = H - 1 - y,
+ * pipeline.cpp:48, fbo.cpp:103-106).
+ */
+#include <string.h>
+#include <stdexcept>
+#include <new>
+#include "pipeline.h"
+#include "defproc.h"
+#include "cfgproc.h"
+
+int logicCPUs(void); /* refshim/win32_runtime.cpp */
+
+namespace {
+
+class HeadlessRenderer : public PuresoftRenderer
+{
+public:
+    void startup(uintptr_t, int width, int height)
+    {
+        m_width = width;
+        m_height = height;
+        m_buffer = (uint8_t*)_aligned_malloc((size_t)width * 4 * height, 64);
+        memset(m_buffer, 0, (size_t)width * 4 * height);
+    }
+    void shutdown(void) {}
+    void setCanvas(uintptr_t) {}
+    void getDesc(PURESOFTIMGBUFF32* desc)
+    {
+        desc->width = m_width;
+        desc->scanline = m_width * 4;
+        desc->height = m_height;
+        desc->elemLen = 4;
+        desc->pixels = m_buffer;
+    }
+    void* swapBuffers(void) { return m_buffer; }
+    void release(void)
+    {
+        _aligned_free(m_buffer);
+        delete this;
+    }
+    uint8_t* m_buffer = nullptr;
+    int m_width = 0, m_height = 0;
+};
+
+struct RefCtx {
+    PuresoftPipeline* pipe;
+    HeadlessRenderer* rndr;
+    int width, height;
+};
+
+template <class F> int guarded(F f)
+{
+    try {
+        return f();
+    } catch (const std::out_of_range&) {
+        return -1;
+    } catch (const std::invalid_argument&) {
+        return -2;
+    } catch (const std::bad_alloc&) {
+        return -3;
+    }
+}
+
+PuresoftProcessor* make_processor(int id)
+{
+    switch (id) {
+    case 0x0101: return new VertexProcesserDEF01;
+    case 0x0102: return new InterpolationProcessorDEF01;
+    case 0x0103: return new FragmentProcessorDEF01;
+    case 0x0501: return new VertexProcesserDEF05;
+    case 0x0502: return new InterpolationProcessorDEF05;
+    case 0x0503: return new FragmentProcessorDEF05;
+    case 0x0601: return new VertexProcesserSHADOW;
+    case 0x1103: return new FragmentProcessorLIT1;
+    case 0x1303: return new FragmentProcessorLIT3;
+    case 0x1201: return new VertexProcesserLIT2;
+    case 0x1202: return new InterpolationProcessorLIT2;
+    case 0x1203: return new FragmentProcessorLIT2;
+    default: return nullptr;
+    }
+}
+
+} // namespace
+
+extern "C" {
+
+void* ps3dr_create(int width, int height)
+{
+    RefCtx* c = new RefCtx();
+    c->rndr = new HeadlessRenderer();
+    c->rndr->startup(0, width, height);
+    c->pipe = new PuresoftPipeline(0, width, height, c->rndr);
+    c->width = width;
+    c->height = height;
+    return c;
+}
+
+void ps3dr_destroy(void* h)
+{
+    RefCtx* c = (RefCtx*)h;
+    delete c->pipe; /* releases the renderer */
+    delete c;
+}
+
+int ps3dr_thread_count(void) { return logicCPUs(); }
+
+int ps3dr_texture_create(void* h, int width, int height, int scanline, int elemLen, const void* pixels, int wrap)
+{
+    RefCtx* c = (RefCtx*)h;
+    return guarded([&] {
+        PURESOFTIMGBUFF32 img;
+        img.width = width;
+        img.height = height;
+        img.scanline = scanline;
+        img.elemLen = elemLen;
+        img.pixels = (void*)pixels;
+        return c->pipe->createTexture(&img, 0, wrap ? PuresoftFBO::WRAP : PuresoftFBO::CLAMP);
+    });
+}
+
+int ps3dr_texture_read(void* h, int idx, void* out, size_t bytes)
+{
+    RefCtx* c = (RefCtx*)h;
+    return guarded([&] {
+        PURESOFTIMGBUFF32 img;
+        c->pipe->getTexture(idx, &img);
+        size_t n = (size_t)img.scanline * img.height;
+        memcpy(out, img.pixels, n < bytes ? n : bytes);
+        return 0;
+    });
+}
+
+int ps3dr_processor_add(void* h, int id)
+{
+    RefCtx* c = (RefCtx*)h;
+    PuresoftProcessor* p = make_processor(id);
+    if (!p) return -2;
+    return c->pipe->addProcessor(p);
+}
+
+int ps3dr_programme_create(void* h, int vid, int iid, int fid)
+{
+    RefCtx* c = (RefCtx*)h;
+    return guarded([&] { return c->pipe->createProgramme(vid, iid, fid); });
+}
+
+int ps3dr_programme_use(void* h, int idx)
+{
+    RefCtx* c = (RefCtx*)h;
+    return guarded([&] {
+        c->pipe->useProgramme(idx);
+        return 0;
+    });
+}
+
+int ps3dr_vao_create(void* h) { return ((RefCtx*)h)->pipe->createVAO(); }
+
+int ps3dr_vbo_attach(void* h, int vao, int slot, int unitBytes, int count, const void* data)
+{
+    RefCtx* c = (RefCtx*)h;
+    return guarded([&] {
+        PuresoftVBO* vbo = new PuresoftVBO(unitBytes, count);
+        vbo->updateContent(data);
+        PuresoftVBO* old = c->pipe->attachVBO(vao, slot, vbo);
+        delete old;
+        return 0;
+    });
+}
+
+int ps3dr_set_uniform(void* h, int idx, const void* data, size_t len)
+{
+    RefCtx* c = (RefCtx*)h;
+    return guarded([&] {
+        c->pipe->setUniform(idx, data, len);
+        return 0;
+    });
+}
+
+int ps3dr_set_depth(void* h, int idx)
+{
+    RefCtx* c = (RefCtx*)h;
+    return guarded([&] {
+        c->pipe->setDepth(idx);
+        return 0;
+    });
+}
+
+int ps3dr_set_viewport(void* h, int width, int height)
+{
+    ((RefCtx*)h)->pipe->setViewport(width, height);
+    return 0;
+}
+
+int ps3dr_enable(void* h, int bits)
+{
+    ((RefCtx*)h)->pipe->enable(bits);
+    return 0;
+}
+
+int ps3dr_disable(void* h, int bits)
+{
+    ((RefCtx*)h)->pipe->disable(bits);
+    return 0;
+}
+
+int ps3dr_clear_depth(void* h, float v)
+{
+    ((RefCtx*)h)->pipe->clearDepth(v);
+    return 0;
+}
+
+/* The reference's clearColour skips the last memory row of the display
+   (fbo.cpp:332-346 loops y < m_height - 1).  The harness completes that row
+   so that a clear means "every pixel", which is what the product does. */
+int ps3dr_clear_colour(void* h, uint32_t bgra)
+{
+    RefCtx* c = (RefCtx*)h;
+    PURESOFTBGRA v;
+    v.i32 = bgra;
+    c->pipe->clearColour(v);
+    uint32_t* last = (uint32_t*)(c->rndr->m_buffer + (size_t)(c->height - 1) * c->width * 4);
+    for (int x = 0; x < c->width; x++) last[x] = bgra;
+    return 0;
+}
+
+int ps3dr_draw(void* h, int vao)
+{
+    ((RefCtx*)h)->pipe->drawVAO(vao, false);
+    return 0;
+}
+
+int ps3dr_read_colour(void* h, void* out)
+{
+    RefCtx* c = (RefCtx*)h;
+    memcpy(out, c->rndr->m_buffer, (size_t)c->width * 4 * c->height);
+    return 0;
+}
+
+} /* extern "C" */

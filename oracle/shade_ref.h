@@ -1,0 +1,333 @@
+/*
+ * shade_ref.h -- CPU definition of the shading and sampling used by the
+ * benchmark scenes.  TEST INFRASTRUCTURE: included only by the oracle port
+ * (ps3d_oracle.c) and by the config processors of the reference build
+ * (refshim/cfgproc.cpp).  The product (puresoft3d_gb300/csrc) has its own,
+ * independent CUDA implementation that is checked against this one.
+ *
+ * The reference (CallMeZhou/Puresoft3D) samples textures nearest-only
+ * (src/puresoft3d/samplr2d.cpp:19-25) and has no mipmaps, no bilinear, no
+ * PCF and no directional light.  The scene shaders are therefore new plugins
+ * written against the reference's processor API (src/puresoft3d/proc.h:26-71).
+ * They keep the reference's texel addressing rules:
+ *   - texel i is centred on coordinate i: the nearest sampler reads
+ *     (unsigned)(size * t + 0.5f)  (samplr2d.cpp:19-25);
+ *   - WRAP maps an index i to i % (size - 1), plus (size - 1) when negative
+ *     (fbo.cpp:580-591) -- the modulus is size - 1, so texel size-1 is never
+ *     read; CLAMP clamps to [0, size - 1] (fbo.cpp:556-579);
+ *   - texture rows are stored bottom-up from the FBO base (topDown = false,
+ *     tex.cpp:17, fbo.cpp:103-106).
+ * Every float operation below is IEEE single precision, evaluated in the
+ * written order with no FMA contraction (compile with -ffp-contract=off).
+ */
+#ifndef PS3D_SHADE_REF_H
+#define PS3D_SHADE_REF_H
+
+#include <stdint.h>
+#include <string.h>
+#include <math.h>
+#include <limits.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* x86 cvttss2si: truncation toward zero; NaN and out-of-range give INT_MIN.
+   The reference's (int) casts compile to this instruction on x86; spelling it
+   out keeps the oracle's results identical on hosts whose float->int cast
+   saturates instead (AArch64). */
+static inline int sr_f2i(float x)
+{
+    if (x >= -2147483648.0f && x < 2147483648.0f) return (int)x;
+    return INT_MIN;
+}
+
+/* GCC x86-64 (unsigned int)(float): converts through a 64-bit signed
+   truncation and keeps the low 32 bits; NaN / |x| >= 2^63 give 0.  Used by
+   the reference samplers (samplr2d.cpp:19-25, samplrproj.cpp:29-30). */
+static inline unsigned int sr_f2u(float x)
+{
+    if (x >= -9223372036854775808.0f && x < 9223372036854775808.0f) return (unsigned int)(uint64_t)(int64_t)x;
+    return 0u;
+}
+
+static inline float sr_u2f(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
+static inline uint32_t sr_f2bits(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
+
+/* IEEE half -> float (exact). */
+static inline float sr_half2float(uint16_t h)
+{
+    uint32_t s = (uint32_t)(h & 0x8000u) << 16, e = (h >> 10) & 0x1fu, m = h & 0x3ffu, bits;
+    if (e == 0) {
+        if (m == 0) bits = s;
+        else {
+            e = 113;
+            while (!(m & 0x400u)) { m <<= 1; e--; }
+            bits = s | (e << 23) | ((m & 0x3ffu) << 13);
+        }
+    } else if (e == 31) bits = s | 0x7f800000u | (m << 13);
+    else bits = s | ((e + 112u) << 23) | (m << 13);
+    return sr_u2f(bits);
+}
+
+/* Reference WRAP addressing (fbo.cpp:580-591) with modulus size-1; a 1-texel
+   dimension (modulus 0, undefined in the reference) maps to index 0. */
+static inline int sr_wrap(int i, int size)
+{
+    int m = size - 1, r;
+    if (m <= 0) return 0;
+    r = i % m;
+    if (r < 0) r += m;
+    return r;
+}
+
+static inline int sr_clampi(int i, int size)
+{
+    return i < 0 ? 0 : (i > size - 1 ? size - 1 : i);
+}
+
+static inline float sr_dot3(const float* a, const float* b) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+
+/* v /= |v| as v * (1 / sqrt(v.v)); a zero vector stays zero. */
+static inline void sr_normalize3(float* v)
+{
+    float s = sr_dot3(v, v), r;
+    if (!(s > 0.0f)) { v[0] = v[1] = v[2] = 0.0f; return; }
+    r = 1.0f / sqrtf(s);
+    v[0] = v[0] * r;
+    v[1] = v[1] * r;
+    v[2] = v[2] * r;
+}
+
+static inline float sr_pow32(float x)
+{
+    float x2 = x * x, x4 = x2 * x2, x8 = x4 * x4, x16 = x8 * x8;
+    return x16 * x16;
+}
+
+/* Truncating 0..255 store of a shaded channel; NaN and negatives give 0. */
+static inline uint8_t sr_to_u8(float v)
+{
+    if (!(v > 0.0f)) return 0;
+    if (v > 255.0f) return 255;
+    return (uint8_t)(int)v;
+}
+
+/* A 2D texture level as the FBO stores it: row r starts at base + r*scanline. */
+typedef struct {
+    const uint8_t* base;
+    int width, height, scanline; /* scanline in bytes */
+} sr_level;
+
+/* Bilinear filter of a BGRA8 level with REPEAT (reference WRAP) addressing.
+   Sample position (W*u, H*v) in texel units, texel centres on integers. */
+static inline void sr_bilinear_bgra8(const sr_level* t, float u, float v, float out[4])
+{
+    float fx = (float)t->width * u, fy = (float)t->height * v;
+    float x0f = floorf(fx), y0f = floorf(fy);
+    float ax = fx - x0f, ay = fy - y0f;
+    int ix = sr_f2i(x0f), iy = sr_f2i(y0f);
+    int c0 = sr_wrap(ix, t->width), c1 = sr_wrap(ix + 1, t->width);
+    int r0 = sr_wrap(iy, t->height), r1 = sr_wrap(iy + 1, t->height);
+    const uint8_t* p00 = t->base + (size_t)r0 * t->scanline + 4 * c0;
+    const uint8_t* p10 = t->base + (size_t)r0 * t->scanline + 4 * c1;
+    const uint8_t* p01 = t->base + (size_t)r1 * t->scanline + 4 * c0;
+    const uint8_t* p11 = t->base + (size_t)r1 * t->scanline + 4 * c1;
+    for (int k = 0; k < 4; k++) {
+        float a = (float)p00[k], b = (float)p10[k], c = (float)p01[k], d = (float)p11[k];
+        float top = a + (b - a) * ax;
+        float bot = c + (d - c) * ax;
+        out[k] = top + (bot - top) * ay;
+    }
+}
+
+/* Same filter for an RGBA16F level (8 bytes per texel). */
+static inline void sr_bilinear_rgba16f(const sr_level* t, float u, float v, float out[4])
+{
+    float fx = (float)t->width * u, fy = (float)t->height * v;
+    float x0f = floorf(fx), y0f = floorf(fy);
+    float ax = fx - x0f, ay = fy - y0f;
+    int ix = sr_f2i(x0f), iy = sr_f2i(y0f);
+    int c0 = sr_wrap(ix, t->width), c1 = sr_wrap(ix + 1, t->width);
+    int r0 = sr_wrap(iy, t->height), r1 = sr_wrap(iy + 1, t->height);
+    const uint16_t* p00 = (const uint16_t*)(t->base + (size_t)r0 * t->scanline) + 4 * c0;
+    const uint16_t* p10 = (const uint16_t*)(t->base + (size_t)r0 * t->scanline) + 4 * c1;
+    const uint16_t* p01 = (const uint16_t*)(t->base + (size_t)r1 * t->scanline) + 4 * c0;
+    const uint16_t* p11 = (const uint16_t*)(t->base + (size_t)r1 * t->scanline) + 4 * c1;
+    for (int k = 0; k < 4; k++) {
+        float a = sr_half2float(p00[k]), b = sr_half2float(p10[k]);
+        float c = sr_half2float(p01[k]), d = sr_half2float(p11[k]);
+        float top = a + (b - a) * ax;
+        float bot = c + (d - c) * ax;
+        out[k] = top + (bot - top) * ay;
+    }
+}
+
+/* Mip selection from the distance footprint x = dist * lodScale:
+   x <= 1 (or NaN) -> level 0, weight 0; otherwise level = floor(log2 x) taken
+   from the float exponent and weight = mantissa - 1 (a piecewise-linear
+   log2), so selection is exact bit arithmetic on every host. */
+static inline void sr_mip_select(float x, int* level, float* weight)
+{
+    uint32_t bits;
+    if (!(x > 1.0f)) { *level = 0; *weight = 0.0f; return; }
+    bits = sr_f2bits(x);
+    *level = (int)((bits >> 23) & 0xffu) - 127;
+    *weight = sr_u2f((bits & 0x7fffffu) | 0x3f800000u) - 1.0f;
+}
+
+/* Trilinear blend between two bilinear taps; levels past the chain end use
+   the last level alone.  Each level is a texture object of the chain. */
+static inline void sr_trilinear(const sr_level* chain, int levels, int half16, int level, float w, float u, float v,
+                                float out[4])
+{
+    float a[4], b[4];
+    if (level >= levels - 1) {
+        if (half16) sr_bilinear_rgba16f(&chain[levels - 1], u, v, out);
+        else sr_bilinear_bgra8(&chain[levels - 1], u, v, out);
+        return;
+    }
+    if (half16) {
+        sr_bilinear_rgba16f(&chain[level], u, v, a);
+        sr_bilinear_rgba16f(&chain[level + 1], u, v, b);
+    } else {
+        sr_bilinear_bgra8(&chain[level], u, v, a);
+        sr_bilinear_bgra8(&chain[level + 1], u, v, b);
+    }
+    for (int k = 0; k < 4; k++) out[k] = a[k] + (b[k] - a[k]) * w;
+}
+
+/* 3x3 percentage-closer filter on an FP32 shadow map of size S x S (rows
+   bottom-up, CLAMP addressing).  shadowPos is the light-space clip position.
+   The map was rasterised with the reference's viewport mapping
+   x = (S/2) * ndc + S/2 (rasterizer.cpp:73-77) and pixel rounding (int)(x + 0.5f)
+   (rasterizer.cpp:100-111); a sample is lit when ndc.z - bias <= stored depth.
+   Returns the lit fraction in [0, 1]; outside the light frustum it is 1. */
+static inline float sr_pcf3x3(const float* map, int size, int scanlineFloats, const float* sp, float bias)
+{
+    float rw, nx, ny, nz, half, sx, sy;
+    int cx, cy, cnt = 0;
+    if (!(sp[3] > 0.0f)) return 1.0f;
+    rw = 1.0f / sp[3];
+    nx = sp[0] * rw;
+    ny = sp[1] * rw;
+    nz = sp[2] * rw;
+    if (!(nx >= -1.0f && nx <= 1.0f && ny >= -1.0f && ny <= 1.0f)) return 1.0f;
+    half = (float)(size / 2);
+    sx = half * nx + half;
+    sy = half * ny + half;
+    cx = sr_f2i(sx + 0.5f);
+    cy = sr_f2i(sy + 0.5f);
+    for (int dy = -1; dy <= 1; dy++)
+        for (int dx = -1; dx <= 1; dx++) {
+            int r = sr_clampi(cy + dy, size), c = sr_clampi(cx + dx, size);
+            float d = map[(size_t)r * scanlineFloats + c];
+            if (nz - bias <= d) cnt++;
+        }
+    return (float)cnt / 9.0f;
+}
+
+/* Blinn-Phong with one directional light: the colour equation shared by the
+   scene shaders.  albedo is BGRA (0..255), n the unit normal, L the unit
+   direction towards the light, E the unit direction towards the eye, vis the
+   lit fraction.  Writes BGRA8 with alpha 255. */
+static inline void sr_blinn_phong(const float albedo[4], const float* n, const float* L, const float* E, float vis,
+                                  uint8_t out[4])
+{
+    float Hv[3], ndl, ndh, spec, diff, s255;
+    Hv[0] = E[0] + L[0];
+    Hv[1] = E[1] + L[1];
+    Hv[2] = E[2] + L[2];
+    sr_normalize3(Hv);
+    ndl = sr_dot3(n, L);
+    if (ndl < 0.0f) ndl = 0.0f;
+    ndh = sr_dot3(n, Hv);
+    if (ndh < 0.0f) ndh = 0.0f;
+    spec = ndl > 0.0f ? sr_pow32(ndh) : 0.0f;
+    diff = 0.15f + 0.85f * (ndl * vis);
+    s255 = 127.5f * (spec * vis);
+    out[0] = sr_to_u8(albedo[0] * diff + s255);
+    out[1] = sr_to_u8(albedo[1] * diff + s255);
+    out[2] = sr_to_u8(albedo[2] * diff + s255);
+    out[3] = 255;
+}
+
+/* Scene shader LIT1 (configs 1 and 4): bilinear REPEAT albedo, directional
+   Lambert + Blinn-Phong (shininess 32).  Inputs are the DEF01 varyings
+   (reference tex1light1.h:4-9): normal[4], worldPos[4], texcoord[4]. */
+static inline void sr_shade_lit1(const sr_level* tex, const float* lightDir, const float* camPos, const float* normal,
+                                 const float* worldPos, const float* texcoord, uint8_t out[4])
+{
+    float albedo[4], n[3], E[3];
+    sr_bilinear_bgra8(tex, texcoord[0], texcoord[1], albedo);
+    n[0] = normal[0]; n[1] = normal[1]; n[2] = normal[2];
+    sr_normalize3(n);
+    E[0] = camPos[0] - worldPos[0];
+    E[1] = camPos[1] - worldPos[1];
+    E[2] = camPos[2] - worldPos[2];
+    sr_normalize3(E);
+    sr_blinn_phong(albedo, n, lightDir, E, 1.0f, out);
+}
+
+/* Scene shader LIT3 (config 3): LIT1 with a trilinear mip chain. */
+static inline void sr_shade_lit3(const sr_level* chain, int levels, float lodScale, const float* lightDir,
+                                 const float* camPos, const float* normal, const float* worldPos, const float* texcoord,
+                                 uint8_t out[4])
+{
+    float albedo[4], n[3], E[3], dist, w;
+    int level;
+    E[0] = camPos[0] - worldPos[0];
+    E[1] = camPos[1] - worldPos[1];
+    E[2] = camPos[2] - worldPos[2];
+    dist = sqrtf(sr_dot3(E, E));
+    sr_mip_select(dist * lodScale, &level, &w);
+    sr_trilinear(chain, levels, 0, level, w, texcoord[0], texcoord[1], albedo);
+    n[0] = normal[0]; n[1] = normal[1]; n[2] = normal[2];
+    sr_normalize3(n);
+    sr_normalize3(E);
+    sr_blinn_phong(albedo, n, lightDir, E, 1.0f, out);
+}
+
+/* Scene shader LIT2 (config 2): trilinear albedo, tangent-space normal map
+   (RGBA16F chain, same mip selection), 3x3 PCF shadow.  Varyings: normal[4],
+   tangent[4] (w = handedness), worldPos[4], texcoord[4], shadowPos[4]. */
+static inline void sr_shade_lit2(const sr_level* albedoChain, int albedoLevels, const sr_level* normalChain,
+                                 int normalLevels, const float* shadowMap, int shadowSize, int shadowScanlineFloats,
+                                 float lodScale, float shadowBias, const float* lightDir, const float* camPos,
+                                 const float* varyings, uint8_t out[4])
+{
+    const float* nrm = varyings;
+    const float* tan = varyings + 4;
+    const float* wp = varyings + 8;
+    const float* tc = varyings + 12;
+    const float* sp = varyings + 16;
+    float N[3], T[3], B[3], E[3], nts[4], albedo[4], n[3], dist, w, vis;
+    int level;
+    N[0] = nrm[0]; N[1] = nrm[1]; N[2] = nrm[2];
+    sr_normalize3(N);
+    T[0] = tan[0]; T[1] = tan[1]; T[2] = tan[2];
+    sr_normalize3(T);
+    B[0] = N[1] * T[2] - N[2] * T[1];
+    B[1] = N[2] * T[0] - N[0] * T[2];
+    B[2] = N[0] * T[1] - N[1] * T[0];
+    if (tan[3] < 0.0f) { B[0] = -B[0]; B[1] = -B[1]; B[2] = -B[2]; }
+    E[0] = camPos[0] - wp[0];
+    E[1] = camPos[1] - wp[1];
+    E[2] = camPos[2] - wp[2];
+    dist = sqrtf(sr_dot3(E, E));
+    sr_mip_select(dist * lodScale, &level, &w);
+    sr_trilinear(albedoChain, albedoLevels, 0, level, w, tc[0], tc[1], albedo);
+    sr_trilinear(normalChain, normalLevels, 1, level, w, tc[0], tc[1], nts);
+    n[0] = (T[0] * nts[0] + B[0] * nts[1]) + N[0] * nts[2];
+    n[1] = (T[1] * nts[0] + B[1] * nts[1]) + N[1] * nts[2];
+    n[2] = (T[2] * nts[0] + B[2] * nts[1]) + N[2] * nts[2];
+    sr_normalize3(n);
+    vis = sr_pcf3x3(shadowMap, shadowSize, shadowScanlineFloats, sp, shadowBias);
+    sr_normalize3(E);
+    sr_blinn_phong(albedo, n, lightDir, E, vis, out);
+}
+
+#ifdef __cplusplus
+}
+#endif
+#endif
