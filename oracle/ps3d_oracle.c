@@ -1,0 +1,1018 @@
+/*
+ * ps3d_oracle.c -- C restatement of the reference (CallMeZhou/Puresoft3D)
+ * pipeline for the per-fragment path: vertex fetch and processing, perspective
+ * divide, back-face cull, z-reject, scanline rasterisation, span set-up,
+ * perspective-correct interpolation, depth test, fragment shading, FBO write.
+ *
+ * TEST INFRASTRUCTURE ONLY (the oracle).  Loaded by tests/, by
+ * __graft_entry__.smoke() and by bench.py's CPU-baseline leg; nothing in the
+ * product calls it.
+ *
+ * It follows the reference operation by operation, in the same FP32 order
+ * (compile with -ffp-contract=off).  Parity with the reference itself is
+ * pinned by golden fixtures rendered by the reference's own sources
+ * (oracle/_ref, tests/golden).  Citations are file:line in
+ * src/puresoft3d/ or src/mcemath/ of the reference.
+ *
+ * Threads: the reference hands row y to fragment thread y % (N-1)
+ * (drawvao.cpp:77-83); each thread walks its rows' spans in submission order.
+ * Results depend only on that per-row order, so here each draw first builds
+ * the span tasks (serially, like the reference's producer thread) and then
+ * `threads` workers process rows y % threads == t in task order.
+ *
+ * Deviations (all in cases the benchmark scenes never reach):
+ *  - TEST_DEPTH without UPDATE_DEPTH: the reference never positions the depth
+ *    cursor in that mode (fragthrd.cpp:184-203) and reads a stale pixel; here
+ *    the pixel under the fragment is read.
+ *  - FragmentProcessorDEF01 uses rcpps/rsqrtss (vector.cpp:158-169,
+ *    225-250), whose results depend on the x86 model; here 1/x and 1/sqrt(x)
+ *    are IEEE.  Colour of DEF01 may differ by a few LSB; depth and coverage
+ *    are unaffected.
+ *  - Triangles with non-finite vertex coordinates make the reference index
+ *    its row table out of range (rasterizer.cpp:93-118); here they draw nothing.
+ */
+#include <math.h>
+#include <float.h>
+#include <limits.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+#include "ps3d_oracle.h"
+#include "shade_ref.h"
+
+#define MAX_VBOS 16      /* config.h:4 */
+#define MAX_UNIFORMS 1024 /* config.h:5 */
+#define MAX_VECS 8       /* float4 varyings per vertex, enough for every built-in processor */
+#define MAX_LEVELS 16
+
+#define BEHAVIOR_UPDATE_DEPTH 1 /* pipeline.h:16-19 */
+#define BEHAVIOR_TEST_DEPTH 2
+#define BEHAVIOR_FACE_CULLING 4
+#define BEHAVIOR_ALPHABLEND 8
+
+/* processor ids (include/ps3d.h) */
+enum {
+    VP_DEF01 = 0x0101, IP_DEF01 = 0x0102, FP_DEF01 = 0x0103,
+    VP_DEF05 = 0x0501, IP_DEF05 = 0x0502, FP_DEF05 = 0x0503,
+    VP_SHADOW = 0x0601,
+    FP_LIT1 = 0x1103, FP_LIT3 = 0x1303,
+    VP_LIT2 = 0x1201, IP_LIT2 = 0x1202, FP_LIT2 = 0x1203
+};
+
+typedef struct {
+    int width, height, scanline, elemLen, wrap, topDown;
+    uint8_t* buf;
+} o_fbo;
+
+typedef struct {
+    int unitBytes, count;
+    uint8_t* data;
+} o_vbo;
+
+typedef struct {
+    o_vbo* vbo[MAX_VBOS];
+} o_vao;
+
+typedef struct {
+    size_t cap;
+    void* data;
+} o_uniform;
+
+typedef struct {
+    int vp, ip, fp;
+} o_prog;
+
+typedef struct {
+    int x1, x2, y;
+    float pzStart, pzStep, cf2Start, cf2Step;
+    float user[2 * MAX_VECS * 4]; /* start vectors then step vectors */
+} o_task;
+
+typedef struct {
+    o_task* items;
+    size_t n, cap;
+} o_tasklist;
+
+struct ps3do {
+    int devW, devH;   /* device size: display and default depth */
+    int W, H;         /* rasteriser size (setViewport, pipeline.cpp:364-373) */
+    o_fbo display;    /* BGRA8, topDown (pipeline.cpp:48) */
+    o_fbo defDepth;   /* FP32, scanline rounded to 4 floats (pipeline.cpp:31) */
+    o_fbo* depth;
+    o_fbo** tex;
+    int ntex;
+    int* procs;
+    int nprocs;
+    o_prog* progs;
+    int nprogs;
+    int vp, ip, fp; /* processor ids in use, 0 = none */
+    o_vao** vaos;
+    int nvao;
+    o_uniform uni[MAX_UNIFORMS];
+    int behavior;
+    int threads;
+    o_tasklist* lists; /* one per worker */
+    long long tested, passed;
+    /* worker pool */
+    pthread_t* th;
+    pthread_mutex_t mu;
+    pthread_cond_t cv, done;
+    int gen, finished, quit;
+    void* cur_draw; /* the draw the pool is working on (guarded by gen) */
+};
+
+/* ------------------------------------------------------------------ maths */
+/* mcemaths semantics (vector.cpp, matrix.cpp): 4-wide lane-wise ops. */
+
+static void m4v4(float* r, const float* m, const float* v) /* matrix.cpp:515-557 */
+{
+    float o[4];
+    for (int i = 0; i < 4; i++) o[i] = ((v[0] * m[i] + v[1] * m[4 + i]) + v[2] * m[8 + i]) + v[3] * m[12 + i];
+    memcpy(r, o, 16);
+}
+
+static void m4m4(float* d, const float* l, const float* r) /* matrix.cpp:588-690 */
+{
+    for (int c = 0; c < 4; c++) m4v4(d + 4 * c, l, r + 4 * c);
+}
+
+static float hsum4(const float* a) { return (a[0] + a[1]) + (a[2] + a[3]); } /* haddps x2 */
+
+/* ------------------------------------------------------------ object pools */
+
+static int grow(void** arr, int n, size_t elem)
+{
+    void* q = realloc(*arr, (size_t)(n + 1) * elem);
+    if (!q) return -3;
+    *arr = q;
+    return 0;
+}
+
+static void* worker(void* arg);
+
+ps3do* ps3do_create(int width, int height, int threads)
+{
+    ps3do* p = (ps3do*)calloc(1, sizeof(ps3do));
+    if (!p) return NULL;
+    if (threads < 1) threads = 1;
+    p->devW = p->W = width;
+    p->devH = p->H = height;
+    p->display.width = width;
+    p->display.height = height;
+    p->display.scanline = width * 4;
+    p->display.elemLen = 4;
+    p->display.topDown = 1;
+    p->display.buf = (uint8_t*)calloc((size_t)width * 4 * height, 1);
+    p->defDepth.width = width;
+    p->defDepth.height = height;
+    p->defDepth.scanline = ((int)(width / 4.0f + 0.5f) * 4) * 4;
+    p->defDepth.elemLen = 4;
+    p->defDepth.buf = (uint8_t*)calloc((size_t)p->defDepth.scanline * height, 1);
+    p->depth = &p->defDepth;
+    p->behavior = BEHAVIOR_UPDATE_DEPTH | BEHAVIOR_TEST_DEPTH | BEHAVIOR_FACE_CULLING; /* pipeline.cpp:34 */
+    p->threads = threads;
+    p->lists = (o_tasklist*)calloc((size_t)threads, sizeof(o_tasklist));
+    pthread_mutex_init(&p->mu, NULL);
+    pthread_cond_init(&p->cv, NULL);
+    pthread_cond_init(&p->done, NULL);
+    if (threads > 1) {
+        p->th = (pthread_t*)calloc((size_t)threads, sizeof(pthread_t));
+        for (int i = 1; i < threads; i++) {
+            void** a = (void**)malloc(2 * sizeof(void*));
+            a[0] = p;
+            a[1] = (void*)(intptr_t)i;
+            pthread_create(&p->th[i], NULL, worker, a);
+        }
+    }
+    return p;
+}
+
+void ps3do_destroy(ps3do* p)
+{
+    if (!p) return;
+    if (p->threads > 1) {
+        pthread_mutex_lock(&p->mu);
+        p->quit = 1;
+        p->gen++;
+        pthread_cond_broadcast(&p->cv);
+        pthread_mutex_unlock(&p->mu);
+        for (int i = 1; i < p->threads; i++) pthread_join(p->th[i], NULL);
+        free(p->th);
+    }
+    for (int i = 0; i < p->ntex; i++)
+        if (p->tex[i]) { free(p->tex[i]->buf); free(p->tex[i]); }
+    free(p->tex);
+    for (int i = 0; i < p->nvao; i++)
+        if (p->vaos[i]) {
+            for (int j = 0; j < MAX_VBOS; j++)
+                if (p->vaos[i]->vbo[j]) { free(p->vaos[i]->vbo[j]->data); free(p->vaos[i]->vbo[j]); }
+            free(p->vaos[i]);
+        }
+    free(p->vaos);
+    for (int i = 0; i < MAX_UNIFORMS; i++) free(p->uni[i].data);
+    for (int i = 0; i < p->threads; i++) free(p->lists[i].items);
+    free(p->lists);
+    free(p->procs);
+    free(p->progs);
+    free(p->display.buf);
+    free(p->defDepth.buf);
+    pthread_mutex_destroy(&p->mu);
+    pthread_cond_destroy(&p->cv);
+    pthread_cond_destroy(&p->done);
+    free(p);
+}
+
+/* tex.cpp:3-25: copies pixels into a pipeline-owned FBO (topDown = false). */
+int ps3do_texture_create(ps3do* p, int width, int height, int scanline, int elemLen, const void* pixels, int wrap)
+{
+    o_fbo* f;
+    int slot = 0;
+    if (elemLen != 1 && elemLen != 4) return -2; /* fbo.cpp:21-24 */
+    if (width <= 0 || height <= 0 || scanline < width * elemLen) return -2;
+    for (; slot < p->ntex; slot++)
+        if (!p->tex[slot]) break;
+    if (slot == p->ntex) {
+        if (grow((void**)&p->tex, p->ntex, sizeof(o_fbo*))) return -3;
+        p->tex[p->ntex++] = NULL;
+    }
+    f = (o_fbo*)calloc(1, sizeof(o_fbo));
+    if (!f) return -3;
+    f->width = width;
+    f->height = height;
+    f->scanline = scanline;
+    f->elemLen = elemLen;
+    f->wrap = wrap;
+    f->buf = (uint8_t*)calloc((size_t)scanline * height, 1);
+    if (!f->buf) { free(f); return -3; }
+    if (pixels) memcpy(f->buf, pixels, (size_t)scanline * height);
+    p->tex[slot] = f;
+    return slot;
+}
+
+int ps3do_texture_read(ps3do* p, int idx, void* out, size_t bytes)
+{
+    size_t n;
+    if (idx < 0 || idx >= p->ntex || !p->tex[idx]) return -1;
+    n = (size_t)p->tex[idx]->scanline * p->tex[idx]->height;
+    memcpy(out, p->tex[idx]->buf, n < bytes ? n : bytes);
+    return 0;
+}
+
+static int known_processor(int id)
+{
+    switch (id) {
+    case VP_DEF01: case IP_DEF01: case FP_DEF01: case VP_DEF05: case IP_DEF05: case FP_DEF05:
+    case VP_SHADOW: case FP_LIT1: case FP_LIT3: case VP_LIT2: case IP_LIT2: case FP_LIT2:
+        return 1;
+    }
+    return 0;
+}
+
+static int proc_kind(int id) { return id & 0xf; } /* 1 = VP, 2 = IP, 3 = FP */
+
+int ps3do_processor_add(ps3do* p, int id) /* prog.cpp:3-20 */
+{
+    if (!known_processor(id)) return -2;
+    if (grow((void**)&p->procs, p->nprocs, sizeof(int))) return -3;
+    p->procs[p->nprocs] = id;
+    return p->nprocs++;
+}
+
+int ps3do_programme_create(ps3do* p, int vid, int iid, int fid) /* prog.cpp:43-108 */
+{
+    if (vid < 0 || vid >= p->nprocs || iid < 0 || iid >= p->nprocs || fid < 0 || fid >= p->nprocs) return -1;
+    if (grow((void**)&p->progs, p->nprogs, sizeof(o_prog))) return -3;
+    p->progs[p->nprogs].vp = vid;
+    p->progs[p->nprogs].ip = iid;
+    p->progs[p->nprogs].fp = fid;
+    return p->nprogs++;
+}
+
+int ps3do_programme_use(ps3do* p, int idx) /* prog.cpp:121-131: dynamic_cast yields NULL on a kind mismatch */
+{
+    int v, i, f;
+    if (idx < 0 || idx >= p->nprogs) return -1;
+    v = p->procs[p->progs[idx].vp];
+    i = p->procs[p->progs[idx].ip];
+    f = p->procs[p->progs[idx].fp];
+    p->vp = proc_kind(v) == 1 ? v : 0;
+    p->ip = proc_kind(i) == 2 ? i : 0;
+    p->fp = proc_kind(f) == 3 ? f : 0;
+    return 0;
+}
+
+int ps3do_vao_create(ps3do* p) /* pipeline.cpp:118-136 */
+{
+    int slot = 0;
+    for (; slot < p->nvao; slot++)
+        if (!p->vaos[slot]) break;
+    if (slot == p->nvao) {
+        if (grow((void**)&p->vaos, p->nvao, sizeof(o_vao*))) return -3;
+        p->vaos[p->nvao++] = NULL;
+    }
+    p->vaos[slot] = (o_vao*)calloc(1, sizeof(o_vao));
+    return p->vaos[slot] ? slot : -3;
+}
+
+int ps3do_vbo_attach(ps3do* p, int vao, int slot, int unitBytes, int count, const void* data)
+{
+    o_vbo* v;
+    if (vao < 0 || vao >= p->nvao || !p->vaos[vao]) return -1;
+    if (slot < 0 || slot >= MAX_VBOS) return -1;
+    v = (o_vbo*)calloc(1, sizeof(o_vbo));
+    v->unitBytes = unitBytes;
+    v->count = count;
+    v->data = (uint8_t*)malloc((size_t)unitBytes * count + 16);
+    if (data) memcpy(v->data, data, (size_t)unitBytes * count);
+    if (p->vaos[vao]->vbo[slot]) { free(p->vaos[vao]->vbo[slot]->data); free(p->vaos[vao]->vbo[slot]); }
+    p->vaos[vao]->vbo[slot] = v;
+    return 0;
+}
+
+int ps3do_set_uniform(ps3do* p, int idx, const void* data, size_t len) /* pipeline.cpp:277-312 */
+{
+    if (idx < 0 || idx >= MAX_UNIFORMS) return -1;
+    if (!data) {
+        free(p->uni[idx].data);
+        p->uni[idx].data = NULL;
+        p->uni[idx].cap = 0;
+        return 0;
+    }
+    if (p->uni[idx].cap < len) {
+        free(p->uni[idx].data);
+        p->uni[idx].data = malloc(len);
+        if (!p->uni[idx].data) return -3;
+        p->uni[idx].cap = len;
+    }
+    memcpy(p->uni[idx].data, data, len);
+    return 0;
+}
+
+int ps3do_set_depth(ps3do* p, int idx) /* pipeline.cpp:218-239 */
+{
+    if (idx == -1) { p->depth = &p->defDepth; return 0; }
+    if (idx < 0 || idx >= p->ntex || !p->tex[idx]) return -1;
+    if (p->tex[idx]->elemLen != 4 || p->tex[idx]->scanline % 4) return -2;
+    p->depth = p->tex[idx];
+    return 0;
+}
+
+int ps3do_set_viewport(ps3do* p, int width, int height)
+{
+    if (width <= 0 || height <= 0) return -2;
+    p->W = width;
+    p->H = height;
+    return 0;
+}
+
+int ps3do_enable(ps3do* p, int bits) { p->behavior |= bits; return 0; }
+int ps3do_disable(ps3do* p, int bits) { p->behavior &= ~bits; return 0; }
+
+int ps3do_clear_depth(ps3do* p, float v) /* pipeline.cpp:334-338 -> fbo.cpp clear16: every byte */
+{
+    size_t n = (size_t)p->depth->scanline * p->depth->height / 4;
+    float* d = (float*)p->depth->buf;
+    for (size_t i = 0; i < n; i++) d[i] = v;
+    return 0;
+}
+
+/* pipeline.cpp:340-343.  The reference's clear4 skips the last memory row
+   (fbo.cpp:336); a clear here covers every pixel, as the product's does. */
+int ps3do_clear_colour(ps3do* p, uint32_t bgra)
+{
+    uint32_t* d = (uint32_t*)p->display.buf;
+    for (size_t i = 0; i < (size_t)p->display.width * p->display.height; i++) d[i] = bgra;
+    return 0;
+}
+
+int ps3do_read_colour(ps3do* p, void* out)
+{
+    memcpy(out, p->display.buf, (size_t)p->display.scanline * p->display.height);
+    return 0;
+}
+
+int ps3do_read_depth(ps3do* p, void* out)
+{
+    memcpy(out, p->defDepth.buf, (size_t)p->defDepth.scanline * p->defDepth.height);
+    return 0;
+}
+
+long long ps3do_fragments_tested(ps3do* p) { return p->tested; }
+long long ps3do_fragments_passed(ps3do* p) { return p->passed; }
+
+/* ------------------------------------------------------ processors (VP/IP/FP) */
+
+static int ip_vecs(int ip)
+{
+    switch (ip) {
+    case IP_DEF01: return 3; /* PROCDATA_DEF01: normal, worldPos, texcoord (tex1light1.h:4-9) */
+    case IP_LIT2: return 5;  /* normal, tangent, worldPos, texcoord, shadowPos */
+    default: return 0;       /* IP_DEF05: no varyings (shadow.h) */
+    }
+}
+
+static const float* ufl(const ps3do* p, int i) { return (const float*)p->uni[i].data; }
+static const int* uin(const ps3do* p, int i) { return (const int*)p->uni[i].data; }
+
+/* Vertex processors.  in[j] points at this vertex's element of VBO j. */
+static void run_vp(const ps3do* p, const void* const* in, float* pos, float* user)
+{
+    switch (p->vp) {
+    case VP_DEF01: { /* tex1light1.cpp:22-41 */
+        float* nrm = user, * wp = user + 4, * tc = user + 8;
+        const float* uv = (const float*)in[4];
+        m4v4(wp, ufl(p, 4), (const float*)in[0]);
+        memcpy(pos, wp, 16);
+        wp[3] = 0;
+        m4v4(pos, ufl(p, 3), pos);
+        m4v4(nrm, ufl(p, 5), (const float*)in[3]);
+        tc[0] = uv[0];
+        tc[1] = uv[1];
+        tc[2] = tc[3] = 0.0f;
+        break;
+    }
+    case VP_DEF05: { /* shadow.cpp:21-29 */
+        float adj[4], pvm[16];
+        memcpy(adj, in[0], 16);
+        adj[0] = adj[0] * 0.9f; /* mcemaths_mul_3: three lanes (vector.cpp:517-534) */
+        adj[1] = adj[1] * 0.9f;
+        adj[2] = adj[2] * 0.9f;
+        m4m4(pvm, ufl(p, 3), ufl(p, 4));
+        m4v4(pos, pvm, adj);
+        break;
+    }
+    case VP_SHADOW: { /* DEF05 without the x0.9 scale */
+        float pvm[16];
+        m4m4(pvm, ufl(p, 3), ufl(p, 4));
+        m4v4(pos, pvm, (const float*)in[0]);
+        break;
+    }
+    case VP_LIT2: {
+        float* nrm = user, * tan = user + 4, * wp = user + 8, * tc = user + 12, * sp = user + 16;
+        const float* t = (const float*)in[1];
+        const float* uv = (const float*)in[4];
+        float t3[4] = {t[0], t[1], t[2], 0.0f};
+        m4v4(wp, ufl(p, 4), (const float*)in[0]);
+        memcpy(pos, wp, 16);
+        m4v4(sp, ufl(p, 6), wp);
+        wp[3] = 0;
+        m4v4(pos, ufl(p, 3), pos);
+        m4v4(nrm, ufl(p, 5), (const float*)in[3]);
+        m4v4(tan, ufl(p, 5), t3);
+        tan[3] = t[3];
+        tc[0] = uv[0];
+        tc[1] = uv[1];
+        tc[2] = tc[3] = 0.0f;
+        break;
+    }
+    default: break;
+    }
+}
+
+/* Interpolation processors: every reference IP is 4-wide linear algebra over
+   its float4 varyings (tex1light1.cpp:60-135), so one routine serves all. */
+static void ip_by_contributes(int nv, float* out, const float* const* vert, const float* c)
+{
+    for (int k = 0; k < nv; k++)
+        for (int l = 0; l < 4; l++) {
+            float t0 = vert[0][4 * k + l] * c[0], t1 = vert[1][4 * k + l] * c[1], t2 = vert[2][4 * k + l] * c[2];
+            out[4 * k + l] = (t0 + t1) + t2;
+        }
+}
+
+static void ip_calc_step(int nv, float* step, const float* start, const float* end, int n)
+{
+    float r = 0 == n ? 1.0f : 1.0f / (float)n;
+    for (int i = 0; i < 4 * nv; i++) step[i] = (end[i] - start[i]) * r;
+}
+
+static void ip_step_forward(int nv, float* start, const float* step, int n)
+{
+    if (1 == n)
+        for (int i = 0; i < 4 * nv; i++) start[i] = start[i] + step[i];
+    else {
+        float fn = (float)n;
+        for (int i = 0; i < 4 * nv; i++) start[i] = start[i] + step[i] * fn;
+    }
+}
+
+static sr_level level_of(const o_fbo* f)
+{
+    sr_level l;
+    l.base = f->buf;
+    l.width = f->width;
+    l.height = f->height;
+    l.scanline = f->scanline;
+    return l;
+}
+
+/* Per-draw fragment-processor state (the FP's preprocess, drawvao.cpp:18-20). */
+typedef struct {
+    const float* light;
+    const float* cam;
+    const o_fbo* tex;
+    sr_level chainA[MAX_LEVELS], chainN[MAX_LEVELS];
+    int levelsA, levelsN;
+    const float* shadow;
+    int shadowSize, shadowScan;
+    float lodScale, bias;
+} fp_state;
+
+static int fp_prepare(const ps3do* p, fp_state* s)
+{
+    memset(s, 0, sizeof *s);
+    switch (p->fp) {
+    case FP_DEF01:
+    case FP_LIT1: {
+        int t = *uin(p, 9);
+        if (t < 0 || t >= p->ntex || !p->tex[t]) return -1;
+        s->light = ufl(p, 7);
+        s->cam = ufl(p, 8);
+        s->tex = p->tex[t];
+        break;
+    }
+    case FP_LIT3:
+    case FP_LIT2: {
+        const int* a = uin(p, 9);
+        s->light = ufl(p, 7);
+        s->cam = ufl(p, 8);
+        s->levelsA = a[1] > MAX_LEVELS ? MAX_LEVELS : a[1];
+        for (int i = 0; i < s->levelsA; i++) {
+            if (a[0] + i < 0 || a[0] + i >= p->ntex || !p->tex[a[0] + i]) return -1;
+            s->chainA[i] = level_of(p->tex[a[0] + i]);
+        }
+        s->lodScale = ufl(p, 12)[0];
+        s->bias = ufl(p, 12)[1];
+        if (p->fp == FP_LIT2) {
+            const int* n = uin(p, 10);
+            int sm = *uin(p, 11);
+            s->levelsN = n[1] > MAX_LEVELS ? MAX_LEVELS : n[1];
+            for (int i = 0; i < s->levelsN; i++) {
+                if (n[0] + i < 0 || n[0] + i >= p->ntex || !p->tex[n[0] + i]) return -1;
+                s->chainN[i] = level_of(p->tex[n[0] + i]);
+                s->chainN[i].width /= 2; /* RGBA16F stored as a 4-byte-element FBO twice as wide */
+            }
+            if (sm < 0 || sm >= p->ntex || !p->tex[sm]) return -1;
+            s->shadow = (const float*)p->tex[sm]->buf;
+            s->shadowSize = p->tex[sm]->width;
+            s->shadowScan = p->tex[sm]->scanline / 4;
+        }
+        break;
+    }
+    default: break;
+    }
+    return 0;
+}
+
+/* FragmentProcessorDEF01::process (tex1light1.cpp:152-193) with IEEE 1/x and
+   1/sqrt in place of rcpps / rsqrtss (see the header note). */
+static void fp_def01(const fp_state* s, const float* in, uint8_t* bgra)
+{
+    const float* nrm = in, * wp = in + 4, * tc = in + 8;
+    const o_fbo* t = s->tex;
+    float c[4], L[4], E[4], Hv[4], dist, lambert, spec, r;
+    int row = (int)sr_f2u((float)t->height * tc[1] + 0.5f);
+    int col = (int)sr_f2u((float)t->width * tc[0] + 0.5f);
+    const uint8_t* px;
+    /* directRead4 -> clampCoord (fbo.cpp:287-291, 552-594) */
+    if (t->wrap) {
+        int mr = t->height - 1, mc = t->width - 1;
+        row = mr > 0 ? row % mr : 0;
+        if (row < 0) row += mr;
+        col = mc > 0 ? col % mc : 0;
+        if (col < 0) col += mc;
+    } else {
+        row = sr_clampi(row, t->height);
+        col = sr_clampi(col, t->width);
+    }
+    px = t->buf + (size_t)row * t->scanline + 4 * col;
+    for (int k = 0; k < 4; k++) c[k] = (float)px[k];
+    for (int k = 0; k < 4; k++) L[k] = s->light[k] - wp[k];
+    dist = sqrtf((L[0] * L[0] + L[1] * L[1]) + (L[2] * L[2] + L[3] * L[3]));
+    r = 1.0f / dist;
+    for (int k = 0; k < 4; k++) L[k] = L[k] * r;
+    for (int k = 0; k < 4; k++) E[k] = s->cam[k] - wp[k];
+    r = 1.0f / sqrtf((E[0] * E[0] + E[1] * E[1]) + (E[2] * E[2] + E[3] * E[3]));
+    for (int k = 0; k < 4; k++) E[k] = E[k] * r;
+    for (int k = 0; k < 4; k++) Hv[k] = E[k] + L[k];
+    r = 1.0f / sqrtf((Hv[0] * Hv[0] + Hv[1] * Hv[1]) + (Hv[2] * Hv[2] + Hv[3] * Hv[3]));
+    for (int k = 0; k < 4; k++) Hv[k] = Hv[k] * r;
+    lambert = (L[0] * nrm[0] + L[1] * nrm[1]) + (L[2] * nrm[2] + L[3] * nrm[3]);
+    spec = (Hv[0] * nrm[0] + Hv[1] * nrm[1]) + (Hv[2] * nrm[2] + Hv[3] * nrm[3]);
+    spec = spec < 0 ? 0 : spec;
+    { /* opt_pow(spec, 50) (proc.h:73-86) */
+        float pw = 1.0f, x = spec;
+        unsigned n = 50;
+        while (n > 0) {
+            if (n & 1) pw *= x;
+            x *= x;
+            n >>= 1;
+        }
+        spec = pw;
+    }
+    for (int k = 0; k < 4; k++) c[k] = c[k] + 255.0f * spec;
+    for (int k = 0; k < 4; k++) c[k] = c[k] * lambert;
+    for (int k = 0; k < 4; k++) { /* clamp_3_4: maxps then minps (vector.cpp:370-383) */
+        float v = c[k];
+        v = v > 0.0f ? v : 0.0f; /* maxps returns the second operand for NaN */
+        v = v < 255.0f ? v : 255.0f;
+        c[k] = v;
+    }
+    bgra[0] = (uint8_t)(int)c[0];
+    bgra[1] = (uint8_t)(int)c[1];
+    bgra[2] = (uint8_t)(int)c[2];
+    bgra[3] = 0;
+}
+
+/* Returns 1 if the processor wrote colour (the reference FPs never discard). */
+static int run_fp(const ps3do* p, const fp_state* s, const float* in, uint8_t* bgra)
+{
+    switch (p->fp) {
+    case FP_DEF01: fp_def01(s, in, bgra); return 1;
+    case FP_LIT1: {
+        sr_level t = level_of(s->tex);
+        sr_shade_lit1(&t, s->light, s->cam, in, in + 4, in + 8, bgra);
+        return 1;
+    }
+    case FP_LIT3:
+        sr_shade_lit3(s->chainA, s->levelsA, s->lodScale, s->light, s->cam, in, in + 4, in + 8, bgra);
+        return 1;
+    case FP_LIT2:
+        sr_shade_lit2(s->chainA, s->levelsA, s->chainN, s->levelsN, s->shadow, s->shadowSize, s->shadowScan,
+                      s->lodScale, s->bias, s->light, s->cam, in, bgra);
+        return 1;
+    default: return 0; /* FP_DEF05 writes nothing */
+    }
+}
+
+/* ------------------------------------------------------------- rasteriser */
+/* PuresoftRasterizer (rasterizer.h:3-49, rasterizer.cpp). */
+
+typedef struct { float x, y; } v2f;
+typedef struct { int left, leftClamped, leftVerts[2], right, rightClamped, rightVerts[2]; } o_row;
+typedef struct { float dx, dy, x0, y0; int i0, i1; } o_edge;
+
+typedef struct {
+    int W, H, halfW, halfH;
+    v2f v[3];
+    int firstRow, lastRow;
+    o_row* rows;
+} o_raster;
+
+static o_edge edge_make(const v2f* v, int a, int b) /* LineSegment, rasterizer.cpp:46-64 */
+{
+    o_edge e;
+    e.x0 = v[a].x;
+    e.y0 = v[a].y;
+    e.dx = v[b].x - e.x0;
+    e.dy = v[b].y - e.y0;
+    e.i0 = a;
+    e.i1 = b;
+    if (fabsf(e.dy) < 0.000001f) e.dy = FLT_MAX;
+    return e;
+}
+
+static float edge_at(const o_edge* e, float y) { return e->dx * (y - e->y0) / e->dy + e->x0; } /* :66-69 */
+
+static void process_triangle(o_raster* r, const o_edge* L, const o_edge* R, float yMin, float yMax) /* :93-118 */
+{
+    int iy = yMin < 0 ? 0 : sr_f2i(yMin);
+    int last = r->H - 1;
+    int iyMax = yMax > (float)last ? last : sr_f2i(yMax);
+    if (iy < 0) iy = 0; /* non-finite yMin: see the header note */
+    for (; iy <= iyMax; iy++) {
+        o_row* row = &r->rows[iy];
+        row->left = sr_f2i(edge_at(L, (float)iy) + 0.5f);
+        row->leftClamped = row->left < 0 ? 0 : row->left;
+        row->right = sr_f2i(edge_at(R, (float)iy) + 0.5f);
+        row->rightClamped = row->right >= r->W ? r->W - 1 : row->right;
+        row->leftVerts[0] = L->i0;
+        row->leftVerts[1] = L->i1;
+        row->rightVerts[0] = R->i0;
+        row->rightVerts[1] = R->i1;
+    }
+}
+
+static void push_vertex(o_raster* r, int idx, const float* v) /* :73-90 */
+{
+    r->v[idx].y = ((float)r->halfH * v[1]) + (float)r->halfH;
+    r->v[idx].x = ((float)r->halfW * v[0]) + (float)r->halfW;
+    if (0 == idx) r->firstRow = r->lastRow = sr_f2i(r->v[0].y);
+    else if (r->v[idx].y > (float)r->lastRow) r->lastRow = sr_f2i(r->v[idx].y);
+    else if (r->v[idx].y < (float)r->firstRow) r->firstRow = sr_f2i(r->v[idx].y);
+}
+
+static int push_triangle(o_raster* r, const float* p0, const float* p1, const float* p2) /* :142-234 */
+{
+    const v2f* v = r->v;
+    push_vertex(r, 0, p0);
+    push_vertex(r, 1, p1);
+    push_vertex(r, 2, p2);
+    if (!(isfinite(v[0].x) && isfinite(v[0].y) && isfinite(v[1].x) && isfinite(v[1].y) && isfinite(v[2].x) &&
+          isfinite(v[2].y)))
+        return 0; /* see the header note */
+    if (r->firstRow >= r->H || r->lastRow < 0) { r->firstRow = 0; r->lastRow = -1; }
+    if (r->firstRow < 0) r->firstRow = 0;
+    if (r->lastRow >= r->H) r->lastRow = r->H - 1;
+    if (r->firstRow == r->lastRow) return 0;
+    if (v[0].y == v[1].y) {
+        o_edge a = edge_make(v, 0, 2), b = edge_make(v, 1, 2);
+        if (v[0].x < v[1].x) process_triangle(r, &a, &b, (float)r->firstRow, (float)r->lastRow);
+        else process_triangle(r, &b, &a, (float)r->firstRow, (float)r->lastRow);
+    } else if (v[0].y == v[2].y) {
+        o_edge a = edge_make(v, 0, 1), b = edge_make(v, 2, 1);
+        if (v[0].x < v[2].x) process_triangle(r, &a, &b, (float)r->firstRow, (float)r->lastRow);
+        else process_triangle(r, &b, &a, (float)r->firstRow, (float)r->lastRow);
+    } else if (v[1].y == v[2].y) {
+        o_edge a = edge_make(v, 1, 0), b = edge_make(v, 2, 0);
+        if (v[1].x < v[2].x) process_triangle(r, &a, &b, (float)r->firstRow, (float)r->lastRow);
+        else process_triangle(r, &b, &a, (float)r->firstRow, (float)r->lastRow);
+    } else {
+        int top, bottom, third = 2, t;
+        if (v[0].y > v[1].y) { top = 0; bottom = 1; }
+        else { top = 1; bottom = 0; }
+        if (v[top].y < v[third].y) { t = top; top = third; third = t; }
+        else if (v[bottom].y > v[third].y) { t = bottom; bottom = third; third = t; }
+        { /* processStandingTriangle (:121-140) */
+            o_edge tt = edge_make(v, top, third), tb = edge_make(v, top, bottom), thb = edge_make(v, third, bottom);
+            if (edge_at(&tb, v[third].y) > edge_at(&tt, v[third].y)) {
+                process_triangle(r, &tt, &tb, v[third].y, v[top].y);
+                process_triangle(r, &thb, &tb, v[bottom].y, v[third].y);
+            } else {
+                process_triangle(r, &tb, &tt, v[third].y, v[top].y);
+                process_triangle(r, &tb, &thb, v[bottom].y, v[third].y);
+            }
+        }
+    }
+    return 1;
+}
+
+/* isBackFace (vertthrd.cpp:56-65): sign of the normalised cross product's z.
+   norm_3_4 scales by rsqrtss(|c|^2); the test only depends on that factor
+   being finite and positive, which holds exactly when |c|^2 is a finite
+   normal number.  With an infinite factor (|c|^2 zero or denormal) the dot
+   product is NaN and the face is not culled; with a zero factor (|c|^2
+   infinite) it is +-0 and not culled. */
+static int is_back_face(const float* v0, const float* v1, const float* v2)
+{
+    float a[4], b[4], c[4], s;
+    for (int k = 0; k < 4; k++) {
+        a[k] = v1[k] - v0[k];
+        b[k] = v2[k] - v1[k];
+    }
+    c[0] = a[1] * b[2] - a[2] * b[1]; /* cross_3 shuffles (vector.cpp:114-144) */
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
+    c[3] = a[3] * b[3] - a[3] * b[3];
+    s = (c[0] * c[0] + c[1] * c[1]) + (c[2] * c[2] + c[3] * c[3]);
+    if (!(s >= FLT_MIN && s <= FLT_MAX)) return 0;
+    if (!isfinite(c[0]) || !isfinite(c[1]) || !isfinite(c[3])) return 0;
+    return c[2] < 0.0f;
+}
+
+/* -------------------------------------------------------------- span set-up */
+
+/* lineSegmentlinearInterpolate (interp.cpp:151-160) */
+static void line_contrib(const v2f* v, int v1, int v2, float x, float y, float* c)
+{
+    float dx = v[v1].x - v[v2].x, dy = v[v1].y - v[v2].y;
+    c[v1] = fabsf(dx) > fabsf(dy) ? ((x - v[v2].x) / dx) : ((y - v[v2].y) / dy);
+    c[v2] = 1.0f - c[v1];
+    c[3 - v1 - v2] = 0;
+}
+
+/* interpolateStartAndStep (interp.cpp:26-80) */
+static void span_setup(const o_raster* r, const o_row* row, int y, const float* rw, const float* pz, int nv,
+                       const float* const* vuser, o_task* t)
+{
+    float cl[4], cr[4], ccl[4], ccr[4], recip;
+    float* start = t->user, * step = t->user + 4 * MAX_VECS;
+    int stepCount, skip;
+    cl[3] = cr[3] = 0;
+    line_contrib(r->v, row->leftVerts[0], row->leftVerts[1], (float)row->left, (float)y, cl);
+    line_contrib(r->v, row->rightVerts[0], row->rightVerts[1], (float)row->right, (float)y, cr);
+    for (int k = 0; k < 4; k++) {
+        ccl[k] = cl[k] * rw[k];
+        ccr[k] = cr[k] * rw[k];
+    }
+    ip_by_contributes(nv, start, vuser, ccl);
+    ip_by_contributes(nv, step, vuser, ccr);
+    stepCount = row->right - row->left;
+    ip_calc_step(nv, step, start, step, stepCount);
+    recip = 1.0f / (float)stepCount;
+    {
+        float m[4];
+        for (int k = 0; k < 4; k++) m[k] = ccl[k] * pz[k];
+        t->pzStart = hsum4(m);
+        for (int k = 0; k < 4; k++) m[k] = ccr[k] * pz[k];
+        t->pzStep = hsum4(m);
+    }
+    t->pzStep = (t->pzStep - t->pzStart) * recip;
+    t->cf2Start = hsum4(ccl);
+    t->cf2Step = hsum4(ccr);
+    t->cf2Step = (t->cf2Step - t->cf2Start) * recip;
+    skip = row->leftClamped - row->left;
+    if (skip > 0) {
+        t->cf2Start += t->cf2Step * (float)skip;
+        t->pzStart += t->pzStep * (float)skip;
+        ip_step_forward(nv, start, step, skip);
+    }
+    t->x1 = row->leftClamped;
+    t->x2 = row->rightClamped;
+    t->y = y;
+}
+
+static int push_task(o_tasklist* l, const o_task* t)
+{
+    if (l->n == l->cap) {
+        size_t cap = l->cap ? 2 * l->cap : 1024;
+        o_task* q = (o_task*)realloc(l->items, cap * sizeof(o_task));
+        if (!q) return -3;
+        l->items = q;
+        l->cap = cap;
+    }
+    l->items[l->n++] = *t;
+    return 0;
+}
+
+/* ------------------------------------------------------- per-pixel loop */
+
+typedef struct {
+    ps3do* p;
+    fp_state fs;
+    int nv;
+} draw_ctx;
+
+/* One FBO cursor (PuresoftFBO::WORKRANGE and setCurRow/setCurCol/nextCol,
+   fbo.cpp:98-173) for a CLAMP-mode buffer. */
+typedef struct {
+    uint8_t* rowEntry;
+    int col, maxCol, overflow, elemLen;
+} o_cursor;
+
+static void cursor_set(o_cursor* c, const o_fbo* f, int row, int col)
+{
+    int r = sr_clampi(row, f->height); /* the row's overflow flag is overwritten by setCurCol */
+    int mem = f->topDown ? f->height - r - 1 : r;
+    c->rowEntry = f->buf + (size_t)mem * f->scanline;
+    c->maxCol = f->width - 1;
+    c->elemLen = f->elemLen;
+    c->overflow = (col > c->maxCol || col < 0);
+    c->col = sr_clampi(col, f->width);
+}
+
+static void cursor_next(o_cursor* c)
+{
+    if (c->col >= c->maxCol) c->overflow = 1;
+    else c->col++;
+}
+
+/* fragmentThread's DRAW branch (fragthrd.cpp:160-252) for one task. */
+static void run_task(draw_ctx* d, const o_task* t, long long* tested, long long* passed)
+{
+    ps3do* p = d->p;
+    int nv = d->nv, behav = p->behavior;
+    float start[4 * MAX_VECS], step[4 * MAX_VECS], frag[4 * MAX_VECS];
+    float cf2 = t->cf2Start, pz = t->pzStart;
+    o_cursor cc, dc;
+    memcpy(start, t->user, sizeof(float) * 4 * nv);
+    memcpy(step, t->user + 4 * MAX_VECS, sizeof(float) * 4 * nv);
+    cursor_set(&cc, &p->display, t->y, t->x1);
+    cursor_set(&dc, p->depth, t->y, t->x1);
+    for (int x = t->x1; x <= t->x2; x++) {
+        /* interpolateNextStep (interp.cpp:82-92) */
+        float inv = 1.0f / cf2, z, cur;
+        cf2 += t->cf2Step;
+        for (int i = 0; i < 4 * nv; i++) frag[i] = start[i] * inv;
+        for (int i = 0; i < 4 * nv; i++) start[i] = start[i] + step[i];
+        z = pz * inv;
+        pz += t->pzStep;
+        (*tested)++;
+        cur = (behav & BEHAVIOR_TEST_DEPTH) ? *(const float*)(dc.rowEntry + (size_t)dc.col * 4) : 1.0f;
+        if (-1.0f < z && (z - cur < -0.0001f)) { /* fragthrd.cpp:227 */
+            uint8_t bgra[4];
+            (*passed)++;
+            if (run_fp(p, &d->fs, frag, bgra) && !cc.overflow) memcpy(cc.rowEntry + (size_t)cc.col * 4, bgra, 4);
+            if ((behav & BEHAVIOR_UPDATE_DEPTH) && !dc.overflow) memcpy(dc.rowEntry + (size_t)dc.col * 4, &z, 4);
+        }
+        cursor_next(&cc);
+        cursor_next(&dc);
+    }
+}
+
+static void run_list(draw_ctx* d, int t, long long* tested, long long* passed)
+{
+    o_tasklist* l = &d->p->lists[t];
+    for (size_t i = 0; i < l->n; i++) run_task(d, &l->items[i], tested, passed);
+}
+
+static void* worker(void* arg)
+{
+    ps3do* p = (ps3do*)((void**)arg)[0];
+    int idx = (int)(intptr_t)((void**)arg)[1];
+    int seen = 0;
+    free(arg);
+    for (;;) {
+        long long tested = 0, passed = 0;
+        draw_ctx* d;
+        pthread_mutex_lock(&p->mu);
+        while (p->gen == seen) pthread_cond_wait(&p->cv, &p->mu);
+        seen = p->gen;
+        if (p->quit) { pthread_mutex_unlock(&p->mu); return NULL; }
+        d = (draw_ctx*)p->cur_draw;
+        pthread_mutex_unlock(&p->mu);
+        run_list(d, idx, &tested, &passed);
+        pthread_mutex_lock(&p->mu);
+        p->tested += tested;
+        p->passed += passed;
+        p->finished++;
+        pthread_cond_signal(&p->done);
+        pthread_mutex_unlock(&p->mu);
+    }
+}
+
+/* drawVAO (drawvao.cpp:3-133) */
+int ps3do_draw(ps3do* p, int vao)
+{
+    o_vao* va;
+    draw_ctx d;
+    o_raster r;
+    float rw[4] = {0, 0, 0, 0}, pz[4] = {0, 0, 0, 0};
+    float pos[3][4], vuser[3][4 * MAX_VECS];
+    const float* vu[3] = {vuser[0], vuser[1], vuser[2]};
+    size_t cursor[MAX_VBOS];
+    int nv, rc = 0;
+
+    if (!p->vp || !p->ip || !p->fp || vao < 0 || vao >= p->nvao || !p->vaos[vao]) return 0;
+    va = p->vaos[vao];
+    d.p = p;
+    nv = d.nv = ip_vecs(p->ip);
+    if (fp_prepare(p, &d.fs)) return -1;
+    memset(vuser, 0, sizeof vuser);
+    memset(&r, 0, sizeof r);
+    r.W = p->W;
+    r.H = p->H;
+    r.halfW = p->W / 2;
+    r.halfH = p->H / 2;
+    r.rows = (o_row*)calloc((size_t)p->H, sizeof(o_row));
+    if (!r.rows) return -3;
+    for (int t = 0; t < p->threads; t++) p->lists[t].n = 0;
+    memset(cursor, 0, sizeof cursor);
+
+    for (;;) {
+        int done = 0;
+        /* processVertices (vertthrd.cpp:14-51) */
+        for (int i = 0; i < 3 && !done; i++) {
+            const void* in[MAX_VBOS] = {0};
+            for (int j = 0; j < MAX_VBOS; j++) {
+                o_vbo* b = va->vbo[j];
+                if (!b) continue;
+                if (cursor[j] >= (size_t)b->count) { done = 1; break; } /* vbo.cpp:69-84 */
+                in[j] = b->data + cursor[j] * b->unitBytes;
+                cursor[j]++;
+            }
+            if (done) break;
+            run_vp(p, in, pos[i], vuser[i]);
+            {
+                float rcp = 1.0f / pos[i][3];
+                for (int k = 0; k < 4; k++) pos[i][k] = pos[i][k] * rcp; /* mul_3_4 is 4-wide */
+                pz[i] = pos[i][2];
+                rw[i] = rcp;
+            }
+        }
+        if (done) break;
+        if ((p->behavior & BEHAVIOR_FACE_CULLING) && is_back_face(pos[0], pos[1], pos[2])) continue;
+        if (pos[0][2] < -1.0f || pos[0][2] > 1.0f) continue; /* drawvao.cpp:51-56 */
+        if (pos[1][2] < -1.0f || pos[1][2] > 1.0f) continue;
+        if (pos[2][2] < -1.0f || pos[2][2] > 1.0f) continue;
+        if (!push_triangle(&r, pos[0], pos[1], pos[2])) continue;
+        for (int y = r.firstRow; y <= r.lastRow; y++) {
+            const o_row* row = &r.rows[y];
+            o_task t;
+            if (row->left == row->right) continue; /* drawvao.cpp:72-75 */
+            span_setup(&r, row, y, rw, pz, nv, vu, &t);
+            if ((rc = push_task(&p->lists[y % p->threads], &t)) != 0) goto out;
+        }
+    }
+
+    if (p->threads > 1) {
+        long long tested = 0, passed = 0;
+        pthread_mutex_lock(&p->mu);
+        p->cur_draw = &d;
+        p->finished = 0;
+        p->gen++;
+        pthread_cond_broadcast(&p->cv);
+        pthread_mutex_unlock(&p->mu);
+        run_list(&d, 0, &tested, &passed);
+        pthread_mutex_lock(&p->mu);
+        p->tested += tested;
+        p->passed += passed;
+        while (p->finished < p->threads - 1) pthread_cond_wait(&p->done, &p->mu);
+        pthread_mutex_unlock(&p->mu);
+    } else {
+        run_list(&d, 0, &p->tested, &p->passed);
+    }
+out:
+    free(r.rows);
+    return rc;
+}
