@@ -1,0 +1,199 @@
+/*
+ * ps3d.h -- C ABI of puresoft3d_gb300, a GB300 (sm_103a) implementation of
+ * the per-fragment path of Puresoft3D (CallMeZhou/Puresoft3D): vertex
+ * processing, triangle set-up, scanline rasterisation, perspective-correct
+ * interpolation, depth test, fragment shading, framebuffer write and 2D
+ * texture sampling.
+ *
+ * Every entry point replaces one method of the reference's PuresoftPipeline
+ * (src/puresoft3d/pipeline.h:26-69) and is cited beside it.  Plain C types
+ * only; a pipeline is an opaque handle.  All calls on one pipeline must come
+ * from one host thread (the reference has the same rule: one API thread,
+ * pipeline.cpp).  Rendering is asynchronous on the pipeline's CUDA stream:
+ * ps3d_draw records work, ps3d_flush launches it, and ps3d_finish or any
+ * read-back waits for it.
+ *
+ * Return values: >= 0 success (an index where the reference returns one);
+ * negative status codes mirror the reference's C++ exceptions:
+ *   PS3D_ERR_RANGE   std::out_of_range     (bad index)
+ *   PS3D_ERR_INVALID std::invalid_argument (bad format / combination)
+ *   PS3D_ERR_NOMEM   std::bad_alloc        (host or device allocation)
+ * and two for the device:
+ *   PS3D_ERR_DEVICE  a CUDA call failed (the message: ps3d_last_error)
+ *   PS3D_ERR_TIMEOUT a bounded device wait gave up (batch/serve paths)
+ * ps3d_draw on a pipeline with no usable programme, or with a bad VAO index,
+ * does nothing and returns PS3D_OK, as drawVAO does (drawvao.cpp:12-15).
+ */
+#ifndef PS3D_H
+#define PS3D_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PS3D_OK 0
+#define PS3D_ERR_RANGE (-1)
+#define PS3D_ERR_INVALID (-2)
+#define PS3D_ERR_NOMEM (-3)
+#define PS3D_ERR_DEVICE (-4)
+#define PS3D_ERR_TIMEOUT (-5)
+
+/* behaviour bits (reference pipeline.h:16-19) */
+#define PS3D_BEHAVIOR_UPDATE_DEPTH 0x1
+#define PS3D_BEHAVIOR_TEST_DEPTH 0x2
+#define PS3D_BEHAVIOR_FACE_CULLING 0x4
+#define PS3D_BEHAVIOR_ALPHABLEND 0x8
+
+/* Built-in processor classes.  The reference's processors are C++ classes
+ * that run on the CPU (proc.h:26-71); here each class is a device functor
+ * selected by id.  Low nibble: 1 vertex, 2 interpolation, 3 fragment.
+ *   DEF01  VertexProcesserDEF01 / InterpolationProcessorDEF01 /
+ *          FragmentProcessorDEF01 (tex1light1.cpp): point light, nearest
+ *          texture; the fragment stage uses IEEE 1/x and 1/sqrt where the
+ *          reference uses rcpps/rsqrtss.
+ *   DEF05  the depth-only shadow programme (shadow.cpp), positions x0.9.
+ *   SHADOW DEF05's vertex stage without the x0.9 scale.
+ *   LIT1   fragment stage over DEF01 varyings: bilinear REPEAT albedo,
+ *          directional Lambert + Blinn-Phong (shininess 32).
+ *   LIT3   LIT1 with a trilinear mip chain.
+ *   LIT2   vertex/interpolation/fragment stages with tangent, light-space
+ *          position, trilinear albedo, tangent-space normal map and 3x3 PCF.
+ */
+#define PS3D_VP_DEF01 0x0101
+#define PS3D_IP_DEF01 0x0102
+#define PS3D_FP_DEF01 0x0103
+#define PS3D_VP_DEF05 0x0501
+#define PS3D_IP_DEF05 0x0502
+#define PS3D_FP_DEF05 0x0503
+#define PS3D_VP_SHADOW 0x0601
+#define PS3D_FP_LIT1 0x1103
+#define PS3D_FP_LIT3 0x1303
+#define PS3D_VP_LIT2 0x1201
+#define PS3D_IP_LIT2 0x1202
+#define PS3D_FP_LIT2 0x1203
+
+/* limits (reference config.h:3-9) */
+#define PS3D_MAX_VBOS 16
+#define PS3D_MAX_UNIFORMS 1024
+#define PS3D_MAX_FBOS 16
+
+typedef struct ps3d_pipeline ps3d_pipeline;
+
+/* Counters since creation (ps3d_stats). */
+typedef struct {
+    uint64_t draws;           /* ps3d_draw calls that drew */
+    uint64_t batches;         /* device passes executed */
+    uint64_t kernel_launches; /* kernels this library launched */
+    uint64_t triangles;       /* triangles sent through set-up */
+    uint64_t fragments;       /* fragments that reached the depth test (when counting is on) */
+    uint64_t fragments_passed;/* fragments that passed it (when counting is on) */
+    uint64_t replays;         /* passes re-run after a bin-list capacity miss */
+} ps3d_stats_t;
+
+/* PuresoftPipeline::PuresoftPipeline(canvas, w, h, rndr) (pipeline.cpp:24-61).
+ * Creates the default FP32 depth buffer (scanline rounded to 4 floats,
+ * pipeline.cpp:31) and a BGRA8 top-down colour buffer in device memory in
+ * place of the renderer's back buffer.  `stream` is a cudaStream_t, or NULL
+ * for a stream the pipeline creates and owns. */
+int ps3d_pipeline_create(int width, int height, void* stream, ps3d_pipeline** out);
+/* PuresoftPipeline::~PuresoftPipeline (pipeline.cpp:63-116). */
+int ps3d_pipeline_destroy(ps3d_pipeline* p);
+/* Message of the last failing call on this thread. */
+const char* ps3d_last_error(void);
+
+/* PuresoftPipeline::createTexture (tex.cpp:3-25): copies `pixels` (host
+ * memory, scanline*height bytes; NULL leaves it zeroed) into a
+ * pipeline-owned device texture.  elemLen must be 1 or 4 (fbo.cpp:21-24);
+ * wrap 0 = CLAMP, 1 = WRAP. */
+int ps3d_texture_create(ps3d_pipeline* p, int width, int height, int scanline, int elemLen, const void* pixels,
+                        int wrap);
+/* Same, from device memory (cudaMemcpyDeviceToDevice). */
+int ps3d_texture_create_device(ps3d_pipeline* p, int width, int height, int scanline, int elemLen,
+                               const void* devPixels, int wrap);
+/* PuresoftPipeline::destroyTexture (tex.cpp:39-51). */
+int ps3d_texture_destroy(ps3d_pipeline* p, int idx);
+/* PuresoftPipeline::getTexture (tex.cpp:27-37): waits for pending work, then
+ * copies min(bytes, scanline*height) bytes of the texture to host memory. */
+int ps3d_texture_read(ps3d_pipeline* p, int idx, void* out, size_t bytes);
+/* Device address of a texture's first byte (rows bottom-up). */
+int ps3d_texture_device_ptr(ps3d_pipeline* p, int idx, void** out);
+
+/* PuresoftPipeline::addProcessor (prog.cpp:3-20) with a built-in class id. */
+int ps3d_processor_add(ps3d_pipeline* p, int processorId);
+/* PuresoftPipeline::destroyProcessor (prog.cpp:22-41). */
+int ps3d_processor_destroy(ps3d_pipeline* p, int idx);
+/* PuresoftPipeline::createProgramme (prog.cpp:43-108).  The reference lets
+ * any three processors combine and reinterprets user-data bytes; here the
+ * interpolation stage must carry the varyings its fragment stage reads
+ * (DEF01 varyings for DEF01/LIT1/LIT3, LIT2 varyings for LIT2), else
+ * PS3D_ERR_INVALID. */
+int ps3d_programme_create(ps3d_pipeline* p, int vid, int iid, int fid);
+/* PuresoftPipeline::destroyProgramme (prog.cpp:110-119). */
+int ps3d_programme_destroy(ps3d_pipeline* p, int idx);
+/* PuresoftPipeline::useProgramme (prog.cpp:121-131). */
+int ps3d_programme_use(ps3d_pipeline* p, int idx);
+
+/* PuresoftPipeline::createVAO (pipeline.cpp:118-136). */
+int ps3d_vao_create(ps3d_pipeline* p);
+/* PuresoftPipeline::destroyVAO (pipeline.cpp:183-205): frees attached VBOs. */
+int ps3d_vao_destroy(ps3d_pipeline* p, int vao);
+/* new PuresoftVBO(unitBytes, count) + updateContent(data) + attachVBO(vao,
+ * slot, vbo) (vbo.cpp:16-31, pipeline.cpp:138-151): uploads `count` elements
+ * of `unitBytes` from host memory into VBO slot `slot` of `vao`; replaces and
+ * frees a VBO already there. */
+int ps3d_vbo_attach(ps3d_pipeline* p, int vao, int slot, int unitBytes, int count, const void* data);
+/* Same, from device memory. */
+int ps3d_vbo_attach_device(ps3d_pipeline* p, int vao, int slot, int unitBytes, int count, const void* devData);
+/* PuresoftPipeline::detachVBO + delete (pipeline.cpp:153-166). */
+int ps3d_vbo_detach(ps3d_pipeline* p, int vao, int slot);
+
+/* PuresoftPipeline::setUniform (pipeline.cpp:277-312): copies len bytes into
+ * slot idx; data == NULL frees the slot. */
+int ps3d_set_uniform(ps3d_pipeline* p, int idx, const void* data, size_t len);
+/* PuresoftPipeline::setDepth (pipeline.cpp:218-239): -1 = default buffer;
+ * a texture must have elemLen 4 and a scanline multiple of 4 (else
+ * PS3D_ERR_INVALID).  The depth target must be CLAMP-addressed. */
+int ps3d_set_depth(ps3d_pipeline* p, int idx);
+/* PuresoftPipeline::setViewport (pipeline.cpp:207-216): rasteriser size. */
+int ps3d_set_viewport(ps3d_pipeline* p, int width, int height);
+/* PuresoftPipeline::enable / disable (pipeline.cpp:324-332). */
+int ps3d_enable(ps3d_pipeline* p, int bits);
+int ps3d_disable(ps3d_pipeline* p, int bits);
+/* PuresoftPipeline::clearDepth (pipeline.cpp:334-338): every element of the
+ * current depth target. */
+int ps3d_clear_depth(ps3d_pipeline* p, float furthest);
+/* PuresoftPipeline::clearColour (pipeline.cpp:340-343): every pixel of the
+ * colour buffer (the reference skips the last memory row, fbo.cpp:336). */
+int ps3d_clear_colour(ps3d_pipeline* p, uint32_t bgra);
+/* PuresoftPipeline::drawVAO(vao, false) (drawvao.cpp:3-133): records the draw
+ * with a snapshot of the programme, uniforms, behaviour, viewport and
+ * targets.  Work is launched by ps3d_flush / ps3d_finish / a read-back. */
+int ps3d_draw(ps3d_pipeline* p, int vao);
+/* Launch recorded work on the stream without waiting. */
+int ps3d_flush(ps3d_pipeline* p);
+/* Launch recorded work and wait for it (drawVAO's synchronous return,
+ * drawvao.cpp:121-132). */
+int ps3d_finish(ps3d_pipeline* p);
+
+/* Read-back of the colour buffer: width*height*4 bytes, BGRA8, top-down
+ * (memory row = H-1-y, the display FBO layout, pipeline.cpp:48). */
+int ps3d_read_colour(ps3d_pipeline* p, void* out);
+/* Read-back of the default depth buffer: scanline*height bytes. */
+int ps3d_read_depth(ps3d_pipeline* p, void* out);
+/* Device address of the colour buffer. */
+int ps3d_colour_device_ptr(ps3d_pipeline* p, void** out);
+/* The pipeline's CUDA stream (cudaStream_t). */
+int ps3d_get_stream(ps3d_pipeline* p, void** out);
+
+/* Count fragments reaching / passing the depth test (off by default: it
+ * adds one atomic per warp-span). */
+int ps3d_set_fragment_counting(ps3d_pipeline* p, int on);
+int ps3d_stats(ps3d_pipeline* p, ps3d_stats_t* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
