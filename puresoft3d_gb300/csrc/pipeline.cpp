@@ -1,0 +1,1038 @@
+// pipeline.cpp -- host runtime behind the C ABI (include/ps3d.h).
+//
+// The pipeline keeps the reference's object model (PuresoftPipeline,
+// src/puresoft3d/pipeline.h:24-156): pools of textures, processors,
+// programmes and VAOs addressed by small integer indices, 1024 uniform slots,
+// a behaviour word, a depth target and a viewport.  Resources live in device
+// memory.  ps3d_draw records a draw with a snapshot of everything the device
+// needs; a flush groups consecutive draws into one target into a "pass" and
+// launches it (set-up + binning + raster + shade kernels).  Clears that
+// precede a pass on the same target are fused into it.
+//
+// Bin lists are written into buffers sized from the previous frames.  If a
+// pass needs more room, its kernels raise a flag and every later kernel of
+// the flush does nothing; at the next synchronisation point the runtime grows
+// the buffers and re-runs the recorded passes from the one that overflowed.
+// Targets are never touched by an aborted pass, so the re-run sees exactly
+// the state the first run saw.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <algorithm>
+#include <new>
+#include <string>
+#include <vector>
+#include "ps3d.h"
+#include "ps3d_internal.h"
+
+namespace ps3d {
+void launch_setup_and_bin(const PassParams& P, int* scanTmp, cudaStream_t s, int& launches);
+int scan_block_sums_needed(int nMax);
+int max_bins();
+void launch_raster_shade(const PassParams& P, cudaStream_t s, int& launches);
+void launch_fill_u32(void* base, int width, int height, int pitchElems, uint32_t v, const int* status,
+                     cudaStream_t s, int& launches);
+}  // namespace ps3d
+
+using namespace ps3d;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CU(call)                                                                                 \
+    do {                                                                                         \
+        cudaError_t e_ = (call);                                                                 \
+        if (e_ != cudaSuccess) return fail(PS3D_ERR_DEVICE, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+struct Texture {
+    uint8_t* dev = nullptr;
+    int width = 0, height = 0, scanline = 0, elemLen = 0, wrap = 0;
+    bool alive = false;
+};
+
+struct Vbo {
+    uint8_t* dev = nullptr;
+    int unitBytes = 0, count = 0;
+};
+
+struct Vao {
+    Vbo* vbo[PS3D_MAX_VBOS] = {};
+    bool alive = false;
+};
+
+struct Programme {
+    int vp = -1, ip = -1, fp = -1;
+};
+
+// one recorded command
+struct Command {
+    enum Kind { DRAW, CLEAR_DEPTH, CLEAR_COLOUR } kind;
+    int depthTarget;  // -1 = default buffer
+    int vpW, vpH;
+    float depthValue;
+    uint32_t colourValue;
+    DrawDesc desc;
+    DrawUniforms uni;
+};
+
+struct Pass {
+    size_t first, last;  // commands [first, last) are its draws
+    bool clearDepth = false, clearColour = false;
+    float depthValue = 1.0f;
+    uint32_t colourValue = 0;
+};
+
+template <class T> bool dev_alloc(T*& p, size_t& cap, size_t need)
+{
+    if (need <= cap && p) return true;
+    size_t n = std::max(need, cap + cap / 2);
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    if (cudaMalloc((void**)&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return false;
+    cap = n;
+    return true;
+}
+
+// mcemaths_transform_m4m4 (matrix.cpp:588-690): column c of d = l * (column c of r),
+// each lane ((l0*r0 + l4*r1) + l8*r2) + l12*r3.  Built with -ffp-contract=off.
+void m4m4(float* d, const float* l, const float* r)
+{
+    for (int c = 0; c < 4; c++) {
+        const float* v = r + 4 * c;
+        for (int i = 0; i < 4; i++) {
+            float a = v[0] * l[i];
+            float b = v[1] * l[4 + i];
+            float s = a + b;
+            float e = v[2] * l[8 + i];
+            s = s + e;
+            float f = v[3] * l[12 + i];
+            d[4 * c + i] = s + f;
+        }
+    }
+}
+
+}  // namespace
+
+struct ps3d_pipeline {
+    int devW, devH;      // device size (colour buffer, default depth)
+    int W, H;            // viewport
+    int behavior = B_UPDATE_DEPTH | B_TEST_DEPTH | B_FACE_CULLING;  // pipeline.cpp:34
+    int depthTarget = -1;
+    int binW = 32;
+    bool countFrags = false;
+    cudaStream_t stream = nullptr;
+    bool ownStream = false;
+
+    uint8_t* colour = nullptr;      // BGRA8, top-down
+    float* defDepth = nullptr;
+    int defDepthScan = 0;           // floats
+
+    std::vector<Texture> tex;
+    std::vector<int> procs;         // processor class ids, 0 = destroyed
+    std::vector<Programme> progs;
+    std::vector<Vao> vaos;
+    std::vector<std::vector<uint8_t>> uni = std::vector<std::vector<uint8_t>>(PS3D_MAX_UNIFORMS);
+    int vp = 0, ip = 0, fp = 0;     // processor class ids in use
+
+    std::vector<Command> pending;   // recorded, not launched
+    std::vector<Command> launched;  // launched since the last verification
+    std::vector<size_t> passStart;  // per launched pass: index in `launched` to re-run it from
+
+    // device scratch
+    TriRaster* tris = nullptr; size_t trisCap = 0;
+    float* vary = nullptr; size_t varyCap = 0;
+    int* pairCount = nullptr; size_t pairCountCap = 0;
+    int4* rect = nullptr; size_t rectCap = 0;
+    int* pairOffset = nullptr; size_t pairOffsetCap = 0;
+    int* pairKey = nullptr; size_t pairKeyCap = 0;
+    int* pairTri = nullptr; size_t pairTriCap = 0;
+    int* binTri = nullptr; size_t binTriCap = 0;
+    int* binHist = nullptr; size_t binHistCap = 0;
+    int* scanTmp = nullptr; size_t scanTmpCap = 0;
+    int* winner = nullptr; size_t winnerCap = 0;
+    DrawDesc* draws = nullptr; size_t drawsCap = 0;
+    DrawUniforms* unis = nullptr; size_t unisCap = 0;
+    int* status = nullptr;
+    int pairCap = 1 << 18;
+
+    ps3d_stats_t stats = {};
+};
+
+namespace {
+
+int required_vary(int ip)
+{
+    switch (ip) {
+    case IP_DEF01: return 9;
+    case IP_LIT2: return 16;
+    default: return 0;
+    }
+}
+
+int fp_needs(int fp)
+{
+    switch (fp) {
+    case FP_DEF01: case FP_LIT1: case FP_LIT3: return IP_DEF01;
+    case FP_LIT2: return IP_LIT2;
+    default: return 0;
+    }
+}
+
+int vp_gives(int vp)
+{
+    switch (vp) {
+    case VP_DEF01: return IP_DEF01;
+    case VP_LIT2: return IP_LIT2;
+    default: return 0;
+    }
+}
+
+bool known_processor(int id)
+{
+    switch (id) {
+    case VP_DEF01: case IP_DEF01: case FP_DEF01: case VP_DEF05: case IP_DEF05: case FP_DEF05:
+    case VP_SHADOW: case FP_LIT1: case FP_LIT3: case VP_LIT2: case IP_LIT2: case FP_LIT2:
+        return true;
+    }
+    return false;
+}
+
+bool tex_ok(const ps3d_pipeline* p, int i) { return i >= 0 && i < (int)p->tex.size() && p->tex[i].alive; }
+
+TexLevel level_of(const Texture& t)
+{
+    TexLevel l;
+    l.base = t.dev;
+    l.width = t.width;
+    l.height = t.height;
+    l.scanline = t.scanline;
+    l.wrap = t.wrap;
+    return l;
+}
+
+const float* ufl(const ps3d_pipeline* p, int slot, size_t floats)
+{
+    const auto& u = p->uni[slot];
+    return u.size() >= floats * 4 ? (const float*)u.data() : nullptr;
+}
+
+const int* uint_(const ps3d_pipeline* p, int slot, size_t ints)
+{
+    const auto& u = p->uni[slot];
+    return u.size() >= ints * 4 ? (const int*)u.data() : nullptr;
+}
+
+int chain_of(const ps3d_pipeline* p, int slot, TexLevel* out, int& levels, bool half)
+{
+    const int* c = uint_(p, slot, 2);
+    if (!c) return fail(PS3D_ERR_INVALID, "uniform %d must hold {first texture, levels}", slot);
+    if (c[1] < 1 || c[1] > kMaxLevels) return fail(PS3D_ERR_INVALID, "uniform %d: %d levels", slot, c[1]);
+    for (int i = 0; i < c[1]; i++) {
+        if (!tex_ok(p, c[0] + i)) return fail(PS3D_ERR_RANGE, "uniform %d: texture %d", slot, c[0] + i);
+        out[i] = level_of(p->tex[c[0] + i]);
+        if (half) out[i].width /= 2;
+    }
+    levels = c[1];
+    return 0;
+}
+
+// Snapshot of the uniforms the programme's processors read (their
+// preprocess(), reference drawvao.cpp:18-20).
+int snapshot_uniforms(const ps3d_pipeline* p, DrawUniforms& U)
+{
+    memset(&U, 0, sizeof U);
+    auto need = [&](int slot, float* dst, size_t n) -> int {
+        const float* f = ufl(p, slot, n);
+        if (!f) return fail(PS3D_ERR_INVALID, "uniform %d is not set (the processor reads %zu floats)", slot, n);
+        memcpy(dst, f, n * 4);
+        return 0;
+    };
+    int rc;
+    switch (p->vp) {
+    case VP_DEF01:
+        if ((rc = need(3, U.PV, 16)) || (rc = need(4, U.M, 16)) || (rc = need(5, U.Mrot, 16))) return rc;
+        break;
+    case VP_DEF05:
+    case VP_SHADOW:
+        if ((rc = need(3, U.PV, 16)) || (rc = need(4, U.M, 16))) return rc;
+        m4m4(U.PVM, U.PV, U.M);
+        break;
+    case VP_LIT2:
+        if ((rc = need(3, U.PV, 16)) || (rc = need(4, U.M, 16)) || (rc = need(5, U.Mrot, 16)) ||
+            (rc = need(6, U.LPV, 16)))
+            return rc;
+        break;
+    }
+    switch (p->fp) {
+    case FP_DEF01:
+    case FP_LIT1: {
+        if ((rc = need(7, U.light, 4)) || (rc = need(8, U.cam, 4))) return rc;
+        const int* t = uint_(p, 9, 1);
+        if (!t) return fail(PS3D_ERR_INVALID, "uniform 9 (texture index) is not set");
+        if (!tex_ok(p, *t)) return fail(PS3D_ERR_RANGE, "uniform 9: texture %d", *t);
+        if (p->tex[*t].elemLen != 4) return fail(PS3D_ERR_INVALID, "texture %d is not BGRA8", *t);
+        U.tex = level_of(p->tex[*t]);
+        break;
+    }
+    case FP_LIT3:
+        if ((rc = need(7, U.light, 4)) || (rc = need(8, U.cam, 4)) || (rc = need(12, U.params, 4))) return rc;
+        if ((rc = chain_of(p, 9, U.albedo, U.albedoLevels, false))) return rc;
+        break;
+    case FP_LIT2: {
+        if ((rc = need(7, U.light, 4)) || (rc = need(8, U.cam, 4)) || (rc = need(12, U.params, 4))) return rc;
+        if ((rc = chain_of(p, 9, U.albedo, U.albedoLevels, false))) return rc;
+        if ((rc = chain_of(p, 10, U.normal, U.normalLevels, true))) return rc;
+        const int* s = uint_(p, 11, 1);
+        if (!s || !tex_ok(p, *s)) return fail(PS3D_ERR_RANGE, "uniform 11: shadow map");
+        const Texture& t = p->tex[*s];
+        if (t.elemLen != 4 || t.width != t.height) return fail(PS3D_ERR_INVALID, "shadow map must be square FP32");
+        U.shadow = (const float*)t.dev;
+        U.shadowSize = t.width;
+        U.shadowScan = t.scanline / 4;
+        break;
+    }
+    }
+    return 0;
+}
+
+int ensure_scratch(ps3d_pipeline* p, int nTris, int nvMax, int W, int H, int binsX, int binsY, bool colour)
+{
+    size_t nBins = (size_t)binsX * binsY;
+    int sortBlocks = (p->pairCap + kSortChunk - 1) / kSortChunk;
+    bool ok = dev_alloc(p->tris, p->trisCap, nTris) && dev_alloc(p->vary, p->varyCap, (size_t)nTris * 3 * std::max(nvMax, 1)) &&
+              dev_alloc(p->pairCount, p->pairCountCap, nTris) && dev_alloc(p->rect, p->rectCap, nTris) &&
+              dev_alloc(p->pairOffset, p->pairOffsetCap, (size_t)nTris + 1) &&
+              dev_alloc(p->pairKey, p->pairKeyCap, p->pairCap) && dev_alloc(p->pairTri, p->pairTriCap, p->pairCap) &&
+              dev_alloc(p->binTri, p->binTriCap, p->pairCap) &&
+              dev_alloc(p->binHist, p->binHistCap, nBins * sortBlocks + 1) &&
+              dev_alloc(p->scanTmp, p->scanTmpCap,
+                        (size_t)scan_block_sums_needed((int)std::max<size_t>(nTris, nBins * sortBlocks)) + 1);
+    if (ok && colour) ok = dev_alloc(p->winner, p->winnerCap, (size_t)W * H);
+    if (!ok) return fail(PS3D_ERR_NOMEM, "device scratch allocation failed");
+    return 0;
+}
+
+struct Target {
+    float* depth;
+    int scan, w, h;
+};
+
+int depth_target(ps3d_pipeline* p, int idx, Target& t)
+{
+    if (idx == -1) {
+        t.depth = p->defDepth;
+        t.scan = p->defDepthScan;
+        t.w = p->devW;
+        t.h = p->devH;
+        return 0;
+    }
+    if (!tex_ok(p, idx)) return fail(PS3D_ERR_RANGE, "depth target %d was destroyed", idx);
+    const Texture& x = p->tex[idx];
+    t.depth = (float*)x.dev;
+    t.scan = x.scanline / 4;
+    t.w = x.width;
+    t.h = x.height;
+    return 0;
+}
+
+int fill_depth(ps3d_pipeline* p, int target, float v)
+{
+    Target t;
+    int rc = depth_target(p, target, t);
+    if (rc) return rc;
+    uint32_t bits;
+    memcpy(&bits, &v, 4);
+    int launches = 0;
+    launch_fill_u32(t.depth, t.scan, t.h, t.scan, bits, p->status, p->stream, launches);
+    p->stats.kernel_launches += launches;
+    return 0;
+}
+
+int fill_colour(ps3d_pipeline* p, uint32_t v)
+{
+    int launches = 0;
+    launch_fill_u32(p->colour, p->devW, p->devH, p->devW, v, p->status, p->stream, launches);
+    p->stats.kernel_launches += launches;
+    return 0;
+}
+
+int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps, size_t replayFrom)
+{
+    int seq = (int)p->passStart.size();
+    p->passStart.push_back(replayFrom);
+    const Command& c0 = cmds[ps.first];
+    int W = c0.vpW, H = c0.vpH;
+    Target tg;
+    int rc = depth_target(p, c0.depthTarget, tg);
+    if (rc) return rc;
+    std::vector<DrawDesc> dd;
+    std::vector<DrawUniforms> uu;
+    int nTris = 0, nvMax = 0;
+    bool anyColour = false;
+    for (size_t i = ps.first; i < ps.last; i++) {
+        DrawDesc d = cmds[i].desc;
+        if (d.triCount == 0) continue;
+        d.triBase = nTris;
+        d.uni = (int)uu.size();
+        nTris += d.triCount;
+        nvMax = std::max(nvMax, d.nv);
+        anyColour |= (d.flags & F_COLOUR) != 0;
+        dd.push_back(d);
+        uu.push_back(cmds[i].uni);
+    }
+    if (nTris == 0) {
+        if (ps.clearDepth) fill_depth(p, c0.depthTarget, ps.depthValue);
+        if (ps.clearColour) fill_colour(p, ps.colourValue);
+        return 0;
+    }
+    int binW = p->binW;
+    while ((long long)((W + binW - 1) / binW) * ((H + kBinH - 1) / kBinH) > max_bins() && binW < kMaxBinW) binW *= 2;
+    int binsX = (W + binW - 1) / binW, binsY = (H + kBinH - 1) / kBinH;
+    if ((long long)binsX * binsY > max_bins()) return fail(PS3D_ERR_INVALID, "viewport %dx%d has too many bins", W, H);
+    if ((rc = ensure_scratch(p, nTris, nvMax, W, H, binsX, binsY, anyColour))) return rc;
+    if (!dev_alloc(p->draws, p->drawsCap, dd.size()) || !dev_alloc(p->unis, p->unisCap, uu.size()))
+        return fail(PS3D_ERR_NOMEM, "device allocation for draw descriptors failed");
+    CU(cudaMemcpyAsync(p->draws, dd.data(), dd.size() * sizeof(DrawDesc), cudaMemcpyHostToDevice, p->stream));
+    CU(cudaMemcpyAsync(p->unis, uu.data(), uu.size() * sizeof(DrawUniforms), cudaMemcpyHostToDevice, p->stream));
+
+    // A clear fuses into the pass when the pass covers the whole buffer.
+    bool fuseDepth = ps.clearDepth && tg.w == W && tg.h == H && tg.scan == W;
+    bool fuseColour = ps.clearColour && p->devW == W && p->devH == H;
+    if (ps.clearDepth && !fuseDepth && (rc = fill_depth(p, c0.depthTarget, ps.depthValue))) return rc;
+    if (ps.clearColour && !fuseColour && (rc = fill_colour(p, ps.colourValue))) return rc;
+
+    PassParams P;
+    memset(&P, 0, sizeof P);
+    P.W = W;
+    P.H = H;
+    P.binW = binW;
+    P.binsX = binsX;
+    P.binsY = binsY;
+    P.nTris = nTris;
+    P.nDraws = (int)dd.size();
+    P.draws = p->draws;
+    P.unis = p->unis;
+    P.tris = p->tris;
+    P.vary = p->vary;
+    P.nvMax = std::max(nvMax, 1);
+    P.pairCount = p->pairCount;
+    P.rect = p->rect;
+    P.pairOffset = p->pairOffset;
+    P.pairKey = p->pairKey;
+    P.pairTri = p->pairTri;
+    P.pairCap = p->pairCap;
+    P.sortBlocks = (p->pairCap + kSortChunk - 1) / kSortChunk;
+    P.binHist = p->binHist;
+    P.binTri = p->binTri;
+    P.status = p->status;
+    P.depth = tg.depth;
+    P.depthScan = tg.scan;
+    P.depthW = tg.w;
+    P.depthH = tg.h;
+    P.winner = p->winner;
+    P.colour = p->colour;
+    P.colourW = p->devW;
+    P.colourH = p->devH;
+    P.clearDepth = fuseDepth;
+    P.clearColour = fuseColour;
+    P.anyColour = anyColour;
+    P.countFrags = p->countFrags;
+    P.depthClearValue = fuseDepth ? ps.depthValue : 1.0f;
+    P.colourClearValue = ps.colourValue;
+    P.passSeq = seq;
+    int launches = 0;
+    launch_setup_and_bin(P, p->scanTmp, p->stream, launches);
+    launch_raster_shade(P, p->stream, launches);
+    CU(cudaGetLastError());
+    p->stats.kernel_launches += launches;
+    p->stats.batches++;
+    p->stats.triangles += nTris;
+    return 0;
+}
+
+// Splits launched[from..] into passes and launches them.
+int launch_range(ps3d_pipeline* p, size_t from)
+{
+    const std::vector<Command>& cmds = p->launched;
+    size_t i = from, n = cmds.size();
+    int rc;
+    while (i < n) {
+        const Command& c = cmds[i];
+        Pass ps;
+        size_t j = i;
+        int depthClearTarget = -2;
+        // the clears in front of the next run of draws
+        for (; j < n && cmds[j].kind != Command::DRAW; j++) {
+            if (cmds[j].kind == Command::CLEAR_DEPTH) {
+                if (ps.clearDepth && depthClearTarget != cmds[j].depthTarget &&
+                    (rc = fill_depth(p, depthClearTarget, ps.depthValue)))
+                    return rc;
+                ps.clearDepth = true;
+                ps.depthValue = cmds[j].depthValue;
+                depthClearTarget = cmds[j].depthTarget;
+            } else {
+                ps.clearColour = true;
+                ps.colourValue = cmds[j].colourValue;
+            }
+        }
+        if (j == n) {
+            if (ps.clearDepth && (rc = fill_depth(p, depthClearTarget, ps.depthValue))) return rc;
+            if (ps.clearColour && (rc = fill_colour(p, ps.colourValue))) return rc;
+            break;
+        }
+        size_t k = j;
+        while (k < n && cmds[k].kind == Command::DRAW && cmds[k].depthTarget == cmds[j].depthTarget &&
+               cmds[k].vpW == cmds[j].vpW && cmds[k].vpH == cmds[j].vpH)
+            k++;
+        if (ps.clearDepth && depthClearTarget != cmds[j].depthTarget) {
+            if ((rc = fill_depth(p, depthClearTarget, ps.depthValue))) return rc;
+            ps.clearDepth = false;
+        }
+        ps.first = j;
+        ps.last = k;
+        if ((rc = run_pass(p, cmds, ps, i))) return rc;
+        (void)c;
+        i = k;
+    }
+    return 0;
+}
+
+int do_flush(ps3d_pipeline* p)
+{
+    if (p->pending.empty()) return 0;
+    size_t from = p->launched.size();
+    p->launched.insert(p->launched.end(), p->pending.begin(), p->pending.end());
+    p->pending.clear();
+    return launch_range(p, from);
+}
+
+// Waits for the stream.  If a pass ran out of bin-list room it set the
+// overflow flag and recorded its sequence number; it and every pass after it
+// did nothing, while the passes before it completed.  The buffers grow and
+// the commands are re-run from that pass (including the clears in front of
+// it, which are idempotent).
+int do_finish(ps3d_pipeline* p)
+{
+    int rc = do_flush(p);
+    if (rc) return rc;
+    for (int attempt = 0; attempt < 8; attempt++) {
+        CU(cudaStreamSynchronize(p->stream));
+        int st[4];
+        CU(cudaMemcpy(st, p->status, sizeof st, cudaMemcpyDeviceToHost));
+        if (!st[0]) {
+            p->launched.clear();
+            p->passStart.clear();
+            return 0;
+        }
+        int seq = st[3];
+        if (seq < 0 || seq >= (int)p->passStart.size()) return fail(PS3D_ERR_DEVICE, "bad overflow record");
+        p->pairCap = (int)std::min<long long>(std::max<long long>((long long)p->pairCap * 2, (long long)st[1] * 5 / 4 + 1024),
+                                              0x7fffffff);
+        CU(cudaMemsetAsync(p->status, 0, 4 * sizeof(int), p->stream));
+        p->stats.replays++;
+        size_t from = p->passStart[seq];
+        p->passStart.resize(seq);
+        if ((rc = launch_range(p, from))) return rc;
+    }
+    return fail(PS3D_ERR_NOMEM, "bin lists did not fit after growing the buffers");
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* ps3d_last_error(void) { return g_err.c_str(); }
+
+int ps3d_pipeline_create(int width, int height, void* stream, ps3d_pipeline** out)
+{
+    if (!out || width <= 0 || height <= 0) return fail(PS3D_ERR_INVALID, "bad pipeline size");
+    ps3d_pipeline* p = new (std::nothrow) ps3d_pipeline();
+    if (!p) return fail(PS3D_ERR_NOMEM, "host allocation failed");
+    p->devW = p->W = width;
+    p->devH = p->H = height;
+    if (const char* cap = getenv("PS3D_PAIR_CAP")) {
+        long v = atol(cap);
+        if (v >= 32 && v < (1L << 30)) p->pairCap = (int)v;
+    }
+    if (const char* bw = getenv("PS3D_BIN_W")) {
+        int v = atoi(bw);
+        if (v == 16 || v == 32 || v == 64) p->binW = v;
+    }
+    if (stream) p->stream = (cudaStream_t)stream;
+    else {
+        if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            delete p;
+            return fail(PS3D_ERR_DEVICE, "cudaStreamCreate failed");
+        }
+        p->ownStream = true;
+    }
+    p->defDepthScan = (int)(width / 4.0f + 0.5f) * 4;  // pipeline.cpp:31
+    if (p->defDepthScan < width) p->defDepthScan = (width + 3) / 4 * 4;
+    bool ok = cudaMalloc((void**)&p->colour, (size_t)width * 4 * height) == cudaSuccess &&
+              cudaMalloc((void**)&p->defDepth, (size_t)p->defDepthScan * 4 * height) == cudaSuccess &&
+              cudaMalloc((void**)&p->status, 64) == cudaSuccess;
+    if (!ok) {
+        ps3d_pipeline_destroy(p);
+        return fail(PS3D_ERR_NOMEM, "device allocation failed");
+    }
+    cudaMemsetAsync(p->colour, 0, (size_t)width * 4 * height, p->stream);
+    cudaMemsetAsync(p->defDepth, 0, (size_t)p->defDepthScan * 4 * height, p->stream);
+    cudaMemsetAsync(p->status, 0, 64, p->stream);
+    *out = p;
+    return 0;
+}
+
+int ps3d_pipeline_destroy(ps3d_pipeline* p)
+{
+    if (!p) return 0;
+    if (p->stream) cudaStreamSynchronize(p->stream);
+    for (auto& t : p->tex)
+        if (t.alive) cudaFree(t.dev);
+    for (auto& v : p->vaos)
+        for (auto* b : v.vbo)
+            if (b) {
+                cudaFree(b->dev);
+                delete b;
+            }
+    void* bufs[] = {p->colour, p->defDepth, p->status, p->tris, p->vary, p->pairCount, p->rect, p->pairOffset,
+                    p->pairKey, p->pairTri, p->binTri, p->binHist, p->scanTmp, p->winner, p->draws, p->unis};
+    for (void* b : bufs)
+        if (b) cudaFree(b);
+    if (p->ownStream && p->stream) cudaStreamDestroy(p->stream);
+    delete p;
+    return 0;
+}
+
+static int texture_create(ps3d_pipeline* p, int width, int height, int scanline, int elemLen, const void* pixels,
+                          int wrap, cudaMemcpyKind kind)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    if (elemLen != 1 && elemLen != 4) return fail(PS3D_ERR_INVALID, "elemLen must be 1 or 4 (fbo.cpp:21-24)");
+    if (width <= 0 || height <= 0 || scanline < width * elemLen) return fail(PS3D_ERR_INVALID, "bad texture size");
+    size_t slot = 0;
+    for (; slot < p->tex.size(); slot++)
+        if (!p->tex[slot].alive) break;
+    if (slot == p->tex.size()) p->tex.emplace_back();
+    Texture t;
+    t.width = width;
+    t.height = height;
+    t.scanline = scanline;
+    t.elemLen = elemLen;
+    t.wrap = wrap ? 1 : 0;
+    size_t bytes = (size_t)scanline * height;
+    if (cudaMalloc((void**)&t.dev, (bytes + 15) / 16 * 16) != cudaSuccess)
+        return fail(PS3D_ERR_NOMEM, "texture allocation of %zu bytes failed", bytes);
+    if (pixels) CU(cudaMemcpyAsync(t.dev, pixels, bytes, kind, p->stream));
+    else CU(cudaMemsetAsync(t.dev, 0, bytes, p->stream));
+    t.alive = true;
+    p->tex[slot] = t;
+    return (int)slot;
+}
+
+int ps3d_texture_create(ps3d_pipeline* p, int width, int height, int scanline, int elemLen, const void* pixels,
+                        int wrap)
+{
+    int rc = texture_create(p, width, height, scanline, elemLen, pixels, wrap, cudaMemcpyHostToDevice);
+    if (rc >= 0 && pixels && p) cudaStreamSynchronize(p->stream);  // the caller may free its pixels on return
+    return rc;
+}
+
+int ps3d_texture_create_device(ps3d_pipeline* p, int width, int height, int scanline, int elemLen,
+                               const void* devPixels, int wrap)
+{
+    return texture_create(p, width, height, scanline, elemLen, devPixels, wrap, cudaMemcpyDeviceToDevice);
+}
+
+int ps3d_texture_destroy(ps3d_pipeline* p, int idx)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    if (idx < 0 || idx >= (int)p->tex.size()) return fail(PS3D_ERR_RANGE, "texture %d", idx);
+    if (!p->tex[idx].alive) return 0;
+    int rc = do_finish(p);
+    if (rc) return rc;
+    if (p->depthTarget == idx) p->depthTarget = -1;
+    cudaFree(p->tex[idx].dev);
+    p->tex[idx] = Texture();
+    return 0;
+}
+
+int ps3d_texture_read(ps3d_pipeline* p, int idx, void* out, size_t bytes)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    if (!tex_ok(p, idx)) return fail(PS3D_ERR_RANGE, "texture %d", idx);
+    int rc = do_finish(p);
+    if (rc) return rc;
+    const Texture& t = p->tex[idx];
+    size_t n = std::min(bytes, (size_t)t.scanline * t.height);
+    CU(cudaMemcpyAsync(out, t.dev, n, cudaMemcpyDeviceToHost, p->stream));
+    CU(cudaStreamSynchronize(p->stream));
+    return 0;
+}
+
+int ps3d_texture_device_ptr(ps3d_pipeline* p, int idx, void** out)
+{
+    if (!p || !out) return fail(PS3D_ERR_INVALID, "null argument");
+    if (!tex_ok(p, idx)) return fail(PS3D_ERR_RANGE, "texture %d", idx);
+    *out = p->tex[idx].dev;
+    return 0;
+}
+
+int ps3d_processor_add(ps3d_pipeline* p, int id)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    if (!known_processor(id)) return fail(PS3D_ERR_INVALID, "unknown processor class 0x%04x", id);
+    size_t slot = 0;
+    for (; slot < p->procs.size(); slot++)
+        if (!p->procs[slot]) break;
+    if (slot == p->procs.size()) p->procs.push_back(0);
+    p->procs[slot] = id;
+    return (int)slot;
+}
+
+int ps3d_processor_destroy(ps3d_pipeline* p, int idx)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    if (idx < 0 || idx >= (int)p->procs.size()) return fail(PS3D_ERR_RANGE, "processor %d", idx);
+    int id = p->procs[idx];
+    if (!id) return 0;
+    // prog.cpp:32-37: a processor in use is unbound
+    if (p->vp == id) p->vp = 0;
+    if (p->ip == id) p->ip = 0;
+    if (p->fp == id) p->fp = 0;
+    p->procs[idx] = 0;
+    return 0;
+}
+
+int ps3d_programme_create(ps3d_pipeline* p, int vid, int iid, int fid)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    int n = (int)p->procs.size();
+    if (vid < 0 || vid >= n) return fail(PS3D_ERR_RANGE, "createProgramme, vid");
+    if (iid < 0 || iid >= n) return fail(PS3D_ERR_RANGE, "createProgramme, iid");
+    if (fid < 0 || fid >= n) return fail(PS3D_ERR_RANGE, "createProgramme, fid");
+    int v = p->procs[vid], i = p->procs[iid], f = p->procs[fid];
+    if ((i & 0xf) == 2 && (f & 0xf) == 3 && fp_needs(f)) {
+        if (fp_needs(f) != i || ((v & 0xf) == 1 && vp_gives(v) != i))
+            return fail(PS3D_ERR_INVALID, "processors 0x%04x/0x%04x/0x%04x do not share a varying layout", v, i, f);
+    }
+    size_t slot = 0;
+    for (; slot < p->progs.size(); slot++)
+        if (p->progs[slot].vp == -1) break;
+    if (slot == p->progs.size()) p->progs.emplace_back();
+    p->progs[slot].vp = vid;
+    p->progs[slot].ip = iid;
+    p->progs[slot].fp = fid;
+    return (int)slot;
+}
+
+int ps3d_programme_destroy(ps3d_pipeline* p, int idx)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    if (idx < 0 || idx >= (int)p->progs.size()) return fail(PS3D_ERR_RANGE, "destroyProgramme");
+    p->progs[idx] = Programme();
+    return 0;
+}
+
+int ps3d_programme_use(ps3d_pipeline* p, int idx)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    if (idx < 0 || idx >= (int)p->progs.size()) return fail(PS3D_ERR_RANGE, "useProgramme");
+    const Programme& g = p->progs[idx];
+    auto pick = [&](int slot, int kind) {
+        if (slot < 0 || slot >= (int)p->procs.size()) return 0;
+        int id = p->procs[slot];
+        return (id & 0xf) == kind ? id : 0;  // dynamic_cast yields NULL on a kind mismatch
+    };
+    p->vp = pick(g.vp, 1);
+    p->ip = pick(g.ip, 2);
+    p->fp = pick(g.fp, 3);
+    return 0;
+}
+
+int ps3d_vao_create(ps3d_pipeline* p)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    size_t slot = 0;
+    for (; slot < p->vaos.size(); slot++)
+        if (!p->vaos[slot].alive) break;
+    if (slot == p->vaos.size()) p->vaos.emplace_back();
+    p->vaos[slot] = Vao();
+    p->vaos[slot].alive = true;
+    return (int)slot;
+}
+
+int ps3d_vao_destroy(ps3d_pipeline* p, int vao)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    if (vao < 0 || vao >= (int)p->vaos.size()) return fail(PS3D_ERR_RANGE, "destroyVAO");
+    if (!p->vaos[vao].alive) return 0;
+    int rc = do_finish(p);
+    if (rc) return rc;
+    for (auto*& b : p->vaos[vao].vbo)
+        if (b) {
+            cudaFree(b->dev);
+            delete b;
+            b = nullptr;
+        }
+    p->vaos[vao].alive = false;
+    return 0;
+}
+
+static int vbo_attach(ps3d_pipeline* p, int vao, int slot, int unitBytes, int count, const void* data,
+                      cudaMemcpyKind kind)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    if (vao < 0 || vao >= (int)p->vaos.size() || !p->vaos[vao].alive) return fail(PS3D_ERR_RANGE, "attachVBO vao");
+    if (slot < 0 || slot >= PS3D_MAX_VBOS) return fail(PS3D_ERR_RANGE, "attachVBO idx");
+    if (unitBytes <= 0 || count < 0 || (unitBytes % 4)) return fail(PS3D_ERR_INVALID, "bad VBO layout");
+    if (p->vaos[vao].vbo[slot]) {
+        int rc = do_finish(p);
+        if (rc) return rc;
+        cudaFree(p->vaos[vao].vbo[slot]->dev);
+        delete p->vaos[vao].vbo[slot];
+        p->vaos[vao].vbo[slot] = nullptr;
+    }
+    Vbo* b = new (std::nothrow) Vbo();
+    if (!b) return fail(PS3D_ERR_NOMEM, "host allocation failed");
+    b->unitBytes = unitBytes;
+    b->count = count;
+    size_t bytes = (size_t)unitBytes * count;
+    if (cudaMalloc((void**)&b->dev, std::max<size_t>(bytes, 16)) != cudaSuccess) {
+        delete b;
+        return fail(PS3D_ERR_NOMEM, "VBO allocation failed");
+    }
+    if (data && bytes) CU(cudaMemcpyAsync(b->dev, data, bytes, kind, p->stream));
+    if (kind == cudaMemcpyHostToDevice) CU(cudaStreamSynchronize(p->stream));
+    p->vaos[vao].vbo[slot] = b;
+    return 0;
+}
+
+int ps3d_vbo_attach(ps3d_pipeline* p, int vao, int slot, int unitBytes, int count, const void* data)
+{
+    return vbo_attach(p, vao, slot, unitBytes, count, data, cudaMemcpyHostToDevice);
+}
+
+int ps3d_vbo_attach_device(ps3d_pipeline* p, int vao, int slot, int unitBytes, int count, const void* devData)
+{
+    return vbo_attach(p, vao, slot, unitBytes, count, devData, cudaMemcpyDeviceToDevice);
+}
+
+int ps3d_vbo_detach(ps3d_pipeline* p, int vao, int slot)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    if (vao < 0 || vao >= (int)p->vaos.size() || !p->vaos[vao].alive) return fail(PS3D_ERR_RANGE, "detachVBO vao");
+    if (slot < 0 || slot >= PS3D_MAX_VBOS) return fail(PS3D_ERR_RANGE, "detachVBO idx");
+    if (!p->vaos[vao].vbo[slot]) return 0;
+    int rc = do_finish(p);
+    if (rc) return rc;
+    cudaFree(p->vaos[vao].vbo[slot]->dev);
+    delete p->vaos[vao].vbo[slot];
+    p->vaos[vao].vbo[slot] = nullptr;
+    return 0;
+}
+
+int ps3d_set_uniform(ps3d_pipeline* p, int idx, const void* data, size_t len)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    if (idx < 0 || idx >= PS3D_MAX_UNIFORMS) return fail(PS3D_ERR_RANGE, "setUniform");
+    if (!data) p->uni[idx].clear();
+    else p->uni[idx].assign((const uint8_t*)data, (const uint8_t*)data + len);
+    return 0;
+}
+
+int ps3d_set_depth(ps3d_pipeline* p, int idx)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    if (idx == -1) {
+        p->depthTarget = -1;
+        return 0;
+    }
+    if (!tex_ok(p, idx)) return fail(PS3D_ERR_RANGE, "setDepth");
+    const Texture& t = p->tex[idx];
+    if (t.elemLen != 4 || t.scanline % 4) return fail(PS3D_ERR_INVALID, "setDepth: not an FP32 texture");
+    if (t.wrap) return fail(PS3D_ERR_INVALID, "setDepth: a depth target must be CLAMP-addressed");
+    p->depthTarget = idx;
+    return 0;
+}
+
+int ps3d_set_viewport(ps3d_pipeline* p, int width, int height)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    if (width <= 0 || height <= 0 || width > 32767 || height > 32767) return fail(PS3D_ERR_INVALID, "bad viewport");
+    p->W = width;
+    p->H = height;
+    return 0;
+}
+
+int ps3d_enable(ps3d_pipeline* p, int bits)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    p->behavior |= bits;
+    return 0;
+}
+
+int ps3d_disable(ps3d_pipeline* p, int bits)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    p->behavior &= ~bits;
+    return 0;
+}
+
+int ps3d_clear_depth(ps3d_pipeline* p, float v)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    Command c;
+    memset(&c, 0, sizeof c);
+    c.kind = Command::CLEAR_DEPTH;
+    c.depthTarget = p->depthTarget;
+    c.depthValue = v;
+    p->pending.push_back(c);
+    return 0;
+}
+
+int ps3d_clear_colour(ps3d_pipeline* p, uint32_t bgra)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    Command c;
+    memset(&c, 0, sizeof c);
+    c.kind = Command::CLEAR_COLOUR;
+    c.depthTarget = p->depthTarget;
+    c.colourValue = bgra;
+    p->pending.push_back(c);
+    return 0;
+}
+
+int ps3d_draw(ps3d_pipeline* p, int vao)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    // drawvao.cpp:12-15: silently nothing without a programme or with a bad VAO
+    if (!p->vp || !p->ip || !p->fp || vao < 0 || vao >= (int)p->vaos.size() || !p->vaos[vao].alive) return 0;
+    if (p->behavior & B_ALPHABLEND) return fail(PS3D_ERR_INVALID, "ALPHABLEND is not supported on this path");
+    const Vao& va = p->vaos[vao];
+    Command c;
+    memset(&c, 0, sizeof c);
+    c.kind = Command::DRAW;
+    c.depthTarget = p->depthTarget;
+    c.vpW = p->W;
+    c.vpH = p->H;
+    DrawDesc& d = c.desc;
+    d.vp = p->vp;
+    d.fp = p->fp;
+    int need = fp_needs(p->fp);
+    d.nv = need ? required_vary(need) : 0;
+    d.flags = (p->behavior & 0xf) | (p->fp != FP_DEF05 ? F_COLOUR : 0);
+    // processVertices stops at the first VBO that runs out (vertthrd.cpp:18-31)
+    long long minCount = -1;
+    for (int s = 0; s < PS3D_MAX_VBOS; s++)
+        if (va.vbo[s]) minCount = minCount < 0 ? va.vbo[s]->count : std::min<long long>(minCount, va.vbo[s]->count);
+    if (minCount < 0) return 0;
+    int reqSlots[5] = {1, 0, 0, 0, 0};
+    if (p->vp == VP_DEF01 && d.nv) reqSlots[3] = reqSlots[4] = 1;
+    if (p->vp == VP_LIT2 && d.nv) reqSlots[1] = reqSlots[3] = reqSlots[4] = 1;
+    for (int s = 0; s < kVboSlots; s++) {
+        if (reqSlots[s] && !va.vbo[s]) return fail(PS3D_ERR_INVALID, "the vertex processor reads VBO slot %d", s);
+        if (va.vbo[s]) {
+            d.vbo[s] = va.vbo[s]->dev;
+            d.stride[s] = va.vbo[s]->unitBytes;
+            int minBytes = s == 4 ? 8 : 16;
+            if (reqSlots[s] && va.vbo[s]->unitBytes < minBytes)
+                return fail(PS3D_ERR_INVALID, "VBO slot %d elements are %d bytes", s, va.vbo[s]->unitBytes);
+        }
+    }
+    d.triCount = (int)(minCount / 3);
+    int rc = snapshot_uniforms(p, c.uni);
+    if (rc) return rc;
+    Target tg;
+    if ((rc = depth_target(p, p->depthTarget, tg))) return rc;
+    if (tg.w < p->W || tg.h < p->H) return fail(PS3D_ERR_INVALID, "the depth target is smaller than the viewport");
+    if ((d.flags & F_COLOUR) && (p->devW < p->W || p->devH < p->H))
+        return fail(PS3D_ERR_INVALID, "the colour buffer is smaller than the viewport");
+    p->pending.push_back(c);
+    p->stats.draws++;
+    return 0;
+}
+
+int ps3d_flush(ps3d_pipeline* p)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    return do_flush(p);
+}
+
+int ps3d_finish(ps3d_pipeline* p)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    return do_finish(p);
+}
+
+int ps3d_read_colour(ps3d_pipeline* p, void* out)
+{
+    if (!p || !out) return fail(PS3D_ERR_INVALID, "null argument");
+    int rc = do_finish(p);
+    if (rc) return rc;
+    CU(cudaMemcpyAsync(out, p->colour, (size_t)p->devW * 4 * p->devH, cudaMemcpyDeviceToHost, p->stream));
+    CU(cudaStreamSynchronize(p->stream));
+    return 0;
+}
+
+int ps3d_read_depth(ps3d_pipeline* p, void* out)
+{
+    if (!p || !out) return fail(PS3D_ERR_INVALID, "null argument");
+    int rc = do_finish(p);
+    if (rc) return rc;
+    CU(cudaMemcpyAsync(out, p->defDepth, (size_t)p->defDepthScan * 4 * p->devH, cudaMemcpyDeviceToHost, p->stream));
+    CU(cudaStreamSynchronize(p->stream));
+    return 0;
+}
+
+int ps3d_colour_device_ptr(ps3d_pipeline* p, void** out)
+{
+    if (!p || !out) return fail(PS3D_ERR_INVALID, "null argument");
+    *out = p->colour;
+    return 0;
+}
+
+int ps3d_get_stream(ps3d_pipeline* p, void** out)
+{
+    if (!p || !out) return fail(PS3D_ERR_INVALID, "null argument");
+    *out = (void*)p->stream;
+    return 0;
+}
+
+int ps3d_set_fragment_counting(ps3d_pipeline* p, int on)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    p->countFrags = on != 0;
+    return 0;
+}
+
+int ps3d_stats(ps3d_pipeline* p, ps3d_stats_t* out)
+{
+    if (!p || !out) return fail(PS3D_ERR_INVALID, "null argument");
+    int rc = do_finish(p);
+    if (rc) return rc;
+    unsigned long long c[2];
+    CU(cudaMemcpy(c, p->status + 4, sizeof c, cudaMemcpyDeviceToHost));
+    *out = p->stats;
+    out->fragments = c[0];
+    out->fragments_passed = c[1];
+    return 0;
+}
+
+}  // extern "C"

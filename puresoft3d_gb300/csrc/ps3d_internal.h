@@ -1,0 +1,107 @@
+// ps3d_internal.h -- data shared between the host runtime (pipeline.cpp) and
+// the device kernels (raster.cu, shade.cu, bin.cu).  Not part of the C ABI.
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+namespace ps3d {
+
+constexpr int kMaxLevels = 16;
+constexpr int kMaxVary = 16;     // varying floats per vertex (LIT2: 16)
+constexpr int kVboSlots = 5;     // VBO slots the built-in vertex stages read (0..4)
+constexpr int kBinH = 32;        // bin height in rows: one warp lane per row
+constexpr int kMaxBinW = 64;
+
+// processor ids (include/ps3d.h)
+enum : int {
+    VP_DEF01 = 0x0101, IP_DEF01 = 0x0102, FP_DEF01 = 0x0103,
+    VP_DEF05 = 0x0501, IP_DEF05 = 0x0502, FP_DEF05 = 0x0503,
+    VP_SHADOW = 0x0601,
+    FP_LIT1 = 0x1103, FP_LIT3 = 0x1303,
+    VP_LIT2 = 0x1201, IP_LIT2 = 0x1202, FP_LIT2 = 0x1203,
+};
+
+// behaviour bits (reference pipeline.h:16-19) and per-draw flags
+enum : int {
+    B_UPDATE_DEPTH = 1, B_TEST_DEPTH = 2, B_FACE_CULLING = 4, B_ALPHABLEND = 8,
+    F_COLOUR = 16,   // the fragment stage writes colour
+};
+
+// One 2D texture level in device memory; row r starts at base + r*scanline
+// (rows bottom-up, reference tex.cpp:17).
+struct TexLevel {
+    const uint8_t* base;
+    int width, height, scanline, wrap;
+};
+
+// Per-draw snapshot of the uniforms and textures the built-in processors
+// read (uniform slot convention of the reference, tex1light1.cpp:15-20).
+struct DrawUniforms {
+    float PV[16], M[16], Mrot[16], LPV[16], PVM[16];
+    float light[4], cam[4], params[4];
+    TexLevel tex;                   // DEF01 / LIT1 texture
+    TexLevel albedo[kMaxLevels];    // LIT2 / LIT3 albedo chain
+    TexLevel normal[kMaxLevels];    // LIT2 normal-map chain (RGBA16F)
+    int albedoLevels, normalLevels;
+    const float* shadow;            // LIT2 shadow map (FP32, CLAMP)
+    int shadowSize, shadowScan;     // size and scanline in floats
+};
+
+struct DrawDesc {
+    int triBase, triCount;
+    int vp, fp;
+    int nv;      // varying floats per vertex carried by this draw's interpolation stage
+    int flags;   // behaviour bits | F_COLOUR
+    int uni;     // index into the batch's DrawUniforms
+    int pad;
+    const uint8_t* vbo[kVboSlots];
+    int stride[kVboSlots];
+};
+
+// Triangle after set-up (64 bytes).  vx/vy are the rasteriser's pixel-space
+// vertices (rasterizer.h:7-28), rw = 1/w, pz = NDC z per vertex.
+struct TriRaster {
+    float vx[3], vy[3], rw[3], pz[3];
+    short firstRow, lastRow;  // after clamping; firstRow > lastRow: nothing to draw
+    int split;                // rows <= split use the lower edge pair
+    int edges;                // 4 edges x (i0,i1) x 2 bits | flags << 16
+    int draw;
+};
+static_assert(sizeof(TriRaster) == 64, "TriRaster must be 64 bytes");
+
+// Kernel parameters of one device pass (a run of draws into one target).
+struct PassParams {
+    int W, H;                 // viewport = rasteriser size
+    int binW, binsX, binsY;   // bins of kBinH x binW pixels
+    int nTris, nDraws;
+    const DrawDesc* draws;
+    const DrawUniforms* unis;
+    TriRaster* tris;
+    float* vary;              // [tri][3][nvMax]
+    int nvMax;
+    int* pairCount;           // per triangle: bins its rectangle touches
+    int4* rect;               // per triangle: bin rectangle {x0, x1, y0, y1}
+    int* pairOffset;          // exclusive scan of pairCount (+ total at [nTris])
+    int* pairKey;             // bin of each (tri, bin) pair, in triangle order
+    int* pairTri;
+    int pairCap;              // capacity of pairKey / pairTri / binTri
+    int sortBlocks;           // pairCap / kSortChunk
+    int* binHist;             // [bin][sortBlock] counts, then their exclusive scan
+    int* binTri;              // triangles of each bin, in submission order
+    int* status;              // [0] overflow flag, [1] pairs needed, [2] bin-histogram length,
+                              // [3] overflowing pass, [4..5] fragments tested, [6..7] passed (u64)
+    float* depth;             // depth target (rows bottom-up)
+    int depthScan;            // in floats
+    int depthW, depthH;
+    int* winner;              // per viewport pixel: last colour-writing fragment that passed, or -1
+    uint8_t* colour;          // BGRA8, top-down
+    int colourW, colourH;
+    int clearDepth, clearColour, anyColour, countFrags;
+    float depthClearValue;
+    uint32_t colourClearValue;
+    int passSeq;              // recorded in status[3] when this pass overflows
+};
+
+constexpr int kSortChunk = 4096;   // pairs per stable-sort block
+
+}  // namespace ps3d

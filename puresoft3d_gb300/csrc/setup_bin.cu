@@ -1,0 +1,483 @@
+// setup_bin.cu -- vertex stage, triangle set-up and ordered tile binning.
+//
+//   k_setup    one thread per triangle: VBO fetch, vertex processor,
+//              perspective divide, back-face cull, z-reject and the
+//              rasteriser's triangle set-up (reference drawvao.cpp:36-63,
+//              vertthrd.cpp:14-65, rasterizer.cpp:73-234), plus the bin
+//              rectangle the triangle's spans can touch.
+//   scan       exclusive prefix sums (three-phase reduce / scan / down-sweep).
+//   k_emit     (bin, triangle) pairs in triangle order.
+//   k_hist / k_scatter
+//              a stable counting sort of the pairs by bin, so that each bin
+//              lists its triangles in submission order -- per pixel the
+//              reference applies fragments in that order (its per-row FIFO
+//              queues, drawvao.cpp:77-109), and the depth test's epsilon
+//              makes the order observable (fragthrd.cpp:227).
+#include <cuda_runtime.h>
+#include "device_common.cuh"
+
+namespace ps3d {
+
+// ----------------------------------------------------------------- vertex stage
+
+__device__ __forceinline__ void ld4(const uint8_t* p, float v[4])
+{
+    const float* f = (const float*)p;
+    v[0] = __ldg(f);
+    v[1] = __ldg(f + 1);
+    v[2] = __ldg(f + 2);
+    v[3] = __ldg(f + 3);
+}
+
+// Runs the draw's vertex processor on vertex `idx`; writes the clip position
+// and the varyings its interpolation stage carries.
+__device__ __forceinline__ void run_vp(const DrawDesc& d, const DrawUniforms& U, int idx, float pos[4], float* vary)
+{
+    float p[4];
+    ld4(d.vbo[0] + (size_t)idx * d.stride[0], p);
+    switch (d.vp) {
+    case VP_DEF01: {  // tex1light1.cpp:22-41
+        float wp[4], n[4], nrm[4];
+        m4v4(wp, U.M, p);
+        m4v4(pos, U.PV, wp);
+        if (d.nv) {
+            ld4(d.vbo[3] + (size_t)idx * d.stride[3], n);
+            m4v4(nrm, U.Mrot, n);
+            const float* uv = (const float*)(d.vbo[4] + (size_t)idx * d.stride[4]);
+            vary[0] = nrm[0]; vary[1] = nrm[1]; vary[2] = nrm[2]; vary[3] = nrm[3];
+            vary[4] = wp[0]; vary[5] = wp[1]; vary[6] = wp[2];
+            vary[7] = __ldg(uv); vary[8] = __ldg(uv + 1);
+        }
+        break;
+    }
+    case VP_DEF05: {  // shadow.cpp:21-29: positions x0.9 (mcemaths_mul_3), then (PV*M) * p
+        float a[4] = {fmul(p[0], 0.9f), fmul(p[1], 0.9f), fmul(p[2], 0.9f), p[3]};
+        m4v4(pos, U.PVM, a);
+        break;
+    }
+    case VP_SHADOW:
+        m4v4(pos, U.PVM, p);
+        break;
+    case VP_LIT2: {
+        float wp[4], sp[4], n[4], nrm[4], t[4], tan[4];
+        m4v4(wp, U.M, p);
+        m4v4(sp, U.LPV, wp);
+        m4v4(pos, U.PV, wp);
+        if (d.nv) {
+            ld4(d.vbo[3] + (size_t)idx * d.stride[3], n);
+            ld4(d.vbo[1] + (size_t)idx * d.stride[1], t);
+            float t3[4] = {t[0], t[1], t[2], 0.0f};
+            m4v4(nrm, U.Mrot, n);
+            m4v4(tan, U.Mrot, t3);
+            const float* uv = (const float*)(d.vbo[4] + (size_t)idx * d.stride[4]);
+            vary[0] = nrm[0]; vary[1] = nrm[1]; vary[2] = nrm[2];
+            vary[3] = tan[0]; vary[4] = tan[1]; vary[5] = tan[2]; vary[6] = t[3];
+            vary[7] = wp[0]; vary[8] = wp[1]; vary[9] = wp[2];
+            vary[10] = __ldg(uv); vary[11] = __ldg(uv + 1);
+            vary[12] = sp[0]; vary[13] = sp[1]; vary[14] = sp[2]; vary[15] = sp[3];
+        }
+        break;
+    }
+    default:
+        pos[0] = pos[1] = pos[2] = pos[3] = 0.0f;
+    }
+}
+
+// isBackFace (vertthrd.cpp:56-65): the z of cross(v1 - v0, v2 - v1) scaled by
+// rsqrtss(|c|^2), compared with 0.  The scale factor is finite and positive
+// exactly when |c|^2 (haddps order) is a finite normal number; otherwise the
+// reference's dot product is NaN or +-0 and the face is kept.
+__device__ __forceinline__ bool back_face(const float p[3][4])
+{
+    float a[4], b[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        a[k] = fsub(p[1][k], p[0][k]);
+        b[k] = fsub(p[2][k], p[1][k]);
+    }
+    float c0 = fsub(fmul(a[1], b[2]), fmul(a[2], b[1]));
+    float c1 = fsub(fmul(a[2], b[0]), fmul(a[0], b[2]));
+    float c2 = fsub(fmul(a[0], b[1]), fmul(a[1], b[0]));
+    float c3 = fsub(fmul(a[3], b[3]), fmul(a[3], b[3]));
+    float s = fadd(fadd(fmul(c0, c0), fmul(c1, c1)), fadd(fmul(c2, c2), fmul(c3, c3)));
+    if (!(s >= FLT_MIN && s <= FLT_MAX)) return false;
+    if (!isfinite(c0) || !isfinite(c1) || !isfinite(c3)) return false;
+    return c2 < 0.0f;
+}
+
+__device__ __forceinline__ int edge_code(int a, int b) { return a | (b << 2); }
+
+__global__ void k_setup(PassParams P)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= P.nTris) return;
+    int lo = 0, hi = P.nDraws - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (P.draws[mid].triBase <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    const DrawDesc& d = P.draws[lo];
+    const DrawUniforms& U = P.unis[d.uni];
+    int lt = t - d.triBase;
+
+    float pos[3][4], rw[3], pz[3];
+    float* vout = P.vary + (size_t)t * 3 * P.nvMax;
+#pragma unroll
+    for (int v = 0; v < 3; v++) {
+        float vary[kMaxVary];
+        run_vp(d, U, 3 * lt + v, pos[v], vary);
+        for (int k = 0; k < d.nv; k++) vout[v * P.nvMax + k] = vary[k];
+        float r = frcp(pos[v][3]);  // vertthrd.cpp:37-47: 1/w, then a 4-wide multiply
+#pragma unroll
+        for (int k = 0; k < 4; k++) pos[v][k] = fmul(pos[v][k], r);
+        pz[v] = pos[v][2];
+        rw[v] = r;
+    }
+
+    TriRaster tr;
+    tr.draw = lo;
+    tr.split = INT_MAX;
+    tr.edges = (d.flags & 0xff) << 16;
+    tr.firstRow = 1;
+    tr.lastRow = 0;
+    int count = 0;
+    bool keep = true;
+    if ((d.flags & B_FACE_CULLING) && back_face(pos)) keep = false;
+#pragma unroll
+    for (int v = 0; v < 3; v++)
+        if (pos[v][2] < -1.0f || pos[v][2] > 1.0f) keep = false;  // drawvao.cpp:51-56
+
+    const int W = P.W, H = P.H, halfW = W / 2, halfH = H / 2;
+#pragma unroll
+    for (int v = 0; v < 3; v++) {
+        tr.vx[v] = fadd(fmul((float)halfW, pos[v][0]), (float)halfW);  // rasterizer.cpp:73-77
+        tr.vy[v] = fadd(fmul((float)halfH, pos[v][1]), (float)halfH);
+        tr.rw[v] = rw[v];
+        tr.pz[v] = pz[v];
+    }
+    int bx0 = 0, bx1 = -1, by0 = 0, by1 = -1;
+    if (keep) {
+        const float* vx = tr.vx;
+        const float* vy = tr.vy;
+        // pushVertex's running min / max of (int)y (rasterizer.cpp:78-89)
+        int firstRow = f2i(vy[0]), lastRow = firstRow;
+#pragma unroll
+        for (int v = 1; v < 3; v++) {
+            if (vy[v] > (float)lastRow) lastRow = f2i(vy[v]);
+            else if (vy[v] < (float)firstRow) firstRow = f2i(vy[v]);
+        }
+        bool finite = isfinite(vx[0]) && isfinite(vx[1]) && isfinite(vx[2]) && isfinite(vy[0]) && isfinite(vy[1]) &&
+                      isfinite(vy[2]);
+        if (firstRow >= H || lastRow < 0) {  // rasterizer.cpp:149-168
+            firstRow = 0;
+            lastRow = -1;
+        }
+        if (firstRow < 0) firstRow = 0;
+        if (lastRow >= H) lastRow = H - 1;
+        if (finite && firstRow != lastRow && firstRow <= lastRow) {
+            int lower, upper = 0, split = INT_MAX;
+            if (vy[0] == vy[1]) {  // flat cases (rasterizer.cpp:171-203)
+                lower = vx[0] < vx[1] ? edge_code(0, 2) | (edge_code(1, 2) << 4) : edge_code(1, 2) | (edge_code(0, 2) << 4);
+            } else if (vy[0] == vy[2]) {
+                lower = vx[0] < vx[2] ? edge_code(0, 1) | (edge_code(2, 1) << 4) : edge_code(2, 1) | (edge_code(0, 1) << 4);
+            } else if (vy[1] == vy[2]) {
+                lower = vx[1] < vx[2] ? edge_code(1, 0) | (edge_code(2, 0) << 4) : edge_code(2, 0) | (edge_code(1, 0) << 4);
+            } else {  // sort by y, then split at the middle vertex (rasterizer.cpp:205-233, 121-140)
+                int top, bottom, third = 2, tmp;
+                if (vy[0] > vy[1]) { top = 0; bottom = 1; }
+                else { top = 1; bottom = 0; }
+                if (vy[top] < vy[third]) { tmp = top; top = third; third = tmp; }
+                else if (vy[bottom] > vy[third]) { tmp = bottom; bottom = third; third = tmp; }
+                Edge tt = mk_edge(vx, vy, top, third), tb = mk_edge(vx, vy, top, bottom);
+                float yt = sel3(vy, third);
+                if (edge_at(tb, yt) > edge_at(tt, yt)) {  // pointing left
+                    upper = edge_code(top, third) | (edge_code(top, bottom) << 4);
+                    lower = edge_code(third, bottom) | (edge_code(top, bottom) << 4);
+                } else {
+                    upper = edge_code(top, bottom) | (edge_code(top, third) << 4);
+                    lower = edge_code(top, bottom) | (edge_code(third, bottom) << 4);
+                }
+                // the lower half is processed second, so it owns the shared row
+                split = yt > (float)(H - 1) ? H - 1 : f2i(yt);
+            }
+            tr.edges |= lower | (upper << 8);
+            tr.split = split;
+            tr.firstRow = (short)firstRow;
+            tr.lastRow = (short)lastRow;
+            // Column bounds: edge_at is monotonic in y, so each half's span
+            // ends are extreme at that half's first and last rows.
+            int colLo = INT_MAX, colHi = INT_MIN;
+            int ra[2], rb[2], nh;
+            if (split == INT_MAX) {
+                ra[0] = firstRow; rb[0] = lastRow; nh = 1;
+            } else {
+                ra[0] = firstRow; rb[0] = min(split, lastRow);
+                ra[1] = max(split, firstRow - 1) + 1; rb[1] = lastRow; nh = 2;
+            }
+            for (int h = 0; h < nh; h++) {
+                if (ra[h] > rb[h]) continue;
+                int rows2[2] = {ra[h], rb[h]};
+#pragma unroll
+                for (int q = 0; q < 2; q++) {
+                    Span sp;
+                    span_row(tr, rows2[q], W, sp);
+                    colLo = min(colLo, min(sp.left, sp.right));
+                    colHi = max(colHi, max(sp.left, sp.right));
+                }
+            }
+            colLo = max(colLo, 0);
+            colHi = min(colHi, W - 1);
+            if (colLo <= colHi) {
+                bx0 = colLo / P.binW;
+                bx1 = colHi / P.binW;
+                by0 = firstRow / kBinH;
+                by1 = lastRow / kBinH;
+                count = (bx1 - bx0 + 1) * (by1 - by0 + 1);
+            }
+        }
+    }
+    if (count == 0) {
+        tr.firstRow = 1;
+        tr.lastRow = 0;
+    }
+    float4* dst = (float4*)(P.tris + t);
+    const float4* src = (const float4*)&tr;
+#pragma unroll
+    for (int k = 0; k < 4; k++) dst[k] = src[k];
+    P.pairCount[t] = count;
+    P.rect[t] = make_int4(bx0, bx1, by0, by1);
+}
+
+// ---------------------------------------------------------------- prefix sum
+
+constexpr int kScanBlock = 256;
+constexpr int kScanItems = 16;
+constexpr int kScanTile = kScanBlock * kScanItems;
+
+__device__ __forceinline__ int warp_incl_scan(int v)
+{
+    int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int n = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += n;
+    }
+    return v;
+}
+
+// Block-wide exclusive scan of one value per thread; returns the block total.
+__device__ __forceinline__ int block_excl_scan(int v, int& total)
+{
+    __shared__ int warpSums[kScanBlock / 32];
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int inc = warp_incl_scan(v);
+    if (lane == 31) warpSums[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        int s = lane < kScanBlock / 32 ? warpSums[lane] : 0;
+        s = warp_incl_scan(s);
+        if (lane < kScanBlock / 32) warpSums[lane] = s;
+    }
+    __syncthreads();
+    int base = wid ? warpSums[wid - 1] : 0;
+    total = warpSums[kScanBlock / 32 - 1];
+    __syncthreads();
+    return base + inc - v;
+}
+
+// n is read from *nPtr when nPtr != nullptr (sizes only known on the device).
+__global__ void k_scan_reduce(const int* in, int n, const int* nPtr, int* blockSums, const int* abortFlag)
+{
+    if (abortFlag && *abortFlag) return;
+    if (nPtr) n = *nPtr;
+    int base = blockIdx.x * kScanTile;
+    if (base >= n) return;
+    int s = 0;
+    for (int i = threadIdx.x; i < kScanTile; i += kScanBlock)
+        if (base + i < n) s += in[base + i];
+    int total;
+    block_excl_scan(s, total);
+    if (threadIdx.x == 0) blockSums[blockIdx.x] = total;
+}
+
+// Exclusive scan of the block sums in one block (up to kScanTile blocks).
+__global__ void k_scan_top(int* blockSums, int nBlocksMax, int n, const int* nPtr, const int* abortFlag)
+{
+    if (abortFlag && *abortFlag) return;
+    if (nPtr) n = *nPtr;
+    int nb = (n + kScanTile - 1) / kScanTile;
+    if (nb > nBlocksMax) nb = nBlocksMax;
+    int carry = 0;
+    for (int base = 0; base < nb; base += kScanBlock) {
+        int i = base + threadIdx.x;
+        int v = i < nb ? blockSums[i] : 0;
+        int total;
+        int ex = block_excl_scan(v, total);
+        if (i < nb) blockSums[i] = carry + ex;
+        carry += total;
+    }
+}
+
+// out[i] = exclusive prefix of in (in-place allowed); out[n] = total when
+// writeTotal.
+__global__ void k_scan_down(const int* in, int* out, int n, const int* nPtr, const int* blockSums, int writeTotal,
+                            const int* abortFlag)
+{
+    if (abortFlag && *abortFlag) return;
+    if (nPtr) n = *nPtr;
+    int base = blockIdx.x * kScanTile;
+    if (base >= n) return;
+    int v[kScanItems], s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        int i = base + threadIdx.x * kScanItems + k;
+        v[k] = i < n ? in[i] : 0;
+        s += v[k];
+    }
+    int total;
+    int ex = block_excl_scan(s, total) + blockSums[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        int i = base + threadIdx.x * kScanItems + k;
+        if (i < n) out[i] = ex;
+        ex += v[k];
+        if (writeTotal && i == n - 1) out[n] = ex;
+    }
+}
+
+// ------------------------------------------------------------------- binning
+
+// Writes the (bin, triangle) pairs.  If they would not fit, raises the
+// overflow flag instead; every later kernel of the flush then does nothing
+// and the host re-runs the pass with room for status[1] pairs.
+__global__ void k_emit(PassParams P)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (P.status[0]) return;
+    int total = P.pairOffset[P.nTris];
+    if (total > P.pairCap) {
+        if (t == 0) {
+            P.status[1] = total;
+            P.status[2] = 0;
+            P.status[3] = P.passSeq;
+            __threadfence();
+            atomicExch(P.status, 1);
+        }
+        return;
+    }
+    if (t == 0) P.status[2] = P.binsX * P.binsY * ((total + kSortChunk - 1) / kSortChunk);
+    if (t >= P.nTris) return;
+    int count = P.pairCount[t];
+    if (!count) return;
+    int4 r = P.rect[t];
+    int o = P.pairOffset[t];
+    for (int by = r.z; by <= r.w; by++)
+        for (int bx = r.x; bx <= r.y; bx++) {
+            P.pairKey[o] = by * P.binsX + bx;
+            P.pairTri[o] = t;
+            o++;
+        }
+}
+
+// Per sort block (kSortChunk consecutive pairs, one warp): counts per bin,
+// stored bin-major ([bin][block]) so that one exclusive scan over the array
+// yields each (bin, block)'s first output position.
+__global__ void k_hist(PassParams P)
+{
+    extern __shared__ int cnt[];
+    if (P.status[0]) return;
+    int total = P.pairOffset[P.nTris];
+    int nb = (total + kSortChunk - 1) / kSortChunk;
+    int b = blockIdx.x;
+    if (b >= nb) return;
+    int nBins = P.binsX * P.binsY;
+    for (int i = threadIdx.x; i < nBins; i += 32) cnt[i] = 0;
+    __syncwarp();
+    int lane = threadIdx.x;
+    int end = min(total, (b + 1) * kSortChunk);
+    for (int base = b * kSortChunk; base < end; base += 32) {
+        int i = base + lane;
+        int key = i < end ? P.pairKey[i] : -1 - lane;
+        unsigned peers = __match_any_sync(0xffffffffu, key);
+        if (i < end && lane == __ffs(peers) - 1) cnt[key] += __popc(peers);
+        __syncwarp();
+    }
+    __syncwarp();
+    for (int i = lane; i < nBins; i += 32) P.binHist[(size_t)i * nb + b] = cnt[i];
+}
+
+// Stable scatter: each pair lands at its (bin, block) base plus its rank
+// among same-bin pairs earlier in the block.
+__global__ void k_scatter(PassParams P)
+{
+    extern __shared__ int cnt[];
+    if (P.status[0]) return;
+    int total = P.pairOffset[P.nTris];
+    int nb = (total + kSortChunk - 1) / kSortChunk;
+    int b = blockIdx.x;
+    if (b >= nb) return;
+    int nBins = P.binsX * P.binsY;
+    int lane = threadIdx.x;
+    for (int i = lane; i < nBins; i += 32) cnt[i] = P.binHist[(size_t)i * nb + b];
+    __syncwarp();
+    unsigned lt = (1u << lane) - 1u;
+    int end = min(total, (b + 1) * kSortChunk);
+    for (int base = b * kSortChunk; base < end; base += 32) {
+        int i = base + lane;
+        int key = i < end ? P.pairKey[i] : -1 - lane;
+        unsigned peers = __match_any_sync(0xffffffffu, key);
+        int pos = 0;
+        if (i < end) pos = cnt[key] + __popc(peers & lt);
+        __syncwarp();
+        if (i < end) {
+            P.binTri[pos] = P.pairTri[i];
+            if (lane == __ffs(peers) - 1) cnt[key] += __popc(peers);
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------ launches
+
+static inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+void scan_exclusive(const int* in, int* out, int n, const int* nPtr, int nMax, int* blockSums, int writeTotal,
+                    const int* abortFlag, cudaStream_t s, int& launches)
+{
+    int nb = ceil_div(nMax > 0 ? nMax : 1, kScanTile);
+    k_scan_reduce<<<nb, kScanBlock, 0, s>>>(in, n, nPtr, blockSums, abortFlag);
+    k_scan_top<<<1, kScanBlock, 0, s>>>(blockSums, nb, n, nPtr, abortFlag);
+    k_scan_down<<<nb, kScanBlock, 0, s>>>(in, out, n, nPtr, blockSums, writeTotal, abortFlag);
+    launches += 3;
+}
+
+int scan_block_sums_needed(int nMax) { return ceil_div(nMax > 0 ? nMax : 1, kScanTile) + 1; }
+
+// Largest bin grid whose per-bin counters fit in one block's shared memory.
+int max_bins() { return (227 * 1024) / (int)sizeof(int); }
+
+void launch_setup_and_bin(const PassParams& P, int* scanTmp, cudaStream_t s, int& launches)
+{
+    static bool attrs = false;
+    if (!attrs) {
+        cudaFuncSetAttribute(k_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        cudaFuncSetAttribute(k_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        attrs = true;
+    }
+    int nBins = P.binsX * P.binsY;
+    k_setup<<<ceil_div(P.nTris, 128), 128, 0, s>>>(P);
+    launches++;
+    scan_exclusive(P.pairCount, P.pairOffset, P.nTris, nullptr, P.nTris, scanTmp, 1, P.status, s, launches);
+    k_emit<<<ceil_div(P.nTris, 256), 256, 0, s>>>(P);
+    launches++;
+    size_t smem = (size_t)nBins * sizeof(int);
+    k_hist<<<P.sortBlocks, 32, smem, s>>>(P);
+    launches++;
+    // binHist holds nBins * nb counts, nb known on the device only
+    scan_exclusive(P.binHist, P.binHist, 0, P.status + 2, nBins * P.sortBlocks, scanTmp, 0, P.status, s, launches);
+    k_scatter<<<P.sortBlocks, 32, smem, s>>>(P);
+    launches++;
+}
+
+}  // namespace ps3d

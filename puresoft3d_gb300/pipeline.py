@@ -1,0 +1,232 @@
+"""Python binding of the C ABI (include/ps3d.h) with the reference's method
+names (PuresoftPipeline, src/puresoft3d/pipeline.h:26-69), so scenes and tests
+drive the GPU pipeline exactly as the reference's demos drive theirs.
+
+The library is the in-tree CUDA build (puresoft3d_gb300/_lib/libps3d.so).
+There is no CPU fallback: if the library or a GPU is missing, construction
+raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+PS3D_OK = 0
+ERRORS = {-1: IndexError, -2: ValueError, -3: MemoryError, -4: RuntimeError, -5: TimeoutError}
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in ("draws", "batches", "kernel_launches", "triangles", "fragments",
+                                                "fragments_passed", "replays")]
+
+
+_lib = None
+_c_int, _c_void_p, _c_size_t = ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t
+_SIGS = {
+    "ps3d_pipeline_create": [_c_int, _c_int, _c_void_p, ctypes.POINTER(_c_void_p)],
+    "ps3d_pipeline_destroy": [_c_void_p],
+    "ps3d_texture_create": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p, _c_int],
+    "ps3d_texture_create_device": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p, _c_int],
+    "ps3d_texture_destroy": [_c_void_p, _c_int],
+    "ps3d_texture_read": [_c_void_p, _c_int, _c_void_p, _c_size_t],
+    "ps3d_texture_device_ptr": [_c_void_p, _c_int, ctypes.POINTER(_c_void_p)],
+    "ps3d_processor_add": [_c_void_p, _c_int],
+    "ps3d_processor_destroy": [_c_void_p, _c_int],
+    "ps3d_programme_create": [_c_void_p, _c_int, _c_int, _c_int],
+    "ps3d_programme_destroy": [_c_void_p, _c_int],
+    "ps3d_programme_use": [_c_void_p, _c_int],
+    "ps3d_vao_create": [_c_void_p],
+    "ps3d_vao_destroy": [_c_void_p, _c_int],
+    "ps3d_vbo_attach": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p],
+    "ps3d_vbo_attach_device": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p],
+    "ps3d_vbo_detach": [_c_void_p, _c_int, _c_int],
+    "ps3d_set_uniform": [_c_void_p, _c_int, _c_void_p, _c_size_t],
+    "ps3d_set_depth": [_c_void_p, _c_int],
+    "ps3d_set_viewport": [_c_void_p, _c_int, _c_int],
+    "ps3d_enable": [_c_void_p, _c_int],
+    "ps3d_disable": [_c_void_p, _c_int],
+    "ps3d_clear_depth": [_c_void_p, ctypes.c_float],
+    "ps3d_clear_colour": [_c_void_p, ctypes.c_uint32],
+    "ps3d_draw": [_c_void_p, _c_int],
+    "ps3d_flush": [_c_void_p],
+    "ps3d_finish": [_c_void_p],
+    "ps3d_read_colour": [_c_void_p, _c_void_p],
+    "ps3d_read_depth": [_c_void_p, _c_void_p],
+    "ps3d_colour_device_ptr": [_c_void_p, ctypes.POINTER(_c_void_p)],
+    "ps3d_get_stream": [_c_void_p, ctypes.POINTER(_c_void_p)],
+    "ps3d_set_fragment_counting": [_c_void_p, _c_int],
+    "ps3d_stats": [_c_void_p, ctypes.POINTER(Stats)],
+}
+
+
+def library(path: str | None = None) -> ctypes.CDLL:
+    """Loads (building first if stale) the in-tree CUDA library."""
+    global _lib
+    if _lib is None:
+        path = path or _build.LIB
+        if not os.path.exists(path):
+            path = _build.build()
+        lib = ctypes.CDLL(path)
+        for name, args in _SIGS.items():
+            f = getattr(lib, name)
+            f.argtypes = args
+            f.restype = ctypes.c_int
+        lib.ps3d_last_error.restype = ctypes.c_char_p
+        lib.ps3d_last_error.argtypes = []
+        _lib = lib
+    return _lib
+
+
+def exported_symbols() -> list:
+    return sorted(list(_SIGS) + ["ps3d_last_error"])
+
+
+class PuresoftPipeline:
+    """GPU pipeline with the reference's API.  Indices returned by the create
+    calls follow the reference's vacant-slot policy."""
+
+    def __init__(self, width: int, height: int, stream: int | None = None):
+        self.lib = library()
+        h = ctypes.c_void_p()
+        self._check(self.lib.ps3d_pipeline_create(width, height, stream, ctypes.byref(h)))
+        self.h = h
+        self.width, self.height = width, height
+        self._tex = {}
+
+    def _check(self, rc: int) -> int:
+        if rc < 0:
+            msg = self.lib.ps3d_last_error().decode(errors="replace")
+            raise ERRORS.get(rc, RuntimeError)(msg)
+        return rc
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ps3d_pipeline_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- textures
+    def createTexture(self, width, height, scanline, elem_len, pixels=None, wrap=0) -> int:
+        ptr = None
+        if pixels is not None:
+            pixels = np.ascontiguousarray(pixels)
+            if pixels.nbytes != scanline * height:
+                raise ValueError("pixel buffer is %d bytes, expected %d" % (pixels.nbytes, scanline * height))
+            ptr = pixels.ctypes.data
+        idx = self._check(self.lib.ps3d_texture_create(self.h, width, height, scanline, elem_len, ptr, int(wrap)))
+        self._tex[idx] = (width, height, scanline, elem_len)
+        return idx
+
+    def destroyTexture(self, idx):
+        self._check(self.lib.ps3d_texture_destroy(self.h, idx))
+        self._tex.pop(idx, None)
+
+    def readTexture(self, idx) -> np.ndarray:
+        w, h, scan, elem = self._tex[idx]
+        out = np.empty((h, scan), dtype=np.uint8)
+        self._check(self.lib.ps3d_texture_read(self.h, idx, out.ctypes.data, out.nbytes))
+        return out
+
+    def readDepthTexture(self, idx) -> np.ndarray:
+        w, h, scan, elem = self._tex[idx]
+        return self.readTexture(idx).view(np.float32)[:, :w]
+
+    # -- processors and programmes
+    def addProcessor(self, pid) -> int:
+        return self._check(self.lib.ps3d_processor_add(self.h, pid))
+
+    def destroyProcessor(self, idx):
+        self._check(self.lib.ps3d_processor_destroy(self.h, idx))
+
+    def createProgramme(self, v, i, f) -> int:
+        return self._check(self.lib.ps3d_programme_create(self.h, v, i, f))
+
+    def destroyProgramme(self, idx):
+        self._check(self.lib.ps3d_programme_destroy(self.h, idx))
+
+    def useProgramme(self, idx):
+        self._check(self.lib.ps3d_programme_use(self.h, idx))
+
+    # -- vertex arrays
+    def createVAO(self) -> int:
+        return self._check(self.lib.ps3d_vao_create(self.h))
+
+    def destroyVAO(self, vao):
+        self._check(self.lib.ps3d_vao_destroy(self.h, vao))
+
+    def attachVBO(self, vao, slot, arr):
+        arr = np.ascontiguousarray(arr)
+        self._check(self.lib.ps3d_vbo_attach(self.h, vao, slot, arr.nbytes // max(len(arr), 1), len(arr),
+                                             arr.ctypes.data))
+
+    def detachVBO(self, vao, slot):
+        self._check(self.lib.ps3d_vbo_detach(self.h, vao, slot))
+
+    # -- state
+    def setUniform(self, idx, data):
+        if data is None:
+            self._check(self.lib.ps3d_set_uniform(self.h, idx, None, 0))
+            return
+        data = np.ascontiguousarray(data)
+        self._check(self.lib.ps3d_set_uniform(self.h, idx, data.ctypes.data, data.nbytes))
+
+    def setDepth(self, idx=-1):
+        self._check(self.lib.ps3d_set_depth(self.h, idx))
+
+    def setViewport(self, w, h):
+        self._check(self.lib.ps3d_set_viewport(self.h, w, h))
+
+    def enable(self, bits):
+        self._check(self.lib.ps3d_enable(self.h, bits))
+
+    def disable(self, bits):
+        self._check(self.lib.ps3d_disable(self.h, bits))
+
+    def clearDepth(self, v=1.0):
+        self._check(self.lib.ps3d_clear_depth(self.h, v))
+
+    def clearColour(self, bgra=0):
+        self._check(self.lib.ps3d_clear_colour(self.h, bgra))
+
+    def drawVAO(self, vao):
+        self._check(self.lib.ps3d_draw(self.h, vao))
+
+    def flush(self):
+        self._check(self.lib.ps3d_flush(self.h))
+
+    def finish(self):
+        self._check(self.lib.ps3d_finish(self.h))
+
+    # -- read-back
+    def readColour(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty((self.height, self.width, 4), dtype=np.uint8)
+        self._check(self.lib.ps3d_read_colour(self.h, out.ctypes.data))
+        return out
+
+    def colourDevicePtr(self) -> int:
+        v = ctypes.c_void_p()
+        self._check(self.lib.ps3d_colour_device_ptr(self.h, ctypes.byref(v)))
+        return v.value
+
+    def stream(self) -> int:
+        v = ctypes.c_void_p()
+        self._check(self.lib.ps3d_get_stream(self.h, ctypes.byref(v)))
+        return v.value
+
+    def setFragmentCounting(self, on: bool):
+        self._check(self.lib.ps3d_set_fragment_counting(self.h, int(on)))
+
+    def stats(self) -> dict:
+        s = Stats()
+        self._check(self.lib.ps3d_stats(self.h, ctypes.byref(s)))
+        return {n: int(getattr(s, n)) for n, _ in Stats._fields_}

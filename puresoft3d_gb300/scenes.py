@@ -357,7 +357,11 @@ class _Builder:
         return self.ntex - 1
 
     def empty_texture(self, width: int, height: int, elem_len: int = 4, wrap: bool = False) -> int:
-        self.setup.append(("createTexture", width, height, width * elem_len, elem_len, None, int(wrap)))
+        """A zeroed texture; for depth targets the scanline is rounded up to
+        whole 16-byte vectors as the reference's default depth buffer does
+        (pipeline.cpp:31) -- its clear16 requires it (fbo.cpp:348-371)."""
+        scan = (width * elem_len + 15) // 16 * 16
+        self.setup.append(("createTexture", width, height, scan, elem_len, None, int(wrap)))
         self.ntex += 1
         return self.ntex - 1
 
@@ -437,7 +441,7 @@ def _random_rotation(rng) -> np.ndarray:
 
 
 def scene_c2(seed: int = 1236, width: int = 1920, height: int = 1080, shadow_size: int = 2048,
-             meshes: int = 64, tex_size: int = 1024) -> Scene:
+             meshes: int = 64, tex_size: int = 1024, spread: float = 20.0) -> Scene:
     """Config 2: 64 seeded meshes (sphere / torus / box, uniform type, scale
     U[0.2, 2], rotation uniform on SO(3), position U[-20, 20]^3), ~200k
     triangles; four tex_size^2 BGRA8 albedo mip chains and one RGBA16F
@@ -460,18 +464,19 @@ def scene_c2(seed: int = 1236, width: int = 1920, height: int = 1080, shadow_siz
         mesh = uv_sphere(40, 40) if kind == 0 else torus(40, 40) if kind == 1 else box(16)
         scale = float(rng.uniform(0.2, 2.0))
         R = _random_rotation(rng)
-        pos = rng.uniform(-20, 20, size=3)
+        pos = rng.uniform(-spread, spread, size=3)
         M = translation(*pos) @ R @ scaling(scale)
         vao = b.vao(mesh)
         tri_total += mesh_triangles(mesh)
         objs.append((vao, M, R, albedo[int(rng.integers(0, 4))], scale, kind))
-    eye = np.array([0.0, 10.0, 55.0])
-    P = perspective(1.0, 200.0, width / height, math.radians(60.0))
+    eye = np.array([0.0, 10.0, 55.0]) * (spread / 20.0)
+    P = perspective(1.0 * spread / 20.0, 200.0 * spread / 20.0, width / height, math.radians(60.0))
     V = look_at(eye, (0, 0, 0), (0, 1, 0))
     light = np.array([0.4, 0.8, 0.45])
     light /= np.linalg.norm(light)
-    LV = look_at(light * 70.0, (0, 0, 0), (0, 1, 0))
-    LP = orthographic(1.0, 140.0, -38.0, 38.0, -38.0, 38.0)
+    k = spread / 20.0
+    LV = look_at(light * 70.0 * k, (0, 0, 0), (0, 1, 0))
+    LP = orthographic(1.0 * k, 140.0 * k, -38.0 * k, 38.0 * k, -38.0 * k, 38.0 * k)
     LPV = col_major(LP @ LV)
     focal = (height / 2) / math.tan(math.radians(30.0))
     # shadow pass

@@ -1,0 +1,117 @@
+"""Known-answer scenes for the rasteriser, interpolator and depth test.
+
+Each scene feeds clip-space positions straight through (PV = M = identity),
+so a case states exactly which pixels and depths it exercises: flat tops and
+bottoms, left- and right-pointing triangles, edges off every side of the
+viewport, shared edges (the depth test's -1e-4 epsilon, reference
+fragthrd.cpp:227), equal-depth overlaps (first one wins), zero-area and
+needle triangles, back faces with and without culling, z-reject
+(drawvao.cpp:51-56), depth test off, strong perspective, and a seeded random
+soup with heavy overlap.  Odd viewport sizes exercise the integer half-size
+viewport mapping (rasterizer.cpp:30-31).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from puresoft3d_gb300 import scenes as S
+
+
+def _tri_mesh(clip):
+    """clip: (n_tris*3, 4) positions -> a mesh with normal/uv varyings."""
+    clip = np.asarray(clip, dtype=np.float32).reshape(-1, 4)
+    n = len(clip)
+    idx = np.arange(n)
+    normal = np.stack([np.sin(idx * 0.7), np.cos(idx * 0.3), np.ones(n) * 0.5, np.zeros(n)], 1).astype(np.float32)
+    uv = np.stack([(idx % 7) / 3.0 - 0.5, (idx % 5) / 2.0 - 0.25], 1).astype(np.float32)
+    return {"position": clip, "normal": normal, "uv": uv, "tangent": np.tile([1, 0, 0, 1], (n, 1)).astype(np.float32)}
+
+
+def _scene(name, w, h, clip, lit=True, behavior_off=0, texture_seed=7):
+    b = S._Builder()
+    rng = np.random.default_rng(texture_seed)
+    tex = b.texture(S.checker_noise_bgra(16, 4, rng))
+    depth = b.empty_texture(w, h)
+    prog = b.programme(S.VP_DEF01, S.IP_DEF01, S.FP_LIT1) if lit else b.programme(S.VP_SHADOW, S.IP_DEF05,
+                                                                                  S.FP_DEF05)
+    mesh = _tri_mesh(clip)
+    vao = b.vao(mesh, slots=(0, 3, 4) if lit else (0,))
+    eye = np.eye(4)
+    b.f("setDepth", depth)
+    b.f("clearDepth", 1.0)
+    b.f("clearColour", 0xFF101010)
+    if behavior_off:
+        b.f("disable", behavior_off)
+    b.f("useProgramme", prog)
+    b.f("setUniform", 3, S.col_major(eye))
+    b.f("setUniform", 4, S.col_major(eye))
+    b.f("setUniform", 5, S.col_major(eye))
+    b.f("setUniform", 7, S.vec4(0.3, 0.5, 0.81))
+    b.f("setUniform", 8, S.vec4(0, 0, 2, 1))
+    b.f("setUniform", 9, np.array([tex], dtype=np.int32))
+    b.f("drawVAO", vao)
+    return S.Scene(name, w, h, b.setup, b.frame, {"triangles": len(mesh["position"]) // 3, "depth_texture": depth})
+
+
+def _v(x, y, z=0.0, w=1.0):
+    return [x * w, y * w, z * w, w]
+
+
+def basic_cases(w=64, h=48):
+    """Hand-placed triangles (counter-clockwise = front)."""
+    T = []
+    T += [_v(-0.9, 0.5, 0.1), _v(-0.5, 0.5, 0.1), _v(-0.7, 0.9, 0.1)]      # flat bottom
+    T += [_v(-0.3, 0.9, 0.2), _v(-0.5, 0.5, 0.2), _v(-0.1, 0.9, 0.2)]      # flat top
+    T += [_v(0.1, 0.3, 0.3), _v(0.5, 0.5, 0.3), _v(0.2, 0.9, 0.3)]         # right-pointing
+    T += [_v(0.9, 0.3, 0.3), _v(0.8, 0.9, 0.3), _v(0.6, 0.6, 0.3)]         # left-pointing
+    T += [_v(-1.4, -0.2, 0.0), _v(-0.8, -0.1, 0.0), _v(-1.1, 0.25, 0.0)]    # off the left edge
+    T += [_v(0.8, -0.2, 0.0), _v(1.5, -0.1, 0.0), _v(1.1, 0.25, 0.0)]      # off the right edge
+    T += [_v(-0.2, 0.85, 0.0), _v(0.2, 0.85, 0.0), _v(0.0, 1.4, 0.0)]      # off the top
+    T += [_v(-0.2, -1.5, 0.0), _v(0.2, -0.85, 0.0), _v(-0.3, -0.8, 0.0)]   # off the bottom
+    T += [_v(-0.6, -0.6, 0.5), _v(-0.2, -0.6, 0.5), _v(-0.2, -0.2, 0.5)]   # quad, shared diagonal
+    T += [_v(-0.6, -0.6, 0.5), _v(-0.2, -0.2, 0.5), _v(-0.6, -0.2, 0.5)]
+    T += [_v(0.0, -0.6, 0.4), _v(0.4, -0.6, 0.4), _v(0.2, -0.2, 0.4)]      # equal-depth overlap pair
+    T += [_v(0.05, -0.55, 0.4), _v(0.45, -0.55, 0.4), _v(0.25, -0.15, 0.4)]
+    T += [_v(0.5, -0.6, 0.40005), _v(0.9, -0.6, 0.40005), _v(0.7, -0.2, 0.40005)]  # within epsilon
+    T += [_v(0.5, -0.6, 0.3999), _v(0.9, -0.6, 0.3999), _v(0.7, -0.2, 0.3999)]     # beyond epsilon
+    T += [_v(0.1, 0.1, 0.0), _v(0.1, 0.1, 0.0), _v(0.3, 0.2, 0.0)]         # zero area (repeated vertex)
+    T += [_v(-0.5, 0.0, 0.0), _v(0.0, 0.0, 0.0), _v(0.5, 0.0, 0.0)]        # collinear, horizontal
+    T += [_v(-0.95, -0.95, 0.0), _v(0.95, -0.9, 0.0), _v(-0.95, -0.93, 0.0)]  # needle, tiny dy
+    T += [_v(0.6, 0.0, 0.2), _v(0.62, 0.0, 0.2), _v(0.61, 0.8, 0.2)]       # thin vertical sliver
+    T += [_v(-0.1, -0.1, 0.2), _v(-0.3, 0.1, 0.2), _v(0.1, 0.1, 0.2)]      # back face (clockwise)
+    T += [_v(-0.9, -0.9, 1.2), _v(-0.7, -0.9, 0.0), _v(-0.8, -0.7, 0.0)]   # z-reject: z > 1
+    T += [_v(0.3, -0.95, -1.3), _v(0.5, -0.95, 0.0), _v(0.4, -0.7, 0.0)]   # z-reject: z < -1
+    T += [_v(-0.3, -0.3, -0.2, 0.5), _v(0.3, -0.3, 0.6, 3.0), _v(0.0, 0.3, 0.2, 1.2)]  # perspective
+    pix = [[(2 * px / w - 1), (2 * py / h - 1)] for px, py in ((10, 5), (20, 5), (15, 15))]
+    T += [_v(pix[0][0], pix[0][1], -0.5), _v(pix[1][0], pix[1][1], -0.5), _v(pix[2][0], pix[2][1], -0.5)]
+    return np.array(T, dtype=np.float32)
+
+
+def random_soup(n, seed, persp=True):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        c = rng.uniform(-1.1, 1.1, size=2)
+        z = rng.uniform(-0.95, 0.95)
+        size = rng.uniform(0.02, 0.7)
+        for _v_ in range(3):
+            w = rng.uniform(0.6, 2.5) if persp else 1.0
+            p = c + rng.normal(size=2) * size
+            zz = np.clip(z + rng.normal() * 0.05, -0.99, 0.99)
+            out.append([p[0] * w, p[1] * w, zz * w, w])
+    return np.array(out, dtype=np.float32)
+
+
+def kat_scenes():
+    """(name, scene) pairs used for the golden fixtures and the GPU parity tests."""
+    out = []
+    base = basic_cases()
+    out.append(("kat_basic_lit_64x48", _scene("kat_basic_lit", 64, 48, base)))
+    out.append(("kat_basic_depth_64x48", _scene("kat_basic_depth", 64, 48, base, lit=False)))
+    out.append(("kat_basic_nocull_61x37", _scene("kat_basic_nocull", 61, 37, base, behavior_off=S.FACE_CULLING)))
+    out.append(("kat_basic_notest_64x48", _scene("kat_basic_notest", 64, 48, base, behavior_off=S.TEST_DEPTH)))
+    out.append(("kat_soup_lit_96x64", _scene("kat_soup_lit", 96, 64, random_soup(300, 11))))
+    out.append(("kat_soup_depth_97x63", _scene("kat_soup_depth", 97, 63, random_soup(400, 12), lit=False)))
+    out.append(("kat_soup_ortho_nocull_80x80",
+                _scene("kat_soup_ortho", 80, 80, random_soup(300, 13, persp=False), behavior_off=S.FACE_CULLING)))
+    return out

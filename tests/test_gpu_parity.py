@@ -1,0 +1,80 @@
+"""GPU path against the oracle and the golden fixtures: depth (hence
+coverage) bit-exact, colour within 1 LSB per 8-bit channel."""
+import numpy as np
+import pytest
+
+from common import assert_depth_exact, colour_diff, load_golden, render, sha
+from cpu_backends import OraclePipeline
+from golden.make_golden import golden_cases, scene_digest
+
+CASES = golden_cases()
+COLOUR_TOL = 1  # LSB per channel
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,scene", CASES, ids=[c[0] for c in CASES])
+def test_gpu_matches_oracle(name, scene, gpu_lib):
+    from puresoft3d_gb300.pipeline import PuresoftPipeline
+    gpu = render(PuresoftPipeline(scene.width, scene.height), scene)
+    ora = render(OraclePipeline(scene.width, scene.height), scene)
+    assert_depth_exact(gpu["depth"], ora["depth"], name)
+    if "shadow" in ora:
+        assert_depth_exact(gpu["shadow"], ora["shadow"], name + " shadow map")
+    mx, mean = colour_diff(gpu["colour"], ora["colour"])
+    assert mx <= COLOUR_TOL, "%s: colour differs by up to %d LSB (mean %.4f)" % (name, mx, mean)
+    g = load_golden(name)
+    if scene_digest(scene) == str(g["digest"]):
+        assert sha(gpu["depth"]) == str(g["depth_sha"]), name
+
+
+@pytest.mark.gpu
+def test_fragment_counts_match_oracle(gpu_lib):
+    from puresoft3d_gb300.pipeline import PuresoftPipeline
+    name, scene = [c for c in CASES if c[0].startswith("kat_soup_lit")][0]
+    g = PuresoftPipeline(scene.width, scene.height)
+    g.setFragmentCounting(True)
+    render(g, scene)
+    o = OraclePipeline(scene.width, scene.height)
+    render(o, scene)
+    st = g.stats()
+    assert (st["fragments"], st["fragments_passed"]) == o.fragments()
+
+
+@pytest.mark.gpu
+def test_bin_capacity_replay(gpu_lib, monkeypatch):
+    """A pass whose bin lists overflow the preallocated room is re-run
+    transparently with larger buffers; the result is unchanged."""
+    from puresoft3d_gb300.pipeline import PuresoftPipeline
+    name, scene = [c for c in CASES if c[0].startswith("c3_small")][0]
+    monkeypatch.setenv("PS3D_PAIR_CAP", "64")
+    g = PuresoftPipeline(scene.width, scene.height)
+    out = render(g, scene)
+    assert g.stats()["replays"] >= 1
+    ref = render(OraclePipeline(scene.width, scene.height), scene)
+    assert_depth_exact(out["depth"], ref["depth"], name)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("bin_w", [16, 32, 64])
+def test_bin_widths_agree(gpu_lib, monkeypatch, bin_w):
+    from puresoft3d_gb300.pipeline import PuresoftPipeline
+    name, scene = [c for c in CASES if c[0].startswith("kat_soup_depth")][0]
+    monkeypatch.setenv("PS3D_BIN_W", str(bin_w))
+    out = render(PuresoftPipeline(scene.width, scene.height), scene)
+    ref = render(OraclePipeline(scene.width, scene.height), scene)
+    assert_depth_exact(out["depth"], ref["depth"], name)
+
+
+@pytest.mark.gpu
+def test_repeated_frames_identical(gpu_lib):
+    from puresoft3d_gb300 import scenes as S
+    from puresoft3d_gb300.pipeline import PuresoftPipeline
+    scene = S.scene_c1()
+    g = PuresoftPipeline(scene.width, scene.height)
+    S.replay_setup(scene, g)
+    outs = []
+    for _ in range(3):
+        S.replay_frame(scene, g)
+        g.flush()
+        outs.append(g.readColour().copy())
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[1], outs[2])
