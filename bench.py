@@ -1,0 +1,353 @@
+"""Benchmark: frames/s of the per-fragment path on a seeded synthetic scene.
+
+Default workload: config 2 -- 1920x1080 Blinn-Phong pass with trilinear
+albedo, tangent-space normal map and 3x3 PCF, preceded by a 2048^2 FP32
+shadow pass, 64 seeded meshes (~200k triangles).  One step renders one frame
+(both passes).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--config c1|c2|c3]
+                  [--impl ours|reference]
+
+Arms
+  ours       value: frames/s with everything resident in HBM, frame = one
+             replay of the recorded command buffer (a CUDA graph running every
+             kernel of both passes: vertex set-up, binning, raster, shade);
+             CUDA events on the pipeline's stream around each frame, the L2
+             scrubbed (256 MB written) before each timed frame.
+             e2e: the same through the public API with host buffers: each step
+             copies the frame's draw descriptors and uniforms from pinned host
+             memory and reads the BGRA8 frame back to host memory.
+  reference  the reference pipeline's CPU path (the oracle port of it, on all
+             host cores), a bounded sample of frames of the same workload.
+
+With --gpus N (launched by torch.distributed.run) each rank renders its own
+replica of the scene on its own GPU ("replicas only": a frame is ordered per
+pixel and does not shard); value = all ranks' frames / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+RANK = int(os.environ.get("RANK", "0"))
+WORLD = int(os.environ.get("WORLD_SIZE", "1"))
+LOCAL_RANK = int(os.environ.get("LOCAL_RANK", "0"))
+if WORLD > 1:  # one GPU per rank: make it device 0 of this process before CUDA starts
+    os.environ["CUDA_VISIBLE_DEVICES"] = str(LOCAL_RANK)
+
+import numpy as np  # noqa: E402
+
+CONFIGS = {
+    "c1": dict(desc="c1: 640x480, one 32x16 UV sphere (992 triangles), 256^2 texture, LIT1 bilinear REPEAT",
+               args={}),
+    "c2": dict(desc="c2: 1920x1080 LIT2 pass (trilinear albedo, FP16 normal map, 3x3 PCF) after a 2048^2 FP32 "
+                    "shadow pass; 64 seeded meshes, ~200k triangles; 4x1024^2 albedo + 1024^2 normal mip chains",
+               args={}),
+    "c3": dict(desc="c3: 3840x2160 LIT3, 256 seeded meshes, ~2M triangles in 4 depth layers, 16x2048^2 trilinear",
+               args={}),
+}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            m = json.load(f)
+        return float(m["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                          "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                                          "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_scene(cfg):
+    from puresoft3d_gb300 import scenes as S
+    return {"c1": S.scene_c1, "c2": S.scene_c2, "c3": S.scene_c3}[cfg]()
+
+
+def algorithmic_bytes(scene, pairs_per_frame):
+    """Algorithmic bytes of one launch of each kernel family, and of a whole
+    frame: what the work must move at least once (writes of every target
+    pixel, reads of every input element the pass consumes)."""
+    info = scene.info
+    w, h = scene.width, scene.height
+    tris = scene.triangles()
+    out = {}
+    if scene.name == "c2":
+        ss = info["shadow_size"]
+        px_raster = ss * ss * 4 + w * h * 4 * 2          # shadow depth; main depth + winner
+        out["raster_per_frame"] = px_raster + pairs_per_frame * (64 + 4)
+        out["raster_launches_per_frame"] = 2
+    else:
+        out["raster_per_frame"] = w * h * 4 * 2 + pairs_per_frame * (64 + 4)
+        out["raster_launches_per_frame"] = 1
+    out["tris"] = tris
+    return out
+
+
+def run_ours(args):
+    from puresoft3d_gb300 import scenes as S
+    from puresoft3d_gb300.pipeline import PuresoftPipeline, KERNELS
+    scene = make_scene(args.config)
+    pipe = PuresoftPipeline(scene.width, scene.height)
+    S.replay_setup(scene, pipe)
+    pipe.finish()
+
+    # fragments and pairs per frame (counting run, untimed)
+    pipe.setFragmentCounting(True)
+    st0 = pipe.stats()
+    S.replay_frame(scene, pipe)
+    pipe.finish()
+    st1 = pipe.stats()
+    pipe.setFragmentCounting(False)
+    frags = st1["fragments"] - st0["fragments"]
+    pairs = st1["bin_pairs"] - st0["bin_pairs"]
+    launches_per_frame = st1["kernel_launches"] - st0["kernel_launches"]
+
+    # per-kernel event timing over the non-graph path (untimed for value)
+    pipe.profile(True)
+    pipe.profileRead()
+    prof_frames = max(3, min(args.steps, 10))
+    for _ in range(prof_frames):
+        pipe.scrubL2()
+        S.replay_frame(scene, pipe)
+        pipe.finish()
+    prof = pipe.profileRead()
+    pipe.profile(False)
+
+    # recorded frame, replayed as a CUDA graph
+    pipe.beginCommands()
+    S.replay_frame(scene, pipe)
+    cb = pipe.endCommands()
+    for _ in range(max(3, args.warmup)):
+        cb.submit()
+    pipe.finish()
+
+    barrier()
+    clocks = ClockSampler()
+    clocks.start()
+    frame_ms = []
+    for _ in range(args.steps):
+        pipe.scrubL2()
+        pipe.timerBegin()
+        cb.submit()
+        frame_ms.append(pipe.timerEnd())
+    pipe.finish()
+    clk = clocks.stop()
+    total_ms = sum(frame_ms)
+    total_ms = allreduce_max(total_ms)
+
+    # e2e through the public API with host buffers
+    try:
+        import torch
+        host = torch.empty((scene.height, scene.width, 4), dtype=torch.uint8, pin_memory=True).numpy()
+    except Exception:
+        host = np.empty((scene.height, scene.width, 4), dtype=np.uint8)
+    for _ in range(2):
+        cb.submit(upload_inputs=True)
+        pipe.readColour(host)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cb.submit(upload_inputs=True)
+        pipe.readColour(host)
+    e2e_s = allreduce_max(time.perf_counter() - t0)
+
+    fps = WORLD * args.steps / (total_ms / 1e3)
+    fps_e2e = WORLD * args.steps / e2e_s
+    ab = algorithmic_bytes(scene, pairs)
+    # dominant kernel by event time share
+    dom = max(prof, key=lambda k: prof[k][1])
+    n_launch, ms = prof[dom]
+    avg_ms = ms / max(n_launch, 1)
+    peak, peak_kind = peaks()
+    if dom == "raster":
+        bytes_per_launch = ab["raster_per_frame"] / ab["raster_launches_per_frame"]
+    else:
+        bytes_per_launch = None
+    achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9 if bytes_per_launch else None
+    line = {
+        "metric": "frames/s", "value": round(fps, 3), "unit": "frames/s", "n_gpus": WORLD,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded meshes and procedural textures)",
+        "config": {"workload": CONFIGS[args.config]["desc"], "width": scene.width, "height": scene.height,
+                   "triangles": scene.triangles(), "l2": "256 MB scrub before each timed frame",
+                   "parallelism": "replicas" if WORLD > 1 else "single GPU"},
+        "gfrag_per_s": round(frags * fps / WORLD / 1e9 * WORLD, 4),
+        "fragments_per_frame": frags,
+        "gpu_launches": launches_per_frame * args.steps,
+        "e2e": {"value": round(fps_e2e, 3), "unit": "frames/s", "h2d_bytes_per_step": cb.input_bytes(),
+                "d2h_bytes_per_step": scene.width * scene.height * 4},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2) if achieved else None,
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5) if achieved else None,
+                     "peak_source": peak_kind, "avg_launch_ms": round(avg_ms, 5),
+                     "bytes_per_launch": bytes_per_launch, "traffic": None},
+        "kernel_ms_per_frame": {k: round(prof[k][1] / prof_frames, 5) for k in KERNELS if prof[k][0]},
+        "clocks": clk,
+    }
+    if RANK == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(scene, budget_s=args.cpu_budget)
+    cb.destroy()
+    pipe.close()
+    return line
+
+
+def cpu_baseline(scene, budget_s=15.0, threads=None):
+    """The reference pipeline's CPU path timed on this host's cores: the
+    reference build where it compiled here, else the oracle port of it."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from puresoft3d_gb300 import scenes as S
+    from cpu_backends import OraclePipeline, RefPipeline
+    threads = threads or os.cpu_count() or 1
+    use_ref = os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libps3dref.so")) and os.uname().machine == "x86_64"
+    if use_ref:
+        os.environ["PS3D_REF_THREADS"] = str(threads)
+        pipe = RefPipeline(scene.width, scene.height, threads)
+        kind = "reference"
+    else:
+        pipe = OraclePipeline(scene.width, scene.height, threads)
+        kind = "port"
+    S.replay_setup(scene, pipe)
+    S.replay_frame(scene, pipe)  # warm-up
+    frames, t0 = 0, time.perf_counter()
+    while True:
+        S.replay_frame(scene, pipe)
+        frames += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or frames >= 200:
+            break
+    pipe.close()
+    return {"value": round(frames / el, 4), "unit": "frames/s", "cores": threads, "kind": kind,
+            "sample": "%d frames of the same workload in %.1f s" % (frames, el)}
+
+
+def run_reference(args):
+    scene = make_scene(args.config)
+    per = max(2.0, args.cpu_budget / max(args.steps, 1))
+    vals = []
+    cb = None
+    for _ in range(args.warmup):
+        cpu_baseline(scene, budget_s=0.1)
+    t0 = time.perf_counter()
+    frames = 0
+    for _ in range(args.steps):
+        cb = cpu_baseline(scene, budget_s=per)
+        vals.append(cb["value"])
+        frames += int(cb["sample"].split()[0])
+    el = time.perf_counter() - t0
+    v = statistics.median(vals)
+    return {"impl": "reference", "metric": "frames/s", "value": v, "unit": "frames/s", "n_gpus": WORLD,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 / v, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": CONFIGS[args.config]["desc"]},
+            "cpu_baseline": {"value": v, "unit": "frames/s", "cores": cb["cores"], "kind": cb["kind"],
+                             "sample": "%d steps, %d frames in %.1f s" % (args.steps, frames, el)},
+            "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+_pg = None
+
+
+def init_dist():
+    global _pg
+    if WORLD > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        _pg = dist
+
+
+def barrier():
+    if _pg:
+        _pg.barrier()
+
+
+def allreduce_max(x):
+    if not _pg:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    _pg.all_reduce(t, op=_pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.impl == "reference":
+        if RANK != 0:
+            return
+        print(json.dumps(run_reference(args)), flush=True)
+        return
+    init_dist()
+    line = run_ours(args)
+    if RANK == 0:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

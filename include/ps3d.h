@@ -81,6 +81,7 @@ extern "C" {
 #define PS3D_MAX_FBOS 16
 
 typedef struct ps3d_pipeline ps3d_pipeline;
+typedef struct ps3d_cmdbuf ps3d_cmdbuf;
 
 /* Counters since creation (ps3d_stats). */
 typedef struct {
@@ -91,6 +92,7 @@ typedef struct {
     uint64_t fragments;       /* fragments that reached the depth test (when counting is on) */
     uint64_t fragments_passed;/* fragments that passed it (when counting is on) */
     uint64_t replays;         /* passes re-run after a bin-list capacity miss */
+    uint64_t bin_pairs;       /* (bin, triangle) pairs written by the binning passes */
 } ps3d_stats_t;
 
 /* PuresoftPipeline::PuresoftPipeline(canvas, w, h, rndr) (pipeline.cpp:24-61).
@@ -192,6 +194,44 @@ int ps3d_get_stream(ps3d_pipeline* p, void** out);
  * adds one atomic per warp-span). */
 int ps3d_set_fragment_counting(ps3d_pipeline* p, int on);
 int ps3d_stats(ps3d_pipeline* p, ps3d_stats_t* out);
+
+/* ---- command buffers (no counterpart in the reference, whose drawVAO runs
+ * immediately).  Between ps3d_cmdbuf_begin and ps3d_cmdbuf_end, clears and
+ * draws are recorded into a command buffer instead of the pipeline's queue.
+ * ps3d_cmdbuf_submit runs it: the first submission runs it like ps3d_finish
+ * and then captures its kernels into a CUDA graph; later submissions launch
+ * that graph (asynchronously) after, if uploadInputs, copying the recorded
+ * draw descriptors and uniforms from pinned host memory again.  A command
+ * buffer refers to the textures and VBOs it was recorded with: after one of
+ * them is destroyed or replaced, submitting it returns PS3D_ERR_INVALID. */
+int ps3d_cmdbuf_begin(ps3d_pipeline* p);
+int ps3d_cmdbuf_end(ps3d_pipeline* p, ps3d_cmdbuf** out);
+int ps3d_cmdbuf_submit(ps3d_pipeline* p, ps3d_cmdbuf* cb, int uploadInputs);
+int ps3d_cmdbuf_destroy(ps3d_pipeline* p, ps3d_cmdbuf* cb);
+/* Bytes a submission with uploadInputs copies host -> device. */
+int ps3d_cmdbuf_input_bytes(ps3d_pipeline* p, ps3d_cmdbuf* cb, size_t* out);
+
+/* ---- timing on the pipeline's stream (CUDA events) */
+int ps3d_timer_begin(ps3d_pipeline* p);
+int ps3d_timer_end(ps3d_pipeline* p, float* ms);
+/* Kernel families for ps3d_profile_read. */
+#define PS3D_K_SETUP 0
+#define PS3D_K_SCAN 1
+#define PS3D_K_EMIT 2
+#define PS3D_K_HIST 3
+#define PS3D_K_SCATTER 4
+#define PS3D_K_RASTER 5
+#define PS3D_K_SHADE 6
+#define PS3D_K_FILL 7
+#define PS3D_K_COUNT 8
+/* Overwrites `bytes` of an internal device buffer on the pipeline's stream
+ * (benchmarking aid: evicts the 126 MB L2 between timed frames). */
+int ps3d_l2_scrub(ps3d_pipeline* p, size_t bytes);
+/* When on, each kernel launch outside graphs is bracketed by CUDA events. */
+int ps3d_profile_enable(ps3d_pipeline* p, int on);
+/* Waits, then returns per family the launches and milliseconds since the
+ * last read (arrays of PS3D_K_COUNT). */
+int ps3d_profile_read(ps3d_pipeline* p, int* launches, double* ms);
 
 #ifdef __cplusplus
 }

@@ -29,12 +29,12 @@
 #include "ps3d_internal.h"
 
 namespace ps3d {
-void launch_setup_and_bin(const PassParams& P, int* scanTmp, cudaStream_t s, int& launches);
+void launch_setup_and_bin(const PassParams& P, int* scanTmp, cudaStream_t s, int& launches, Prof* pr);
 int scan_block_sums_needed(int nMax);
 int max_bins();
-void launch_raster_shade(const PassParams& P, cudaStream_t s, int& launches);
+void launch_raster_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr);
 void launch_fill_u32(void* base, int width, int height, int pitchElems, uint32_t v, const int* status,
-                     cudaStream_t s, int& launches);
+                     cudaStream_t s, int& launches, Prof* pr);
 }  // namespace ps3d
 
 using namespace ps3d;
@@ -98,11 +98,19 @@ struct Pass {
     uint32_t colourValue = 0;
 };
 
+// Device buffers that grow.  While a captured graph exists its kernels hold
+// the old addresses, so a buffer being replaced is retired (freed when the
+// last graph goes) instead of freed.
+thread_local std::vector<void*>* g_retire = nullptr;
+
 template <class T> bool dev_alloc(T*& p, size_t& cap, size_t need)
 {
     if (need <= cap && p) return true;
     size_t n = std::max(need, cap + cap / 2);
-    if (p) cudaFree(p);
+    if (p) {
+        if (g_retire) g_retire->push_back(p);
+        else cudaFree(p);
+    }
     p = nullptr;
     cap = 0;
     if (cudaMalloc((void**)&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return false;
@@ -173,6 +181,35 @@ struct ps3d_pipeline {
     int pairCap = 1 << 18;
 
     ps3d_stats_t stats = {};
+    Prof prof;
+    cudaEvent_t timerA = nullptr, timerB = nullptr;
+    void* scrub = nullptr;
+    size_t scrubBytes = 0;
+    ps3d_cmdbuf* recording = nullptr;   // command buffer being recorded
+    int liveGraphs = 0;
+    std::vector<void*> retired;          // scratch replaced while graphs hold it
+    std::vector<ps3d_cmdbuf*> cmdbufs;
+    ps3d_cmdbuf* graphUnverified = nullptr;  // graph launched since the last verification
+    const DrawDesc* cbDraws = nullptr;   // set while a command buffer's graph is captured
+    const DrawUniforms* cbUnis = nullptr;
+    const std::vector<size_t>* cbOffsets = nullptr;
+};
+
+// A recorded command sequence (ps3d_cmdbuf_*): its draw descriptors live in
+// its own device buffers, and after its first submission it replays as a
+// CUDA graph.
+struct ps3d_cmdbuf {
+    std::vector<Command> cmds;
+    std::vector<size_t> passOffset;      // per pass of its plan: first descriptor index
+    std::vector<DrawDesc> hDraws;        // host copies (pinned) of all passes' descriptors
+    std::vector<DrawUniforms> hUnis;
+    DrawDesc* dDraws = nullptr;
+    DrawUniforms* dUnis = nullptr;
+    DrawDesc* pinDraws = nullptr;        // pinned staging for per-submission uploads
+    DrawUniforms* pinUnis = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool stale = false;
 };
 
 namespace {
@@ -360,7 +397,7 @@ int fill_depth(ps3d_pipeline* p, int target, float v)
     uint32_t bits;
     memcpy(&bits, &v, 4);
     int launches = 0;
-    launch_fill_u32(t.depth, t.scan, t.h, t.scan, bits, p->status, p->stream, launches);
+    launch_fill_u32(t.depth, t.scan, t.h, t.scan, bits, p->status, p->stream, launches, &p->prof);
     p->stats.kernel_launches += launches;
     return 0;
 }
@@ -368,9 +405,27 @@ int fill_depth(ps3d_pipeline* p, int target, float v)
 int fill_colour(ps3d_pipeline* p, uint32_t v)
 {
     int launches = 0;
-    launch_fill_u32(p->colour, p->devW, p->devH, p->devW, v, p->status, p->stream, launches);
+    launch_fill_u32(p->colour, p->devW, p->devH, p->devW, v, p->status, p->stream, launches, &p->prof);
     p->stats.kernel_launches += launches;
     return 0;
+}
+
+// The draws of a pass as device descriptors: triangle bases are running
+// sums, so a pass's triangles are numbered in submission order.
+void pass_descriptors(const std::vector<Command>& cmds, const Pass& ps, std::vector<DrawDesc>& dd,
+                      std::vector<DrawUniforms>& uu, int& nTris, int& nvMax, bool& anyColour)
+{
+    for (size_t i = ps.first; i < ps.last; i++) {
+        DrawDesc d = cmds[i].desc;
+        if (d.triCount == 0) continue;
+        d.triBase = nTris;
+        d.uni = (int)uu.size();
+        nTris += d.triCount;
+        nvMax = std::max(nvMax, d.nv);
+        anyColour |= (d.flags & F_COLOUR) != 0;
+        dd.push_back(d);
+        uu.push_back(cmds[i].uni);
+    }
 }
 
 int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps, size_t replayFrom)
@@ -386,31 +441,33 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     std::vector<DrawUniforms> uu;
     int nTris = 0, nvMax = 0;
     bool anyColour = false;
-    for (size_t i = ps.first; i < ps.last; i++) {
-        DrawDesc d = cmds[i].desc;
-        if (d.triCount == 0) continue;
-        d.triBase = nTris;
-        d.uni = (int)uu.size();
-        nTris += d.triCount;
-        nvMax = std::max(nvMax, d.nv);
-        anyColour |= (d.flags & F_COLOUR) != 0;
-        dd.push_back(d);
-        uu.push_back(cmds[i].uni);
-    }
+    pass_descriptors(cmds, ps, dd, uu, nTris, nvMax, anyColour);
     if (nTris == 0) {
-        if (ps.clearDepth) fill_depth(p, c0.depthTarget, ps.depthValue);
-        if (ps.clearColour) fill_colour(p, ps.colourValue);
+        if (ps.clearDepth && (rc = fill_depth(p, c0.depthTarget, ps.depthValue))) return rc;
+        if (ps.clearColour && (rc = fill_colour(p, ps.colourValue))) return rc;
         return 0;
     }
+    g_retire = p->liveGraphs ? &p->retired : nullptr;
     int binW = p->binW;
     while ((long long)((W + binW - 1) / binW) * ((H + kBinH - 1) / kBinH) > max_bins() && binW < kMaxBinW) binW *= 2;
     int binsX = (W + binW - 1) / binW, binsY = (H + kBinH - 1) / kBinH;
     if ((long long)binsX * binsY > max_bins()) return fail(PS3D_ERR_INVALID, "viewport %dx%d has too many bins", W, H);
     if ((rc = ensure_scratch(p, nTris, nvMax, W, H, binsX, binsY, anyColour))) return rc;
-    if (!dev_alloc(p->draws, p->drawsCap, dd.size()) || !dev_alloc(p->unis, p->unisCap, uu.size()))
-        return fail(PS3D_ERR_NOMEM, "device allocation for draw descriptors failed");
-    CU(cudaMemcpyAsync(p->draws, dd.data(), dd.size() * sizeof(DrawDesc), cudaMemcpyHostToDevice, p->stream));
-    CU(cudaMemcpyAsync(p->unis, uu.data(), uu.size() * sizeof(DrawUniforms), cudaMemcpyHostToDevice, p->stream));
+    const DrawDesc* devDraws;
+    const DrawUniforms* devUnis;
+    if (p->cbOffsets) {  // capturing a command buffer: its descriptors are already on the device
+        size_t off = (*p->cbOffsets)[seq];
+        devDraws = p->cbDraws + off;
+        devUnis = p->cbUnis + off;
+    } else {
+        if (!dev_alloc(p->draws, p->drawsCap, dd.size()) || !dev_alloc(p->unis, p->unisCap, uu.size()))
+            return fail(PS3D_ERR_NOMEM, "device allocation for draw descriptors failed");
+        CU(cudaMemcpyAsync(p->draws, dd.data(), dd.size() * sizeof(DrawDesc), cudaMemcpyHostToDevice, p->stream));
+        CU(cudaMemcpyAsync(p->unis, uu.data(), uu.size() * sizeof(DrawUniforms), cudaMemcpyHostToDevice,
+                           p->stream));
+        devDraws = p->draws;
+        devUnis = p->unis;
+    }
 
     // A clear fuses into the pass when the pass covers the whole buffer.
     bool fuseDepth = ps.clearDepth && tg.w == W && tg.h == H && tg.scan == W;
@@ -427,8 +484,8 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     P.binsY = binsY;
     P.nTris = nTris;
     P.nDraws = (int)dd.size();
-    P.draws = p->draws;
-    P.unis = p->unis;
+    P.draws = devDraws;
+    P.unis = devUnis;
     P.tris = p->tris;
     P.vary = p->vary;
     P.nvMax = std::max(nvMax, 1);
@@ -458,8 +515,8 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     P.colourClearValue = ps.colourValue;
     P.passSeq = seq;
     int launches = 0;
-    launch_setup_and_bin(P, p->scanTmp, p->stream, launches);
-    launch_raster_shade(P, p->stream, launches);
+    launch_setup_and_bin(P, p->scanTmp, p->stream, launches, &p->prof);
+    launch_raster_shade(P, p->stream, launches, &p->prof);
     CU(cudaGetLastError());
     p->stats.kernel_launches += launches;
     p->stats.batches++;
@@ -467,22 +524,22 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     return 0;
 }
 
-// Splits launched[from..] into passes and launches them.
-int launch_range(ps3d_pipeline* p, size_t from)
+// Splits cmds[from..] into passes (each run of draws into one target, with
+// the clears in front of it) and hands them to `onPass`; clears that cannot
+// fuse go to `onFill` (target -3 = colour).
+template <class PassFn, class FillFn>
+int plan_commands(const std::vector<Command>& cmds, size_t from, PassFn onPass, FillFn onFill)
 {
-    const std::vector<Command>& cmds = p->launched;
     size_t i = from, n = cmds.size();
     int rc;
     while (i < n) {
-        const Command& c = cmds[i];
         Pass ps;
         size_t j = i;
         int depthClearTarget = -2;
-        // the clears in front of the next run of draws
         for (; j < n && cmds[j].kind != Command::DRAW; j++) {
             if (cmds[j].kind == Command::CLEAR_DEPTH) {
                 if (ps.clearDepth && depthClearTarget != cmds[j].depthTarget &&
-                    (rc = fill_depth(p, depthClearTarget, ps.depthValue)))
+                    (rc = onFill(depthClearTarget, ps.depthValue, 0u)))
                     return rc;
                 ps.clearDepth = true;
                 ps.depthValue = cmds[j].depthValue;
@@ -493,8 +550,8 @@ int launch_range(ps3d_pipeline* p, size_t from)
             }
         }
         if (j == n) {
-            if (ps.clearDepth && (rc = fill_depth(p, depthClearTarget, ps.depthValue))) return rc;
-            if (ps.clearColour && (rc = fill_colour(p, ps.colourValue))) return rc;
+            if (ps.clearDepth && (rc = onFill(depthClearTarget, ps.depthValue, 0u))) return rc;
+            if (ps.clearColour && (rc = onFill(-3, 0.0f, ps.colourValue))) return rc;
             break;
         }
         size_t k = j;
@@ -502,17 +559,25 @@ int launch_range(ps3d_pipeline* p, size_t from)
                cmds[k].vpW == cmds[j].vpW && cmds[k].vpH == cmds[j].vpH)
             k++;
         if (ps.clearDepth && depthClearTarget != cmds[j].depthTarget) {
-            if ((rc = fill_depth(p, depthClearTarget, ps.depthValue))) return rc;
+            if ((rc = onFill(depthClearTarget, ps.depthValue, 0u))) return rc;
             ps.clearDepth = false;
         }
         ps.first = j;
         ps.last = k;
-        if ((rc = run_pass(p, cmds, ps, i))) return rc;
-        (void)c;
+        if ((rc = onPass(ps, i))) return rc;
         i = k;
     }
     return 0;
 }
+
+int launch_cmds(ps3d_pipeline* p, const std::vector<Command>& cmds, size_t from)
+{
+    return plan_commands(
+        cmds, from, [&](const Pass& ps, size_t start) { return run_pass(p, cmds, ps, start); },
+        [&](int target, float v, uint32_t c) { return target == -3 ? fill_colour(p, c) : fill_depth(p, target, v); });
+}
+
+int launch_range(ps3d_pipeline* p, size_t from) { return launch_cmds(p, p->launched, from); }
 
 int do_flush(ps3d_pipeline* p)
 {
@@ -539,7 +604,16 @@ int do_finish(ps3d_pipeline* p)
         if (!st[0]) {
             p->launched.clear();
             p->passStart.clear();
+            p->graphUnverified = nullptr;
             return 0;
+        }
+        if (p->launched.empty() && p->graphUnverified) {
+            // a graph launch outgrew the room its first submission verified
+            CU(cudaMemsetAsync(p->status, 0, 4 * sizeof(int), p->stream));
+            ps3d_cmdbuf* cb = p->graphUnverified;
+            p->graphUnverified = nullptr;
+            cb->stale = true;
+            return fail(PS3D_ERR_NOMEM, "a command buffer outgrew its bin lists; record it again");
         }
         int seq = st[3];
         if (seq < 0 || seq >= (int)p->passStart.size()) return fail(PS3D_ERR_DEVICE, "bad overflow record");
@@ -603,6 +677,16 @@ int ps3d_pipeline_destroy(ps3d_pipeline* p)
 {
     if (!p) return 0;
     if (p->stream) cudaStreamSynchronize(p->stream);
+    while (!p->cmdbufs.empty()) ps3d_cmdbuf_destroy(p, p->cmdbufs.back());
+    for (void* r : p->retired) cudaFree(r);
+    for (auto& m : p->prof.marks) {
+        cudaEventDestroy(m.a);
+        cudaEventDestroy(m.b);
+    }
+    for (auto e : p->prof.pool) cudaEventDestroy(e);
+    if (p->scrub) cudaFree(p->scrub);
+    if (p->timerA) cudaEventDestroy(p->timerA);
+    if (p->timerB) cudaEventDestroy(p->timerB);
     for (auto& t : p->tex)
         if (t.alive) cudaFree(t.dev);
     for (auto& v : p->vaos)
@@ -668,6 +752,7 @@ int ps3d_texture_destroy(ps3d_pipeline* p, int idx)
     int rc = do_finish(p);
     if (rc) return rc;
     if (p->depthTarget == idx) p->depthTarget = -1;
+    for (auto* cb : p->cmdbufs) cb->stale = true;
     cudaFree(p->tex[idx].dev);
     p->tex[idx] = Texture();
     return 0;
@@ -785,6 +870,7 @@ int ps3d_vao_destroy(ps3d_pipeline* p, int vao)
     if (!p->vaos[vao].alive) return 0;
     int rc = do_finish(p);
     if (rc) return rc;
+    for (auto* cb : p->cmdbufs) cb->stale = true;
     for (auto*& b : p->vaos[vao].vbo)
         if (b) {
             cudaFree(b->dev);
@@ -805,6 +891,7 @@ static int vbo_attach(ps3d_pipeline* p, int vao, int slot, int unitBytes, int co
     if (p->vaos[vao].vbo[slot]) {
         int rc = do_finish(p);
         if (rc) return rc;
+        for (auto* cb : p->cmdbufs) cb->stale = true;
         cudaFree(p->vaos[vao].vbo[slot]->dev);
         delete p->vaos[vao].vbo[slot];
         p->vaos[vao].vbo[slot] = nullptr;
@@ -842,6 +929,7 @@ int ps3d_vbo_detach(ps3d_pipeline* p, int vao, int slot)
     if (!p->vaos[vao].vbo[slot]) return 0;
     int rc = do_finish(p);
     if (rc) return rc;
+    for (auto* cb : p->cmdbufs) cb->stale = true;
     cudaFree(p->vaos[vao].vbo[slot]->dev);
     delete p->vaos[vao].vbo[slot];
     p->vaos[vao].vbo[slot] = nullptr;
@@ -903,7 +991,7 @@ int ps3d_clear_depth(ps3d_pipeline* p, float v)
     c.kind = Command::CLEAR_DEPTH;
     c.depthTarget = p->depthTarget;
     c.depthValue = v;
-    p->pending.push_back(c);
+    (p->recording ? p->recording->cmds : p->pending).push_back(c);
     return 0;
 }
 
@@ -915,7 +1003,7 @@ int ps3d_clear_colour(ps3d_pipeline* p, uint32_t bgra)
     c.kind = Command::CLEAR_COLOUR;
     c.depthTarget = p->depthTarget;
     c.colourValue = bgra;
-    p->pending.push_back(c);
+    (p->recording ? p->recording->cmds : p->pending).push_back(c);
     return 0;
 }
 
@@ -964,7 +1052,7 @@ int ps3d_draw(ps3d_pipeline* p, int vao)
     if (tg.w < p->W || tg.h < p->H) return fail(PS3D_ERR_INVALID, "the depth target is smaller than the viewport");
     if ((d.flags & F_COLOUR) && (p->devW < p->W || p->devH < p->H))
         return fail(PS3D_ERR_INVALID, "the colour buffer is smaller than the viewport");
-    p->pending.push_back(c);
+    (p->recording ? p->recording->cmds : p->pending).push_back(c);
     p->stats.draws++;
     return 0;
 }
@@ -1027,11 +1115,213 @@ int ps3d_stats(ps3d_pipeline* p, ps3d_stats_t* out)
     if (!p || !out) return fail(PS3D_ERR_INVALID, "null argument");
     int rc = do_finish(p);
     if (rc) return rc;
-    unsigned long long c[2];
+    unsigned long long c[3];
     CU(cudaMemcpy(c, p->status + 4, sizeof c, cudaMemcpyDeviceToHost));
     *out = p->stats;
     out->fragments = c[0];
     out->fragments_passed = c[1];
+    out->bin_pairs = c[2];
+    return 0;
+}
+
+int ps3d_cmdbuf_begin(ps3d_pipeline* p)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    if (p->recording) return fail(PS3D_ERR_INVALID, "a command buffer is already being recorded");
+    p->recording = new (std::nothrow) ps3d_cmdbuf();
+    if (!p->recording) return fail(PS3D_ERR_NOMEM, "host allocation failed");
+    return 0;
+}
+
+int ps3d_cmdbuf_end(ps3d_pipeline* p, ps3d_cmdbuf** out)
+{
+    if (!p || !out) return fail(PS3D_ERR_INVALID, "null argument");
+    if (!p->recording) return fail(PS3D_ERR_INVALID, "no command buffer is being recorded");
+    ps3d_cmdbuf* cb = p->recording;
+    p->recording = nullptr;
+    // Lay every pass's descriptors out once, in plan order.
+    plan_commands(
+        cb->cmds, 0,
+        [&](const Pass& ps, size_t) {
+            std::vector<DrawDesc> dd;
+            std::vector<DrawUniforms> uu;
+            int nTris = 0, nvMax = 0;
+            bool anyColour = false;
+            pass_descriptors(cb->cmds, ps, dd, uu, nTris, nvMax, anyColour);
+            cb->passOffset.push_back(cb->hDraws.size());
+            cb->hDraws.insert(cb->hDraws.end(), dd.begin(), dd.end());
+            cb->hUnis.insert(cb->hUnis.end(), uu.begin(), uu.end());
+            return 0;
+        },
+        [&](int, float, uint32_t) { return 0; });
+    size_t n = std::max<size_t>(cb->hDraws.size(), 1);
+    bool ok = cudaMalloc((void**)&cb->dDraws, n * sizeof(DrawDesc)) == cudaSuccess &&
+              cudaMalloc((void**)&cb->dUnis, n * sizeof(DrawUniforms)) == cudaSuccess &&
+              cudaMallocHost((void**)&cb->pinDraws, n * sizeof(DrawDesc)) == cudaSuccess &&
+              cudaMallocHost((void**)&cb->pinUnis, n * sizeof(DrawUniforms)) == cudaSuccess;
+    if (!ok) {
+        p->cmdbufs.push_back(cb);
+        ps3d_cmdbuf_destroy(p, cb);
+        return fail(PS3D_ERR_NOMEM, "command buffer allocation failed");
+    }
+    if (!cb->hDraws.empty()) {
+        memcpy(cb->pinDraws, cb->hDraws.data(), cb->hDraws.size() * sizeof(DrawDesc));
+        memcpy(cb->pinUnis, cb->hUnis.data(), cb->hUnis.size() * sizeof(DrawUniforms));
+        CU(cudaMemcpyAsync(cb->dDraws, cb->pinDraws, cb->hDraws.size() * sizeof(DrawDesc), cudaMemcpyHostToDevice,
+                           p->stream));
+        CU(cudaMemcpyAsync(cb->dUnis, cb->pinUnis, cb->hUnis.size() * sizeof(DrawUniforms), cudaMemcpyHostToDevice,
+                           p->stream));
+        CU(cudaStreamSynchronize(p->stream));
+    }
+    p->cmdbufs.push_back(cb);
+    *out = cb;
+    return 0;
+}
+
+int ps3d_cmdbuf_input_bytes(ps3d_pipeline* p, ps3d_cmdbuf* cb, size_t* out)
+{
+    if (!p || !cb || !out) return fail(PS3D_ERR_INVALID, "null argument");
+    *out = cb->hDraws.size() * (sizeof(DrawDesc) + sizeof(DrawUniforms));
+    return 0;
+}
+
+int ps3d_cmdbuf_submit(ps3d_pipeline* p, ps3d_cmdbuf* cb, int uploadInputs)
+{
+    if (!p || !cb) return fail(PS3D_ERR_INVALID, "null argument");
+    if (cb->stale) return fail(PS3D_ERR_INVALID, "a texture or VBO of this command buffer changed; record it again");
+    int rc;
+    if (!cb->exec) {
+        // First submission: run and verify like ps3d_finish, then capture.
+        p->pending.insert(p->pending.end(), cb->cmds.begin(), cb->cmds.end());
+        if ((rc = do_finish(p))) return rc;
+        ps3d_stats_t saved = p->stats;
+        bool profOn = p->prof.on;
+        p->prof.on = false;
+        p->liveGraphs++;
+        p->cbDraws = cb->dDraws;
+        p->cbUnis = cb->dUnis;
+        p->cbOffsets = &cb->passOffset;
+        CU(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeRelaxed));
+        rc = launch_cmds(p, cb->cmds, 0);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(p->stream, &g);
+        p->cbDraws = nullptr;
+        p->cbUnis = nullptr;
+        p->cbOffsets = nullptr;
+        p->passStart.clear();
+        p->prof.on = profOn;
+        p->stats = saved;
+        if (rc || e != cudaSuccess || !g) {
+            p->liveGraphs--;
+            if (g) cudaGraphDestroy(g);
+            return rc ? rc : fail(PS3D_ERR_DEVICE, "graph capture failed: %s", cudaGetErrorString(e));
+        }
+        cb->graph = g;
+        if (cudaGraphInstantiate(&cb->exec, g, 0) != cudaSuccess) {
+            p->liveGraphs--;
+            cudaGraphDestroy(g);
+            cb->graph = nullptr;
+            cb->exec = nullptr;
+            return fail(PS3D_ERR_DEVICE, "graph instantiation failed");
+        }
+        return 0;
+    }
+    if (!p->pending.empty() || !p->launched.empty())
+        if ((rc = do_finish(p))) return rc;
+    if (uploadInputs && !cb->hDraws.empty()) {
+        CU(cudaMemcpyAsync(cb->dDraws, cb->pinDraws, cb->hDraws.size() * sizeof(DrawDesc), cudaMemcpyHostToDevice,
+                           p->stream));
+        CU(cudaMemcpyAsync(cb->dUnis, cb->pinUnis, cb->hUnis.size() * sizeof(DrawUniforms), cudaMemcpyHostToDevice,
+                           p->stream));
+    }
+    CU(cudaGraphLaunch(cb->exec, p->stream));
+    p->graphUnverified = cb;
+    p->stats.batches += cb->passOffset.size();
+    return 0;
+}
+
+int ps3d_cmdbuf_destroy(ps3d_pipeline* p, ps3d_cmdbuf* cb)
+{
+    if (!p || !cb) return fail(PS3D_ERR_INVALID, "null argument");
+    if (p->stream) cudaStreamSynchronize(p->stream);
+    if (p->graphUnverified == cb) p->graphUnverified = nullptr;
+    if (cb->exec) {
+        cudaGraphExecDestroy(cb->exec);
+        cudaGraphDestroy(cb->graph);
+        if (--p->liveGraphs == 0) {
+            for (void* r : p->retired) cudaFree(r);
+            p->retired.clear();
+        }
+    }
+    if (cb->dDraws) cudaFree(cb->dDraws);
+    if (cb->dUnis) cudaFree(cb->dUnis);
+    if (cb->pinDraws) cudaFreeHost(cb->pinDraws);
+    if (cb->pinUnis) cudaFreeHost(cb->pinUnis);
+    p->cmdbufs.erase(std::remove(p->cmdbufs.begin(), p->cmdbufs.end(), cb), p->cmdbufs.end());
+    delete cb;
+    return 0;
+}
+
+int ps3d_timer_begin(ps3d_pipeline* p)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    if (!p->timerA) {
+        CU(cudaEventCreate(&p->timerA));
+        CU(cudaEventCreate(&p->timerB));
+    }
+    CU(cudaEventRecord(p->timerA, p->stream));
+    return 0;
+}
+
+int ps3d_timer_end(ps3d_pipeline* p, float* ms)
+{
+    if (!p || !ms || !p->timerA) return fail(PS3D_ERR_INVALID, "timer not started");
+    CU(cudaEventRecord(p->timerB, p->stream));
+    CU(cudaEventSynchronize(p->timerB));
+    CU(cudaEventElapsedTime(ms, p->timerA, p->timerB));
+    return 0;
+}
+
+int ps3d_l2_scrub(ps3d_pipeline* p, size_t bytes)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    if (p->scrubBytes < bytes) {
+        if (p->scrub) cudaFree(p->scrub);
+        p->scrub = nullptr;
+        p->scrubBytes = 0;
+        CU(cudaMalloc(&p->scrub, bytes));
+        p->scrubBytes = bytes;
+    }
+    static unsigned char v = 0;
+    CU(cudaMemsetAsync(p->scrub, ++v, bytes, p->stream));
+    return 0;
+}
+
+int ps3d_profile_enable(ps3d_pipeline* p, int on)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    p->prof.on = on != 0;
+    return 0;
+}
+
+int ps3d_profile_read(ps3d_pipeline* p, int* launches, double* ms)
+{
+    if (!p || !launches || !ms) return fail(PS3D_ERR_INVALID, "null argument");
+    int rc = do_finish(p);
+    if (rc) return rc;
+    for (int k = 0; k < K_COUNT; k++) {
+        launches[k] = 0;
+        ms[k] = 0.0;
+    }
+    for (auto& m : p->prof.marks) {
+        float t = 0.0f;
+        CU(cudaEventElapsedTime(&t, m.a, m.b));
+        launches[m.id]++;
+        ms[m.id] += t;
+        p->prof.pool.push_back(m.a);
+        p->prof.pool.push_back(m.b);
+    }
+    p->prof.marks.clear();
     return 0;
 }
 

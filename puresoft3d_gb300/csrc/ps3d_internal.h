@@ -3,6 +3,7 @@
 #pragma once
 #include <stdint.h>
 #include <cuda_runtime.h>
+#include <vector>
 
 namespace ps3d {
 
@@ -89,7 +90,8 @@ struct PassParams {
     int* binHist;             // [bin][sortBlock] counts, then their exclusive scan
     int* binTri;              // triangles of each bin, in submission order
     int* status;              // [0] overflow flag, [1] pairs needed, [2] bin-histogram length,
-                              // [3] overflowing pass, [4..5] fragments tested, [6..7] passed (u64)
+                              // [3] overflowing pass, [4..5] fragments tested, [6..7] passed,
+                              // [8..9] pairs binned (u64)
     float* depth;             // depth target (rows bottom-up)
     int depthScan;            // in floats
     int depthW, depthH;
@@ -103,5 +105,41 @@ struct PassParams {
 };
 
 constexpr int kSortChunk = 4096;   // pairs per stable-sort block
+
+// Kernel families timed by the profiler (ps3d_profile_*).
+enum KernelId { K_SETUP, K_SCAN, K_EMIT, K_HIST, K_SCATTER, K_RASTER, K_SHADE, K_FILL, K_COUNT };
+
+// CUDA-event brackets around kernel launches, on the launching stream.
+struct Prof {
+    bool on = false;
+    struct Mark {
+        int id;
+        cudaEvent_t a, b;
+    };
+    std::vector<Mark> marks;
+    std::vector<cudaEvent_t> pool;
+    cudaEvent_t take()
+    {
+        if (!pool.empty()) {
+            cudaEvent_t e = pool.back();
+            pool.pop_back();
+            return e;
+        }
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        return e;
+    }
+    void begin(int id, cudaStream_t s)
+    {
+        if (!on) return;
+        Mark m{id, take(), take()};
+        cudaEventRecord(m.a, s);
+        marks.push_back(m);
+    }
+    void end(cudaStream_t s)
+    {
+        if (on && !marks.empty()) cudaEventRecord(marks.back().b, s);
+    }
+};
 
 }  // namespace ps3d

@@ -256,26 +256,32 @@ __global__ void k_fill_u32(uint32_t* base, int width, int height, int pitchElems
 
 static inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
-void launch_raster_shade(const PassParams& P, cudaStream_t s, int& launches)
+void launch_raster_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
 {
     int nBins = P.binsX * P.binsY;
+    pr->begin(K_RASTER, s);
     switch (P.binW) {
     case 16: k_raster<16><<<nBins, 32, 0, s>>>(P); break;
     case 32: k_raster<32><<<nBins, 32, 0, s>>>(P); break;
     default: k_raster<64><<<nBins, 32, 0, s>>>(P); break;
     }
+    pr->end(s);
     launches++;
     if (P.anyColour || P.clearColour) {
         dim3 g(ceil_div(P.W, 32), ceil_div(P.H, 8));
+        pr->begin(K_SHADE, s);
         k_shade<<<g, dim3(32, 8), 0, s>>>(P);
+        pr->end(s);
         launches++;
     }
 }
 
 void launch_fill_u32(void* base, int width, int height, int pitchElems, uint32_t v, const int* status,
-                     cudaStream_t s, int& launches)
+                     cudaStream_t s, int& launches, Prof* pr)
 {
+    pr->begin(K_FILL, s);
     k_fill_u32<<<dim3(ceil_div(width, 256), height), 256, 0, s>>>((uint32_t*)base, width, height, pitchElems, v, status);
+    pr->end(s);
     launches++;
 }
 

@@ -366,7 +366,10 @@ __global__ void k_emit(PassParams P)
         }
         return;
     }
-    if (t == 0) P.status[2] = P.binsX * P.binsY * ((total + kSortChunk - 1) / kSortChunk);
+    if (t == 0) {
+        P.status[2] = P.binsX * P.binsY * ((total + kSortChunk - 1) / kSortChunk);
+        atomicAdd((unsigned long long*)(P.status + 8), (unsigned long long)total);
+    }
     if (t >= P.nTris) return;
     int count = P.pairCount[t];
     if (!count) return;
@@ -443,12 +446,14 @@ __global__ void k_scatter(PassParams P)
 static inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
 void scan_exclusive(const int* in, int* out, int n, const int* nPtr, int nMax, int* blockSums, int writeTotal,
-                    const int* abortFlag, cudaStream_t s, int& launches)
+                    const int* abortFlag, cudaStream_t s, int& launches, Prof* pr)
 {
     int nb = ceil_div(nMax > 0 ? nMax : 1, kScanTile);
+    pr->begin(K_SCAN, s);
     k_scan_reduce<<<nb, kScanBlock, 0, s>>>(in, n, nPtr, blockSums, abortFlag);
     k_scan_top<<<1, kScanBlock, 0, s>>>(blockSums, nb, n, nPtr, abortFlag);
     k_scan_down<<<nb, kScanBlock, 0, s>>>(in, out, n, nPtr, blockSums, writeTotal, abortFlag);
+    pr->end(s);
     launches += 3;
 }
 
@@ -457,7 +462,7 @@ int scan_block_sums_needed(int nMax) { return ceil_div(nMax > 0 ? nMax : 1, kSca
 // Largest bin grid whose per-bin counters fit in one block's shared memory.
 int max_bins() { return (227 * 1024) / (int)sizeof(int); }
 
-void launch_setup_and_bin(const PassParams& P, int* scanTmp, cudaStream_t s, int& launches)
+void launch_setup_and_bin(const PassParams& P, int* scanTmp, cudaStream_t s, int& launches, Prof* pr)
 {
     static bool attrs = false;
     if (!attrs) {
@@ -466,17 +471,25 @@ void launch_setup_and_bin(const PassParams& P, int* scanTmp, cudaStream_t s, int
         attrs = true;
     }
     int nBins = P.binsX * P.binsY;
+    pr->begin(K_SETUP, s);
     k_setup<<<ceil_div(P.nTris, 128), 128, 0, s>>>(P);
+    pr->end(s);
     launches++;
-    scan_exclusive(P.pairCount, P.pairOffset, P.nTris, nullptr, P.nTris, scanTmp, 1, P.status, s, launches);
+    scan_exclusive(P.pairCount, P.pairOffset, P.nTris, nullptr, P.nTris, scanTmp, 1, P.status, s, launches, pr);
+    pr->begin(K_EMIT, s);
     k_emit<<<ceil_div(P.nTris, 256), 256, 0, s>>>(P);
+    pr->end(s);
     launches++;
     size_t smem = (size_t)nBins * sizeof(int);
+    pr->begin(K_HIST, s);
     k_hist<<<P.sortBlocks, 32, smem, s>>>(P);
+    pr->end(s);
     launches++;
     // binHist holds nBins * nb counts, nb known on the device only
-    scan_exclusive(P.binHist, P.binHist, 0, P.status + 2, nBins * P.sortBlocks, scanTmp, 0, P.status, s, launches);
+    scan_exclusive(P.binHist, P.binHist, 0, P.status + 2, nBins * P.sortBlocks, scanTmp, 0, P.status, s, launches, pr);
+    pr->begin(K_SCATTER, s);
     k_scatter<<<P.sortBlocks, 32, smem, s>>>(P);
+    pr->end(s);
     launches++;
 }
 

@@ -21,7 +21,7 @@ ERRORS = {-1: IndexError, -2: ValueError, -3: MemoryError, -4: RuntimeError, -5:
 
 class Stats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in ("draws", "batches", "kernel_launches", "triangles", "fragments",
-                                                "fragments_passed", "replays")]
+                                                "fragments_passed", "replays", "bin_pairs")]
 
 
 _lib = None
@@ -60,7 +60,19 @@ _SIGS = {
     "ps3d_get_stream": [_c_void_p, ctypes.POINTER(_c_void_p)],
     "ps3d_set_fragment_counting": [_c_void_p, _c_int],
     "ps3d_stats": [_c_void_p, ctypes.POINTER(Stats)],
+    "ps3d_cmdbuf_begin": [_c_void_p],
+    "ps3d_cmdbuf_end": [_c_void_p, ctypes.POINTER(_c_void_p)],
+    "ps3d_cmdbuf_submit": [_c_void_p, _c_void_p, _c_int],
+    "ps3d_cmdbuf_destroy": [_c_void_p, _c_void_p],
+    "ps3d_cmdbuf_input_bytes": [_c_void_p, _c_void_p, ctypes.POINTER(_c_size_t)],
+    "ps3d_timer_begin": [_c_void_p],
+    "ps3d_timer_end": [_c_void_p, ctypes.POINTER(ctypes.c_float)],
+    "ps3d_profile_enable": [_c_void_p, _c_int],
+    "ps3d_l2_scrub": [_c_void_p, _c_size_t],
+    "ps3d_profile_read": [_c_void_p, ctypes.POINTER(_c_int), ctypes.POINTER(ctypes.c_double)],
 }
+
+KERNELS = ["setup", "scan", "emit", "hist", "scatter", "raster", "shade", "fill"]
 
 
 def library(path: str | None = None) -> ctypes.CDLL:
@@ -230,3 +242,54 @@ class PuresoftPipeline:
         s = Stats()
         self._check(self.lib.ps3d_stats(self.h, ctypes.byref(s)))
         return {n: int(getattr(s, n)) for n, _ in Stats._fields_}
+
+    # -- command buffers (recorded once, replayed as CUDA graphs)
+    def beginCommands(self):
+        self._check(self.lib.ps3d_cmdbuf_begin(self.h))
+
+    def endCommands(self) -> "CommandBuffer":
+        cb = ctypes.c_void_p()
+        self._check(self.lib.ps3d_cmdbuf_end(self.h, ctypes.byref(cb)))
+        return CommandBuffer(self, cb)
+
+    # -- timing
+    def timerBegin(self):
+        self._check(self.lib.ps3d_timer_begin(self.h))
+
+    def timerEnd(self) -> float:
+        ms = ctypes.c_float()
+        self._check(self.lib.ps3d_timer_end(self.h, ctypes.byref(ms)))
+        return float(ms.value)
+
+    def scrubL2(self, nbytes: int = 256 << 20):
+        self._check(self.lib.ps3d_l2_scrub(self.h, nbytes))
+
+    def profile(self, on: bool):
+        self._check(self.lib.ps3d_profile_enable(self.h, int(on)))
+
+    def profileRead(self) -> dict:
+        n = (ctypes.c_int * len(KERNELS))()
+        ms = (ctypes.c_double * len(KERNELS))()
+        self._check(self.lib.ps3d_profile_read(self.h, n, ms))
+        return {k: (int(n[i]), float(ms[i])) for i, k in enumerate(KERNELS)}
+
+
+class CommandBuffer:
+    """A recorded frame; submit() replays it (as a CUDA graph after the first
+    submission)."""
+
+    def __init__(self, pipe: PuresoftPipeline, handle):
+        self.pipe, self.h = pipe, handle
+
+    def submit(self, upload_inputs: bool = False):
+        self.pipe._check(self.pipe.lib.ps3d_cmdbuf_submit(self.pipe.h, self.h, int(upload_inputs)))
+
+    def input_bytes(self) -> int:
+        n = ctypes.c_size_t()
+        self.pipe._check(self.pipe.lib.ps3d_cmdbuf_input_bytes(self.pipe.h, self.h, ctypes.byref(n)))
+        return int(n.value)
+
+    def destroy(self):
+        if self.h and self.pipe.h:
+            self.pipe._check(self.pipe.lib.ps3d_cmdbuf_destroy(self.pipe.h, self.h))
+        self.h = None
