@@ -173,6 +173,7 @@ struct ps3d_pipeline {
     int* pairTri = nullptr; size_t pairTriCap = 0;
     int* binTri = nullptr; size_t binTriCap = 0;
     int* binHist = nullptr; size_t binHistCap = 0;
+    int* binStart = nullptr; size_t binStartCap = 0;
     int* scanTmp = nullptr; size_t scanTmpCap = 0;
     int* winner = nullptr; size_t winnerCap = 0;
     DrawDesc* draws = nullptr; size_t drawsCap = 0;
@@ -359,6 +360,7 @@ int ensure_scratch(ps3d_pipeline* p, int nTris, int nvMax, int W, int H, int bin
               dev_alloc(p->pairKey, p->pairKeyCap, p->pairCap) && dev_alloc(p->pairTri, p->pairTriCap, p->pairCap) &&
               dev_alloc(p->binTri, p->binTriCap, p->pairCap) &&
               dev_alloc(p->binHist, p->binHistCap, nBins * sortBlocks + 1) &&
+              dev_alloc(p->binStart, p->binStartCap, nBins + 1) &&
               dev_alloc(p->scanTmp, p->scanTmpCap,
                         (size_t)scan_block_sums_needed((int)std::max<size_t>(nTris, nBins * sortBlocks)) + 1);
     if (ok && colour) ok = dev_alloc(p->winner, p->winnerCap, (size_t)W * H);
@@ -497,6 +499,7 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     P.pairCap = p->pairCap;
     P.sortBlocks = (p->pairCap + kSortChunk - 1) / kSortChunk;
     P.binHist = p->binHist;
+    P.binStart = p->binStart;
     P.binTri = p->binTri;
     P.status = p->status;
     P.depth = tg.depth;
@@ -696,7 +699,8 @@ int ps3d_pipeline_destroy(ps3d_pipeline* p)
                 delete b;
             }
     void* bufs[] = {p->colour, p->defDepth, p->status, p->tris, p->vary, p->pairCount, p->rect, p->pairOffset,
-                    p->pairKey, p->pairTri, p->binTri, p->binHist, p->scanTmp, p->winner, p->draws, p->unis};
+                    p->pairKey, p->pairTri, p->binTri, p->binHist, p->binStart, p->scanTmp, p->winner, p->draws,
+                    p->unis};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (p->ownStream && p->stream) cudaStreamDestroy(p->stream);

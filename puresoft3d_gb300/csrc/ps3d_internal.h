@@ -87,9 +87,10 @@ struct PassParams {
     int* pairTri;
     int pairCap;              // capacity of pairKey / pairTri / binTri
     int sortBlocks;           // pairCap / kSortChunk
-    int* binHist;             // [bin][sortBlock] counts, then their exclusive scan
+    int* binHist;             // [sortBlock][bin] counts, then per-bin prefixes over blocks
+    int* binStart;            // first position of each bin's list; [nBins] = total
     int* binTri;              // triangles of each bin, in submission order
-    int* status;              // [0] overflow flag, [1] pairs needed, [2] bin-histogram length,
+    int* status;              // [0] overflow flag, [1] pairs needed, [2] sort blocks in use,
                               // [3] overflowing pass, [4..5] fragments tested, [6..7] passed,
                               // [8..9] pairs binned (u64)
     float* depth;             // depth target (rows bottom-up)

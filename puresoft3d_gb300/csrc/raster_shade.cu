@@ -1,14 +1,18 @@
 // raster_shade.cu -- visibility and shading passes.
 //
-// k_raster  one warp per bin of 32 rows x binW columns.  Lane r owns row r of
-//           the bin, so every row is walked by exactly one thread, in
-//           triangle order -- the reference's guarantee that a row's spans
-//           are processed FIFO by one fragment thread (drawvao.cpp:77-109).
-//           The bin's depth and "winner" (last colour-writing fragment that
-//           passed) live in shared memory; each span is set up by the lane
-//           that owns its row (interp.cpp:26-80) and walked pixel by pixel
-//           with the reference's sequential accumulation (interp.cpp:82-92)
-//           and epsilon depth test (fragthrd.cpp:227).
+// k_raster  one 128-thread block per bin of 32 rows x binW columns.  The
+//           bin's depth and "winner" (last colour-writing fragment that
+//           passed) live in shared memory.  Triangles arrive in submission
+//           order, 128 at a time.  Set-up phase: one thread per (triangle,
+//           row) span computes the reference's row result and span set-up
+//           (rasterizer.cpp:93-118, interp.cpp:26-80), stepped sequentially
+//           to the bin's first column.  Walk phase: thread (warp w, lane r)
+//           owns row r, columns [w*binW/4, (w+1)*binW/4), and applies that
+//           row's spans in triangle order with the reference's sequential
+//           accumulation (interp.cpp:82-92) and epsilon depth test
+//           (fragthrd.cpp:227) -- every pixel has exactly one owner, so the
+//           per-pixel order is the reference's per-row FIFO order
+//           (drawvao.cpp:77-109).
 // k_shade   one thread per pixel: re-derives the winning fragment's
 //           varyings (same span set-up and sequential steps) and runs the
 //           draw's fragment stage once.  With no discard and no blending the
@@ -22,30 +26,48 @@ namespace ps3d {
 
 __device__ __forceinline__ void bin_range(const PassParams& P, int bin, int& start, int& end)
 {
-    int nHist = P.status[2];
-    int nBins = P.binsX * P.binsY;
-    int nb = nHist / nBins;
-    if (nb == 0) {
+    if (P.status[2] == 0) {  // no pairs
         start = end = 0;
         return;
     }
-    start = P.binHist[(size_t)bin * nb];
-    end = bin + 1 < nBins ? P.binHist[(size_t)(bin + 1) * nb] : P.pairOffset[P.nTris];
+    start = P.binStart[bin];
+    end = P.binStart[bin + 1];
 }
 
+// Span record staged in shared memory by the set-up phase: the depth state
+// (cf2, pz) at column xs after the sequential steps from leftClamped.
+struct SpanRec {
+    float cf2, cf2Step, pz, pzStep;
+    short xs, xe;   // bin-relative, inclusive
+    short j;        // triangle slot in the chunk
+    short flags;
+};
+
+constexpr int kRasterThreads = 128;  // 4 warps per bin
+constexpr int kChunk = 128;          // triangles per chunk (one per thread)
+constexpr int kSlots = 512;          // (triangle, row) spans set up per round
+
 template <int BW>
-__global__ void __launch_bounds__(32) k_raster(PassParams P)
+__global__ void __launch_bounds__(kRasterThreads) k_raster(PassParams P)
 {
-    constexpr int S = BW + 1;  // padded row stride: lanes at one column hit distinct banks
+    constexpr int S = BW + 1;      // padded row stride: lanes at one column hit distinct banks
+    constexpr int Q = BW / 4;      // columns per warp in the walk phase
     __shared__ float sDepth[kBinH * S];
     __shared__ int sWin[kBinH * S];
-    __shared__ __align__(16) TriRaster sTri[32];
+    __shared__ __align__(16) TriRaster sTri[kChunk];
+    __shared__ int sTid[kChunk];
+    __shared__ int sBase[kChunk + 1];
+    __shared__ unsigned char sR0[kChunk];
+    __shared__ int sSlot[kSlots];          // (row << 8) | triangle slot, per span slot of the round
+    __shared__ SpanRec sRec[kSlots];
+    __shared__ unsigned sMask[kBinH][kSlots / 32];
+    __shared__ int sWarpSum[kRasterThreads / 32];
     if (P.status[0]) return;
 
     const int bin = blockIdx.x;
     const int bx = bin % P.binsX, by = bin / P.binsX;
     const int x0 = bx * BW, y0 = by * kBinH;
-    const int lane = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int cols = min(BW, P.W - x0);
     const int rows = min(kBinH, P.H - y0);
     int start, end;
@@ -53,87 +75,155 @@ __global__ void __launch_bounds__(32) k_raster(PassParams P)
 
     if (start == end) {
         if (P.clearDepth)
-            for (int r = 0; r < rows; r++)
-                for (int c = lane; c < cols; c += 32)
-                    P.depth[(size_t)(y0 + r) * P.depthScan + x0 + c] = P.depthClearValue;
+            for (int i = tid; i < rows * cols; i += kRasterThreads) {
+                int r = i / cols, c = i - r * cols;
+                P.depth[(size_t)(y0 + r) * P.depthScan + x0 + c] = P.depthClearValue;
+            }
         return;
     }
-    for (int r = 0; r < kBinH; r++)
-        for (int c = lane; c < BW; c += 32) {
-            float d = P.depthClearValue;
-            if (!P.clearDepth && r < rows && c < cols) d = P.depth[(size_t)(y0 + r) * P.depthScan + x0 + c];
-            sDepth[r * S + c] = d;
-            sWin[r * S + c] = -1;
-        }
-    __syncwarp();
+    for (int i = tid; i < kBinH * BW; i += kRasterThreads) {
+        int r = i / BW, c = i - r * BW;
+        float d = P.depthClearValue;
+        if (!P.clearDepth && r < rows && c < cols) d = P.depth[(size_t)(y0 + r) * P.depthScan + x0 + c];
+        sDepth[r * S + c] = d;
+        sWin[r * S + c] = -1;
+    }
 
-    const int y = y0 + lane;
-    const int xLast = x0 + cols - 1;
+    // prefetch: record of the first chunk, index of the second
+    float4 rec[4];
+    int recTid = -1, nextIdx = -1;
+    if (start + tid < end) {
+        recTid = P.binTri[start + tid];
+        const float4* src = (const float4*)(P.tris + recTid);
+#pragma unroll
+        for (int k = 0; k < 4; k++) rec[k] = __ldg(src + k);
+    }
+    if (start + kChunk + tid < end) nextIdx = P.binTri[start + kChunk + tid];
+
     unsigned long long tested = 0, passed = 0;
-    for (int chunk = start; chunk < end; chunk += 32) {
-        int n = min(32, end - chunk);
-        int tid = -1;
-        unsigned mask = 0;
-        if (lane < n) {
-            tid = P.binTri[chunk + lane];
-            const float4* src = (const float4*)(P.tris + tid);
-            float4* dst = (float4*)(sTri + lane);
+    const int qs = warp * Q, qe = qs + Q - 1;  // this thread's walk columns (bin-relative)
+    for (int chunk = start; chunk < end; chunk += kChunk) {
+        // ---- phase A: stage the chunk's triangles, count their rows in the bin
+        int cnt = 0;
+        if (recTid >= 0) {
+            float4* dst = (float4*)(sTri + tid);
 #pragma unroll
-            for (int k = 0; k < 4; k++) dst[k] = src[k];
-            int r0 = max((int)sTri[lane].firstRow - y0, 0), r1 = min((int)sTri[lane].lastRow - y0, kBinH - 1);
-            if (r0 <= r1) mask = (r1 == 31 ? 0xffffffffu : ((1u << (r1 + 1)) - 1u)) & ~((1u << r0) - 1u);
+            for (int k = 0; k < 4; k++) dst[k] = rec[k];
+            sTid[tid] = recTid;
+            int r0 = max((int)sTri[tid].firstRow - y0, 0), r1 = min((int)sTri[tid].lastRow - y0, rows - 1);
+            if (r0 <= r1) cnt = r1 - r0 + 1;
+            sR0[tid] = (unsigned char)r0;
         }
-        // transpose: lane r collects the chunk's triangles that cover row r
-        unsigned mine = 0;
+        // prefetch the next chunk while this one is processed
+        recTid = nextIdx;
+        if (recTid >= 0) {
+            const float4* src = (const float4*)(P.tris + recTid);
 #pragma unroll
-        for (int r = 0; r < 32; r++) {
-            unsigned w = __ballot_sync(0xffffffffu, (mask >> r) & 1u);
-            if (lane == r) mine = w;
+            for (int k = 0; k < 4; k++) rec[k] = __ldg(src + k);
         }
-        __syncwarp();
-        if (y < P.H) {
-            while (mine) {
-                int j = __ffs(mine) - 1;
-                mine &= mine - 1;
+        nextIdx = (chunk + 2 * kChunk + tid < end) ? P.binTri[chunk + 2 * kChunk + tid] : -1;
+        // block-wide exclusive scan of the row counts
+        int inc = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int v = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += v;
+        }
+        if (lane == 31) sWarpSum[warp] = inc;
+        __syncthreads();
+        int wbase = 0, total = 0;
+#pragma unroll
+        for (int w = 0; w < kRasterThreads / 32; w++) {
+            int v = sWarpSum[w];
+            if (w < warp) wbase += v;
+            total += v;
+        }
+        sBase[tid] = wbase + inc - cnt;
+        __syncthreads();
+
+        for (int round = 0; round < total; round += kSlots) {
+            // expand: each triangle names its slots in this round
+            {
+                int b = sBase[tid], e = b + cnt;
+                int lo = max(b, round), hi = min(e, round + kSlots);
+                for (int s2 = lo; s2 < hi; s2++) sSlot[s2 - round] = ((sR0[tid] + (s2 - b)) << 8) | tid;
+            }
+            for (int i = tid; i < kBinH * (kSlots / 32); i += kRasterThreads) (&sMask[0][0])[i] = 0u;
+            __syncthreads();
+            // ---- phase B: one thread per (triangle, row) span: the reference's
+            // row result and span set-up, stepped to the bin's first column
+            int nSlots = min(kSlots, total - round);
+            for (int s2 = tid; s2 < nSlots; s2 += kRasterThreads) {
+                int code = sSlot[s2], j = code & 0xff, r = code >> 8, y = y0 + r;
                 const TriRaster& t = sTri[j];
-                Span s;
-                if (!span_row(t, y, P.W, s)) continue;
-                int xs = max(s.leftClamped, x0), xe = min(s.rightClamped, xLast);
+                Span sp;
+                if (!span_row(t, y, P.W, sp)) continue;
+                int xs = max(sp.leftClamped, x0), xe = min(sp.rightClamped, x0 + cols - 1);
                 if (xs > xe) continue;
                 SpanZ z;
-                span_z(t, s, y, z);
-                int flags = t.edges >> 16;
+                span_z(t, sp, y, z);
                 float cf2 = z.cf2, pz = z.pz;
-                for (int x = s.leftClamped; x < xs; x++) {  // the steps taken left of this bin
+                for (int x = sp.leftClamped; x < xs; x++) {
                     cf2 = fadd(cf2, z.cf2Step);
                     pz = fadd(pz, z.pzStep);
                 }
-                int triId = P.binTri[chunk + j];
-                float* dRow = sDepth + lane * S - x0;
-                int* wRow = sWin + lane * S - x0;
-                for (int x = xs; x <= xe; x++) {
-                    float inv = frcp(cf2);
-                    cf2 = fadd(cf2, z.cf2Step);
-                    float zz = fmul(pz, inv);
-                    pz = fadd(pz, z.pzStep);
-                    float cur = (flags & B_TEST_DEPTH) ? dRow[x] : 1.0f;
-                    if (-1.0f < zz && fsub(zz, cur) < -0.0001f) {
-                        if (flags & B_UPDATE_DEPTH) dRow[x] = zz;
-                        if (flags & F_COLOUR) wRow[x] = triId;
-                        passed++;
+                SpanRec& R = sRec[s2];
+                R.cf2 = cf2;
+                R.cf2Step = z.cf2Step;
+                R.pz = pz;
+                R.pzStep = z.pzStep;
+                R.xs = (short)(xs - x0);
+                R.xe = (short)(xe - x0);
+                R.j = (short)j;
+                R.flags = (short)(t.edges >> 16);
+                atomicOr(&sMask[r][s2 >> 5], 1u << (s2 & 31));
+            }
+            __syncthreads();
+            // ---- phase C: thread (warp w, lane r) applies row r's spans, in
+            // triangle order, to columns [qs, qe]: the reference's per-pixel
+            // loop (interp.cpp:82-92, fragthrd.cpp:208-252)
+            if (lane < rows) {
+                float* dRow = sDepth + lane * S;
+                int* wRow = sWin + lane * S;
+                for (int w = 0; w < (nSlots + 31) / 32; w++) {
+                    unsigned bits = sMask[lane][w];
+                    while (bits) {
+                        int k = __ffs(bits) - 1;
+                        bits &= bits - 1;
+                        const SpanRec& R = sRec[w * 32 + k];
+                        int a = max((int)R.xs, qs), b = min((int)R.xe, qe);
+                        if (a > b) continue;
+                        float cf2 = R.cf2, pz = R.pz;
+                        for (int x = R.xs; x < a; x++) {
+                            cf2 = fadd(cf2, R.cf2Step);
+                            pz = fadd(pz, R.pzStep);
+                        }
+                        int flags = R.flags;
+                        int triId = sTid[R.j];
+                        for (int x = a; x <= b; x++) {
+                            float inv = frcp(cf2);
+                            cf2 = fadd(cf2, R.cf2Step);
+                            float zz = fmul(pz, inv);
+                            pz = fadd(pz, R.pzStep);
+                            float cur = (flags & B_TEST_DEPTH) ? dRow[x] : 1.0f;
+                            if (-1.0f < zz && fsub(zz, cur) < -0.0001f) {
+                                if (flags & B_UPDATE_DEPTH) dRow[x] = zz;
+                                if (flags & F_COLOUR) wRow[x] = triId;
+                                passed++;
+                            }
+                        }
+                        tested += (unsigned long long)(b - a + 1);
                     }
                 }
-                tested += (unsigned long long)(xe - xs + 1);
             }
+            __syncthreads();
         }
-        __syncwarp();
     }
-    __syncwarp();
-    for (int r = 0; r < rows; r++)
-        for (int c = lane; c < cols; c += 32) {
-            P.depth[(size_t)(y0 + r) * P.depthScan + x0 + c] = sDepth[r * S + c];
-            if (P.anyColour) P.winner[(size_t)(y0 + r) * P.W + x0 + c] = sWin[r * S + c];
-        }
+    for (int i = tid; i < rows * cols; i += kRasterThreads) {
+        int r = i / cols, c = i - r * cols;
+        P.depth[(size_t)(y0 + r) * P.depthScan + x0 + c] = sDepth[r * S + c];
+        if (P.anyColour) P.winner[(size_t)(y0 + r) * P.W + x0 + c] = sWin[r * S + c];
+    }
     if (P.countFrags) {
 #pragma unroll
         for (int o = 16; o; o >>= 1) {
@@ -261,9 +351,9 @@ void launch_raster_shade(const PassParams& P, cudaStream_t s, int& launches, Pro
     int nBins = P.binsX * P.binsY;
     pr->begin(K_RASTER, s);
     switch (P.binW) {
-    case 16: k_raster<16><<<nBins, 32, 0, s>>>(P); break;
-    case 32: k_raster<32><<<nBins, 32, 0, s>>>(P); break;
-    default: k_raster<64><<<nBins, 32, 0, s>>>(P); break;
+    case 16: k_raster<16><<<nBins, kRasterThreads, 0, s>>>(P); break;
+    case 32: k_raster<32><<<nBins, kRasterThreads, 0, s>>>(P); break;
+    default: k_raster<64><<<nBins, kRasterThreads, 0, s>>>(P); break;
     }
     pr->end(s);
     launches++;

@@ -367,7 +367,7 @@ __global__ void k_emit(PassParams P)
         return;
     }
     if (t == 0) {
-        P.status[2] = P.binsX * P.binsY * ((total + kSortChunk - 1) / kSortChunk);
+        P.status[2] = (total + kSortChunk - 1) / kSortChunk;
         atomicAdd((unsigned long long*)(P.status + 8), (unsigned long long)total);
     }
     if (t >= P.nTris) return;
@@ -383,61 +383,127 @@ __global__ void k_emit(PassParams P)
         }
 }
 
-// Per sort block (kSortChunk consecutive pairs, one warp): counts per bin,
-// stored bin-major ([bin][block]) so that one exclusive scan over the array
-// yields each (bin, block)'s first output position.
-__global__ void k_hist(PassParams P)
+// Stable counting sort of the pairs by bin.  Sort block b covers pairs
+// [b*kSortChunk, (b+1)*kSortChunk).  k_hist counts each bin's pairs in the
+// block (hist[b][bin]); k_colscan turns each bin's column into exclusive
+// prefixes over blocks and totals; a scan of the totals gives each bin's
+// first position; k_scatter places every pair at its bin start + its block's
+// prefix + its rank among earlier same-bin pairs of the block.  Both passes
+// stage the block's keys in shared memory and rank them with one warp in
+// submission order (__match_any_sync per 32 keys).
+constexpr int kSortThreads = 256;
+
+__device__ __forceinline__ int sort_blocks(const PassParams& P)
 {
-    extern __shared__ int cnt[];
-    if (P.status[0]) return;
-    int total = P.pairOffset[P.nTris];
-    int nb = (total + kSortChunk - 1) / kSortChunk;
-    int b = blockIdx.x;
-    if (b >= nb) return;
-    int nBins = P.binsX * P.binsY;
-    for (int i = threadIdx.x; i < nBins; i += 32) cnt[i] = 0;
-    __syncwarp();
-    int lane = threadIdx.x;
-    int end = min(total, (b + 1) * kSortChunk);
-    for (int base = b * kSortChunk; base < end; base += 32) {
-        int i = base + lane;
-        int key = i < end ? P.pairKey[i] : -1 - lane;
-        unsigned peers = __match_any_sync(0xffffffffu, key);
-        if (i < end && lane == __ffs(peers) - 1) cnt[key] += __popc(peers);
-        __syncwarp();
-    }
-    __syncwarp();
-    for (int i = lane; i < nBins; i += 32) P.binHist[(size_t)i * nb + b] = cnt[i];
+    return (P.pairOffset[P.nTris] + kSortChunk - 1) / kSortChunk;
 }
 
-// Stable scatter: each pair lands at its (bin, block) base plus its rank
-// among same-bin pairs earlier in the block.
-__global__ void k_scatter(PassParams P)
+__global__ void __launch_bounds__(kSortThreads) k_hist(PassParams P)
 {
     extern __shared__ int cnt[];
+    __shared__ int keys[kSortChunk];
     if (P.status[0]) return;
     int total = P.pairOffset[P.nTris];
-    int nb = (total + kSortChunk - 1) / kSortChunk;
     int b = blockIdx.x;
-    if (b >= nb) return;
+    if (b >= sort_blocks(P)) return;
     int nBins = P.binsX * P.binsY;
-    int lane = threadIdx.x;
-    for (int i = lane; i < nBins; i += 32) cnt[i] = P.binHist[(size_t)i * nb + b];
-    __syncwarp();
-    unsigned lt = (1u << lane) - 1u;
-    int end = min(total, (b + 1) * kSortChunk);
-    for (int base = b * kSortChunk; base < end; base += 32) {
-        int i = base + lane;
-        int key = i < end ? P.pairKey[i] : -1 - lane;
-        unsigned peers = __match_any_sync(0xffffffffu, key);
-        int pos = 0;
-        if (i < end) pos = cnt[key] + __popc(peers & lt);
-        __syncwarp();
-        if (i < end) {
-            P.binTri[pos] = P.pairTri[i];
-            if (lane == __ffs(peers) - 1) cnt[key] += __popc(peers);
+    int base = b * kSortChunk, n = min(kSortChunk, total - base);
+    for (int i = threadIdx.x; i < nBins; i += kSortThreads) cnt[i] = 0;
+    for (int i = threadIdx.x; i < n; i += kSortThreads) keys[i] = P.pairKey[base + i];
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        int lane = threadIdx.x;
+        for (int i0 = 0; i0 < n; i0 += 32) {
+            int i = i0 + lane;
+            int key = i < n ? keys[i] : -1 - lane;
+            unsigned peers = __match_any_sync(0xffffffffu, key);
+            if (i < n && lane == __ffs(peers) - 1) cnt[key] += __popc(peers);
+            __syncwarp();
         }
-        __syncwarp();
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nBins; i += kSortThreads) P.binHist[(size_t)b * nBins + i] = cnt[i];
+}
+
+// Per bin: exclusive prefix of its counts over the sort blocks (in place) and
+// the bin's total into binStart[bin].
+__global__ void k_colscan(PassParams P)
+{
+    if (P.status[0]) return;
+    int nBins = P.binsX * P.binsY;
+    int bin = blockIdx.x * blockDim.x + threadIdx.x;
+    if (bin >= nBins) return;
+    int nb = sort_blocks(P), run = 0;
+    for (int b = 0; b < nb; b++) {
+        int* h = P.binHist + (size_t)b * nBins + bin;
+        int v = *h;
+        *h = run;
+        run += v;
+    }
+    P.binStart[bin] = run;
+}
+
+// Exclusive scan of the bin totals in one block; binStart[nBins] = total.
+__global__ void __launch_bounds__(1024) k_binscan(PassParams P)
+{
+    __shared__ int warpSums[32];
+    __shared__ int carry;
+    if (P.status[0]) return;
+    int nBins = P.binsX * P.binsY;
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < nBins; base += 1024) {
+        int i = base + threadIdx.x;
+        int v = i < nBins ? P.binStart[i] : 0;
+        int inc = warp_incl_scan(v);
+        if (lane == 31) warpSums[wid] = inc;
+        __syncthreads();
+        if (wid == 0) warpSums[lane] = warp_incl_scan(warpSums[lane]);
+        __syncthreads();
+        int ex = carry + (wid ? warpSums[wid - 1] : 0) + inc - v;
+        int tot = warpSums[31];
+        __syncthreads();
+        if (i < nBins) P.binStart[i] = ex;
+        if (threadIdx.x == 0) carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) P.binStart[nBins] = carry;
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_scatter(PassParams P)
+{
+    extern __shared__ int cnt[];
+    __shared__ int keys[kSortChunk];
+    __shared__ int tris[kSortChunk];
+    if (P.status[0]) return;
+    int total = P.pairOffset[P.nTris];
+    int b = blockIdx.x;
+    if (b >= sort_blocks(P)) return;
+    int nBins = P.binsX * P.binsY;
+    int base = b * kSortChunk, n = min(kSortChunk, total - base);
+    for (int i = threadIdx.x; i < nBins; i += kSortThreads)
+        cnt[i] = P.binStart[i] + P.binHist[(size_t)b * nBins + i];
+    for (int i = threadIdx.x; i < n; i += kSortThreads) {
+        keys[i] = P.pairKey[base + i];
+        tris[i] = P.pairTri[base + i];
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        int lane = threadIdx.x;
+        unsigned lt = (1u << lane) - 1u;
+        for (int i0 = 0; i0 < n; i0 += 32) {
+            int i = i0 + lane;
+            int key = i < n ? keys[i] : -1 - lane;
+            unsigned peers = __match_any_sync(0xffffffffu, key);
+            int pos = i < n ? cnt[key] + __popc(peers & lt) : 0;
+            __syncwarp();
+            if (i < n) {
+                P.binTri[pos] = tris[i];
+                if (lane == __ffs(peers) - 1) cnt[key] += __popc(peers);
+            }
+            __syncwarp();
+        }
     }
 }
 
@@ -459,15 +525,20 @@ void scan_exclusive(const int* in, int* out, int n, const int* nPtr, int nMax, i
 
 int scan_block_sums_needed(int nMax) { return ceil_div(nMax > 0 ? nMax : 1, kScanTile) + 1; }
 
-// Largest bin grid whose per-bin counters fit in one block's shared memory.
-int max_bins() { return (227 * 1024) / (int)sizeof(int); }
+// Largest bin grid whose per-bin counters fit in one block's shared memory
+// (beside the staged keys).
+int max_bins() { return (227 * 1024 - 2 * kSortChunk * (int)sizeof(int) - 1024) / (int)sizeof(int); }
 
 void launch_setup_and_bin(const PassParams& P, int* scanTmp, cudaStream_t s, int& launches, Prof* pr)
 {
     static bool attrs = false;
-    if (!attrs) {
-        cudaFuncSetAttribute(k_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        cudaFuncSetAttribute(k_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    if (!attrs) {  // opt in to the largest dynamic allocation beside each kernel's static arrays
+        cudaFuncAttributes a;
+        cudaFuncGetAttributes(&a, k_hist);
+        cudaFuncSetAttribute(k_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024 - (int)a.sharedSizeBytes);
+        cudaFuncGetAttributes(&a, k_scatter);
+        cudaFuncSetAttribute(k_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             227 * 1024 - (int)a.sharedSizeBytes);
         attrs = true;
     }
     int nBins = P.binsX * P.binsY;
@@ -482,15 +553,16 @@ void launch_setup_and_bin(const PassParams& P, int* scanTmp, cudaStream_t s, int
     launches++;
     size_t smem = (size_t)nBins * sizeof(int);
     pr->begin(K_HIST, s);
-    k_hist<<<P.sortBlocks, 32, smem, s>>>(P);
+    k_hist<<<P.sortBlocks, kSortThreads, smem, s>>>(P);
     pr->end(s);
-    launches++;
-    // binHist holds nBins * nb counts, nb known on the device only
-    scan_exclusive(P.binHist, P.binHist, 0, P.status + 2, nBins * P.sortBlocks, scanTmp, 0, P.status, s, launches, pr);
+    pr->begin(K_SCAN, s);
+    k_colscan<<<ceil_div(nBins, 256), 256, 0, s>>>(P);
+    k_binscan<<<1, 1024, 0, s>>>(P);
+    pr->end(s);
     pr->begin(K_SCATTER, s);
-    k_scatter<<<P.sortBlocks, 32, smem, s>>>(P);
+    k_scatter<<<P.sortBlocks, kSortThreads, smem, s>>>(P);
     pr->end(s);
-    launches++;
+    launches += 4;
 }
 
 }  // namespace ps3d
