@@ -54,6 +54,8 @@ CONFIGS = {
                args={}),
     "c3": dict(desc="c3: 3840x2160 LIT3, 256 seeded meshes, ~2M triangles in 4 depth layers, 16x2048^2 trilinear",
                args={}),
+    "c3s": dict(desc="c3s (profiling case): 1920x1080 LIT3, 128 meshes, ~500k triangles, 4x2048^2 trilinear",
+                args={}),
 }
 
 
@@ -119,7 +121,23 @@ class ClockSampler:
 
 def make_scene(cfg):
     from puresoft3d_gb300 import scenes as S
+    if cfg == "c3s":
+        return S.scene_c3(width=1920, height=1080, meshes=128, tri_target=500_000, textures=4)
     return {"c1": S.scene_c1, "c2": S.scene_c2, "c3": S.scene_c3}[cfg]()
+
+
+def run_frames_only(args):
+    """For profilers: set up, then render --ncu-frames frames through the
+    immediate path (no graph, no extra runs) and exit."""
+    from puresoft3d_gb300 import scenes as S
+    from puresoft3d_gb300.pipeline import PuresoftPipeline
+    scene = make_scene(args.config)
+    pipe = PuresoftPipeline(scene.width, scene.height)
+    S.replay_setup(scene, pipe)
+    for _ in range(args.ncu_frames):
+        S.replay_frame(scene, pipe)
+        pipe.finish()
+    pipe.close()
 
 
 def algorithmic_bytes(scene, pairs_per_frame):
@@ -336,7 +354,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ncu-frames", type=int, default=0, help="render N frames for a profiler and exit")
     args = ap.parse_args()
+    if args.ncu_frames:
+        run_frames_only(args)
+        return
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
         if RANK != 0:

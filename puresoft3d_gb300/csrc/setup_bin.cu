@@ -127,7 +127,13 @@ __global__ void k_setup(PassParams P)
     for (int v = 0; v < 3; v++) {
         float vary[kMaxVary];
         run_vp(d, U, 3 * lt + v, pos[v], vary);
-        for (int k = 0; k < d.nv; k++) vout[v * P.nvMax + k] = vary[k];
+        if (d.nv == 9) {
+#pragma unroll
+            for (int k = 0; k < 9; k++) vout[v * P.nvMax + k] = vary[k];
+        } else if (d.nv == 16) {
+#pragma unroll
+            for (int k = 0; k < 16; k++) vout[v * P.nvMax + k] = vary[k];
+        }
         float r = frcp(pos[v][3]);  // vertthrd.cpp:37-47: 1/w, then a 4-wide multiply
 #pragma unroll
         for (int k = 0; k < 4; k++) pos[v][k] = fmul(pos[v][k], r);
@@ -205,29 +211,22 @@ __global__ void k_setup(PassParams P)
             tr.split = split;
             tr.firstRow = (short)firstRow;
             tr.lastRow = (short)lastRow;
-            // Column bounds: edge_at is monotonic in y, so each half's span
-            // ends are extreme at that half's first and last rows.
-            int colLo = INT_MAX, colHi = INT_MIN;
-            int ra[2], rb[2], nh;
-            if (split == INT_MAX) {
-                ra[0] = firstRow; rb[0] = lastRow; nh = 1;
-            } else {
-                ra[0] = firstRow; rb[0] = min(split, lastRow);
-                ra[1] = max(split, firstRow - 1) + 1; rb[1] = lastRow; nh = 2;
-            }
-            for (int h = 0; h < nh; h++) {
-                if (ra[h] > rb[h]) continue;
-                int rows2[2] = {ra[h], rb[h]};
+            // Column bounds (conservative; only used for binning).  Each edge
+            // is evaluated at rows within (its lowest y - 1, its highest y]
+            // (row numbers are truncations), so a span end lies within the
+            // triangle's x range widened by one row of the steepest edge's
+            // run |dx/dy|, plus the +0.5 rounding and a pixel of margin.
+            float ext = 0.0f;
 #pragma unroll
-                for (int q = 0; q < 2; q++) {
-                    Span sp;
-                    span_row(tr, rows2[q], W, sp);
-                    colLo = min(colLo, min(sp.left, sp.right));
-                    colHi = max(colHi, max(sp.left, sp.right));
-                }
+            for (int a = 0; a < 3; a++) {
+                int b2 = a == 2 ? 0 : a + 1;
+                float dy = fabsf(vy[b2] - vy[a]), dx = fabsf(vx[b2] - vx[a]);
+                if (dy >= 0.000001f) ext = fmaxf(ext, __fdividef(dx, dy) * 1.0001f);
             }
-            colLo = max(colLo, 0);
-            colHi = min(colHi, W - 1);
+            float xmin = fminf(vx[0], fminf(vx[1], vx[2])) - ext - 2.0f;
+            float xmax = fmaxf(vx[0], fmaxf(vx[1], vx[2])) + ext + 2.0f;
+            int colLo = xmin < 0.0f ? 0 : (xmin > (float)W ? W : (int)xmin);
+            int colHi = xmax > (float)(W - 1) ? W - 1 : (xmax < 0.0f ? -1 : (int)xmax);
             if (colLo <= colHi) {
                 bx0 = colLo / P.binW;
                 bx1 = colHi / P.binW;
