@@ -491,6 +491,7 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     P.tris = p->tris;
     P.vary = p->vary;
     P.nvMax = std::max(nvMax, 1);
+    P.anyVary = nvMax > 0;
     P.pairCount = p->pairCount;
     P.rect = p->rect;
     P.pairOffset = p->pairOffset;

@@ -80,6 +80,7 @@ struct PassParams {
     TriRaster* tris;
     float* vary;              // [tri][3][nvMax]
     int nvMax;
+    int anyVary;              // some draw of the pass carries varyings
     int* pairCount;           // per triangle: bins its rectangle touches
     int4* rect;               // per triangle: bin rectangle {x0, x1, y0, y1}
     int* pairOffset;          // exclusive scan of pairCount (+ total at [nTris])

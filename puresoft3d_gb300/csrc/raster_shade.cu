@@ -200,16 +200,30 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(PassParams P)
                         }
                         int flags = R.flags;
                         int triId = sTid[R.j];
-                        for (int x = a; x <= b; x++) {
-                            float inv = frcp(cf2);
-                            cf2 = fadd(cf2, R.cf2Step);
-                            float zz = fmul(pz, inv);
-                            pz = fadd(pz, R.pzStep);
-                            float cur = (flags & B_TEST_DEPTH) ? dRow[x] : 1.0f;
-                            if (-1.0f < zz && fsub(zz, cur) < -0.0001f) {
-                                if (flags & B_UPDATE_DEPTH) dRow[x] = zz;
-                                if (flags & F_COLOUR) wRow[x] = triId;
-                                passed++;
+                        int n = b - a + 1;
+                        // the state at columns a .. a+Q-1 by sequential steps (the
+                        // values past b are computed and ignored), then one
+                        // independent depth test per column
+                        float cfv[Q], pzv[Q];
+                        cfv[0] = cf2;
+                        pzv[0] = pz;
+#pragma unroll
+                        for (int i = 1; i < Q; i++) {
+                            cfv[i] = fadd(cfv[i - 1], R.cf2Step);
+                            pzv[i] = fadd(pzv[i - 1], R.pzStep);
+                        }
+                        float* dA = dRow + a;
+                        int* wA = wRow + a;
+#pragma unroll
+                        for (int i = 0; i < Q; i++) {
+                            if (i < n) {
+                                float zz = fmul(pzv[i], frcp(cfv[i]));
+                                float cur = (flags & B_TEST_DEPTH) ? dA[i] : 1.0f;
+                                if (-1.0f < zz && fsub(zz, cur) < -0.0001f) {
+                                    if (flags & B_UPDATE_DEPTH) dA[i] = zz;
+                                    if (flags & F_COLOUR) wA[i] = triId;
+                                    passed++;
+                                }
                             }
                         }
                         tested += (unsigned long long)(b - a + 1);

@@ -107,10 +107,10 @@ __device__ __forceinline__ bool back_face(const float p[3][4])
 
 __device__ __forceinline__ int edge_code(int a, int b) { return a | (b << 2); }
 
-__global__ void k_setup(PassParams P)
+constexpr int kSetupThreads = 128;
+
+__device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float* sVary)
 {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= P.nTris) return;
     int lo = 0, hi = P.nDraws - 1;
     while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
@@ -122,7 +122,7 @@ __global__ void k_setup(PassParams P)
     int lt = t - d.triBase;
 
     float pos[3][4], rw[3], pz[3];
-    float* vout = P.vary + (size_t)t * 3 * P.nvMax;
+    float* vout = sVary + threadIdx.x * 3 * P.nvMax;
 #pragma unroll
     for (int v = 0; v < 3; v++) {
         float vary[kMaxVary];
@@ -246,6 +246,21 @@ __global__ void k_setup(PassParams P)
     for (int k = 0; k < 4; k++) dst[k] = src[k];
     P.pairCount[t] = count;
     P.rect[t] = make_int4(bx0, bx1, by0, by1);
+}
+
+// The varyings go out through shared memory so that the block's stores are
+// contiguous: triangle t's 3*nvMax floats start at vary + t*3*nvMax.
+__global__ void __launch_bounds__(kSetupThreads) k_setup(PassParams P)
+{
+    __shared__ float sVary[kSetupThreads * 3 * kMaxVary];
+    int t = blockIdx.x * kSetupThreads + threadIdx.x;
+    if (t < P.nTris) setup_triangle(P, t, sVary);
+    if (!P.anyVary) return;
+    __syncthreads();
+    int first = blockIdx.x * kSetupThreads, n = min(kSetupThreads, P.nTris - first);
+    int nf = n * 3 * P.nvMax;
+    float* dst = P.vary + (size_t)first * 3 * P.nvMax;
+    for (int i = threadIdx.x; i < nf; i += kSetupThreads) dst[i] = sVary[i];
 }
 
 // ---------------------------------------------------------------- prefix sum
@@ -542,7 +557,7 @@ void launch_setup_and_bin(const PassParams& P, int* scanTmp, cudaStream_t s, int
     }
     int nBins = P.binsX * P.binsY;
     pr->begin(K_SETUP, s);
-    k_setup<<<ceil_div(P.nTris, 128), 128, 0, s>>>(P);
+    k_setup<<<ceil_div(P.nTris, kSetupThreads), kSetupThreads, 0, s>>>(P);
     pr->end(s);
     launches++;
     scan_exclusive(P.pairCount, P.pairOffset, P.nTris, nullptr, P.nTris, scanTmp, 1, P.status, s, launches, pr);
