@@ -113,6 +113,7 @@ struct ps3do {
     int threads;
     o_tasklist* lists; /* one per worker */
     long long tested, passed;
+    long long spanHist[32]; /* spans by floor(log2(x2 - x1 + 1)) */
     /* worker pool */
     pthread_t* th;
     pthread_mutex_t mu;
@@ -398,6 +399,7 @@ int ps3do_read_depth(ps3do* p, void* out)
 }
 
 long long ps3do_fragments_tested(ps3do* p) { return p->tested; }
+void ps3do_span_histogram(ps3do* p, long long* out) { memcpy(out, p->spanHist, sizeof p->spanHist); }
 long long ps3do_fragments_passed(ps3do* p) { return p->passed; }
 
 /* ------------------------------------------------------ processors (VP/IP/FP) */
@@ -991,6 +993,11 @@ int ps3do_draw(ps3do* p, int vao)
             o_task t;
             if (row->left == row->right) continue; /* drawvao.cpp:72-75 */
             span_setup(&r, row, y, rw, pz, nv, vu, &t);
+            if (t.x2 >= t.x1) {
+                int len = t.x2 - t.x1 + 1, b = 0;
+                while (len >>= 1) b++;
+                p->spanHist[b]++;
+            }
             if ((rc = push_task(&p->lists[y % p->threads], &t)) != 0) goto out;
         }
     }

@@ -45,6 +45,8 @@ int ps3do_read_depth(ps3do* p, void* out);
    iterations, fragthrd.cpp:208) and fragments that passed it, since create. */
 long long ps3do_fragments_tested(ps3do* p);
 long long ps3do_fragments_passed(ps3do* p);
+/* Spans drawn since create, bucketed by floor(log2(length in pixels)). */
+void ps3do_span_histogram(ps3do* p, long long* out32);
 
 #ifdef __cplusplus
 }

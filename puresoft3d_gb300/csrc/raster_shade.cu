@@ -1,18 +1,16 @@
 // raster_shade.cu -- visibility and shading passes.
 //
-// k_raster  one 128-thread block per bin of 32 rows x binW columns.  The
+// k_raster  one 128-thread block per bin of 128 rows x binW columns.  The
 //           bin's depth and "winner" (last colour-writing fragment that
 //           passed) live in shared memory.  Triangles arrive in submission
 //           order, 128 at a time.  Set-up phase: one thread per (triangle,
 //           row) span computes the reference's row result and span set-up
 //           (rasterizer.cpp:93-118, interp.cpp:26-80), stepped sequentially
-//           to the bin's first column.  Walk phase: thread (warp w, lane r)
-//           owns row r, columns [w*binW/4, (w+1)*binW/4), and applies that
-//           row's spans in triangle order with the reference's sequential
-//           accumulation (interp.cpp:82-92) and epsilon depth test
-//           (fragthrd.cpp:227) -- every pixel has exactly one owner, so the
-//           per-pixel order is the reference's per-row FIFO order
-//           (drawvao.cpp:77-109).
+//           to the bin's first column.  Walk phase: thread r owns row r and
+//           applies that row's spans in triangle order with the reference's
+//           sequential accumulation (interp.cpp:82-92) and epsilon depth test
+//           (fragthrd.cpp:227) -- one owner per row, so the per-pixel order is
+//           the reference's per-row FIFO order (drawvao.cpp:77-109).
 // k_shade   one thread per pixel: re-derives the winning fragment's
 //           varyings (same span set-up and sequential steps) and runs the
 //           draw's fragment stage once.  With no discard and no blending the
@@ -43,21 +41,19 @@ struct SpanRec {
     short flags;
 };
 
-constexpr int kRasterThreads = 128;  // 4 warps per bin
-constexpr int kChunk = 128;          // triangles per chunk (one per thread)
-constexpr int kSlots = 512;          // (triangle, row) spans set up per round
+constexpr int kRasterThreads = kBinH;  // one thread per bin row
+constexpr int kChunk = 128;            // triangles per chunk (one per thread)
+constexpr int kSlots = 256;            // (triangle, row) spans set up per round
 
 template <int BW>
-__global__ void __launch_bounds__(kRasterThreads) k_raster(PassParams P)
+__global__ void __launch_bounds__(kRasterThreads, 3) k_raster(PassParams P)
 {
-    constexpr int S = BW + 1;      // padded row stride: lanes at one column hit distinct banks
-    constexpr int Q = BW / 4;      // columns per warp in the walk phase
-    __shared__ float sDepth[kBinH * S];
-    __shared__ int sWin[kBinH * S];
+    constexpr int S = BW + 1;  // padded row stride: threads at one column hit distinct banks
+    extern __shared__ float sDyn[];  // depth then winner, kBinH * S each
+    float* sDepth = sDyn;
+    int* sWin = (int*)(sDyn + kBinH * S);
     __shared__ __align__(16) TriRaster sTri[kChunk];
     __shared__ int sTid[kChunk];
-    __shared__ int sBase[kChunk + 1];
-    __shared__ unsigned char sR0[kChunk];
     __shared__ int sSlot[kSlots];          // (row << 8) | triangle slot, per span slot of the round
     __shared__ SpanRec sRec[kSlots];
     __shared__ unsigned sMask[kBinH][kSlots / 32];
@@ -101,18 +97,19 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(PassParams P)
     if (start + kChunk + tid < end) nextIdx = P.binTri[start + kChunk + tid];
 
     unsigned long long tested = 0, passed = 0;
-    const int qs = warp * Q, qe = qs + Q - 1;  // this thread's walk columns (bin-relative)
+    float* dRow = sDepth + tid * S;
+    int* wRow = sWin + tid * S;
     for (int chunk = start; chunk < end; chunk += kChunk) {
-        // ---- phase A: stage the chunk's triangles, count their rows in the bin
-        int cnt = 0;
+        // ---- stage the chunk's triangles, count their rows in the bin
+        int cnt = 0, r0 = 0;
         if (recTid >= 0) {
             float4* dst = (float4*)(sTri + tid);
 #pragma unroll
             for (int k = 0; k < 4; k++) dst[k] = rec[k];
             sTid[tid] = recTid;
-            int r0 = max((int)sTri[tid].firstRow - y0, 0), r1 = min((int)sTri[tid].lastRow - y0, rows - 1);
+            r0 = max((int)sTri[tid].firstRow - y0, 0);
+            int r1 = min((int)sTri[tid].lastRow - y0, rows - 1);
             if (r0 <= r1) cnt = r1 - r0 + 1;
-            sR0[tid] = (unsigned char)r0;
         }
         // prefetch the next chunk while this one is processed
         recTid = nextIdx;
@@ -138,20 +135,19 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(PassParams P)
             if (w < warp) wbase += v;
             total += v;
         }
-        sBase[tid] = wbase + inc - cnt;
-        __syncthreads();
+        const int base = wbase + inc - cnt;
 
         for (int round = 0; round < total; round += kSlots) {
-            // expand: each triangle names its slots in this round
+            // each triangle names its spans in this round; masks cleared
             {
-                int b = sBase[tid], e = b + cnt;
-                int lo = max(b, round), hi = min(e, round + kSlots);
-                for (int s2 = lo; s2 < hi; s2++) sSlot[s2 - round] = ((sR0[tid] + (s2 - b)) << 8) | tid;
+                int lo = max(base, round), hi = min(base + cnt, round + kSlots);
+                for (int s2 = lo; s2 < hi; s2++) sSlot[s2 - round] = ((r0 + (s2 - base)) << 8) | tid;
             }
-            for (int i = tid; i < kBinH * (kSlots / 32); i += kRasterThreads) (&sMask[0][0])[i] = 0u;
+#pragma unroll
+            for (int w = 0; w < kSlots / 32; w++) sMask[tid][w] = 0u;
             __syncthreads();
-            // ---- phase B: one thread per (triangle, row) span: the reference's
-            // row result and span set-up, stepped to the bin's first column
+            // ---- one thread per (triangle, row) span: the reference's row
+            // result and span set-up, stepped to the bin's first column
             int nSlots = min(kSlots, total - round);
             for (int s2 = tid; s2 < nSlots; s2 += kRasterThreads) {
                 int code = sSlot[s2], j = code & 0xff, r = code >> 8, y = y0 + r;
@@ -179,51 +175,29 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(PassParams P)
                 atomicOr(&sMask[r][s2 >> 5], 1u << (s2 & 31));
             }
             __syncthreads();
-            // ---- phase C: thread (warp w, lane r) applies row r's spans, in
-            // triangle order, to columns [qs, qe]: the reference's per-pixel
-            // loop (interp.cpp:82-92, fragthrd.cpp:208-252)
-            if (lane < rows) {
-                float* dRow = sDepth + lane * S;
-                int* wRow = sWin + lane * S;
+            // ---- thread r applies row r's spans in triangle order: the
+            // reference's per-pixel loop (interp.cpp:82-92, fragthrd.cpp:208-252)
+            if (tid < rows) {
                 for (int w = 0; w < (nSlots + 31) / 32; w++) {
-                    unsigned bits = sMask[lane][w];
+                    unsigned bits = sMask[tid][w];
                     while (bits) {
                         int k = __ffs(bits) - 1;
                         bits &= bits - 1;
                         const SpanRec& R = sRec[w * 32 + k];
-                        int a = max((int)R.xs, qs), b = min((int)R.xe, qe);
-                        if (a > b) continue;
                         float cf2 = R.cf2, pz = R.pz;
-                        for (int x = R.xs; x < a; x++) {
-                            cf2 = fadd(cf2, R.cf2Step);
-                            pz = fadd(pz, R.pzStep);
-                        }
-                        int flags = R.flags;
-                        int triId = sTid[R.j];
-                        int n = b - a + 1;
-                        // the state at columns a .. a+Q-1 by sequential steps (the
-                        // values past b are computed and ignored), then one
-                        // independent depth test per column
-                        float cfv[Q], pzv[Q];
-                        cfv[0] = cf2;
-                        pzv[0] = pz;
-#pragma unroll
-                        for (int i = 1; i < Q; i++) {
-                            cfv[i] = fadd(cfv[i - 1], R.cf2Step);
-                            pzv[i] = fadd(pzv[i - 1], R.pzStep);
-                        }
-                        float* dA = dRow + a;
-                        int* wA = wRow + a;
-#pragma unroll
-                        for (int i = 0; i < Q; i++) {
-                            if (i < n) {
-                                float zz = fmul(pzv[i], frcp(cfv[i]));
-                                float cur = (flags & B_TEST_DEPTH) ? dA[i] : 1.0f;
-                                if (-1.0f < zz && fsub(zz, cur) < -0.0001f) {
-                                    if (flags & B_UPDATE_DEPTH) dA[i] = zz;
-                                    if (flags & F_COLOUR) wA[i] = triId;
-                                    passed++;
-                                }
+                        const float cs = R.cf2Step, ps = R.pzStep;
+                        const int flags = R.flags, a = R.xs, b = R.xe;
+                        const int triId = sTid[R.j];
+                        for (int x = a; x <= b; x++) {
+                            float inv = frcp(cf2);
+                            cf2 = fadd(cf2, cs);
+                            float zz = fmul(pz, inv);
+                            pz = fadd(pz, ps);
+                            float cur = (flags & B_TEST_DEPTH) ? dRow[x] : 1.0f;
+                            if (-1.0f < zz && fsub(zz, cur) < -0.0001f) {
+                                if (flags & B_UPDATE_DEPTH) dRow[x] = zz;
+                                if (flags & F_COLOUR) wRow[x] = triId;
+                                passed++;
                             }
                         }
                         tested += (unsigned long long)(b - a + 1);
@@ -232,6 +206,7 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(PassParams P)
             }
             __syncthreads();
         }
+        if (total == 0) __syncthreads();  // sWarpSum / sTri are rewritten by the next chunk
     }
     for (int i = tid; i < rows * cols; i += kRasterThreads) {
         int r = i / cols, c = i - r * cols;
@@ -360,14 +335,27 @@ __global__ void k_fill_u32(uint32_t* base, int width, int height, int pitchElems
 
 static inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
+template <int BW> void launch_raster(const PassParams& P, int nBins, cudaStream_t s)
+{
+    size_t dyn = (size_t)2 * kBinH * (BW + 1) * sizeof(float);
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncAttributes a;
+        cudaFuncGetAttributes(&a, k_raster<BW>);
+        cudaFuncSetAttribute(k_raster<BW>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024 - (int)a.sharedSizeBytes);
+        attr = true;
+    }
+    k_raster<BW><<<nBins, kRasterThreads, dyn, s>>>(P);
+}
+
 void launch_raster_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
 {
     int nBins = P.binsX * P.binsY;
     pr->begin(K_RASTER, s);
     switch (P.binW) {
-    case 16: k_raster<16><<<nBins, kRasterThreads, 0, s>>>(P); break;
-    case 32: k_raster<32><<<nBins, kRasterThreads, 0, s>>>(P); break;
-    default: k_raster<64><<<nBins, kRasterThreads, 0, s>>>(P); break;
+    case 16: launch_raster<16>(P, nBins, s); break;
+    case 32: launch_raster<32>(P, nBins, s); break;
+    default: launch_raster<64>(P, nBins, s); break;
     }
     pr->end(s);
     launches++;
