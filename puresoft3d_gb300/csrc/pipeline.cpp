@@ -651,7 +651,7 @@ int ps3d_pipeline_create(int width, int height, void* stream, ps3d_pipeline** ou
     }
     if (const char* bw = getenv("PS3D_BIN_W")) {
         int v = atoi(bw);
-        if (v == 16 || v == 32 || v == 64) p->binW = v;
+        if (v == 16 || v == 32) p->binW = v;
     }
     if (stream) p->stream = (cudaStream_t)stream;
     else {

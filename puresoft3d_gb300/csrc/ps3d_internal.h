@@ -10,8 +10,8 @@ namespace ps3d {
 constexpr int kMaxLevels = 16;
 constexpr int kMaxVary = 16;     // varying floats per vertex (LIT2: 16)
 constexpr int kVboSlots = 5;     // VBO slots the built-in vertex stages read (0..4)
-constexpr int kBinH = 128;       // bin height in rows: one raster thread per row
-constexpr int kMaxBinW = 64;
+constexpr int kBinH = 32;        // bin height in rows: one warp lane per row
+constexpr int kMaxBinW = 32;
 
 // processor ids (include/ps3d.h)
 enum : int {

@@ -1,16 +1,18 @@
 // raster_shade.cu -- visibility and shading passes.
 //
-// k_raster  one 128-thread block per bin of 128 rows x binW columns.  The
+// k_raster  one 128-thread block per bin of 32 rows x binW columns.  The
 //           bin's depth and "winner" (last colour-writing fragment that
 //           passed) live in shared memory.  Triangles arrive in submission
-//           order, 128 at a time.  Set-up phase: one thread per (triangle,
-//           row) span computes the reference's row result and span set-up
-//           (rasterizer.cpp:93-118, interp.cpp:26-80), stepped sequentially
-//           to the bin's first column.  Walk phase: thread r owns row r and
-//           applies that row's spans in triangle order with the reference's
-//           sequential accumulation (interp.cpp:82-92) and epsilon depth test
-//           (fragthrd.cpp:227) -- one owner per row, so the per-pixel order is
-//           the reference's per-row FIFO order (drawvao.cpp:77-109).
+//           order, 128 at a time, and their (triangle, row) spans are handled
+//           128 at a time.  Set-up: one thread per span computes the
+//           reference's row result and span set-up (rasterizer.cpp:93-118,
+//           interp.cpp:26-80) and the exact z of each of its pixels with the
+//           reference's sequential accumulation (interp.cpp:82-92).  Walk:
+//           thread (warp w, lane r) owns row r, columns
+//           [w*binW/4, (w+1)*binW/4), and applies that row's spans in
+//           triangle order with the epsilon depth test (fragthrd.cpp:227) --
+//           every pixel has exactly one owner, so the per-pixel order is the
+//           reference's per-row FIFO order (drawvao.cpp:77-109).
 // k_shade   one thread per pixel: re-derives the winning fragment's
 //           varyings (same span set-up and sequential steps) and runs the
 //           draw's fragment stage once.  With no discard and no blending the
@@ -32,31 +34,31 @@ __device__ __forceinline__ void bin_range(const PassParams& P, int bin, int& sta
     end = P.binStart[bin + 1];
 }
 
-// Span record staged in shared memory by the set-up phase: the depth state
-// (cf2, pz) at column xs after the sequential steps from leftClamped.
+// Per span of a round: its columns in the bin, its triangle slot and flags.
 struct SpanRec {
-    float cf2, cf2Step, pz, pzStep;
     short xs, xe;   // bin-relative, inclusive
     short j;        // triangle slot in the chunk
     short flags;
 };
 
-constexpr int kRasterThreads = kBinH;  // one thread per bin row
-constexpr int kChunk = 128;            // triangles per chunk (one per thread)
-constexpr int kSlots = 256;            // (triangle, row) spans set up per round
+constexpr int kRasterThreads = 128;  // 4 warps: warp = column quarter, lane = bin row
+constexpr int kChunk = 128;          // triangles per chunk (one per thread)
+constexpr int kSlots = 128;          // (triangle, row) spans per round (one per thread)
 
 template <int BW>
-__global__ void __launch_bounds__(kRasterThreads, 3) k_raster(PassParams P)
+__global__ void __launch_bounds__(kRasterThreads) k_raster(PassParams P)
 {
-    constexpr int S = BW + 1;  // padded row stride: threads at one column hit distinct banks
-    extern __shared__ float sDyn[];  // depth then winner, kBinH * S each
-    float* sDepth = sDyn;
-    int* sWin = (int*)(sDyn + kBinH * S);
+    constexpr int S = BW + 1;   // padded strides: threads at one column hit distinct banks
+    constexpr int Q = BW / 4;   // columns per quarter
+    __shared__ float sDepth[kBinH * S];
+    __shared__ int sWin[kBinH * S];
+    __shared__ float sZ[kSlots * S];             // exact z of every pixel of each span
+    __shared__ float sZmin[4][kSlots];           // per span and quarter: min z over its pixels
     __shared__ __align__(16) TriRaster sTri[kChunk];
     __shared__ int sTid[kChunk];
-    __shared__ int sSlot[kSlots];          // (row << 8) | triangle slot, per span slot of the round
+    __shared__ int sSlot[kSlots];                // (row << 8) | triangle slot
     __shared__ SpanRec sRec[kSlots];
-    __shared__ unsigned sMask[kBinH][kSlots / 32];
+    __shared__ unsigned sMask[4][kBinH][kSlots / 32];
     __shared__ int sWarpSum[kRasterThreads / 32];
     if (P.status[0]) return;
 
@@ -97,8 +99,9 @@ __global__ void __launch_bounds__(kRasterThreads, 3) k_raster(PassParams P)
     if (start + kChunk + tid < end) nextIdx = P.binTri[start + kChunk + tid];
 
     unsigned long long tested = 0, passed = 0;
-    float* dRow = sDepth + tid * S;
-    int* wRow = sWin + tid * S;
+    const int qs = warp * Q, qe = qs + Q - 1;  // this thread's columns (bin-relative)
+    float* dRow = sDepth + lane * S;
+    int* wRow = sWin + lane * S;
     for (int chunk = start; chunk < end; chunk += kChunk) {
         // ---- stage the chunk's triangles, count their rows in the bin
         int cnt = 0, r0 = 0;
@@ -111,16 +114,14 @@ __global__ void __launch_bounds__(kRasterThreads, 3) k_raster(PassParams P)
             int r1 = min((int)sTri[tid].lastRow - y0, rows - 1);
             if (r0 <= r1) cnt = r1 - r0 + 1;
         }
-        // prefetch the next chunk while this one is processed
-        recTid = nextIdx;
+        recTid = nextIdx;  // prefetch the next chunk while this one is processed
         if (recTid >= 0) {
             const float4* src = (const float4*)(P.tris + recTid);
 #pragma unroll
             for (int k = 0; k < 4; k++) rec[k] = __ldg(src + k);
         }
         nextIdx = (chunk + 2 * kChunk + tid < end) ? P.binTri[chunk + 2 * kChunk + tid] : -1;
-        // block-wide exclusive scan of the row counts
-        int inc = cnt;
+        int inc = cnt;  // block-wide exclusive scan of the row counts
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             int v = __shfl_up_sync(0xffffffffu, inc, o);
@@ -138,61 +139,88 @@ __global__ void __launch_bounds__(kRasterThreads, 3) k_raster(PassParams P)
         const int base = wbase + inc - cnt;
 
         for (int round = 0; round < total; round += kSlots) {
-            // each triangle names its spans in this round; masks cleared
             {
                 int lo = max(base, round), hi = min(base + cnt, round + kSlots);
                 for (int s2 = lo; s2 < hi; s2++) sSlot[s2 - round] = ((r0 + (s2 - base)) << 8) | tid;
             }
-#pragma unroll
-            for (int w = 0; w < kSlots / 32; w++) sMask[tid][w] = 0u;
+            for (int i = tid; i < 4 * kBinH * (kSlots / 32); i += kRasterThreads) (&sMask[0][0][0])[i] = 0u;
             __syncthreads();
-            // ---- one thread per (triangle, row) span: the reference's row
-            // result and span set-up, stepped to the bin's first column
-            int nSlots = min(kSlots, total - round);
-            for (int s2 = tid; s2 < nSlots; s2 += kRasterThreads) {
+            // ---- set-up: thread s2 takes span s2 of the round -- the reference's
+            // row result and span set-up (rasterizer.cpp:93-118, interp.cpp:26-80),
+            // then the sequential per-pixel steps (interp.cpp:82-92) through the
+            // bin's columns, storing each pixel's exact z
+            const int nSlots = min(kSlots, total - round);
+            if (tid < nSlots) {
+                const int s2 = tid;
                 int code = sSlot[s2], j = code & 0xff, r = code >> 8, y = y0 + r;
                 const TriRaster& t = sTri[j];
                 Span sp;
-                if (!span_row(t, y, P.W, sp)) continue;
-                int xs = max(sp.leftClamped, x0), xe = min(sp.rightClamped, x0 + cols - 1);
-                if (xs > xe) continue;
-                SpanZ z;
-                span_z(t, sp, y, z);
-                float cf2 = z.cf2, pz = z.pz;
-                for (int x = sp.leftClamped; x < xs; x++) {
-                    cf2 = fadd(cf2, z.cf2Step);
-                    pz = fadd(pz, z.pzStep);
+                if (span_row(t, y, P.W, sp)) {
+                    int xs = max(sp.leftClamped, x0), xe = min(sp.rightClamped, x0 + cols - 1);
+                    if (xs <= xe) {
+                        SpanZ z;
+                        span_z(t, sp, y, z);
+                        float cf2 = z.cf2, pz = z.pz;
+                        for (int x = sp.leftClamped; x < xs; x++) {
+                            cf2 = fadd(cf2, z.cf2Step);
+                            pz = fadd(pz, z.pzStep);
+                        }
+                        float* zrow = sZ + s2 * S - x0;
+                        float zmin = 0.0f;
+                        int q = (xs - x0) / Q;
+                        for (int x = xs; x <= xe; x++) {
+                            float zz = fmul(pz, frcp(cf2));
+                            cf2 = fadd(cf2, z.cf2Step);
+                            pz = fadd(pz, z.pzStep);
+                            zrow[x] = zz;
+                            int qx = (x - x0) / Q;
+                            if (qx != q || x == xs) {
+                                if (x != xs) {
+                                    sZmin[q][s2] = zmin;
+                                    atomicOr(&sMask[q][r][s2 >> 5], 1u << (s2 & 31));
+                                }
+                                q = qx;
+                                zmin = zz;
+                            } else {
+                                zmin = fminf(zmin, zz);
+                            }
+                        }
+                        sZmin[q][s2] = zmin;
+                        atomicOr(&sMask[q][r][s2 >> 5], 1u << (s2 & 31));
+                        SpanRec& R = sRec[s2];
+                        R.xs = (short)(xs - x0);
+                        R.xe = (short)(xe - x0);
+                        R.j = (short)j;
+                        R.flags = (short)(t.edges >> 16);
+                    }
                 }
-                SpanRec& R = sRec[s2];
-                R.cf2 = cf2;
-                R.cf2Step = z.cf2Step;
-                R.pz = pz;
-                R.pzStep = z.pzStep;
-                R.xs = (short)(xs - x0);
-                R.xe = (short)(xe - x0);
-                R.j = (short)j;
-                R.flags = (short)(t.edges >> 16);
-                atomicOr(&sMask[r][s2 >> 5], 1u << (s2 & 31));
             }
             __syncthreads();
-            // ---- thread r applies row r's spans in triangle order: the
-            // reference's per-pixel loop (interp.cpp:82-92, fragthrd.cpp:208-252)
-            if (tid < rows) {
+            // ---- walk: thread (quarter w, row r) applies row r's spans in
+            // triangle order to its columns -- the reference's depth test and
+            // writes (fragthrd.cpp:208-252).  A span none of whose pixels can
+            // pass (z >= zmin >= every current depth here + epsilon) is skipped:
+            // with TEST_DEPTH on, depth only decreases, so curMax stays an
+            // upper bound and the skip never changes a result.
+            if (lane < rows) {
+                float curMax = dRow[qs];
+#pragma unroll
+                for (int c = 1; c < Q; c++) curMax = fmaxf(curMax, dRow[qs + c]);
                 for (int w = 0; w < (nSlots + 31) / 32; w++) {
-                    unsigned bits = sMask[tid][w];
+                    unsigned bits = sMask[warp][lane][w];
                     while (bits) {
                         int k = __ffs(bits) - 1;
                         bits &= bits - 1;
-                        const SpanRec& R = sRec[w * 32 + k];
-                        float cf2 = R.cf2, pz = R.pz;
-                        const float cs = R.cf2Step, ps = R.pzStep;
-                        const int flags = R.flags, a = R.xs, b = R.xe;
+                        const int s2 = w * 32 + k;
+                        const SpanRec R = sRec[s2];
+                        const int a = max((int)R.xs, qs), b = min((int)R.xe, qe);
+                        const int flags = R.flags;
+                        tested += (unsigned long long)(b - a + 1);
+                        if ((flags & B_TEST_DEPTH) && fsub(sZmin[warp][s2], curMax) >= -0.0001f) continue;
+                        const float* zrow = sZ + s2 * S;
                         const int triId = sTid[R.j];
                         for (int x = a; x <= b; x++) {
-                            float inv = frcp(cf2);
-                            cf2 = fadd(cf2, cs);
-                            float zz = fmul(pz, inv);
-                            pz = fadd(pz, ps);
+                            float zz = zrow[x];
                             float cur = (flags & B_TEST_DEPTH) ? dRow[x] : 1.0f;
                             if (-1.0f < zz && fsub(zz, cur) < -0.0001f) {
                                 if (flags & B_UPDATE_DEPTH) dRow[x] = zz;
@@ -200,7 +228,11 @@ __global__ void __launch_bounds__(kRasterThreads, 3) k_raster(PassParams P)
                                 passed++;
                             }
                         }
-                        tested += (unsigned long long)(b - a + 1);
+                        if (!(flags & B_TEST_DEPTH)) {  // depth may have risen: recompute the bound
+                            curMax = dRow[qs];
+#pragma unroll
+                            for (int c = 1; c < Q; c++) curMax = fmaxf(curMax, dRow[qs + c]);
+                        }
                     }
                 }
             }
@@ -337,15 +369,7 @@ static inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) 
 
 template <int BW> void launch_raster(const PassParams& P, int nBins, cudaStream_t s)
 {
-    size_t dyn = (size_t)2 * kBinH * (BW + 1) * sizeof(float);
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncAttributes a;
-        cudaFuncGetAttributes(&a, k_raster<BW>);
-        cudaFuncSetAttribute(k_raster<BW>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024 - (int)a.sharedSizeBytes);
-        attr = true;
-    }
-    k_raster<BW><<<nBins, kRasterThreads, dyn, s>>>(P);
+    k_raster<BW><<<nBins, kRasterThreads, 0, s>>>(P);
 }
 
 void launch_raster_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
@@ -354,8 +378,7 @@ void launch_raster_shade(const PassParams& P, cudaStream_t s, int& launches, Pro
     pr->begin(K_RASTER, s);
     switch (P.binW) {
     case 16: launch_raster<16>(P, nBins, s); break;
-    case 32: launch_raster<32>(P, nBins, s); break;
-    default: launch_raster<64>(P, nBins, s); break;
+    default: launch_raster<32>(P, nBins, s); break;
     }
     pr->end(s);
     launches++;
