@@ -224,6 +224,11 @@ int ps3d_timer_end(ps3d_pipeline* p, float* ms);
 #define PS3D_K_SHADE 6
 #define PS3D_K_FILL 7
 #define PS3D_K_COUNT 8
+/* Checks the kernels' fast correctly rounded reciprocal and quotient
+ * against CUDA's IEEE ones on the current device: every float mantissa of
+ * exponents -100..100 for the reciprocal, `pairs` hashed pairs for the
+ * quotient.  Both counts must be 0. */
+int ps3d_selftest_division(uint64_t pairs, uint64_t* rcpMismatches, uint64_t* divMismatches);
 /* Overwrites `bytes` of an internal device buffer on the pipeline's stream
  * (benchmarking aid: evicts the 126 MB L2 between timed frames). */
 int ps3d_l2_scrub(ps3d_pipeline* p, size_t bytes);

@@ -32,6 +32,7 @@ namespace ps3d {
 void launch_setup_and_bin(const PassParams& P, int* scanTmp, cudaStream_t s, int& launches, Prof* pr);
 int scan_block_sums_needed(int nMax);
 int max_bins();
+int selftest_division(unsigned long long pairs, unsigned long long* rcpBad, unsigned long long* divBad);
 void launch_raster_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr);
 void launch_fill_u32(void* base, int width, int height, int pitchElems, uint32_t v, const int* status,
                      cudaStream_t s, int& launches, Prof* pr);
@@ -1284,6 +1285,16 @@ int ps3d_timer_end(ps3d_pipeline* p, float* ms)
     CU(cudaEventRecord(p->timerB, p->stream));
     CU(cudaEventSynchronize(p->timerB));
     CU(cudaEventElapsedTime(ms, p->timerA, p->timerB));
+    return 0;
+}
+
+int ps3d_selftest_division(uint64_t pairs, uint64_t* rcpMismatches, uint64_t* divMismatches)
+{
+    if (!rcpMismatches || !divMismatches) return fail(PS3D_ERR_INVALID, "null argument");
+    unsigned long long a = 0, b = 0;
+    if (selftest_division(pairs, &a, &b)) return fail(PS3D_ERR_DEVICE, "self-test launch failed");
+    *rcpMismatches = a;
+    *divMismatches = b;
     return 0;
 }
 

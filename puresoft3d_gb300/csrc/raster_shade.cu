@@ -401,3 +401,57 @@ void launch_fill_u32(void* base, int width, int height, int pitchElems, uint32_t
 }
 
 }  // namespace ps3d
+
+namespace ps3d {
+
+// Self-test of the fast correctly rounded reciprocal and quotient against
+// the CUDA intrinsics: every mantissa of biased exponents [27, 227] (both
+// signs) for the reciprocal, and `pairs` hashed operand pairs with exponents
+// in [-60, 60) for the quotient.
+__device__ __forceinline__ unsigned st_hash(unsigned x)
+{
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+__global__ void k_selftest_rcp(int biasedExp, unsigned long long* bad)
+{
+    unsigned m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= (1u << 23)) return;
+    float b = __uint_as_float(((unsigned)biasedExp << 23) | m);
+    if (__float_as_uint(frcp(b)) != __float_as_uint(__frcp_rn(b))) atomicAdd(bad, 1ull);
+    if (__float_as_uint(frcp(-b)) != __float_as_uint(__frcp_rn(-b))) atomicAdd(bad, 1ull);
+}
+
+__global__ void k_selftest_div(unsigned seed, unsigned long long n, unsigned long long* bad)
+{
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    unsigned h1 = st_hash((unsigned)i * 2654435761u ^ seed), h2 = st_hash(h1 + 0x9e3779b9u), h3 = st_hash(h2 ^ 0x85ebca6bu);
+    int ea = -60 + (int)(h3 % 120u), eb = -60 + (int)((h3 >> 10) % 120u);
+    float a = __uint_as_float(((unsigned)(ea + 127) << 23) | (h1 & 0x7fffffu) | ((h3 >> 31) << 31));
+    float b = __uint_as_float(((unsigned)(eb + 127) << 23) | (h2 & 0x7fffffu) | (((h3 >> 30) & 1u) << 31));
+    if (__float_as_uint(fdiv(a, b)) != __float_as_uint(__fdiv_rn(a, b))) atomicAdd(bad, 1ull);
+}
+
+int selftest_division(unsigned long long pairs, unsigned long long* rcpBad, unsigned long long* divBad)
+{
+    unsigned long long* d = nullptr;
+    if (cudaMalloc(&d, 16) != cudaSuccess) return -1;
+    cudaMemset(d, 0, 16);
+    for (int e = 27; e <= 227; e++) k_selftest_rcp<<<(1 << 23) / 256, 256>>>(e, d);
+    if (pairs) k_selftest_div<<<(unsigned)((pairs + 255) / 256), 256>>>(12345u, pairs, d + 1);
+    unsigned long long h[2];
+    cudaError_t e = cudaMemcpy(h, d, 16, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return -1;
+    *rcpBad = h[0];
+    *divBad = h[1];
+    return 0;
+}
+
+}  // namespace ps3d

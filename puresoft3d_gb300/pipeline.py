@@ -69,6 +69,7 @@ _SIGS = {
     "ps3d_timer_end": [_c_void_p, ctypes.POINTER(ctypes.c_float)],
     "ps3d_profile_enable": [_c_void_p, _c_int],
     "ps3d_l2_scrub": [_c_void_p, _c_size_t],
+    "ps3d_selftest_division": [ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)],
     "ps3d_profile_read": [_c_void_p, ctypes.POINTER(_c_int), ctypes.POINTER(ctypes.c_double)],
 }
 
@@ -91,6 +92,17 @@ def library(path: str | None = None) -> ctypes.CDLL:
         lib.ps3d_last_error.argtypes = []
         _lib = lib
     return _lib
+
+
+def selftest_division(pairs: int = 1 << 28):
+    """(reciprocal mismatches, quotient mismatches) of the kernels' fast exact
+    division against CUDA's IEEE results."""
+    lib = library()
+    a, b = ctypes.c_uint64(), ctypes.c_uint64()
+    rc = lib.ps3d_selftest_division(pairs, ctypes.byref(a), ctypes.byref(b))
+    if rc < 0:
+        raise RuntimeError(lib.ps3d_last_error().decode())
+    return int(a.value), int(b.value)
 
 
 def exported_symbols() -> list:

@@ -103,3 +103,11 @@ def test_command_buffer_graph_replay_matches_immediate(gpu_lib):
         assert np.array_equal(col, ref[0]), i
         assert np.array_equal(dep.view(np.uint32), ref[1].view(np.uint32)), i
     cb.destroy()
+
+
+@pytest.mark.gpu
+def test_fast_division_is_correctly_rounded(gpu_lib):
+    """The kernels' FMA-corrected reciprocal and quotient equal CUDA's IEEE
+    results (every mantissa of exponents -100..100; 2^28 random pairs)."""
+    from puresoft3d_gb300.pipeline import selftest_division
+    assert selftest_division(1 << 28) == (0, 0)
