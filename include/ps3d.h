@@ -161,6 +161,12 @@ int ps3d_set_uniform(ps3d_pipeline* p, int idx, const void* data, size_t len);
 int ps3d_set_depth(ps3d_pipeline* p, int idx);
 /* PuresoftPipeline::setViewport (pipeline.cpp:207-216): rasteriser size. */
 int ps3d_set_viewport(ps3d_pipeline* p, int width, int height);
+/* Extension (no reference counterpart): a viewport of width x height -- the
+ * rasteriser size, exactly as setViewport -- whose pixel (0, 0) is written at
+ * pixel (x, y) of the colour and depth targets.  Draws into one target with
+ * different rectangles run in one device pass: many small views rendered into
+ * tiles of an atlas are one batched launch. */
+int ps3d_set_viewport_rect(ps3d_pipeline* p, int x, int y, int width, int height);
 /* PuresoftPipeline::enable / disable (pipeline.cpp:324-332). */
 int ps3d_enable(ps3d_pipeline* p, int bits);
 int ps3d_disable(ps3d_pipeline* p, int bits);

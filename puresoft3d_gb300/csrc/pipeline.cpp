@@ -85,7 +85,7 @@ struct Programme {
 struct Command {
     enum Kind { DRAW, CLEAR_DEPTH, CLEAR_COLOUR } kind;
     int depthTarget;  // -1 = default buffer
-    int vpW, vpH;
+    int vpX, vpY, vpW, vpH;
     float depthValue;
     uint32_t colourValue;
     DrawDesc desc;
@@ -141,7 +141,8 @@ void m4m4(float* d, const float* l, const float* r)
 
 struct ps3d_pipeline {
     int devW, devH;      // device size (colour buffer, default depth)
-    int W, H;            // viewport
+    int W, H;            // viewport size
+    int vpX = 0, vpY = 0;  // viewport origin in the targets (ps3d_set_viewport_rect)
     int behavior = B_UPDATE_DEPTH | B_TEST_DEPTH | B_FACE_CULLING;  // pipeline.cpp:34
     int depthTarget = -1;
     int binW = 32;
@@ -436,10 +437,10 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     int seq = (int)p->passStart.size();
     p->passStart.push_back(replayFrom);
     const Command& c0 = cmds[ps.first];
-    int W = c0.vpW, H = c0.vpH;
     Target tg;
     int rc = depth_target(p, c0.depthTarget, tg);
     if (rc) return rc;
+    int W = tg.w, H = tg.h;  // bins cover the depth target; each draw has its viewport rectangle
     std::vector<DrawDesc> dd;
     std::vector<DrawUniforms> uu;
     int nTris = 0, nvMax = 0;
@@ -452,9 +453,7 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     }
     g_retire = p->liveGraphs ? &p->retired : nullptr;
     int binW = p->binW;
-    while ((long long)((W + binW - 1) / binW) * ((H + kBinH - 1) / kBinH) > max_bins() && binW < kMaxBinW) binW *= 2;
     int binsX = (W + binW - 1) / binW, binsY = (H + kBinH - 1) / kBinH;
-    if ((long long)binsX * binsY > max_bins()) return fail(PS3D_ERR_INVALID, "viewport %dx%d has too many bins", W, H);
     if ((rc = ensure_scratch(p, nTris, nvMax, W, H, binsX, binsY, anyColour))) return rc;
     const DrawDesc* devDraws;
     const DrawUniforms* devUnis;
@@ -500,6 +499,7 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     P.pairTri = p->pairTri;
     P.pairCap = p->pairCap;
     P.sortBlocks = (p->pairCap + kSortChunk - 1) / kSortChunk;
+    P.binWindow = max_bins();
     P.binHist = p->binHist;
     P.binStart = p->binStart;
     P.binTri = p->binTri;
@@ -560,9 +560,7 @@ int plan_commands(const std::vector<Command>& cmds, size_t from, PassFn onPass, 
             break;
         }
         size_t k = j;
-        while (k < n && cmds[k].kind == Command::DRAW && cmds[k].depthTarget == cmds[j].depthTarget &&
-               cmds[k].vpW == cmds[j].vpW && cmds[k].vpH == cmds[j].vpH)
-            k++;
+        while (k < n && cmds[k].kind == Command::DRAW && cmds[k].depthTarget == cmds[j].depthTarget) k++;
         if (ps.clearDepth && depthClearTarget != cmds[j].depthTarget) {
             if ((rc = onFill(depthClearTarget, ps.depthValue, 0u))) return rc;
             ps.clearDepth = false;
@@ -966,10 +964,16 @@ int ps3d_set_depth(ps3d_pipeline* p, int idx)
     return 0;
 }
 
-int ps3d_set_viewport(ps3d_pipeline* p, int width, int height)
+int ps3d_set_viewport(ps3d_pipeline* p, int width, int height) { return ps3d_set_viewport_rect(p, 0, 0, width, height); }
+
+int ps3d_set_viewport_rect(ps3d_pipeline* p, int x, int y, int width, int height)
 {
     if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
-    if (width <= 0 || height <= 0 || width > 32767 || height > 32767) return fail(PS3D_ERR_INVALID, "bad viewport");
+    if (width <= 0 || height <= 0 || width > 32767 || height > 32767 || x < 0 || y < 0 || x + width > 32767 ||
+        y + height > 32767)
+        return fail(PS3D_ERR_INVALID, "bad viewport");
+    p->vpX = x;
+    p->vpY = y;
     p->W = width;
     p->H = height;
     return 0;
@@ -1024,6 +1028,8 @@ int ps3d_draw(ps3d_pipeline* p, int vao)
     memset(&c, 0, sizeof c);
     c.kind = Command::DRAW;
     c.depthTarget = p->depthTarget;
+    c.vpX = p->vpX;
+    c.vpY = p->vpY;
     c.vpW = p->W;
     c.vpH = p->H;
     DrawDesc& d = c.desc;
@@ -1051,13 +1057,18 @@ int ps3d_draw(ps3d_pipeline* p, int vao)
         }
     }
     d.triCount = (int)(minCount / 3);
+    d.vpX = p->vpX;
+    d.vpY = p->vpY;
+    d.vpW = p->W;
+    d.vpH = p->H;
     int rc = snapshot_uniforms(p, c.uni);
     if (rc) return rc;
     Target tg;
     if ((rc = depth_target(p, p->depthTarget, tg))) return rc;
-    if (tg.w < p->W || tg.h < p->H) return fail(PS3D_ERR_INVALID, "the depth target is smaller than the viewport");
-    if ((d.flags & F_COLOUR) && (p->devW < p->W || p->devH < p->H))
-        return fail(PS3D_ERR_INVALID, "the colour buffer is smaller than the viewport");
+    if (tg.w < p->vpX + p->W || tg.h < p->vpY + p->H)
+        return fail(PS3D_ERR_INVALID, "the viewport rectangle is not inside the depth target");
+    if ((d.flags & F_COLOUR) && (p->devW < p->vpX + p->W || p->devH < p->vpY + p->H))
+        return fail(PS3D_ERR_INVALID, "the viewport rectangle is not inside the colour buffer");
     (p->recording ? p->recording->cmds : p->pending).push_back(c);
     p->stats.draws++;
     return 0;

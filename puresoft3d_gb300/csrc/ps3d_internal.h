@@ -54,7 +54,7 @@ struct DrawDesc {
     int nv;      // varying floats per vertex carried by this draw's interpolation stage
     int flags;   // behaviour bits | F_COLOUR
     int uni;     // index into the batch's DrawUniforms
-    int pad;
+    int vpX, vpY, vpW, vpH;  // viewport: rasteriser size vpW x vpH, its pixel (0,0) at target pixel (vpX, vpY)
     const uint8_t* vbo[kVboSlots];
     int stride[kVboSlots];
 };
@@ -72,7 +72,7 @@ static_assert(sizeof(TriRaster) == 64, "TriRaster must be 64 bytes");
 
 // Kernel parameters of one device pass (a run of draws into one target).
 struct PassParams {
-    int W, H;                 // viewport = rasteriser size
+    int W, H;                 // target (depth buffer) size; each draw has its own viewport rectangle
     int binW, binsX, binsY;   // bins of kBinH x binW pixels
     int nTris, nDraws;
     const DrawDesc* draws;
@@ -88,6 +88,7 @@ struct PassParams {
     int* pairTri;
     int pairCap;              // capacity of pairKey / pairTri / binTri
     int sortBlocks;           // pairCap / kSortChunk
+    int binWindow;            // bins counted per shared-memory window in the sort
     int* binHist;             // [sortBlock][bin] counts, then per-bin prefixes over blocks
     int* binStart;            // first position of each bin's list; [nBins] = total
     int* binTri;              // triangles of each bin, in submission order

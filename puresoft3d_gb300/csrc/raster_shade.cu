@@ -56,6 +56,7 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(PassParams P)
     __shared__ float sZmin[4][kSlots];           // per span and quarter: min z over its pixels
     __shared__ __align__(16) TriRaster sTri[kChunk];
     __shared__ int sTid[kChunk];
+    __shared__ short sOx[kChunk], sOy[kChunk], sLw[kChunk];  // each triangle's viewport origin and width
     __shared__ int sSlot[kSlots];                // (row << 8) | triangle slot
     __shared__ SpanRec sRec[kSlots];
     __shared__ unsigned sMask[4][kBinH][kSlots / 32];
@@ -110,8 +111,13 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(PassParams P)
 #pragma unroll
             for (int k = 0; k < 4; k++) dst[k] = rec[k];
             sTid[tid] = recTid;
-            r0 = max((int)sTri[tid].firstRow - y0, 0);
-            int r1 = min((int)sTri[tid].lastRow - y0, rows - 1);
+            const DrawDesc& dd = P.draws[sTri[tid].draw];
+            int oy = dd.vpY;
+            sOx[tid] = (short)dd.vpX;
+            sOy[tid] = (short)oy;
+            sLw[tid] = (short)dd.vpW;
+            r0 = max((int)sTri[tid].firstRow + oy - y0, 0);
+            int r1 = min((int)sTri[tid].lastRow + oy - y0, rows - 1);
             if (r0 <= r1) cnt = r1 - r0 + 1;
         }
         recTid = nextIdx;  // prefetch the next chunk while this one is processed
@@ -152,16 +158,17 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(PassParams P)
             const int nSlots = min(kSlots, total - round);
             if (tid < nSlots) {
                 const int s2 = tid;
-                int code = sSlot[s2], j = code & 0xff, r = code >> 8, y = y0 + r;
+                int code = sSlot[s2], j = code & 0xff, r = code >> 8;
+                const int ox = sOx[j], yl = y0 + r - sOy[j];  // the draw's rasteriser row
                 const TriRaster& t = sTri[j];
                 Span sp;
-                if (span_row(t, y, P.W, sp)) {
-                    int xs = max(sp.leftClamped, x0), xe = min(sp.rightClamped, x0 + cols - 1);
+                if (span_row(t, yl, sLw[j], sp)) {
+                    int xs = max(sp.leftClamped + ox, x0), xe = min(sp.rightClamped + ox, x0 + cols - 1);
                     if (xs <= xe) {
                         SpanZ z;
-                        span_z(t, sp, y, z);
+                        span_z(t, sp, yl, z);
                         float cf2 = z.cf2, pz = z.pz;
-                        for (int x = sp.leftClamped; x < xs; x++) {
+                        for (int x = sp.leftClamped + ox; x < xs; x++) {
                             cf2 = fadd(cf2, z.cf2Step);
                             pz = fadd(pz, z.pzStep);
                         }
@@ -322,34 +329,35 @@ __global__ void __launch_bounds__(256) k_shade(PassParams P)
     }
     const DrawDesc& d = P.draws[t.draw];
     const DrawUniforms& U = P.unis[d.uni];
+    const int xl = x - d.vpX, yl = y - d.vpY;  // the draw's rasteriser coordinates
     Span s;
-    span_row(t, y, P.W, s);
+    span_row(t, yl, d.vpW, s);
     SpanZ z;
-    span_z(t, s, y, z);
+    span_z(t, s, yl, z);
     const float* vary = P.vary + (size_t)w * 3 * P.nvMax;
     uint32_t bgra;
     switch (d.fp) {
     case FP_LIT2: {
         float in[16];
-        fragment_varyings<16>(t, vary, P.nvMax, s, z, x, in);
+        fragment_varyings<16>(t, vary, P.nvMax, s, z, xl, in);
         bgra = shade_lit2(U, in);
         break;
     }
     case FP_LIT1: {
         float in[9];
-        fragment_varyings<9>(t, vary, P.nvMax, s, z, x, in);
+        fragment_varyings<9>(t, vary, P.nvMax, s, z, xl, in);
         bgra = shade_lit1(U, in);
         break;
     }
     case FP_LIT3: {
         float in[9];
-        fragment_varyings<9>(t, vary, P.nvMax, s, z, x, in);
+        fragment_varyings<9>(t, vary, P.nvMax, s, z, xl, in);
         bgra = shade_lit3(U, in);
         break;
     }
     default: {  // FP_DEF01
         float in[9];
-        fragment_varyings<9>(t, vary, P.nvMax, s, z, x, in);
+        fragment_varyings<9>(t, vary, P.nvMax, s, z, xl, in);
         bgra = shade_def01(U, in);
         break;
     }

@@ -154,7 +154,7 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float
     for (int v = 0; v < 3; v++)
         if (pos[v][2] < -1.0f || pos[v][2] > 1.0f) keep = false;  // drawvao.cpp:51-56
 
-    const int W = P.W, H = P.H, halfW = W / 2, halfH = H / 2;
+    const int W = d.vpW, H = d.vpH, halfW = W / 2, halfH = H / 2;  // the draw's rasteriser size
 #pragma unroll
     for (int v = 0; v < 3; v++) {
         tr.vx[v] = fadd(fmul((float)halfW, pos[v][0]), (float)halfW);  // rasterizer.cpp:73-77
@@ -227,11 +227,11 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float
             float xmax = fmaxf(vx[0], fmaxf(vx[1], vx[2])) + ext + 2.0f;
             int colLo = xmin < 0.0f ? 0 : (xmin > (float)W ? W : (int)xmin);
             int colHi = xmax > (float)(W - 1) ? W - 1 : (xmax < 0.0f ? -1 : (int)xmax);
-            if (colLo <= colHi) {
-                bx0 = colLo / P.binW;
-                bx1 = colHi / P.binW;
-                by0 = firstRow / kBinH;
-                by1 = lastRow / kBinH;
+            if (colLo <= colHi) {  // bins are in target pixels: offset by the viewport origin
+                bx0 = (colLo + d.vpX) / P.binW;
+                bx1 = (colHi + d.vpX) / P.binW;
+                by0 = (firstRow + d.vpY) / kBinH;
+                by1 = (lastRow + d.vpY) / kBinH;
                 count = (bx1 - bx0 + 1) * (by1 - by0 + 1);
             }
         }
@@ -422,39 +422,66 @@ __global__ void __launch_bounds__(kSortThreads) k_hist(PassParams P)
     if (b >= sort_blocks(P)) return;
     int nBins = P.binsX * P.binsY;
     int base = b * kSortChunk, n = min(kSortChunk, total - base);
-    for (int i = threadIdx.x; i < nBins; i += kSortThreads) cnt[i] = 0;
     for (int i = threadIdx.x; i < n; i += kSortThreads) keys[i] = P.pairKey[base + i];
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        int lane = threadIdx.x;
-        for (int i0 = 0; i0 < n; i0 += 32) {
-            int i = i0 + lane;
-            int key = i < n ? keys[i] : -1 - lane;
-            unsigned peers = __match_any_sync(0xffffffffu, key);
-            if (i < n && lane == __ffs(peers) - 1) cnt[key] += __popc(peers);
-            __syncwarp();
+    // bins are counted in windows of P.binWindow (one shared counter each)
+    for (int lo = 0; lo < nBins; lo += P.binWindow) {
+        int nw = min(P.binWindow, nBins - lo);
+        __syncthreads();
+        for (int i = threadIdx.x; i < nw; i += kSortThreads) cnt[i] = 0;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            int lane = threadIdx.x;
+            for (int i0 = 0; i0 < n; i0 += 32) {
+                int i = i0 + lane;
+                int key = i < n ? keys[i] - lo : -1;
+                bool in = i < n && key >= 0 && key < nw;
+                if (!in) key = -1 - lane;
+                unsigned peers = __match_any_sync(0xffffffffu, key);
+                if (in && lane == __ffs(peers) - 1) cnt[key] += __popc(peers);
+                __syncwarp();
+            }
         }
+        __syncthreads();
+        for (int i = threadIdx.x; i < nw; i += kSortThreads) P.binHist[(size_t)b * nBins + lo + i] = cnt[i];
     }
-    __syncthreads();
-    for (int i = threadIdx.x; i < nBins; i += kSortThreads) P.binHist[(size_t)b * nBins + i] = cnt[i];
 }
 
 // Per bin: exclusive prefix of its counts over the sort blocks (in place) and
-// the bin's total into binStart[bin].
-__global__ void k_colscan(PassParams P)
+// the bin's total into binStart[bin].  A block takes 32 consecutive bins
+// (lane = bin, so every row read is one coalesced 128-byte line); its 8 warps
+// take contiguous runs of sort blocks, add their runs, exchange run totals,
+// then write the prefixes.
+constexpr int kColScanWarps = 8;
+
+__global__ void __launch_bounds__(32 * kColScanWarps) k_colscan(PassParams P)
 {
+    __shared__ int runTotal[kColScanWarps][32];
     if (P.status[0]) return;
     int nBins = P.binsX * P.binsY;
-    int bin = blockIdx.x * blockDim.x + threadIdx.x;
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int bin = blockIdx.x * 32 + lane;
+    int nb = sort_blocks(P);
+    int per = (nb + kColScanWarps - 1) / kColScanWarps;
+    int b0 = warp * per, b1 = min(nb, b0 + per);
+    int sum = 0;
+    if (bin < nBins)
+        for (int b = b0; b < b1; b++) sum += P.binHist[(size_t)b * nBins + bin];
+    runTotal[warp][lane] = sum;
+    __syncthreads();
+    int run = 0, total = 0;
+    for (int w = 0; w < kColScanWarps; w++) {
+        int v = runTotal[w][lane];
+        if (w < warp) run += v;
+        total += v;
+    }
     if (bin >= nBins) return;
-    int nb = sort_blocks(P), run = 0;
-    for (int b = 0; b < nb; b++) {
+    for (int b = b0; b < b1; b++) {
         int* h = P.binHist + (size_t)b * nBins + bin;
         int v = *h;
         *h = run;
         run += v;
     }
-    P.binStart[bin] = run;
+    if (warp == 0) P.binStart[bin] = total;
 }
 
 // Exclusive scan of the bin totals in one block; binStart[nBins] = total.
@@ -496,27 +523,33 @@ __global__ void __launch_bounds__(kSortThreads) k_scatter(PassParams P)
     if (b >= sort_blocks(P)) return;
     int nBins = P.binsX * P.binsY;
     int base = b * kSortChunk, n = min(kSortChunk, total - base);
-    for (int i = threadIdx.x; i < nBins; i += kSortThreads)
-        cnt[i] = P.binStart[i] + P.binHist[(size_t)b * nBins + i];
     for (int i = threadIdx.x; i < n; i += kSortThreads) {
         keys[i] = P.pairKey[base + i];
         tris[i] = P.pairTri[base + i];
     }
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        int lane = threadIdx.x;
-        unsigned lt = (1u << lane) - 1u;
-        for (int i0 = 0; i0 < n; i0 += 32) {
-            int i = i0 + lane;
-            int key = i < n ? keys[i] : -1 - lane;
-            unsigned peers = __match_any_sync(0xffffffffu, key);
-            int pos = i < n ? cnt[key] + __popc(peers & lt) : 0;
-            __syncwarp();
-            if (i < n) {
-                P.binTri[pos] = tris[i];
-                if (lane == __ffs(peers) - 1) cnt[key] += __popc(peers);
+    for (int lo = 0; lo < nBins; lo += P.binWindow) {
+        int nw = min(P.binWindow, nBins - lo);
+        __syncthreads();
+        for (int i = threadIdx.x; i < nw; i += kSortThreads)
+            cnt[i] = P.binStart[lo + i] + P.binHist[(size_t)b * nBins + lo + i];
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            int lane = threadIdx.x;
+            unsigned lt = (1u << lane) - 1u;
+            for (int i0 = 0; i0 < n; i0 += 32) {
+                int i = i0 + lane;
+                int key = i < n ? keys[i] - lo : -1;
+                bool in = i < n && key >= 0 && key < nw;
+                if (!in) key = -1 - lane;
+                unsigned peers = __match_any_sync(0xffffffffu, key);
+                int pos = in ? cnt[key] + __popc(peers & lt) : 0;
+                __syncwarp();
+                if (in) {
+                    P.binTri[pos] = tris[i];
+                    if (lane == __ffs(peers) - 1) cnt[key] += __popc(peers);
+                }
+                __syncwarp();
             }
-            __syncwarp();
         }
     }
 }
@@ -565,12 +598,12 @@ void launch_setup_and_bin(const PassParams& P, int* scanTmp, cudaStream_t s, int
     k_emit<<<ceil_div(P.nTris, 256), 256, 0, s>>>(P);
     pr->end(s);
     launches++;
-    size_t smem = (size_t)nBins * sizeof(int);
+    size_t smem = (size_t)min(nBins, P.binWindow) * sizeof(int);
     pr->begin(K_HIST, s);
     k_hist<<<P.sortBlocks, kSortThreads, smem, s>>>(P);
     pr->end(s);
     pr->begin(K_SCAN, s);
-    k_colscan<<<ceil_div(nBins, 256), 256, 0, s>>>(P);
+    k_colscan<<<ceil_div(nBins, 32), 32 * kColScanWarps, 0, s>>>(P);
     k_binscan<<<1, 1024, 0, s>>>(P);
     pr->end(s);
     pr->begin(K_SCATTER, s);

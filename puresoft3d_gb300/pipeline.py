@@ -47,6 +47,7 @@ _SIGS = {
     "ps3d_set_uniform": [_c_void_p, _c_int, _c_void_p, _c_size_t],
     "ps3d_set_depth": [_c_void_p, _c_int],
     "ps3d_set_viewport": [_c_void_p, _c_int, _c_int],
+    "ps3d_set_viewport_rect": [_c_void_p, _c_int, _c_int, _c_int, _c_int],
     "ps3d_enable": [_c_void_p, _c_int],
     "ps3d_disable": [_c_void_p, _c_int],
     "ps3d_clear_depth": [_c_void_p, ctypes.c_float],
@@ -208,6 +209,9 @@ class PuresoftPipeline:
 
     def setViewport(self, w, h):
         self._check(self.lib.ps3d_set_viewport(self.h, w, h))
+
+    def setViewportRect(self, x, y, w, h):
+        self._check(self.lib.ps3d_set_viewport_rect(self.h, x, y, w, h))
 
     def enable(self, bits):
         self._check(self.lib.ps3d_enable(self.h, bits))

@@ -11,7 +11,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def declared():
     names = set()
-    for h in os.listdir(os.path.join(ROOT, "include")):
+    for h in [f for f in os.listdir(os.path.join(ROOT, "include")) if f.endswith(".h")]:
         txt = open(os.path.join(ROOT, "include", h)).read()
         names |= set(re.findall(r"^\s*(?:const\s+)?\w[\w\s\*]*?\b(ps3d_\w+)\s*\(", txt, re.M))
     return names
