@@ -191,6 +191,10 @@ int ps3d_finish(ps3d_pipeline* p);
 int ps3d_read_colour(ps3d_pipeline* p, void* out);
 /* Read-back of the default depth buffer: scanline*height bytes. */
 int ps3d_read_depth(ps3d_pipeline* p, void* out);
+/* Records a copy of the colour buffer (width*height*4 bytes, BGRA8 top-down)
+ * to device memory at devDst, ordered after the draws recorded before it
+ * (like a read-back, but asynchronous and on the device). */
+int ps3d_read_colour_device(ps3d_pipeline* p, void* devDst);
 /* Device address of the colour buffer. */
 int ps3d_colour_device_ptr(ps3d_pipeline* p, void** out);
 /* The pipeline's CUDA stream (cudaStream_t). */

@@ -83,7 +83,8 @@ struct Programme {
 
 // one recorded command
 struct Command {
-    enum Kind { DRAW, CLEAR_DEPTH, CLEAR_COLOUR } kind;
+    enum Kind { DRAW, CLEAR_DEPTH, CLEAR_COLOUR, COPY_COLOUR } kind;
+    void* copyDst;    // COPY_COLOUR: device destination of the colour buffer
     int depthTarget;  // -1 = default buffer
     int vpX, vpY, vpW, vpH;
     float depthValue;
@@ -532,8 +533,8 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
 // Splits cmds[from..] into passes (each run of draws into one target, with
 // the clears in front of it) and hands them to `onPass`; clears that cannot
 // fuse go to `onFill` (target -3 = colour).
-template <class PassFn, class FillFn>
-int plan_commands(const std::vector<Command>& cmds, size_t from, PassFn onPass, FillFn onFill)
+template <class PassFn, class FillFn, class CopyFn>
+int plan_commands(const std::vector<Command>& cmds, size_t from, PassFn onPass, FillFn onFill, CopyFn onCopy)
 {
     size_t i = from, n = cmds.size();
     int rc;
@@ -542,6 +543,13 @@ int plan_commands(const std::vector<Command>& cmds, size_t from, PassFn onPass, 
         size_t j = i;
         int depthClearTarget = -2;
         for (; j < n && cmds[j].kind != Command::DRAW; j++) {
+            if (cmds[j].kind == Command::COPY_COLOUR) {  // in order: clears gathered so far first
+                if (ps.clearDepth && (rc = onFill(depthClearTarget, ps.depthValue, 0u))) return rc;
+                if (ps.clearColour && (rc = onFill(-3, 0.0f, ps.colourValue))) return rc;
+                ps.clearDepth = ps.clearColour = false;
+                if ((rc = onCopy(cmds[j].copyDst))) return rc;
+                continue;
+            }
             if (cmds[j].kind == Command::CLEAR_DEPTH) {
                 if (ps.clearDepth && depthClearTarget != cmds[j].depthTarget &&
                     (rc = onFill(depthClearTarget, ps.depthValue, 0u)))
@@ -577,7 +585,11 @@ int launch_cmds(ps3d_pipeline* p, const std::vector<Command>& cmds, size_t from)
 {
     return plan_commands(
         cmds, from, [&](const Pass& ps, size_t start) { return run_pass(p, cmds, ps, start); },
-        [&](int target, float v, uint32_t c) { return target == -3 ? fill_colour(p, c) : fill_depth(p, target, v); });
+        [&](int target, float v, uint32_t c) { return target == -3 ? fill_colour(p, c) : fill_depth(p, target, v); },
+        [&](void* dst) -> int {
+            CU(cudaMemcpyAsync(dst, p->colour, (size_t)p->devW * 4 * p->devH, cudaMemcpyDeviceToDevice, p->stream));
+            return 0;
+        });
 }
 
 int launch_range(ps3d_pipeline* p, size_t from) { return launch_cmds(p, p->launched, from); }
@@ -1106,6 +1118,18 @@ int ps3d_read_depth(ps3d_pipeline* p, void* out)
     return 0;
 }
 
+int ps3d_read_colour_device(ps3d_pipeline* p, void* devDst)
+{
+    if (!p || !devDst) return fail(PS3D_ERR_INVALID, "null argument");
+    Command c;
+    memset(&c, 0, sizeof c);
+    c.kind = Command::COPY_COLOUR;
+    c.depthTarget = p->depthTarget;
+    c.copyDst = devDst;
+    (p->recording ? p->recording->cmds : p->pending).push_back(c);
+    return 0;
+}
+
 int ps3d_colour_device_ptr(ps3d_pipeline* p, void** out)
 {
     if (!p || !out) return fail(PS3D_ERR_INVALID, "null argument");
@@ -1170,7 +1194,7 @@ int ps3d_cmdbuf_end(ps3d_pipeline* p, ps3d_cmdbuf** out)
             cb->hUnis.insert(cb->hUnis.end(), uu.begin(), uu.end());
             return 0;
         },
-        [&](int, float, uint32_t) { return 0; });
+        [&](int, float, uint32_t) { return 0; }, [&](void*) { return 0; });
     size_t n = std::max<size_t>(cb->hDraws.size(), 1);
     bool ok = cudaMalloc((void**)&cb->dDraws, n * sizeof(DrawDesc)) == cudaSuccess &&
               cudaMalloc((void**)&cb->dUnis, n * sizeof(DrawUniforms)) == cudaSuccess &&

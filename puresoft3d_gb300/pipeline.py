@@ -58,6 +58,7 @@ _SIGS = {
     "ps3d_read_colour": [_c_void_p, _c_void_p],
     "ps3d_read_depth": [_c_void_p, _c_void_p],
     "ps3d_colour_device_ptr": [_c_void_p, ctypes.POINTER(_c_void_p)],
+    "ps3d_read_colour_device": [_c_void_p, _c_void_p],
     "ps3d_get_stream": [_c_void_p, ctypes.POINTER(_c_void_p)],
     "ps3d_set_fragment_counting": [_c_void_p, _c_int],
     "ps3d_stats": [_c_void_p, ctypes.POINTER(Stats)],
@@ -239,6 +240,22 @@ class PuresoftPipeline:
         if out is None:
             out = np.empty((self.height, self.width, 4), dtype=np.uint8)
         self._check(self.lib.ps3d_read_colour(self.h, out.ctypes.data))
+        return out
+
+    def readColourDevice(self, dev_ptr: int):
+        self._check(self.lib.ps3d_read_colour_device(self.h, dev_ptr))
+
+    def textureDevicePtr(self, idx) -> int:
+        v = ctypes.c_void_p()
+        self._check(self.lib.ps3d_texture_device_ptr(self.h, idx, ctypes.byref(v)))
+        return v.value
+
+    def readDepth(self) -> np.ndarray:
+        """The default depth buffer, (height, scanline floats)."""
+        scan = int(self.width / 4.0 + 0.5) * 4
+        scan = max(scan, (self.width + 3) // 4 * 4)
+        out = np.empty((self.height, scan), dtype=np.float32)
+        self._check(self.lib.ps3d_read_depth(self.h, out.ctypes.data))
         return out
 
     def colourDevicePtr(self) -> int:

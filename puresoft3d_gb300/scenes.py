@@ -569,6 +569,81 @@ def scene_c3(seed: int = 1237, width: int = 3840, height: int = 2160, meshes: in
                  {"triangles": tri_total, "depth_texture": depth, "draws": meshes})
 
 
+def mesh_with_triangles(n: int, kind: int) -> Dict[str, np.ndarray]:
+    """A sphere / torus / box tessellated to roughly n triangles."""
+    if kind == 0:
+        s_ = max(3, int(round(math.sqrt(n / 4.0))))
+        return uv_sphere(2 * s_, s_)
+    if kind == 1:
+        b_ = max(3, int(round(math.sqrt(n / 4.0))))
+        return torus(2 * b_, b_)
+    return box(max(1, int(round(math.sqrt(n / 12.0)))))
+
+
+def scene_c4(seed: int = 1238, views: int = 4096, size: int = 128, tex_size: int = 256,
+             tri_min: int = 100, tri_max: int = 5000):
+    """Config 4: `views` independent size x size views, each with its own
+    seeded mesh (sphere / torus / box, triangles log-uniform in
+    [tri_min, tri_max]), its own orbit camera (azimuth U[0, 2pi), elevation
+    U[-60, 60] deg, distance U[2.5, 4]) and its own tex_size^2 texture; LIT1.
+
+    Returns (batched, plain): `batched` renders every view in one pass into
+    tiles of a square atlas (ps3d_set_viewport_rect), `plain` is the same
+    setup with one frame per view (info["view_frames"]) for a size x size
+    pipeline.  View v's tile origin is info["origins"][v]."""
+    rng = np.random.default_rng(seed)
+    cols = int(math.ceil(math.sqrt(views)))
+    rows_ = int(math.ceil(views / cols))
+    b = _Builder()
+    prog = b.programme(VP_DEF01, IP_DEF01, FP_LIT1)
+    light = np.array([0.3, 0.8, 0.5])
+    light /= np.linalg.norm(light)
+    P = perspective(0.5, 20.0, 1.0, math.radians(50.0))
+    yy, xx = np.mgrid[0:tex_size, 0:tex_size]
+    per_view = []
+    tri_total = 0
+    for v in range(views):
+        n = int(round(math.exp(rng.uniform(math.log(tri_min), math.log(tri_max)))))
+        kind = int(rng.integers(0, 3))
+        mesh = mesh_with_triangles(n, kind)
+        tri_total += mesh_triangles(mesh)
+        cells = int(rng.integers(2, 9))
+        base = rng.integers(30, 226, size=(2, 3))
+        chk = ((yy * cells // tex_size) + (xx * cells // tex_size)) % 2
+        img = np.empty((tex_size, tex_size, 4), dtype=np.uint8)
+        img[..., :3] = base[chk]
+        img[..., 3] = 255
+        tex = b.texture(img)
+        vao = b.vao(mesh, slots=(0, 3, 4))
+        az = rng.uniform(0, 2 * math.pi)
+        el = math.radians(rng.uniform(-60, 60))
+        dist = rng.uniform(2.5, 4.0)
+        eye = dist * np.array([math.cos(el) * math.sin(az), math.sin(el), math.cos(el) * math.cos(az)])
+        V = look_at(eye, (0, 0, 0), (0, 1, 0))
+        R = _random_rotation(rng)
+        per_view.append((vao, tex, col_major(P @ V), col_major(R), eye))
+    origins = [((v % cols) * size, (v // cols) * size) for v in range(views)]
+    common = [("useProgramme", prog), ("setUniform", 7, vec4(*light))]
+
+    def view_ops(v):
+        vao, tex, PV, R, eye = per_view[v]
+        return [("setUniform", 3, PV), ("setUniform", 4, R), ("setUniform", 5, R),
+                ("setUniform", 8, vec4(*eye, 1.0)), ("setUniform", 9, _u(np.array([tex], dtype=np.int32))),
+                ("drawVAO", vao)]
+
+    frame = [("clearDepth", 1.0), ("clearColour", 0xFF000000)] + common
+    for v in range(views):
+        frame.append(("setViewportRect", origins[v][0], origins[v][1], size, size))
+        frame += view_ops(v)
+    batched = Scene("c4", cols * size, rows_ * size, b.setup, frame,
+                    {"triangles": tri_total, "views": views, "view_size": size, "origins": origins,
+                     "depth_texture": None})
+    view_frames = [[("clearDepth", 1.0), ("clearColour", 0xFF000000)] + common + view_ops(v) for v in range(views)]
+    plain = Scene("c4_plain", size, size, b.setup, [], {"triangles": tri_total, "views": views,
+                                                        "view_size": size, "view_frames": view_frames})
+    return batched, plain
+
+
 # --------------------------------------------------------------------------
 # replay
 
@@ -598,6 +673,11 @@ def replay_setup(scene: Scene, pipe) -> Dict[str, List[int]]:
 
 def replay_frame(scene: Scene, pipe) -> None:
     for op in scene.frame:
+        getattr(pipe, op[0])(*op[1:])
+
+
+def replay_ops(ops, pipe) -> None:
+    for op in ops:
         getattr(pipe, op[0])(*op[1:])
 
 
