@@ -186,6 +186,34 @@ int ps3d_flush(ps3d_pipeline* p);
  * drawvao.cpp:121-132). */
 int ps3d_finish(ps3d_pipeline* p);
 
+/* ps3d_finish for callers that must not allocate device memory; it has no
+ * counterpart in the reference, whose CPU pipeline allocates no device memory
+ * at all.  Who needs it: a real-time render thread that may not block in
+ * cudaMalloc/cudaFree (both can synchronise the whole device), a process whose
+ * device memory is fully committed up front, a service that must not grow
+ * after admission control has accounted for its memory.
+ *
+ * The recorded passes run the same kernels with the same results as
+ * ps3d_finish, but take all their scratch from one fixed 16 MiB device array
+ * (a file-scope __device__ array, carved afresh per pass); the call makes no
+ * cudaMalloc, cudaFree or other allocating call.  Limits:
+ *   - a pass needs its triangle records, varyings, descriptors and (when it
+ *     writes colour) 4 bytes per target pixel to fit in 16 MiB with room for
+ *     at least 4096 bin pairs, and has at most 1024 draws.  Otherwise the call
+ *     returns PS3D_ERR_RANGE before anything runs and the commands stay
+ *     recorded (ps3d_finish renders them);
+ *   - if a pass finds more bin pairs than fit, it and the passes after it do
+ *     nothing and the call returns PS3D_ERR_NOMEM; ps3d_finish then completes
+ *     the frame (and may allocate).
+ * First call: the array's device address is looked up once per device
+ * (cudaGetSymbolAddress, with that device current); make one call with
+ * nothing recorded, before any stream capture starts, to do this set-up.
+ * Overlap: every pipeline of the process shares the array, so two calls
+ * whose work overlapped on the device would race; calls are serialised by a
+ * process-wide lock and each returns only after its work has completed.
+ * Flushed work (ps3d_flush) must be finished with ps3d_finish first. */
+int ps3d_finish_noalloc(ps3d_pipeline* p);
+
 /* Read-back of the colour buffer: width*height*4 bytes, BGRA8, top-down
  * (memory row = H-1-y, the display FBO layout, pipeline.cpp:48). */
 int ps3d_read_colour(ps3d_pipeline* p, void* out);

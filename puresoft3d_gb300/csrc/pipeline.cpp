@@ -22,6 +22,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <algorithm>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -1377,3 +1378,263 @@ int ps3d_profile_read(ps3d_pipeline* p, int* launches, double* ms)
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// ps3d_finish_noalloc: ps3d_finish for callers that must not allocate device
+// memory -- a real-time render thread that may not block in cudaMalloc or
+// cudaFree (both can synchronise the whole device), a process whose device
+// memory is fully committed up front, or a service that must not grow after
+// admission control has accounted for it.  The recorded passes take their
+// scratch (descriptors, triangle records, varyings, bin lists, histograms,
+// winner buffer) from one fixed array instead of the pipeline's growable
+// buffers, and run the same kernels with the same results.
+
+namespace {
+
+// The fixed scratch: 16 MiB per device, carved afresh for every pass.  It
+// holds, for example, a 1024x1024 colour pass of ~50k triangles and ~700k
+// bin pairs, or a 1920x1080 pass of ~20k triangles.
+constexpr size_t kNoAllocBytes = (size_t)16 << 20;
+constexpr int kNoAllocMaxDraws = 1024;  // draws per pass (host staging below)
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocBytes];
+
+std::mutex g_noallocLock;                       // one caller at a time: they share the array
+unsigned char* g_noallocPtr[kNoAllocMaxDevices];  // its address per device, looked up once
+DrawDesc g_noallocDraws[kNoAllocMaxDraws];      // a pass's descriptors, staged on the host
+DrawUniforms g_noallocUnis[kNoAllocMaxDraws];
+
+// Byte offsets of one pass's buffers in the array, each 256-byte aligned.
+struct NoAllocLayout {
+    size_t draws, unis, tris, vary, pairCount, rect, pairOffset, scanTmp, winner, binStart, binHist, pairKey,
+        pairTri, binTri;
+};
+
+size_t noalloc_layout(NoAllocLayout& L, int nd, int nTris, int nv, int W, int H, bool colour, size_t nBins,
+                      int pairCap)
+{
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t at = off;
+        off = (off + bytes + 255) & ~(size_t)255;
+        return at;
+    };
+    size_t sortBlocks = ((size_t)pairCap + kSortChunk - 1) / kSortChunk;
+    size_t scanN = std::max<size_t>((size_t)nTris, nBins * sortBlocks);
+    if (scanN > 0x7fffffff) return (size_t)-1;
+    L.draws = take((size_t)nd * sizeof(DrawDesc));
+    L.unis = take((size_t)nd * sizeof(DrawUniforms));
+    L.tris = take((size_t)nTris * sizeof(TriRaster));
+    L.vary = take((size_t)nTris * 3 * std::max(nv, 1) * sizeof(float));
+    L.pairCount = take((size_t)nTris * sizeof(int));
+    L.rect = take((size_t)nTris * sizeof(int4));
+    L.pairOffset = take(((size_t)nTris + 1) * sizeof(int));
+    L.scanTmp = take(((size_t)scan_block_sums_needed((int)scanN) + 1) * sizeof(int));
+    L.winner = colour ? take((size_t)W * H * sizeof(int)) : 0;
+    L.binStart = take((nBins + 1) * sizeof(int));
+    L.binHist = take((nBins * sortBlocks + 1) * sizeof(int));
+    L.pairKey = take((size_t)pairCap * sizeof(int));
+    L.pairTri = take((size_t)pairCap * sizeof(int));
+    L.binTri = take((size_t)pairCap * sizeof(int));
+    return off;
+}
+
+// A pass's shape: its draws staged in g_noallocDraws/g_noallocUnis.
+struct NoAllocPass {
+    Target tg;
+    int nd = 0, nTris = 0, nvMax = 0;
+    bool anyColour = false;
+    int binsX = 0, binsY = 0;
+    size_t nBins = 0;
+    int pairCap = 0;  // largest multiple of the sort chunk that fits, 0 if none does
+};
+
+int noalloc_shape(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps, NoAllocPass& s, bool stage)
+{
+    int rc = depth_target(p, cmds[ps.first].depthTarget, s.tg);
+    if (rc) return rc;
+    for (size_t i = ps.first; i < ps.last; i++) {
+        const DrawDesc& d = cmds[i].desc;
+        if (d.triCount == 0) continue;
+        if (s.nd == kNoAllocMaxDraws)
+            return fail(PS3D_ERR_RANGE, "ps3d_finish_noalloc: a pass has more than %d draws", kNoAllocMaxDraws);
+        if (stage) {
+            g_noallocDraws[s.nd] = d;
+            g_noallocDraws[s.nd].triBase = s.nTris;
+            g_noallocDraws[s.nd].uni = s.nd;
+            g_noallocUnis[s.nd] = cmds[i].uni;
+        }
+        s.nd++;
+        s.nTris += d.triCount;
+        s.nvMax = std::max(s.nvMax, d.nv);
+        s.anyColour |= (d.flags & F_COLOUR) != 0;
+    }
+    if (s.nTris == 0) return 0;
+    s.binsX = (s.tg.w + p->binW - 1) / p->binW;
+    s.binsY = (s.tg.h + kBinH - 1) / kBinH;
+    s.nBins = (size_t)s.binsX * s.binsY;
+    NoAllocLayout L;
+    size_t base = noalloc_layout(L, s.nd, s.nTris, s.nvMax, s.tg.w, s.tg.h, s.anyColour, s.nBins, kSortChunk);
+    if (base > kNoAllocBytes) {
+        if (base == (size_t)-1) base = 0;
+        return fail(PS3D_ERR_RANGE,
+                    "ps3d_finish_noalloc: a pass of %d triangles into a %dx%d target needs %zu bytes of scratch "
+                    "before its bin lists; the fixed scratch is %zu bytes (ps3d_finish has no such limit)",
+                    s.nTris, s.tg.w, s.tg.h, base, kNoAllocBytes);
+    }
+    // each further sort chunk costs its three pair arrays and one histogram row
+    size_t perChunk = (size_t)kSortChunk * 3 * sizeof(int) + s.nBins * sizeof(int);
+    long long chunks = 1 + (long long)((kNoAllocBytes - base) / perChunk);
+    chunks = std::min<long long>(chunks, 0x7fffffff / kSortChunk);
+    while (chunks > 1 &&
+           noalloc_layout(L, s.nd, s.nTris, s.nvMax, s.tg.w, s.tg.h, s.anyColour, s.nBins,
+                          (int)(chunks * kSortChunk)) > kNoAllocBytes)
+        chunks--;
+    s.pairCap = (int)(chunks * kSortChunk);
+    return 0;
+}
+
+int noalloc_run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps, size_t replayFrom,
+                     unsigned char* base)
+{
+    int seq = (int)p->passStart.size();
+    p->passStart.push_back(replayFrom);
+    const Command& c0 = cmds[ps.first];
+    NoAllocPass s;
+    int rc = noalloc_shape(p, cmds, ps, s, true);
+    if (rc) return rc;
+    if (s.nTris == 0) {
+        if (ps.clearDepth && (rc = fill_depth(p, c0.depthTarget, ps.depthValue))) return rc;
+        if (ps.clearColour && (rc = fill_colour(p, ps.colourValue))) return rc;
+        return 0;
+    }
+    int W = s.tg.w, H = s.tg.h;
+    NoAllocLayout L;
+    noalloc_layout(L, s.nd, s.nTris, s.nvMax, W, H, s.anyColour, s.nBins, s.pairCap);
+    // Pageable-source copies: each returns once the staging arrays are copied
+    // out, so the next pass may overwrite them.
+    CU(cudaMemcpyAsync(base + L.draws, g_noallocDraws, s.nd * sizeof(DrawDesc), cudaMemcpyHostToDevice, p->stream));
+    CU(cudaMemcpyAsync(base + L.unis, g_noallocUnis, s.nd * sizeof(DrawUniforms), cudaMemcpyHostToDevice,
+                       p->stream));
+
+    bool fuseDepth = ps.clearDepth && s.tg.scan == W;
+    bool fuseColour = ps.clearColour && p->devW == W && p->devH == H;
+    if (ps.clearDepth && !fuseDepth && (rc = fill_depth(p, c0.depthTarget, ps.depthValue))) return rc;
+    if (ps.clearColour && !fuseColour && (rc = fill_colour(p, ps.colourValue))) return rc;
+
+    PassParams P;
+    memset(&P, 0, sizeof P);
+    P.W = W;
+    P.H = H;
+    P.binW = p->binW;
+    P.binsX = s.binsX;
+    P.binsY = s.binsY;
+    P.nTris = s.nTris;
+    P.nDraws = s.nd;
+    P.draws = (const DrawDesc*)(base + L.draws);
+    P.unis = (const DrawUniforms*)(base + L.unis);
+    P.tris = (TriRaster*)(base + L.tris);
+    P.vary = (float*)(base + L.vary);
+    P.nvMax = std::max(s.nvMax, 1);
+    P.anyVary = s.nvMax > 0;
+    P.pairCount = (int*)(base + L.pairCount);
+    P.rect = (int4*)(base + L.rect);
+    P.pairOffset = (int*)(base + L.pairOffset);
+    P.pairKey = (int*)(base + L.pairKey);
+    P.pairTri = (int*)(base + L.pairTri);
+    P.pairCap = s.pairCap;
+    P.sortBlocks = (s.pairCap + kSortChunk - 1) / kSortChunk;
+    P.binWindow = max_bins();
+    P.binHist = (int*)(base + L.binHist);
+    P.binStart = (int*)(base + L.binStart);
+    P.binTri = (int*)(base + L.binTri);
+    P.status = p->status;
+    P.depth = s.tg.depth;
+    P.depthScan = s.tg.scan;
+    P.depthW = s.tg.w;
+    P.depthH = s.tg.h;
+    P.winner = s.anyColour ? (int*)(base + L.winner) : nullptr;
+    P.colour = p->colour;
+    P.colourW = p->devW;
+    P.colourH = p->devH;
+    P.clearDepth = fuseDepth;
+    P.clearColour = fuseColour;
+    P.anyColour = s.anyColour;
+    P.countFrags = p->countFrags;
+    P.depthClearValue = fuseDepth ? ps.depthValue : 1.0f;
+    P.colourClearValue = ps.colourValue;
+    P.passSeq = seq;
+    Prof off;  // never records events
+    int launches = 0;
+    launch_setup_and_bin(P, (int*)(base + L.scanTmp), p->stream, launches, &off);
+    launch_raster_shade(P, p->stream, launches, &off);
+    CU(cudaGetLastError());
+    p->stats.kernel_launches += launches;
+    p->stats.batches++;
+    p->stats.triangles += s.nTris;
+    return 0;
+}
+
+}  // namespace
+
+extern "C" int ps3d_finish_noalloc(ps3d_pipeline* p)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    if (p->recording) return fail(PS3D_ERR_INVALID, "ps3d_finish_noalloc: a command buffer is being recorded");
+    if (!p->launched.empty() || p->graphUnverified)
+        return fail(PS3D_ERR_INVALID, "ps3d_finish_noalloc: flushed work is not verified yet; call ps3d_finish");
+    std::lock_guard<std::mutex> lock(g_noallocLock);
+    int dev = -1;
+    CU(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(PS3D_ERR_DEVICE, "device %d out of range", dev);
+    if (!g_noallocPtr[dev]) {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noallocScratch);
+        if (e != cudaSuccess || !ptr)
+            return fail(PS3D_ERR_DEVICE, "cudaGetSymbolAddress of the fixed scratch: %s", cudaGetErrorString(e));
+        g_noallocPtr[dev] = (unsigned char*)ptr;
+    }
+    unsigned char* base = g_noallocPtr[dev];
+    if (p->pending.empty()) return 0;
+
+    // Every pass must fit before anything runs; otherwise the commands stay
+    // recorded for ps3d_finish.
+    const std::vector<Command>& rec = p->pending;
+    int rc = plan_commands(
+        rec, 0,
+        [&](const Pass& ps, size_t) {
+            NoAllocPass s;
+            return noalloc_shape(p, rec, ps, s, false);
+        },
+        [&](int, float, uint32_t) { return 0; }, [&](void*) { return 0; });
+    if (rc) return rc;
+
+    // The abort flag and the overflow record must start at zero.
+    CU(cudaMemsetAsync(p->status, 0, 4 * sizeof(int), p->stream));
+    p->launched.swap(p->pending);
+    const std::vector<Command>& cmds = p->launched;
+    rc = plan_commands(
+        cmds, 0, [&](const Pass& ps, size_t start) { return noalloc_run_pass(p, cmds, ps, start, base); },
+        [&](int target, float v, uint32_t c) { return target == -3 ? fill_colour(p, c) : fill_depth(p, target, v); },
+        [&](void* dst) -> int {
+            CU(cudaMemcpyAsync(dst, p->colour, (size_t)p->devW * 4 * p->devH, cudaMemcpyDeviceToDevice, p->stream));
+            return 0;
+        });
+    if (rc) return rc;
+    CU(cudaStreamSynchronize(p->stream));
+    int st[4];
+    CU(cudaMemcpy(st, p->status, sizeof st, cudaMemcpyDeviceToHost));
+    if (st[0]) {
+        // A pass found more bin pairs than the array holds: it and the passes
+        // after it did nothing.  The commands and the overflow record stay as
+        // ps3d_finish's own recovery expects them.
+        return fail(PS3D_ERR_NOMEM,
+                    "ps3d_finish_noalloc: pass %d needs %d bin pairs, more than the fixed scratch holds; it and "
+                    "the passes after it did not run; ps3d_finish completes the frame (and may allocate)",
+                    st[3], st[1]);
+    }
+    p->launched.clear();
+    p->passStart.clear();
+    return 0;
+}

@@ -55,6 +55,7 @@ _SIGS = {
     "ps3d_draw": [_c_void_p, _c_int],
     "ps3d_flush": [_c_void_p],
     "ps3d_finish": [_c_void_p],
+    "ps3d_finish_noalloc": [_c_void_p],
     "ps3d_read_colour": [_c_void_p, _c_void_p],
     "ps3d_read_depth": [_c_void_p, _c_void_p],
     "ps3d_colour_device_ptr": [_c_void_p, ctypes.POINTER(_c_void_p)],
@@ -234,6 +235,14 @@ class PuresoftPipeline:
 
     def finish(self):
         self._check(self.lib.ps3d_finish(self.h))
+
+    def finishNoAlloc(self):
+        """ps3d_finish_noalloc: finish() with every pass's scratch taken from
+        a fixed 16 MiB device array; allocates no device memory.  Raises
+        IndexError (nothing ran) when a pass is too large for the array, and
+        MemoryError when a pass's bin lists overflowed it (finish() then
+        completes the frame)."""
+        self._check(self.lib.ps3d_finish_noalloc(self.h))
 
     # -- read-back
     def readColour(self, out: np.ndarray | None = None) -> np.ndarray:
