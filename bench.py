@@ -56,6 +56,9 @@ CONFIGS = {
                args={}),
     "c3s": dict(desc="c3s (profiling case): 1920x1080 LIT3, 128 meshes, ~500k triangles, 4x2048^2 trilinear",
                 args={}),
+    "c4": dict(desc="c4: 4096 independent 128x128 views (own seeded mesh, 100-5000 triangles log-uniform, own "
+                    "orbit camera, own 256^2 texture, LIT1), batched into tiles of an 8192^2 atlas in one pass",
+               args={}),
 }
 
 
@@ -121,9 +124,182 @@ class ClockSampler:
 
 def make_scene(cfg):
     from puresoft3d_gb300 import scenes as S
+    if cfg == "c4":
+        return S.scene_c4()[0]
     if cfg == "c3s":
         return S.scene_c3(width=1920, height=1080, meshes=128, tri_target=500_000, textures=4)
     return {"c1": S.scene_c1, "c2": S.scene_c2, "c3": S.scene_c3}[cfg]()
+
+
+def run_c4(args):
+    """Config 4: images/s of the batched pass (every view in one pass over
+    an atlas, replayed as one CUDA graph) against the plain path (one pass
+    per view in a 128x128 pipeline, the frame copied out after each view),
+    both with every mesh and texture resident."""
+    import torch
+    from puresoft3d_gb300 import scenes as S
+    from puresoft3d_gb300.pipeline import PuresoftPipeline, KERNELS
+    views = args.views
+    batched, plain = S.scene_c4(views=views)
+    size = batched.info["view_size"]
+    pipe = PuresoftPipeline(batched.width, batched.height)
+    S.replay_setup(batched, pipe)
+    pipe.finish()
+    pipe.setFragmentCounting(True)
+    st0 = pipe.stats()
+    S.replay_frame(batched, pipe)
+    pipe.finish()
+    st1 = pipe.stats()
+    pipe.setFragmentCounting(False)
+    frags = st1["fragments"] - st0["fragments"]
+    pairs = st1["bin_pairs"] - st0["bin_pairs"]
+    launches_per_frame = st1["kernel_launches"] - st0["kernel_launches"]
+
+    pipe.profile(True)
+    pipe.profileRead()
+    prof_frames = 3
+    for _ in range(prof_frames):
+        pipe.scrubL2()
+        S.replay_frame(batched, pipe)
+        pipe.finish()
+    prof = pipe.profileRead()
+    pipe.profile(False)
+
+    pipe.beginCommands()
+    S.replay_frame(batched, pipe)
+    cb = pipe.endCommands()
+    for _ in range(max(3, args.warmup)):
+        cb.submit()
+    pipe.finish()
+    clocks = ClockSampler()
+    clocks.start()
+    frame_ms = []
+    for _ in range(args.steps):
+        pipe.scrubL2()
+        pipe.timerBegin()
+        cb.submit()
+        frame_ms.append(pipe.timerEnd())
+    pipe.finish()
+    clk = clocks.stop()
+    total_ms = allreduce_max(sum(frame_ms))
+    ips = WORLD * views * args.steps / (total_ms / 1e3)
+
+    host = torch.empty((batched.height, batched.width, 4), dtype=torch.uint8, pin_memory=True).numpy()
+    for _ in range(2):
+        cb.submit(upload_inputs=True)
+        pipe.readColour(host)
+    e2e_steps = max(3, args.steps // 2)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        cb.submit(upload_inputs=True)
+        pipe.readColour(host)
+    e2e_s = allreduce_max(time.perf_counter() - t0)
+    in_bytes = cb.input_bytes()
+    cb.destroy()
+    pipe.close()
+
+    # plain: one pass per view, each frame copied to its own slot of a device array
+    alone = PuresoftPipeline(size, size)
+    S.replay_setup(plain, alone)
+    out = torch.empty((views, size, size, 4), dtype=torch.uint8, device="cuda")
+    base, stride = out.data_ptr(), size * size * 4
+
+    def plain_frame():
+        for v in range(views):
+            S.replay_ops(plain.info["view_frames"][v], alone)
+            alone.readColourDevice(base + v * stride)
+
+    plain_frame()
+    alone.finish()
+    st0 = alone.stats()
+    alone.scrubL2()
+    alone.timerBegin()
+    plain_frame()
+    plain_ms = alone.timerEnd()
+    plain_launches = alone.stats()["kernel_launches"] - st0["kernel_launches"]
+    alone.beginCommands()
+    plain_frame()
+    pcb = alone.endCommands()
+    for _ in range(2):
+        pcb.submit()
+    alone.finish()
+    pg_ms = []
+    for _ in range(max(2, args.steps // 4)):
+        alone.scrubL2()
+        alone.timerBegin()
+        pcb.submit()
+        pg_ms.append(alone.timerEnd())
+    pcb.destroy()
+    alone.close()
+    plain_ips = views / (plain_ms / 1e3)
+    plain_graph_ips = views / (statistics.median(pg_ms) / 1e3)
+
+    ab = algorithmic_bytes(batched, pairs)
+    dom = max(prof, key=lambda k: prof[k][1])
+    n_launch, ms = prof[dom]
+    avg_ms = ms / max(n_launch, 1)
+    peak, peak_kind = peaks()
+    bytes_per_launch = ab["raster_per_frame"] if dom == "raster" else None
+    achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9 if bytes_per_launch else None
+    line = {
+        "metric": "images/s", "value": round(ips, 2), "unit": "images/s", "n_gpus": WORLD,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded meshes, cameras and textures per view)",
+        "config": {"workload": CONFIGS["c4"]["desc"], "views": views, "view_size": size,
+                   "atlas": [batched.width, batched.height], "triangles": batched.triangles(),
+                   "l2": "256 MB scrub before each timed step",
+                   "parallelism": "replicas" if WORLD > 1 else "single GPU"},
+        "plain_images_per_s": {"immediate": round(plain_ips, 2), "graph": round(plain_graph_ips, 2),
+                               "launches_per_view": round(plain_launches / views, 2)},
+        "batched_over_plain": {"immediate": round(ips / WORLD / plain_ips, 2),
+                               "graph": round(ips / WORLD / plain_graph_ips, 2)},
+        "gfrag_per_s": round(frags * ips / views / 1e9, 4),
+        "fragments_per_step": frags,
+        "gpu_launches": launches_per_frame * args.steps,
+        "e2e": {"value": round(WORLD * views * e2e_steps / e2e_s, 2), "unit": "images/s",
+                "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": batched.width * batched.height * 4},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2) if achieved else None,
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5) if achieved else None,
+                     "peak_source": peak_kind, "avg_launch_ms": round(avg_ms, 5),
+                     "bytes_per_launch": bytes_per_launch, "traffic": None},
+        "kernel_ms_per_step": {k: round(prof[k][1] / prof_frames, 5) for k in KERNELS if prof[k][0]},
+        "clocks": clk,
+    }
+    if RANK == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_views(budget_s=args.cpu_budget)
+    return line
+
+
+def cpu_baseline_views(budget_s=15.0, threads=None, sample_views=256):
+    """Config 4 on the host cores: the reference pipeline (or its oracle
+    port) rendering the first views of the same seeded set one at a time in a
+    128x128 pipeline."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from puresoft3d_gb300 import scenes as S
+    from cpu_backends import OraclePipeline, RefPipeline
+    threads = threads or os.cpu_count() or 1
+    _, plain = S.scene_c4(views=sample_views)
+    size = plain.info["view_size"]
+    use_ref = os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libps3dref.so")) and os.uname().machine == "x86_64"
+    if use_ref:
+        os.environ["PS3D_REF_THREADS"] = str(threads)
+        pipe, kind = RefPipeline(size, size, threads), "reference"
+    else:
+        pipe, kind = OraclePipeline(size, size, threads), "port"
+    S.replay_setup(plain, pipe)
+    S.replay_ops(plain.info["view_frames"][0], pipe)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        S.replay_ops(plain.info["view_frames"][n % sample_views], pipe)
+        pipe.readColour()
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or n >= 20 * sample_views:
+            break
+    pipe.close()
+    return {"value": round(n / el, 3), "unit": "images/s", "cores": threads, "kind": kind,
+            "sample": "%d views (of the first %d of the seeded set) in %.1f s" % (n, sample_views, el)}
 
 
 def run_frames_only(args):
@@ -297,6 +473,8 @@ def cpu_baseline(scene, budget_s=15.0, threads=None):
 
 
 def run_reference(args):
+    if args.config == "c4":
+        return run_reference_views(args)
     scene = make_scene(args.config)
     per = max(2.0, args.cpu_budget / max(args.steps, 1))
     vals = []
@@ -318,6 +496,26 @@ def run_reference(args):
             "cpu_baseline": {"value": v, "unit": "frames/s", "cores": cb["cores"], "kind": cb["kind"],
                              "sample": "%d steps, %d frames in %.1f s" % (args.steps, frames, el)},
             "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def run_reference_views(args):
+    per = max(2.0, args.cpu_budget / max(args.steps, 1))
+    cpu_baseline_views(budget_s=0.1)
+    vals, n_total, t0 = [], 0, time.perf_counter()
+    cb = None
+    for _ in range(args.steps):
+        cb = cpu_baseline_views(budget_s=per)
+        vals.append(cb["value"])
+        n_total += int(cb["sample"].split()[0])
+    el = time.perf_counter() - t0
+    v = statistics.median(vals)
+    return {"impl": "reference", "metric": "images/s", "value": v, "unit": "images/s", "n_gpus": WORLD,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 / v, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": CONFIGS["c4"]["desc"]},
+            "cpu_baseline": {"value": v, "unit": "images/s", "cores": cb["cores"], "kind": cb["kind"],
+                             "sample": "%d steps, %d views in %.1f s" % (args.steps, n_total, el)},
+            "e2e": {"value": v, "unit": "images/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
 _pg = None
@@ -355,6 +553,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ncu-frames", type=int, default=0, help="render N frames for a profiler and exit")
+    ap.add_argument("--views", type=int, default=4096, help="config 4: number of views")
     args = ap.parse_args()
     if args.ncu_frames:
         run_frames_only(args)
@@ -366,7 +565,7 @@ def main():
         print(json.dumps(run_reference(args)), flush=True)
         return
     init_dist()
-    line = run_ours(args)
+    line = run_c4(args) if args.config == "c4" else run_ours(args)
     if RANK == 0:
         print(json.dumps(line), flush=True)
 
