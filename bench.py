@@ -131,6 +131,17 @@ def make_scene(cfg):
     return {"c1": S.scene_c1, "c2": S.scene_c2, "c3": S.scene_c3}[cfg]()
 
 
+def autotune(pipe, record, key, args):
+    """Bin width for this workload, picked by timing each candidate on the
+    frame itself (puresoft3d_gb300.autotune); untimed."""
+    from puresoft3d_gb300.autotune import Autotuner
+    if args.bin_width:
+        pipe.setBinWidth(args.bin_width)
+        return {"bin_width": args.bin_width, "source": "--bin-width"}
+    best, ms = Autotuner().tune(pipe, record, key, reps=3)
+    return {"bin_width": best, "source": "autotuner", "candidate_ms": {str(k): round(v, 4) for k, v in ms.items()}}
+
+
 def run_c4(args):
     """Config 4: images/s of the batched pass (every view in one pass over
     an atlas, replayed as one CUDA graph) against the plain path (one pass
@@ -145,6 +156,8 @@ def run_c4(args):
     pipe = PuresoftPipeline(batched.width, batched.height)
     S.replay_setup(batched, pipe)
     pipe.finish()
+    tune = autotune(pipe, lambda p: S.replay_frame(batched, p), "c4:%d:%dx%d" % (views, batched.width, batched.height),
+                    args)
     pipe.setFragmentCounting(True)
     st0 = pipe.stats()
     S.replay_frame(batched, pipe)
@@ -209,6 +222,8 @@ def run_c4(args):
             S.replay_ops(plain.info["view_frames"][v], alone)
             alone.readColourDevice(base + v * stride)
 
+    tune_plain = autotune(alone, lambda p: [S.replay_ops(plain.info["view_frames"][v], p) for v in range(256)],
+                          "c4plain:256:%d" % size, args)
     plain_frame()
     alone.finish()
     st0 = alone.stats()
@@ -249,9 +264,9 @@ def run_c4(args):
         "config": {"workload": CONFIGS["c4"]["desc"], "views": views, "view_size": size,
                    "atlas": [batched.width, batched.height], "triangles": batched.triangles(),
                    "l2": "256 MB scrub before each timed step",
-                   "parallelism": "replicas" if WORLD > 1 else "single GPU"},
+                   "parallelism": "replicas" if WORLD > 1 else "single GPU", "schedule": tune},
         "plain_images_per_s": {"immediate": round(plain_ips, 2), "graph": round(plain_graph_ips, 2),
-                               "launches_per_view": round(plain_launches / views, 2)},
+                               "launches_per_view": round(plain_launches / views, 2), "schedule": tune_plain},
         "batched_over_plain": {"immediate": round(ips / WORLD / plain_ips, 2),
                                "graph": round(ips / WORLD / plain_graph_ips, 2)},
         "gfrag_per_s": round(frags * ips / views / 1e9, 4),
@@ -343,6 +358,8 @@ def run_ours(args):
     pipe = PuresoftPipeline(scene.width, scene.height)
     S.replay_setup(scene, pipe)
     pipe.finish()
+    tune = autotune(pipe, lambda p: S.replay_frame(scene, p), "%s:%dx%d:%d" % (
+        args.config, scene.width, scene.height, scene.triangles()), args)
 
     # fragments and pairs per frame (counting run, untimed)
     pipe.setFragmentCounting(True)
@@ -423,7 +440,7 @@ def run_ours(args):
         "data": "synthetic (seeded meshes and procedural textures)",
         "config": {"workload": CONFIGS[args.config]["desc"], "width": scene.width, "height": scene.height,
                    "triangles": scene.triangles(), "l2": "256 MB scrub before each timed frame",
-                   "parallelism": "replicas" if WORLD > 1 else "single GPU"},
+                   "parallelism": "replicas" if WORLD > 1 else "single GPU", "schedule": tune},
         "gfrag_per_s": round(frags * fps / WORLD / 1e9 * WORLD, 4),
         "fragments_per_frame": frags,
         "gpu_launches": launches_per_frame * args.steps,
@@ -554,6 +571,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ncu-frames", type=int, default=0, help="render N frames for a profiler and exit")
     ap.add_argument("--views", type=int, default=4096, help="config 4: number of views")
+    ap.add_argument("--bin-width", type=int, default=0, choices=[0, 8, 16, 32],
+                    help="fix the bin width instead of autotuning it")
     args = ap.parse_args()
     if args.ncu_frames:
         run_frames_only(args)

@@ -186,6 +186,13 @@ int ps3d_flush(ps3d_pipeline* p);
  * drawvao.cpp:121-132). */
 int ps3d_finish(ps3d_pipeline* p);
 
+/* Schedule knob (no reference counterpart): the width in columns (8, 16 or
+ * 32) of the 32-row bins the passes launched from now on are cut into.  It
+ * changes time only, never results; puresoft3d_gb300.autotune picks it per
+ * workload.  Default 32 (or PS3D_BIN_W). */
+int ps3d_set_bin_width(ps3d_pipeline* p, int columns);
+int ps3d_get_bin_width(ps3d_pipeline* p, int* columns);
+
 /* ps3d_finish for callers that must not allocate device memory; it has no
  * counterpart in the reference, whose CPU pipeline allocates no device memory
  * at all.  Who needs it: a real-time render thread that may not block in

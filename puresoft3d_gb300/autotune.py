@@ -1,0 +1,116 @@
+"""Schedule autotuner for the device passes.
+
+The one schedule knob of a pass is its bin width (8, 16 or 32 columns; bins
+are always 32 rows).  It sets how the raster kernel's work is cut:
+
+* the number of bins, hence blocks, a pass launches (more, smaller bins give
+  small views and thin targets more parallelism);
+* the pixels each walker thread owns per span (bin width / 4: the four warps
+  of a bin split its columns into quarters, one lane per row), i.e. the
+  fragments per warp per span;
+* the (bin, triangle) pairs binning emits (a triangle crosses more narrow
+  bins) and the span set-up work they carry.
+
+Which width wins depends on the workload (triangle sizes, depth complexity,
+target size), so the tuner times every candidate on the caller's own frame:
+the frame is recorded as a command buffer, replayed as a CUDA graph with the
+L2 scrubbed before each replay, and timed with CUDA events on the pipeline's
+stream; the fastest median wins.  Results are cached per workload key and
+device in a JSON file (``PS3D_AUTOTUNE_CACHE``, default
+``~/.cache/puresoft3d_gb300/autotune.json``), so a service tunes a workload
+once.  Results are identical for every width (the parity tests check 16 and
+32 against the oracle); only the time differs.
+"""
+from __future__ import annotations
+
+import json
+import os
+import statistics
+from typing import Callable, Dict, Optional, Sequence, Tuple
+
+CANDIDATES = (8, 16, 32)
+
+
+def _default_cache() -> str:
+    return os.environ.get("PS3D_AUTOTUNE_CACHE") or os.path.join(
+        os.path.expanduser("~"), ".cache", "puresoft3d_gb300", "autotune.json")
+
+
+def device_name() -> str:
+    try:
+        import torch
+        return torch.cuda.get_device_name(0)
+    except Exception:
+        return "cuda"
+
+
+class Autotuner:
+    def __init__(self, cache_path: Optional[str] = None, use_cache: bool = True):
+        self.path = cache_path or _default_cache()
+        self.use_cache = use_cache
+        self.table: Dict[str, dict] = {}
+        if use_cache and os.path.exists(self.path):
+            try:
+                with open(self.path) as f:
+                    self.table = json.load(f)
+            except (OSError, ValueError):
+                self.table = {}
+
+    def _save(self):
+        if not self.use_cache:
+            return
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            tmp = self.path + ".tmp"
+            with open(tmp, "w") as f:
+                json.dump(self.table, f, indent=1, sort_keys=True)
+            os.replace(tmp, self.path)
+        except OSError:
+            pass
+
+    @staticmethod
+    def time_frame(pipe, record: Callable[[object], None], reps: int = 5, warmup: int = 2,
+                   scrub: bool = True) -> float:
+        """Median ms of one replay of `record`'s frame as a command buffer."""
+        pipe.beginCommands()
+        record(pipe)
+        cb = pipe.endCommands()
+        try:
+            cb.submit()          # first submission runs and verifies the bin-list room
+            pipe.finish()
+            for _ in range(warmup):
+                cb.submit()
+            pipe.finish()
+            times = []
+            for _ in range(reps):
+                if scrub:
+                    pipe.scrubL2()
+                pipe.timerBegin()
+                cb.submit()
+                times.append(pipe.timerEnd())
+            pipe.finish()
+        finally:
+            cb.destroy()
+        return statistics.median(times)
+
+    def tune(self, pipe, record: Callable[[object], None], key: str,
+             candidates: Sequence[int] = CANDIDATES, reps: int = 5, warmup: int = 2,
+             retune: bool = False) -> Tuple[int, Dict[int, float]]:
+        """Sets `pipe`'s bin width to the fastest candidate for `record`'s
+        frame and returns (width, {width: median ms}).  A cached result for
+        (key, device, candidates) is reused unless `retune`."""
+        full = "%s|%s|%s" % (key, device_name(), ",".join(str(c) for c in candidates))
+        hit = self.table.get(full)
+        if hit and not retune:
+            best = int(hit["best"])
+            pipe.setBinWidth(best)
+            return best, {int(k): v for k, v in hit["ms"].items()}
+        ms: Dict[int, float] = {}
+        for c in candidates:
+            pipe.setBinWidth(c)
+            ms[c] = self.time_frame(pipe, record, reps=reps, warmup=warmup)
+        best = min(ms, key=ms.get)
+        pipe.setBinWidth(best)
+        self.table[full] = {"best": best, "ms": {str(k): round(v, 5) for k, v in ms.items()}}
+        self._save()
+        return best, ms

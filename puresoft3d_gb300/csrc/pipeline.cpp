@@ -663,7 +663,7 @@ int ps3d_pipeline_create(int width, int height, void* stream, ps3d_pipeline** ou
     }
     if (const char* bw = getenv("PS3D_BIN_W")) {
         int v = atoi(bw);
-        if (v == 16 || v == 32) p->binW = v;
+        if (v == 8 || v == 16 || v == 32) p->binW = v;
     }
     if (stream) p->stream = (cudaStream_t)stream;
     else {
@@ -1084,6 +1084,22 @@ int ps3d_draw(ps3d_pipeline* p, int vao)
         return fail(PS3D_ERR_INVALID, "the viewport rectangle is not inside the colour buffer");
     (p->recording ? p->recording->cmds : p->pending).push_back(c);
     p->stats.draws++;
+    return 0;
+}
+
+int ps3d_set_bin_width(ps3d_pipeline* p, int columns)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    if (columns != 8 && columns != 16 && columns != 32)
+        return fail(PS3D_ERR_INVALID, "bin width %d: 8, 16 or 32 columns", columns);
+    p->binW = columns;
+    return 0;
+}
+
+int ps3d_get_bin_width(ps3d_pipeline* p, int* columns)
+{
+    if (!p || !columns) return fail(PS3D_ERR_INVALID, "null argument");
+    *columns = p->binW;
     return 0;
 }
 

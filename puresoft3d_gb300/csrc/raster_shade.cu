@@ -385,6 +385,7 @@ void launch_raster_shade(const PassParams& P, cudaStream_t s, int& launches, Pro
     int nBins = P.binsX * P.binsY;
     pr->begin(K_RASTER, s);
     switch (P.binW) {
+    case 8: launch_raster<8>(P, nBins, s); break;
     case 16: launch_raster<16>(P, nBins, s); break;
     default: launch_raster<32>(P, nBins, s); break;
     }

@@ -56,6 +56,8 @@ _SIGS = {
     "ps3d_flush": [_c_void_p],
     "ps3d_finish": [_c_void_p],
     "ps3d_finish_noalloc": [_c_void_p],
+    "ps3d_set_bin_width": [_c_void_p, _c_int],
+    "ps3d_get_bin_width": [_c_void_p, ctypes.POINTER(_c_int)],
     "ps3d_read_colour": [_c_void_p, _c_void_p],
     "ps3d_read_depth": [_c_void_p, _c_void_p],
     "ps3d_colour_device_ptr": [_c_void_p, ctypes.POINTER(_c_void_p)],
@@ -235,6 +237,15 @@ class PuresoftPipeline:
 
     def finish(self):
         self._check(self.lib.ps3d_finish(self.h))
+
+    def setBinWidth(self, columns: int):
+        """Bin width (8, 16 or 32 columns) of the passes launched from now on."""
+        self._check(self.lib.ps3d_set_bin_width(self.h, columns))
+
+    def binWidth(self) -> int:
+        v = _c_int()
+        self._check(self.lib.ps3d_get_bin_width(self.h, ctypes.byref(v)))
+        return v.value
 
     def finishNoAlloc(self):
         """ps3d_finish_noalloc: finish() with every pass's scratch taken from

@@ -1,0 +1,82 @@
+"""The schedule autotuner's selection and cache logic, on a fake pipeline
+whose frame time depends on the bin width (no GPU)."""
+import json
+
+from puresoft3d_gb300.autotune import Autotuner
+
+
+class _FakeCb:
+    def __init__(self, pipe):
+        self.pipe = pipe
+
+    def submit(self):
+        self.pipe.submits += 1
+
+    def destroy(self):
+        pass
+
+
+class _FakePipe:
+    COST = {8: 3.0, 16: 1.5, 32: 2.0}
+
+    def __init__(self):
+        self.bw = 32
+        self.submits = 0
+        self.recorded = 0
+
+    def setBinWidth(self, w):
+        assert w in self.COST
+        self.bw = w
+
+    def beginCommands(self):
+        pass
+
+    def endCommands(self):
+        return _FakeCb(self)
+
+    def finish(self):
+        pass
+
+    def scrubL2(self):
+        pass
+
+    def timerBegin(self):
+        pass
+
+    def timerEnd(self):
+        return self.COST[self.bw]
+
+
+def _record(pipe):
+    pipe.recorded += 1
+
+
+def test_picks_fastest_and_sets_it(tmp_path):
+    t = Autotuner(cache_path=str(tmp_path / "tune.json"))
+    p = _FakePipe()
+    best, ms = t.tune(p, _record, key="w1")
+    assert best == 16 and p.bw == 16
+    assert ms == {8: 3.0, 16: 1.5, 32: 2.0}
+    assert p.recorded == 3
+
+
+def test_cache_is_reused_and_keyed(tmp_path):
+    path = str(tmp_path / "tune.json")
+    Autotuner(cache_path=path).tune(_FakePipe(), _record, key="w1")
+    table = json.load(open(path))
+    assert len(table) == 1 and list(table.values())[0]["best"] == 16
+    p = _FakePipe()
+    best, _ = Autotuner(cache_path=path).tune(p, _record, key="w1")
+    assert best == 16 and p.bw == 16 and p.recorded == 0  # from the cache, nothing timed
+    p2 = _FakePipe()
+    Autotuner(cache_path=path).tune(p2, _record, key="w2", candidates=(8, 32))
+    assert p2.bw == 32 and p2.recorded == 2
+    assert len(json.load(open(path))) == 2
+
+
+def test_retune_ignores_cache(tmp_path):
+    path = str(tmp_path / "tune.json")
+    Autotuner(cache_path=path).tune(_FakePipe(), _record, key="w1")
+    p = _FakePipe()
+    Autotuner(cache_path=path).tune(p, _record, key="w1", retune=True)
+    assert p.recorded == 3

@@ -55,14 +55,19 @@ def test_bin_capacity_replay(gpu_lib, monkeypatch):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("bin_w", [16, 32])
-def test_bin_widths_agree(gpu_lib, monkeypatch, bin_w):
+@pytest.mark.parametrize("bin_w", [8, 16, 32])
+@pytest.mark.parametrize("case", ["kat_soup_depth", "c3_small"])
+def test_bin_widths_agree(gpu_lib, bin_w, case):
     from puresoft3d_gb300.pipeline import PuresoftPipeline
-    name, scene = [c for c in CASES if c[0].startswith("kat_soup_depth")][0]
-    monkeypatch.setenv("PS3D_BIN_W", str(bin_w))
-    out = render(PuresoftPipeline(scene.width, scene.height), scene)
+    name, scene = [c for c in CASES if c[0].startswith(case)][0]
+    g = PuresoftPipeline(scene.width, scene.height)
+    g.setBinWidth(bin_w)
+    assert g.binWidth() == bin_w
+    out = render(g, scene)
     ref = render(OraclePipeline(scene.width, scene.height), scene)
     assert_depth_exact(out["depth"], ref["depth"], name)
+    mx, mean = colour_diff(out["colour"], ref["colour"])
+    assert mx <= COLOUR_TOL, "%s: colour differs by up to %d LSB (mean %.4f)" % (name, mx, mean)
 
 
 @pytest.mark.gpu
