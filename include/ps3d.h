@@ -263,8 +263,8 @@ int ps3d_timer_end(ps3d_pipeline* p, float* ms);
 #define PS3D_K_SETUP 0
 #define PS3D_K_SCAN 1
 #define PS3D_K_EMIT 2
-#define PS3D_K_HIST 3
-#define PS3D_K_SCATTER 4
+#define PS3D_K_BOUNDS 3  /* per-bin list starts */
+#define PS3D_K_SORT 4    /* radix passes of the (bin, triangle) pairs */
 #define PS3D_K_RASTER 5
 #define PS3D_K_SHADE 6
 #define PS3D_K_FILL 7

@@ -32,7 +32,8 @@
 namespace ps3d {
 void launch_setup_and_bin(const PassParams& P, int* scanTmp, cudaStream_t s, int& launches, Prof* pr);
 int scan_block_sums_needed(int nMax);
-int max_bins();
+int radix_passes(int nBins);
+size_t radix_scratch_ints(int sortBlocks, int passes);
 int selftest_division(unsigned long long pairs, unsigned long long* rcpBad, unsigned long long* divBad);
 void launch_raster_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr);
 void launch_fill_u32(void* base, int width, int height, int pitchElems, uint32_t v, const int* status,
@@ -61,6 +62,9 @@ int fail(int code, const char* fmt, ...)
         cudaError_t e_ = (call);                                                                 \
         if (e_ != cudaSuccess) return fail(PS3D_ERR_DEVICE, "%s: %s", #call, cudaGetErrorString(e_)); \
     } while (0)
+
+// The sort's look-back descriptors hold prefixes in 30 bits.
+constexpr int kMaxPairs = (1 << 30) - kSortChunk;
 
 struct Texture {
     uint8_t* dev = nullptr;
@@ -176,7 +180,8 @@ struct ps3d_pipeline {
     int* pairKey = nullptr; size_t pairKeyCap = 0;
     int* pairTri = nullptr; size_t pairTriCap = 0;
     int* binTri = nullptr; size_t binTriCap = 0;
-    int* binHist = nullptr; size_t binHistCap = 0;
+    int* radix = nullptr; size_t radixCap = 0;
+    int* keyB = nullptr; size_t keyBCap = 0;
     int* binStart = nullptr; size_t binStartCap = 0;
     int* scanTmp = nullptr; size_t scanTmpCap = 0;
     int* winner = nullptr; size_t winnerCap = 0;
@@ -362,11 +367,10 @@ int ensure_scratch(ps3d_pipeline* p, int nTris, int nvMax, int W, int H, int bin
               dev_alloc(p->pairCount, p->pairCountCap, nTris) && dev_alloc(p->rect, p->rectCap, nTris) &&
               dev_alloc(p->pairOffset, p->pairOffsetCap, (size_t)nTris + 1) &&
               dev_alloc(p->pairKey, p->pairKeyCap, p->pairCap) && dev_alloc(p->pairTri, p->pairTriCap, p->pairCap) &&
-              dev_alloc(p->binTri, p->binTriCap, p->pairCap) &&
-              dev_alloc(p->binHist, p->binHistCap, nBins * sortBlocks + 1) &&
+              dev_alloc(p->keyB, p->keyBCap, p->pairCap) && dev_alloc(p->binTri, p->binTriCap, p->pairCap) &&
+              dev_alloc(p->radix, p->radixCap, radix_scratch_ints(sortBlocks, radix_passes((int)nBins))) &&
               dev_alloc(p->binStart, p->binStartCap, nBins + 1) &&
-              dev_alloc(p->scanTmp, p->scanTmpCap,
-                        (size_t)scan_block_sums_needed((int)std::max<size_t>(nTris, nBins * sortBlocks)) + 1);
+              dev_alloc(p->scanTmp, p->scanTmpCap, (size_t)scan_block_sums_needed(nTris) + 1);
     if (ok && colour) ok = dev_alloc(p->winner, p->winnerCap, (size_t)W * H);
     if (!ok) return fail(PS3D_ERR_NOMEM, "device scratch allocation failed");
     return 0;
@@ -501,10 +505,12 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     P.pairTri = p->pairTri;
     P.pairCap = p->pairCap;
     P.sortBlocks = (p->pairCap + kSortChunk - 1) / kSortChunk;
-    P.binWindow = max_bins();
-    P.binHist = p->binHist;
+    P.radixPasses = radix_passes(binsX * binsY);
+    P.radix = p->radix;
+    P.keyB = p->keyB;
     P.binStart = p->binStart;
     P.binTri = p->binTri;
+    P.sortedTri = (P.radixPasses & 1) ? p->binTri : p->pairTri;
     P.status = p->status;
     P.depth = tg.depth;
     P.depthScan = tg.scan;
@@ -623,6 +629,13 @@ int do_finish(ps3d_pipeline* p)
             p->graphUnverified = nullptr;
             return 0;
         }
+        if (st[0] == 2) {
+            CU(cudaMemsetAsync(p->status, 0, 4 * sizeof(int), p->stream));
+            p->launched.clear();
+            p->passStart.clear();
+            p->graphUnverified = nullptr;
+            return fail(PS3D_ERR_TIMEOUT, "a device-side wait of the bin sort expired; the frame is incomplete");
+        }
         if (p->launched.empty() && p->graphUnverified) {
             // a graph launch outgrew the room its first submission verified
             CU(cudaMemsetAsync(p->status, 0, 4 * sizeof(int), p->stream));
@@ -633,8 +646,9 @@ int do_finish(ps3d_pipeline* p)
         }
         int seq = st[3];
         if (seq < 0 || seq >= (int)p->passStart.size()) return fail(PS3D_ERR_DEVICE, "bad overflow record");
+        if (st[1] > kMaxPairs) return fail(PS3D_ERR_NOMEM, "a pass needs %d bin pairs (at most %d)", st[1], kMaxPairs);
         p->pairCap = (int)std::min<long long>(std::max<long long>((long long)p->pairCap * 2, (long long)st[1] * 5 / 4 + 1024),
-                                              0x7fffffff);
+                                              kMaxPairs);
         CU(cudaMemsetAsync(p->status, 0, 4 * sizeof(int), p->stream));
         p->stats.replays++;
         size_t from = p->passStart[seq];
@@ -659,7 +673,7 @@ int ps3d_pipeline_create(int width, int height, void* stream, ps3d_pipeline** ou
     p->devH = p->H = height;
     if (const char* cap = getenv("PS3D_PAIR_CAP")) {
         long v = atol(cap);
-        if (v >= 32 && v < (1L << 30)) p->pairCap = (int)v;
+        if (v >= 32 && v <= kMaxPairs) p->pairCap = (int)v;
     }
     if (const char* bw = getenv("PS3D_BIN_W")) {
         int v = atoi(bw);
@@ -712,7 +726,7 @@ int ps3d_pipeline_destroy(ps3d_pipeline* p)
                 delete b;
             }
     void* bufs[] = {p->colour, p->defDepth, p->status, p->tris, p->vary, p->pairCount, p->rect, p->pairOffset,
-                    p->pairKey, p->pairTri, p->binTri, p->binHist, p->binStart, p->scanTmp, p->winner, p->draws,
+                    p->pairKey, p->pairTri, p->keyB, p->binTri, p->radix, p->binStart, p->scanTmp, p->winner, p->draws,
                     p->unis};
     for (void* b : bufs)
         if (b) cudaFree(b);
@@ -1423,8 +1437,8 @@ DrawUniforms g_noallocUnis[kNoAllocMaxDraws];
 
 // Byte offsets of one pass's buffers in the array, each 256-byte aligned.
 struct NoAllocLayout {
-    size_t draws, unis, tris, vary, pairCount, rect, pairOffset, scanTmp, winner, binStart, binHist, pairKey,
-        pairTri, binTri;
+    size_t draws, unis, tris, vary, pairCount, rect, pairOffset, scanTmp, winner, binStart, radix, pairKey,
+        pairTri, keyB, binTri;
 };
 
 size_t noalloc_layout(NoAllocLayout& L, int nd, int nTris, int nv, int W, int H, bool colour, size_t nBins,
@@ -1437,8 +1451,7 @@ size_t noalloc_layout(NoAllocLayout& L, int nd, int nTris, int nv, int W, int H,
         return at;
     };
     size_t sortBlocks = ((size_t)pairCap + kSortChunk - 1) / kSortChunk;
-    size_t scanN = std::max<size_t>((size_t)nTris, nBins * sortBlocks);
-    if (scanN > 0x7fffffff) return (size_t)-1;
+    if (nBins > 0x7fffffff) return (size_t)-1;
     L.draws = take((size_t)nd * sizeof(DrawDesc));
     L.unis = take((size_t)nd * sizeof(DrawUniforms));
     L.tris = take((size_t)nTris * sizeof(TriRaster));
@@ -1446,12 +1459,13 @@ size_t noalloc_layout(NoAllocLayout& L, int nd, int nTris, int nv, int W, int H,
     L.pairCount = take((size_t)nTris * sizeof(int));
     L.rect = take((size_t)nTris * sizeof(int4));
     L.pairOffset = take(((size_t)nTris + 1) * sizeof(int));
-    L.scanTmp = take(((size_t)scan_block_sums_needed((int)scanN) + 1) * sizeof(int));
+    L.scanTmp = take(((size_t)scan_block_sums_needed(nTris) + 1) * sizeof(int));
     L.winner = colour ? take((size_t)W * H * sizeof(int)) : 0;
     L.binStart = take((nBins + 1) * sizeof(int));
-    L.binHist = take((nBins * sortBlocks + 1) * sizeof(int));
+    L.radix = take(radix_scratch_ints((int)sortBlocks, radix_passes((int)nBins)) * sizeof(int));
     L.pairKey = take((size_t)pairCap * sizeof(int));
     L.pairTri = take((size_t)pairCap * sizeof(int));
+    L.keyB = take((size_t)pairCap * sizeof(int));
     L.binTri = take((size_t)pairCap * sizeof(int));
     return off;
 }
@@ -1499,8 +1513,8 @@ int noalloc_shape(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass
                     "before its bin lists; the fixed scratch is %zu bytes (ps3d_finish has no such limit)",
                     s.nTris, s.tg.w, s.tg.h, base, kNoAllocBytes);
     }
-    // each further sort chunk costs its three pair arrays and one histogram row
-    size_t perChunk = (size_t)kSortChunk * 3 * sizeof(int) + s.nBins * sizeof(int);
+    // each further sort tile costs its four pair arrays and its look-back descriptors
+    size_t perChunk = (size_t)kSortChunk * 4 * sizeof(int) + (size_t)kRadixMaxPasses * kRadixDigits * sizeof(int);
     long long chunks = 1 + (long long)((kNoAllocBytes - base) / perChunk);
     chunks = std::min<long long>(chunks, 0x7fffffff / kSortChunk);
     while (chunks > 1 &&
@@ -1561,10 +1575,12 @@ int noalloc_run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const P
     P.pairTri = (int*)(base + L.pairTri);
     P.pairCap = s.pairCap;
     P.sortBlocks = (s.pairCap + kSortChunk - 1) / kSortChunk;
-    P.binWindow = max_bins();
-    P.binHist = (int*)(base + L.binHist);
+    P.radixPasses = radix_passes((int)s.nBins);
+    P.radix = (int*)(base + L.radix);
+    P.keyB = (int*)(base + L.keyB);
     P.binStart = (int*)(base + L.binStart);
     P.binTri = (int*)(base + L.binTri);
+    P.sortedTri = (P.radixPasses & 1) ? P.binTri : P.pairTri;
     P.status = p->status;
     P.depth = s.tg.depth;
     P.depthScan = s.tg.scan;
@@ -1641,6 +1657,12 @@ extern "C" int ps3d_finish_noalloc(ps3d_pipeline* p)
     CU(cudaStreamSynchronize(p->stream));
     int st[4];
     CU(cudaMemcpy(st, p->status, sizeof st, cudaMemcpyDeviceToHost));
+    if (st[0] == 2) {
+        CU(cudaMemsetAsync(p->status, 0, 4 * sizeof(int), p->stream));
+        p->launched.clear();
+        p->passStart.clear();
+        return fail(PS3D_ERR_TIMEOUT, "a device-side wait of the bin sort expired; the frame is incomplete");
+    }
     if (st[0]) {
         // A pass found more bin pairs than the array holds: it and the passes
         // after it did nothing.  The commands and the overflow record stay as

@@ -86,12 +86,15 @@ struct PassParams {
     int* pairOffset;          // exclusive scan of pairCount (+ total at [nTris])
     int* pairKey;             // bin of each (tri, bin) pair, in triangle order
     int* pairTri;
-    int pairCap;              // capacity of pairKey / pairTri / binTri
-    int sortBlocks;           // pairCap / kSortChunk
-    int binWindow;            // bins counted per shared-memory window in the sort
-    int* binHist;             // [sortBlock][bin] counts, then per-bin prefixes over blocks
+    int pairCap;              // capacity of pairKey / pairTri / keyB / binTri
+    int sortBlocks;           // sort tiles that fit pairCap: ceil(pairCap / kSortChunk)
+    int radixPasses;          // 8-bit digit passes the bin numbers need (0 for one bin)
+    int* radix;               // [pass][256] digit counts, [pass] tile tickets, then at kRadixHdr
+                              // the look-back descriptors [pass][tile][256]
+    int* keyB;                // the sort's second key buffer
     int* binStart;            // first position of each bin's list; [nBins] = total
-    int* binTri;              // triangles of each bin, in submission order
+    int* binTri;              // the sort's second triangle buffer
+    const int* sortedTri;     // triangles of each bin, in submission order (binTri or pairTri)
     int* status;              // [0] overflow flag, [1] pairs needed, [2] sort blocks in use,
                               // [3] overflowing pass, [4..5] fragments tested, [6..7] passed,
                               // [8..9] pairs binned (u64)
@@ -107,10 +110,13 @@ struct PassParams {
     int passSeq;              // recorded in status[3] when this pass overflows
 };
 
-constexpr int kSortChunk = 4096;   // pairs per stable-sort block
+constexpr int kSortChunk = 4096;   // pairs per sort tile
+constexpr int kRadixDigits = 256;
+constexpr int kRadixMaxPasses = 3;  // bin numbers below 2^24
+constexpr int kRadixHdr = 1024;     // ints before the descriptors (counts + tickets, padded)
 
 // Kernel families timed by the profiler (ps3d_profile_*).
-enum KernelId { K_SETUP, K_SCAN, K_EMIT, K_HIST, K_SCATTER, K_RASTER, K_SHADE, K_FILL, K_COUNT };
+enum KernelId { K_SETUP, K_SCAN, K_EMIT, K_BOUNDS, K_SORT, K_RASTER, K_SHADE, K_FILL, K_COUNT };
 
 // CUDA-event brackets around kernel launches, on the launching stream.
 struct Prof {

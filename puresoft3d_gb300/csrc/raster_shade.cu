@@ -92,12 +92,12 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(PassParams P)
     float4 rec[4];
     int recTid = -1, nextIdx = -1;
     if (start + tid < end) {
-        recTid = P.binTri[start + tid];
+        recTid = P.sortedTri[start + tid];
         const float4* src = (const float4*)(P.tris + recTid);
 #pragma unroll
         for (int k = 0; k < 4; k++) rec[k] = __ldg(src + k);
     }
-    if (start + kChunk + tid < end) nextIdx = P.binTri[start + kChunk + tid];
+    if (start + kChunk + tid < end) nextIdx = P.sortedTri[start + kChunk + tid];
 
     unsigned long long tested = 0, passed = 0;
     const int qs = warp * Q, qe = qs + Q - 1;  // this thread's columns (bin-relative)
@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(PassParams P)
 #pragma unroll
             for (int k = 0; k < 4; k++) rec[k] = __ldg(src + k);
         }
-        nextIdx = (chunk + 2 * kChunk + tid < end) ? P.binTri[chunk + 2 * kChunk + tid] : -1;
+        nextIdx = (chunk + 2 * kChunk + tid < end) ? P.sortedTri[chunk + 2 * kChunk + tid] : -1;
         int inc = cnt;  // block-wide exclusive scan of the row counts
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {

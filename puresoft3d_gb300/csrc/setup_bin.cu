@@ -254,6 +254,8 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(PassParams P)
 {
     __shared__ float sVary[kSetupThreads * 3 * kMaxVary];
     int t = blockIdx.x * kSetupThreads + threadIdx.x;
+    if (blockIdx.x == 0)  // the sort's digit counts and tile tickets start at zero
+        for (int i = threadIdx.x; i < kRadixHdr; i += kSetupThreads) P.radix[i] = 0;
     if (t < P.nTris) setup_triangle(P, t, sVary);
     if (!P.anyVary) return;
     __syncthreads();
@@ -364,9 +366,13 @@ __global__ void k_scan_down(const int* in, int* out, int n, const int* nPtr, con
 
 // Writes the (bin, triangle) pairs.  If they would not fit, raises the
 // overflow flag instead; every later kernel of the flush then does nothing
-// and the host re-runs the pass with room for status[1] pairs.
-__global__ void k_emit(PassParams P)
+// and the host re-runs the pass with room for status[1] pairs.  Beside the
+// pairs it counts their radix digits (the sort's global histograms, zeroed by
+// k_setup) and zeroes the look-back descriptors of the tiles the sort will
+// use.
+__global__ void __launch_bounds__(256) k_emit(PassParams P)
 {
+    __shared__ int sHist[kRadixMaxPasses][kRadixDigits];
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (P.status[0]) return;
     int total = P.pairOffset[P.nTris];
@@ -380,178 +386,185 @@ __global__ void k_emit(PassParams P)
         }
         return;
     }
+    const int tiles = (total + kSortChunk - 1) / kSortChunk;
     if (t == 0) {
-        P.status[2] = (total + kSortChunk - 1) / kSortChunk;
+        P.status[2] = tiles;
         atomicAdd((unsigned long long*)(P.status + 8), (unsigned long long)total);
     }
-    if (t >= P.nTris) return;
-    int count = P.pairCount[t];
-    if (!count) return;
-    int4 r = P.rect[t];
-    int o = P.pairOffset[t];
-    for (int by = r.z; by <= r.w; by++)
-        for (int bx = r.x; bx <= r.y; bx++) {
-            P.pairKey[o] = by * P.binsX + bx;
-            P.pairTri[o] = t;
-            o++;
+    const int passes = P.radixPasses;
+    {
+        unsigned* desc = (unsigned*)P.radix + kRadixHdr;
+        size_t perPass = (size_t)tiles * kRadixDigits;
+        size_t stride = (size_t)gridDim.x * blockDim.x;
+        for (size_t i = t; i < passes * perPass; i += stride) {
+            size_t ps = i / perPass;
+            desc[ps * P.sortBlocks * kRadixDigits + (i - ps * perPass)] = 0u;
         }
-}
-
-// Stable counting sort of the pairs by bin.  Sort block b covers pairs
-// [b*kSortChunk, (b+1)*kSortChunk).  k_hist counts each bin's pairs in the
-// block (hist[b][bin]); k_colscan turns each bin's column into exclusive
-// prefixes over blocks and totals; a scan of the totals gives each bin's
-// first position; k_scatter places every pair at its bin start + its block's
-// prefix + its rank among earlier same-bin pairs of the block.  Both passes
-// stage the block's keys in shared memory and rank them with one warp in
-// submission order (__match_any_sync per 32 keys).
-constexpr int kSortThreads = 256;
-
-__device__ __forceinline__ int sort_blocks(const PassParams& P)
-{
-    return (P.pairOffset[P.nTris] + kSortChunk - 1) / kSortChunk;
-}
-
-__global__ void __launch_bounds__(kSortThreads) k_hist(PassParams P)
-{
-    extern __shared__ int cnt[];
-    __shared__ int keys[kSortChunk];
-    if (P.status[0]) return;
-    int total = P.pairOffset[P.nTris];
-    int b = blockIdx.x;
-    if (b >= sort_blocks(P)) return;
-    int nBins = P.binsX * P.binsY;
-    int base = b * kSortChunk, n = min(kSortChunk, total - base);
-    for (int i = threadIdx.x; i < n; i += kSortThreads) keys[i] = P.pairKey[base + i];
-    // bins are counted in windows of P.binWindow (one shared counter each)
-    for (int lo = 0; lo < nBins; lo += P.binWindow) {
-        int nw = min(P.binWindow, nBins - lo);
-        __syncthreads();
-        for (int i = threadIdx.x; i < nw; i += kSortThreads) cnt[i] = 0;
-        __syncthreads();
-        if (threadIdx.x < 32) {
-            int lane = threadIdx.x;
-            for (int i0 = 0; i0 < n; i0 += 32) {
-                int i = i0 + lane;
-                int key = i < n ? keys[i] - lo : -1;
-                bool in = i < n && key >= 0 && key < nw;
-                if (!in) key = -1 - lane;
-                unsigned peers = __match_any_sync(0xffffffffu, key);
-                if (in && lane == __ffs(peers) - 1) cnt[key] += __popc(peers);
-                __syncwarp();
-            }
-        }
-        __syncthreads();
-        for (int i = threadIdx.x; i < nw; i += kSortThreads) P.binHist[(size_t)b * nBins + lo + i] = cnt[i];
     }
-}
-
-// Per bin: exclusive prefix of its counts over the sort blocks (in place) and
-// the bin's total into binStart[bin].  A block takes 32 consecutive bins
-// (lane = bin, so every row read is one coalesced 128-byte line); its 8 warps
-// take contiguous runs of sort blocks, add their runs, exchange run totals,
-// then write the prefixes.
-constexpr int kColScanWarps = 8;
-
-__global__ void __launch_bounds__(32 * kColScanWarps) k_colscan(PassParams P)
-{
-    __shared__ int runTotal[kColScanWarps][32];
-    if (P.status[0]) return;
-    int nBins = P.binsX * P.binsY;
-    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    int bin = blockIdx.x * 32 + lane;
-    int nb = sort_blocks(P);
-    int per = (nb + kColScanWarps - 1) / kColScanWarps;
-    int b0 = warp * per, b1 = min(nb, b0 + per);
-    int sum = 0;
-    if (bin < nBins)
-        for (int b = b0; b < b1; b++) sum += P.binHist[(size_t)b * nBins + bin];
-    runTotal[warp][lane] = sum;
+    for (int i = threadIdx.x; i < kRadixMaxPasses * kRadixDigits; i += blockDim.x) (&sHist[0][0])[i] = 0;
     __syncthreads();
-    int run = 0, total = 0;
-    for (int w = 0; w < kColScanWarps; w++) {
-        int v = runTotal[w][lane];
-        if (w < warp) run += v;
-        total += v;
-    }
-    if (bin >= nBins) return;
-    for (int b = b0; b < b1; b++) {
-        int* h = P.binHist + (size_t)b * nBins + bin;
-        int v = *h;
-        *h = run;
-        run += v;
-    }
-    if (warp == 0) P.binStart[bin] = total;
-}
-
-// Exclusive scan of the bin totals in one block; binStart[nBins] = total.
-__global__ void __launch_bounds__(1024) k_binscan(PassParams P)
-{
-    __shared__ int warpSums[32];
-    __shared__ int carry;
-    if (P.status[0]) return;
-    int nBins = P.binsX * P.binsY;
-    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    for (int base = 0; base < nBins; base += 1024) {
-        int i = base + threadIdx.x;
-        int v = i < nBins ? P.binStart[i] : 0;
-        int inc = warp_incl_scan(v);
-        if (lane == 31) warpSums[wid] = inc;
-        __syncthreads();
-        if (wid == 0) warpSums[lane] = warp_incl_scan(warpSums[lane]);
-        __syncthreads();
-        int ex = carry + (wid ? warpSums[wid - 1] : 0) + inc - v;
-        int tot = warpSums[31];
-        __syncthreads();
-        if (i < nBins) P.binStart[i] = ex;
-        if (threadIdx.x == 0) carry += tot;
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) P.binStart[nBins] = carry;
-}
-
-__global__ void __launch_bounds__(kSortThreads) k_scatter(PassParams P)
-{
-    extern __shared__ int cnt[];
-    __shared__ int keys[kSortChunk];
-    __shared__ int tris[kSortChunk];
-    if (P.status[0]) return;
-    int total = P.pairOffset[P.nTris];
-    int b = blockIdx.x;
-    if (b >= sort_blocks(P)) return;
-    int nBins = P.binsX * P.binsY;
-    int base = b * kSortChunk, n = min(kSortChunk, total - base);
-    for (int i = threadIdx.x; i < n; i += kSortThreads) {
-        keys[i] = P.pairKey[base + i];
-        tris[i] = P.pairTri[base + i];
-    }
-    for (int lo = 0; lo < nBins; lo += P.binWindow) {
-        int nw = min(P.binWindow, nBins - lo);
-        __syncthreads();
-        for (int i = threadIdx.x; i < nw; i += kSortThreads)
-            cnt[i] = P.binStart[lo + i] + P.binHist[(size_t)b * nBins + lo + i];
-        __syncthreads();
-        if (threadIdx.x < 32) {
-            int lane = threadIdx.x;
-            unsigned lt = (1u << lane) - 1u;
-            for (int i0 = 0; i0 < n; i0 += 32) {
-                int i = i0 + lane;
-                int key = i < n ? keys[i] - lo : -1;
-                bool in = i < n && key >= 0 && key < nw;
-                if (!in) key = -1 - lane;
-                unsigned peers = __match_any_sync(0xffffffffu, key);
-                int pos = in ? cnt[key] + __popc(peers & lt) : 0;
-                __syncwarp();
-                if (in) {
-                    P.binTri[pos] = tris[i];
-                    if (lane == __ffs(peers) - 1) cnt[key] += __popc(peers);
+    if (t < P.nTris) {
+        int count = P.pairCount[t];
+        if (count) {
+            int4 r = P.rect[t];
+            int o = P.pairOffset[t];
+            for (int by = r.z; by <= r.w; by++)
+                for (int bx = r.x; bx <= r.y; bx++) {
+                    int key = by * P.binsX + bx;
+                    P.pairKey[o] = key;
+                    P.pairTri[o] = t;
+                    o++;
+                    for (int ps = 0; ps < passes; ps++) atomicAdd(&sHist[ps][(key >> (8 * ps)) & 255], 1);
                 }
-                __syncwarp();
-            }
         }
     }
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * kRadixDigits; i += blockDim.x) {
+        int v = (&sHist[0][0])[i];
+        if (v) atomicAdd(P.radix + i, v);
+    }
+}
+
+// Stable LSD radix sort of the pairs by bin, 8 bits per pass, one kernel per
+// pass ("one sweep": each tile ranks its keys, publishes its per-digit counts
+// and finds its per-digit prefix over earlier tiles by decoupled look-back).
+//
+// A tile is kSortChunk consecutive pairs; warp w of the block takes pairs
+// [w*512, (w+1)*512) of it in 16 groups of 32 and ranks each key among the
+// equal digits before it (__match_any_sync per group, a running per-warp
+// count per digit), so ranks follow input order and the sort is stable.
+// Tiles are numbered by an atomic ticket taken when the block starts, so a
+// tile only waits for tiles whose blocks are already running; each wait is
+// bounded (on expiry the pass raises status[0] = 2 and stops).
+//
+// Descriptor word: flag (bits 30-31: 0 not ready, 1 tile count, 2 inclusive
+// prefix) | value (bits 0-29).
+constexpr int kSortThreads = 256;
+constexpr int kSortWarps = kSortThreads / 32;
+constexpr int kSortGroups = kSortChunk / kSortThreads;  // 32-key groups per warp
+constexpr unsigned kFlagCount = 1u << 30, kFlagPrefix = 2u << 30, kValueMask = (1u << 30) - 1;
+constexpr int kLookbackSpins = 1 << 22;
+
+__global__ void __launch_bounds__(kSortThreads) k_onesweep(PassParams P, int pass, const int* __restrict__ inKey,
+                                                           const int* __restrict__ inTri, int* __restrict__ outKey,
+                                                           int* __restrict__ outTri)
+{
+    __shared__ int sTicket;
+    __shared__ int sWarpCnt[kSortWarps][kRadixDigits];
+    __shared__ int sBase[kRadixDigits];
+    __shared__ int sScan[kSortWarps];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0)  // one read of the flag for the whole block (it may change while the pass runs)
+        sTicket = P.status[0] ? -1 : atomicAdd(P.radix + kRadixMaxPasses * kRadixDigits + pass, 1);
+    for (int i = tid; i < kSortWarps * kRadixDigits; i += kSortThreads) (&sWarpCnt[0][0])[i] = 0;
+    __syncthreads();
+    const int tile = sTicket;
+    if (tile < 0) return;
+    const int total = P.pairOffset[P.nTris];
+    if (tile * kSortChunk >= total) return;
+    const int shift = 8 * pass;
+    const unsigned lt = (1u << lane) - 1u;
+    const int w0 = tile * kSortChunk + warp * (kSortChunk / kSortWarps);
+
+    int key[kSortGroups], tri[kSortGroups], rank[kSortGroups];
+#pragma unroll
+    for (int g = 0; g < kSortGroups; g++) {
+        int i = w0 + g * 32 + lane;
+        key[g] = i < total ? __ldg(inKey + i) : -1;
+        tri[g] = i < total ? __ldg(inTri + i) : 0;
+    }
+#pragma unroll
+    for (int g = 0; g < kSortGroups; g++) {
+        bool valid = key[g] >= 0;
+        int d = valid ? (key[g] >> shift) & 255 : -1 - lane;
+        unsigned peers = __match_any_sync(0xffffffffu, d);
+        int base = valid ? sWarpCnt[warp][d] : 0;
+        rank[g] = base + __popc(peers & lt);
+        __syncwarp();
+        if (valid && lane == __ffs(peers) - 1) sWarpCnt[warp][d] = base + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+
+    // thread = digit: offsets of the warps within the tile, the tile's count
+    const int d = tid;
+    int count = 0;
+#pragma unroll
+    for (int w = 0; w < kSortWarps; w++) {
+        int v = sWarpCnt[w][d];
+        sWarpCnt[w][d] = count;
+        count += v;
+    }
+    unsigned* desc = (unsigned*)P.radix + kRadixHdr + ((size_t)pass * P.sortBlocks) * kRadixDigits;
+    volatile unsigned* mine = desc + (size_t)tile * kRadixDigits + d;
+    int prefix = 0;
+    if (tile == 0) {
+        *mine = kFlagPrefix | (unsigned)count;
+    } else {
+        *mine = kFlagCount | (unsigned)count;
+        int j = tile - 1, spins = 0;
+        while (true) {
+            unsigned v = *(volatile unsigned*)(desc + (size_t)j * kRadixDigits + d);
+            unsigned f = v & ~kValueMask;
+            if (f == 0u) {
+                if (++spins > kLookbackSpins) {
+                    atomicExch(P.status, 2);
+                    __threadfence();  // the flag is visible before the prefix below
+                    break;
+                }
+                __nanosleep(32);
+                continue;
+            }
+            prefix += (int)(v & kValueMask);
+            if (f == kFlagPrefix) break;
+            j--;
+        }
+        *mine = kFlagPrefix | (unsigned)(prefix + count);
+    }
+    // global start of digit d: exclusive scan of the digit counts
+    int g = P.radix[pass * kRadixDigits + d];
+    int inc = g;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int n = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += n;
+    }
+    if (lane == 31) sScan[warp] = inc;
+    __syncthreads();
+    int wsum = 0;
+    for (int w = 0; w < warp; w++) wsum += sScan[w];
+    sBase[d] = wsum + inc - g + prefix;
+    __threadfence();
+    __syncthreads();
+    if (*(volatile int*)P.status) return;  // a wait expired somewhere: prefixes may be wrong
+#pragma unroll
+    for (int gi = 0; gi < kSortGroups; gi++) {
+        if (key[gi] < 0) continue;
+        int dg = (key[gi] >> shift) & 255;
+        int pos = sBase[dg] + sWarpCnt[warp][dg] + rank[gi];
+        if ((unsigned)pos >= (unsigned)total) continue;  // only reachable after an expired wait
+        outKey[pos] = key[gi];
+        outTri[pos] = tri[gi];
+    }
+}
+
+// binStart[b] = first position of bin b in the sorted keys (a lower bound by
+// binary search, one thread per bin); binStart[nBins] = total.
+__global__ void k_bin_bounds(PassParams P, const int* __restrict__ keys)
+{
+    if (P.status[0]) return;
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    int nBins = P.binsX * P.binsY;
+    if (b > nBins) return;
+    int total = P.pairOffset[P.nTris];
+    int lo = 0, hi = total;
+    if (b == nBins) lo = total;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (__ldg(keys + mid) < b) lo = mid + 1;
+        else hi = mid;
+    }
+    P.binStart[b] = lo;
 }
 
 // ------------------------------------------------------------------ launches
@@ -572,22 +585,20 @@ void scan_exclusive(const int* in, int* out, int n, const int* nPtr, int nMax, i
 
 int scan_block_sums_needed(int nMax) { return ceil_div(nMax > 0 ? nMax : 1, kScanTile) + 1; }
 
-// Largest bin grid whose per-bin counters fit in one block's shared memory
-// (beside the staged keys).
-int max_bins() { return (227 * 1024 - 2 * kSortChunk * (int)sizeof(int) - 1024) / (int)sizeof(int); }
+int radix_passes(int nBins)
+{
+    int bits = 0;
+    while (bits < 31 && (1 << bits) < nBins) bits++;
+    return (bits + 7) / 8;
+}
+
+size_t radix_scratch_ints(int sortBlocks, int passes)
+{
+    return (size_t)kRadixHdr + (size_t)passes * sortBlocks * kRadixDigits;
+}
 
 void launch_setup_and_bin(const PassParams& P, int* scanTmp, cudaStream_t s, int& launches, Prof* pr)
 {
-    static bool attrs = false;
-    if (!attrs) {  // opt in to the largest dynamic allocation beside each kernel's static arrays
-        cudaFuncAttributes a;
-        cudaFuncGetAttributes(&a, k_hist);
-        cudaFuncSetAttribute(k_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024 - (int)a.sharedSizeBytes);
-        cudaFuncGetAttributes(&a, k_scatter);
-        cudaFuncSetAttribute(k_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             227 * 1024 - (int)a.sharedSizeBytes);
-        attrs = true;
-    }
     int nBins = P.binsX * P.binsY;
     pr->begin(K_SETUP, s);
     k_setup<<<ceil_div(P.nTris, kSetupThreads), kSetupThreads, 0, s>>>(P);
@@ -598,18 +609,22 @@ void launch_setup_and_bin(const PassParams& P, int* scanTmp, cudaStream_t s, int
     k_emit<<<ceil_div(P.nTris, 256), 256, 0, s>>>(P);
     pr->end(s);
     launches++;
-    size_t smem = (size_t)min(nBins, P.binWindow) * sizeof(int);
-    pr->begin(K_HIST, s);
-    k_hist<<<P.sortBlocks, kSortThreads, smem, s>>>(P);
+    const int* key = P.pairKey;
+    const int* tri = P.pairTri;
+    pr->begin(K_SORT, s);
+    for (int ps = 0; ps < P.radixPasses; ps++) {
+        int* oKey = (ps & 1) ? P.pairKey : P.keyB;
+        int* oTri = (ps & 1) ? P.pairTri : P.binTri;
+        k_onesweep<<<P.sortBlocks, kSortThreads, 0, s>>>(P, ps, key, tri, oKey, oTri);
+        key = oKey;
+        tri = oTri;
+        launches++;
+    }
     pr->end(s);
-    pr->begin(K_SCAN, s);
-    k_colscan<<<ceil_div(nBins, 32), 32 * kColScanWarps, 0, s>>>(P);
-    k_binscan<<<1, 1024, 0, s>>>(P);
+    pr->begin(K_BOUNDS, s);
+    k_bin_bounds<<<ceil_div(nBins + 1, 256), 256, 0, s>>>(P, key);
     pr->end(s);
-    pr->begin(K_SCATTER, s);
-    k_scatter<<<P.sortBlocks, kSortThreads, smem, s>>>(P);
-    pr->end(s);
-    launches += 4;
+    launches++;
 }
 
 }  // namespace ps3d

@@ -78,7 +78,7 @@ _SIGS = {
     "ps3d_profile_read": [_c_void_p, ctypes.POINTER(_c_int), ctypes.POINTER(ctypes.c_double)],
 }
 
-KERNELS = ["setup", "scan", "emit", "hist", "scatter", "raster", "shade", "fill"]
+KERNELS = ["setup", "scan", "emit", "bounds", "sort", "raster", "shade", "fill"]
 
 
 def library(path: str | None = None) -> ctypes.CDLL:

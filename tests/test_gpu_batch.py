@@ -92,12 +92,12 @@ def test_batched_command_buffer_replay(gpu_lib):
     p.close()
 
 
-def _small_soup(n, w, h, seed=11):
+def _small_soup(n, w, h, seed=11, size=0.02):
     """n small triangles scattered over the whole target at random depths."""
     from kat_scenes import _scene
     rng = np.random.default_rng(seed)
     c = rng.uniform(-1, 1, size=(n, 1, 2))
-    d = rng.uniform(-0.02, 0.02, size=(n, 3, 2))
+    d = rng.uniform(-size, size, size=(n, 3, 2))
     z = rng.uniform(-0.9, 0.9, size=(n, 3, 1))
     xy = c + d
     clip = np.concatenate([xy, z, np.ones((n, 3, 1))], axis=2).reshape(-1, 4)
@@ -105,16 +105,35 @@ def _small_soup(n, w, h, seed=11):
 
 
 @pytest.mark.gpu
-def test_bin_sort_in_windows(gpu_lib, monkeypatch):
-    """6144x4224 with 16-pixel bins: 50688 bins, more than one shared-memory
-    window of bin counters, so the sort runs in two windows."""
+@pytest.mark.parametrize("bin_w,passes", [(16, 2), (8, 3)])
+def test_bin_sort_large_grids(gpu_lib, bin_w, passes):
+    """6144x4224: 50688 bins of 16 columns (16-bit bin numbers, two radix
+    passes) or 101376 bins of 8 columns (17 bits, three passes)."""
     from common import assert_depth_exact, render
     from puresoft3d_gb300.pipeline import PuresoftPipeline
     scene = _small_soup(3000, 6144, 4224)
-    monkeypatch.setenv("PS3D_BIN_W", "16")
-    gpu = render(PuresoftPipeline(scene.width, scene.height), scene)
+    bins = -(-6144 // bin_w) * -(-4224 // 32)
+    assert (bins - 1).bit_length() > 8 * (passes - 1)
+    g = PuresoftPipeline(scene.width, scene.height)
+    g.setBinWidth(bin_w)
+    gpu = render(g, scene)
     ora = render(OraclePipeline(scene.width, scene.height), scene)
     assert (gpu["depth"] < 1.0).sum() > 100000
     assert_depth_exact(gpu["depth"], ora["depth"], scene.name)
     mx, mean = colour_diff(gpu["colour"], ora["colour"])
     assert mx <= 1, "colour differs by up to %d LSB (mean %.4f)" % (mx, mean)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("bin_w", [8, 32])
+def test_single_bin_and_tiny_targets(gpu_lib, bin_w):
+    """A 24x20 target: one bin at 32 columns (nothing to sort), three at 8."""
+    from common import assert_depth_exact, render
+    from puresoft3d_gb300.pipeline import PuresoftPipeline
+    scene = _small_soup(40, 24, 20, seed=5, size=0.5)
+    g = PuresoftPipeline(scene.width, scene.height)
+    g.setBinWidth(bin_w)
+    gpu = render(g, scene)
+    ora = render(OraclePipeline(scene.width, scene.height), scene)
+    assert_depth_exact(gpu["depth"], ora["depth"], scene.name)
+    assert colour_diff(gpu["colour"], ora["colour"])[0] <= 1
