@@ -27,6 +27,7 @@ pixel and does not shard); value = all ranks' frames / the slowest rank's time.
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import os
 import statistics
@@ -56,6 +57,10 @@ CONFIGS = {
                args={}),
     "c3s": dict(desc="c3s (profiling case): 1920x1080 LIT3, 128 meshes, ~500k triangles, 4x2048^2 trilinear",
                 args={}),
+    "c5": dict(desc="c5: serving -- 2000 seeded jobs, Poisson arrivals, resolution uniform over 256^2, 512^2, "
+                    "1024^2, 1920x1080; meshes from a resident pool of 128 (1k-500k triangles log-uniform), 64 "
+                    "resident 512^2 mip chains, LIT3; continuous batching into two 4096^2 atlas slots",
+               args={}),
     "c4": dict(desc="c4: 4096 independent 128x128 views (own seeded mesh, 100-5000 triangles log-uniform, own "
                     "orbit camera, own 256^2 texture, LIT1), batched into tiles of an 8192^2 atlas in one pass",
                args={}),
@@ -286,6 +291,67 @@ def run_c4(args):
     return line
 
 
+def run_c5(args):
+    """Config 5: the request loop with continuous batching against the
+    one-request-at-a-time plain loop, on the same seeded job stream: closed
+    loop (all jobs queued at t=0: capacity) and open loop (Poisson arrivals
+    at 80 % of each arm's capacity: latency under load)."""
+    from puresoft3d_gb300 import scenes as S
+    from puresoft3d_gb300.serving import PlainLoop, RenderServer, summarize
+    pool = S.scene_c5_pool()
+    base = S.c5_jobs(pool, n=args.jobs, rate=1.0)
+    bw = args.bin_width or 16
+    srv = RenderServer(pool, atlas=(4096, 4096), slots=2, bin_width=bw)
+    plain = PlainLoop(pool, bin_width=bw)
+    warm = base[:64]
+    srv.serve(warm, realtime=False)
+    plain.serve(warm, realtime=False)
+
+    def at_rate(rate):
+        return [dataclasses.replace(j, arrival=j.arrival / rate) for j in base]
+
+    clocks = ClockSampler()
+    clocks.start()
+    cap_b = summarize(srv.serve(base, realtime=False), realtime=False)
+    cap_p = summarize(plain.serve(base, realtime=False), realtime=False)
+    loads = {}
+    for name, cap in (("batched_capacity", cap_b["images_per_s"]), ("plain_capacity", cap_p["images_per_s"])):
+        rate = 0.8 * cap
+        jobs = at_rate(rate)
+        loads[name] = {"rate_jobs_per_s": round(rate, 1),
+                       "batched": {k: round(v, 3) for k, v in summarize(srv.serve(jobs)).items()},
+                       "plain": {k: round(v, 3) for k, v in summarize(plain.serve(jobs)).items()}}
+    clk = clocks.stop()
+    d2h = sum(j.width * j.height * 4 for j in base) / len(base)
+    cpu = cpu_baseline_jobs(budget_s=args.cpu_budget, pool=pool, jobs=base) if (
+        RANK == 0 and not args.no_cpu_baseline) else None
+    line = {
+        "metric": "images/s", "value": round(cap_b["images_per_s"], 2), "unit": "images/s", "n_gpus": WORLD,
+        "steps": len(base), "warmup": len(warm), "ms_per_step": round(1e3 / cap_b["images_per_s"], 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded job stream over a seeded resident pool)",
+        "config": {"workload": CONFIGS["c5"]["desc"], "jobs": len(base), "bin_width": bw,
+                   "pool_triangles": sum(pool.info["mesh_triangles"]),
+                   "l2": "inputs (9.7M resident triangles, 1.2 GB of vertices) exceed L2",
+                   "parallelism": "replicas" if WORLD > 1 else "single GPU"},
+        "closed_loop": {"batched": {k: round(v, 3) for k, v in cap_b.items()},
+                        "plain": {k: round(v, 3) for k, v in cap_p.items()}},
+        "open_loop": loads,
+        "batched_over_plain": round(cap_b["images_per_s"] / cap_p["images_per_s"], 2),
+        "gpu_launches": None,
+        "e2e": {"value": round(cap_b["images_per_s"], 2), "unit": "images/s",
+                "h2d_bytes_per_step": None, "d2h_bytes_per_step": int(d2h),
+                "note": "the serving loop is end to end: jobs enter from the host, images land in pinned host memory"},
+        "roofline": None,
+        "clocks": clk,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    srv.close()
+    plain.close()
+    return line
+
+
 def cpu_baseline_views(budget_s=15.0, threads=None, sample_views=256):
     """Config 4 on the host cores: the reference pipeline (or its oracle
     port) rendering the first views of the same seeded set one at a time in a
@@ -455,9 +521,27 @@ def run_ours(args):
     }
     if RANK == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(scene, budget_s=args.cpu_budget)
+        line["colour_error_vs_fp64"] = shading_error(scene)
     cb.destroy()
     pipe.close()
     return line
+
+
+def shading_error(scene):
+    """The frame's shaded fragments: FP32 pre-truncation colour against an
+    FP64 re-shade of the same fragments, per channel in 8-bit units (from the
+    oracle, whose colour the GPU matches bit for bit)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from puresoft3d_gb300 import scenes as S
+    from cpu_backends import OraclePipeline
+    o = OraclePipeline(scene.width, scene.height, os.cpu_count() or 1)
+    o.measureColourError()
+    S.replay_setup(scene, o)
+    S.replay_frame(scene, o)
+    e = o.colourError()
+    o.close()
+    return {"max": round(e["max"], 6), "mean": round(e["mean"], 9), "channels": e["channels"],
+            "channels_off_by_1_or_more": e["over_1"]}
 
 
 def cpu_baseline(scene, budget_s=15.0, threads=None):
@@ -489,9 +573,51 @@ def cpu_baseline(scene, budget_s=15.0, threads=None):
             "sample": "%d frames of the same workload in %.1f s" % (frames, el)}
 
 
+def cpu_baseline_jobs(budget_s=15.0, threads=None, pool=None, jobs=None):
+    """Config 5 on the host cores: the reference pipeline (or its oracle
+    port) rendering the seeded jobs one at a time, one pipeline per
+    resolution, for a bounded time."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from puresoft3d_gb300 import scenes as S
+    from cpu_backends import OraclePipeline, RefPipeline
+    threads = threads or os.cpu_count() or 1
+    pool = pool or S.scene_c5_pool()
+    jobs = jobs or S.c5_jobs(pool, n=2000, rate=1.0)
+    use_ref = os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libps3dref.so")) and os.uname().machine == "x86_64"
+    if use_ref:
+        os.environ["PS3D_REF_THREADS"] = str(threads)
+    pipes = {}
+    for wh in S.C5_RESOLUTIONS:
+        p = RefPipeline(wh[0], wh[1], threads) if use_ref else OraclePipeline(wh[0], wh[1], threads)
+        S.replay_setup(pool, p)
+        pipes[wh] = p
+    n, t0 = 0, time.perf_counter()
+    while True:
+        j = jobs[n % len(jobs)]
+        p = pipes[(j.width, j.height)]
+        S.replay_ops([("clearDepth", 1.0), ("clearColour", 0xFF000000)] + pool.info["common"] + j.ops, p)
+        p.readColour()
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or n >= len(jobs):
+            break
+    for p in pipes.values():
+        p.close()
+    return {"value": round(n / el, 3), "unit": "images/s", "cores": threads,
+            "kind": "reference" if use_ref else "port",
+            "sample": "the first %d jobs of the seeded stream, one at a time, in %.1f s" % (n, el)}
+
+
 def run_reference(args):
     if args.config == "c4":
         return run_reference_views(args)
+    if args.config == "c5":
+        v = cpu_baseline_jobs(budget_s=args.cpu_budget)
+        return {"impl": "reference", "metric": "images/s", "value": v["value"], "unit": "images/s",
+                "n_gpus": WORLD, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 / v["value"], 3),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "config": {"workload": CONFIGS["c5"]["desc"]}, "cpu_baseline": v,
+                "e2e": {"value": v["value"], "unit": "images/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     scene = make_scene(args.config)
     per = max(2.0, args.cpu_budget / max(args.steps, 1))
     vals = []
@@ -571,6 +697,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ncu-frames", type=int, default=0, help="render N frames for a profiler and exit")
     ap.add_argument("--views", type=int, default=4096, help="config 4: number of views")
+    ap.add_argument("--jobs", type=int, default=2000, help="config 5: number of jobs")
     ap.add_argument("--bin-width", type=int, default=0, choices=[0, 8, 16, 32],
                     help="fix the bin width instead of autotuning it")
     args = ap.parse_args()
@@ -584,7 +711,7 @@ def main():
         print(json.dumps(run_reference(args)), flush=True)
         return
     init_dist()
-    line = run_c4(args) if args.config == "c4" else run_ours(args)
+    line = {"c4": run_c4, "c5": run_c5}.get(args.config, run_ours)(args)
     if RANK == 0:
         print(json.dumps(line), flush=True)
 

@@ -230,6 +230,16 @@ int ps3d_read_depth(ps3d_pipeline* p, void* out);
  * to device memory at devDst, ordered after the draws recorded before it
  * (like a read-back, but asynchronous and on the device). */
 int ps3d_read_colour_device(ps3d_pipeline* p, void* devDst);
+/* Records a copy of the colour rectangle (x, y, width, height; pixels from
+ * the bottom-left corner, as ps3d_set_viewport_rect) to dst -- device or
+ * host memory (pinned for an asynchronous copy) -- rows top-down, dstPitch
+ * bytes apart, ordered after the draws recorded before it.  With
+ * ps3d_set_viewport_rect this reads out one view of a batched pass. */
+int ps3d_copy_colour_rect(ps3d_pipeline* p, int x, int y, int width, int height, void* dst, size_t dstPitch);
+/* 1 when all launched work of the pipeline has completed, 0 while some is
+ * still running (cudaStreamQuery; no wait, no verification: ps3d_finish
+ * verifies and, after a bin-list overflow, re-runs -- copies included). */
+int ps3d_query(ps3d_pipeline* p);
 /* Device address of the colour buffer. */
 int ps3d_colour_device_ptr(ps3d_pipeline* p, void** out);
 /* The pipeline's CUDA stream (cudaStream_t). */

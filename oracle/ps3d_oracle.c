@@ -114,6 +114,9 @@ struct ps3do {
     o_tasklist* lists; /* one per worker */
     long long tested, passed;
     long long spanHist[32]; /* spans by floor(log2(x2 - x1 + 1)) */
+    int errOn;              /* measure the FP32 shading error against an FP64 re-shade */
+    double errMax, errSum;
+    long long errN, errOver;
     /* worker pool */
     pthread_t* th;
     pthread_mutex_t mu;
@@ -398,6 +401,16 @@ int ps3do_read_depth(ps3do* p, void* out)
     return 0;
 }
 
+void ps3do_set_colour_error(ps3do* p, int on) { p->errOn = on != 0; }
+
+void ps3do_colour_error(ps3do* p, double* maxErr, double* meanErr, long long* channels, long long* over1)
+{
+    *maxErr = p->errMax;
+    *meanErr = p->errN ? p->errSum / (double)p->errN : 0.0;
+    *channels = p->errN;
+    *over1 = p->errOver;
+}
+
 long long ps3do_fragments_tested(ps3do* p) { return p->tested; }
 void ps3do_span_histogram(ps3do* p, long long* out) { memcpy(out, p->spanHist, sizeof p->spanHist); }
 long long ps3do_fragments_passed(ps3do* p) { return p->passed; }
@@ -624,6 +637,47 @@ static void fp_def01(const fp_state* s, const float* in, uint8_t* bgra)
     bgra[1] = (uint8_t)(int)c[1];
     bgra[2] = (uint8_t)(int)c[2];
     bgra[3] = 0;
+}
+
+/* Per-thread error accumulator of the FP32 vs FP64 shading comparison. */
+typedef struct {
+    double max, sum;
+    long long n, over;
+} err_acc;
+
+/* The scene shaders' pre-truncation FP32 colour against the FP64 re-shade of
+   the same fragment; |difference| per colour channel. */
+static void shade_error(const ps3do* p, const fp_state* s, const float* in, err_acc* e)
+{
+    float pre[3];
+    double ref[3];
+    uint8_t bgra[4];
+    switch (p->fp) {
+    case FP_LIT1: {
+        sr_level t = level_of(s->tex);
+        sr_shade_lit1_pre(&t, s->light, s->cam, in, in + 4, in + 8, pre, bgra);
+        srd_shade_lit13(&t, 1, 0, 0.0, s->light, s->cam, in, in + 4, in + 8, ref);
+        break;
+    }
+    case FP_LIT3:
+        sr_shade_lit3_pre(s->chainA, s->levelsA, s->lodScale, s->light, s->cam, in, in + 4, in + 8, pre, bgra);
+        srd_shade_lit13(s->chainA, s->levelsA, 1, s->lodScale, s->light, s->cam, in, in + 4, in + 8, ref);
+        break;
+    case FP_LIT2:
+        sr_shade_lit2_pre(s->chainA, s->levelsA, s->chainN, s->levelsN, s->shadow, s->shadowSize, s->shadowScan,
+                          s->lodScale, s->bias, s->light, s->cam, in, pre, bgra);
+        srd_shade_lit2(s->chainA, s->levelsA, s->chainN, s->levelsN, s->shadow, s->shadowSize, s->shadowScan,
+                       s->lodScale, s->bias, s->light, s->cam, in, ref);
+        break;
+    default: return;
+    }
+    for (int k = 0; k < 3; k++) {
+        double d = fabs((double)pre[k] - ref[k]);
+        if (d > e->max) e->max = d;
+        e->sum += d;
+        e->n++;
+        if (d >= 1.0) e->over++;
+    }
 }
 
 /* Returns 1 if the processor wrote colour (the reference FPs never discard). */
@@ -870,7 +924,7 @@ static void cursor_next(o_cursor* c)
 }
 
 /* fragmentThread's DRAW branch (fragthrd.cpp:160-252) for one task. */
-static void run_task(draw_ctx* d, const o_task* t, long long* tested, long long* passed)
+static void run_task(draw_ctx* d, const o_task* t, long long* tested, long long* passed, err_acc* e)
 {
     ps3do* p = d->p;
     int nv = d->nv, behav = p->behavior;
@@ -895,6 +949,7 @@ static void run_task(draw_ctx* d, const o_task* t, long long* tested, long long*
             uint8_t bgra[4];
             (*passed)++;
             if (run_fp(p, &d->fs, frag, bgra) && !cc.overflow) memcpy(cc.rowEntry + (size_t)cc.col * 4, bgra, 4);
+            if (p->errOn) shade_error(p, &d->fs, frag, e);
             if ((behav & BEHAVIOR_UPDATE_DEPTH) && !dc.overflow) memcpy(dc.rowEntry + (size_t)dc.col * 4, &z, 4);
         }
         cursor_next(&cc);
@@ -905,7 +960,17 @@ static void run_task(draw_ctx* d, const o_task* t, long long* tested, long long*
 static void run_list(draw_ctx* d, int t, long long* tested, long long* passed)
 {
     o_tasklist* l = &d->p->lists[t];
-    for (size_t i = 0; i < l->n; i++) run_task(d, &l->items[i], tested, passed);
+    err_acc e = {0.0, 0.0, 0, 0};
+    for (size_t i = 0; i < l->n; i++) run_task(d, &l->items[i], tested, passed, &e);
+    if (e.n) {
+        ps3do* p = d->p;
+        if (p->threads > 1) pthread_mutex_lock(&p->mu);
+        if (e.max > p->errMax) p->errMax = e.max;
+        p->errSum += e.sum;
+        p->errN += e.n;
+        p->errOver += e.over;
+        if (p->threads > 1) pthread_mutex_unlock(&p->mu);
+    }
 }
 
 static void* worker(void* arg)

@@ -45,6 +45,13 @@ int ps3do_read_depth(ps3do* p, void* out);
    iterations, fragthrd.cpp:208) and fragments that passed it, since create. */
 long long ps3do_fragments_tested(ps3do* p);
 long long ps3do_fragments_passed(ps3do* p);
+/* Colour error of the scene shaders (LIT1/2/3): with measurement on, every
+   shaded fragment's pre-truncation FP32 colour is compared with an FP64
+   re-shade of the same fragment (same varyings, texels and shadow map);
+   max and mean |difference| per colour channel (in 8-bit units), the number
+   of channels compared and how many differed by 1 or more. */
+void ps3do_set_colour_error(ps3do* p, int on);
+void ps3do_colour_error(ps3do* p, double* maxErr, double* meanErr, long long* channels, long long* over1);
 /* Spans drawn since create, bucketed by floor(log2(length in pixels)). */
 void ps3do_span_histogram(ps3do* p, long long* out32);
 

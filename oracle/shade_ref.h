@@ -231,8 +231,8 @@ static inline float sr_pcf3x3(const float* map, int size, int scanlineFloats, co
    scene shaders.  albedo is BGRA (0..255), n the unit normal, L the unit
    direction towards the light, E the unit direction towards the eye, vis the
    lit fraction.  Writes BGRA8 with alpha 255. */
-static inline void sr_blinn_phong(const float albedo[4], const float* n, const float* L, const float* E, float vis,
-                                  uint8_t out[4])
+static inline void sr_blinn_phong_pre(const float albedo[4], const float* n, const float* L, const float* E,
+                                      float vis, float pre[3])
 {
     float Hv[3], ndl, ndh, spec, diff, s255;
     Hv[0] = E[0] + L[0];
@@ -246,17 +246,27 @@ static inline void sr_blinn_phong(const float albedo[4], const float* n, const f
     spec = ndl > 0.0f ? sr_pow32(ndh) : 0.0f;
     diff = 0.15f + 0.85f * (ndl * vis);
     s255 = 127.5f * (spec * vis);
-    out[0] = sr_to_u8(albedo[0] * diff + s255);
-    out[1] = sr_to_u8(albedo[1] * diff + s255);
-    out[2] = sr_to_u8(albedo[2] * diff + s255);
+    pre[0] = albedo[0] * diff + s255;
+    pre[1] = albedo[1] * diff + s255;
+    pre[2] = albedo[2] * diff + s255;
+}
+
+static inline void sr_blinn_phong(const float albedo[4], const float* n, const float* L, const float* E, float vis,
+                                  float pre[3], uint8_t out[4])
+{
+    sr_blinn_phong_pre(albedo, n, L, E, vis, pre);
+    out[0] = sr_to_u8(pre[0]);
+    out[1] = sr_to_u8(pre[1]);
+    out[2] = sr_to_u8(pre[2]);
     out[3] = 255;
 }
 
 /* Scene shader LIT1 (configs 1 and 4): bilinear REPEAT albedo, directional
    Lambert + Blinn-Phong (shininess 32).  Inputs are the DEF01 varyings
    (reference tex1light1.h:4-9): normal[4], worldPos[4], texcoord[4]. */
-static inline void sr_shade_lit1(const sr_level* tex, const float* lightDir, const float* camPos, const float* normal,
-                                 const float* worldPos, const float* texcoord, uint8_t out[4])
+static inline void sr_shade_lit1_pre(const sr_level* tex, const float* lightDir, const float* camPos,
+                                     const float* normal, const float* worldPos, const float* texcoord, float pre[3],
+                                     uint8_t out[4])
 {
     float albedo[4], n[3], E[3];
     sr_bilinear_bgra8(tex, texcoord[0], texcoord[1], albedo);
@@ -266,13 +276,13 @@ static inline void sr_shade_lit1(const sr_level* tex, const float* lightDir, con
     E[1] = camPos[1] - worldPos[1];
     E[2] = camPos[2] - worldPos[2];
     sr_normalize3(E);
-    sr_blinn_phong(albedo, n, lightDir, E, 1.0f, out);
+    sr_blinn_phong(albedo, n, lightDir, E, 1.0f, pre, out);
 }
 
 /* Scene shader LIT3 (config 3): LIT1 with a trilinear mip chain. */
-static inline void sr_shade_lit3(const sr_level* chain, int levels, float lodScale, const float* lightDir,
-                                 const float* camPos, const float* normal, const float* worldPos, const float* texcoord,
-                                 uint8_t out[4])
+static inline void sr_shade_lit3_pre(const sr_level* chain, int levels, float lodScale, const float* lightDir,
+                                     const float* camPos, const float* normal, const float* worldPos,
+                                     const float* texcoord, float pre[3], uint8_t out[4])
 {
     float albedo[4], n[3], E[3], dist, w;
     int level;
@@ -285,16 +295,17 @@ static inline void sr_shade_lit3(const sr_level* chain, int levels, float lodSca
     n[0] = normal[0]; n[1] = normal[1]; n[2] = normal[2];
     sr_normalize3(n);
     sr_normalize3(E);
-    sr_blinn_phong(albedo, n, lightDir, E, 1.0f, out);
+    sr_blinn_phong(albedo, n, lightDir, E, 1.0f, pre, out);
 }
 
 /* Scene shader LIT2 (config 2): trilinear albedo, tangent-space normal map
    (RGBA16F chain, same mip selection), 3x3 PCF shadow.  Varyings: normal[4],
    tangent[4] (w = handedness), worldPos[4], texcoord[4], shadowPos[4]. */
-static inline void sr_shade_lit2(const sr_level* albedoChain, int albedoLevels, const sr_level* normalChain,
-                                 int normalLevels, const float* shadowMap, int shadowSize, int shadowScanlineFloats,
-                                 float lodScale, float shadowBias, const float* lightDir, const float* camPos,
-                                 const float* varyings, uint8_t out[4])
+static inline void sr_shade_lit2_pre(const sr_level* albedoChain, int albedoLevels, const sr_level* normalChain,
+                                     int normalLevels, const float* shadowMap, int shadowSize,
+                                     int shadowScanlineFloats, float lodScale, float shadowBias,
+                                     const float* lightDir, const float* camPos, const float* varyings, float pre[3],
+                                     uint8_t out[4])
 {
     const float* nrm = varyings;
     const float* tan = varyings + 4;
@@ -324,7 +335,189 @@ static inline void sr_shade_lit2(const sr_level* albedoChain, int albedoLevels, 
     sr_normalize3(n);
     vis = sr_pcf3x3(shadowMap, shadowSize, shadowScanlineFloats, sp, shadowBias);
     sr_normalize3(E);
-    sr_blinn_phong(albedo, n, lightDir, E, vis, out);
+    sr_blinn_phong(albedo, n, lightDir, E, vis, pre, out);
+}
+
+static inline void sr_shade_lit1(const sr_level* tex, const float* lightDir, const float* camPos, const float* normal,
+                                 const float* worldPos, const float* texcoord, uint8_t out[4])
+{
+    float pre[3];
+    sr_shade_lit1_pre(tex, lightDir, camPos, normal, worldPos, texcoord, pre, out);
+}
+
+static inline void sr_shade_lit3(const sr_level* chain, int levels, float lodScale, const float* lightDir,
+                                 const float* camPos, const float* normal, const float* worldPos, const float* texcoord,
+                                 uint8_t out[4])
+{
+    float pre[3];
+    sr_shade_lit3_pre(chain, levels, lodScale, lightDir, camPos, normal, worldPos, texcoord, pre, out);
+}
+
+static inline void sr_shade_lit2(const sr_level* albedoChain, int albedoLevels, const sr_level* normalChain,
+                                 int normalLevels, const float* shadowMap, int shadowSize, int shadowScanlineFloats,
+                                 float lodScale, float shadowBias, const float* lightDir, const float* camPos,
+                                 const float* varyings, uint8_t out[4])
+{
+    float pre[3];
+    sr_shade_lit2_pre(albedoChain, albedoLevels, normalChain, normalLevels, shadowMap, shadowSize,
+                      shadowScanlineFloats, lodScale, shadowBias, lightDir, camPos, varyings, pre, out);
+}
+
+/* ------------------------------------------------------------------------
+   FP64 re-shade, for measuring the FP32 shaders' error only: the same
+   equations on the same fragment inputs (the FP32 varyings, the same texels
+   and shadow map), every operation in double.  Mip selection uses the same
+   piecewise-linear log2 (continuous across levels); texel addressing is the
+   same floor / wrap / clamp, applied to the double sample position. */
+
+static inline double srd_dot3(const double* a, const double* b) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+
+static inline void srd_normalize3(double* v)
+{
+    double s = srd_dot3(v, v), r;
+    if (!(s > 0.0)) { v[0] = v[1] = v[2] = 0.0; return; }
+    r = 1.0 / sqrt(s);
+    v[0] *= r;
+    v[1] *= r;
+    v[2] *= r;
+}
+
+static inline double srd_texel(const sr_level* t, int half16, int r, int c, int k)
+{
+    if (half16) return (double)sr_half2float(((const uint16_t*)(t->base + (size_t)r * t->scanline))[4 * c + k]);
+    return (double)t->base[(size_t)r * t->scanline + 4 * c + k];
+}
+
+static inline void srd_bilinear(const sr_level* t, int half16, double u, double v, double out[4])
+{
+    double fx = (double)t->width * u, fy = (double)t->height * v;
+    double x0f = floor(fx), y0f = floor(fy);
+    double ax = fx - x0f, ay = fy - y0f;
+    int ix, iy, c0, c1, r0, r1;
+    if (!(x0f > -2147483648.0 && x0f < 2147483647.0)) x0f = 0.0;
+    if (!(y0f > -2147483648.0 && y0f < 2147483647.0)) y0f = 0.0;
+    ix = (int)x0f;
+    iy = (int)y0f;
+    c0 = sr_wrap(ix, t->width);
+    c1 = sr_wrap(ix + 1, t->width);
+    r0 = sr_wrap(iy, t->height);
+    r1 = sr_wrap(iy + 1, t->height);
+    for (int k = 0; k < 4; k++) {
+        double a = srd_texel(t, half16, r0, c0, k), b = srd_texel(t, half16, r0, c1, k);
+        double c = srd_texel(t, half16, r1, c0, k), d = srd_texel(t, half16, r1, c1, k);
+        double top = a + (b - a) * ax, bot = c + (d - c) * ax;
+        out[k] = top + (bot - top) * ay;
+    }
+}
+
+static inline void srd_mip_select(double x, int* level, double* weight)
+{
+    int e;
+    double m;
+    if (!(x > 1.0)) { *level = 0; *weight = 0.0; return; }
+    m = frexp(x, &e); /* x = m * 2^e, m in [0.5, 1) */
+    *level = e - 1;
+    *weight = 2.0 * m - 1.0;
+}
+
+static inline void srd_trilinear(const sr_level* chain, int levels, int half16, int level, double w, double u,
+                                 double v, double out[4])
+{
+    double a[4], b[4];
+    if (level >= levels - 1) {
+        srd_bilinear(&chain[levels - 1], half16, u, v, out);
+        return;
+    }
+    srd_bilinear(&chain[level], half16, u, v, a);
+    srd_bilinear(&chain[level + 1], half16, u, v, b);
+    for (int k = 0; k < 4; k++) out[k] = a[k] + (b[k] - a[k]) * w;
+}
+
+static inline double srd_pcf3x3(const float* map, int size, int scanlineFloats, const float* spf, double bias)
+{
+    double sp[4] = {spf[0], spf[1], spf[2], spf[3]}, rw, nx, ny, nz, half, sx, sy;
+    int cx, cy, cnt = 0;
+    if (!(sp[3] > 0.0)) return 1.0;
+    rw = 1.0 / sp[3];
+    nx = sp[0] * rw;
+    ny = sp[1] * rw;
+    nz = sp[2] * rw;
+    if (!(nx >= -1.0 && nx <= 1.0 && ny >= -1.0 && ny <= 1.0)) return 1.0;
+    half = (double)(size / 2);
+    sx = half * nx + half;
+    sy = half * ny + half;
+    cx = (int)(sx + 0.5);
+    cy = (int)(sy + 0.5);
+    for (int dy = -1; dy <= 1; dy++)
+        for (int dx = -1; dx <= 1; dx++) {
+            int r = sr_clampi(cy + dy, size), c = sr_clampi(cx + dx, size);
+            if (nz - bias <= (double)map[(size_t)r * scanlineFloats + c]) cnt++;
+        }
+    return (double)cnt / 9.0;
+}
+
+static inline void srd_blinn_phong(const double albedo[4], const double* n, const double* L, const double* E,
+                                   double vis, double pre[3])
+{
+    double Hv[3] = {E[0] + L[0], E[1] + L[1], E[2] + L[2]}, ndl, ndh, spec, diff, s255, x2, x4, x8, x16;
+    srd_normalize3(Hv);
+    ndl = srd_dot3(n, L);
+    if (ndl < 0.0) ndl = 0.0;
+    ndh = srd_dot3(n, Hv);
+    if (ndh < 0.0) ndh = 0.0;
+    x2 = ndh * ndh;
+    x4 = x2 * x2;
+    x8 = x4 * x4;
+    x16 = x8 * x8;
+    spec = ndl > 0.0 ? x16 * x16 : 0.0;
+    diff = 0.15 + 0.85 * (ndl * vis);
+    s255 = 127.5 * (spec * vis);
+    for (int k = 0; k < 3; k++) pre[k] = albedo[k] * diff + s255;
+}
+
+/* lightDir/camPos/varyings as the FP32 shader receives them. */
+static inline void srd_shade_lit13(const sr_level* chain, int levels, int trilinear, double lodScale,
+                                   const float* lightDir, const float* camPos, const float* normal,
+                                   const float* worldPos, const float* texcoord, double pre[3])
+{
+    double albedo[4], n[3] = {normal[0], normal[1], normal[2]}, L[3] = {lightDir[0], lightDir[1], lightDir[2]};
+    double E[3] = {(double)camPos[0] - worldPos[0], (double)camPos[1] - worldPos[1], (double)camPos[2] - worldPos[2]};
+    if (trilinear) {
+        int level;
+        double w;
+        srd_mip_select(sqrt(srd_dot3(E, E)) * lodScale, &level, &w);
+        srd_trilinear(chain, levels, 0, level, w, texcoord[0], texcoord[1], albedo);
+    } else {
+        srd_bilinear(chain, 0, texcoord[0], texcoord[1], albedo);
+    }
+    srd_normalize3(n);
+    srd_normalize3(E);
+    srd_blinn_phong(albedo, n, L, E, 1.0, pre);
+}
+
+static inline void srd_shade_lit2(const sr_level* albedoChain, int albedoLevels, const sr_level* normalChain,
+                                  int normalLevels, const float* shadowMap, int shadowSize, int shadowScanlineFloats,
+                                  double lodScale, double shadowBias, const float* lightDir, const float* camPos,
+                                  const float* v, double pre[3])
+{
+    double N[3] = {v[0], v[1], v[2]}, T[3] = {v[4], v[5], v[6]}, B[3], nts[4], albedo[4], n[3], w, vis;
+    double L[3] = {lightDir[0], lightDir[1], lightDir[2]};
+    double E[3] = {(double)camPos[0] - v[8], (double)camPos[1] - v[9], (double)camPos[2] - v[10]};
+    int level;
+    srd_normalize3(N);
+    srd_normalize3(T);
+    B[0] = N[1] * T[2] - N[2] * T[1];
+    B[1] = N[2] * T[0] - N[0] * T[2];
+    B[2] = N[0] * T[1] - N[1] * T[0];
+    if (v[7] < 0.0f) { B[0] = -B[0]; B[1] = -B[1]; B[2] = -B[2]; }
+    srd_mip_select(sqrt(srd_dot3(E, E)) * lodScale, &level, &w);
+    srd_trilinear(albedoChain, albedoLevels, 0, level, w, v[12], v[13], albedo);
+    srd_trilinear(normalChain, normalLevels, 1, level, w, v[12], v[13], nts);
+    for (int k = 0; k < 3; k++) n[k] = (T[k] * nts[0] + B[k] * nts[1]) + N[k] * nts[2];
+    srd_normalize3(n);
+    vis = srd_pcf3x3(shadowMap, shadowSize, shadowScanlineFloats, v + 16, shadowBias);
+    srd_normalize3(E);
+    srd_blinn_phong(albedo, n, L, E, vis, pre);
 }
 
 #ifdef __cplusplus

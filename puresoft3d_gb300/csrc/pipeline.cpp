@@ -89,7 +89,9 @@ struct Programme {
 // one recorded command
 struct Command {
     enum Kind { DRAW, CLEAR_DEPTH, CLEAR_COLOUR, COPY_COLOUR } kind;
-    void* copyDst;    // COPY_COLOUR: device destination of the colour buffer
+    void* copyDst;    // COPY_COLOUR: destination (device or host) of a rectangle of the colour buffer
+    int copyX, copyY, copyW, copyH;  // the rectangle, in pixels from the bottom-left corner
+    size_t copyPitch;                // destination bytes per row (rows top-down)
     int depthTarget;  // -1 = default buffer
     int vpX, vpY, vpW, vpH;
     float depthValue;
@@ -554,7 +556,7 @@ int plan_commands(const std::vector<Command>& cmds, size_t from, PassFn onPass, 
                 if (ps.clearDepth && (rc = onFill(depthClearTarget, ps.depthValue, 0u))) return rc;
                 if (ps.clearColour && (rc = onFill(-3, 0.0f, ps.colourValue))) return rc;
                 ps.clearDepth = ps.clearColour = false;
-                if ((rc = onCopy(cmds[j].copyDst))) return rc;
+                if ((rc = onCopy(cmds[j]))) return rc;
                 continue;
             }
             if (cmds[j].kind == Command::CLEAR_DEPTH) {
@@ -588,15 +590,22 @@ int plan_commands(const std::vector<Command>& cmds, size_t from, PassFn onPass, 
     return 0;
 }
 
+// A recorded colour read-out: the rectangle's rows top-down (memory row
+// H-1-y of the display layout) into dst, copyPitch bytes apart.
+int copy_colour(ps3d_pipeline* p, const Command& c)
+{
+    const uint8_t* src = p->colour + ((size_t)(p->devH - c.copyY - c.copyH) * p->devW + c.copyX) * 4;
+    CU(cudaMemcpy2DAsync(c.copyDst, c.copyPitch, src, (size_t)p->devW * 4, (size_t)c.copyW * 4, c.copyH,
+                         cudaMemcpyDefault, p->stream));
+    return 0;
+}
+
 int launch_cmds(ps3d_pipeline* p, const std::vector<Command>& cmds, size_t from)
 {
     return plan_commands(
         cmds, from, [&](const Pass& ps, size_t start) { return run_pass(p, cmds, ps, start); },
         [&](int target, float v, uint32_t c) { return target == -3 ? fill_colour(p, c) : fill_depth(p, target, v); },
-        [&](void* dst) -> int {
-            CU(cudaMemcpyAsync(dst, p->colour, (size_t)p->devW * 4 * p->devH, cudaMemcpyDeviceToDevice, p->stream));
-            return 0;
-        });
+        [&](const Command& c) { return copy_colour(p, c); });
 }
 
 int launch_range(ps3d_pipeline* p, size_t from) { return launch_cmds(p, p->launched, from); }
@@ -1157,8 +1166,41 @@ int ps3d_read_colour_device(ps3d_pipeline* p, void* devDst)
     c.kind = Command::COPY_COLOUR;
     c.depthTarget = p->depthTarget;
     c.copyDst = devDst;
+    c.copyW = p->devW;
+    c.copyH = p->devH;
+    c.copyPitch = (size_t)p->devW * 4;
     (p->recording ? p->recording->cmds : p->pending).push_back(c);
     return 0;
+}
+
+int ps3d_copy_colour_rect(ps3d_pipeline* p, int x, int y, int width, int height, void* dst, size_t dstPitch)
+{
+    if (!p || !dst) return fail(PS3D_ERR_INVALID, "null argument");
+    if (x < 0 || y < 0 || width <= 0 || height <= 0 || x + width > p->devW || y + height > p->devH)
+        return fail(PS3D_ERR_RANGE, "rectangle %d,%d %dx%d outside the %dx%d colour buffer", x, y, width, height,
+                    p->devW, p->devH);
+    if (dstPitch < (size_t)width * 4) return fail(PS3D_ERR_INVALID, "destination pitch below the row size");
+    Command c;
+    memset(&c, 0, sizeof c);
+    c.kind = Command::COPY_COLOUR;
+    c.depthTarget = p->depthTarget;
+    c.copyDst = dst;
+    c.copyX = x;
+    c.copyY = y;
+    c.copyW = width;
+    c.copyH = height;
+    c.copyPitch = dstPitch;
+    (p->recording ? p->recording->cmds : p->pending).push_back(c);
+    return 0;
+}
+
+int ps3d_query(ps3d_pipeline* p)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    cudaError_t e = cudaStreamQuery(p->stream);
+    if (e == cudaSuccess) return 1;
+    if (e == cudaErrorNotReady) return 0;
+    return fail(PS3D_ERR_DEVICE, "cudaStreamQuery: %s", cudaGetErrorString(e));
 }
 
 int ps3d_colour_device_ptr(ps3d_pipeline* p, void** out)
@@ -1225,7 +1267,7 @@ int ps3d_cmdbuf_end(ps3d_pipeline* p, ps3d_cmdbuf** out)
             cb->hUnis.insert(cb->hUnis.end(), uu.begin(), uu.end());
             return 0;
         },
-        [&](int, float, uint32_t) { return 0; }, [&](void*) { return 0; });
+        [&](int, float, uint32_t) { return 0; }, [&](const Command&) { return 0; });
     size_t n = std::max<size_t>(cb->hDraws.size(), 1);
     bool ok = cudaMalloc((void**)&cb->dDraws, n * sizeof(DrawDesc)) == cudaSuccess &&
               cudaMalloc((void**)&cb->dUnis, n * sizeof(DrawUniforms)) == cudaSuccess &&
@@ -1639,7 +1681,7 @@ extern "C" int ps3d_finish_noalloc(ps3d_pipeline* p)
             NoAllocPass s;
             return noalloc_shape(p, rec, ps, s, false);
         },
-        [&](int, float, uint32_t) { return 0; }, [&](void*) { return 0; });
+        [&](int, float, uint32_t) { return 0; }, [&](const Command&) { return 0; });
     if (rc) return rc;
 
     // The abort flag and the overflow record must start at zero.
@@ -1649,10 +1691,7 @@ extern "C" int ps3d_finish_noalloc(ps3d_pipeline* p)
     rc = plan_commands(
         cmds, 0, [&](const Pass& ps, size_t start) { return noalloc_run_pass(p, cmds, ps, start, base); },
         [&](int target, float v, uint32_t c) { return target == -3 ? fill_colour(p, c) : fill_depth(p, target, v); },
-        [&](void* dst) -> int {
-            CU(cudaMemcpyAsync(dst, p->colour, (size_t)p->devW * 4 * p->devH, cudaMemcpyDeviceToDevice, p->stream));
-            return 0;
-        });
+        [&](const Command& c) { return copy_colour(p, c); });
     if (rc) return rc;
     CU(cudaStreamSynchronize(p->stream));
     int st[4];

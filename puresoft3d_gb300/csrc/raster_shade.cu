@@ -331,7 +331,7 @@ __global__ void __launch_bounds__(256) k_shade(PassParams P)
     const DrawUniforms& U = P.unis[d.uni];
     const int xl = x - d.vpX, yl = y - d.vpY;  // the draw's rasteriser coordinates
     Span s;
-    span_row(t, yl, d.vpW, s);
+    span_row<true>(t, yl, d.vpW, s);
     SpanZ z;
     span_z(t, s, yl, z);
     const float* vary = P.vary + (size_t)w * 3 * P.nvMax;

@@ -193,9 +193,9 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float
                 int top, bottom, third = 2, tmp;
                 if (vy[0] > vy[1]) { top = 0; bottom = 1; }
                 else { top = 1; bottom = 0; }
-                if (vy[top] < vy[third]) { tmp = top; top = third; third = tmp; }
-                else if (vy[bottom] > vy[third]) { tmp = bottom; bottom = third; third = tmp; }
-                Edge tt = mk_edge(vx, vy, top, third), tb = mk_edge(vx, vy, top, bottom);
+                if (sel3(vy, top) < vy[2]) { tmp = top; top = third; third = tmp; }
+                else if (sel3(vy, bottom) > vy[2]) { tmp = bottom; bottom = third; third = tmp; }
+                Edge tt = mk_edge<true>(vx, vy, top, third), tb = mk_edge<true>(vx, vy, top, bottom);
                 float yt = sel3(vy, third);
                 if (edge_at(tb, yt) > edge_at(tt, yt)) {  // pointing left
                     upper = edge_code(top, third) | (edge_code(top, bottom) << 4);

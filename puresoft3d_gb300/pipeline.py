@@ -62,6 +62,8 @@ _SIGS = {
     "ps3d_read_depth": [_c_void_p, _c_void_p],
     "ps3d_colour_device_ptr": [_c_void_p, ctypes.POINTER(_c_void_p)],
     "ps3d_read_colour_device": [_c_void_p, _c_void_p],
+    "ps3d_copy_colour_rect": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p, _c_size_t],
+    "ps3d_query": [_c_void_p],
     "ps3d_get_stream": [_c_void_p, ctypes.POINTER(_c_void_p)],
     "ps3d_set_fragment_counting": [_c_void_p, _c_int],
     "ps3d_stats": [_c_void_p, ctypes.POINTER(Stats)],
@@ -264,6 +266,15 @@ class PuresoftPipeline:
 
     def readColourDevice(self, dev_ptr: int):
         self._check(self.lib.ps3d_read_colour_device(self.h, dev_ptr))
+
+    def copyColourRect(self, x, y, w, h, dst_ptr: int, pitch: int):
+        """Records a read-out of the colour rectangle (x, y, w, h) to dst_ptr
+        (device or pinned host memory), rows top-down, `pitch` bytes apart."""
+        self._check(self.lib.ps3d_copy_colour_rect(self.h, x, y, w, h, dst_ptr, pitch))
+
+    def query(self) -> bool:
+        """True when all launched work has completed (no wait)."""
+        return self._check(self.lib.ps3d_query(self.h)) == 1
 
     def textureDevicePtr(self, idx) -> int:
         v = ctypes.c_void_p()

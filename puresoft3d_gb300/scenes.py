@@ -644,6 +644,76 @@ def scene_c4(seed: int = 1238, views: int = 4096, size: int = 128, tex_size: int
     return batched, plain
 
 
+C5_RESOLUTIONS = ((256, 256), (512, 512), (1024, 1024), (1920, 1080))
+
+
+def scene_c5_pool(seed: int = 1239, meshes: int = 128, tri_min: int = 1000, tri_max: int = 500_000,
+                  textures: int = 64, tex_size: int = 512) -> Scene:
+    """Config 5's device-resident pool: `meshes` seeded meshes (sphere / torus
+    / box, triangles log-uniform in [tri_min, tri_max]) and `textures`
+    tex_size^2 procedural mip chains, plus the LIT3 programme (trilinear).
+    Setup only; jobs come from `c5_jobs`."""
+    rng = np.random.default_rng(seed)
+    b = _Builder()
+    chains = [b.chain_u8(procedural_bgra(tex_size, rng)) for _ in range(textures)]
+    prog = b.programme(VP_DEF01, IP_DEF01, FP_LIT3)
+    vaos, tris = [], []
+    for _ in range(meshes):
+        n = int(round(math.exp(rng.uniform(math.log(tri_min), math.log(tri_max)))))
+        mesh = mesh_with_triangles(n, int(rng.integers(0, 3)))
+        vaos.append(b.vao(mesh, slots=(0, 3, 4)))
+        tris.append(mesh_triangles(mesh))
+    light = np.array([0.35, 0.75, 0.55])
+    light /= np.linalg.norm(light)
+    return Scene("c5_pool", 0, 0, b.setup, [], {
+        "programme": prog, "vaos": vaos, "mesh_triangles": tris, "chains": chains, "tex_size": tex_size,
+        "common": [("useProgramme", prog), ("setUniform", 7, vec4(*light))]})
+
+
+@dataclasses.dataclass
+class Job:
+    """One render request: a mesh of the pool seen by an orbit camera at one
+    resolution.  `ops` are the calls that draw it into the current viewport
+    (no clears, no viewport)."""
+    id: int
+    arrival: float          # seconds after the stream starts
+    width: int
+    height: int
+    mesh: int
+    triangles: int
+    ops: List[Tuple[Any, ...]]
+
+
+def c5_jobs(pool: Scene, n: int = 2000, rate: float = 1000.0, seed: int = 1240) -> List[Job]:
+    """A seeded Poisson stream of n jobs at `rate` jobs/s: resolution uniform
+    over C5_RESOLUTIONS, mesh and texture uniform over the pool, camera on a
+    random orbit (azimuth U[0, 2pi), elevation U[-60, 60] deg, distance
+    U[2.5, 4]), object under a random rotation."""
+    rng = np.random.default_rng(seed)
+    info = pool.info
+    t = 0.0
+    jobs = []
+    for k in range(n):
+        t += float(rng.exponential(1.0 / rate))
+        w, h = C5_RESOLUTIONS[int(rng.integers(0, len(C5_RESOLUTIONS)))]
+        m = int(rng.integers(0, len(info["vaos"])))
+        chain = info["chains"][int(rng.integers(0, len(info["chains"])))]
+        az = rng.uniform(0, 2 * math.pi)
+        el = math.radians(rng.uniform(-60, 60))
+        dist = rng.uniform(2.5, 4.0)
+        eye = dist * np.array([math.cos(el) * math.sin(az), math.sin(el), math.cos(el) * math.cos(az)])
+        P = perspective(0.5, 20.0, w / h, math.radians(50.0))
+        V = look_at(eye, (0, 0, 0), (0, 1, 0))
+        R = _random_rotation(rng)
+        focal = (h / 2) / math.tan(math.radians(25.0))
+        lod = info["tex_size"] / (2 * math.pi) / focal * dist
+        ops = [("setUniform", 3, col_major(P @ V)), ("setUniform", 4, col_major(R)), ("setUniform", 5, col_major(R)),
+               ("setUniform", 8, vec4(*eye, 1.0)), ("setUniform", 9, _u(np.array(chain, dtype=np.int32))),
+               ("setUniform", 12, vec4(lod, 0.0, 0.0, 0.0)), ("drawVAO", info["vaos"][m])]
+        jobs.append(Job(k, t, w, h, m, info["mesh_triangles"][m], ops))
+    return jobs
+
+
 # --------------------------------------------------------------------------
 # replay
 

@@ -157,6 +157,9 @@ class OraclePipeline(_CPipeline):
             lib.ps3do_fragments_tested.argtypes = [ctypes.c_void_p]
             lib.ps3do_fragments_passed.restype = ctypes.c_longlong
             lib.ps3do_fragments_passed.argtypes = [ctypes.c_void_p]
+            lib.ps3do_set_colour_error.argtypes = [ctypes.c_void_p, ctypes.c_int]
+            lib.ps3do_colour_error.argtypes = [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_double)] * 2 + [
+                ctypes.POINTER(ctypes.c_longlong)] * 2
             _bind(lib, "ps3do_")
             OraclePipeline._lib = lib
         lib = OraclePipeline._lib
@@ -164,6 +167,18 @@ class OraclePipeline(_CPipeline):
 
     def fragments(self):
         return self.lib.ps3do_fragments_tested(self.h), self.lib.ps3do_fragments_passed(self.h)
+
+    def measureColourError(self, on=True):
+        """Compare every shaded fragment's FP32 colour with an FP64 re-shade."""
+        self.lib.ps3do_set_colour_error(self.h, int(on))
+
+    def colourError(self):
+        """{max, mean} |FP32 - FP64| per colour channel (8-bit units), the
+        channels compared and how many differed by 1 or more."""
+        mx, mean = ctypes.c_double(), ctypes.c_double()
+        n, over = ctypes.c_longlong(), ctypes.c_longlong()
+        self.lib.ps3do_colour_error(self.h, ctypes.byref(mx), ctypes.byref(mean), ctypes.byref(n), ctypes.byref(over))
+        return {"max": mx.value, "mean": mean.value, "channels": n.value, "over_1": over.value}
 
     def close(self):
         if self.h:
