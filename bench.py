@@ -127,10 +127,10 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def make_scene(cfg):
+def make_scene(cfg, views=4096):
     from puresoft3d_gb300 import scenes as S
     if cfg == "c4":
-        return S.scene_c4()[0]
+        return S.scene_c4(views=views)[0]
     if cfg == "c3s":
         return S.scene_c3(width=1920, height=1080, meshes=128, tri_target=500_000, textures=4)
     return {"c1": S.scene_c1, "c2": S.scene_c2, "c3": S.scene_c3}[cfg]()
@@ -142,9 +142,11 @@ def autotune(pipe, record, key, args):
     from puresoft3d_gb300.autotune import Autotuner
     if args.bin_width:
         pipe.setBinWidth(args.bin_width)
-        return {"bin_width": args.bin_width, "source": "--bin-width"}
+        pipe.setRasterOccupancy(args.raster_occupancy)
+        return {"bin_width": args.bin_width, "raster_occupancy": args.raster_occupancy, "source": "flags"}
     best, ms = Autotuner().tune(pipe, record, key, reps=3)
-    return {"bin_width": best, "source": "autotuner", "candidate_ms": {str(k): round(v, 4) for k, v in ms.items()}}
+    return {"bin_width": best[0], "raster_occupancy": best[1], "source": "autotuner",
+            "candidate_ms": {k: round(v, 4) for k, v in ms.items()}}
 
 
 def run_c4(args):
@@ -388,9 +390,12 @@ def run_frames_only(args):
     immediate path (no graph, no extra runs) and exit."""
     from puresoft3d_gb300 import scenes as S
     from puresoft3d_gb300.pipeline import PuresoftPipeline
-    scene = make_scene(args.config)
+    scene = make_scene(args.config, args.views)
     pipe = PuresoftPipeline(scene.width, scene.height)
     S.replay_setup(scene, pipe)
+    if args.bin_width:
+        pipe.setBinWidth(args.bin_width)
+        pipe.setRasterOccupancy(args.raster_occupancy)
     for _ in range(args.ncu_frames):
         S.replay_frame(scene, pipe)
         pipe.finish()
@@ -699,7 +704,8 @@ def main():
     ap.add_argument("--views", type=int, default=4096, help="config 4: number of views")
     ap.add_argument("--jobs", type=int, default=2000, help="config 5: number of jobs")
     ap.add_argument("--bin-width", type=int, default=0, choices=[0, 8, 16, 32],
-                    help="fix the bin width instead of autotuning it")
+                    help="fix the schedule (with --raster-occupancy) instead of autotuning it")
+    ap.add_argument("--raster-occupancy", type=int, default=0, choices=[0, 8])
     args = ap.parse_args()
     if args.ncu_frames:
         run_frames_only(args)

@@ -192,6 +192,11 @@ int ps3d_finish(ps3d_pipeline* p);
  * workload.  Default 32 (or PS3D_BIN_W). */
 int ps3d_set_bin_width(ps3d_pipeline* p, int columns);
 int ps3d_get_bin_width(ps3d_pipeline* p, int* columns);
+/* Second schedule knob: the raster kernel variant.  0 lets each thread use
+ * the registers it wants (fewer resident blocks); 8 caps registers so that
+ * 8 blocks fit per SM where shared memory allows (more warps to hide
+ * latency).  Time only, never results. */
+int ps3d_set_raster_occupancy(ps3d_pipeline* p, int blocksPerSM);
 
 /* ps3d_finish for callers that must not allocate device memory; it has no
  * counterpart in the reference, whose CPU pipeline allocates no device memory
@@ -205,7 +210,7 @@ int ps3d_get_bin_width(ps3d_pipeline* p, int* columns);
  * (a file-scope __device__ array, carved afresh per pass); the call makes no
  * cudaMalloc, cudaFree or other allocating call.  Limits:
  *   - a pass needs its triangle records, varyings, descriptors and (when it
- *     writes colour) 4 bytes per target pixel to fit in 16 MiB with room for
+ *     writes colour) 8 bytes per target pixel to fit in 16 MiB with room for
  *     at least 4096 bin pairs, and has at most 1024 draws.  Otherwise the call
  *     returns PS3D_ERR_RANGE before anything runs and the commands stay
  *     recorded (ps3d_finish renders them);

@@ -1,7 +1,8 @@
 """Schedule autotuner for the device passes.
 
-The one schedule knob of a pass is its bin width (8, 16 or 32 columns; bins
-are always 32 rows).  It sets how the raster kernel's work is cut:
+A schedule is a pair (bin width, raster occupancy).  The bin width (8, 16 or
+32 columns; bins are always 32 rows) sets how the raster kernel's work is
+cut:
 
 * the number of bins, hence blocks, a pass launches (more, smaller bins give
   small views and thin targets more parallelism);
@@ -11,15 +12,19 @@ are always 32 rows).  It sets how the raster kernel's work is cut:
 * the (bin, triangle) pairs binning emits (a triangle crosses more narrow
   bins) and the span set-up work they carry.
 
-Which width wins depends on the workload (triangle sizes, depth complexity,
+The raster occupancy picks the raster kernel variant: 0 lets each thread use
+the registers it wants, 8 caps them so that up to 8 blocks are resident per
+SM (more warps to hide latency, less room per thread).
+
+Which schedule wins depends on the workload (triangle sizes, depth complexity,
 target size), so the tuner times every candidate on the caller's own frame:
 the frame is recorded as a command buffer, replayed as a CUDA graph with the
 L2 scrubbed before each replay, and timed with CUDA events on the pipeline's
 stream; the fastest median wins.  Results are cached per workload key and
 device in a JSON file (``PS3D_AUTOTUNE_CACHE``, default
 ``~/.cache/puresoft3d_gb300/autotune.json``), so a service tunes a workload
-once.  Results are identical for every width (the parity tests check 16 and
-32 against the oracle); only the time differs.
+once.  Results are identical for every schedule (the parity tests check
+every bin width against the oracle); only the time differs.
 """
 from __future__ import annotations
 
@@ -28,7 +33,23 @@ import os
 import statistics
 from typing import Callable, Dict, Optional, Sequence, Tuple
 
-CANDIDATES = (8, 16, 32)
+CANDIDATES = tuple((bw, occ) for bw in (8, 16, 32) for occ in (0, 8))
+
+
+def _pair(c):
+    return (int(c[0]), int(c[1])) if isinstance(c, (tuple, list)) else (int(c), 0)
+
+
+def _name(c) -> str:
+    bw, occ = _pair(c)
+    return "%d/%d" % (bw, occ)
+
+
+def apply(pipe, c) -> None:
+    bw, occ = _pair(c)
+    pipe.setBinWidth(bw)
+    if hasattr(pipe, "setRasterOccupancy"):
+        pipe.setRasterOccupancy(occ)
 
 
 def _default_cache() -> str:
@@ -94,23 +115,25 @@ class Autotuner:
         return statistics.median(times)
 
     def tune(self, pipe, record: Callable[[object], None], key: str,
-             candidates: Sequence[int] = CANDIDATES, reps: int = 5, warmup: int = 2,
-             retune: bool = False) -> Tuple[int, Dict[int, float]]:
-        """Sets `pipe`'s bin width to the fastest candidate for `record`'s
-        frame and returns (width, {width: median ms}).  A cached result for
-        (key, device, candidates) is reused unless `retune`."""
-        full = "%s|%s|%s" % (key, device_name(), ",".join(str(c) for c in candidates))
+             candidates: Sequence = CANDIDATES, reps: int = 5, warmup: int = 2,
+             retune: bool = False) -> Tuple[Tuple[int, int], Dict[str, float]]:
+        """Sets `pipe`'s schedule to the fastest candidate for `record`'s
+        frame and returns ((bin width, raster occupancy), {"bw/occ": median
+        ms}).  A candidate is a (bin width, occupancy) pair or a bare bin
+        width.  A cached result for (key, device, candidates) is reused
+        unless `retune`."""
+        full = "%s|%s|%s" % (key, device_name(), ",".join(_name(c) for c in candidates))
         hit = self.table.get(full)
         if hit and not retune:
-            best = int(hit["best"])
-            pipe.setBinWidth(best)
-            return best, {int(k): v for k, v in hit["ms"].items()}
-        ms: Dict[int, float] = {}
+            best = _pair(hit["best"])
+            apply(pipe, best)
+            return best, dict(hit["ms"])
+        ms: Dict[str, float] = {}
         for c in candidates:
-            pipe.setBinWidth(c)
-            ms[c] = self.time_frame(pipe, record, reps=reps, warmup=warmup)
-        best = min(ms, key=ms.get)
-        pipe.setBinWidth(best)
-        self.table[full] = {"best": best, "ms": {str(k): round(v, 5) for k, v in ms.items()}}
+            apply(pipe, c)
+            ms[_name(c)] = self.time_frame(pipe, record, reps=reps, warmup=warmup)
+        best = _pair(min(candidates, key=lambda c: ms[_name(c)]))
+        apply(pipe, best)
+        self.table[full] = {"best": list(best), "ms": {k: round(v, 5) for k, v in ms.items()}}
         self._save()
         return best, ms

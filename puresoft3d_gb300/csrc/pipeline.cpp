@@ -154,6 +154,7 @@ struct ps3d_pipeline {
     int behavior = B_UPDATE_DEPTH | B_TEST_DEPTH | B_FACE_CULLING;  // pipeline.cpp:34
     int depthTarget = -1;
     int binW = 32;
+    int rasterBlocks = 0;
     bool countFrags = false;
     cudaStream_t stream = nullptr;
     bool ownStream = false;
@@ -186,7 +187,7 @@ struct ps3d_pipeline {
     int* keyB = nullptr; size_t keyBCap = 0;
     int* binStart = nullptr; size_t binStartCap = 0;
     int* scanTmp = nullptr; size_t scanTmpCap = 0;
-    int* winner = nullptr; size_t winnerCap = 0;
+    int2* shadeList = nullptr; size_t shadeListCap = 0;
     DrawDesc* draws = nullptr; size_t drawsCap = 0;
     DrawUniforms* unis = nullptr; size_t unisCap = 0;
     int* status = nullptr;
@@ -373,7 +374,7 @@ int ensure_scratch(ps3d_pipeline* p, int nTris, int nvMax, int W, int H, int bin
               dev_alloc(p->radix, p->radixCap, radix_scratch_ints(sortBlocks, radix_passes((int)nBins))) &&
               dev_alloc(p->binStart, p->binStartCap, nBins + 1) &&
               dev_alloc(p->scanTmp, p->scanTmpCap, (size_t)scan_block_sums_needed(nTris) + 1);
-    if (ok && colour) ok = dev_alloc(p->winner, p->winnerCap, (size_t)W * H);
+    if (ok && colour) ok = dev_alloc(p->shadeList, p->shadeListCap, (size_t)W * H);
     if (!ok) return fail(PS3D_ERR_NOMEM, "device scratch allocation failed");
     return 0;
 }
@@ -490,6 +491,7 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     P.W = W;
     P.H = H;
     P.binW = binW;
+    P.rasterBlocks = p->rasterBlocks;
     P.binsX = binsX;
     P.binsY = binsY;
     P.nTris = nTris;
@@ -518,7 +520,7 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     P.depthScan = tg.scan;
     P.depthW = tg.w;
     P.depthH = tg.h;
-    P.winner = p->winner;
+    P.shadeList = p->shadeList;
     P.colour = p->colour;
     P.colourW = p->devW;
     P.colourH = p->devH;
@@ -735,7 +737,7 @@ int ps3d_pipeline_destroy(ps3d_pipeline* p)
                 delete b;
             }
     void* bufs[] = {p->colour, p->defDepth, p->status, p->tris, p->vary, p->pairCount, p->rect, p->pairOffset,
-                    p->pairKey, p->pairTri, p->keyB, p->binTri, p->radix, p->binStart, p->scanTmp, p->winner, p->draws,
+                    p->pairKey, p->pairTri, p->keyB, p->binTri, p->radix, p->binStart, p->scanTmp, p->shadeList, p->draws,
                     p->unis};
     for (void* b : bufs)
         if (b) cudaFree(b);
@@ -1119,6 +1121,15 @@ int ps3d_set_bin_width(ps3d_pipeline* p, int columns)
     return 0;
 }
 
+int ps3d_set_raster_occupancy(ps3d_pipeline* p, int blocksPerSM)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    if (blocksPerSM != 0 && blocksPerSM != 8)
+        return fail(PS3D_ERR_INVALID, "raster occupancy %d: 0 (default) or 8 blocks per SM", blocksPerSM);
+    p->rasterBlocks = blocksPerSM;
+    return 0;
+}
+
 int ps3d_get_bin_width(ps3d_pipeline* p, int* columns)
 {
     if (!p || !columns) return fail(PS3D_ERR_INVALID, "null argument");
@@ -1457,15 +1468,15 @@ int ps3d_profile_read(ps3d_pipeline* p, int* launches, double* ms)
 // cudaFree (both can synchronise the whole device), a process whose device
 // memory is fully committed up front, or a service that must not grow after
 // admission control has accounted for it.  The recorded passes take their
-// scratch (descriptors, triangle records, varyings, bin lists, histograms,
-// winner buffer) from one fixed array instead of the pipeline's growable
+// scratch (descriptors, triangle records, varyings, bin lists, look-back
+// descriptors, shade list) from one fixed array instead of the pipeline's growable
 // buffers, and run the same kernels with the same results.
 
 namespace {
 
 // The fixed scratch: 16 MiB per device, carved afresh for every pass.  It
-// holds, for example, a 1024x1024 colour pass of ~50k triangles and ~700k
-// bin pairs, or a 1920x1080 pass of ~20k triangles.
+// holds, for example, a 1024x1024 colour pass of ~15k triangles and ~200k
+// bin pairs, or a 2048x2048 depth-only pass of ~40k triangles.
 constexpr size_t kNoAllocBytes = (size_t)16 << 20;
 constexpr int kNoAllocMaxDraws = 1024;  // draws per pass (host staging below)
 constexpr int kNoAllocMaxDevices = 64;
@@ -1479,7 +1490,7 @@ DrawUniforms g_noallocUnis[kNoAllocMaxDraws];
 
 // Byte offsets of one pass's buffers in the array, each 256-byte aligned.
 struct NoAllocLayout {
-    size_t draws, unis, tris, vary, pairCount, rect, pairOffset, scanTmp, winner, binStart, radix, pairKey,
+    size_t draws, unis, tris, vary, pairCount, rect, pairOffset, scanTmp, shadeList, binStart, radix, pairKey,
         pairTri, keyB, binTri;
 };
 
@@ -1502,7 +1513,7 @@ size_t noalloc_layout(NoAllocLayout& L, int nd, int nTris, int nv, int W, int H,
     L.rect = take((size_t)nTris * sizeof(int4));
     L.pairOffset = take(((size_t)nTris + 1) * sizeof(int));
     L.scanTmp = take(((size_t)scan_block_sums_needed(nTris) + 1) * sizeof(int));
-    L.winner = colour ? take((size_t)W * H * sizeof(int)) : 0;
+    L.shadeList = colour ? take((size_t)W * H * sizeof(int2)) : 0;
     L.binStart = take((nBins + 1) * sizeof(int));
     L.radix = take(radix_scratch_ints((int)sortBlocks, radix_passes((int)nBins)) * sizeof(int));
     L.pairKey = take((size_t)pairCap * sizeof(int));
@@ -1600,6 +1611,7 @@ int noalloc_run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const P
     P.W = W;
     P.H = H;
     P.binW = p->binW;
+    P.rasterBlocks = p->rasterBlocks;
     P.binsX = s.binsX;
     P.binsY = s.binsY;
     P.nTris = s.nTris;
@@ -1628,7 +1640,7 @@ int noalloc_run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const P
     P.depthScan = s.tg.scan;
     P.depthW = s.tg.w;
     P.depthH = s.tg.h;
-    P.winner = s.anyColour ? (int*)(base + L.winner) : nullptr;
+    P.shadeList = s.anyColour ? (int2*)(base + L.shadeList) : nullptr;
     P.colour = p->colour;
     P.colourW = p->devW;
     P.colourH = p->devH;

@@ -74,6 +74,7 @@ static_assert(sizeof(TriRaster) == 64, "TriRaster must be 64 bytes");
 struct PassParams {
     int W, H;                 // target (depth buffer) size; each draw has its own viewport rectangle
     int binW, binsX, binsY;   // bins of kBinH x binW pixels
+    int rasterBlocks;         // raster variant: 0 = registers as needed, 8 = capped for 8 blocks per SM
     int nTris, nDraws;
     const DrawDesc* draws;
     const DrawUniforms* unis;
@@ -95,13 +96,13 @@ struct PassParams {
     int* binStart;            // first position of each bin's list; [nBins] = total
     int* binTri;              // the sort's second triangle buffer
     const int* sortedTri;     // triangles of each bin, in submission order (binTri or pairTri)
-    int* status;              // [0] overflow flag, [1] pairs needed, [2] sort blocks in use,
-                              // [3] overflowing pass, [4..5] fragments tested, [6..7] passed,
-                              // [8..9] pairs binned (u64)
+    int* status;              // [0] overflow flag (2: a wait expired), [1] pairs needed, [2] sort
+                              // tiles in use, [3] overflowing pass, [4..5] fragments tested,
+                              // [6..7] passed, [8..9] pairs binned (u64), [10] shade-list length
     float* depth;             // depth target (rows bottom-up)
     int depthScan;            // in floats
     int depthW, depthH;
-    int* winner;              // per viewport pixel: last colour-writing fragment that passed, or -1
+    int2* shadeList;          // per covered pixel: (y * W + x, last colour-writing fragment that passed)
     uint8_t* colour;          // BGRA8, top-down
     int colourW, colourH;
     int clearDepth, clearColour, anyColour, countFrags;
@@ -111,6 +112,7 @@ struct PassParams {
 };
 
 constexpr int kSortChunk = 4096;   // pairs per sort tile
+constexpr int kShadeCount = 10;    // status word holding the pass's shade-list length
 constexpr int kRadixDigits = 256;
 constexpr int kRadixMaxPasses = 3;  // bin numbers below 2^24
 constexpr int kRadixHdr = 1024;     // ints before the descriptors (counts + tickets, padded)

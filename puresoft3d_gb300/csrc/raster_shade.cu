@@ -13,13 +13,18 @@
 //           triangle order with the epsilon depth test (fragthrd.cpp:227) --
 //           every pixel has exactly one owner, so the per-pixel order is the
 //           reference's per-row FIFO order (drawvao.cpp:77-109).
-// k_shade   one thread per pixel: re-derives the winning fragment's
-//           varyings (same span set-up and sequential steps) and runs the
-//           draw's fragment stage once.  With no discard and no blending the
-//           colour of a pixel is the colour of the last fragment that passed
-//           the depth test, so shading only that fragment gives the
-//           reference's framebuffer bit for bit.
+//           At the end the block writes the bin's depth back, appends one
+//           (pixel, winner) entry per covered pixel to the pass's shade list
+//           and, when the pass clears colour, writes the clear colour to the
+//           pixels no fragment reached.
+// k_shade   one thread per shade-list entry: re-derives the winning
+//           fragment's varyings (same span set-up and sequential steps) and
+//           runs the draw's fragment stage once.  With no discard and no
+//           blending the colour of a pixel is the colour of the last fragment
+//           that passed the depth test, so shading only that fragment gives
+//           the reference's framebuffer bit for bit.
 #include <cuda_runtime.h>
+#include <algorithm>
 #include "device_common.cuh"
 
 namespace ps3d {
@@ -34,6 +39,12 @@ __device__ __forceinline__ void bin_range(const PassParams& P, int bin, int& sta
     end = P.binStart[bin + 1];
 }
 
+// The pass's clear colour at target pixel (x, y) (colour rows top-down).
+__device__ __forceinline__ void clear_colour_px(const PassParams& P, int x, int y)
+{
+    ((uint32_t*)P.colour)[(size_t)(P.colourH - 1 - y) * P.colourW + x] = P.colourClearValue;
+}
+
 // Per span of a round: its columns in the bin, its triangle slot and flags.
 struct SpanRec {
     short xs, xe;   // bin-relative, inclusive
@@ -45,8 +56,8 @@ constexpr int kRasterThreads = 128;  // 4 warps: warp = column quarter, lane = b
 constexpr int kChunk = 128;          // triangles per chunk (one per thread)
 constexpr int kSlots = 128;          // (triangle, row) spans per round (one per thread)
 
-template <int BW>
-__global__ void __launch_bounds__(kRasterThreads) k_raster(PassParams P)
+template <int BW, int MINB>
+__global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
 {
     constexpr int S = BW + 1;   // padded strides: threads at one column hit distinct banks
     constexpr int Q = BW / 4;   // columns per quarter
@@ -57,10 +68,12 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(PassParams P)
     __shared__ __align__(16) TriRaster sTri[kChunk];
     __shared__ int sTid[kChunk];
     __shared__ short sOx[kChunk], sOy[kChunk], sLw[kChunk];  // each triangle's viewport origin and width
-    __shared__ int sSlot[kSlots];                // (row << 8) | triangle slot
+    __shared__ int sBase[kChunk];                // first span (in chunk order) of each triangle
+    __shared__ unsigned char sR0[kChunk];        // first bin row of each triangle
     __shared__ SpanRec sRec[kSlots];
-    __shared__ unsigned sMask[4][kBinH][kSlots / 32];
+    __shared__ unsigned sMask[2][4][kBinH][kSlots / 32];  // by round parity: rounds alternate buffers
     __shared__ int sWarpSum[kRasterThreads / 32];
+    __shared__ int sListBase;
     if (P.status[0]) return;
 
     const int bin = blockIdx.x;
@@ -73,22 +86,16 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(PassParams P)
     bin_range(P, bin, start, end);
 
     if (start == end) {
-        if (P.clearDepth)
+        if (P.clearDepth || P.clearColour)
             for (int i = tid; i < rows * cols; i += kRasterThreads) {
                 int r = i / cols, c = i - r * cols;
-                P.depth[(size_t)(y0 + r) * P.depthScan + x0 + c] = P.depthClearValue;
+                if (P.clearDepth) P.depth[(size_t)(y0 + r) * P.depthScan + x0 + c] = P.depthClearValue;
+                if (P.clearColour) clear_colour_px(P, x0 + c, y0 + r);
             }
         return;
     }
-    for (int i = tid; i < kBinH * BW; i += kRasterThreads) {
-        int r = i / BW, c = i - r * BW;
-        float d = P.depthClearValue;
-        if (!P.clearDepth && r < rows && c < cols) d = P.depth[(size_t)(y0 + r) * P.depthScan + x0 + c];
-        sDepth[r * S + c] = d;
-        sWin[r * S + c] = -1;
-    }
-
-    // prefetch: record of the first chunk, index of the second
+    // prefetch (record of the first chunk, index of the second), in flight
+    // while the bin's depth is loaded
     float4 rec[4];
     int recTid = -1, nextIdx = -1;
     if (start + tid < end) {
@@ -98,6 +105,15 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(PassParams P)
         for (int k = 0; k < 4; k++) rec[k] = __ldg(src + k);
     }
     if (start + kChunk + tid < end) nextIdx = P.sortedTri[start + kChunk + tid];
+    for (int i = tid; i < kBinH * BW; i += kRasterThreads) {
+        int r = i / BW, c = i - r * BW;
+        float d = P.depthClearValue;
+        if (!P.clearDepth && r < rows && c < cols) d = P.depth[(size_t)(y0 + r) * P.depthScan + x0 + c];
+        sDepth[r * S + c] = d;
+        sWin[r * S + c] = -1;
+    }
+    for (int i = tid; i < 2 * 4 * kBinH * (kSlots / 32); i += kRasterThreads) (&sMask[0][0][0][0])[i] = 0u;
+    int par = 0;  // mask buffer of the current round
 
     unsigned long long tested = 0, passed = 0;
     const int qs = warp * Q, qe = qs + Q - 1;  // this thread's columns (bin-relative)
@@ -142,23 +158,26 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(PassParams P)
             if (w < warp) wbase += v;
             total += v;
         }
-        const int base = wbase + inc - cnt;
+        sBase[tid] = wbase + inc - cnt;  // triangles with no rows get the next one's base
+        sR0[tid] = (unsigned char)r0;
+        __syncthreads();
 
         for (int round = 0; round < total; round += kSlots) {
-            {
-                int lo = max(base, round), hi = min(base + cnt, round + kSlots);
-                for (int s2 = lo; s2 < hi; s2++) sSlot[s2 - round] = ((r0 + (s2 - base)) << 8) | tid;
-            }
-            for (int i = tid; i < 4 * kBinH * (kSlots / 32); i += kRasterThreads) (&sMask[0][0][0])[i] = 0u;
-            __syncthreads();
+            unsigned (*mask)[kBinH][kSlots / 32] = sMask[par];
+            // the other buffer was last read by the previous round's walk: clear it for the next round
+            for (int i = tid; i < 4 * kBinH * (kSlots / 32); i += kRasterThreads) (&sMask[par ^ 1][0][0][0])[i] = 0u;
             // ---- set-up: thread s2 takes span s2 of the round -- the reference's
             // row result and span set-up (rasterizer.cpp:93-118, interp.cpp:26-80),
             // then the sequential per-pixel steps (interp.cpp:82-92) through the
             // bin's columns, storing each pixel's exact z
             const int nSlots = min(kSlots, total - round);
             if (tid < nSlots) {
-                const int s2 = tid;
-                int code = sSlot[s2], j = code & 0xff, r = code >> 8;
+                const int s2 = tid, g = round + s2;
+                int j = 0;  // the triangle of span g: the last one whose first span is <= g
+#pragma unroll
+                for (int step = kChunk / 2; step; step >>= 1)
+                    if (sBase[j + step] <= g) j += step;
+                const int r = sR0[j] + (g - sBase[j]);
                 const int ox = sOx[j], yl = y0 + r - sOy[j];  // the draw's rasteriser row
                 const TriRaster& t = sTri[j];
                 Span sp;
@@ -184,7 +203,7 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(PassParams P)
                             if (qx != q || x == xs) {
                                 if (x != xs) {
                                     sZmin[q][s2] = zmin;
-                                    atomicOr(&sMask[q][r][s2 >> 5], 1u << (s2 & 31));
+                                    atomicOr(&mask[q][r][s2 >> 5], 1u << (s2 & 31));
                                 }
                                 q = qx;
                                 zmin = zz;
@@ -193,7 +212,7 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(PassParams P)
                             }
                         }
                         sZmin[q][s2] = zmin;
-                        atomicOr(&sMask[q][r][s2 >> 5], 1u << (s2 & 31));
+                        atomicOr(&mask[q][r][s2 >> 5], 1u << (s2 & 31));
                         SpanRec& R = sRec[s2];
                         R.xs = (short)(xs - x0);
                         R.xe = (short)(xe - x0);
@@ -214,7 +233,7 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(PassParams P)
 #pragma unroll
                 for (int c = 1; c < Q; c++) curMax = fmaxf(curMax, dRow[qs + c]);
                 for (int w = 0; w < (nSlots + 31) / 32; w++) {
-                    unsigned bits = sMask[warp][lane][w];
+                    unsigned bits = mask[warp][lane][w];
                     while (bits) {
                         int k = __ffs(bits) - 1;
                         bits &= bits - 1;
@@ -244,13 +263,48 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(PassParams P)
                 }
             }
             __syncthreads();
+            par ^= 1;
         }
-        if (total == 0) __syncthreads();  // sWarpSum / sTri are rewritten by the next chunk
     }
+    // depth write-back; count of covered pixels per thread
+    int covered = 0;
     for (int i = tid; i < rows * cols; i += kRasterThreads) {
         int r = i / cols, c = i - r * cols;
         P.depth[(size_t)(y0 + r) * P.depthScan + x0 + c] = sDepth[r * S + c];
-        if (P.anyColour) P.winner[(size_t)(y0 + r) * P.W + x0 + c] = sWin[r * S + c];
+        covered += sWin[r * S + c] >= 0;
+    }
+    if (P.anyColour || P.clearColour) {
+        // one block-wide reservation in the shade list, then each thread's
+        // covered pixels in order; uncovered pixels get the clear colour
+        int inc = covered;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int v = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += v;
+        }
+        __syncthreads();  // sWarpSum was last read before the final round's barrier
+        if (lane == 31) sWarpSum[warp] = inc;
+        __syncthreads();
+        if (tid == 0) {
+            int run = 0;
+            for (int w = 0; w < kRasterThreads / 32; w++) {
+                int v = sWarpSum[w];
+                sWarpSum[w] = run;
+                run += v;
+            }
+            sListBase = (P.anyColour && run) ? atomicAdd(P.status + kShadeCount, run) : 0;
+        }
+        __syncthreads();
+        int pos = sListBase + sWarpSum[warp] + inc - covered;
+        for (int i = tid; i < rows * cols; i += kRasterThreads) {
+            int r = i / cols, c = i - r * cols;
+            int w = sWin[r * S + c];
+            if (w >= 0) {
+                if (P.anyColour) P.shadeList[pos++] = make_int2((y0 + r) * P.W + x0 + c, w);
+            } else if (P.clearColour) {
+                clear_colour_px(P, x0 + c, y0 + r);
+            }
+        }
     }
     if (P.countFrags) {
 #pragma unroll
@@ -304,22 +358,10 @@ __device__ __forceinline__ void fragment_varyings(const TriRaster& t, const floa
     for (int k = 0; k < NV; k++) out[k] = fmul(st[k], inv);
 }
 
-__global__ void __launch_bounds__(256) k_shade(PassParams P)
+__device__ __forceinline__ void shade_entry(const PassParams& P, int2 e)
 {
-    if (P.status[0]) return;
-    int x = blockIdx.x * 32 + threadIdx.x;
-    int y = blockIdx.y * 8 + threadIdx.y;
-    if (x >= P.W || y >= P.H || x >= P.colourW || y >= P.colourH) return;
-    int bin = (y / kBinH) * P.binsX + x / P.binW;
-    int start, end;
-    bin_range(P, bin, start, end);
-    int w = -1;
-    if (start != end && P.anyColour) w = P.winner[(size_t)y * P.W + x];
+    const int y = e.x / P.W, x = e.x - y * P.W, w = e.y;
     uint32_t* dst = (uint32_t*)P.colour + (size_t)(P.colourH - 1 - y) * P.colourW + x;
-    if (w < 0) {
-        if (P.clearColour) *dst = P.colourClearValue;
-        return;
-    }
     TriRaster t;
     {
         const float4* src = (const float4*)(P.tris + w);
@@ -365,6 +407,16 @@ __global__ void __launch_bounds__(256) k_shade(PassParams P)
     *dst = bgra;
 }
 
+// One thread per shade-list entry; the grid strides over the list, whose
+// length the raster kernel left in status[kShadeCount].
+__global__ void __launch_bounds__(256) k_shade(PassParams P)
+{
+    if (P.status[0]) return;
+    const int n = P.status[kShadeCount];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        shade_entry(P, P.shadeList[i]);
+}
+
 __global__ void k_fill_u32(uint32_t* base, int width, int height, int pitchElems, uint32_t v, const int* status)
 {
     if (status && status[0]) return;
@@ -377,7 +429,8 @@ static inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) 
 
 template <int BW> void launch_raster(const PassParams& P, int nBins, cudaStream_t s)
 {
-    k_raster<BW><<<nBins, kRasterThreads, 0, s>>>(P);
+    if (P.rasterBlocks == 8) k_raster<BW, 8><<<nBins, kRasterThreads, 0, s>>>(P);
+    else k_raster<BW, 1><<<nBins, kRasterThreads, 0, s>>>(P);
 }
 
 void launch_raster_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
@@ -391,10 +444,15 @@ void launch_raster_shade(const PassParams& P, cudaStream_t s, int& launches, Pro
     }
     pr->end(s);
     launches++;
-    if (P.anyColour || P.clearColour) {
-        dim3 g(ceil_div(P.W, 32), ceil_div(P.H, 8));
+    if (P.anyColour) {  // a grid that fills the GPU, striding over the shade list
+        int dev = 0, sms = 0, perSM = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shade, 256, 0);
+        long long need = ((long long)P.W * P.H + 255) / 256;
+        int grid = (int)std::min<long long>(need, (long long)std::max(sms, 1) * std::max(perSM, 1));
         pr->begin(K_SHADE, s);
-        k_shade<<<g, dim3(32, 8), 0, s>>>(P);
+        k_shade<<<std::max(grid, 1), 256, 0, s>>>(P);
         pr->end(s);
         launches++;
     }

@@ -254,8 +254,10 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(PassParams P)
 {
     __shared__ float sVary[kSetupThreads * 3 * kMaxVary];
     int t = blockIdx.x * kSetupThreads + threadIdx.x;
-    if (blockIdx.x == 0)  // the sort's digit counts and tile tickets start at zero
+    if (blockIdx.x == 0) {  // the sort's digit counts and tile tickets, and the shade list, start empty
         for (int i = threadIdx.x; i < kRadixHdr; i += kSetupThreads) P.radix[i] = 0;
+        if (threadIdx.x == 0) P.status[kShadeCount] = 0;
+    }
     if (t < P.nTris) setup_triangle(P, t, sVary);
     if (!P.anyVary) return;
     __syncthreads();

@@ -58,6 +58,7 @@ _SIGS = {
     "ps3d_finish_noalloc": [_c_void_p],
     "ps3d_set_bin_width": [_c_void_p, _c_int],
     "ps3d_get_bin_width": [_c_void_p, ctypes.POINTER(_c_int)],
+    "ps3d_set_raster_occupancy": [_c_void_p, _c_int],
     "ps3d_read_colour": [_c_void_p, _c_void_p],
     "ps3d_read_depth": [_c_void_p, _c_void_p],
     "ps3d_colour_device_ptr": [_c_void_p, ctypes.POINTER(_c_void_p)],
@@ -243,6 +244,10 @@ class PuresoftPipeline:
     def setBinWidth(self, columns: int):
         """Bin width (8, 16 or 32 columns) of the passes launched from now on."""
         self._check(self.lib.ps3d_set_bin_width(self.h, columns))
+
+    def setRasterOccupancy(self, blocks_per_sm: int):
+        """Raster kernel variant: 0 (registers as needed) or 8 blocks per SM."""
+        self._check(self.lib.ps3d_set_raster_occupancy(self.h, blocks_per_sm))
 
     def binWidth(self) -> int:
         v = _c_int()

@@ -21,12 +21,17 @@ class _FakePipe:
 
     def __init__(self):
         self.bw = 32
+        self.occ = 0
         self.submits = 0
         self.recorded = 0
 
     def setBinWidth(self, w):
         assert w in self.COST
         self.bw = w
+
+    def setRasterOccupancy(self, o):
+        assert o in (0, 8)
+        self.occ = o
 
     def beginCommands(self):
         pass
@@ -44,7 +49,7 @@ class _FakePipe:
         pass
 
     def timerEnd(self):
-        return self.COST[self.bw]
+        return self.COST[self.bw] - (0.25 if self.occ == 8 else 0.0)
 
 
 def _record(pipe):
@@ -54,20 +59,28 @@ def _record(pipe):
 def test_picks_fastest_and_sets_it(tmp_path):
     t = Autotuner(cache_path=str(tmp_path / "tune.json"))
     p = _FakePipe()
-    best, ms = t.tune(p, _record, key="w1")
-    assert best == 16 and p.bw == 16
-    assert ms == {8: 3.0, 16: 1.5, 32: 2.0}
+    best, ms = t.tune(p, _record, key="w1", candidates=(8, 16, 32))
+    assert best == (16, 0) and p.bw == 16
+    assert ms == {"8/0": 3.0, "16/0": 1.5, "32/0": 2.0}
     assert p.recorded == 3
+
+
+def test_pairs_of_width_and_occupancy(tmp_path):
+    t = Autotuner(cache_path=str(tmp_path / "tune.json"))
+    p = _FakePipe()
+    best, ms = t.tune(p, _record, key="w1")
+    assert best == (16, 8) and (p.bw, p.occ) == (16, 8)
+    assert len(ms) == 6 and p.recorded == 6
 
 
 def test_cache_is_reused_and_keyed(tmp_path):
     path = str(tmp_path / "tune.json")
     Autotuner(cache_path=path).tune(_FakePipe(), _record, key="w1")
     table = json.load(open(path))
-    assert len(table) == 1 and list(table.values())[0]["best"] == 16
+    assert len(table) == 1 and list(table.values())[0]["best"] == [16, 8]
     p = _FakePipe()
     best, _ = Autotuner(cache_path=path).tune(p, _record, key="w1")
-    assert best == 16 and p.bw == 16 and p.recorded == 0  # from the cache, nothing timed
+    assert best == (16, 8) and p.bw == 16 and p.recorded == 0  # from the cache, nothing timed
     p2 = _FakePipe()
     Autotuner(cache_path=path).tune(p2, _record, key="w2", candidates=(8, 32))
     assert p2.bw == 32 and p2.recorded == 2
@@ -79,4 +92,4 @@ def test_retune_ignores_cache(tmp_path):
     Autotuner(cache_path=path).tune(_FakePipe(), _record, key="w1")
     p = _FakePipe()
     Autotuner(cache_path=path).tune(p, _record, key="w1", retune=True)
-    assert p.recorded == 3
+    assert p.recorded == 6

@@ -55,13 +55,17 @@ def test_bin_capacity_replay(gpu_lib, monkeypatch):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("occupancy", [0, 8])
 @pytest.mark.parametrize("bin_w", [8, 16, 32])
 @pytest.mark.parametrize("case", ["kat_soup_depth", "c3_small"])
-def test_bin_widths_agree(gpu_lib, bin_w, case):
+def test_schedules_agree(gpu_lib, bin_w, occupancy, case):
+    """Every schedule (bin width x raster kernel variant) gives the oracle's
+    result."""
     from puresoft3d_gb300.pipeline import PuresoftPipeline
     name, scene = [c for c in CASES if c[0].startswith(case)][0]
     g = PuresoftPipeline(scene.width, scene.height)
     g.setBinWidth(bin_w)
+    g.setRasterOccupancy(occupancy)
     assert g.binWidth() == bin_w
     out = render(g, scene)
     ref = render(OraclePipeline(scene.width, scene.height), scene)

@@ -73,7 +73,7 @@ def _quads(n, w, h):
 
 @pytest.mark.gpu
 def test_noalloc_refuses_oversized_pass(gpu_lib):
-    """A 2048x2048 colour pass needs 16 MiB for its winner buffer alone."""
+    """A 2048x2048 colour pass needs 32 MiB for its shade list alone."""
     from puresoft3d_gb300 import scenes as S
     from puresoft3d_gb300.pipeline import PuresoftPipeline
     scene = _quads(4, 2048, 2048)
