@@ -30,13 +30,16 @@
 #include "ps3d_internal.h"
 
 namespace ps3d {
-void launch_setup_and_bin(const PassParams& P, int* scanTmp, cudaStream_t s, int& launches, Prof* pr);
+void launch_setup(const PassParams& P, int* scanTmp, cudaStream_t s, int& launches, Prof* pr);
+void launch_emit(const PassParams& P, cudaStream_t s, int& launches, Prof* pr);
+void launch_sort(const PassParams& P, cudaStream_t s, int& launches, Prof* pr);
 int scan_block_sums_needed(int nMax);
 int radix_passes(int nBins);
 size_t radix_scratch_ints(int sortBlocks, int passes);
 int selftest_division(unsigned long long pairs, unsigned long long* rcpBad, unsigned long long* divBad);
-void launch_raster_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr);
-void launch_fill_u32(void* base, int width, int height, int pitchElems, uint32_t v, const int* status,
+void launch_raster(const PassParams& P, cudaStream_t s, int& launches, Prof* pr);
+void launch_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr);
+void launch_fill_u32(void* base, int width, int height, int pitchElems, uint32_t v, const int* status, int seq,
                      cudaStream_t s, int& launches, Prof* pr);
 }  // namespace ps3d
 
@@ -145,6 +148,52 @@ void m4m4(float* d, const float* l, const float* r)
     }
 }
 
+constexpr int kSlots = 2;
+
+// Device scratch of one pass.
+struct Scratch {
+    TriRaster* tris = nullptr; size_t trisCap = 0;
+    float* vary = nullptr; size_t varyCap = 0;
+    int* pairCount = nullptr; size_t pairCountCap = 0;
+    int4* rect = nullptr; size_t rectCap = 0;
+    int* pairOffset = nullptr; size_t pairOffsetCap = 0;
+    int* pairKey = nullptr; size_t pairKeyCap = 0;
+    int* pairTri = nullptr; size_t pairTriCap = 0;
+    int* binTri = nullptr; size_t binTriCap = 0;
+    int* radix = nullptr; size_t radixCap = 0;
+    int* keyB = nullptr; size_t keyBCap = 0;
+    int* binStart = nullptr; size_t binStartCap = 0;
+    int* scanTmp = nullptr; size_t scanTmpCap = 0;
+    int2* shadeList = nullptr; size_t shadeListCap = 0;
+    DrawDesc* draws = nullptr; size_t drawsCap = 0;
+    DrawUniforms* unis = nullptr; size_t unisCap = 0;
+    int* slotStatus = nullptr;  // 16 ints, allocated with the pipeline
+};
+
+// Cross-stream hazards within one launch: per buffer (colour buffer, depth
+// targets, by device address) the event of its last writer and of the
+// readers since; and the previous pass's emit.
+struct Hazard {
+    cudaEvent_t write = nullptr;
+    std::vector<cudaEvent_t> reads;
+};
+struct Tracker {
+    std::vector<std::pair<const void*, Hazard>> res;
+    cudaEvent_t lastEmit = nullptr;
+    Hazard& at(const void* key)
+    {
+        for (auto& r : res)
+            if (r.first == key) return r.second;
+        res.emplace_back(key, Hazard());
+        return res.back().second;
+    }
+    void clear()
+    {
+        res.clear();
+        lastEmit = nullptr;
+    }
+};
+
 }  // namespace
 
 struct ps3d_pipeline {
@@ -174,24 +223,18 @@ struct ps3d_pipeline {
     std::vector<Command> launched;  // launched since the last verification
     std::vector<size_t> passStart;  // per launched pass: index in `launched` to re-run it from
 
-    // device scratch
-    TriRaster* tris = nullptr; size_t trisCap = 0;
-    float* vary = nullptr; size_t varyCap = 0;
-    int* pairCount = nullptr; size_t pairCountCap = 0;
-    int4* rect = nullptr; size_t rectCap = 0;
-    int* pairOffset = nullptr; size_t pairOffsetCap = 0;
-    int* pairKey = nullptr; size_t pairKeyCap = 0;
-    int* pairTri = nullptr; size_t pairTriCap = 0;
-    int* binTri = nullptr; size_t binTriCap = 0;
-    int* radix = nullptr; size_t radixCap = 0;
-    int* keyB = nullptr; size_t keyBCap = 0;
-    int* binStart = nullptr; size_t binStartCap = 0;
-    int* scanTmp = nullptr; size_t scanTmpCap = 0;
-    int2* shadeList = nullptr; size_t shadeListCap = 0;
-    DrawDesc* draws = nullptr; size_t drawsCap = 0;
-    DrawUniforms* unis = nullptr; size_t unisCap = 0;
+    // Passes alternate between two scratch slots, each with its own stream:
+    // pass k uses slot k % 2, so a pass can run while the previous one does
+    // (a slot is reused only by the pass two later, on the same stream).
+    // Work between passes and the cross-pass hazards go through `stream`.
+    Scratch scr[kSlots];
+    cudaStream_t gs[kSlots] = {};
     int* status = nullptr;
     int pairCap = 1 << 18;
+    std::vector<cudaEvent_t> evPool;     // events for cross-stream ordering, reused per launch
+    size_t evUsed = 0;
+    Tracker trk;
+    std::vector<const void*> depthTargetPtrs;  // textures ever bound as depth targets
 
     ps3d_stats_t stats = {};
     Prof prof;
@@ -362,19 +405,20 @@ int snapshot_uniforms(const ps3d_pipeline* p, DrawUniforms& U)
     return 0;
 }
 
-int ensure_scratch(ps3d_pipeline* p, int nTris, int nvMax, int W, int H, int binsX, int binsY, bool colour)
+int ensure_scratch(ps3d_pipeline* p, Scratch& x, int nTris, int nvMax, int W, int H, int binsX, int binsY,
+                   bool colour)
 {
     size_t nBins = (size_t)binsX * binsY;
     int sortBlocks = (p->pairCap + kSortChunk - 1) / kSortChunk;
-    bool ok = dev_alloc(p->tris, p->trisCap, nTris) && dev_alloc(p->vary, p->varyCap, (size_t)nTris * 3 * std::max(nvMax, 1)) &&
-              dev_alloc(p->pairCount, p->pairCountCap, nTris) && dev_alloc(p->rect, p->rectCap, nTris) &&
-              dev_alloc(p->pairOffset, p->pairOffsetCap, (size_t)nTris + 1) &&
-              dev_alloc(p->pairKey, p->pairKeyCap, p->pairCap) && dev_alloc(p->pairTri, p->pairTriCap, p->pairCap) &&
-              dev_alloc(p->keyB, p->keyBCap, p->pairCap) && dev_alloc(p->binTri, p->binTriCap, p->pairCap) &&
-              dev_alloc(p->radix, p->radixCap, radix_scratch_ints(sortBlocks, radix_passes((int)nBins))) &&
-              dev_alloc(p->binStart, p->binStartCap, nBins + 1) &&
-              dev_alloc(p->scanTmp, p->scanTmpCap, (size_t)scan_block_sums_needed(nTris) + 1);
-    if (ok && colour) ok = dev_alloc(p->shadeList, p->shadeListCap, (size_t)W * H);
+    bool ok = dev_alloc(x.tris, x.trisCap, nTris) && dev_alloc(x.vary, x.varyCap, (size_t)nTris * 3 * std::max(nvMax, 1)) &&
+              dev_alloc(x.pairCount, x.pairCountCap, nTris) && dev_alloc(x.rect, x.rectCap, nTris) &&
+              dev_alloc(x.pairOffset, x.pairOffsetCap, (size_t)nTris + 1) &&
+              dev_alloc(x.pairKey, x.pairKeyCap, p->pairCap) && dev_alloc(x.pairTri, x.pairTriCap, p->pairCap) &&
+              dev_alloc(x.keyB, x.keyBCap, p->pairCap) && dev_alloc(x.binTri, x.binTriCap, p->pairCap) &&
+              dev_alloc(x.radix, x.radixCap, radix_scratch_ints(sortBlocks, radix_passes((int)nBins))) &&
+              dev_alloc(x.binStart, x.binStartCap, nBins + 1) &&
+              dev_alloc(x.scanTmp, x.scanTmpCap, (size_t)scan_block_sums_needed(nTris) + 1);
+    if (ok && colour) ok = dev_alloc(x.shadeList, x.shadeListCap, (size_t)W * H);
     if (!ok) return fail(PS3D_ERR_NOMEM, "device scratch allocation failed");
     return 0;
 }
@@ -402,6 +446,55 @@ int depth_target(ps3d_pipeline* p, int idx, Target& t)
     return 0;
 }
 
+// ---- cross-stream ordering (see Tracker)
+cudaEvent_t next_event(ps3d_pipeline* p)
+{
+    if (p->evUsed == p->evPool.size()) {
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+        p->evPool.push_back(e);
+    }
+    return p->evPool[p->evUsed++];
+}
+
+int mark(ps3d_pipeline* p, cudaStream_t s, cudaEvent_t& e)
+{
+    e = next_event(p);
+    if (!e) return fail(PS3D_ERR_DEVICE, "cudaEventCreate failed");
+    CU(cudaEventRecord(e, s));
+    return 0;
+}
+
+int wait_event(cudaStream_t s, cudaEvent_t e)
+{
+    if (e) CU(cudaStreamWaitEvent(s, e, 0));
+    return 0;
+}
+
+// Before an operation on stream s writes `key`: after its last writer and readers.
+int before_write(ps3d_pipeline* p, cudaStream_t s, const void* key)
+{
+    Hazard& h = p->trk.at(key);
+    int rc = wait_event(s, h.write);
+    for (cudaEvent_t e : h.reads)
+        if (!rc) rc = wait_event(s, e);
+    return rc;
+}
+
+int before_read(ps3d_pipeline* p, cudaStream_t s, const void* key) { return wait_event(s, p->trk.at(key).write); }
+
+void wrote(ps3d_pipeline* p, const void* key, cudaEvent_t e)
+{
+    Hazard& h = p->trk.at(key);
+    h.write = e;
+    h.reads.clear();
+}
+
+void read_by(ps3d_pipeline* p, const void* key, cudaEvent_t e) { p->trk.at(key).reads.push_back(e); }
+
+// The index the next pass gets; fills and copies in front of it fail with it.
+int next_seq(const ps3d_pipeline* p) { return (int)p->passStart.size(); }
+
 int fill_depth(ps3d_pipeline* p, int target, float v)
 {
     Target t;
@@ -409,17 +502,57 @@ int fill_depth(ps3d_pipeline* p, int target, float v)
     if (rc) return rc;
     uint32_t bits;
     memcpy(&bits, &v, 4);
+    if ((rc = before_write(p, p->stream, t.depth))) return rc;
     int launches = 0;
-    launch_fill_u32(t.depth, t.scan, t.h, t.scan, bits, p->status, p->stream, launches, &p->prof);
+    launch_fill_u32(t.depth, t.scan, t.h, t.scan, bits, p->status, next_seq(p), p->stream, launches, &p->prof);
     p->stats.kernel_launches += launches;
+    cudaEvent_t e;
+    if ((rc = mark(p, p->stream, e))) return rc;
+    wrote(p, t.depth, e);
     return 0;
 }
 
 int fill_colour(ps3d_pipeline* p, uint32_t v)
 {
+    int rc = before_write(p, p->stream, p->colour);
+    if (rc) return rc;
     int launches = 0;
-    launch_fill_u32(p->colour, p->devW, p->devH, p->devW, v, p->status, p->stream, launches, &p->prof);
+    launch_fill_u32(p->colour, p->devW, p->devH, p->devW, v, p->status, next_seq(p), p->stream, launches, &p->prof);
     p->stats.kernel_launches += launches;
+    cudaEvent_t e;
+    if ((rc = mark(p, p->stream, e))) return rc;
+    wrote(p, p->colour, e);
+    return 0;
+}
+
+// The same on the pipeline's stream alone, for the single-stream
+// no-allocation path (no events).
+int fill_depth_plain(ps3d_pipeline* p, int target, float v)
+{
+    Target t;
+    int rc = depth_target(p, target, t);
+    if (rc) return rc;
+    uint32_t bits;
+    memcpy(&bits, &v, 4);
+    int launches = 0;
+    launch_fill_u32(t.depth, t.scan, t.h, t.scan, bits, p->status, next_seq(p), p->stream, launches, &p->prof);
+    p->stats.kernel_launches += launches;
+    return 0;
+}
+
+int fill_colour_plain(ps3d_pipeline* p, uint32_t v)
+{
+    int launches = 0;
+    launch_fill_u32(p->colour, p->devW, p->devH, p->devW, v, p->status, next_seq(p), p->stream, launches, &p->prof);
+    p->stats.kernel_launches += launches;
+    return 0;
+}
+
+int copy_colour_plain(ps3d_pipeline* p, const Command& c)
+{
+    const uint8_t* src = p->colour + ((size_t)(p->devH - c.copyY - c.copyH) * p->devW + c.copyX) * 4;
+    CU(cudaMemcpy2DAsync(c.copyDst, c.copyPitch, src, (size_t)p->devW * 4, (size_t)c.copyW * 4, c.copyH,
+                         cudaMemcpyDefault, p->stream));
     return 0;
 }
 
@@ -441,9 +574,33 @@ void pass_descriptors(const std::vector<Command>& cmds, const Pass& ps, std::vec
     }
 }
 
+// The textures a pass's shaders sample that are also depth targets (and so
+// may be written by passes of the same launch).
+void sampled_targets(const ps3d_pipeline* p, const std::vector<DrawUniforms>& uu, std::vector<const void*>& out)
+{
+    if (p->depthTargetPtrs.empty()) return;
+    auto add = [&](const void* ptr) {
+        if (!ptr) return;
+        if (std::find(p->depthTargetPtrs.begin(), p->depthTargetPtrs.end(), ptr) == p->depthTargetPtrs.end()) return;
+        if (std::find(out.begin(), out.end(), ptr) == out.end()) out.push_back(ptr);
+    };
+    for (const DrawUniforms& u : uu) {
+        add(u.tex.base);
+        for (int k = 0; k < u.albedoLevels && k < kMaxLevels; k++) add(u.albedo[k].base);
+        for (int k = 0; k < u.normalLevels && k < kMaxLevels; k++) add(u.normal[k].base);
+        add(u.shadow);
+    }
+}
+
+// One pass on its slot's stream: set-up and pair counts; the emit, after the
+// previous pass's emit (so that every later pass sees an overflow before it
+// rasterises); the sort; the raster, after the last writer and readers of its
+// depth target (and of the colour buffer when it clears colour); the shade,
+// after the last writer and readers of the colour buffer and the last writers
+// of the depth targets it samples.
 int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps, size_t replayFrom)
 {
-    int seq = (int)p->passStart.size();
+    const int seq = next_seq(p);
     p->passStart.push_back(replayFrom);
     const Command& c0 = cmds[ps.first];
     Target tg;
@@ -461,9 +618,13 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
         return 0;
     }
     g_retire = p->liveGraphs ? &p->retired : nullptr;
+    const int slot = seq % kSlots;
+    Scratch& x = p->scr[slot];
+    cudaStream_t s = p->gs[slot];
     int binW = p->binW;
     int binsX = (W + binW - 1) / binW, binsY = (H + kBinH - 1) / kBinH;
-    if ((rc = ensure_scratch(p, nTris, nvMax, W, H, binsX, binsY, anyColour))) return rc;
+    if (radix_passes(binsX * binsY) > kRadixMaxPasses) return fail(PS3D_ERR_RANGE, "target too large for the bin sort");
+    if ((rc = ensure_scratch(p, x, nTris, nvMax, W, H, binsX, binsY, anyColour))) return rc;
     const DrawDesc* devDraws;
     const DrawUniforms* devUnis;
     if (p->cbOffsets) {  // capturing a command buffer: its descriptors are already on the device
@@ -471,13 +632,13 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
         devDraws = p->cbDraws + off;
         devUnis = p->cbUnis + off;
     } else {
-        if (!dev_alloc(p->draws, p->drawsCap, dd.size()) || !dev_alloc(p->unis, p->unisCap, uu.size()))
+        if (!dev_alloc(x.draws, x.drawsCap, dd.size()) || !dev_alloc(x.unis, x.unisCap, uu.size()))
             return fail(PS3D_ERR_NOMEM, "device allocation for draw descriptors failed");
-        CU(cudaMemcpyAsync(p->draws, dd.data(), dd.size() * sizeof(DrawDesc), cudaMemcpyHostToDevice, p->stream));
-        CU(cudaMemcpyAsync(p->unis, uu.data(), uu.size() * sizeof(DrawUniforms), cudaMemcpyHostToDevice,
-                           p->stream));
-        devDraws = p->draws;
-        devUnis = p->unis;
+        // pageable sources: each copy returns once its source has been read
+        CU(cudaMemcpyAsync(x.draws, dd.data(), dd.size() * sizeof(DrawDesc), cudaMemcpyHostToDevice, s));
+        CU(cudaMemcpyAsync(x.unis, uu.data(), uu.size() * sizeof(DrawUniforms), cudaMemcpyHostToDevice, s));
+        devDraws = x.draws;
+        devUnis = x.unis;
     }
 
     // A clear fuses into the pass when the pass covers the whole buffer.
@@ -498,29 +659,30 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     P.nDraws = (int)dd.size();
     P.draws = devDraws;
     P.unis = devUnis;
-    P.tris = p->tris;
-    P.vary = p->vary;
+    P.tris = x.tris;
+    P.vary = x.vary;
     P.nvMax = std::max(nvMax, 1);
     P.anyVary = nvMax > 0;
-    P.pairCount = p->pairCount;
-    P.rect = p->rect;
-    P.pairOffset = p->pairOffset;
-    P.pairKey = p->pairKey;
-    P.pairTri = p->pairTri;
+    P.pairCount = x.pairCount;
+    P.rect = x.rect;
+    P.pairOffset = x.pairOffset;
+    P.pairKey = x.pairKey;
+    P.pairTri = x.pairTri;
     P.pairCap = p->pairCap;
     P.sortBlocks = (p->pairCap + kSortChunk - 1) / kSortChunk;
     P.radixPasses = radix_passes(binsX * binsY);
-    P.radix = p->radix;
-    P.keyB = p->keyB;
-    P.binStart = p->binStart;
-    P.binTri = p->binTri;
-    P.sortedTri = (P.radixPasses & 1) ? p->binTri : p->pairTri;
+    P.radix = x.radix;
+    P.keyB = x.keyB;
+    P.binStart = x.binStart;
+    P.binTri = x.binTri;
+    P.sortedTri = (P.radixPasses & 1) ? x.binTri : x.pairTri;
     P.status = p->status;
+    P.slotStatus = x.slotStatus;
     P.depth = tg.depth;
     P.depthScan = tg.scan;
     P.depthW = tg.w;
     P.depthH = tg.h;
-    P.shadeList = p->shadeList;
+    P.shadeList = x.shadeList;
     P.colour = p->colour;
     P.colourW = p->devW;
     P.colourH = p->devH;
@@ -532,8 +694,30 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     P.colourClearValue = ps.colourValue;
     P.passSeq = seq;
     int launches = 0;
-    launch_setup_and_bin(P, p->scanTmp, p->stream, launches, &p->prof);
-    launch_raster_shade(P, p->stream, launches, &p->prof);
+    cudaEvent_t e;
+    launch_setup(P, x.scanTmp, s, launches, &p->prof);
+    if ((rc = wait_event(s, p->trk.lastEmit))) return rc;
+    launch_emit(P, s, launches, &p->prof);
+    if ((rc = mark(p, s, e))) return rc;
+    p->trk.lastEmit = e;
+    launch_sort(P, s, launches, &p->prof);
+    if ((rc = before_write(p, s, tg.depth))) return rc;
+    if (fuseColour && (rc = before_write(p, s, p->colour))) return rc;
+    launch_raster(P, s, launches, &p->prof);
+    if ((rc = mark(p, s, e))) return rc;
+    wrote(p, tg.depth, e);
+    if (fuseColour) wrote(p, p->colour, e);
+    if (anyColour) {
+        std::vector<const void*> sampled;
+        sampled_targets(p, uu, sampled);
+        if ((rc = before_write(p, s, p->colour))) return rc;
+        for (const void* t : sampled)
+            if ((rc = before_read(p, s, t))) return rc;
+        launch_shade(P, s, launches, &p->prof);
+        if ((rc = mark(p, s, e))) return rc;
+        wrote(p, p->colour, e);
+        for (const void* t : sampled) read_by(p, t, e);
+    }
     CU(cudaGetLastError());
     p->stats.kernel_launches += launches;
     p->stats.batches++;
@@ -597,12 +781,38 @@ int plan_commands(const std::vector<Command>& cmds, size_t from, PassFn onPass, 
 int copy_colour(ps3d_pipeline* p, const Command& c)
 {
     const uint8_t* src = p->colour + ((size_t)(p->devH - c.copyY - c.copyH) * p->devW + c.copyX) * 4;
+    int rc = before_read(p, p->stream, p->colour);
+    if (rc) return rc;
     CU(cudaMemcpy2DAsync(c.copyDst, c.copyPitch, src, (size_t)p->devW * 4, (size_t)c.copyW * 4, c.copyH,
                          cudaMemcpyDefault, p->stream));
+    cudaEvent_t e;
+    if ((rc = mark(p, p->stream, e))) return rc;
+    read_by(p, p->colour, e);
     return 0;
 }
 
+// A launch forks the pass streams from the pipeline's stream and joins them
+// back at the end, so that everything before it precedes it and the
+// pipeline's stream sees all of it complete.
+int launch_cmds_inner(ps3d_pipeline* p, const std::vector<Command>& cmds, size_t from);
+
 int launch_cmds(ps3d_pipeline* p, const std::vector<Command>& cmds, size_t from)
+{
+    p->evUsed = 0;
+    p->trk.clear();
+    cudaEvent_t fork;
+    int rc = mark(p, p->stream, fork);
+    for (int k = 0; k < kSlots && !rc; k++) rc = wait_event(p->gs[k], fork);
+    if (rc) return rc;
+    int rc2 = launch_cmds_inner(p, cmds, from);
+    for (int k = 0; k < kSlots; k++) {  // join even after an error, so no work is left outside the stream
+        cudaEvent_t j;
+        if ((rc = mark(p, p->gs[k], j)) || (rc = wait_event(p->stream, j))) return rc;
+    }
+    return rc2;
+}
+
+int launch_cmds_inner(ps3d_pipeline* p, const std::vector<Command>& cmds, size_t from)
 {
     return plan_commands(
         cmds, from, [&](const Pass& ps, size_t start) { return run_pass(p, cmds, ps, start); },
@@ -621,9 +831,18 @@ int do_flush(ps3d_pipeline* p)
     return launch_range(p, from);
 }
 
-// Waits for the stream.  If a pass ran out of bin-list room it set the
-// overflow flag and recorded its sequence number; it and every pass after it
-// did nothing, while the passes before it completed.  The buffers grow and
+// Clears the failure words: flags and most pairs needed to 0, the first
+// failed pass to kNoPass.
+int reset_flags(ps3d_pipeline* p)
+{
+    CU(cudaMemsetAsync(p->status, 0, 3 * sizeof(int), p->stream));
+    CU(cudaMemsetAsync(p->status + kFirstFailed, 0x7f, sizeof(int), p->stream));
+    return 0;
+}
+
+// Waits for the stream.  If a pass ran out of bin-list room it recorded
+// itself as the first failed pass (the lowest such); it and every pass after
+// it did nothing, while the passes before it completed.  The buffers grow and
 // the commands are re-run from that pass (including the clears in front of
 // it, which are idempotent).
 int do_finish(ps3d_pipeline* p)
@@ -640,8 +859,8 @@ int do_finish(ps3d_pipeline* p)
             p->graphUnverified = nullptr;
             return 0;
         }
-        if (st[0] == 2) {
-            CU(cudaMemsetAsync(p->status, 0, 4 * sizeof(int), p->stream));
+        if (st[0] & 2) {
+            if ((rc = reset_flags(p))) return rc;
             p->launched.clear();
             p->passStart.clear();
             p->graphUnverified = nullptr;
@@ -649,7 +868,7 @@ int do_finish(ps3d_pipeline* p)
         }
         if (p->launched.empty() && p->graphUnverified) {
             // a graph launch outgrew the room its first submission verified
-            CU(cudaMemsetAsync(p->status, 0, 4 * sizeof(int), p->stream));
+            if ((rc = reset_flags(p))) return rc;
             ps3d_cmdbuf* cb = p->graphUnverified;
             p->graphUnverified = nullptr;
             cb->stale = true;
@@ -660,7 +879,7 @@ int do_finish(ps3d_pipeline* p)
         if (st[1] > kMaxPairs) return fail(PS3D_ERR_NOMEM, "a pass needs %d bin pairs (at most %d)", st[1], kMaxPairs);
         p->pairCap = (int)std::min<long long>(std::max<long long>((long long)p->pairCap * 2, (long long)st[1] * 5 / 4 + 1024),
                                               kMaxPairs);
-        CU(cudaMemsetAsync(p->status, 0, 4 * sizeof(int), p->stream));
+        if ((rc = reset_flags(p))) return rc;
         p->stats.replays++;
         size_t from = p->passStart[seq];
         p->passStart.resize(seq);
@@ -702,14 +921,19 @@ int ps3d_pipeline_create(int width, int height, void* stream, ps3d_pipeline** ou
     if (p->defDepthScan < width) p->defDepthScan = (width + 3) / 4 * 4;
     bool ok = cudaMalloc((void**)&p->colour, (size_t)width * 4 * height) == cudaSuccess &&
               cudaMalloc((void**)&p->defDepth, (size_t)p->defDepthScan * 4 * height) == cudaSuccess &&
-              cudaMalloc((void**)&p->status, 64) == cudaSuccess;
+              cudaMalloc((void**)&p->status, 64 * sizeof(int)) == cudaSuccess;
+    for (int k = 0; k < kSlots && ok; k++) {
+        p->scr[k].slotStatus = p->status + 16 * (k + 1);
+        ok = cudaStreamCreateWithFlags(&p->gs[k], cudaStreamNonBlocking) == cudaSuccess;
+    }
     if (!ok) {
         ps3d_pipeline_destroy(p);
         return fail(PS3D_ERR_NOMEM, "device allocation failed");
     }
     cudaMemsetAsync(p->colour, 0, (size_t)width * 4 * height, p->stream);
     cudaMemsetAsync(p->defDepth, 0, (size_t)p->defDepthScan * 4 * height, p->stream);
-    cudaMemsetAsync(p->status, 0, 64, p->stream);
+    cudaMemsetAsync(p->status, 0, 64 * sizeof(int), p->stream);
+    reset_flags(p);
     *out = p;
     return 0;
 }
@@ -736,9 +960,19 @@ int ps3d_pipeline_destroy(ps3d_pipeline* p)
                 cudaFree(b->dev);
                 delete b;
             }
-    void* bufs[] = {p->colour, p->defDepth, p->status, p->tris, p->vary, p->pairCount, p->rect, p->pairOffset,
-                    p->pairKey, p->pairTri, p->keyB, p->binTri, p->radix, p->binStart, p->scanTmp, p->shadeList, p->draws,
-                    p->unis};
+    for (int k = 0; k < kSlots; k++) {
+        Scratch& x = p->scr[k];
+        void* sb[] = {x.tris, x.vary, x.pairCount, x.rect, x.pairOffset, x.pairKey, x.pairTri, x.keyB, x.binTri,
+                      x.radix, x.binStart, x.scanTmp, x.shadeList, x.draws, x.unis};
+        for (void* b : sb)
+            if (b) cudaFree(b);
+        if (p->gs[k]) {
+            cudaStreamSynchronize(p->gs[k]);
+            cudaStreamDestroy(p->gs[k]);
+        }
+    }
+    for (cudaEvent_t e : p->evPool) cudaEventDestroy(e);
+    void* bufs[] = {p->colour, p->defDepth, p->status};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (p->ownStream && p->stream) cudaStreamDestroy(p->stream);
@@ -999,6 +1233,8 @@ int ps3d_set_depth(ps3d_pipeline* p, int idx)
     if (t.elemLen != 4 || t.scanline % 4) return fail(PS3D_ERR_INVALID, "setDepth: not an FP32 texture");
     if (t.wrap) return fail(PS3D_ERR_INVALID, "setDepth: a depth target must be CLAMP-addressed");
     p->depthTarget = idx;
+    if (std::find(p->depthTargetPtrs.begin(), p->depthTargetPtrs.end(), (const void*)t.dev) == p->depthTargetPtrs.end())
+        p->depthTargetPtrs.push_back(t.dev);
     return 0;
 }
 
@@ -1588,8 +1824,8 @@ int noalloc_run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const P
     int rc = noalloc_shape(p, cmds, ps, s, true);
     if (rc) return rc;
     if (s.nTris == 0) {
-        if (ps.clearDepth && (rc = fill_depth(p, c0.depthTarget, ps.depthValue))) return rc;
-        if (ps.clearColour && (rc = fill_colour(p, ps.colourValue))) return rc;
+        if (ps.clearDepth && (rc = fill_depth_plain(p, c0.depthTarget, ps.depthValue))) return rc;
+        if (ps.clearColour && (rc = fill_colour_plain(p, ps.colourValue))) return rc;
         return 0;
     }
     int W = s.tg.w, H = s.tg.h;
@@ -1603,8 +1839,8 @@ int noalloc_run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const P
 
     bool fuseDepth = ps.clearDepth && s.tg.scan == W;
     bool fuseColour = ps.clearColour && p->devW == W && p->devH == H;
-    if (ps.clearDepth && !fuseDepth && (rc = fill_depth(p, c0.depthTarget, ps.depthValue))) return rc;
-    if (ps.clearColour && !fuseColour && (rc = fill_colour(p, ps.colourValue))) return rc;
+    if (ps.clearDepth && !fuseDepth && (rc = fill_depth_plain(p, c0.depthTarget, ps.depthValue))) return rc;
+    if (ps.clearColour && !fuseColour && (rc = fill_colour_plain(p, ps.colourValue))) return rc;
 
     PassParams P;
     memset(&P, 0, sizeof P);
@@ -1636,6 +1872,7 @@ int noalloc_run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const P
     P.binTri = (int*)(base + L.binTri);
     P.sortedTri = (P.radixPasses & 1) ? P.binTri : P.pairTri;
     P.status = p->status;
+    P.slotStatus = p->scr[0].slotStatus;
     P.depth = s.tg.depth;
     P.depthScan = s.tg.scan;
     P.depthW = s.tg.w;
@@ -1653,8 +1890,11 @@ int noalloc_run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const P
     P.passSeq = seq;
     Prof off;  // never records events
     int launches = 0;
-    launch_setup_and_bin(P, (int*)(base + L.scanTmp), p->stream, launches, &off);
-    launch_raster_shade(P, p->stream, launches, &off);
+    launch_setup(P, (int*)(base + L.scanTmp), p->stream, launches, &off);
+    launch_emit(P, p->stream, launches, &off);
+    launch_sort(P, p->stream, launches, &off);
+    launch_raster(P, p->stream, launches, &off);
+    launch_shade(P, p->stream, launches, &off);
     CU(cudaGetLastError());
     p->stats.kernel_launches += launches;
     p->stats.batches++;
@@ -1696,20 +1936,22 @@ extern "C" int ps3d_finish_noalloc(ps3d_pipeline* p)
         [&](int, float, uint32_t) { return 0; }, [&](const Command&) { return 0; });
     if (rc) return rc;
 
-    // The abort flag and the overflow record must start at zero.
-    CU(cudaMemsetAsync(p->status, 0, 4 * sizeof(int), p->stream));
+    // The failure words must start clear.
+    if ((rc = reset_flags(p))) return rc;
     p->launched.swap(p->pending);
     const std::vector<Command>& cmds = p->launched;
     rc = plan_commands(
         cmds, 0, [&](const Pass& ps, size_t start) { return noalloc_run_pass(p, cmds, ps, start, base); },
-        [&](int target, float v, uint32_t c) { return target == -3 ? fill_colour(p, c) : fill_depth(p, target, v); },
-        [&](const Command& c) { return copy_colour(p, c); });
+        [&](int target, float v, uint32_t c) {
+            return target == -3 ? fill_colour_plain(p, c) : fill_depth_plain(p, target, v);
+        },
+        [&](const Command& c) { return copy_colour_plain(p, c); });
     if (rc) return rc;
     CU(cudaStreamSynchronize(p->stream));
     int st[4];
     CU(cudaMemcpy(st, p->status, sizeof st, cudaMemcpyDeviceToHost));
-    if (st[0] == 2) {
-        CU(cudaMemsetAsync(p->status, 0, 4 * sizeof(int), p->stream));
+    if (st[0] & 2) {
+        if ((rc = reset_flags(p))) return rc;
         p->launched.clear();
         p->passStart.clear();
         return fail(PS3D_ERR_TIMEOUT, "a device-side wait of the bin sort expired; the frame is incomplete");

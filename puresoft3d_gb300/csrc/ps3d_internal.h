@@ -96,9 +96,11 @@ struct PassParams {
     int* binStart;            // first position of each bin's list; [nBins] = total
     int* binTri;              // the sort's second triangle buffer
     const int* sortedTri;     // triangles of each bin, in submission order (binTri or pairTri)
-    int* status;              // [0] overflow flag (2: a wait expired), [1] pairs needed, [2] sort
-                              // tiles in use, [3] overflowing pass, [4..5] fragments tested,
-                              // [6..7] passed, [8..9] pairs binned (u64), [10] shade-list length
+    int* status;              // the pipeline's: [0] bit 1 = a pass overflowed, bit 2 = a wait
+                              // expired; [1] most pairs a pass needed; [3] first pass that failed
+                              // (kNoPass when none); [4..5] fragments tested, [6..7] passed,
+                              // [8..9] pairs binned (u64)
+    int* slotStatus;          // this pass's scratch slot: [0] sort tiles in use, [1] shade-list length
     float* depth;             // depth target (rows bottom-up)
     int depthScan;            // in floats
     int depthW, depthH;
@@ -112,7 +114,19 @@ struct PassParams {
 };
 
 constexpr int kSortChunk = 4096;   // pairs per sort tile
-constexpr int kShadeCount = 10;    // status word holding the pass's shade-list length
+constexpr int kFirstFailed = 3;    // status word: the first pass that overflowed or timed out
+constexpr int kNoPass = 0x7f7f7f7f; // its value when none did (a byte-wise memset)
+constexpr int kSlotTiles = 0, kSlotShade = 1;  // slot status words
+
+// A pass's kernels do nothing once this pass or an earlier one has failed;
+// the host then re-runs the commands from the first failed pass.  Passes run
+// on two streams, so the word is read volatile: it can change while they run.
+#ifdef __CUDACC__
+__device__ __forceinline__ bool pass_failed(const int* status, int seq)
+{
+    return *(volatile const int*)(status + kFirstFailed) <= seq;
+}
+#endif
 constexpr int kRadixDigits = 256;
 constexpr int kRadixMaxPasses = 3;  // bin numbers below 2^24
 constexpr int kRadixHdr = 1024;     // ints before the descriptors (counts + tickets, padded)

@@ -31,7 +31,7 @@ namespace ps3d {
 
 __device__ __forceinline__ void bin_range(const PassParams& P, int bin, int& start, int& end)
 {
-    if (P.status[2] == 0) {  // no pairs
+    if (P.slotStatus[kSlotTiles] == 0) {  // no pairs
         start = end = 0;
         return;
     }
@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
     __shared__ unsigned sMask[2][4][kBinH][kSlots / 32];  // by round parity: rounds alternate buffers
     __shared__ int sWarpSum[kRasterThreads / 32];
     __shared__ int sListBase;
-    if (P.status[0]) return;
+    if (pass_failed(P.status, P.passSeq)) return;
 
     const int bin = blockIdx.x;
     const int bx = bin % P.binsX, by = bin / P.binsX;
@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
                 sWarpSum[w] = run;
                 run += v;
             }
-            sListBase = (P.anyColour && run) ? atomicAdd(P.status + kShadeCount, run) : 0;
+            sListBase = (P.anyColour && run) ? atomicAdd(P.slotStatus + kSlotShade, run) : 0;
         }
         __syncthreads();
         int pos = sListBase + sWarpSum[warp] + inc - covered;
@@ -411,15 +411,16 @@ __device__ __forceinline__ void shade_entry(const PassParams& P, int2 e)
 // length the raster kernel left in status[kShadeCount].
 __global__ void __launch_bounds__(256) k_shade(PassParams P)
 {
-    if (P.status[0]) return;
-    const int n = P.status[kShadeCount];
+    if (pass_failed(P.status, P.passSeq)) return;
+    const int n = P.slotStatus[kSlotShade];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         shade_entry(P, P.shadeList[i]);
 }
 
-__global__ void k_fill_u32(uint32_t* base, int width, int height, int pitchElems, uint32_t v, const int* status)
+__global__ void k_fill_u32(uint32_t* base, int width, int height, int pitchElems, uint32_t v, const int* status,
+                           int seq)
 {
-    if (status && status[0]) return;
+    if (status && pass_failed(status, seq)) return;
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int y = blockIdx.y;
     if (x < width && y < height) base[(size_t)y * pitchElems + x] = v;
@@ -433,7 +434,7 @@ template <int BW> void launch_raster(const PassParams& P, int nBins, cudaStream_
     else k_raster<BW, 1><<<nBins, kRasterThreads, 0, s>>>(P);
 }
 
-void launch_raster_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
+void launch_raster(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
 {
     int nBins = P.binsX * P.binsY;
     pr->begin(K_RASTER, s);
@@ -444,25 +445,29 @@ void launch_raster_shade(const PassParams& P, cudaStream_t s, int& launches, Pro
     }
     pr->end(s);
     launches++;
-    if (P.anyColour) {  // a grid that fills the GPU, striding over the shade list
-        int dev = 0, sms = 0, perSM = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shade, 256, 0);
-        long long need = ((long long)P.W * P.H + 255) / 256;
-        int grid = (int)std::min<long long>(need, (long long)std::max(sms, 1) * std::max(perSM, 1));
-        pr->begin(K_SHADE, s);
-        k_shade<<<std::max(grid, 1), 256, 0, s>>>(P);
-        pr->end(s);
-        launches++;
-    }
 }
 
-void launch_fill_u32(void* base, int width, int height, int pitchElems, uint32_t v, const int* status,
+void launch_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
+{
+    if (!P.anyColour) return;
+    // a grid that fills the GPU, striding over the shade list
+    int dev = 0, sms = 0, perSM = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shade, 256, 0);
+    long long need = ((long long)P.W * P.H + 255) / 256;
+    int grid = (int)std::min<long long>(need, (long long)std::max(sms, 1) * std::max(perSM, 1));
+    pr->begin(K_SHADE, s);
+    k_shade<<<std::max(grid, 1), 256, 0, s>>>(P);
+    pr->end(s);
+    launches++;
+}
+
+void launch_fill_u32(void* base, int width, int height, int pitchElems, uint32_t v, const int* status, int seq,
                      cudaStream_t s, int& launches, Prof* pr)
 {
     pr->begin(K_FILL, s);
-    k_fill_u32<<<dim3(ceil_div(width, 256), height), 256, 0, s>>>((uint32_t*)base, width, height, pitchElems, v, status);
+    k_fill_u32<<<dim3(ceil_div(width, 256), height), 256, 0, s>>>((uint32_t*)base, width, height, pitchElems, v, status, seq);
     pr->end(s);
     launches++;
 }

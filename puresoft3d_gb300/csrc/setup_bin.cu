@@ -256,7 +256,7 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(PassParams P)
     int t = blockIdx.x * kSetupThreads + threadIdx.x;
     if (blockIdx.x == 0) {  // the sort's digit counts and tile tickets, and the shade list, start empty
         for (int i = threadIdx.x; i < kRadixHdr; i += kSetupThreads) P.radix[i] = 0;
-        if (threadIdx.x == 0) P.status[kShadeCount] = 0;
+        if (threadIdx.x == 0) P.slotStatus[kSlotShade] = 0;
     }
     if (t < P.nTris) setup_triangle(P, t, sVary);
     if (!P.anyVary) return;
@@ -305,9 +305,9 @@ __device__ __forceinline__ int block_excl_scan(int v, int& total)
 }
 
 // n is read from *nPtr when nPtr != nullptr (sizes only known on the device).
-__global__ void k_scan_reduce(const int* in, int n, const int* nPtr, int* blockSums, const int* abortFlag)
+__global__ void k_scan_reduce(const int* in, int n, const int* nPtr, int* blockSums, const int* status, int seq)
 {
-    if (abortFlag && *abortFlag) return;
+    if (status && pass_failed(status, seq)) return;
     if (nPtr) n = *nPtr;
     int base = blockIdx.x * kScanTile;
     if (base >= n) return;
@@ -320,9 +320,9 @@ __global__ void k_scan_reduce(const int* in, int n, const int* nPtr, int* blockS
 }
 
 // Exclusive scan of the block sums in one block (up to kScanTile blocks).
-__global__ void k_scan_top(int* blockSums, int nBlocksMax, int n, const int* nPtr, const int* abortFlag)
+__global__ void k_scan_top(int* blockSums, int nBlocksMax, int n, const int* nPtr, const int* status, int seq)
 {
-    if (abortFlag && *abortFlag) return;
+    if (status && pass_failed(status, seq)) return;
     if (nPtr) n = *nPtr;
     int nb = (n + kScanTile - 1) / kScanTile;
     if (nb > nBlocksMax) nb = nBlocksMax;
@@ -340,9 +340,9 @@ __global__ void k_scan_top(int* blockSums, int nBlocksMax, int n, const int* nPt
 // out[i] = exclusive prefix of in (in-place allowed); out[n] = total when
 // writeTotal.
 __global__ void k_scan_down(const int* in, int* out, int n, const int* nPtr, const int* blockSums, int writeTotal,
-                            const int* abortFlag)
+                            const int* status, int seq)
 {
-    if (abortFlag && *abortFlag) return;
+    if (status && pass_failed(status, seq)) return;
     if (nPtr) n = *nPtr;
     int base = blockIdx.x * kScanTile;
     if (base >= n) return;
@@ -376,21 +376,20 @@ __global__ void __launch_bounds__(256) k_emit(PassParams P)
 {
     __shared__ int sHist[kRadixMaxPasses][kRadixDigits];
     int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (P.status[0]) return;
+    if (pass_failed(P.status, P.passSeq)) return;
     int total = P.pairOffset[P.nTris];
     if (total > P.pairCap) {
         if (t == 0) {
-            P.status[1] = total;
-            P.status[2] = 0;
-            P.status[3] = P.passSeq;
-            __threadfence();
-            atomicExch(P.status, 1);
+            P.slotStatus[kSlotTiles] = 0;
+            atomicMax(P.status + 1, total);
+            atomicMin(P.status + kFirstFailed, P.passSeq);
+            atomicOr(P.status, 1);
         }
         return;
     }
     const int tiles = (total + kSortChunk - 1) / kSortChunk;
     if (t == 0) {
-        P.status[2] = tiles;
+        P.slotStatus[kSlotTiles] = tiles;
         atomicAdd((unsigned long long*)(P.status + 8), (unsigned long long)total);
     }
     const int passes = P.radixPasses;
@@ -457,7 +456,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(PassParams P, int pas
     __shared__ int sScan[kSortWarps];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid == 0)  // one read of the flag for the whole block (it may change while the pass runs)
-        sTicket = P.status[0] ? -1 : atomicAdd(P.radix + kRadixMaxPasses * kRadixDigits + pass, 1);
+        sTicket = pass_failed(P.status, P.passSeq) ? -1 : atomicAdd(P.radix + kRadixMaxPasses * kRadixDigits + pass, 1);
     for (int i = tid; i < kSortWarps * kRadixDigits; i += kSortThreads) (&sWarpCnt[0][0])[i] = 0;
     __syncthreads();
     const int tile = sTicket;
@@ -510,8 +509,9 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(PassParams P, int pas
             unsigned f = v & ~kValueMask;
             if (f == 0u) {
                 if (++spins > kLookbackSpins) {
-                    atomicExch(P.status, 2);
-                    __threadfence();  // the flag is visible before the prefix below
+                    atomicMin(P.status + kFirstFailed, P.passSeq);
+                    atomicOr(P.status, 2);
+                    __threadfence();  // the failure is visible before the prefix below
                     break;
                 }
                 __nanosleep(32);
@@ -538,7 +538,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(PassParams P, int pas
     sBase[d] = wsum + inc - g + prefix;
     __threadfence();
     __syncthreads();
-    if (*(volatile int*)P.status) return;  // a wait expired somewhere: prefixes may be wrong
+    if (pass_failed(P.status, P.passSeq)) return;  // a wait expired: prefixes may be wrong
 #pragma unroll
     for (int gi = 0; gi < kSortGroups; gi++) {
         if (key[gi] < 0) continue;
@@ -554,7 +554,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(PassParams P, int pas
 // binary search, one thread per bin); binStart[nBins] = total.
 __global__ void k_bin_bounds(PassParams P, const int* __restrict__ keys)
 {
-    if (P.status[0]) return;
+    if (pass_failed(P.status, P.passSeq)) return;
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     int nBins = P.binsX * P.binsY;
     if (b > nBins) return;
@@ -574,13 +574,13 @@ __global__ void k_bin_bounds(PassParams P, const int* __restrict__ keys)
 static inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
 void scan_exclusive(const int* in, int* out, int n, const int* nPtr, int nMax, int* blockSums, int writeTotal,
-                    const int* abortFlag, cudaStream_t s, int& launches, Prof* pr)
+                    const int* status, int seq, cudaStream_t s, int& launches, Prof* pr)
 {
     int nb = ceil_div(nMax > 0 ? nMax : 1, kScanTile);
     pr->begin(K_SCAN, s);
-    k_scan_reduce<<<nb, kScanBlock, 0, s>>>(in, n, nPtr, blockSums, abortFlag);
-    k_scan_top<<<1, kScanBlock, 0, s>>>(blockSums, nb, n, nPtr, abortFlag);
-    k_scan_down<<<nb, kScanBlock, 0, s>>>(in, out, n, nPtr, blockSums, writeTotal, abortFlag);
+    k_scan_reduce<<<nb, kScanBlock, 0, s>>>(in, n, nPtr, blockSums, status, seq);
+    k_scan_top<<<1, kScanBlock, 0, s>>>(blockSums, nb, n, nPtr, status, seq);
+    k_scan_down<<<nb, kScanBlock, 0, s>>>(in, out, n, nPtr, blockSums, writeTotal, status, seq);
     pr->end(s);
     launches += 3;
 }
@@ -599,18 +599,33 @@ size_t radix_scratch_ints(int sortBlocks, int passes)
     return (size_t)kRadixHdr + (size_t)passes * sortBlocks * kRadixDigits;
 }
 
-void launch_setup_and_bin(const PassParams& P, int* scanTmp, cudaStream_t s, int& launches, Prof* pr)
+// A pass's set-up and binning in three parts, so that the host can order the
+// emits of passes on different streams (a pass must see every earlier pass's
+// overflow before it rasterises): set-up and the pair-count scan; the emit;
+// the radix passes and the bin starts.
+void launch_setup(const PassParams& P, int* scanTmp, cudaStream_t s, int& launches, Prof* pr)
 {
-    int nBins = P.binsX * P.binsY;
     pr->begin(K_SETUP, s);
     k_setup<<<ceil_div(P.nTris, kSetupThreads), kSetupThreads, 0, s>>>(P);
     pr->end(s);
     launches++;
-    scan_exclusive(P.pairCount, P.pairOffset, P.nTris, nullptr, P.nTris, scanTmp, 1, P.status, s, launches, pr);
+    scan_exclusive(P.pairCount, P.pairOffset, P.nTris, nullptr, P.nTris, scanTmp, 1, P.status, P.passSeq, s, launches,
+                   pr);
+}
+
+// The emit kernel alone, then the rest (the host waits for the previous
+// pass's emit in between).
+void launch_emit(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
+{
     pr->begin(K_EMIT, s);
     k_emit<<<ceil_div(P.nTris, 256), 256, 0, s>>>(P);
     pr->end(s);
     launches++;
+}
+
+void launch_sort(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
+{
+    int nBins = P.binsX * P.binsY;
     const int* key = P.pairKey;
     const int* tri = P.pairTri;
     pr->begin(K_SORT, s);
