@@ -67,6 +67,14 @@ CONFIGS = {
 }
 
 
+# DRAM bytes (read + write) of one raster launch on each workload, from one
+# ncu capture of the same kernel on the same full-size workload (one-pass
+# metrics dram__bytes_read.sum / dram__bytes_write.sum; the command and the
+# per-launch figures are in profiles/raster_dram_traffic.md).  Averages over
+# the captured launches that ran to completion.
+RASTER_TRAFFIC = {"c1": 89344, "c2": 7052864, "c3": 114543000, "c4": 784941000}
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -77,54 +85,116 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons, sampled during the timed region."""
+    """SM clocks and throttle reasons sampled during the timed region: NVML
+    through ctypes every millisecond (reads only), else nvidia-smi."""
 
-    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
-         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-         "clocks_event_reasons.sw_power_cap")
+    # NVML clocks-event reason bits
+    REASONS = {0x8: "hw_slowdown", 0x40: "hw_thermal_slowdown", 0x20: "sw_thermal_slowdown", 0x4: "sw_power_cap"}
 
     def __init__(self):
+        self.samples = []      # (sm_mhz, reasons bitmask)
+        self.max_mhz = None
+        self.stop_flag = threading.Event()
+        self.thread = None
+        self.nvml = None
         self.proc = None
         self.lines = []
 
+    def _nvml_open(self):
+        import ctypes
+        for name in ("libnvidia-ml.so.1", "libnvidia-ml.so"):
+            try:
+                lib = ctypes.CDLL(name)
+                break
+            except OSError:
+                lib = None
+        if lib is None or lib.nvmlInit_v2() != 0:
+            return False
+        idx = int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or 0)
+        h = ctypes.c_void_p()
+        if lib.nvmlDeviceGetHandleByIndex_v2(idx, ctypes.byref(h)) != 0:
+            return False
+        mx = ctypes.c_uint()
+        if lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0:  # NVML_CLOCK_SM
+            self.max_mhz = float(mx.value)
+        reasons = None
+        for fn in ("nvmlDeviceGetCurrentClocksEventReasons", "nvmlDeviceGetCurrentClocksThrottleReasons"):
+            try:
+                reasons = getattr(lib, fn)
+                break
+            except AttributeError:
+                continue
+        self.nvml = (lib, h, reasons)
+        return True
+
+    def _nvml_loop(self):
+        import ctypes
+        lib, h, reasons = self.nvml
+        clk, rs = ctypes.c_uint(), ctypes.c_ulonglong()
+        while not self.stop_flag.is_set():
+            r = lib.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(clk))
+            rs.value = 0
+            if reasons is not None:
+                reasons(h, ctypes.byref(rs))
+            if r == 0:
+                self.samples.append((float(clk.value), int(rs.value)))
+            time.sleep(0.001)
+
     def start(self):
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+            if self._nvml_open():
+                self.thread = threading.Thread(target=self._nvml_loop, daemon=True)
+                self.thread.start()
+                return
+        except Exception:
+            self.nvml = None
+        try:
+            q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits",
                                           "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
-                                          "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
-            self.t.start()
+                                          "-lms", "20"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._smi_loop, daemon=True)
+            self.thread.start()
         except Exception:
             self.proc = None
 
-    def _read(self):
+    def _smi_loop(self):
+        bits = [0x8, 0x40, 0x20, 0x4]
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
-
-    def stop(self):
-        if not self.proc:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except Exception:
-            self.proc.kill()
-        sm, mx, reasons = [], None, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
-            parts = [x.strip() for x in ln.split(",")]
-            if len(parts) < 7:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 6:
                 continue
             try:
-                sm.append(float(parts[0]))
-                mx = float(parts[1])
+                mhz, self.max_mhz = float(parts[0]), float(parts[1])
             except ValueError:
                 continue
-            for n, v in zip(names, parts[3:7]):
+            m = 0
+            for b, v in zip(bits, parts[2:6]):
                 if v.lower() == "active":
+                    m |= b
+            self.samples.append((mhz, m))
+
+    def stop(self):
+        self.stop_flag.set()
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": self.max_mhz, "reasons": [], "samples": 0,
+                    "source": "nvml" if self.nvml else ("nvidia-smi" if self.proc else "unavailable")}
+        reasons = set()
+        for _, m in self.samples:
+            for b, n in self.REASONS.items():
+                if m & b:
                     reasons.add(n)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        return {"sm_mhz": statistics.median(x for x, _ in self.samples), "sm_max_mhz": self.max_mhz,
+                "reasons": sorted(reasons), "samples": len(self.samples), "source": "nvml" if self.nvml else "nvidia-smi"}
 
 
 def make_scene(cfg, views=4096):
@@ -173,6 +243,8 @@ def run_c4(args):
     pipe.setFragmentCounting(False)
     frags = st1["fragments"] - st0["fragments"]
     pairs = st1["bin_pairs"] - st0["bin_pairs"]
+    counts = {"pairs": pairs, "triangles": st1["triangles"] - st0["triangles"],
+              "shaded": st1["shaded"] - st0["shaded"]}
     launches_per_frame = st1["kernel_launches"] - st0["kernel_launches"]
 
     pipe.profile(True)
@@ -256,7 +328,7 @@ def run_c4(args):
     plain_ips = views / (plain_ms / 1e3)
     plain_graph_ips = views / (statistics.median(pg_ms) / 1e3)
 
-    ab = algorithmic_bytes(batched, pairs)
+    ab = algorithmic_bytes(batched, counts)
     dom = max(prof, key=lambda k: prof[k][1])
     n_launch, ms = prof[dom]
     avg_ms = ms / max(n_launch, 1)
@@ -284,7 +356,8 @@ def run_c4(args):
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2) if achieved else None,
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5) if achieved else None,
                      "peak_source": peak_kind, "avg_launch_ms": round(avg_ms, 5),
-                     "bytes_per_launch": bytes_per_launch, "traffic": None},
+                     "bytes_per_launch": bytes_per_launch,
+                     "traffic": RASTER_TRAFFIC.get("c4") if dom == "raster" and views == 4096 else None},
         "kernel_ms_per_step": {k: round(prof[k][1] / prof_frames, 5) for k in KERNELS if prof[k][0]},
         "clocks": clk,
     }
@@ -402,24 +475,23 @@ def run_frames_only(args):
     pipe.close()
 
 
-def algorithmic_bytes(scene, pairs_per_frame):
-    """Algorithmic bytes of one launch of each kernel family, and of a whole
-    frame: what the work must move at least once (writes of every target
-    pixel, reads of every input element the pass consumes)."""
+def algorithmic_bytes(scene, counts):
+    """Algorithmic bytes of the raster kernel per frame and per launch: what
+    its work must move at least once -- the depth target's write (every pass
+    here clears depth, fused into the raster), each triangle record once
+    (64 B), each (bin, triangle) index once (4 B), one shade-list entry per
+    covered pixel (8 B) and the clear colour of every uncovered pixel (4 B)."""
     info = scene.info
     w, h = scene.width, scene.height
-    tris = scene.triangles()
-    out = {}
+    depth = w * h * 4
+    launches = 1
     if scene.name == "c2":
         ss = info["shadow_size"]
-        px_raster = ss * ss * 4 + w * h * 4 * 2          # shadow depth; main depth + winner
-        out["raster_per_frame"] = px_raster + pairs_per_frame * (64 + 4)
-        out["raster_launches_per_frame"] = 2
-    else:
-        out["raster_per_frame"] = w * h * 4 * 2 + pairs_per_frame * (64 + 4)
-        out["raster_launches_per_frame"] = 1
-    out["tris"] = tris
-    return out
+        depth += ss * ss * 4
+        launches = 2
+    colour = counts["shaded"] * 8 + max(w * h - counts["shaded"], 0) * 4
+    per_frame = depth + colour + counts["triangles"] * 64 + counts["pairs"] * 4
+    return {"raster_per_frame": per_frame, "raster_launches_per_frame": launches}
 
 
 def run_ours(args):
@@ -441,6 +513,8 @@ def run_ours(args):
     pipe.setFragmentCounting(False)
     frags = st1["fragments"] - st0["fragments"]
     pairs = st1["bin_pairs"] - st0["bin_pairs"]
+    counts = {"pairs": pairs, "triangles": st1["triangles"] - st0["triangles"],
+              "shaded": st1["shaded"] - st0["shaded"]}
     launches_per_frame = st1["kernel_launches"] - st0["kernel_launches"]
 
     # per-kernel event timing over the non-graph path (untimed for value)
@@ -493,7 +567,7 @@ def run_ours(args):
 
     fps = WORLD * args.steps / (total_ms / 1e3)
     fps_e2e = WORLD * args.steps / e2e_s
-    ab = algorithmic_bytes(scene, pairs)
+    ab = algorithmic_bytes(scene, counts)
     # dominant kernel by event time share
     dom = max(prof, key=lambda k: prof[k][1])
     n_launch, ms = prof[dom]
@@ -520,7 +594,8 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2) if achieved else None,
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5) if achieved else None,
                      "peak_source": peak_kind, "avg_launch_ms": round(avg_ms, 5),
-                     "bytes_per_launch": bytes_per_launch, "traffic": None},
+                     "bytes_per_launch": bytes_per_launch,
+                     "traffic": RASTER_TRAFFIC.get(args.config) if dom == "raster" else None},
         "kernel_ms_per_frame": {k: round(prof[k][1] / prof_frames, 5) for k in KERNELS if prof[k][0]},
         "clocks": clk,
     }

@@ -30,12 +30,11 @@
 #include "ps3d_internal.h"
 
 namespace ps3d {
-void launch_setup(const PassParams& P, int* scanTmp, cudaStream_t s, int& launches, Prof* pr);
-void launch_emit(const PassParams& P, cudaStream_t s, int& launches, Prof* pr);
+int launch_setup(const PassParams& P, cudaStream_t s, int& launches, Prof* pr);
 void launch_sort(const PassParams& P, cudaStream_t s, int& launches, Prof* pr);
-int scan_block_sums_needed(int nMax);
 int radix_passes(int nBins);
-size_t radix_scratch_ints(int sortBlocks, int passes);
+int sort_desc_offset(int nTris);
+size_t radix_scratch_ints(int sortBlocks, int passes, int nTris);
 int selftest_division(unsigned long long pairs, unsigned long long* rcpBad, unsigned long long* divBad);
 void launch_raster(const PassParams& P, cudaStream_t s, int& launches, Prof* pr);
 void launch_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr);
@@ -149,21 +148,18 @@ void m4m4(float* d, const float* l, const float* r)
 }
 
 constexpr int kSlots = 2;
+constexpr int kMaxOverlapPasses = 16;  // launches with more passes run on one stream
 
 // Device scratch of one pass.
 struct Scratch {
     TriRaster* tris = nullptr; size_t trisCap = 0;
     float* vary = nullptr; size_t varyCap = 0;
-    int* pairCount = nullptr; size_t pairCountCap = 0;
-    int4* rect = nullptr; size_t rectCap = 0;
-    int* pairOffset = nullptr; size_t pairOffsetCap = 0;
     int* pairKey = nullptr; size_t pairKeyCap = 0;
     int* pairTri = nullptr; size_t pairTriCap = 0;
     int* binTri = nullptr; size_t binTriCap = 0;
     int* radix = nullptr; size_t radixCap = 0;
     int* keyB = nullptr; size_t keyBCap = 0;
     int* binStart = nullptr; size_t binStartCap = 0;
-    int* scanTmp = nullptr; size_t scanTmpCap = 0;
     int2* shadeList = nullptr; size_t shadeListCap = 0;
     DrawDesc* draws = nullptr; size_t drawsCap = 0;
     DrawUniforms* unis = nullptr; size_t unisCap = 0;
@@ -231,6 +227,7 @@ struct ps3d_pipeline {
     cudaStream_t gs[kSlots] = {};
     int* status = nullptr;
     int pairCap = 1 << 18;
+    bool oneStream = false;              // this launch has at most one pass: everything on `stream`
     std::vector<cudaEvent_t> evPool;     // events for cross-stream ordering, reused per launch
     size_t evUsed = 0;
     Tracker trk;
@@ -411,13 +408,10 @@ int ensure_scratch(ps3d_pipeline* p, Scratch& x, int nTris, int nvMax, int W, in
     size_t nBins = (size_t)binsX * binsY;
     int sortBlocks = (p->pairCap + kSortChunk - 1) / kSortChunk;
     bool ok = dev_alloc(x.tris, x.trisCap, nTris) && dev_alloc(x.vary, x.varyCap, (size_t)nTris * 3 * std::max(nvMax, 1)) &&
-              dev_alloc(x.pairCount, x.pairCountCap, nTris) && dev_alloc(x.rect, x.rectCap, nTris) &&
-              dev_alloc(x.pairOffset, x.pairOffsetCap, (size_t)nTris + 1) &&
               dev_alloc(x.pairKey, x.pairKeyCap, p->pairCap) && dev_alloc(x.pairTri, x.pairTriCap, p->pairCap) &&
               dev_alloc(x.keyB, x.keyBCap, p->pairCap) && dev_alloc(x.binTri, x.binTriCap, p->pairCap) &&
-              dev_alloc(x.radix, x.radixCap, radix_scratch_ints(sortBlocks, radix_passes((int)nBins))) &&
-              dev_alloc(x.binStart, x.binStartCap, nBins + 1) &&
-              dev_alloc(x.scanTmp, x.scanTmpCap, (size_t)scan_block_sums_needed(nTris) + 1);
+              dev_alloc(x.radix, x.radixCap, radix_scratch_ints(sortBlocks, radix_passes((int)nBins), nTris)) &&
+              dev_alloc(x.binStart, x.binStartCap, nBins + 1);
     if (ok && colour) ok = dev_alloc(x.shadeList, x.shadeListCap, (size_t)W * H);
     if (!ok) return fail(PS3D_ERR_NOMEM, "device scratch allocation failed");
     return 0;
@@ -459,6 +453,8 @@ cudaEvent_t next_event(ps3d_pipeline* p)
 
 int mark(ps3d_pipeline* p, cudaStream_t s, cudaEvent_t& e)
 {
+    e = nullptr;
+    if (p->oneStream) return 0;  // one stream orders everything
     e = next_event(p);
     if (!e) return fail(PS3D_ERR_DEVICE, "cudaEventCreate failed");
     CU(cudaEventRecord(e, s));
@@ -592,10 +588,10 @@ void sampled_targets(const ps3d_pipeline* p, const std::vector<DrawUniforms>& uu
     }
 }
 
-// One pass on its slot's stream: set-up and pair counts; the emit, after the
-// previous pass's emit (so that every later pass sees an overflow before it
-// rasterises); the sort; the raster, after the last writer and readers of its
-// depth target (and of the colour buffer when it clears colour); the shade,
+// One pass on its slot's stream: set-up and pair counts, the emit and the
+// sort; the raster, after every earlier pass has emitted (so that it sees
+// their overflows) and after the last writer and readers of its depth target
+// (and of the colour buffer when it clears colour); the shade,
 // after the last writer and readers of the colour buffer and the last writers
 // of the depth targets it samples.
 int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps, size_t replayFrom)
@@ -620,7 +616,7 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     g_retire = p->liveGraphs ? &p->retired : nullptr;
     const int slot = seq % kSlots;
     Scratch& x = p->scr[slot];
-    cudaStream_t s = p->gs[slot];
+    cudaStream_t s = p->oneStream ? p->stream : p->gs[slot];
     int binW = p->binW;
     int binsX = (W + binW - 1) / binW, binsY = (H + kBinH - 1) / kBinH;
     if (radix_passes(binsX * binsY) > kRadixMaxPasses) return fail(PS3D_ERR_RANGE, "target too large for the bin sort");
@@ -663,15 +659,13 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     P.vary = x.vary;
     P.nvMax = std::max(nvMax, 1);
     P.anyVary = nvMax > 0;
-    P.pairCount = x.pairCount;
-    P.rect = x.rect;
-    P.pairOffset = x.pairOffset;
     P.pairKey = x.pairKey;
     P.pairTri = x.pairTri;
     P.pairCap = p->pairCap;
     P.sortBlocks = (p->pairCap + kSortChunk - 1) / kSortChunk;
     P.radixPasses = radix_passes(binsX * binsY);
     P.radix = x.radix;
+    P.sortDescOff = sort_desc_offset(nTris);
     P.keyB = x.keyB;
     P.binStart = x.binStart;
     P.binTri = x.binTri;
@@ -695,12 +689,13 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     P.passSeq = seq;
     int launches = 0;
     cudaEvent_t e;
-    launch_setup(P, x.scanTmp, s, launches, &p->prof);
+    if (launch_setup(P, s, launches, &p->prof)) return fail(PS3D_ERR_DEVICE, "memset of the sort scratch failed");
+    launch_sort(P, s, launches, &p->prof);
+    // "this pass and every earlier one have emitted": the raster must see
+    // their overflows (the mark after the wait carries the chain on)
     if ((rc = wait_event(s, p->trk.lastEmit))) return rc;
-    launch_emit(P, s, launches, &p->prof);
     if ((rc = mark(p, s, e))) return rc;
     p->trk.lastEmit = e;
-    launch_sort(P, s, launches, &p->prof);
     if ((rc = before_write(p, s, tg.depth))) return rc;
     if (fuseColour && (rc = before_write(p, s, p->colour))) return rc;
     launch_raster(P, s, launches, &p->prof);
@@ -800,6 +795,15 @@ int launch_cmds(ps3d_pipeline* p, const std::vector<Command>& cmds, size_t from)
 {
     p->evUsed = 0;
     p->trk.clear();
+    int passes = 0;
+    plan_commands(
+        cmds, from, [&](const Pass&, size_t) { return ++passes, 0; }, [&](int, float, uint32_t) { return 0; },
+        [&](const Command&) { return 0; });
+    // Two streams pay off for a few large passes (a shadow pass and a lit
+    // pass); for many small passes the events cost more than the overlap
+    // gains, and graphs of them instantiate slowly.
+    p->oneStream = passes <= 1 || passes > kMaxOverlapPasses;
+    if (p->oneStream) return launch_cmds_inner(p, cmds, from);
     cudaEvent_t fork;
     int rc = mark(p, p->stream, fork);
     for (int k = 0; k < kSlots && !rc; k++) rc = wait_event(p->gs[k], fork);
@@ -962,8 +966,8 @@ int ps3d_pipeline_destroy(ps3d_pipeline* p)
             }
     for (int k = 0; k < kSlots; k++) {
         Scratch& x = p->scr[k];
-        void* sb[] = {x.tris, x.vary, x.pairCount, x.rect, x.pairOffset, x.pairKey, x.pairTri, x.keyB, x.binTri,
-                      x.radix, x.binStart, x.scanTmp, x.shadeList, x.draws, x.unis};
+        void* sb[] = {x.tris, x.vary, x.pairKey, x.pairTri, x.keyB, x.binTri, x.radix, x.binStart, x.shadeList,
+                      x.draws, x.unis};
         for (void* b : sb)
             if (b) cudaFree(b);
         if (p->gs[k]) {
@@ -1476,12 +1480,13 @@ int ps3d_stats(ps3d_pipeline* p, ps3d_stats_t* out)
     if (!p || !out) return fail(PS3D_ERR_INVALID, "null argument");
     int rc = do_finish(p);
     if (rc) return rc;
-    unsigned long long c[3];
+    unsigned long long c[4];
     CU(cudaMemcpy(c, p->status + 4, sizeof c, cudaMemcpyDeviceToHost));
     *out = p->stats;
     out->fragments = c[0];
     out->fragments_passed = c[1];
     out->bin_pairs = c[2];
+    out->shaded = c[3];
     return 0;
 }
 
@@ -1726,7 +1731,7 @@ DrawUniforms g_noallocUnis[kNoAllocMaxDraws];
 
 // Byte offsets of one pass's buffers in the array, each 256-byte aligned.
 struct NoAllocLayout {
-    size_t draws, unis, tris, vary, pairCount, rect, pairOffset, scanTmp, shadeList, binStart, radix, pairKey,
+    size_t draws, unis, tris, vary, shadeList, binStart, radix, pairKey,
         pairTri, keyB, binTri;
 };
 
@@ -1745,13 +1750,9 @@ size_t noalloc_layout(NoAllocLayout& L, int nd, int nTris, int nv, int W, int H,
     L.unis = take((size_t)nd * sizeof(DrawUniforms));
     L.tris = take((size_t)nTris * sizeof(TriRaster));
     L.vary = take((size_t)nTris * 3 * std::max(nv, 1) * sizeof(float));
-    L.pairCount = take((size_t)nTris * sizeof(int));
-    L.rect = take((size_t)nTris * sizeof(int4));
-    L.pairOffset = take(((size_t)nTris + 1) * sizeof(int));
-    L.scanTmp = take(((size_t)scan_block_sums_needed(nTris) + 1) * sizeof(int));
     L.shadeList = colour ? take((size_t)W * H * sizeof(int2)) : 0;
     L.binStart = take((nBins + 1) * sizeof(int));
-    L.radix = take(radix_scratch_ints((int)sortBlocks, radix_passes((int)nBins)) * sizeof(int));
+    L.radix = take(radix_scratch_ints((int)sortBlocks, radix_passes((int)nBins), nTris) * sizeof(int));
     L.pairKey = take((size_t)pairCap * sizeof(int));
     L.pairTri = take((size_t)pairCap * sizeof(int));
     L.keyB = take((size_t)pairCap * sizeof(int));
@@ -1858,15 +1859,13 @@ int noalloc_run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const P
     P.vary = (float*)(base + L.vary);
     P.nvMax = std::max(s.nvMax, 1);
     P.anyVary = s.nvMax > 0;
-    P.pairCount = (int*)(base + L.pairCount);
-    P.rect = (int4*)(base + L.rect);
-    P.pairOffset = (int*)(base + L.pairOffset);
     P.pairKey = (int*)(base + L.pairKey);
     P.pairTri = (int*)(base + L.pairTri);
     P.pairCap = s.pairCap;
     P.sortBlocks = (s.pairCap + kSortChunk - 1) / kSortChunk;
     P.radixPasses = radix_passes((int)s.nBins);
     P.radix = (int*)(base + L.radix);
+    P.sortDescOff = sort_desc_offset(s.nTris);
     P.keyB = (int*)(base + L.keyB);
     P.binStart = (int*)(base + L.binStart);
     P.binTri = (int*)(base + L.binTri);
@@ -1890,8 +1889,7 @@ int noalloc_run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const P
     P.passSeq = seq;
     Prof off;  // never records events
     int launches = 0;
-    launch_setup(P, (int*)(base + L.scanTmp), p->stream, launches, &off);
-    launch_emit(P, p->stream, launches, &off);
+    if (launch_setup(P, p->stream, launches, &off)) return fail(PS3D_ERR_DEVICE, "memset of the sort scratch failed");
     launch_sort(P, p->stream, launches, &off);
     launch_raster(P, p->stream, launches, &off);
     launch_shade(P, p->stream, launches, &off);

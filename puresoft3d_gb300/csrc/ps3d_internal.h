@@ -82,16 +82,15 @@ struct PassParams {
     float* vary;              // [tri][3][nvMax]
     int nvMax;
     int anyVary;              // some draw of the pass carries varyings
-    int* pairCount;           // per triangle: bins its rectangle touches
-    int4* rect;               // per triangle: bin rectangle {x0, x1, y0, y1}
-    int* pairOffset;          // exclusive scan of pairCount (+ total at [nTris])
     int* pairKey;             // bin of each (tri, bin) pair, in triangle order
     int* pairTri;
     int pairCap;              // capacity of pairKey / pairTri / keyB / binTri
     int sortBlocks;           // sort tiles that fit pairCap: ceil(pairCap / kSortChunk)
     int radixPasses;          // 8-bit digit passes the bin numbers need (0 for one bin)
-    int* radix;               // [pass][256] digit counts, [pass] tile tickets, then at kRadixHdr
-                              // the look-back descriptors [pass][tile][256]
+    int* radix;               // [pass][256] digit counts, tickets; at kRadixHdr the set-up blocks'
+                              // look-back descriptors (u64), at sortDescOff the radix passes'
+                              // [pass][tile][256]; zeroed before each pass
+    int sortDescOff;
     int* keyB;                // the sort's second key buffer
     int* binStart;            // first position of each bin's list; [nBins] = total
     int* binTri;              // the sort's second triangle buffer
@@ -99,7 +98,7 @@ struct PassParams {
     int* status;              // the pipeline's: [0] bit 1 = a pass overflowed, bit 2 = a wait
                               // expired; [1] most pairs a pass needed; [3] first pass that failed
                               // (kNoPass when none); [4..5] fragments tested, [6..7] passed,
-                              // [8..9] pairs binned (u64)
+                              // [8..9] pairs binned, [10..11] pixels shaded (u64)
     int* slotStatus;          // this pass's scratch slot: [0] sort tiles in use, [1] shade-list length
     float* depth;             // depth target (rows bottom-up)
     int depthScan;            // in floats
@@ -116,7 +115,7 @@ struct PassParams {
 constexpr int kSortChunk = 4096;   // pairs per sort tile
 constexpr int kFirstFailed = 3;    // status word: the first pass that overflowed or timed out
 constexpr int kNoPass = 0x7f7f7f7f; // its value when none did (a byte-wise memset)
-constexpr int kSlotTiles = 0, kSlotShade = 1;  // slot status words
+constexpr int kSlotTiles = 0, kSlotShade = 1, kSlotTotal = 2;  // slot status words: sort tiles, shade list, pairs
 
 // A pass's kernels do nothing once this pass or an earlier one has failed;
 // the host then re-runs the commands from the first failed pass.  Passes run
@@ -130,6 +129,7 @@ __device__ __forceinline__ bool pass_failed(const int* status, int seq)
 constexpr int kRadixDigits = 256;
 constexpr int kRadixMaxPasses = 3;  // bin numbers below 2^24
 constexpr int kRadixHdr = 1024;     // ints before the descriptors (counts + tickets, padded)
+constexpr int kTicketSetup = kRadixMaxPasses * kRadixDigits + kRadixMaxPasses;  // after the sort's tickets
 
 // Kernel families timed by the profiler (ps3d_profile_*).
 enum KernelId { K_SETUP, K_SCAN, K_EMIT, K_BOUNDS, K_SORT, K_RASTER, K_SHADE, K_FILL, K_COUNT };

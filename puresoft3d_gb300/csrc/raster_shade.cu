@@ -307,14 +307,17 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
         }
     }
     if (P.countFrags) {
+        unsigned long long cov = P.anyColour ? (unsigned long long)covered : 0ull;
 #pragma unroll
         for (int o = 16; o; o >>= 1) {
             tested += __shfl_xor_sync(0xffffffffu, tested, o);
             passed += __shfl_xor_sync(0xffffffffu, passed, o);
+            cov += __shfl_xor_sync(0xffffffffu, cov, o);
         }
         if (lane == 0) {
             atomicAdd((unsigned long long*)(P.status + 4), tested);
             atomicAdd((unsigned long long*)(P.status + 6), passed);
+            atomicAdd((unsigned long long*)(P.status + 10), cov);
         }
     }
 }

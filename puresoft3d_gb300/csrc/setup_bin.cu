@@ -1,18 +1,19 @@
 // setup_bin.cu -- vertex stage, triangle set-up and ordered tile binning.
 //
-//   k_setup    one thread per triangle: VBO fetch, vertex processor,
-//              perspective divide, back-face cull, z-reject and the
-//              rasteriser's triangle set-up (reference drawvao.cpp:36-63,
-//              vertthrd.cpp:14-65, rasterizer.cpp:73-234), plus the bin
-//              rectangle the triangle's spans can touch.
-//   scan       exclusive prefix sums (three-phase reduce / scan / down-sweep).
-//   k_emit     (bin, triangle) pairs in triangle order.
-//   k_hist / k_scatter
-//              a stable counting sort of the pairs by bin, so that each bin
-//              lists its triangles in submission order -- per pixel the
-//              reference applies fragments in that order (its per-row FIFO
-//              queues, drawvao.cpp:77-109), and the depth test's epsilon
-//              makes the order observable (fragthrd.cpp:227).
+//   k_setup_emit  one thread per triangle: VBO fetch, vertex processor,
+//                 perspective divide, back-face cull, z-reject and the
+//                 rasteriser's triangle set-up (reference drawvao.cpp:36-63,
+//                 vertthrd.cpp:14-65, rasterizer.cpp:73-234), the bin
+//                 rectangle the triangle's spans can touch, and -- after a
+//                 scan of the pair counts across blocks by decoupled
+//                 look-back -- its (bin, triangle) pairs in triangle order.
+//   k_onesweep    stable LSD radix passes over the pairs by bin, so that
+//                 each bin lists its triangles in submission order -- per
+//                 pixel the reference applies fragments in that order (its
+//                 per-row FIFO queues, drawvao.cpp:77-109), and the depth
+//                 test's epsilon makes the order observable
+//                 (fragthrd.cpp:227).
+//   k_bin_bounds  each bin's first position in the sorted list.
 #include <cuda_runtime.h>
 #include "device_common.cuh"
 
@@ -109,7 +110,7 @@ __device__ __forceinline__ int edge_code(int a, int b) { return a | (b << 2); }
 
 constexpr int kSetupThreads = 128;
 
-__device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float* sVary)
+__device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float* sVary, int& pairs, int4& rect)
 {
     int lo = 0, hi = P.nDraws - 1;
     while (lo < hi) {
@@ -244,183 +245,135 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float
     const float4* src = (const float4*)&tr;
 #pragma unroll
     for (int k = 0; k < 4; k++) dst[k] = src[k];
-    P.pairCount[t] = count;
-    P.rect[t] = make_int4(bx0, bx1, by0, by1);
+    pairs = count;
+    rect = make_int4(bx0, bx1, by0, by1);
 }
 
-// The varyings go out through shared memory so that the block's stores are
-// contiguous: triangle t's 3*nvMax floats start at vary + t*3*nvMax.
-__global__ void __launch_bounds__(kSetupThreads) k_setup(PassParams P)
+// Set-up, pair offsets and pair emission in one kernel.  Block b (numbered
+// by an atomic ticket, so that it only ever waits for blocks already
+// running) sets up triangles [b*128, b*128+128): each thread one triangle
+// (vertex processor, divide, cull, z-reject, row range, bin rectangle); the
+// varyings go out through shared memory so that the block's stores are
+// contiguous.  The block's pair counts are scanned in the block and its
+// global offset found by decoupled look-back over the earlier blocks
+// (64-bit descriptors: flag << 62 | value; each wait bounded), then every
+// triangle writes its (bin, triangle) pairs in triangle order, and the radix
+// sort's digit histograms are counted in shared memory.  The last block
+// knows the total: it records the pass's pair count and sort tiles, or the
+// overflow when the pairs do not fit (pairs past the capacity are never
+// written).  The header (tickets, histograms) and all descriptors are
+// zeroed by a memset before the kernel.
+constexpr int kLookbackSpins = 1 << 22;  // bounded waits: ~0.1 s and more, then the pass fails
+constexpr unsigned long long kDescAgg = 1ull << 62, kDescPrefix = 2ull << 62, kDescValue = (1ull << 62) - 1;
+
+__global__ void __launch_bounds__(kSetupThreads) k_setup_emit(PassParams P)
 {
     __shared__ float sVary[kSetupThreads * 3 * kMaxVary];
-    int t = blockIdx.x * kSetupThreads + threadIdx.x;
-    if (blockIdx.x == 0) {  // the sort's digit counts and tile tickets, and the shade list, start empty
-        for (int i = threadIdx.x; i < kRadixHdr; i += kSetupThreads) P.radix[i] = 0;
-        if (threadIdx.x == 0) P.slotStatus[kSlotShade] = 0;
-    }
-    if (t < P.nTris) setup_triangle(P, t, sVary);
-    if (!P.anyVary) return;
+    __shared__ int sHist[kRadixMaxPasses][kRadixDigits];
+    __shared__ int sWarp[kSetupThreads / 32];
+    __shared__ int sTicket, sPrefix;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) sTicket = atomicAdd(P.radix + kTicketSetup, 1);
+    for (int i = tid; i < kRadixMaxPasses * kRadixDigits; i += kSetupThreads) (&sHist[0][0])[i] = 0;
     __syncthreads();
-    int first = blockIdx.x * kSetupThreads, n = min(kSetupThreads, P.nTris - first);
-    int nf = n * 3 * P.nvMax;
-    float* dst = P.vary + (size_t)first * 3 * P.nvMax;
-    for (int i = threadIdx.x; i < nf; i += kSetupThreads) dst[i] = sVary[i];
-}
+    const int b = sTicket;
+    const int first = b * kSetupThreads, t = first + tid;
+    int count = 0;
+    int4 rect = make_int4(0, -1, 0, -1);
+    if (t < P.nTris) setup_triangle(P, t, sVary, count, rect);
+    if (b == 0 && tid == 0) P.slotStatus[kSlotShade] = 0;  // the shade list starts empty
 
-// ---------------------------------------------------------------- prefix sum
-
-constexpr int kScanBlock = 256;
-constexpr int kScanItems = 16;
-constexpr int kScanTile = kScanBlock * kScanItems;
-
-__device__ __forceinline__ int warp_incl_scan(int v)
-{
-    int lane = threadIdx.x & 31;
+    // block scan of the pair counts
+    int inc = count;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        int n = __shfl_up_sync(0xffffffffu, v, o);
-        if (lane >= o) v += n;
+        int v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += v;
     }
-    return v;
-}
-
-// Block-wide exclusive scan of one value per thread; returns the block total.
-__device__ __forceinline__ int block_excl_scan(int v, int& total)
-{
-    __shared__ int warpSums[kScanBlock / 32];
-    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    int inc = warp_incl_scan(v);
-    if (lane == 31) warpSums[wid] = inc;
+    if (lane == 31) sWarp[warp] = inc;
     __syncthreads();
-    if (wid == 0) {
-        int s = lane < kScanBlock / 32 ? warpSums[lane] : 0;
-        s = warp_incl_scan(s);
-        if (lane < kScanBlock / 32) warpSums[lane] = s;
+    if (P.anyVary) {
+        int n = min(kSetupThreads, P.nTris - first), nf = n * 3 * P.nvMax;
+        float* dst = P.vary + (size_t)first * 3 * P.nvMax;
+        for (int i = tid; i < nf; i += kSetupThreads) dst[i] = sVary[i];
     }
-    __syncthreads();
-    int base = wid ? warpSums[wid - 1] : 0;
-    total = warpSums[kScanBlock / 32 - 1];
-    __syncthreads();
-    return base + inc - v;
-}
-
-// n is read from *nPtr when nPtr != nullptr (sizes only known on the device).
-__global__ void k_scan_reduce(const int* in, int n, const int* nPtr, int* blockSums, const int* status, int seq)
-{
-    if (status && pass_failed(status, seq)) return;
-    if (nPtr) n = *nPtr;
-    int base = blockIdx.x * kScanTile;
-    if (base >= n) return;
-    int s = 0;
-    for (int i = threadIdx.x; i < kScanTile; i += kScanBlock)
-        if (base + i < n) s += in[base + i];
-    int total;
-    block_excl_scan(s, total);
-    if (threadIdx.x == 0) blockSums[blockIdx.x] = total;
-}
-
-// Exclusive scan of the block sums in one block (up to kScanTile blocks).
-__global__ void k_scan_top(int* blockSums, int nBlocksMax, int n, const int* nPtr, const int* status, int seq)
-{
-    if (status && pass_failed(status, seq)) return;
-    if (nPtr) n = *nPtr;
-    int nb = (n + kScanTile - 1) / kScanTile;
-    if (nb > nBlocksMax) nb = nBlocksMax;
-    int carry = 0;
-    for (int base = 0; base < nb; base += kScanBlock) {
-        int i = base + threadIdx.x;
-        int v = i < nb ? blockSums[i] : 0;
-        int total;
-        int ex = block_excl_scan(v, total);
-        if (i < nb) blockSums[i] = carry + ex;
-        carry += total;
-    }
-}
-
-// out[i] = exclusive prefix of in (in-place allowed); out[n] = total when
-// writeTotal.
-__global__ void k_scan_down(const int* in, int* out, int n, const int* nPtr, const int* blockSums, int writeTotal,
-                            const int* status, int seq)
-{
-    if (status && pass_failed(status, seq)) return;
-    if (nPtr) n = *nPtr;
-    int base = blockIdx.x * kScanTile;
-    if (base >= n) return;
-    int v[kScanItems], s = 0;
+    int wbase = 0, blockTotal = 0;
 #pragma unroll
-    for (int k = 0; k < kScanItems; k++) {
-        int i = base + threadIdx.x * kScanItems + k;
-        v[k] = i < n ? in[i] : 0;
-        s += v[k];
+    for (int w = 0; w < kSetupThreads / 32; w++) {
+        int v = sWarp[w];
+        if (w < warp) wbase += v;
+        blockTotal += v;
     }
-    int total;
-    int ex = block_excl_scan(s, total) + blockSums[blockIdx.x];
-#pragma unroll
-    for (int k = 0; k < kScanItems; k++) {
-        int i = base + threadIdx.x * kScanItems + k;
-        if (i < n) out[i] = ex;
-        ex += v[k];
-        if (writeTotal && i == n - 1) out[n] = ex;
-    }
-}
-
-// ------------------------------------------------------------------- binning
-
-// Writes the (bin, triangle) pairs.  If they would not fit, raises the
-// overflow flag instead; every later kernel of the flush then does nothing
-// and the host re-runs the pass with room for status[1] pairs.  Beside the
-// pairs it counts their radix digits (the sort's global histograms, zeroed by
-// k_setup) and zeroes the look-back descriptors of the tiles the sort will
-// use.
-__global__ void __launch_bounds__(256) k_emit(PassParams P)
-{
-    __shared__ int sHist[kRadixMaxPasses][kRadixDigits];
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pass_failed(P.status, P.passSeq)) return;
-    int total = P.pairOffset[P.nTris];
-    if (total > P.pairCap) {
-        if (t == 0) {
-            P.slotStatus[kSlotTiles] = 0;
-            atomicMax(P.status + 1, total);
-            atomicMin(P.status + kFirstFailed, P.passSeq);
-            atomicOr(P.status, 1);
-        }
-        return;
-    }
-    const int tiles = (total + kSortChunk - 1) / kSortChunk;
-    if (t == 0) {
-        P.slotStatus[kSlotTiles] = tiles;
-        atomicAdd((unsigned long long*)(P.status + 8), (unsigned long long)total);
-    }
-    const int passes = P.radixPasses;
-    {
-        unsigned* desc = (unsigned*)P.radix + kRadixHdr;
-        size_t perPass = (size_t)tiles * kRadixDigits;
-        size_t stride = (size_t)gridDim.x * blockDim.x;
-        for (size_t i = t; i < passes * perPass; i += stride) {
-            size_t ps = i / perPass;
-            desc[ps * P.sortBlocks * kRadixDigits + (i - ps * perPass)] = 0u;
-        }
-    }
-    for (int i = threadIdx.x; i < kRadixMaxPasses * kRadixDigits; i += blockDim.x) (&sHist[0][0])[i] = 0;
-    __syncthreads();
-    if (t < P.nTris) {
-        int count = P.pairCount[t];
-        if (count) {
-            int4 r = P.rect[t];
-            int o = P.pairOffset[t];
-            for (int by = r.z; by <= r.w; by++)
-                for (int bx = r.x; bx <= r.y; bx++) {
-                    int key = by * P.binsX + bx;
-                    P.pairKey[o] = key;
-                    P.pairTri[o] = t;
-                    o++;
-                    for (int ps = 0; ps < passes; ps++) atomicAdd(&sHist[ps][(key >> (8 * ps)) & 255], 1);
+    if (warp == 0) {
+        // warp-wide look-back: 32 earlier blocks' descriptors per step, up to
+        // and including the nearest one that holds an inclusive prefix
+        volatile unsigned long long* desc = (volatile unsigned long long*)(P.radix + kRadixHdr);
+        long long prefix = 0;
+        if (b == 0) {
+            if (lane == 0) desc[0] = kDescPrefix | (unsigned long long)blockTotal;
+        } else {
+            if (lane == 0) desc[b] = kDescAgg | (unsigned long long)blockTotal;
+            int top = b - 1, spins = 0;
+            while (true) {
+                const int idx = top - lane;
+                unsigned long long v = kDescPrefix | 0ull;  // before block 0: an empty prefix
+                if (idx >= 0) v = desc[idx];
+                const unsigned long long f = v & ~kDescValue;
+                const unsigned withPrefix = __ballot_sync(0xffffffffu, f == kDescPrefix);
+                const unsigned notReady = __ballot_sync(0xffffffffu, f == 0ull);
+                const int stop = withPrefix ? __ffs(withPrefix) - 1 : 31;   // lanes 0..stop are needed
+                const unsigned need = stop == 31 ? 0xffffffffu : ((2u << stop) - 1u);
+                if (notReady & need) {
+                    if (++spins > kLookbackSpins) {
+                        if (lane == 0) {
+                            atomicMin(P.status + kFirstFailed, P.passSeq);
+                            atomicOr(P.status, 2);
+                        }
+                        break;
+                    }
+                    __nanosleep(32);
+                    continue;
                 }
+                long long val = lane <= stop ? (long long)(v & kDescValue) : 0;
+#pragma unroll
+                for (int o = 16; o; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
+                prefix += val;
+                if (withPrefix) break;
+                top -= 32;
+            }
+            if (lane == 0) desc[b] = kDescPrefix | (unsigned long long)(prefix + blockTotal);
+        }
+        if (lane == 0) {
+            sPrefix = (int)min(prefix, (long long)INT_MAX);
+            if (b == (int)gridDim.x - 1) {  // the last block: the pass's total
+                long long total = prefix + blockTotal;
+                if (total > P.pairCap) {
+                    P.slotStatus[kSlotTiles] = 0;
+                    P.slotStatus[kSlotTotal] = 0;
+                    atomicMax(P.status + 1, (int)min(total, (long long)INT_MAX));
+                    atomicMin(P.status + kFirstFailed, P.passSeq);
+                    atomicOr(P.status, 1);
+                } else {
+                    P.slotStatus[kSlotTotal] = (int)total;
+                    P.slotStatus[kSlotTiles] = (int)((total + kSortChunk - 1) / kSortChunk);
+                    atomicAdd((unsigned long long*)(P.status + 8), (unsigned long long)total);
+                }
+            }
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < passes * kRadixDigits; i += blockDim.x) {
+    const int passes = P.radixPasses;
+    long long o = (long long)sPrefix + wbase + inc - count;
+    for (int by = rect.z; by <= rect.w; by++)
+        for (int bx = rect.x; bx <= rect.y; bx++, o++) {
+            if (o >= P.pairCap) continue;
+            int key = by * P.binsX + bx;
+            P.pairKey[o] = key;
+            P.pairTri[o] = t;
+            for (int ps = 0; ps < passes; ps++) atomicAdd(&sHist[ps][(key >> (8 * ps)) & 255], 1);
+        }
+    __syncthreads();
+    for (int i = tid; i < passes * kRadixDigits; i += kSetupThreads) {
         int v = (&sHist[0][0])[i];
         if (v) atomicAdd(P.radix + i, v);
     }
@@ -444,7 +397,6 @@ constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / 32;
 constexpr int kSortGroups = kSortChunk / kSortThreads;  // 32-key groups per warp
 constexpr unsigned kFlagCount = 1u << 30, kFlagPrefix = 2u << 30, kValueMask = (1u << 30) - 1;
-constexpr int kLookbackSpins = 1 << 22;
 
 __global__ void __launch_bounds__(kSortThreads) k_onesweep(PassParams P, int pass, const int* __restrict__ inKey,
                                                            const int* __restrict__ inTri, int* __restrict__ outKey,
@@ -461,7 +413,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(PassParams P, int pas
     __syncthreads();
     const int tile = sTicket;
     if (tile < 0) return;
-    const int total = P.pairOffset[P.nTris];
+    const int total = P.slotStatus[kSlotTotal];
     if (tile * kSortChunk >= total) return;
     const int shift = 8 * pass;
     const unsigned lt = (1u << lane) - 1u;
@@ -496,7 +448,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(PassParams P, int pas
         sWarpCnt[w][d] = count;
         count += v;
     }
-    unsigned* desc = (unsigned*)P.radix + kRadixHdr + ((size_t)pass * P.sortBlocks) * kRadixDigits;
+    unsigned* desc = (unsigned*)P.radix + P.sortDescOff + ((size_t)pass * P.sortBlocks) * kRadixDigits;
     volatile unsigned* mine = desc + (size_t)tile * kRadixDigits + d;
     int prefix = 0;
     if (tile == 0) {
@@ -558,7 +510,7 @@ __global__ void k_bin_bounds(PassParams P, const int* __restrict__ keys)
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     int nBins = P.binsX * P.binsY;
     if (b > nBins) return;
-    int total = P.pairOffset[P.nTris];
+    int total = P.slotStatus[kSlotTotal];
     int lo = 0, hi = total;
     if (b == nBins) lo = total;
     while (lo < hi) {
@@ -573,20 +525,6 @@ __global__ void k_bin_bounds(PassParams P, const int* __restrict__ keys)
 
 static inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
-void scan_exclusive(const int* in, int* out, int n, const int* nPtr, int nMax, int* blockSums, int writeTotal,
-                    const int* status, int seq, cudaStream_t s, int& launches, Prof* pr)
-{
-    int nb = ceil_div(nMax > 0 ? nMax : 1, kScanTile);
-    pr->begin(K_SCAN, s);
-    k_scan_reduce<<<nb, kScanBlock, 0, s>>>(in, n, nPtr, blockSums, status, seq);
-    k_scan_top<<<1, kScanBlock, 0, s>>>(blockSums, nb, n, nPtr, status, seq);
-    k_scan_down<<<nb, kScanBlock, 0, s>>>(in, out, n, nPtr, blockSums, writeTotal, status, seq);
-    pr->end(s);
-    launches += 3;
-}
-
-int scan_block_sums_needed(int nMax) { return ceil_div(nMax > 0 ? nMax : 1, kScanTile) + 1; }
-
 int radix_passes(int nBins)
 {
     int bits = 0;
@@ -594,33 +532,28 @@ int radix_passes(int nBins)
     return (bits + 7) / 8;
 }
 
-size_t radix_scratch_ints(int sortBlocks, int passes)
+// The sort scratch of a pass: header (histograms, tickets), the set-up
+// blocks' look-back descriptors (two ints each), the radix passes'.
+int sort_desc_offset(int nTris) { return kRadixHdr + (2 * ceil_div(nTris > 0 ? nTris : 1, kSetupThreads) + 63) / 64 * 64; }
+
+size_t radix_scratch_ints(int sortBlocks, int passes, int nTris)
 {
-    return (size_t)kRadixHdr + (size_t)passes * sortBlocks * kRadixDigits;
+    return (size_t)sort_desc_offset(nTris) + (size_t)passes * sortBlocks * kRadixDigits;
 }
 
-// A pass's set-up and binning in three parts, so that the host can order the
-// emits of passes on different streams (a pass must see every earlier pass's
-// overflow before it rasterises): set-up and the pair-count scan; the emit;
-// the radix passes and the bin starts.
-void launch_setup(const PassParams& P, int* scanTmp, cudaStream_t s, int& launches, Prof* pr)
+// A pass's set-up and binning in two parts (the host orders passes on
+// different streams in between): the set-up with the pair emission (after
+// the memset of the sort scratch it uses), then the radix passes and the bin
+// starts.
+int launch_setup(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
 {
+    size_t ints = radix_scratch_ints(P.sortBlocks, P.radixPasses, P.nTris);
+    if (cudaMemsetAsync(P.radix, 0, ints * sizeof(int), s) != cudaSuccess) return -1;
     pr->begin(K_SETUP, s);
-    k_setup<<<ceil_div(P.nTris, kSetupThreads), kSetupThreads, 0, s>>>(P);
+    k_setup_emit<<<ceil_div(P.nTris, kSetupThreads), kSetupThreads, 0, s>>>(P);
     pr->end(s);
     launches++;
-    scan_exclusive(P.pairCount, P.pairOffset, P.nTris, nullptr, P.nTris, scanTmp, 1, P.status, P.passSeq, s, launches,
-                   pr);
-}
-
-// The emit kernel alone, then the rest (the host waits for the previous
-// pass's emit in between).
-void launch_emit(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
-{
-    pr->begin(K_EMIT, s);
-    k_emit<<<ceil_div(P.nTris, 256), 256, 0, s>>>(P);
-    pr->end(s);
-    launches++;
+    return 0;
 }
 
 void launch_sort(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)

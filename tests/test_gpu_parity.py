@@ -126,3 +126,25 @@ def test_fast_division_is_correctly_rounded(gpu_lib):
     results (every mantissa of exponents -100..100; 2^28 random pairs)."""
     from puresoft3d_gb300.pipeline import selftest_division
     assert selftest_division(1 << 28) == (0, 0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("repeats", [2, 3, 9])
+def test_repeated_multipass_frames_in_one_launch(gpu_lib, repeats):
+    """The two-pass frame (shadow map, then the lit pass sampling it)
+    recorded `repeats` times before one finish: 4 and 6 passes run on the two
+    pass streams -- the second shadow pass must wait for the first lit pass
+    that samples the map it overwrites -- and 18 on one stream.  The result
+    equals one frame on the oracle."""
+    from puresoft3d_gb300 import scenes as S
+    from puresoft3d_gb300.pipeline import PuresoftPipeline
+    name, scene = [c for c in CASES if c[0].startswith("c2_small")][0]
+    g = PuresoftPipeline(scene.width, scene.height)
+    S.replay_setup(scene, g)
+    for _ in range(repeats):
+        S.replay_frame(scene, g)
+    g.finish()
+    ref = render(OraclePipeline(scene.width, scene.height), scene)
+    assert_depth_exact(g.readDepthTexture(scene.info["depth_texture"]), ref["depth"], name)
+    assert_depth_exact(g.readDepthTexture(scene.info["shadow_texture"]), ref["shadow"], name + " shadow map")
+    assert colour_diff(g.readColour(), ref["colour"])[0] <= COLOUR_TOL
