@@ -274,7 +274,7 @@ def run_c4(args):
     pipe.finish()
     clk = clocks.stop()
     total_ms = allreduce_max(sum(frame_ms))
-    ips = WORLD * views * args.steps / (total_ms / 1e3)
+    ips = aggregate(views * args.steps, total_ms / 1e3)
 
     host = torch.empty((batched.height, batched.width, 4), dtype=torch.uint8, pin_memory=True).numpy()
     for _ in range(2):
@@ -547,8 +547,7 @@ def run_ours(args):
         frame_ms.append(pipe.timerEnd())
     pipe.finish()
     clk = clocks.stop()
-    total_ms = sum(frame_ms)
-    total_ms = allreduce_max(total_ms)
+    total_ms = allreduce_max(sum(frame_ms))
 
     # e2e through the public API with host buffers
     try:
@@ -563,10 +562,10 @@ def run_ours(args):
     for _ in range(args.steps):
         cb.submit(upload_inputs=True)
         pipe.readColour(host)
-    e2e_s = allreduce_max(time.perf_counter() - t0)
+    e2e_s = time.perf_counter() - t0
 
-    fps = WORLD * args.steps / (total_ms / 1e3)
-    fps_e2e = WORLD * args.steps / e2e_s
+    fps = aggregate(args.steps, total_ms / 1e3)
+    fps_e2e = aggregate(args.steps, e2e_s)
     ab = algorithmic_bytes(scene, counts)
     # dominant kernel by event time share
     dom = max(prof, key=lambda k: prof[k][1])
@@ -764,6 +763,12 @@ def allreduce_max(x):
     t = torch.tensor([x], dtype=torch.float64)
     _pg.all_reduce(t, op=_pg.ReduceOp.MAX)
     return float(t.item())
+
+
+def aggregate(units_per_rank, seconds):
+    """Whole-job throughput of the replicas: every rank processed
+    units_per_rank units; the job took as long as the slowest rank."""
+    return WORLD * units_per_rank / allreduce_max(seconds)
 
 
 def main():

@@ -285,6 +285,12 @@ int ps3d_timer_end(ps3d_pipeline* p, float* ms);
 #define PS3D_K_SHADE 6
 #define PS3D_K_FILL 7
 #define PS3D_K_COUNT 8
+/* Checks the bounded device waits: one warp polls a flag that nothing sets,
+ * sleeping between polls, and gives up after `spins` polls, marking the
+ * failure as an expired look-back of the bin sort does.  Returns
+ * PS3D_ERR_TIMEOUT (the expected outcome: the wait ran out and the host
+ * reported it) with the kernel's time in *ms; the pipeline stays usable. */
+int ps3d_selftest_wait(ps3d_pipeline* p, int spins, float* ms);
 /* Checks the kernels' fast correctly rounded reciprocal and quotient
  * against CUDA's IEEE ones on the current device: every float mantissa of
  * exponents -100..100 for the reciprocal, `pairs` hashed pairs for the

@@ -37,6 +37,7 @@ int sort_desc_offset(int nTris);
 size_t radix_scratch_ints(int sortBlocks, int passes, int nTris);
 int selftest_division(unsigned long long pairs, unsigned long long* rcpBad, unsigned long long* divBad);
 void launch_raster(const PassParams& P, cudaStream_t s, int& launches, Prof* pr);
+void launch_selftest_wait(int* status, const int* flag, int spins, cudaStream_t s);
 void launch_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr);
 void launch_fill_u32(void* base, int width, int height, int pitchElems, uint32_t v, const int* status, int seq,
                      cudaStream_t s, int& launches, Prof* pr);
@@ -554,6 +555,19 @@ int copy_colour_plain(ps3d_pipeline* p, const Command& c)
 
 // The draws of a pass as device descriptors: triangle bases are running
 // sums, so a pass's triangles are numbered in submission order.
+// The fragment processor shared by every colour-writing draw, else 0.
+int pass_fp(const DrawDesc* dd, size_t n)
+{
+    int fp = -1;
+    for (size_t i = 0; i < n; i++) {
+        const DrawDesc& d = dd[i];
+        if (!(d.flags & F_COLOUR)) continue;
+        if (fp == -1) fp = d.fp;
+        else if (fp != d.fp) return 0;
+    }
+    return fp < 0 ? 0 : fp;
+}
+
 void pass_descriptors(const std::vector<Command>& cmds, const Pass& ps, std::vector<DrawDesc>& dd,
                       std::vector<DrawUniforms>& uu, int& nTris, int& nvMax, bool& anyColour)
 {
@@ -649,6 +663,7 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     P.H = H;
     P.binW = binW;
     P.rasterBlocks = p->rasterBlocks;
+    P.passFp = pass_fp(dd.data(), dd.size());
     P.binsX = binsX;
     P.binsY = binsY;
     P.nTris = nTris;
@@ -1658,6 +1673,25 @@ int ps3d_selftest_division(uint64_t pairs, uint64_t* rcpMismatches, uint64_t* di
     return 0;
 }
 
+int ps3d_selftest_wait(ps3d_pipeline* p, int spins, float* ms)
+{
+    if (!p || !ms || spins < 1) return fail(PS3D_ERR_INVALID, "bad argument");
+    int rc = do_finish(p);
+    if (rc) return rc;
+    if (!p->timerA) {
+        CU(cudaEventCreate(&p->timerA));
+        CU(cudaEventCreate(&p->timerB));
+    }
+    CU(cudaEventRecord(p->timerA, p->stream));
+    // status word 15 is never written: the flag that nothing sets
+    launch_selftest_wait(p->status, p->status + 15, spins, p->stream);
+    CU(cudaGetLastError());
+    CU(cudaEventRecord(p->timerB, p->stream));
+    CU(cudaEventSynchronize(p->timerB));
+    CU(cudaEventElapsedTime(ms, p->timerA, p->timerB));
+    return do_finish(p);  // reads the failure words like after a pass
+}
+
 int ps3d_l2_scrub(ps3d_pipeline* p, size_t bytes)
 {
     if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
@@ -1849,6 +1883,7 @@ int noalloc_run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const P
     P.H = H;
     P.binW = p->binW;
     P.rasterBlocks = p->rasterBlocks;
+    P.passFp = pass_fp(g_noallocDraws, (size_t)s.nd);
     P.binsX = s.binsX;
     P.binsY = s.binsY;
     P.nTris = s.nTris;

@@ -361,6 +361,9 @@ __device__ __forceinline__ void fragment_varyings(const TriRaster& t, const floa
     for (int k = 0; k < NV; k++) out[k] = fmul(st[k], inv);
 }
 
+// FPK: the fragment processor when every draw of the pass uses the same
+// one (a kernel with only that shader's registers), else 0 (any).
+template <int FPK>
 __device__ __forceinline__ void shade_entry(const PassParams& P, int2 e)
 {
     const int y = e.x / P.W, x = e.x - y * P.W, w = e.y;
@@ -381,7 +384,7 @@ __device__ __forceinline__ void shade_entry(const PassParams& P, int2 e)
     span_z(t, s, yl, z);
     const float* vary = P.vary + (size_t)w * 3 * P.nvMax;
     uint32_t bgra;
-    switch (d.fp) {
+    switch (FPK ? FPK : d.fp) {
     case FP_LIT2: {
         float in[16];
         fragment_varyings<16>(t, vary, P.nvMax, s, z, xl, in);
@@ -411,13 +414,14 @@ __device__ __forceinline__ void shade_entry(const PassParams& P, int2 e)
 }
 
 // One thread per shade-list entry; the grid strides over the list, whose
-// length the raster kernel left in status[kShadeCount].
+// length the raster kernel left in the slot status.
+template <int FPK>
 __global__ void __launch_bounds__(256) k_shade(PassParams P)
 {
     if (pass_failed(P.status, P.passSeq)) return;
     const int n = P.slotStatus[kSlotShade];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        shade_entry(P, P.shadeList[i]);
+        shade_entry<FPK>(P, P.shadeList[i]);
 }
 
 __global__ void k_fill_u32(uint32_t* base, int width, int height, int pitchElems, uint32_t v, const int* status,
@@ -457,11 +461,19 @@ void launch_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
     int dev = 0, sms = 0, perSM = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shade, 256, 0);
+    void (*kern)(PassParams) = k_shade<0>;
+    switch (P.passFp) {
+    case FP_LIT1: kern = k_shade<FP_LIT1>; break;
+    case FP_LIT2: kern = k_shade<FP_LIT2>; break;
+    case FP_LIT3: kern = k_shade<FP_LIT3>; break;
+    case FP_DEF01: kern = k_shade<FP_DEF01>; break;
+    default: break;
+    }
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, 256, 0);
     long long need = ((long long)P.W * P.H + 255) / 256;
     int grid = (int)std::min<long long>(need, (long long)std::max(sms, 1) * std::max(perSM, 1));
     pr->begin(K_SHADE, s);
-    k_shade<<<std::max(grid, 1), 256, 0, s>>>(P);
+    kern<<<std::max(grid, 1), 256, 0, s>>>(P);
     pr->end(s);
     launches++;
 }
@@ -511,6 +523,30 @@ __global__ void k_selftest_div(unsigned seed, unsigned long long n, unsigned lon
     float a = __uint_as_float(((unsigned)(ea + 127) << 23) | (h1 & 0x7fffffu) | ((h3 >> 31) << 31));
     float b = __uint_as_float(((unsigned)(eb + 127) << 23) | (h2 & 0x7fffffu) | (((h3 >> 30) & 1u) << 31));
     if (__float_as_uint(fdiv(a, b)) != __float_as_uint(__fdiv_rn(a, b))) atomicAdd(bad, 1ull);
+}
+
+// Self-test of the bounded device waits: one warp waits, the way the sort's
+// look-backs do (volatile poll, short sleep, a limit on the polls), for a
+// flag that nothing sets; when the limit runs out it marks the failure words
+// as an expired look-back does and returns.
+__global__ void k_selftest_wait(int* status, const int* flag, int spins)
+{
+    int n = 0;
+    while (*(volatile const int*)flag == 0) {
+        if (++n > spins) {
+            if (threadIdx.x == 0) {
+                atomicMin(status + kFirstFailed, 0);
+                atomicOr(status, 2);
+            }
+            return;
+        }
+        __nanosleep(64);
+    }
+}
+
+void launch_selftest_wait(int* status, const int* flag, int spins, cudaStream_t s)
+{
+    k_selftest_wait<<<1, 32, 0, s>>>(status, flag, spins);
 }
 
 int selftest_division(unsigned long long pairs, unsigned long long* rcpBad, unsigned long long* divBad)

@@ -59,6 +59,7 @@ _SIGS = {
     "ps3d_set_bin_width": [_c_void_p, _c_int],
     "ps3d_get_bin_width": [_c_void_p, ctypes.POINTER(_c_int)],
     "ps3d_set_raster_occupancy": [_c_void_p, _c_int],
+    "ps3d_selftest_wait": [_c_void_p, _c_int, ctypes.POINTER(ctypes.c_float)],
     "ps3d_read_colour": [_c_void_p, _c_void_p],
     "ps3d_read_depth": [_c_void_p, _c_void_p],
     "ps3d_colour_device_ptr": [_c_void_p, ctypes.POINTER(_c_void_p)],
@@ -248,6 +249,17 @@ class PuresoftPipeline:
     def setRasterOccupancy(self, blocks_per_sm: int):
         """Raster kernel variant: 0 (registers as needed) or 8 blocks per SM."""
         self._check(self.lib.ps3d_set_raster_occupancy(self.h, blocks_per_sm))
+
+    def selftestWait(self, spins: int) -> float:
+        """Runs a bounded wait that must run out; raises TimeoutError (with
+        the kernel's milliseconds in the message) as the library reports an
+        expired device wait.  Returns only if the wait did not run out."""
+        ms = ctypes.c_float()
+        rc = self.lib.ps3d_selftest_wait(self.h, spins, ctypes.byref(ms))
+        if rc == -5:
+            raise TimeoutError("%.3f ms: %s" % (ms.value, self.lib.ps3d_last_error().decode(errors="replace")))
+        self._check(rc)
+        return ms.value
 
     def binWidth(self) -> int:
         v = _c_int()

@@ -41,9 +41,9 @@ import numpy as np
 from . import scenes as S
 
 # device scratch per triangle of a pass (triangle record 64 B, varyings
-# 3 x 9 floats, per-triangle counts / rectangles / offsets 24 B) and per
-# (bin, triangle) pair (4 sort arrays x 4 B), with ~2 pairs per triangle
-SCRATCH_BYTES_PER_TRIANGLE = 64 + 108 + 24 + 2 * 16
+# 3 x 9 floats) and per (bin, triangle) pair (4 sort arrays x 4 B), with ~2
+# pairs per triangle, plus margin
+SCRATCH_BYTES_PER_TRIANGLE = 64 + 108 + 2 * 16 + 24
 
 
 class ShelfPacker:

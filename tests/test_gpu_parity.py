@@ -148,3 +148,23 @@ def test_repeated_multipass_frames_in_one_launch(gpu_lib, repeats):
     assert_depth_exact(g.readDepthTexture(scene.info["depth_texture"]), ref["depth"], name)
     assert_depth_exact(g.readDepthTexture(scene.info["shadow_texture"]), ref["shadow"], name + " shadow map")
     assert colour_diff(g.readColour(), ref["colour"])[0] <= COLOUR_TOL
+
+
+@pytest.mark.gpu
+def test_device_wait_runs_out_and_pipeline_recovers(gpu_lib):
+    """A bounded device wait on a flag that nothing sets gives up after its
+    poll limit; the host reports PS3D_ERR_TIMEOUT and the pipeline then
+    renders correctly."""
+    import re
+    from puresoft3d_gb300 import scenes as S
+    from puresoft3d_gb300.pipeline import PuresoftPipeline
+    name, scene = [c for c in CASES if c[0].startswith("kat_soup_lit")][0]
+    g = PuresoftPipeline(scene.width, scene.height)
+    with pytest.raises(TimeoutError) as e:
+        g.selftestWait(1 << 14)
+    ms = float(re.match(r"([0-9.]+) ms", str(e.value)).group(1))
+    assert 0.0 < ms < 2000.0
+    out = render(g, scene)
+    ref = render(OraclePipeline(scene.width, scene.height), scene)
+    assert_depth_exact(out["depth"], ref["depth"], name)
+    assert colour_diff(out["colour"], ref["colour"])[0] <= COLOUR_TOL

@@ -93,3 +93,36 @@ def test_served_images_equal_alone(gpu_lib, monkeypatch):
     assert s["p99_ms"] >= s["p50_ms"] > 0
     srv.close()
     plain.close()
+
+
+@pytest.mark.gpu
+def test_job_larger_than_the_atlas_is_refused(gpu_lib, monkeypatch):
+    monkeypatch.setattr(S, "C5_RESOLUTIONS", ((200, 120),))
+    pool = S.scene_c5_pool(meshes=2, tri_min=200, tri_max=400, textures=1, tex_size=32)
+    jobs = S.c5_jobs(pool, n=2, rate=1000.0, seed=3)
+    srv = RenderServer(pool, atlas=(128, 128), slots=1)
+    with pytest.raises(ValueError, match="never be admitted"):
+        srv.serve(jobs)
+    srv.close()
+
+
+@pytest.mark.gpu
+def test_jobs_wait_for_memory_and_all_complete(gpu_lib, monkeypatch):
+    """A result arena with room for one 200x120 image and a scratch budget of
+    a few thousand triangles per batch: jobs wait for memory to free up,
+    every job still completes, and each image equals the job alone."""
+    monkeypatch.setattr(S, "C5_RESOLUTIONS", RES)
+    pool = S.scene_c5_pool(meshes=6, tri_min=200, tri_max=6000, textures=2, tex_size=32)
+    jobs = S.c5_jobs(pool, n=24, rate=20000.0, seed=5)
+    arena = 200 * 120 * 4 + 256
+    budget = 2 * 7000 * 232   # two slots' share of scratch for ~7000 triangles each
+    srv = RenderServer(pool, atlas=(400, 256), slots=2, hbm_budget=budget, arena_bytes=arena)
+    done = srv.serve(jobs, keep_images=True)
+    assert sorted(d.job.id for d in done) == list(range(len(jobs)))
+    assert len({d.batch for d in done}) >= 6   # memory, not the atlas, bounds the batches
+    plain = PlainLoop(pool, resolutions=RES)
+    alone = {d.job.id: d.image for d in plain.serve(jobs, keep_images=True, realtime=False)}
+    for d in done:
+        assert np.array_equal(d.image, alone[d.job.id]), d.job.id
+    srv.close()
+    plain.close()
