@@ -70,6 +70,10 @@ extern "C" {
 #define PS3D_FP_DEF05 0x0503
 #define PS3D_VP_SHADOW 0x0601
 #define PS3D_FP_LIT1 0x1103
+/* LIT1 with an alpha test (the albedo's alpha below 128 discards the
+ * fragment: no colour, no depth write, fragthrd.cpp:233-237) and the
+ * albedo's alpha as the fragment's alpha (so ALPHABLEND blends by it). */
+#define PS3D_FP_LIT1A 0x1403
 #define PS3D_FP_LIT3 0x1303
 #define PS3D_VP_LIT2 0x1201
 #define PS3D_IP_LIT2 0x1202

@@ -55,7 +55,7 @@ enum {
     VP_DEF01 = 0x0101, IP_DEF01 = 0x0102, FP_DEF01 = 0x0103,
     VP_DEF05 = 0x0501, IP_DEF05 = 0x0502, FP_DEF05 = 0x0503,
     VP_SHADOW = 0x0601,
-    FP_LIT1 = 0x1103, FP_LIT3 = 0x1303,
+    FP_LIT1 = 0x1103, FP_LIT1A = 0x1403, FP_LIT3 = 0x1303,
     VP_LIT2 = 0x1201, IP_LIT2 = 0x1202, FP_LIT2 = 0x1203
 };
 
@@ -266,7 +266,7 @@ static int known_processor(int id)
 {
     switch (id) {
     case VP_DEF01: case IP_DEF01: case FP_DEF01: case VP_DEF05: case IP_DEF05: case FP_DEF05:
-    case VP_SHADOW: case FP_LIT1: case FP_LIT3: case VP_LIT2: case IP_LIT2: case FP_LIT2:
+    case VP_SHADOW: case FP_LIT1: case FP_LIT1A: case FP_LIT3: case VP_LIT2: case IP_LIT2: case FP_LIT2:
         return 1;
     }
     return 0;
@@ -538,7 +538,8 @@ static int fp_prepare(const ps3do* p, fp_state* s)
     memset(s, 0, sizeof *s);
     switch (p->fp) {
     case FP_DEF01:
-    case FP_LIT1: {
+    case FP_LIT1:
+    case FP_LIT1A: {
         int t = *uin(p, 9);
         if (t < 0 || t >= p->ntex || !p->tex[t]) return -1;
         s->light = ufl(p, 7);
@@ -680,7 +681,8 @@ static void shade_error(const ps3do* p, const fp_state* s, const float* in, err_
     }
 }
 
-/* Returns 1 if the processor wrote colour (the reference FPs never discard). */
+/* Returns 1 if the processor wrote colour, 2 if it discarded the fragment
+   (FBOBridge::discard, fragthrd.cpp:21-24: no depth write), 0 otherwise. */
 static int run_fp(const ps3do* p, const fp_state* s, const float* in, uint8_t* bgra)
 {
     switch (p->fp) {
@@ -689,6 +691,10 @@ static int run_fp(const ps3do* p, const fp_state* s, const float* in, uint8_t* b
         sr_level t = level_of(s->tex);
         sr_shade_lit1(&t, s->light, s->cam, in, in + 4, in + 8, bgra);
         return 1;
+    }
+    case FP_LIT1A: {
+        sr_level t = level_of(s->tex);
+        return sr_shade_lit1a(&t, s->light, s->cam, in, in + 4, in + 8, bgra) ? 2 : 1;
     }
     case FP_LIT3:
         sr_shade_lit3(s->chainA, s->levelsA, s->lodScale, s->light, s->cam, in, in + 4, in + 8, bgra);
@@ -947,10 +953,18 @@ static void run_task(draw_ctx* d, const o_task* t, long long* tested, long long*
         cur = (behav & BEHAVIOR_TEST_DEPTH) ? *(const float*)(dc.rowEntry + (size_t)dc.col * 4) : 1.0f;
         if (-1.0f < z && (z - cur < -0.0001f)) { /* fragthrd.cpp:227 */
             uint8_t bgra[4];
+            int w;
             (*passed)++;
-            if (run_fp(p, &d->fs, frag, bgra) && !cc.overflow) memcpy(cc.rowEntry + (size_t)cc.col * 4, bgra, 4);
+            w = run_fp(p, &d->fs, frag, bgra);
+            if (w == 1 && !cc.overflow) {
+                uint8_t* dst = cc.rowEntry + (size_t)cc.col * 4;
+                /* FBOBridge::write4 blends under ALPHABLEND (fragthrd.cpp:70-81, fbo.cpp:208-229);
+                   DEF01 writes through FBOBridge::write, which never blends */
+                if ((behav & BEHAVIOR_ALPHABLEND) && p->fp != FP_DEF01) sr_blend4(dst, bgra);
+                else memcpy(dst, bgra, 4);
+            }
             if (p->errOn) shade_error(p, &d->fs, frag, e);
-            if ((behav & BEHAVIOR_UPDATE_DEPTH) && !dc.overflow) memcpy(dc.rowEntry + (size_t)dc.col * 4, &z, 4);
+            if (w != 2 && (behav & BEHAVIOR_UPDATE_DEPTH) && !dc.overflow) memcpy(dc.rowEntry + (size_t)dc.col * 4, &z, 4);
         }
         cursor_next(&cc);
         cursor_next(&dc);

@@ -7,10 +7,12 @@
  * The reference has no directional-light, bilinear, trilinear, normal-map or
  * PCF shaders; these are new plugins in the style of its DEF01/DEF03/DEF05
  * processors (tex1light1.cpp, tex1bump1light1.cpp, shadow.cpp).  Their maths
- * is the shared CPU definition in ../shade_ref.h.
+ * is the shared CPU definition in ../shade_ref.h.  They write colour with
+ * write4 (fragthrd.cpp:70-81), so BEHAVIOR_ALPHABLEND blends (blend4).
  *
  *   VertexProcesserSHADOW   DEF05 (shadow.cpp:21-29) without the x0.9 scale
  *   FragmentProcessorLIT1   DEF01 varyings, bilinear albedo, Blinn-Phong s=32
+ *   FragmentProcessorLIT1A  LIT1 with an alpha test (discard) and the texture's alpha
  *   FragmentProcessorLIT3   LIT1 with a trilinear mip chain
  *   VertexProcesserLIT2 / InterpolationProcessorLIT2 / FragmentProcessorLIT2
  *                           normal-mapped, trilinear, 3x3-PCF-shadowed shader
@@ -65,7 +67,24 @@ void FragmentProcessorLIT1::process(const FragmentProcessorInput* input, Fragmen
     sr_level t = level_of(m_tex);
     uint8_t bgra[4];
     sr_shade_lit1(&t, m_light, m_camera, in->normal, in->worldPos, in->texcoord, bgra);
-    output->write(0, bgra, 4);
+    output->write4(0, bgra);
+}
+
+/* ---- LIT1A: alpha test + texture alpha -------------------------------------- */
+void FragmentProcessorLIT1A::preprocess(const PURESOFTUNIFORM* uniforms, const void** textures)
+{
+    m_light = (const float*)uniforms[7].data;
+    m_camera = (const float*)uniforms[8].data;
+    m_tex = (const PuresoftFBO*)textures[*(const int*)uniforms[9].data];
+}
+
+void FragmentProcessorLIT1A::process(const FragmentProcessorInput* input, FragmentProcessorOutput* output) const
+{
+    const PROCDATA_DEF01* in = (const PROCDATA_DEF01*)input->user;
+    sr_level t = level_of(m_tex);
+    uint8_t bgra[4];
+    if (sr_shade_lit1a(&t, m_light, m_camera, in->normal, in->worldPos, in->texcoord, bgra)) output->discard();
+    else output->write4(0, bgra);
 }
 
 /* ---- LIT3 ----------------------------------------------------------------- */
@@ -84,7 +103,7 @@ void FragmentProcessorLIT3::process(const FragmentProcessorInput* input, Fragmen
     const PROCDATA_DEF01* in = (const PROCDATA_DEF01*)input->user;
     uint8_t bgra[4];
     sr_shade_lit3(m_chain, m_levels, m_lodScale, m_light, m_camera, in->normal, in->worldPos, in->texcoord, bgra);
-    output->write(0, bgra, 4);
+    output->write4(0, bgra);
 }
 
 /* ---- LIT2 ----------------------------------------------------------------- */
@@ -196,5 +215,5 @@ void FragmentProcessorLIT2::process(const FragmentProcessorInput* input, Fragmen
     uint8_t bgra[4];
     sr_shade_lit2(m_albedo, m_albedoLevels, m_normal, m_normalLevels, m_shadow, m_shadowSize, m_shadowScanlineFloats,
                   m_lodScale, m_bias, m_light, m_camera, (const float*)input->user, bgra);
-    output->write(0, bgra, 4);
+    output->write4(0, bgra);
 }

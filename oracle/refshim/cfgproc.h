@@ -39,6 +39,18 @@ private:
     const PuresoftFBO* m_tex;
 };
 
+class FragmentProcessorLIT1A : public PuresoftFragmentProcessor
+{
+public:
+    void preprocess(const PURESOFTUNIFORM* uniforms, const void** textures);
+    void process(const FragmentProcessorInput* input, FragmentProcessorOutput* output) const;
+
+private:
+    const float* m_light;
+    const float* m_camera;
+    const PuresoftFBO* m_tex;
+};
+
 class FragmentProcessorLIT3 : public PuresoftFragmentProcessor
 {
 public:

@@ -87,6 +87,7 @@ PuresoftProcessor* make_processor(int id)
     case 0x0503: return new FragmentProcessorDEF05;
     case 0x0601: return new VertexProcesserSHADOW;
     case 0x1103: return new FragmentProcessorLIT1;
+    case 0x1403: return new FragmentProcessorLIT1A;
     case 0x1303: return new FragmentProcessorLIT3;
     case 0x1201: return new VertexProcesserLIT2;
     case 0x1202: return new InterpolationProcessorLIT2;

@@ -363,6 +363,50 @@ static inline void sr_shade_lit2(const sr_level* albedoChain, int albedoLevels, 
                       shadowScanlineFloats, lodScale, shadowBias, lightDir, camPos, varyings, pre, out);
 }
 
+/* Scene shader LIT1A: LIT1 with an alpha test and the texture's alpha --
+   the albedo's alpha (bilinear, 0..255) below 128 discards the fragment
+   (no colour, no depth write: fragthrd.cpp:233-237); otherwise the colour
+   is LIT1's with alpha = the albedo's alpha, so ALPHABLEND blends by it.
+   Returns 1 when the fragment is discarded. */
+static inline int sr_shade_lit1a_pre(const sr_level* tex, const float* lightDir, const float* camPos,
+                                     const float* normal, const float* worldPos, const float* texcoord, float pre[3],
+                                     uint8_t out[4])
+{
+    float albedo[4], n[3], E[3];
+    sr_bilinear_bgra8(tex, texcoord[0], texcoord[1], albedo);
+    if (!(albedo[3] >= 128.0f)) return 1;
+    n[0] = normal[0]; n[1] = normal[1]; n[2] = normal[2];
+    sr_normalize3(n);
+    E[0] = camPos[0] - worldPos[0];
+    E[1] = camPos[1] - worldPos[1];
+    E[2] = camPos[2] - worldPos[2];
+    sr_normalize3(E);
+    sr_blinn_phong(albedo, n, lightDir, E, 1.0f, pre, out);
+    out[3] = sr_to_u8(albedo[3]);
+    return 0;
+}
+
+static inline int sr_shade_lit1a(const sr_level* tex, const float* lightDir, const float* camPos, const float* normal,
+                                 const float* worldPos, const float* texcoord, uint8_t out[4])
+{
+    float pre[3];
+    return sr_shade_lit1a_pre(tex, lightDir, camPos, normal, worldPos, texcoord, pre, out);
+}
+
+/* PuresoftFBO::blend4 (fbo.cpp:208-229), the MMX sequence per channel on
+   16-bit lanes: a = the source's alpha; out = sat8(dst + ((sat16(src - dst)
+   * a) >> 8)) -- with the unsigned saturating subtract it can only brighten. */
+static inline void sr_blend4(uint8_t dst[4], const uint8_t src[4])
+{
+    unsigned a = src[3];
+    for (int k = 0; k < 4; k++) {
+        unsigned d = dst[k], sv = src[k];
+        unsigned diff = sv > d ? sv - d : 0u;
+        unsigned v = (((diff * a) & 0xffffu) >> 8) + d;
+        dst[k] = (uint8_t)(v > 255u ? 255u : v);
+    }
+}
+
 /* ------------------------------------------------------------------------
    FP64 re-shade, for measuring the FP32 shaders' error only: the same
    equations on the same fragment inputs (the FP32 varyings, the same texels

@@ -280,7 +280,7 @@ int required_vary(int ip)
 int fp_needs(int fp)
 {
     switch (fp) {
-    case FP_DEF01: case FP_LIT1: case FP_LIT3: return IP_DEF01;
+    case FP_DEF01: case FP_LIT1: case FP_LIT1A: case FP_LIT3: return IP_DEF01;
     case FP_LIT2: return IP_LIT2;
     default: return 0;
     }
@@ -299,7 +299,7 @@ bool known_processor(int id)
 {
     switch (id) {
     case VP_DEF01: case IP_DEF01: case FP_DEF01: case VP_DEF05: case IP_DEF05: case FP_DEF05:
-    case VP_SHADOW: case FP_LIT1: case FP_LIT3: case VP_LIT2: case IP_LIT2: case FP_LIT2:
+    case VP_SHADOW: case FP_LIT1: case FP_LIT1A: case FP_LIT3: case VP_LIT2: case IP_LIT2: case FP_LIT2:
         return true;
     }
     return false;
@@ -373,7 +373,8 @@ int snapshot_uniforms(const ps3d_pipeline* p, DrawUniforms& U)
     }
     switch (p->fp) {
     case FP_DEF01:
-    case FP_LIT1: {
+    case FP_LIT1:
+    case FP_LIT1A: {
         if ((rc = need(7, U.light, 4)) || (rc = need(8, U.cam, 4))) return rc;
         const int* t = uint_(p, 9, 1);
         if (!t) return fail(PS3D_ERR_INVALID, "uniform 9 (texture index) is not set");
@@ -555,6 +556,15 @@ int copy_colour_plain(ps3d_pipeline* p, const Command& c)
 
 // The draws of a pass as device descriptors: triangle bases are running
 // sums, so a pass's triangles are numbered in submission order.
+// A pass is shaded forward (every passing fragment, in order, in the raster)
+// when a draw blends or its fragment processor may discard.
+bool pass_forward(const DrawDesc* dd, size_t n)
+{
+    for (size_t i = 0; i < n; i++)
+        if ((dd[i].flags & F_COLOUR) && ((dd[i].flags & B_ALPHABLEND) || dd[i].fp == FP_LIT1A)) return true;
+    return false;
+}
+
 // The fragment processor shared by every colour-writing draw, else 0.
 int pass_fp(const DrawDesc* dd, size_t n)
 {
@@ -631,7 +641,8 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     const int slot = seq % kSlots;
     Scratch& x = p->scr[slot];
     cudaStream_t s = p->oneStream ? p->stream : p->gs[slot];
-    int binW = p->binW;
+    const bool forward = pass_forward(dd.data(), dd.size());
+    int binW = forward ? 16 : p->binW;  // forward passes run with 16-column bins
     int binsX = (W + binW - 1) / binW, binsY = (H + kBinH - 1) / kBinH;
     if (radix_passes(binsX * binsY) > kRadixMaxPasses) return fail(PS3D_ERR_RANGE, "target too large for the bin sort");
     if ((rc = ensure_scratch(p, x, nTris, nvMax, W, H, binsX, binsY, anyColour))) return rc;
@@ -664,6 +675,7 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     P.binW = binW;
     P.rasterBlocks = p->rasterBlocks;
     P.passFp = pass_fp(dd.data(), dd.size());
+    P.forward = forward;
     P.binsX = binsX;
     P.binsY = binsY;
     P.nTris = nTris;
@@ -1315,7 +1327,6 @@ int ps3d_draw(ps3d_pipeline* p, int vao)
     if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
     // drawvao.cpp:12-15: silently nothing without a programme or with a bad VAO
     if (!p->vp || !p->ip || !p->fp || vao < 0 || vao >= (int)p->vaos.size() || !p->vaos[vao].alive) return 0;
-    if (p->behavior & B_ALPHABLEND) return fail(PS3D_ERR_INVALID, "ALPHABLEND is not supported on this path");
     const Vao& va = p->vaos[vao];
     Command c;
     memset(&c, 0, sizeof c);
@@ -1802,6 +1813,8 @@ struct NoAllocPass {
     int binsX = 0, binsY = 0;
     size_t nBins = 0;
     int pairCap = 0;  // largest multiple of the sort chunk that fits, 0 if none does
+    bool forward = false;
+    int binW = 0;
 };
 
 int noalloc_shape(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps, NoAllocPass& s, bool stage)
@@ -1823,9 +1836,11 @@ int noalloc_shape(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass
         s.nTris += d.triCount;
         s.nvMax = std::max(s.nvMax, d.nv);
         s.anyColour |= (d.flags & F_COLOUR) != 0;
+        s.forward |= pass_forward(&d, 1);
     }
     if (s.nTris == 0) return 0;
-    s.binsX = (s.tg.w + p->binW - 1) / p->binW;
+    s.binW = s.forward ? 16 : p->binW;
+    s.binsX = (s.tg.w + s.binW - 1) / s.binW;
     s.binsY = (s.tg.h + kBinH - 1) / kBinH;
     s.nBins = (size_t)s.binsX * s.binsY;
     NoAllocLayout L;
@@ -1881,9 +1896,10 @@ int noalloc_run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const P
     memset(&P, 0, sizeof P);
     P.W = W;
     P.H = H;
-    P.binW = p->binW;
+    P.binW = s.binW;
     P.rasterBlocks = p->rasterBlocks;
     P.passFp = pass_fp(g_noallocDraws, (size_t)s.nd);
+    P.forward = s.forward;
     P.binsX = s.binsX;
     P.binsY = s.binsY;
     P.nTris = s.nTris;

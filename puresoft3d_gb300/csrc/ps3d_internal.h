@@ -18,7 +18,7 @@ enum : int {
     VP_DEF01 = 0x0101, IP_DEF01 = 0x0102, FP_DEF01 = 0x0103,
     VP_DEF05 = 0x0501, IP_DEF05 = 0x0502, FP_DEF05 = 0x0503,
     VP_SHADOW = 0x0601,
-    FP_LIT1 = 0x1103, FP_LIT3 = 0x1303,
+    FP_LIT1 = 0x1103, FP_LIT1A = 0x1403, FP_LIT3 = 0x1303,
     VP_LIT2 = 0x1201, IP_LIT2 = 0x1202, FP_LIT2 = 0x1203,
 };
 
@@ -76,6 +76,7 @@ struct PassParams {
     int binW, binsX, binsY;   // bins of kBinH x binW pixels
     int rasterBlocks;         // raster variant: 0 = registers as needed, 8 = capped for 8 blocks per SM
     int passFp;               // the fragment processor every colour draw of the pass uses, else 0
+    int forward;              // some draw blends or may discard: shade every passing fragment in order
     int nTris, nDraws;
     const DrawDesc* draws;
     const DrawUniforms* unis;

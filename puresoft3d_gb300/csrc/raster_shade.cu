@@ -52,17 +52,109 @@ struct SpanRec {
     short flags;
 };
 
+// The interpolation stage's state along one span (interp.cpp:26-92 with the
+// draw's interpolation processor): start/step from the corrected
+// contributions, the left-clamp skip, then one step per pixel from
+// leftClamped -- sequential adds, so pixel k needs k steps.
+template <int NV> struct VaryState {
+    float st[NV], sp[NV];
+    float cf2, cf2Step;
+    int x;  // the pixel the state is at
+};
+
+template <int NV>
+__device__ __forceinline__ void vary_begin(const TriRaster& t, const float* vary, int nvMax, const Span& s,
+                                           const SpanZ& z, VaryState<NV>& v)
+{
+    const float* a = vary;
+    const float* b = vary + nvMax;
+    const float* c = vary + 2 * nvMax;
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+        float va = __ldg(a + k), vb = __ldg(b + k), vc = __ldg(c + k);
+        float s0 = fadd(fadd(fmul(va, z.cl[0]), fmul(vb, z.cl[1])), fmul(vc, z.cl[2]));
+        float e0 = fadd(fadd(fmul(va, z.cr[0]), fmul(vb, z.cr[1])), fmul(vc, z.cr[2]));
+        v.st[k] = s0;
+        v.sp[k] = fmul(fsub(e0, s0), z.recip);  // calcStep: stepCount != 0 here
+    }
+    if (z.skip == 1) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) v.st[k] = fadd(v.st[k], v.sp[k]);
+    } else if (z.skip > 1) {
+        float fs = (float)z.skip;
+#pragma unroll
+        for (int k = 0; k < NV; k++) v.st[k] = fadd(v.st[k], fmul(v.sp[k], fs));
+    }
+    v.cf2 = z.cf2;
+    v.cf2Step = z.cf2Step;
+    v.x = s.leftClamped;
+}
+
+template <int NV> __device__ __forceinline__ void vary_advance(VaryState<NV>& v, int x)
+{
+    for (; v.x < x; v.x++) {
+        v.cf2 = fadd(v.cf2, v.cf2Step);
+#pragma unroll
+        for (int k = 0; k < NV; k++) v.st[k] = fadd(v.st[k], v.sp[k]);
+    }
+}
+
+template <int NV> __device__ __forceinline__ void vary_out(const VaryState<NV>& v, float out[NV])
+{
+    float inv = frcp(v.cf2);
+#pragma unroll
+    for (int k = 0; k < NV; k++) out[k] = fmul(v.st[k], inv);
+}
+
+// Varyings of the fragment at x on row y of triangle t.
+template <int NV>
+__device__ __forceinline__ void fragment_varyings(const TriRaster& t, const float* vary, int nvMax, const Span& s,
+                                                  const SpanZ& z, int x, float out[NV])
+{
+    VaryState<NV> v;
+    vary_begin<NV>(t, vary, nvMax, s, z, v);
+    vary_advance<NV>(v, x);
+    vary_out<NV>(v, out);
+}
+
+// The fragment processor of draw d on one fragment: 1 = colour written to
+// bgra, 2 = discarded (no colour, no depth write), 0 = no colour (depth only).
+template <int NV>
+__device__ __forceinline__ int shade_fragment(const DrawDesc& d, const DrawUniforms& U, const float* in,
+                                              uint32_t& bgra)
+{
+    switch (d.fp) {
+    case FP_LIT1: bgra = shade_lit1(U, in); return 1;
+    case FP_LIT1A: return shade_lit1a(U, in, bgra) ? 1 : 2;
+    case FP_LIT3: bgra = shade_lit3(U, in); return 1;
+    case FP_DEF01: bgra = shade_def01(U, in); return 1;
+    case FP_LIT2:
+        if constexpr (NV >= 16) {
+            bgra = shade_lit2(U, in);
+            return 1;
+        }
+        return 0;
+    default: return 0;
+    }
+}
+
 constexpr int kRasterThreads = 128;  // 4 warps: warp = column quarter, lane = bin row
 constexpr int kChunk = 128;          // triangles per chunk (one per thread)
 constexpr int kSlots = 128;          // (triangle, row) spans per round (one per thread)
 
-template <int BW, int MINB>
+// FWD (forward mode, 9 or 16 varyings): for passes that blend or may
+// discard, every fragment that passes the depth test is shaded in the walk,
+// in order, into the bin's colour tile (blend4 under ALPHABLEND; a discard
+// skips the colour and the depth write) -- the reference's per-fragment
+// order (fragthrd.cpp:208-252); no shade list.
+template <int BW, int MINB, int FWD = 0>
 __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
 {
     constexpr int S = BW + 1;   // padded strides: threads at one column hit distinct banks
     constexpr int Q = BW / 4;   // columns per quarter
     __shared__ float sDepth[kBinH * S];
     __shared__ int sWin[kBinH * S];
+    __shared__ uint32_t sCol[FWD ? kBinH * S : 1];  // forward mode: the bin's colour
     __shared__ float sZ[kSlots * S];             // exact z of every pixel of each span
     __shared__ float sZmin[4][kSlots];           // per span and quarter: min z over its pixels
     __shared__ __align__(16) TriRaster sTri[kChunk];
@@ -111,6 +203,13 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
         if (!P.clearDepth && r < rows && c < cols) d = P.depth[(size_t)(y0 + r) * P.depthScan + x0 + c];
         sDepth[r * S + c] = d;
         sWin[r * S + c] = -1;
+        if constexpr (FWD > 0) {
+            uint32_t col = P.colourClearValue;
+            int x = x0 + c, y = y0 + r;
+            if (!P.clearColour && r < rows && c < cols && x < P.colourW && y < P.colourH)
+                col = ((const uint32_t*)P.colour)[(size_t)(P.colourH - 1 - y) * P.colourW + x];
+            sCol[r * S + c] = col;
+        }
     }
     for (int i = tid; i < 2 * 4 * kBinH * (kSlots / 32); i += kRasterThreads) (&sMask[0][0][0][0])[i] = 0u;
     int par = 0;  // mask buffer of the current round
@@ -245,13 +344,52 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
                         if ((flags & B_TEST_DEPTH) && fsub(sZmin[warp][s2], curMax) >= -0.0001f) continue;
                         const float* zrow = sZ + s2 * S;
                         const int triId = sTid[R.j];
-                        for (int x = a; x <= b; x++) {
-                            float zz = zrow[x];
-                            float cur = (flags & B_TEST_DEPTH) ? dRow[x] : 1.0f;
-                            if (-1.0f < zz && fsub(zz, cur) < -0.0001f) {
-                                if (flags & B_UPDATE_DEPTH) dRow[x] = zz;
-                                if (flags & F_COLOUR) wRow[x] = triId;
+                        if constexpr (FWD > 0) {
+                            // shade each passing fragment in order; the span's
+                            // interpolation state is set up at the first one
+                            VaryState<FWD> vs;
+                            bool begun = false;
+                            const int j = R.j, ox = sOx[j], yl = y0 + lane - sOy[j];
+                            const DrawDesc& dd = P.draws[sTri[j].draw];
+                            for (int x = a; x <= b; x++) {
+                                float zz = zrow[x];
+                                float cur = (flags & B_TEST_DEPTH) ? dRow[x] : 1.0f;
+                                if (!(-1.0f < zz && fsub(zz, cur) < -0.0001f)) continue;
                                 passed++;
+                                int w = 0;
+                                uint32_t bgra = 0;
+                                if (flags & F_COLOUR) {
+                                    const TriRaster& t = sTri[j];
+                                    if (!begun) {
+                                        Span sp;
+                                        span_row(t, yl, sLw[j], sp);
+                                        SpanZ zs;
+                                        span_z(t, sp, yl, zs);
+                                        vary_begin<FWD>(t, P.vary + (size_t)triId * 3 * P.nvMax, P.nvMax, sp, zs, vs);
+                                        begun = true;
+                                    }
+                                    vary_advance<FWD>(vs, x0 + x - ox);
+                                    float in[FWD];
+                                    vary_out<FWD>(vs, in);
+                                    w = shade_fragment<FWD>(dd, P.unis[dd.uni], in, bgra);
+                                }
+                                if (w == 1) {
+                                    uint32_t* cp = sCol + lane * S + x;
+                                    // FBOBridge::write4 blends under ALPHABLEND; DEF01 writes
+                                    // through FBOBridge::write, which never blends
+                                    *cp = ((flags & B_ALPHABLEND) && dd.fp != FP_DEF01) ? blend4(*cp, bgra) : bgra;
+                                }
+                                if (w != 2 && (flags & B_UPDATE_DEPTH)) dRow[x] = zz;
+                            }
+                        } else {
+                            for (int x = a; x <= b; x++) {
+                                float zz = zrow[x];
+                                float cur = (flags & B_TEST_DEPTH) ? dRow[x] : 1.0f;
+                                if (-1.0f < zz && fsub(zz, cur) < -0.0001f) {
+                                    if (flags & B_UPDATE_DEPTH) dRow[x] = zz;
+                                    if (flags & F_COLOUR) wRow[x] = triId;
+                                    passed++;
+                                }
                             }
                         }
                         if (!(flags & B_TEST_DEPTH)) {  // depth may have risen: recompute the bound
@@ -273,7 +411,15 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
         P.depth[(size_t)(y0 + r) * P.depthScan + x0 + c] = sDepth[r * S + c];
         covered += sWin[r * S + c] >= 0;
     }
-    if (P.anyColour || P.clearColour) {
+    if constexpr (FWD > 0) {
+        if (P.anyColour || P.clearColour)
+            for (int i = tid; i < rows * cols; i += kRasterThreads) {
+                int r = i / cols, c = i - r * cols, x = x0 + c, y = y0 + r;
+                if (x < P.colourW && y < P.colourH)
+                    ((uint32_t*)P.colour)[(size_t)(P.colourH - 1 - y) * P.colourW + x] = sCol[r * S + c];
+            }
+        covered = 0;  // nothing is left to shade
+    } else if (P.anyColour || P.clearColour) {
         // one block-wide reservation in the shade list, then each thread's
         // covered pixels in order; uncovered pixels get the clear colour
         int inc = covered;
@@ -326,40 +472,6 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
 // with the draw's interpolation stage): start/step from the corrected
 // contributions, the left-clamp skip, then one step per pixel from
 // leftClamped; returns start * (1 / cf2).
-template <int NV>
-__device__ __forceinline__ void fragment_varyings(const TriRaster& t, const float* vary, int nvMax, const Span& s,
-                                                  const SpanZ& z, int x, float out[NV])
-{
-    float st[NV], sp[NV];
-    const float* a = vary;
-    const float* b = vary + nvMax;
-    const float* c = vary + 2 * nvMax;
-#pragma unroll
-    for (int k = 0; k < NV; k++) {
-        float va = __ldg(a + k), vb = __ldg(b + k), vc = __ldg(c + k);
-        float s0 = fadd(fadd(fmul(va, z.cl[0]), fmul(vb, z.cl[1])), fmul(vc, z.cl[2]));
-        float e0 = fadd(fadd(fmul(va, z.cr[0]), fmul(vb, z.cr[1])), fmul(vc, z.cr[2]));
-        st[k] = s0;
-        sp[k] = fmul(fsub(e0, s0), z.recip);  // calcStep: stepCount != 0 here
-    }
-    if (z.skip == 1) {
-#pragma unroll
-        for (int k = 0; k < NV; k++) st[k] = fadd(st[k], sp[k]);
-    } else if (z.skip > 1) {
-        float fs = (float)z.skip;
-#pragma unroll
-        for (int k = 0; k < NV; k++) st[k] = fadd(st[k], fmul(sp[k], fs));
-    }
-    float cf2 = z.cf2;
-    for (int i = s.leftClamped; i < x; i++) {
-        cf2 = fadd(cf2, z.cf2Step);
-#pragma unroll
-        for (int k = 0; k < NV; k++) st[k] = fadd(st[k], sp[k]);
-    }
-    float inv = frcp(cf2);
-#pragma unroll
-    for (int k = 0; k < NV; k++) out[k] = fmul(st[k], inv);
-}
 
 // FPK: the fragment processor when every draw of the pass uses the same
 // one (a kernel with only that shader's registers), else 0 (any).
@@ -441,11 +553,19 @@ template <int BW> void launch_raster(const PassParams& P, int nBins, cudaStream_
     else k_raster<BW, 1><<<nBins, kRasterThreads, 0, s>>>(P);
 }
 
+// Forward passes (blending or discarding draws) run with 16-column bins.
+void launch_raster_forward(const PassParams& P, int nBins, cudaStream_t s)
+{
+    if (P.nvMax <= 9) k_raster<16, 1, 9><<<nBins, kRasterThreads, 0, s>>>(P);
+    else k_raster<16, 1, 16><<<nBins, kRasterThreads, 0, s>>>(P);
+}
+
 void launch_raster(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
 {
     int nBins = P.binsX * P.binsY;
     pr->begin(K_RASTER, s);
-    switch (P.binW) {
+    if (P.forward) launch_raster_forward(P, nBins, s);
+    else switch (P.binW) {
     case 8: launch_raster<8>(P, nBins, s); break;
     case 16: launch_raster<16>(P, nBins, s); break;
     default: launch_raster<32>(P, nBins, s); break;
@@ -456,7 +576,7 @@ void launch_raster(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
 
 void launch_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
 {
-    if (!P.anyColour) return;
+    if (!P.anyColour || P.forward) return;  // a forward pass shaded in the raster
     // a grid that fills the GPU, striding over the shade list
     int dev = 0, sms = 0, perSM = 0;
     cudaGetDevice(&dev);

@@ -38,7 +38,7 @@ import numpy as np
 VP_DEF01, IP_DEF01, FP_DEF01 = 0x0101, 0x0102, 0x0103
 VP_DEF05, IP_DEF05, FP_DEF05 = 0x0501, 0x0502, 0x0503
 VP_SHADOW = 0x0601
-FP_LIT1, FP_LIT3 = 0x1103, 0x1303
+FP_LIT1, FP_LIT1A, FP_LIT3 = 0x1103, 0x1403, 0x1303
 VP_LIT2, IP_LIT2, FP_LIT2 = 0x1201, 0x1202, 0x1203
 
 UPDATE_DEPTH, TEST_DEPTH, FACE_CULLING, ALPHABLEND = 1, 2, 4, 8

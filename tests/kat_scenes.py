@@ -27,13 +27,25 @@ def _tri_mesh(clip):
     return {"position": clip, "normal": normal, "uv": uv, "tangent": np.tile([1, 0, 0, 1], (n, 1)).astype(np.float32)}
 
 
-def _scene(name, w, h, clip, lit=True, behavior_off=0, texture_seed=7):
+def _alpha_texture(seed):
+    """A 16x16 BGRA texture whose alpha runs over 0..255 in a seeded checker,
+    so an alpha test discards some fragments and blending weights differ."""
+    rng = np.random.default_rng(seed)
+    img = S.checker_noise_bgra(16, 4, rng).copy()
+    yy, xx = np.mgrid[0:16, 0:16]
+    img[..., 3] = (np.array([0, 90, 140, 255], dtype=np.uint8)[(yy // 4 + xx // 4) % 4]
+                   + rng.integers(0, 20, size=(16, 16))).clip(0, 255).astype(np.uint8)
+    return img
+
+
+def _scene(name, w, h, clip, lit=True, behavior_off=0, texture_seed=7, fp=None, behavior_on=0):
     b = S._Builder()
     rng = np.random.default_rng(texture_seed)
-    tex = b.texture(S.checker_noise_bgra(16, 4, rng))
+    tex = b.texture(_alpha_texture(texture_seed) if (fp == S.FP_LIT1A or behavior_on & S.ALPHABLEND)
+                    else S.checker_noise_bgra(16, 4, rng))
     depth = b.empty_texture(w, h)
-    prog = b.programme(S.VP_DEF01, S.IP_DEF01, S.FP_LIT1) if lit else b.programme(S.VP_SHADOW, S.IP_DEF05,
-                                                                                  S.FP_DEF05)
+    prog = b.programme(S.VP_DEF01, S.IP_DEF01, fp or S.FP_LIT1) if lit else b.programme(S.VP_SHADOW, S.IP_DEF05,
+                                                                                        S.FP_DEF05)
     mesh = _tri_mesh(clip)
     vao = b.vao(mesh, slots=(0, 3, 4) if lit else (0,))
     eye = np.eye(4)
@@ -42,6 +54,8 @@ def _scene(name, w, h, clip, lit=True, behavior_off=0, texture_seed=7):
     b.f("clearColour", 0xFF101010)
     if behavior_off:
         b.f("disable", behavior_off)
+    if behavior_on:
+        b.f("enable", behavior_on)
     b.f("useProgramme", prog)
     b.f("setUniform", 3, S.col_major(eye))
     b.f("setUniform", 4, S.col_major(eye))
@@ -114,4 +128,14 @@ def kat_scenes():
     out.append(("kat_soup_depth_97x63", _scene("kat_soup_depth", 97, 63, random_soup(400, 12), lit=False)))
     out.append(("kat_soup_ortho_nocull_80x80",
                 _scene("kat_soup_ortho", 80, 80, random_soup(300, 13, persp=False), behavior_off=S.FACE_CULLING)))
+    # blending (fbo.cpp:208-229) and discard (fragthrd.cpp:233-237): every
+    # passing fragment is shaded, in order
+    out.append(("kat_blend_lit_96x64", _scene("kat_blend_lit", 96, 64, random_soup(300, 14),
+                                              behavior_on=S.ALPHABLEND)))
+    out.append(("kat_alphatest_96x64", _scene("kat_alphatest", 96, 64, random_soup(300, 15), fp=S.FP_LIT1A)))
+    out.append(("kat_alphatest_blend_nocull_88x72",
+                _scene("kat_alphatest_blend", 88, 72, random_soup(300, 16), fp=S.FP_LIT1A,
+                       behavior_on=S.ALPHABLEND, behavior_off=S.FACE_CULLING)))
+    out.append(("kat_blend_notest_64x48", _scene("kat_blend_notest", 64, 48, random_soup(120, 17),
+                                                 behavior_on=S.ALPHABLEND, behavior_off=S.TEST_DEPTH)))
     return out
