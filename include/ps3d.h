@@ -65,6 +65,26 @@ extern "C" {
 #define PS3D_VP_DEF01 0x0101
 #define PS3D_IP_DEF01 0x0102
 #define PS3D_FP_DEF01 0x0103
+/* The reference's vertex-colour processors (colr1light1.cpp): VBO slots 0
+ * position, 1 normal, 2 colour (four floats, BGRA order, 0..255); uniforms
+ * 3-5 and 7-8 as DEF01; DEF01's lighting on the interpolated colour. */
+#define PS3D_VP_DEF02 0x0201
+#define PS3D_IP_DEF02 0x0202
+#define PS3D_FP_DEF02 0x0203
+/* The reference's bump-mapped processors (tex1bump1light1.cpp): VBO slots 0
+ * position, 1 tangent, 2 binormal, 3 normal, 4 uv; uniform 9 the diffuse
+ * texture, 10 the bump texture (tangent-space normal in r, g, b). */
+#define PS3D_VP_DEF03 0x0301
+#define PS3D_IP_DEF03 0x0302
+#define PS3D_FP_DEF03 0x0303
+/* The reference's skybox processors (skybox.cpp): VBO slot 0 holds clip-space
+ * positions, passed through; uniform 1 the view matrix, uniform 2 the index
+ * of a cube map (ps3d_texture_create_layers with 5 extra layers, BGRA8).
+ * The fragment stage reads the face texel the view direction points at
+ * (samplrcube.cpp:29-127) and writes it (blended under ALPHABLEND). */
+#define PS3D_VP_DEF04 0x0401
+#define PS3D_IP_DEF04 0x0402
+#define PS3D_FP_DEF04 0x0403
 #define PS3D_VP_DEF05 0x0501
 #define PS3D_IP_DEF05 0x0502
 #define PS3D_FP_DEF05 0x0503
@@ -120,6 +140,20 @@ int ps3d_texture_create(ps3d_pipeline* p, int width, int height, int scanline, i
 /* Same, from device memory (cudaMemcpyDeviceToDevice). */
 int ps3d_texture_create_device(ps3d_pipeline* p, int width, int height, int scanline, int elemLen,
                                const void* devPixels, int wrap);
+/* PuresoftPipeline::createTexture(image, extraLayers, mode) (tex.cpp:3-25,
+ * fbo.cpp:59-73): a texture with 0..5 extra layers of the same size, stored
+ * after the first; `pixels` fills layer 0 and the extra layers start zeroed.
+ * Five extra layers make a cube map, faces in the order +x, -x, +y, -y, +z,
+ * -z (PuresoftFBO::LAYER, fbo.h:19).  More than 5 is PS3D_ERR_RANGE (the
+ * reference throws out_of_range above 6, and 6 overruns its layer array). */
+int ps3d_texture_create_layers(ps3d_pipeline* p, int width, int height, int scanline, int elemLen,
+                               const void* pixels, int wrap, int extraLayers);
+/* PuresoftPipeline::getTexture(idx, image, layer) (tex.cpp:27-37) hands the
+ * caller the layer's buffer to fill or read; these copy min(bytes,
+ * scanline*height) bytes into or out of layer `layer` after pending work
+ * has finished. */
+int ps3d_texture_write_layer(ps3d_pipeline* p, int idx, int layer, const void* pixels, size_t bytes);
+int ps3d_texture_read_layer(ps3d_pipeline* p, int idx, int layer, void* out, size_t bytes);
 /* PuresoftPipeline::destroyTexture (tex.cpp:39-51). */
 int ps3d_texture_destroy(ps3d_pipeline* p, int idx);
 /* PuresoftPipeline::getTexture (tex.cpp:27-37): waits for pending work, then
@@ -288,7 +322,8 @@ int ps3d_timer_end(ps3d_pipeline* p, float* ms);
 #define PS3D_K_RASTER 5
 #define PS3D_K_SHADE 6
 #define PS3D_K_FILL 7
-#define PS3D_K_COUNT 8
+#define PS3D_K_POST 8    /* post-processors */
+#define PS3D_K_COUNT 9
 /* Checks the bounded device waits: one warp polls a flag that nothing sets,
  * sleeping between polls, and gives up after `spins` polls, marking the
  * failure as an expired look-back of the bin sort does.  Returns

@@ -53,14 +53,20 @@
 /* processor ids (include/ps3d.h) */
 enum {
     VP_DEF01 = 0x0101, IP_DEF01 = 0x0102, FP_DEF01 = 0x0103,
+    VP_DEF02 = 0x0201, IP_DEF02 = 0x0202, FP_DEF02 = 0x0203,
+    VP_DEF03 = 0x0301, IP_DEF03 = 0x0302, FP_DEF03 = 0x0303,
+    VP_DEF04 = 0x0401, IP_DEF04 = 0x0402, FP_DEF04 = 0x0403,
     VP_DEF05 = 0x0501, IP_DEF05 = 0x0502, FP_DEF05 = 0x0503,
     VP_SHADOW = 0x0601,
     FP_LIT1 = 0x1103, FP_LIT1A = 0x1403, FP_LIT3 = 0x1303,
     VP_LIT2 = 0x1201, IP_LIT2 = 0x1202, FP_LIT2 = 0x1203
 };
 
+/* A texture: `layers` images of scanline*height bytes each, back to back
+   (layer 0 is the FBO itself, 1.. its extra layers, fbo.cpp:59-73; a cube
+   map has the six faces in LAYER order, fbo.h:19). */
 typedef struct {
-    int width, height, scanline, elemLen, wrap, topDown;
+    int width, height, scanline, elemLen, wrap, topDown, layers;
     uint8_t* buf;
 } o_fbo;
 
@@ -227,12 +233,16 @@ void ps3do_destroy(ps3do* p)
 }
 
 /* tex.cpp:3-25: copies pixels into a pipeline-owned FBO (topDown = false). */
-int ps3do_texture_create(ps3do* p, int width, int height, int scanline, int elemLen, const void* pixels, int wrap)
+int ps3do_texture_create_layers(ps3do* p, int width, int height, int scanline, int elemLen, const void* pixels,
+                                int wrap, int extraLayers)
 {
     o_fbo* f;
     int slot = 0;
+    size_t layer;
     if (elemLen != 1 && elemLen != 4) return -2; /* fbo.cpp:21-24 */
     if (width <= 0 || height <= 0 || scanline < width * elemLen) return -2;
+    /* fbo.cpp:62-72: more than LAYER_MAX - 1 extra layers is out of range */
+    if (extraLayers < 0 || extraLayers > 5) return -1;
     for (; slot < p->ntex; slot++)
         if (!p->tex[slot]) break;
     if (slot == p->ntex) {
@@ -246,26 +256,53 @@ int ps3do_texture_create(ps3do* p, int width, int height, int scanline, int elem
     f->scanline = scanline;
     f->elemLen = elemLen;
     f->wrap = wrap;
-    f->buf = (uint8_t*)calloc((size_t)scanline * height, 1);
+    f->layers = 1 + extraLayers;
+    layer = (size_t)scanline * height;
+    f->buf = (uint8_t*)calloc(layer * f->layers, 1);
     if (!f->buf) { free(f); return -3; }
-    if (pixels) memcpy(f->buf, pixels, (size_t)scanline * height);
+    if (pixels) memcpy(f->buf, pixels, layer); /* tex.cpp:18-23: the default layer */
     p->tex[slot] = f;
     return slot;
 }
 
-int ps3do_texture_read(ps3do* p, int idx, void* out, size_t bytes)
+int ps3do_texture_create(ps3do* p, int width, int height, int scanline, int elemLen, const void* pixels, int wrap)
+{
+    return ps3do_texture_create_layers(p, width, height, scanline, elemLen, pixels, wrap, 0);
+}
+
+/* getTexture(idx, image, layer) (tex.cpp:27-37) hands out the layer's
+   buffer; these copy into or out of it. */
+int ps3do_texture_write_layer(ps3do* p, int idx, int layer, const void* pixels, size_t bytes)
 {
     size_t n;
     if (idx < 0 || idx >= p->ntex || !p->tex[idx]) return -1;
+    if (layer < 0 || layer >= p->tex[idx]->layers) return -1;
     n = (size_t)p->tex[idx]->scanline * p->tex[idx]->height;
-    memcpy(out, p->tex[idx]->buf, n < bytes ? n : bytes);
+    memcpy(p->tex[idx]->buf + n * layer, pixels, n < bytes ? n : bytes);
     return 0;
+}
+
+int ps3do_texture_read_layer(ps3do* p, int idx, int layer, void* out, size_t bytes)
+{
+    size_t n;
+    if (idx < 0 || idx >= p->ntex || !p->tex[idx]) return -1;
+    if (layer < 0 || layer >= p->tex[idx]->layers) return -1;
+    n = (size_t)p->tex[idx]->scanline * p->tex[idx]->height;
+    memcpy(out, p->tex[idx]->buf + n * layer, n < bytes ? n : bytes);
+    return 0;
+}
+
+int ps3do_texture_read(ps3do* p, int idx, void* out, size_t bytes)
+{
+    return ps3do_texture_read_layer(p, idx, 0, out, bytes);
 }
 
 static int known_processor(int id)
 {
     switch (id) {
     case VP_DEF01: case IP_DEF01: case FP_DEF01: case VP_DEF05: case IP_DEF05: case FP_DEF05:
+    case VP_DEF02: case IP_DEF02: case FP_DEF02: case VP_DEF03: case IP_DEF03: case FP_DEF03:
+    case VP_DEF04: case IP_DEF04: case FP_DEF04:
     case VP_SHADOW: case FP_LIT1: case FP_LIT1A: case FP_LIT3: case VP_LIT2: case IP_LIT2: case FP_LIT2:
         return 1;
     }
@@ -422,6 +459,9 @@ static int ip_vecs(int ip)
     switch (ip) {
     case IP_DEF01: return 3; /* PROCDATA_DEF01: normal, worldPos, texcoord (tex1light1.h:4-9) */
     case IP_LIT2: return 5;  /* normal, tangent, worldPos, texcoord, shadowPos */
+    case IP_DEF02: return 3; /* PROCDATA_DEF02: normal, worldPos, colour (colr1light1.h:3-9) */
+    case IP_DEF03: return 5; /* PROCDATA_DEF03: tangent, binormal, normal, worldPos, texcoord (tex1bump1light1.h:4-11) */
+    case IP_DEF04: return 1; /* PROCDATA_DEF04: direction (skybox.h:3-7) */
     default: return 0;       /* IP_DEF05: no varyings (shadow.h) */
     }
 }
@@ -440,6 +480,51 @@ static void run_vp(const ps3do* p, const void* const* in, float* pos, float* use
         memcpy(pos, wp, 16);
         wp[3] = 0;
         m4v4(pos, ufl(p, 3), pos);
+        m4v4(nrm, ufl(p, 5), (const float*)in[3]);
+        tc[0] = uv[0];
+        tc[1] = uv[1];
+        tc[2] = tc[3] = 0.0f;
+        break;
+    }
+    case VP_DEF02: { /* colr1light1.cpp:22-40: normal in VBO 1, colour in VBO 2 */
+        float* nrm = user, * wp = user + 4, * col = user + 8;
+        m4v4(wp, ufl(p, 4), (const float*)in[0]);
+        memcpy(pos, wp, 16);
+        wp[3] = 0;
+        m4v4(pos, ufl(p, 3), pos);
+        m4v4(nrm, ufl(p, 5), (const float*)in[1]);
+        memcpy(col, in[2], 16);
+        break;
+    }
+    case VP_DEF04: { /* skybox.cpp:23-44: the position passes through; the
+                        direction is the view's inverse rotation (the
+                        transposed view matrix with its last column zeroed)
+                        times the normalised vector from the observer
+                        (0, 0, 1) to the vertex */
+        const float* v = (const float*)in[0];
+        float d[4], inv[16], r;
+        d[0] = v[0] - 0.0f;
+        d[1] = v[1] - 0.0f;
+        d[2] = v[2] - 1.0f;
+        d[3] = 0.0f;
+        r = 1.0f / sqrtf((d[0] * d[0] + d[1] * d[1]) + (d[2] * d[2] + d[3] * d[3]));
+        for (int k = 0; k < 4; k++) d[k] = d[k] * r;
+        for (int c = 0; c < 4; c++)
+            for (int rr = 0; rr < 4; rr++) inv[4 * c + rr] = ufl(p, 1)[4 * rr + c];
+        for (int k = 12; k < 16; k++) inv[k] = 0.0f;
+        m4v4(user, inv, d);
+        memcpy(pos, v, 16);
+        break;
+    }
+    case VP_DEF03: { /* tex1bump1light1.cpp:22-46 */
+        float* tan = user, * bin = user + 4, * nrm = user + 8, * wp = user + 12, * tc = user + 16;
+        const float* uv = (const float*)in[4];
+        m4v4(wp, ufl(p, 4), (const float*)in[0]);
+        memcpy(pos, wp, 16);
+        wp[3] = 0;
+        m4v4(pos, ufl(p, 3), pos);
+        m4v4(tan, ufl(p, 5), (const float*)in[1]);
+        m4v4(bin, ufl(p, 5), (const float*)in[2]);
         m4v4(nrm, ufl(p, 5), (const float*)in[3]);
         tc[0] = uv[0];
         tc[1] = uv[1];
@@ -526,6 +611,8 @@ typedef struct {
     const float* light;
     const float* cam;
     const o_fbo* tex;
+    const o_fbo* tex2;  /* DEF03's bump map */
+    const o_fbo* cube;  /* DEF04's cube map */
     sr_level chainA[MAX_LEVELS], chainN[MAX_LEVELS];
     int levelsA, levelsN;
     const float* shadow;
@@ -545,6 +632,27 @@ static int fp_prepare(const ps3do* p, fp_state* s)
         s->light = ufl(p, 7);
         s->cam = ufl(p, 8);
         s->tex = p->tex[t];
+        break;
+    }
+    case FP_DEF02: /* colr1light1.cpp:144-148 */
+        s->light = ufl(p, 7);
+        s->cam = ufl(p, 8);
+        break;
+    case FP_DEF04: { /* skybox.cpp:122-125: the cube map's index at uniform 2 */
+        int t = *uin(p, 2);
+        /* get4 reads four bytes per texel from one of six layers
+           (samplrcube.cpp:119-127) */
+        if (t < 0 || t >= p->ntex || !p->tex[t] || p->tex[t]->layers < 6 || p->tex[t]->elemLen != 4) return -1;
+        s->cube = p->tex[t];
+        break;
+    }
+    case FP_DEF03: { /* tex1bump1light1.cpp:170-176: diffuse at 9, bump at 10 */
+        int t = *uin(p, 9), b = *uin(p, 10);
+        if (t < 0 || t >= p->ntex || !p->tex[t] || b < 0 || b >= p->ntex || !p->tex[b]) return -1;
+        s->light = ufl(p, 7);
+        s->cam = ufl(p, 8);
+        s->tex = p->tex[t];
+        s->tex2 = p->tex[b];
         break;
     }
     case FP_LIT3:
@@ -580,17 +688,14 @@ static int fp_prepare(const ps3do* p, fp_state* s)
     return 0;
 }
 
-/* FragmentProcessorDEF01::process (tex1light1.cpp:152-193) with IEEE 1/x and
-   1/sqrt in place of rcpps / rsqrtss (see the header note). */
-static void fp_def01(const fp_state* s, const float* in, uint8_t* bgra)
+/* PuresoftSampler2D::get4 (samplr2d.cpp:19-25): nearest texel at
+   (unsigned)(size * coord + 0.5f), then directRead4 -> clampCoord
+   (fbo.cpp:287-291, 552-594); the texel's bytes in memory (BGRA) order. */
+static void sample_nearest(const o_fbo* t, const float* tc, float c[4])
 {
-    const float* nrm = in, * wp = in + 4, * tc = in + 8;
-    const o_fbo* t = s->tex;
-    float c[4], L[4], E[4], Hv[4], dist, lambert, spec, r;
     int row = (int)sr_f2u((float)t->height * tc[1] + 0.5f);
     int col = (int)sr_f2u((float)t->width * tc[0] + 0.5f);
     const uint8_t* px;
-    /* directRead4 -> clampCoord (fbo.cpp:287-291, 552-594) */
     if (t->wrap) {
         int mr = t->height - 1, mc = t->width - 1;
         row = mr > 0 ? row % mr : 0;
@@ -603,6 +708,15 @@ static void fp_def01(const fp_state* s, const float* in, uint8_t* bgra)
     }
     px = t->buf + (size_t)row * t->scanline + 4 * col;
     for (int k = 0; k < 4; k++) c[k] = (float)px[k];
+}
+
+/* The lighting shared by DEF01 and DEF03 (tex1light1.cpp:165-192,
+   tex1bump1light1.cpp:212-237) on colour c (BGRA floats), normal n and
+   world position wp (all four lanes, as the 4-wide mcemaths ops use them),
+   with IEEE 1/x and 1/sqrt in place of rcpps / rsqrtss (see the header). */
+static void def_lighting(const fp_state* s, float c[4], const float* nrm, const float* wp, uint8_t* bgra)
+{
+    float L[4], E[4], Hv[4], dist, lambert, spec, r;
     for (int k = 0; k < 4; k++) L[k] = s->light[k] - wp[k];
     dist = sqrtf((L[0] * L[0] + L[1] * L[1]) + (L[2] * L[2] + L[3] * L[3]));
     r = 1.0f / dist;
@@ -638,6 +752,98 @@ static void fp_def01(const fp_state* s, const float* in, uint8_t* bgra)
     bgra[1] = (uint8_t)(int)c[1];
     bgra[2] = (uint8_t)(int)c[2];
     bgra[3] = 0;
+}
+
+/* FragmentProcessorDEF01::process (tex1light1.cpp:152-193). */
+static void fp_def01(const fp_state* s, const float* in, uint8_t* bgra)
+{
+    const float* nrm = in, * wp = in + 4, * tc = in + 8;
+    float c[4];
+    sample_nearest(s->tex, tc, c);
+    def_lighting(s, c, nrm, wp, bgra);
+}
+
+/* FragmentProcessorDEF02::process (colr1light1.cpp:150-190): the
+   interpolated vertex colour, then DEF01's lighting. */
+static void fp_def02(const fp_state* s, const float* in, uint8_t* bgra)
+{
+    const float* nrm = in, * wp = in + 4, * col = in + 8;
+    float c[4];
+    memcpy(c, col, 16);
+    def_lighting(s, c, nrm, wp, bgra);
+}
+
+/* texcoordFromDirection (samplrcube.cpp:29-97): the face of the major axis
+   (ties resolved by the reference's strict comparisons) and its (s, t). */
+static int cube_face(const float* d, float* st)
+{
+    float ax = fabsf(d[0]), ay = fabsf(d[1]), az = fabsf(d[2]);
+    if (ax > ay) {
+        if (ax > az) {
+            if (d[0] > 0) { st[0] = (-d[2] / ax + 1.0f) / 2.0f; st[1] = (-d[1] / ax + 1.0f) / 2.0f; return 0; }
+            st[0] = (d[2] / ax + 1.0f) / 2.0f;
+            st[1] = (-d[1] / ax + 1.0f) / 2.0f;
+            return 1;
+        }
+    } else if (!(az > ay)) { /* Y wins; the sign test is on Z (samplrcube.cpp:83) */
+        if (d[2] > 0) { st[0] = (d[0] / ay + 1.0f) / 2.0f; st[1] = (d[2] / ay + 1.0f) / 2.0f; return 2; }
+        st[0] = (d[0] / ay + 1.0f) / 2.0f;
+        st[1] = (-d[2] / ay + 1.0f) / 2.0f;
+        return 3;
+    }
+    /* Z wins */
+    if (d[2] > 0) { st[0] = (d[0] / az + 1.0f) / 2.0f; st[1] = (-d[1] / az + 1.0f) / 2.0f; return 4; }
+    st[0] = (-d[0] / az + 1.0f) / 2.0f;
+    st[1] = (-d[1] / az + 1.0f) / 2.0f;
+    return 5;
+}
+
+/* PuresoftSamplerCube::get4 (samplrcube.cpp:119-127): row from s times the
+   height, column from t times the width (the reference passes S as the
+   row), each +0.5 and truncated as unsigned, then directRead4 of the face
+   (fbo.cpp:287-291, clampCoord fbo.cpp:552-594). */
+static void sample_cube(const o_fbo* t, const float* d, uint8_t* bgra)
+{
+    float st[2];
+    int layer = cube_face(d, st);
+    int row = (int)sr_f2u((float)t->height * st[0] + 0.5f);
+    int col = (int)sr_f2u((float)t->width * st[1] + 0.5f);
+    if (t->wrap) {
+        row = sr_wrap(row, t->height);
+        col = sr_wrap(col, t->width);
+    } else {
+        row = sr_clampi(row, t->height);
+        col = sr_clampi(col, t->width);
+    }
+    memcpy(bgra, t->buf + (size_t)t->scanline * t->height * layer + (size_t)row * t->scanline + 4 * col, 4);
+}
+
+/* FragmentProcessorDEF03::process (tex1bump1light1.cpp:180-239): the bump
+   texel's (r, g, b, 0) / 255 * 2 - 1 on four lanes, through the matrix whose
+   columns are the tangent, binormal, normal and 0 (mcemaths_make_tbn,
+   matrix.cpp:992-1008), normalised; then DEF01's lighting. */
+static void fp_def03(const fp_state* s, const float* in, uint8_t* bgra)
+{
+    const float* tan = in, * bin = in + 4, * nrm = in + 8, * wp = in + 12, * tc = in + 16;
+    float c[4], bt[4], bn[4], tbn[16], r;
+    sample_nearest(s->tex, tc, c);
+    sample_nearest(s->tex2, tc, bt);
+    bn[0] = bt[2];
+    bn[1] = bt[1];
+    bn[2] = bt[0];
+    bn[3] = 0.0f;
+    r = 1.0f / 255.0f;
+    for (int k = 0; k < 4; k++) bn[k] = bn[k] * r;
+    for (int k = 0; k < 4; k++) bn[k] = bn[k] * 2.0f;
+    for (int k = 0; k < 4; k++) bn[k] = bn[k] - 1.0f;
+    memcpy(tbn, tan, 16);
+    memcpy(tbn + 4, bin, 16);
+    memcpy(tbn + 8, nrm, 16);
+    memset(tbn + 12, 0, 16);
+    m4v4(bn, tbn, bn);
+    r = 1.0f / sqrtf((bn[0] * bn[0] + bn[1] * bn[1]) + (bn[2] * bn[2] + bn[3] * bn[3]));
+    for (int k = 0; k < 4; k++) bn[k] = bn[k] * r;
+    def_lighting(s, c, bn, wp, bgra);
 }
 
 /* Per-thread error accumulator of the FP32 vs FP64 shading comparison. */
@@ -687,6 +893,9 @@ static int run_fp(const ps3do* p, const fp_state* s, const float* in, uint8_t* b
 {
     switch (p->fp) {
     case FP_DEF01: fp_def01(s, in, bgra); return 1;
+    case FP_DEF02: fp_def02(s, in, bgra); return 1;
+    case FP_DEF03: fp_def03(s, in, bgra); return 1;
+    case FP_DEF04: sample_cube(s->cube, in, bgra); return 1; /* skybox.cpp:127-134 */
     case FP_LIT1: {
         sr_level t = level_of(s->tex);
         sr_shade_lit1(&t, s->light, s->cam, in, in + 4, in + 8, bgra);
@@ -959,8 +1168,9 @@ static void run_task(draw_ctx* d, const o_task* t, long long* tested, long long*
             if (w == 1 && !cc.overflow) {
                 uint8_t* dst = cc.rowEntry + (size_t)cc.col * 4;
                 /* FBOBridge::write4 blends under ALPHABLEND (fragthrd.cpp:70-81, fbo.cpp:208-229);
-                   DEF01 writes through FBOBridge::write, which never blends */
-                if ((behav & BEHAVIOR_ALPHABLEND) && p->fp != FP_DEF01) sr_blend4(dst, bgra);
+                   DEF01 / DEF02 / DEF03 write through FBOBridge::write, which never blends */
+                if ((behav & BEHAVIOR_ALPHABLEND) && p->fp != FP_DEF01 && p->fp != FP_DEF02 && p->fp != FP_DEF03)
+                    sr_blend4(dst, bgra);
                 else memcpy(dst, bgra, 4);
             }
             if (p->errOn) shade_error(p, &d->fs, frag, e);

@@ -26,6 +26,12 @@ ps3do* ps3do_create(int width, int height, int threads);
 void ps3do_destroy(ps3do* p);
 int ps3do_texture_create(ps3do* p, int width, int height, int scanline, int elemLen, const void* pixels, int wrap);
 int ps3do_texture_read(ps3do* p, int idx, void* out, size_t bytes);
+/* createTexture with extra layers (tex.cpp:3-25; 5 makes a cube map) and
+   the per-layer access of getTexture (tex.cpp:27-37). */
+int ps3do_texture_create_layers(ps3do* p, int width, int height, int scanline, int elemLen, const void* pixels,
+                                int wrap, int extraLayers);
+int ps3do_texture_write_layer(ps3do* p, int idx, int layer, const void* pixels, size_t bytes);
+int ps3do_texture_read_layer(ps3do* p, int idx, int layer, void* out, size_t bytes);
 int ps3do_processor_add(ps3do* p, int id);
 int ps3do_programme_create(ps3do* p, int vid, int iid, int fid);
 int ps3do_programme_use(ps3do* p, int idx);

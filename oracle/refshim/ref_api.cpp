@@ -82,6 +82,15 @@ PuresoftProcessor* make_processor(int id)
     case 0x0101: return new VertexProcesserDEF01;
     case 0x0102: return new InterpolationProcessorDEF01;
     case 0x0103: return new FragmentProcessorDEF01;
+    case 0x0201: return new VertexProcesserDEF02;
+    case 0x0202: return new InterpolationProcessorDEF02;
+    case 0x0203: return new FragmentProcessorDEF02;
+    case 0x0301: return new VertexProcesserDEF03;
+    case 0x0302: return new InterpolationProcessorDEF03;
+    case 0x0303: return new FragmentProcessorDEF03;
+    case 0x0401: return new VertexProcesserDEF04;
+    case 0x0402: return new InterpolationProcessorDEF04;
+    case 0x0403: return new FragmentProcessorDEF04;
     case 0x0501: return new VertexProcesserDEF05;
     case 0x0502: return new InterpolationProcessorDEF05;
     case 0x0503: return new FragmentProcessorDEF05;
@@ -120,7 +129,8 @@ void ps3dr_destroy(void* h)
 
 int ps3dr_thread_count(void) { return logicCPUs(); }
 
-int ps3dr_texture_create(void* h, int width, int height, int scanline, int elemLen, const void* pixels, int wrap)
+int ps3dr_texture_create_layers(void* h, int width, int height, int scanline, int elemLen, const void* pixels,
+                                int wrap, int extraLayers)
 {
     RefCtx* c = (RefCtx*)h;
     return guarded([&] {
@@ -130,20 +140,44 @@ int ps3dr_texture_create(void* h, int width, int height, int scanline, int elemL
         img.scanline = scanline;
         img.elemLen = elemLen;
         img.pixels = (void*)pixels;
-        return c->pipe->createTexture(&img, 0, wrap ? PuresoftFBO::WRAP : PuresoftFBO::CLAMP);
+        return c->pipe->createTexture(&img, extraLayers, wrap ? PuresoftFBO::WRAP : PuresoftFBO::CLAMP);
+    });
+}
+
+int ps3dr_texture_create(void* h, int width, int height, int scanline, int elemLen, const void* pixels, int wrap)
+{
+    return ps3dr_texture_create_layers(h, width, height, scanline, elemLen, pixels, wrap, 0);
+}
+
+/* getTexture(idx, image, layer) hands out the layer's own buffer (tex.cpp:27-37);
+   these copy into or out of it. */
+int ps3dr_texture_write_layer(void* h, int idx, int layer, const void* pixels, size_t bytes)
+{
+    RefCtx* c = (RefCtx*)h;
+    return guarded([&] {
+        PURESOFTIMGBUFF32 img;
+        c->pipe->getTexture(idx, &img, (PuresoftFBO::LAYER)layer);
+        size_t n = (size_t)img.scanline * img.height;
+        memcpy(img.pixels, pixels, n < bytes ? n : bytes);
+        return 0;
+    });
+}
+
+int ps3dr_texture_read_layer(void* h, int idx, int layer, void* out, size_t bytes)
+{
+    RefCtx* c = (RefCtx*)h;
+    return guarded([&] {
+        PURESOFTIMGBUFF32 img;
+        c->pipe->getTexture(idx, &img, (PuresoftFBO::LAYER)layer);
+        size_t n = (size_t)img.scanline * img.height;
+        memcpy(out, img.pixels, n < bytes ? n : bytes);
+        return 0;
     });
 }
 
 int ps3dr_texture_read(void* h, int idx, void* out, size_t bytes)
 {
-    RefCtx* c = (RefCtx*)h;
-    return guarded([&] {
-        PURESOFTIMGBUFF32 img;
-        c->pipe->getTexture(idx, &img);
-        size_t n = (size_t)img.scanline * img.height;
-        memcpy(out, img.pixels, n < bytes ? n : bytes);
-        return 0;
-    });
+    return ps3dr_texture_read_layer(h, idx, 0, out, bytes);
 }
 
 int ps3dr_processor_add(void* h, int id)

@@ -69,9 +69,12 @@ int fail(int code, const char* fmt, ...)
 // The sort's look-back descriptors hold prefixes in 30 bits.
 constexpr int kMaxPairs = (1 << 30) - kSortChunk;
 
+// A texture: `layers` images of scanline*height bytes back to back (layer 0
+// is the texture itself, 1.. its extra layers; six make a cube map with the
+// faces in the reference's LAYER order +x, -x, +y, -y, +z, -z, fbo.h:19).
 struct Texture {
     uint8_t* dev = nullptr;
-    int width = 0, height = 0, scanline = 0, elemLen = 0, wrap = 0;
+    int width = 0, height = 0, scanline = 0, elemLen = 0, wrap = 0, layers = 1;
     bool alive = false;
 };
 
@@ -272,6 +275,9 @@ int required_vary(int ip)
 {
     switch (ip) {
     case IP_DEF01: return 9;
+    case IP_DEF02: return 11;  // normal xyzw, worldPos xyz, colour xyzw
+    case IP_DEF03: return 17;
+    case IP_DEF04: return 3;   // direction xyz
     case IP_LIT2: return 16;
     default: return 0;
     }
@@ -282,6 +288,9 @@ int fp_needs(int fp)
     switch (fp) {
     case FP_DEF01: case FP_LIT1: case FP_LIT1A: case FP_LIT3: return IP_DEF01;
     case FP_LIT2: return IP_LIT2;
+    case FP_DEF02: return IP_DEF02;
+    case FP_DEF03: return IP_DEF03;
+    case FP_DEF04: return IP_DEF04;
     default: return 0;
     }
 }
@@ -291,6 +300,9 @@ int vp_gives(int vp)
     switch (vp) {
     case VP_DEF01: return IP_DEF01;
     case VP_LIT2: return IP_LIT2;
+    case VP_DEF02: return IP_DEF02;
+    case VP_DEF03: return IP_DEF03;
+    case VP_DEF04: return IP_DEF04;
     default: return 0;
     }
 }
@@ -300,6 +312,8 @@ bool known_processor(int id)
     switch (id) {
     case VP_DEF01: case IP_DEF01: case FP_DEF01: case VP_DEF05: case IP_DEF05: case FP_DEF05:
     case VP_SHADOW: case FP_LIT1: case FP_LIT1A: case FP_LIT3: case VP_LIT2: case IP_LIT2: case FP_LIT2:
+    case VP_DEF02: case IP_DEF02: case FP_DEF02: case VP_DEF03: case IP_DEF03: case FP_DEF03:
+    case VP_DEF04: case IP_DEF04: case FP_DEF04:
         return true;
     }
     return false;
@@ -357,9 +371,19 @@ int snapshot_uniforms(const ps3d_pipeline* p, DrawUniforms& U)
     };
     int rc;
     switch (p->vp) {
-    case VP_DEF01:
+    case VP_DEF01:  // tex1light1.cpp:15-20
+    case VP_DEF02:  // colr1light1.cpp:15-20
+    case VP_DEF03:  // tex1bump1light1.cpp:15-20
         if ((rc = need(3, U.PV, 16)) || (rc = need(4, U.M, 16)) || (rc = need(5, U.Mrot, 16))) return rc;
         break;
+    case VP_DEF04: {  // skybox.cpp:17-21, 34-37: the view's inverse rotation, the
+                      // transposed view matrix with its last column zeroed
+        float V[16];
+        if ((rc = need(1, V, 16))) return rc;
+        for (int c = 0; c < 4; c++)
+            for (int r = 0; r < 4; r++) U.Vrot[4 * c + r] = c < 3 ? V[4 * r + c] : 0.0f;
+        break;
+    }
     case VP_DEF05:
     case VP_SHADOW:
         if ((rc = need(3, U.PV, 16)) || (rc = need(4, U.M, 16))) return rc;
@@ -372,7 +396,23 @@ int snapshot_uniforms(const ps3d_pipeline* p, DrawUniforms& U)
         break;
     }
     switch (p->fp) {
+    case FP_DEF02:  // colr1light1.cpp:144-148
+        if ((rc = need(7, U.light, 4)) || (rc = need(8, U.cam, 4))) return rc;
+        break;
+    case FP_DEF04: {  // skybox.cpp:122-125: the cube map's index at uniform 2
+        const int* t = uint_(p, 2, 1);
+        if (!t) return fail(PS3D_ERR_INVALID, "uniform 2 (cube map index) is not set");
+        if (!tex_ok(p, *t)) return fail(PS3D_ERR_RANGE, "uniform 2: texture %d", *t);
+        const Texture& c = p->tex[*t];
+        // get4 reads a 4-byte texel from one of six layers (samplrcube.cpp:119-127)
+        if (c.elemLen != 4 || c.layers < 6)
+            return fail(PS3D_ERR_INVALID, "texture %d is not a BGRA8 cube map (6 layers)", *t);
+        U.tex = level_of(c);
+        U.layerBytes = (long long)c.scanline * c.height;
+        break;
+    }
     case FP_DEF01:
+    case FP_DEF03:
     case FP_LIT1:
     case FP_LIT1A: {
         if ((rc = need(7, U.light, 4)) || (rc = need(8, U.cam, 4))) return rc;
@@ -381,6 +421,13 @@ int snapshot_uniforms(const ps3d_pipeline* p, DrawUniforms& U)
         if (!tex_ok(p, *t)) return fail(PS3D_ERR_RANGE, "uniform 9: texture %d", *t);
         if (p->tex[*t].elemLen != 4) return fail(PS3D_ERR_INVALID, "texture %d is not BGRA8", *t);
         U.tex = level_of(p->tex[*t]);
+        if (p->fp == FP_DEF03) {  // tex1bump1light1.cpp:170-176: the bump map at 10
+            const int* b = uint_(p, 10, 1);
+            if (!b) return fail(PS3D_ERR_INVALID, "uniform 10 (bump texture index) is not set");
+            if (!tex_ok(p, *b)) return fail(PS3D_ERR_RANGE, "uniform 10: texture %d", *b);
+            if (p->tex[*b].elemLen != 4) return fail(PS3D_ERR_INVALID, "texture %d is not BGRA8", *b);
+            U.tex2 = level_of(p->tex[*b]);
+        }
         break;
     }
     case FP_LIT3:
@@ -642,6 +689,7 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     Scratch& x = p->scr[slot];
     cudaStream_t s = p->oneStream ? p->stream : p->gs[slot];
     const bool forward = pass_forward(dd.data(), dd.size());
+    if (forward) nvMax = forward_vary(nvMax);
     int binW = forward ? 16 : p->binW;  // forward passes run with 16-column bins
     int binsX = (W + binW - 1) / binW, binsY = (H + kBinH - 1) / kBinH;
     if (radix_passes(binsX * binsY) > kRadixMaxPasses) return fail(PS3D_ERR_RANGE, "target too large for the bin sort");
@@ -1012,11 +1060,14 @@ int ps3d_pipeline_destroy(ps3d_pipeline* p)
 }
 
 static int texture_create(ps3d_pipeline* p, int width, int height, int scanline, int elemLen, const void* pixels,
-                          int wrap, cudaMemcpyKind kind)
+                          int wrap, int extraLayers, cudaMemcpyKind kind)
 {
     if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
     if (elemLen != 1 && elemLen != 4) return fail(PS3D_ERR_INVALID, "elemLen must be 1 or 4 (fbo.cpp:21-24)");
     if (width <= 0 || height <= 0 || scanline < width * elemLen) return fail(PS3D_ERR_INVALID, "bad texture size");
+    // fbo.cpp:62-72 throws out_of_range above LAYER_MAX; LAYER_MAX itself
+    // would index one past the reference's layer array, so 5 is the most
+    if (extraLayers < 0 || extraLayers > 5) return fail(PS3D_ERR_RANGE, "extraLayers %d (0..5)", extraLayers);
     size_t slot = 0;
     for (; slot < p->tex.size(); slot++)
         if (!p->tex[slot].alive) break;
@@ -1027,11 +1078,18 @@ static int texture_create(ps3d_pipeline* p, int width, int height, int scanline,
     t.scanline = scanline;
     t.elemLen = elemLen;
     t.wrap = wrap ? 1 : 0;
+    t.layers = 1 + extraLayers;
     size_t bytes = (size_t)scanline * height;
-    if (cudaMalloc((void**)&t.dev, (bytes + 15) / 16 * 16) != cudaSuccess)
-        return fail(PS3D_ERR_NOMEM, "texture allocation of %zu bytes failed", bytes);
-    if (pixels) CU(cudaMemcpyAsync(t.dev, pixels, bytes, kind, p->stream));
-    else CU(cudaMemsetAsync(t.dev, 0, bytes, p->stream));
+    size_t all = bytes * t.layers;
+    if (cudaMalloc((void**)&t.dev, (all + 15) / 16 * 16) != cudaSuccess)
+        return fail(PS3D_ERR_NOMEM, "texture allocation of %zu bytes failed", all);
+    // tex.cpp:20-23: the pixels fill the default layer; extra layers start zeroed
+    if (pixels) {
+        CU(cudaMemcpyAsync(t.dev, pixels, bytes, kind, p->stream));
+        if (all > bytes) CU(cudaMemsetAsync(t.dev + bytes, 0, all - bytes, p->stream));
+    } else {
+        CU(cudaMemsetAsync(t.dev, 0, all, p->stream));
+    }
     t.alive = true;
     p->tex[slot] = t;
     return (int)slot;
@@ -1040,7 +1098,13 @@ static int texture_create(ps3d_pipeline* p, int width, int height, int scanline,
 int ps3d_texture_create(ps3d_pipeline* p, int width, int height, int scanline, int elemLen, const void* pixels,
                         int wrap)
 {
-    int rc = texture_create(p, width, height, scanline, elemLen, pixels, wrap, cudaMemcpyHostToDevice);
+    return ps3d_texture_create_layers(p, width, height, scanline, elemLen, pixels, wrap, 0);
+}
+
+int ps3d_texture_create_layers(ps3d_pipeline* p, int width, int height, int scanline, int elemLen,
+                               const void* pixels, int wrap, int extraLayers)
+{
+    int rc = texture_create(p, width, height, scanline, elemLen, pixels, wrap, extraLayers, cudaMemcpyHostToDevice);
     if (rc >= 0 && pixels && p) cudaStreamSynchronize(p->stream);  // the caller may free its pixels on return
     return rc;
 }
@@ -1048,7 +1112,35 @@ int ps3d_texture_create(ps3d_pipeline* p, int width, int height, int scanline, i
 int ps3d_texture_create_device(ps3d_pipeline* p, int width, int height, int scanline, int elemLen,
                                const void* devPixels, int wrap)
 {
-    return texture_create(p, width, height, scanline, elemLen, devPixels, wrap, cudaMemcpyDeviceToDevice);
+    return texture_create(p, width, height, scanline, elemLen, devPixels, wrap, 0, cudaMemcpyDeviceToDevice);
+}
+
+int ps3d_texture_write_layer(ps3d_pipeline* p, int idx, int layer, const void* pixels, size_t bytes)
+{
+    if (!p || !pixels) return fail(PS3D_ERR_INVALID, "null argument");
+    if (!tex_ok(p, idx)) return fail(PS3D_ERR_RANGE, "texture %d", idx);
+    const Texture& t = p->tex[idx];
+    if (layer < 0 || layer >= t.layers) return fail(PS3D_ERR_RANGE, "texture %d has no layer %d", idx, layer);
+    int rc = do_finish(p);  // passes still sampling the texture finish first
+    if (rc) return rc;
+    size_t n = std::min(bytes, (size_t)t.scanline * t.height);
+    CU(cudaMemcpyAsync(t.dev + (size_t)t.scanline * t.height * layer, pixels, n, cudaMemcpyHostToDevice, p->stream));
+    CU(cudaStreamSynchronize(p->stream));
+    return 0;
+}
+
+int ps3d_texture_read_layer(ps3d_pipeline* p, int idx, int layer, void* out, size_t bytes)
+{
+    if (!p || !out) return fail(PS3D_ERR_INVALID, "null argument");
+    if (!tex_ok(p, idx)) return fail(PS3D_ERR_RANGE, "texture %d", idx);
+    const Texture& t = p->tex[idx];
+    if (layer < 0 || layer >= t.layers) return fail(PS3D_ERR_RANGE, "texture %d has no layer %d", idx, layer);
+    int rc = do_finish(p);
+    if (rc) return rc;
+    size_t n = std::min(bytes, (size_t)t.scanline * t.height);
+    CU(cudaMemcpyAsync(out, t.dev + (size_t)t.scanline * t.height * layer, n, cudaMemcpyDeviceToHost, p->stream));
+    CU(cudaStreamSynchronize(p->stream));
+    return 0;
 }
 
 int ps3d_texture_destroy(ps3d_pipeline* p, int idx)
@@ -1067,15 +1159,7 @@ int ps3d_texture_destroy(ps3d_pipeline* p, int idx)
 
 int ps3d_texture_read(ps3d_pipeline* p, int idx, void* out, size_t bytes)
 {
-    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
-    if (!tex_ok(p, idx)) return fail(PS3D_ERR_RANGE, "texture %d", idx);
-    int rc = do_finish(p);
-    if (rc) return rc;
-    const Texture& t = p->tex[idx];
-    size_t n = std::min(bytes, (size_t)t.scanline * t.height);
-    CU(cudaMemcpyAsync(out, t.dev, n, cudaMemcpyDeviceToHost, p->stream));
-    CU(cudaStreamSynchronize(p->stream));
-    return 0;
+    return ps3d_texture_read_layer(p, idx, 0, out, bytes);
 }
 
 int ps3d_texture_device_ptr(ps3d_pipeline* p, int idx, void** out)
@@ -1350,6 +1434,8 @@ int ps3d_draw(ps3d_pipeline* p, int vao)
     int reqSlots[5] = {1, 0, 0, 0, 0};
     if (p->vp == VP_DEF01 && d.nv) reqSlots[3] = reqSlots[4] = 1;
     if (p->vp == VP_LIT2 && d.nv) reqSlots[1] = reqSlots[3] = reqSlots[4] = 1;
+    if (p->vp == VP_DEF03 && d.nv) reqSlots[1] = reqSlots[2] = reqSlots[3] = reqSlots[4] = 1;
+    if (p->vp == VP_DEF02 && d.nv) reqSlots[1] = reqSlots[2] = 1;
     for (int s = 0; s < kVboSlots; s++) {
         if (reqSlots[s] && !va.vbo[s]) return fail(PS3D_ERR_INVALID, "the vertex processor reads VBO slot %d", s);
         if (va.vbo[s]) {
@@ -1839,6 +1925,7 @@ int noalloc_shape(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass
         s.forward |= pass_forward(&d, 1);
     }
     if (s.nTris == 0) return 0;
+    if (s.forward) s.nvMax = forward_vary(s.nvMax);
     s.binW = s.forward ? 16 : p->binW;
     s.binsX = (s.tg.w + s.binW - 1) / s.binW;
     s.binsY = (s.tg.h + kBinH - 1) / kBinH;

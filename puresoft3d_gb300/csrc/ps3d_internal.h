@@ -8,7 +8,12 @@
 namespace ps3d {
 
 constexpr int kMaxLevels = 16;
-constexpr int kMaxVary = 16;     // varying floats per vertex (LIT2: 16)
+constexpr int kMaxVary = 17;   // varying floats per vertex (DEF03: tangent, binormal, normal xyzw, worldPos xyz, uv)
+// Varyings per vertex of the forward raster variant that serves a pass
+// whose draws carry at most nv (the variants are compiled for 9 and 17); a
+// forward pass lays its varyings out with this stride, so that the variant's
+// reads stay inside each vertex's record.
+constexpr int forward_vary(int nv) { return nv <= 9 ? 9 : kMaxVary; }
 constexpr int kVboSlots = 5;     // VBO slots the built-in vertex stages read (0..4)
 constexpr int kBinH = 32;        // bin height in rows: one warp lane per row
 constexpr int kMaxBinW = 32;
@@ -16,11 +21,17 @@ constexpr int kMaxBinW = 32;
 // processor ids (include/ps3d.h)
 enum : int {
     VP_DEF01 = 0x0101, IP_DEF01 = 0x0102, FP_DEF01 = 0x0103,
+    VP_DEF02 = 0x0201, IP_DEF02 = 0x0202, FP_DEF02 = 0x0203,
+    VP_DEF03 = 0x0301, IP_DEF03 = 0x0302, FP_DEF03 = 0x0303,
+    VP_DEF04 = 0x0401, IP_DEF04 = 0x0402, FP_DEF04 = 0x0403,
     VP_DEF05 = 0x0501, IP_DEF05 = 0x0502, FP_DEF05 = 0x0503,
     VP_SHADOW = 0x0601,
     FP_LIT1 = 0x1103, FP_LIT1A = 0x1403, FP_LIT3 = 0x1303,
     VP_LIT2 = 0x1201, IP_LIT2 = 0x1202, FP_LIT2 = 0x1203,
 };
+
+// built-in post-processors (include/ps3d.h)
+enum : int { PP_ADD8 = 0x7001, PP_FOG = 0x7002 };
 
 // behaviour bits (reference pipeline.h:16-19) and per-draw flags
 enum : int {
@@ -40,7 +51,10 @@ struct TexLevel {
 struct DrawUniforms {
     float PV[16], M[16], Mrot[16], LPV[16], PVM[16];
     float light[4], cam[4], params[4];
-    TexLevel tex;                   // DEF01 / LIT1 texture
+    float Vrot[16];                 // DEF04: transposed view matrix, last column zeroed
+    TexLevel tex;                   // DEF01 / DEF03 / LIT1 texture; DEF04 cube map face 0
+    long long layerBytes;           // DEF04: bytes from one cube face to the next
+    TexLevel tex2;                  // DEF03 bump map
     TexLevel albedo[kMaxLevels];    // LIT2 / LIT3 albedo chain
     TexLevel normal[kMaxLevels];    // LIT2 normal-map chain (RGBA16F)
     int albedoLevels, normalLevels;
@@ -134,7 +148,7 @@ constexpr int kRadixHdr = 1024;     // ints before the descriptors (counts + tic
 constexpr int kTicketSetup = kRadixMaxPasses * kRadixDigits + kRadixMaxPasses;  // after the sort's tickets
 
 // Kernel families timed by the profiler (ps3d_profile_*).
-enum KernelId { K_SETUP, K_SCAN, K_EMIT, K_BOUNDS, K_SORT, K_RASTER, K_SHADE, K_FILL, K_COUNT };
+enum KernelId { K_SETUP, K_SCAN, K_EMIT, K_BOUNDS, K_SORT, K_RASTER, K_SHADE, K_FILL, K_POST, K_COUNT };
 
 // CUDA-event brackets around kernel launches, on the launching stream.
 struct Prof {

@@ -128,9 +128,22 @@ __device__ __forceinline__ int shade_fragment(const DrawDesc& d, const DrawUnifo
     case FP_LIT1A: return shade_lit1a(U, in, bgra) ? 1 : 2;
     case FP_LIT3: bgra = shade_lit3(U, in); return 1;
     case FP_DEF01: bgra = shade_def01(U, in); return 1;
+    case FP_DEF04: bgra = shade_def04(U, in); return 1;
+    case FP_DEF02:
+        if constexpr (NV >= 11) {
+            bgra = shade_def02(U, in);
+            return 1;
+        }
+        return 0;
     case FP_LIT2:
         if constexpr (NV >= 16) {
             bgra = shade_lit2(U, in);
+            return 1;
+        }
+        return 0;
+    case FP_DEF03:
+        if constexpr (NV >= 17) {
+            bgra = shade_def03(U, in);
             return 1;
         }
         return 0;
@@ -375,9 +388,12 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
                                 }
                                 if (w == 1) {
                                     uint32_t* cp = sCol + lane * S + x;
-                                    // FBOBridge::write4 blends under ALPHABLEND; DEF01 writes
-                                    // through FBOBridge::write, which never blends
-                                    *cp = ((flags & B_ALPHABLEND) && dd.fp != FP_DEF01) ? blend4(*cp, bgra) : bgra;
+                                    // FBOBridge::write4 blends under ALPHABLEND; DEF01 / DEF02 /
+                                    // DEF03 write through FBOBridge::write, which never blends
+                                    *cp = ((flags & B_ALPHABLEND) && dd.fp != FP_DEF01 && dd.fp != FP_DEF02 &&
+                                           dd.fp != FP_DEF03)
+                                              ? blend4(*cp, bgra)
+                                              : bgra;
                                 }
                                 if (w != 2 && (flags & B_UPDATE_DEPTH)) dRow[x] = zz;
                             }
@@ -497,6 +513,12 @@ __device__ __forceinline__ void shade_entry(const PassParams& P, int2 e)
     const float* vary = P.vary + (size_t)w * 3 * P.nvMax;
     uint32_t bgra;
     switch (FPK ? FPK : d.fp) {
+    case FP_DEF03: {
+        float in[17];
+        fragment_varyings<17>(t, vary, P.nvMax, s, z, xl, in);
+        bgra = shade_def03(U, in);
+        break;
+    }
     case FP_LIT2: {
         float in[16];
         fragment_varyings<16>(t, vary, P.nvMax, s, z, xl, in);
@@ -507,6 +529,18 @@ __device__ __forceinline__ void shade_entry(const PassParams& P, int2 e)
         float in[9];
         fragment_varyings<9>(t, vary, P.nvMax, s, z, xl, in);
         bgra = shade_lit1(U, in);
+        break;
+    }
+    case FP_DEF02: {
+        float in[11];
+        fragment_varyings<11>(t, vary, P.nvMax, s, z, xl, in);
+        bgra = shade_def02(U, in);
+        break;
+    }
+    case FP_DEF04: {
+        float in[3];
+        fragment_varyings<3>(t, vary, P.nvMax, s, z, xl, in);
+        bgra = shade_def04(U, in);
         break;
     }
     case FP_LIT3: {
@@ -556,8 +590,9 @@ template <int BW> void launch_raster(const PassParams& P, int nBins, cudaStream_
 // Forward passes (blending or discarding draws) run with 16-column bins.
 void launch_raster_forward(const PassParams& P, int nBins, cudaStream_t s)
 {
-    if (P.nvMax <= 9) k_raster<16, 1, 9><<<nBins, kRasterThreads, 0, s>>>(P);
-    else k_raster<16, 1, 16><<<nBins, kRasterThreads, 0, s>>>(P);
+    // the host lays a forward pass's varyings out with stride forward_vary()
+    if (P.nvMax == forward_vary(9)) k_raster<16, 1, 9><<<nBins, kRasterThreads, 0, s>>>(P);
+    else k_raster<16, 1, kMaxVary><<<nBins, kRasterThreads, 0, s>>>(P);
 }
 
 void launch_raster(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
@@ -587,6 +622,9 @@ void launch_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
     case FP_LIT2: kern = k_shade<FP_LIT2>; break;
     case FP_LIT3: kern = k_shade<FP_LIT3>; break;
     case FP_DEF01: kern = k_shade<FP_DEF01>; break;
+    case FP_DEF03: kern = k_shade<FP_DEF03>; break;
+    case FP_DEF02: kern = k_shade<FP_DEF02>; break;
+    case FP_DEF04: kern = k_shade<FP_DEF04>; break;
     default: break;
     }
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, 256, 0);

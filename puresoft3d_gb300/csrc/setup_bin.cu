@@ -51,6 +51,52 @@ __device__ __forceinline__ void run_vp(const DrawDesc& d, const DrawUniforms& U,
         }
         break;
     }
+    case VP_DEF02: {  // colr1light1.cpp:22-40: normal in VBO 1, colour in VBO 2
+        float wp[4], n[4], nrm[4], c[4];
+        m4v4(wp, U.M, p);
+        m4v4(pos, U.PV, wp);
+        if (d.nv) {
+            ld4(d.vbo[1] + (size_t)idx * d.stride[1], n);
+            ld4(d.vbo[2] + (size_t)idx * d.stride[2], c);
+            m4v4(nrm, U.Mrot, n);
+            vary[0] = nrm[0]; vary[1] = nrm[1]; vary[2] = nrm[2]; vary[3] = nrm[3];
+            vary[4] = wp[0]; vary[5] = wp[1]; vary[6] = wp[2];
+            vary[7] = c[0]; vary[8] = c[1]; vary[9] = c[2]; vary[10] = c[3];
+        }
+        break;
+    }
+    case VP_DEF04: {  // skybox.cpp:23-44: the position passes through; the
+                      // direction is Vrot times the normalised vector from
+                      // the observer (0, 0, 1) to the vertex
+        pos[0] = p[0]; pos[1] = p[1]; pos[2] = p[2]; pos[3] = p[3];
+        if (d.nv) {
+            float v[4] = {fsub(p[0], 0.0f), fsub(p[1], 0.0f), fsub(p[2], 1.0f), 0.0f}, dir[4];
+            float r = fdiv(1.0f, fsqrt(fadd(fadd(fmul(v[0], v[0]), fmul(v[1], v[1])),
+                                           fadd(fmul(v[2], v[2]), fmul(v[3], v[3])))));
+#pragma unroll
+            for (int k = 0; k < 4; k++) v[k] = fmul(v[k], r);
+            m4v4(dir, U.Vrot, v);
+            vary[0] = dir[0]; vary[1] = dir[1]; vary[2] = dir[2];
+        }
+        break;
+    }
+    case VP_DEF03: {  // tex1bump1light1.cpp:22-46
+        float wp[4], v[4], o[4];
+        m4v4(wp, U.M, p);
+        m4v4(pos, U.PV, wp);
+        if (d.nv) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) {  // tangent, binormal, normal: Mrot on all four lanes
+                ld4(d.vbo[1 + k] + (size_t)idx * d.stride[1 + k], v);
+                m4v4(o, U.Mrot, v);
+                vary[4 * k] = o[0]; vary[4 * k + 1] = o[1]; vary[4 * k + 2] = o[2]; vary[4 * k + 3] = o[3];
+            }
+            const float* uv = (const float*)(d.vbo[4] + (size_t)idx * d.stride[4]);
+            vary[12] = wp[0]; vary[13] = wp[1]; vary[14] = wp[2];
+            vary[15] = __ldg(uv); vary[16] = __ldg(uv + 1);
+        }
+        break;
+    }
     case VP_DEF05: {  // shadow.cpp:21-29: positions x0.9 (mcemaths_mul_3), then (PV*M) * p
         float a[4] = {fmul(p[0], 0.9f), fmul(p[1], 0.9f), fmul(p[2], 0.9f), p[3]};
         m4v4(pos, U.PVM, a);
@@ -128,12 +174,28 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float
     for (int v = 0; v < 3; v++) {
         float vary[kMaxVary];
         run_vp(d, U, 3 * lt + v, pos[v], vary);
-        if (d.nv == 9) {
+        // constant trip counts keep `vary` in registers
+        switch (d.nv) {
+        case 3:
+#pragma unroll
+            for (int k = 0; k < 3; k++) vout[v * P.nvMax + k] = vary[k];
+            break;
+        case 9:
 #pragma unroll
             for (int k = 0; k < 9; k++) vout[v * P.nvMax + k] = vary[k];
-        } else if (d.nv == 16) {
+            break;
+        case 11:
+#pragma unroll
+            for (int k = 0; k < 11; k++) vout[v * P.nvMax + k] = vary[k];
+            break;
+        case 16:
 #pragma unroll
             for (int k = 0; k < 16; k++) vout[v * P.nvMax + k] = vary[k];
+            break;
+        case 17:
+#pragma unroll
+            for (int k = 0; k < 17; k++) vout[v * P.nvMax + k] = vary[k];
+            break;
         }
         float r = frcp(pos[v][3]);  // vertthrd.cpp:37-47: 1/w, then a 4-wide multiply
 #pragma unroll

@@ -33,6 +33,9 @@ _SIGS = {
     "ps3d_texture_create_device": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p, _c_int],
     "ps3d_texture_destroy": [_c_void_p, _c_int],
     "ps3d_texture_read": [_c_void_p, _c_int, _c_void_p, _c_size_t],
+    "ps3d_texture_create_layers": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p, _c_int, _c_int],
+    "ps3d_texture_write_layer": [_c_void_p, _c_int, _c_int, _c_void_p, _c_size_t],
+    "ps3d_texture_read_layer": [_c_void_p, _c_int, _c_int, _c_void_p, _c_size_t],
     "ps3d_texture_device_ptr": [_c_void_p, _c_int, ctypes.POINTER(_c_void_p)],
     "ps3d_processor_add": [_c_void_p, _c_int],
     "ps3d_processor_destroy": [_c_void_p, _c_int],
@@ -82,7 +85,7 @@ _SIGS = {
     "ps3d_profile_read": [_c_void_p, ctypes.POINTER(_c_int), ctypes.POINTER(ctypes.c_double)],
 }
 
-KERNELS = ["setup", "scan", "emit", "bounds", "sort", "raster", "shade", "fill"]
+KERNELS = ["setup", "scan", "emit", "bounds", "sort", "raster", "shade", "fill", "post"]
 
 
 def library(path: str | None = None) -> ctypes.CDLL:
@@ -148,25 +151,34 @@ class PuresoftPipeline:
             pass
 
     # -- textures
-    def createTexture(self, width, height, scanline, elem_len, pixels=None, wrap=0) -> int:
+    def createTexture(self, width, height, scanline, elem_len, pixels=None, wrap=0, extra_layers=0) -> int:
+        """createTexture(image, extraLayers, mode); `pixels` fills layer 0
+        (five extra layers make a cube map, faces +x, -x, +y, -y, +z, -z)."""
         ptr = None
         if pixels is not None:
             pixels = np.ascontiguousarray(pixels)
             if pixels.nbytes != scanline * height:
                 raise ValueError("pixel buffer is %d bytes, expected %d" % (pixels.nbytes, scanline * height))
             ptr = pixels.ctypes.data
-        idx = self._check(self.lib.ps3d_texture_create(self.h, width, height, scanline, elem_len, ptr, int(wrap)))
+        idx = self._check(self.lib.ps3d_texture_create_layers(self.h, width, height, scanline, elem_len, ptr,
+                                                              int(wrap), int(extra_layers)))
         self._tex[idx] = (width, height, scanline, elem_len)
         return idx
+
+    def writeTextureLayer(self, idx, layer, pixels):
+        """Fills one layer (getTexture(idx, image, layer), then writing
+        image.pixels, in the reference)."""
+        pixels = np.ascontiguousarray(pixels)
+        self._check(self.lib.ps3d_texture_write_layer(self.h, idx, layer, pixels.ctypes.data, pixels.nbytes))
 
     def destroyTexture(self, idx):
         self._check(self.lib.ps3d_texture_destroy(self.h, idx))
         self._tex.pop(idx, None)
 
-    def readTexture(self, idx) -> np.ndarray:
+    def readTexture(self, idx, layer=0) -> np.ndarray:
         w, h, scan, elem = self._tex[idx]
         out = np.empty((h, scan), dtype=np.uint8)
-        self._check(self.lib.ps3d_texture_read(self.h, idx, out.ctypes.data, out.nbytes))
+        self._check(self.lib.ps3d_texture_read_layer(self.h, idx, layer, out.ctypes.data, out.nbytes))
         return out
 
     def readDepthTexture(self, idx) -> np.ndarray:

@@ -36,6 +36,9 @@ import numpy as np
 
 # processor ids (include/ps3d.h)
 VP_DEF01, IP_DEF01, FP_DEF01 = 0x0101, 0x0102, 0x0103
+VP_DEF02, IP_DEF02, FP_DEF02 = 0x0201, 0x0202, 0x0203
+VP_DEF03, IP_DEF03, FP_DEF03 = 0x0301, 0x0302, 0x0303
+VP_DEF04, IP_DEF04, FP_DEF04 = 0x0401, 0x0402, 0x0403
 VP_DEF05, IP_DEF05, FP_DEF05 = 0x0501, 0x0502, 0x0503
 VP_SHADOW = 0x0601
 FP_LIT1, FP_LIT1A, FP_LIT3 = 0x1103, 0x1403, 0x1303
@@ -356,6 +359,17 @@ class _Builder:
         self.ntex += 1
         return self.ntex - 1
 
+    def layered_texture(self, layers: List[np.ndarray], wrap: bool = False) -> int:
+        """A texture with extra layers (six BGRA faces in +x, -x, +y, -y, +z,
+        -z order make a cube map): the first image is the texture itself,
+        the others its extra layers."""
+        layers = [np.ascontiguousarray(a) for a in layers]
+        h = layers[0].shape[0]
+        row_bytes = layers[0].nbytes // h
+        self.setup.append(("createTextureLayers", row_bytes // 4, h, row_bytes, 4, layers, int(wrap)))
+        self.ntex += 1
+        return self.ntex - 1
+
     def empty_texture(self, width: int, height: int, elem_len: int = 4, wrap: bool = False) -> int:
         """A zeroed texture; for depth targets the scanline is rounded up to
         whole 16-byte vectors as the reference's default depth buffer does
@@ -386,8 +400,13 @@ class _Builder:
         return self.nprog - 1
 
     def vao(self, mesh: Dict[str, np.ndarray], slots=(0, 1, 3, 4)) -> int:
-        names = {0: "position", 1: "tangent", 3: "normal", 4: "uv"}
-        vbos = {s: np.ascontiguousarray(mesh[names[s]]) for s in slots}
+        """VBO slots from mesh arrays: `slots` lists slots of the default
+        layout (0 position, 1 tangent, 2 binormal, 3 normal, 4 uv) or maps
+        slot -> array name."""
+        names = {0: "position", 1: "tangent", 2: "binormal", 3: "normal", 4: "uv"}
+        if not isinstance(slots, dict):
+            slots = {s: names[s] for s in slots}
+        vbos = {s: np.ascontiguousarray(mesh[n]) for s, n in slots.items()}
         self.setup.append(("vao", vbos))
         self.nvao += 1
         return self.nvao - 1
@@ -727,6 +746,12 @@ def replay_setup(scene: Scene, pipe) -> Dict[str, List[int]]:
         if kind == "createTexture":
             _, w, h, scan, elem, pixels, wrap = op
             got["texture"].append(pipe.createTexture(w, h, scan, elem, pixels, wrap))
+        elif kind == "createTextureLayers":
+            _, w, h, scan, elem, layers, wrap = op
+            idx = pipe.createTexture(w, h, scan, elem, layers[0], wrap, extra_layers=len(layers) - 1)
+            for k in range(1, len(layers)):
+                pipe.writeTextureLayer(idx, k, layers[k])
+            got["texture"].append(idx)
         elif kind == "programme":
             _, vp, ip, fp = op
             got["programme"].append(pipe.createProgramme(pipe.addProcessor(vp), pipe.addProcessor(ip),

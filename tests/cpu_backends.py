@@ -26,6 +26,10 @@ REF_SRC = "/root/reference/src/puresoft3d"
 _API = [
     ("texture_create", [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]),
     ("texture_read", [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]),
+    ("texture_create_layers", [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                               ctypes.c_int]),
+    ("texture_write_layer", [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]),
+    ("texture_read_layer", [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]),
     ("processor_add", [ctypes.c_int]),
     ("programme_create", [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     ("programme_use", [ctypes.c_int]),
@@ -77,19 +81,23 @@ class _CPipeline:
             raise {-1: IndexError, -2: ValueError, -3: MemoryError}.get(rc, RuntimeError)(f"{name}: {rc}")
         return rc
 
-    def createTexture(self, width, height, scanline, elem_len, pixels, wrap):
+    def createTexture(self, width, height, scanline, elem_len, pixels, wrap, extra_layers=0):
         if pixels is not None:
             pixels = np.ascontiguousarray(pixels)
             assert pixels.nbytes == scanline * height
-        idx = self._call("texture_create", width, height, scanline, elem_len,
-                         None if pixels is None else pixels.ctypes.data, int(wrap))
+        idx = self._call("texture_create_layers", width, height, scanline, elem_len,
+                         None if pixels is None else pixels.ctypes.data, int(wrap), int(extra_layers))
         self._tex[idx] = (width, height, scanline, elem_len)
         return idx
 
-    def readTexture(self, idx) -> np.ndarray:
+    def writeTextureLayer(self, idx, layer, pixels):
+        pixels = np.ascontiguousarray(pixels)
+        self._call("texture_write_layer", idx, layer, pixels.ctypes.data, pixels.nbytes)
+
+    def readTexture(self, idx, layer=0) -> np.ndarray:
         w, h, scan, elem = self._tex[idx]
         out = np.empty((h, scan), dtype=np.uint8)
-        self._call("texture_read", idx, out.ctypes.data, out.nbytes)
+        self._call("texture_read_layer", idx, layer, out.ctypes.data, out.nbytes)
         return out
 
     def addProcessor(self, pid):

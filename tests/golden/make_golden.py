@@ -10,7 +10,8 @@ Each fixture records
   * ``covered``    -- pixels whose depth is below the clear value.
 
 Run from the repository root on an x86-64 host with the reference tree:
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case name ...]
+(no names: every case).
 """
 from __future__ import annotations
 
@@ -40,6 +41,10 @@ def scene_digest(scene) -> str:
                 for k in sorted(item):
                     h.update(str(k).encode())
                     h.update(np.ascontiguousarray(item[k]).tobytes())
+            elif isinstance(item, list):  # the layers of a layered texture
+                for a in item:
+                    h.update(str(a.dtype).encode() + str(a.shape).encode())
+                    h.update(np.ascontiguousarray(a).tobytes())
             else:
                 h.update(repr(item).encode())
     return h.hexdigest()
@@ -73,7 +78,10 @@ def main():
     from cpu_backends import RefPipeline, ref_available
     if not ref_available():
         raise SystemExit("the reference sources are needed to make golden fixtures")
+    only = set(sys.argv[1:])
     for name, scene in golden_cases():
+        if only and name not in only:
+            continue
         out = render(RefPipeline, scene)
         rec = {"digest": scene_digest(scene), "colour_sha": sha(out["colour"]), "depth_sha": sha(out["depth"]),
                "covered": int((out["depth"] < 1.0).sum())}

@@ -24,7 +24,13 @@ def _tri_mesh(clip):
     idx = np.arange(n)
     normal = np.stack([np.sin(idx * 0.7), np.cos(idx * 0.3), np.ones(n) * 0.5, np.zeros(n)], 1).astype(np.float32)
     uv = np.stack([(idx % 7) / 3.0 - 0.5, (idx % 5) / 2.0 - 0.25], 1).astype(np.float32)
-    return {"position": clip, "normal": normal, "uv": uv, "tangent": np.tile([1, 0, 0, 1], (n, 1)).astype(np.float32)}
+    tangent = np.stack([np.ones(n), np.sin(idx * 0.2) * 0.3, np.zeros(n), np.zeros(n)], 1).astype(np.float32)
+    binormal = np.stack([np.cos(idx * 0.5) * 0.2, np.ones(n), np.sin(idx * 0.4) * 0.2, np.zeros(n)], 1).astype(np.float32)
+    # vertex colour (B, G, R, A floats), partly outside 0..255 so that the clamp works
+    colour = np.stack([(idx * 37) % 300 - 20, (idx * 53) % 256, (idx * 71) % 280, (idx * 13) % 256],
+                      1).astype(np.float32)
+    return {"position": clip, "normal": normal, "uv": uv, "tangent": tangent, "binormal": binormal,
+            "colour": colour}
 
 
 def _alpha_texture(seed):
@@ -38,16 +44,37 @@ def _alpha_texture(seed):
     return img
 
 
+def _bump_texture(seed):
+    """A 16x16 BGRA tangent-space bump map: r, g around 128, b near 255."""
+    rng = np.random.default_rng(seed)
+    img = np.empty((16, 16, 4), dtype=np.uint8)
+    img[..., 2] = rng.integers(70, 186, size=(16, 16))   # r -> x
+    img[..., 1] = rng.integers(70, 186, size=(16, 16))   # g -> y
+    img[..., 0] = rng.integers(200, 256, size=(16, 16))  # b -> z
+    img[..., 3] = 255
+    return img
+
+
 def _scene(name, w, h, clip, lit=True, behavior_off=0, texture_seed=7, fp=None, behavior_on=0):
     b = S._Builder()
     rng = np.random.default_rng(texture_seed)
     tex = b.texture(_alpha_texture(texture_seed) if (fp == S.FP_LIT1A or behavior_on & S.ALPHABLEND)
                     else S.checker_noise_bgra(16, 4, rng))
     depth = b.empty_texture(w, h)
-    prog = b.programme(S.VP_DEF01, S.IP_DEF01, fp or S.FP_LIT1) if lit else b.programme(S.VP_SHADOW, S.IP_DEF05,
-                                                                                        S.FP_DEF05)
     mesh = _tri_mesh(clip)
-    vao = b.vao(mesh, slots=(0, 3, 4) if lit else (0,))
+    if fp == S.FP_DEF03:  # the reference's bump-mapped processors (tex1bump1light1.cpp)
+        bump = b.texture(_bump_texture(texture_seed + 1))
+        prog = b.programme(S.VP_DEF03, S.IP_DEF03, S.FP_DEF03)
+        vao = b.vao(mesh, slots=(0, 1, 2, 3, 4))
+    elif fp == S.FP_DEF02:  # the reference's vertex-colour processors (colr1light1.cpp)
+        prog = b.programme(S.VP_DEF02, S.IP_DEF02, S.FP_DEF02)
+        vao = b.vao(mesh, slots={0: "position", 1: "normal", 2: "colour"})
+    elif lit:
+        prog = b.programme(S.VP_DEF01, S.IP_DEF01, fp or S.FP_LIT1)
+        vao = b.vao(mesh, slots=(0, 3, 4))
+    else:
+        prog = b.programme(S.VP_SHADOW, S.IP_DEF05, S.FP_DEF05)
+        vao = b.vao(mesh, slots=(0,))
     eye = np.eye(4)
     b.f("setDepth", depth)
     b.f("clearDepth", 1.0)
@@ -63,8 +90,81 @@ def _scene(name, w, h, clip, lit=True, behavior_off=0, texture_seed=7, fp=None, 
     b.f("setUniform", 7, S.vec4(0.3, 0.5, 0.81))
     b.f("setUniform", 8, S.vec4(0, 0, 2, 1))
     b.f("setUniform", 9, np.array([tex], dtype=np.int32))
+    if fp == S.FP_DEF03:
+        b.f("setUniform", 10, np.array([bump], dtype=np.int32))
     b.f("drawVAO", vao)
     return S.Scene(name, w, h, b.setup, b.frame, {"triangles": len(mesh["position"]) // 3, "depth_texture": depth})
+
+
+def _cube_faces(size, seed):
+    """Six size x size BGRA faces: a per-face base colour, a 4-texel
+    checker and seeded noise, alpha varying, so that every face and texel
+    is told apart."""
+    rng = np.random.default_rng(seed)
+    yy, xx = np.mgrid[0:size, 0:size]
+    faces = []
+    for f in range(6):
+        img = np.empty((size, size, 4), dtype=np.uint8)
+        base = np.array([40 * f + 20, 255 - 35 * f, (97 * f) % 256], dtype=np.int32)
+        chk = ((yy // 4 + xx // 4) % 2) * 50
+        for c in range(3):
+            img[..., c] = np.clip(base[c] + chk + rng.integers(-12, 13, size=(size, size)), 0, 255)
+        img[..., 3] = np.clip(60 + 3 * xx + 2 * yy + 10 * f, 0, 255)
+        faces.append(img)
+    return faces
+
+
+def _rot(yaw, pitch, roll=0.0):
+    cy, sy, cp, sp, cr, sr = (np.cos(yaw), np.sin(yaw), np.cos(pitch), np.sin(pitch), np.cos(roll), np.sin(roll))
+    ry = np.array([[cy, 0, sy, 0], [0, 1, 0, 0], [-sy, 0, cy, 0], [0, 0, 0, 1]])
+    rx = np.array([[1, 0, 0, 0], [0, cp, -sp, 0], [0, sp, cp, 0], [0, 0, 0, 1]])
+    rz = np.array([[cr, -sr, 0, 0], [sr, cr, 0, 0], [0, 0, 1, 0], [0, 0, 0, 1]])
+    v = rz @ rx @ ry
+    v[:3, 3] = [0.3, -0.2, 1.5]  # a translation, which the skybox's rotation drops
+    return v
+
+
+def _skybox_scene(name, w, h, view, face_size, wrap, soup_seed=None, blend=False):
+    """The reference's skybox (skybox.cpp; the demo's Skybox::draw,
+    test/testobjs.cpp:162-224): a full-view quad of two triangles in clip
+    space, depth test and update off, the cube map at uniform 2 and the view
+    at uniform 1; then, optionally, a DEF01 soup over it with depth on."""
+    b = S._Builder()
+    cube = b.layered_texture(_cube_faces(face_size, 5 + face_size), wrap=wrap)
+    depth = b.empty_texture(w, h)
+    quad = np.array([[-1, 1, 0, 1], [-1, -1, 0, 1], [1, -1, 0, 1],
+                     [1, -1, 0, 1], [1, 1, 0, 1], [-1, 1, 0, 1]], dtype=np.float32)
+    sky = b.programme(S.VP_DEF04, S.IP_DEF04, S.FP_DEF04)
+    sky_vao = b.vao({"position": quad}, slots=(0,))
+    b.f("setDepth", depth)
+    b.f("clearDepth", 1.0)
+    b.f("clearColour", 0x80101010)
+    if blend:
+        b.f("enable", S.ALPHABLEND)
+    b.f("useProgramme", sky)
+    b.f("setUniform", 1, S.col_major(view))
+    b.f("setUniform", 2, np.array([cube], dtype=np.int32))
+    b.f("disable", S.UPDATE_DEPTH | S.TEST_DEPTH)
+    b.f("drawVAO", sky_vao)
+    b.f("enable", S.UPDATE_DEPTH | S.TEST_DEPTH)
+    tris = 2
+    if soup_seed is not None:
+        rng = np.random.default_rng(soup_seed)
+        tex = b.texture(S.checker_noise_bgra(16, 4, rng))
+        mesh = _tri_mesh(random_soup(150, soup_seed))
+        prog = b.programme(S.VP_DEF01, S.IP_DEF01, S.FP_DEF01)
+        vao = b.vao(mesh, slots=(0, 3, 4))
+        eye = np.eye(4)
+        b.f("useProgramme", prog)
+        b.f("setUniform", 3, S.col_major(eye))
+        b.f("setUniform", 4, S.col_major(eye))
+        b.f("setUniform", 5, S.col_major(eye))
+        b.f("setUniform", 7, S.vec4(0.3, 0.5, 0.81))
+        b.f("setUniform", 8, S.vec4(0, 0, 2, 1))
+        b.f("setUniform", 9, np.array([tex], dtype=np.int32))
+        b.f("drawVAO", vao)
+        tris += len(mesh["position"]) // 3
+    return S.Scene(name, w, h, b.setup, b.frame, {"triangles": tris, "depth_texture": depth})
 
 
 def _v(x, y, z=0.0, w=1.0):
@@ -138,4 +238,17 @@ def kat_scenes():
                        behavior_on=S.ALPHABLEND, behavior_off=S.FACE_CULLING)))
     out.append(("kat_blend_notest_64x48", _scene("kat_blend_notest", 64, 48, random_soup(120, 17),
                                                  behavior_on=S.ALPHABLEND, behavior_off=S.TEST_DEPTH)))
+    # the reference's own textured processors (x86 rcpps / rsqrtss inside: the
+    # oracle's IEEE restatement matches their depth exactly, colour closely)
+    out.append(("kat_def01_soup_96x64", _scene("kat_def01_soup", 96, 64, random_soup(300, 18), fp=S.FP_DEF01)))
+    out.append(("kat_def03_soup_96x64", _scene("kat_def03_soup", 96, 64, random_soup(300, 19), fp=S.FP_DEF03)))
+    out.append(("kat_def02_soup_96x64", _scene("kat_def02_soup", 96, 64, random_soup(300, 20), fp=S.FP_DEF02)))
+    # the skybox's cube-map sampler (samplrcube.cpp): views that put the
+    # major axis on each face, face edges and the Y faces' sign rule on Z
+    out.append(("kat_def04_sky_soup_96x64", _skybox_scene("kat_def04_sky_soup", 96, 64, _rot(0.7, 0.4), 24, False,
+                                                         soup_seed=21)))
+    out.append(("kat_def04_sky_up_wrap_80x80", _skybox_scene("kat_def04_sky_up_wrap", 80, 80, _rot(2.1, -1.2, 0.3),
+                                                            17, True)))
+    out.append(("kat_def04_sky_down_blend_72x56", _skybox_scene("kat_def04_sky_down_blend", 72, 56,
+                                                               _rot(-2.6, 1.05, -0.5), 32, False, blend=True)))
     return out

@@ -168,3 +168,36 @@ def test_device_wait_runs_out_and_pipeline_recovers(gpu_lib):
     ref = render(OraclePipeline(scene.width, scene.height), scene)
     assert_depth_exact(out["depth"], ref["depth"], name)
     assert colour_diff(out["colour"], ref["colour"])[0] <= COLOUR_TOL
+
+
+@pytest.mark.gpu
+def test_layered_texture_gpu(gpu_lib):
+    """Layered textures on the device: per-layer write and read back, zeroed
+    extra layers, out-of-range layers and layer counts refused, and a
+    skybox draw refused when its texture is not a six-layer cube map."""
+    from puresoft3d_gb300 import scenes as S
+    from puresoft3d_gb300.pipeline import PuresoftPipeline
+    p = PuresoftPipeline(16, 16)
+    face = np.arange(6 * 5 * 4, dtype=np.uint8).reshape(6, 5, 4)
+    idx = p.createTexture(5, 6, 20, 4, face, 0, extra_layers=5)
+    assert np.array_equal(p.readTexture(idx, 0), face.reshape(6, 20))
+    assert not p.readTexture(idx, 3).any()
+    p.writeTextureLayer(idx, 3, face[::-1])
+    assert np.array_equal(p.readTexture(idx, 3), face[::-1].reshape(6, 20))
+    with pytest.raises(IndexError):
+        p.readTexture(idx, 6)
+    with pytest.raises(IndexError):
+        p.createTexture(5, 6, 20, 4, face, 0, extra_layers=6)
+    flat = p.createTexture(5, 6, 20, 4, face, 0)
+    prog = p.createProgramme(p.addProcessor(S.VP_DEF04), p.addProcessor(S.IP_DEF04), p.addProcessor(S.FP_DEF04))
+    p.useProgramme(prog)
+    vao = p.createVAO()
+    p.attachVBO(vao, 0, np.array([[-1, 1, 0, 1], [-1, -1, 0, 1], [1, -1, 0, 1]], dtype=np.float32))
+    p.setUniform(1, S.col_major(np.eye(4)))
+    p.setUniform(2, np.array([flat], dtype=np.int32))
+    with pytest.raises(ValueError):
+        p.drawVAO(vao)
+    p.setUniform(2, np.array([idx], dtype=np.int32))
+    p.drawVAO(vao)
+    p.finish()
+    p.close()
