@@ -280,6 +280,24 @@ int ps3d_read_colour_device(ps3d_pipeline* p, void* devDst);
  * bytes apart, ordered after the draws recorded before it.  With
  * ps3d_set_viewport_rect this reads out one view of a batched pass. */
 int ps3d_copy_colour_rect(ps3d_pipeline* p, int x, int y, int width, int height, void* dst, size_t dstPitch);
+
+/* PuresoftPipeline::postProcess(PuresoftPostProcessor*) (post.cpp:3-19,
+ * proc.h:88-94): records a post-processor pass over the whole colour buffer
+ * (and the depth buffer current now), ordered after everything recorded
+ * before it.  Built-in post-processors only:
+ *   PS3D_PP_ADD8  wrapping per-byte add of 4 bytes (B, G, R, A addends) to
+ *                 every pixel -- the reference demo's post-processor
+ *                 (test2/testpost.cpp:9-43, paddb of eight bytes of 50);
+ *                 params NULL = {50, 50, 50, 50}.
+ *   PS3D_PP_FOG   linear depth fog, params {uint32 fog BGRA, float near,
+ *                 float far}: t = clamp((depth - near) / (far - near), 0, 1),
+ *                 B, G, R = (unsigned char)(c + (fog - c) * t), alpha kept;
+ *                 needs a depth buffer at least the colour buffer's size.
+ * Runs exactly once per recorded call, also when a bin-list overflow makes
+ * the frame replay. */
+#define PS3D_PP_ADD8 0x7001
+#define PS3D_PP_FOG 0x7002
+int ps3d_post_process(ps3d_pipeline* p, int postProcessorId, const void* params, size_t bytes);
 /* 1 when all launched work of the pipeline has completed, 0 while some is
  * still running (cudaStreamQuery; no wait, no verification: ps3d_finish
  * verifies and, after a bin-list overflow, re-runs -- copies included). */

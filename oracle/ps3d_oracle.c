@@ -426,6 +426,53 @@ int ps3do_clear_colour(ps3do* p, uint32_t bgra)
     return 0;
 }
 
+/* PuresoftPipeline::postProcess (post.cpp:3-19) with the built-in
+   post-processors: 0x7001 the demo's per-byte wrapping add (test2/testpost.cpp:
+   9-43) of a BGRA addend, 0x7002 linear depth fog.  The display buffer's
+   memory row H-1-y holds pixel row y; the depth buffer's row y. */
+int ps3do_post_process(ps3do* p, int id, const void* params, size_t bytes)
+{
+    int W = p->display.width, H = p->display.height;
+    if (id == 0x7001) {
+        uint8_t add[4] = {50, 50, 50, 50};
+        if (params) {
+            if (bytes < 4) return -2;
+            memcpy(add, params, 4);
+        }
+        for (int r = 0; r < H; r++) {
+            uint8_t* row = p->display.buf + (size_t)r * p->display.scanline;
+            for (int x = 0; x < 4 * W; x++) row[x] = (uint8_t)(row[x] + add[x & 3]);
+        }
+        return 0;
+    }
+    if (id == 0x7002) {
+        uint32_t fog;
+        float nearD, farD, range;
+        const o_fbo* d = p->depth;
+        if (!params || bytes < 12) return -2;
+        if (d->width < W || d->height < H || d->scanline < 4 * W) return -2;
+        memcpy(&fog, params, 4);
+        memcpy(&nearD, (const uint8_t*)params + 4, 4);
+        memcpy(&farD, (const uint8_t*)params + 8, 4);
+        range = farD - nearD;
+        for (int y = 0; y < H; y++) {
+            const float* drow = (const float*)(d->buf + (size_t)y * d->scanline);
+            uint8_t* crow = p->display.buf + (size_t)(H - 1 - y) * p->display.scanline;
+            for (int x = 0; x < W; x++) {
+                float t = (drow[x] - nearD) / range;
+                t = t > 0.0f ? t : 0.0f;
+                t = t < 1.0f ? t : 1.0f;
+                for (int k = 0; k < 3; k++) {
+                    float c = (float)crow[4 * x + k], f = (float)((fog >> (8 * k)) & 0xff);
+                    crow[4 * x + k] = (uint8_t)(int)(c + (f - c) * t);
+                }
+            }
+        }
+        return 0;
+    }
+    return -2;
+}
+
 int ps3do_read_colour(ps3do* p, void* out)
 {
     memcpy(out, p->display.buf, (size_t)p->display.scanline * p->display.height);

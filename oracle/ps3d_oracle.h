@@ -46,6 +46,8 @@ int ps3do_clear_depth(ps3do* p, float v);
 int ps3do_clear_colour(ps3do* p, uint32_t bgra);
 int ps3do_draw(ps3do* p, int vao);
 int ps3do_read_colour(ps3do* p, void* out);
+/* postProcess with a built-in post-processor (include/ps3d.h PS3D_PP_*). */
+int ps3do_post_process(ps3do* p, int id, const void* params, size_t bytes);
 int ps3do_read_depth(ps3do* p, void* out);
 /* Fragments that reached the depth test (the reference's per-pixel loop
    iterations, fragthrd.cpp:208) and fragments that passed it, since create. */

@@ -217,3 +217,40 @@ void FragmentProcessorLIT2::process(const FragmentProcessorInput* input, Fragmen
                   m_lodScale, m_bias, m_light, m_camera, (const float*)input->user, bgra);
     output->write4(0, bgra);
 }
+
+PostProcessorADD8::PostProcessorADD8(const unsigned char add[4]) { memcpy(m_add, add, 4); }
+
+void PostProcessorADD8::process(int threadIndex, int threadCount, PuresoftFBO* frame, PuresoftFBO* depth)
+{
+    (void)depth;
+    unsigned char* base = (unsigned char*)frame->getBuffer();
+    for (int y = threadIndex; y < frame->getHeight(); y += threadCount) {
+        unsigned char* row = base + (size_t)y * frame->getScanline();
+        for (int x = 0; x < 4 * frame->getWidth(); x++) row[x] = (unsigned char)(row[x] + m_add[x & 3]);
+    }
+}
+
+PostProcessorFOG::PostProcessorFOG(unsigned int fog, float nearD, float farD) : m_fog(fog), m_near(nearD), m_far(farD) {}
+
+/* The frame (the display FBO) is top-down: pixel row y at memory row H-1-y;
+   the depth buffer's pixel row y at memory row y. */
+void PostProcessorFOG::process(int threadIndex, int threadCount, PuresoftFBO* frame, PuresoftFBO* depth)
+{
+    unsigned char* cbase = (unsigned char*)frame->getBuffer();
+    const unsigned char* dbase = (const unsigned char*)depth->getBuffer();
+    const int H = frame->getHeight(), W = frame->getWidth();
+    const float range = m_far - m_near;
+    for (int y = threadIndex; y < H; y += threadCount) {
+        const float* drow = (const float*)(dbase + (size_t)y * depth->getScanline());
+        unsigned char* crow = cbase + (size_t)(H - 1 - y) * frame->getScanline();
+        for (int x = 0; x < W; x++) {
+            float t = (drow[x] - m_near) / range;
+            t = t > 0.0f ? t : 0.0f;
+            t = t < 1.0f ? t : 1.0f;
+            for (int k = 0; k < 3; k++) {
+                float c = (float)crow[4 * x + k], f = (float)((m_fog >> (8 * k)) & 0xff);
+                crow[4 * x + k] = (unsigned char)(int)(c + (f - c) * t);
+            }
+        }
+    }
+}

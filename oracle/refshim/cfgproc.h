@@ -108,3 +108,28 @@ private:
     int m_shadowSize, m_shadowScanlineFloats;
     float m_lodScale, m_bias;
 };
+
+/* Post-processors for PuresoftPipeline::postProcess (post.cpp, proc.h:88-94):
+   the demo's per-byte add (test2/testpost.cpp:9-43, MMX paddb, restated per
+   byte) and a linear depth fog; each thread takes rows threadIndex,
+   threadIndex + threadCount, ... as the demo does. */
+class PostProcessorADD8 : public PuresoftPostProcessor
+{
+public:
+    explicit PostProcessorADD8(const unsigned char add[4]);
+    void process(int threadIndex, int threadCount, PuresoftFBO* frame, PuresoftFBO* depth);
+
+private:
+    unsigned char m_add[4];
+};
+
+class PostProcessorFOG : public PuresoftPostProcessor
+{
+public:
+    PostProcessorFOG(unsigned int fog, float nearD, float farD);
+    void process(int threadIndex, int threadCount, PuresoftFBO* frame, PuresoftFBO* depth);
+
+private:
+    unsigned int m_fog;
+    float m_near, m_far;
+};

@@ -279,6 +279,31 @@ int ps3dr_draw(void* h, int vao)
     return 0;
 }
 
+int ps3dr_post_process(void* h, int id, const void* params, size_t bytes)
+{
+    RefCtx* c = (RefCtx*)h;
+    if (id == 0x7001) {
+        unsigned char add[4] = {50, 50, 50, 50};
+        if (params) {
+            if (bytes < 4) return -2;
+            memcpy(add, params, 4);
+        }
+        PostProcessorADD8 pp(add);
+        return guarded([&] { c->pipe->postProcess(&pp); return 0; });
+    }
+    if (id == 0x7002) {
+        if (!params || bytes < 12) return -2;
+        unsigned int fog;
+        float nearD, farD;
+        memcpy(&fog, params, 4);
+        memcpy(&nearD, (const unsigned char*)params + 4, 4);
+        memcpy(&farD, (const unsigned char*)params + 8, 4);
+        PostProcessorFOG pp(fog, nearD, farD);
+        return guarded([&] { c->pipe->postProcess(&pp); return 0; });
+    }
+    return -2;
+}
+
 int ps3dr_read_colour(void* h, void* out)
 {
     RefCtx* c = (RefCtx*)h;

@@ -39,6 +39,10 @@ int selftest_division(unsigned long long pairs, unsigned long long* rcpBad, unsi
 void launch_raster(const PassParams& P, cudaStream_t s, int& launches, Prof* pr);
 void launch_selftest_wait(int* status, const int* flag, int spins, cudaStream_t s);
 void launch_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr);
+void launch_post_add8(uint32_t* colour, int width, int height, uint32_t add, const int* status, int seq,
+                      cudaStream_t s, int& launches, Prof* pr);
+void launch_post_fog(uint32_t* colour, int width, int height, const float* depth, int depthScan, uint32_t fog,
+                     float nearD, float farD, const int* status, int seq, cudaStream_t s, int& launches, Prof* pr);
 void launch_fill_u32(void* base, int width, int height, int pitchElems, uint32_t v, const int* status, int seq,
                      cudaStream_t s, int& launches, Prof* pr);
 }  // namespace ps3d
@@ -94,7 +98,7 @@ struct Programme {
 
 // one recorded command
 struct Command {
-    enum Kind { DRAW, CLEAR_DEPTH, CLEAR_COLOUR, COPY_COLOUR } kind;
+    enum Kind { DRAW, CLEAR_DEPTH, CLEAR_COLOUR, COPY_COLOUR, POST } kind;
     void* copyDst;    // COPY_COLOUR: destination (device or host) of a rectangle of the colour buffer
     int copyX, copyY, copyW, copyH;  // the rectangle, in pixels from the bottom-left corner
     size_t copyPitch;                // destination bytes per row (rows top-down)
@@ -102,6 +106,9 @@ struct Command {
     int vpX, vpY, vpW, vpH;
     float depthValue;
     uint32_t colourValue;
+    int postId;                // POST: the post-processor (PP_*), its colour parameter and depth range
+    uint32_t postColour;
+    float postNear, postFar;
     DrawDesc desc;
     DrawUniforms uni;
 };
@@ -537,8 +544,12 @@ void wrote(ps3d_pipeline* p, const void* key, cudaEvent_t e)
 
 void read_by(ps3d_pipeline* p, const void* key, cudaEvent_t e) { p->trk.at(key).reads.push_back(e); }
 
-// The index the next pass gets; fills and copies in front of it fail with it.
+// The index the next pass gets.
 int next_seq(const ps3d_pipeline* p) { return (int)p->passStart.size(); }
+// The sequence number of a fill or post-process between passes: it is skipped
+// once a pass before it has failed (the replay starts at or before that pass
+// and runs it then) and runs whatever happens to the passes after it.
+int gap_seq(const ps3d_pipeline* p) { return next_seq(p) - 1; }
 
 int fill_depth(ps3d_pipeline* p, int target, float v)
 {
@@ -549,7 +560,7 @@ int fill_depth(ps3d_pipeline* p, int target, float v)
     memcpy(&bits, &v, 4);
     if ((rc = before_write(p, p->stream, t.depth))) return rc;
     int launches = 0;
-    launch_fill_u32(t.depth, t.scan, t.h, t.scan, bits, p->status, next_seq(p), p->stream, launches, &p->prof);
+    launch_fill_u32(t.depth, t.scan, t.h, t.scan, bits, p->status, gap_seq(p), p->stream, launches, &p->prof);
     p->stats.kernel_launches += launches;
     cudaEvent_t e;
     if ((rc = mark(p, p->stream, e))) return rc;
@@ -562,7 +573,7 @@ int fill_colour(ps3d_pipeline* p, uint32_t v)
     int rc = before_write(p, p->stream, p->colour);
     if (rc) return rc;
     int launches = 0;
-    launch_fill_u32(p->colour, p->devW, p->devH, p->devW, v, p->status, next_seq(p), p->stream, launches, &p->prof);
+    launch_fill_u32(p->colour, p->devW, p->devH, p->devW, v, p->status, gap_seq(p), p->stream, launches, &p->prof);
     p->stats.kernel_launches += launches;
     cudaEvent_t e;
     if ((rc = mark(p, p->stream, e))) return rc;
@@ -580,7 +591,7 @@ int fill_depth_plain(ps3d_pipeline* p, int target, float v)
     uint32_t bits;
     memcpy(&bits, &v, 4);
     int launches = 0;
-    launch_fill_u32(t.depth, t.scan, t.h, t.scan, bits, p->status, next_seq(p), p->stream, launches, &p->prof);
+    launch_fill_u32(t.depth, t.scan, t.h, t.scan, bits, p->status, gap_seq(p), p->stream, launches, &p->prof);
     p->stats.kernel_launches += launches;
     return 0;
 }
@@ -588,13 +599,16 @@ int fill_depth_plain(ps3d_pipeline* p, int target, float v)
 int fill_colour_plain(ps3d_pipeline* p, uint32_t v)
 {
     int launches = 0;
-    launch_fill_u32(p->colour, p->devW, p->devH, p->devW, v, p->status, next_seq(p), p->stream, launches, &p->prof);
+    launch_fill_u32(p->colour, p->devW, p->devH, p->devW, v, p->status, gap_seq(p), p->stream, launches, &p->prof);
     p->stats.kernel_launches += launches;
     return 0;
 }
 
+int post_process(ps3d_pipeline* p, const Command& c, bool tracked);
+
 int copy_colour_plain(ps3d_pipeline* p, const Command& c)
 {
+    if (c.kind == Command::POST) return post_process(p, c, false);
     const uint8_t* src = p->colour + ((size_t)(p->devH - c.copyY - c.copyH) * p->devW + c.copyX) * 4;
     CU(cudaMemcpy2DAsync(c.copyDst, c.copyPitch, src, (size_t)p->devW * 4, (size_t)c.copyW * 4, c.copyH,
                          cudaMemcpyDefault, p->stream));
@@ -808,11 +822,14 @@ int plan_commands(const std::vector<Command>& cmds, size_t from, PassFn onPass, 
         size_t j = i;
         int depthClearTarget = -2;
         for (; j < n && cmds[j].kind != Command::DRAW; j++) {
-            if (cmds[j].kind == Command::COPY_COLOUR) {  // in order: clears gathered so far first
+            if (cmds[j].kind == Command::COPY_COLOUR || cmds[j].kind == Command::POST) {
+                // in order: clears gathered so far first
                 if (ps.clearDepth && (rc = onFill(depthClearTarget, ps.depthValue, 0u))) return rc;
                 if (ps.clearColour && (rc = onFill(-3, 0.0f, ps.colourValue))) return rc;
                 ps.clearDepth = ps.clearColour = false;
                 if ((rc = onCopy(cmds[j]))) return rc;
+                // a post-process is not idempotent: a replay of the next pass starts after it
+                if (cmds[j].kind == Command::POST) i = j + 1;
                 continue;
             }
             if (cmds[j].kind == Command::CLEAR_DEPTH) {
@@ -846,10 +863,48 @@ int plan_commands(const std::vector<Command>& cmds, size_t from, PassFn onPass, 
     return 0;
 }
 
+// A recorded post-process (PuresoftPipeline::postProcess, post.cpp:3-19):
+// one kernel over the colour buffer (and, for PP_FOG, the depth buffer
+// current when it was recorded), after the colour buffer's last writer and
+// readers, the depth buffer's last writer and every earlier pass's emit (so
+// that it sees whether one of them failed).  `tracked` = false on the
+// single-stream no-allocation path.
+int post_process(ps3d_pipeline* p, const Command& c, bool tracked)
+{
+    Target t = {};
+    int rc = 0;
+    if (c.postId == PP_FOG) {
+        if ((rc = depth_target(p, c.depthTarget, t))) return rc;
+        if (t.w < p->devW || t.h < p->devH || t.scan < p->devW)
+            return fail(PS3D_ERR_INVALID, "the fog post-process needs a depth buffer of at least %dx%d", p->devW, p->devH);
+    }
+    if (tracked) {
+        if ((rc = wait_event(p->stream, p->trk.lastEmit)) || (rc = before_write(p, p->stream, p->colour))) return rc;
+        if (t.depth && (rc = before_read(p, p->stream, t.depth))) return rc;
+    }
+    int launches = 0;
+    if (c.postId == PP_ADD8)
+        launch_post_add8((uint32_t*)p->colour, p->devW, p->devH, c.postColour, p->status, gap_seq(p), p->stream,
+                         launches, &p->prof);
+    else
+        launch_post_fog((uint32_t*)p->colour, p->devW, p->devH, t.depth, t.scan, c.postColour, c.postNear, c.postFar,
+                        p->status, gap_seq(p), p->stream, launches, &p->prof);
+    CU(cudaGetLastError());
+    p->stats.kernel_launches += launches;
+    if (tracked) {
+        cudaEvent_t e;
+        if ((rc = mark(p, p->stream, e))) return rc;
+        wrote(p, p->colour, e);
+        if (t.depth) read_by(p, t.depth, e);
+    }
+    return 0;
+}
+
 // A recorded colour read-out: the rectangle's rows top-down (memory row
 // H-1-y of the display layout) into dst, copyPitch bytes apart.
 int copy_colour(ps3d_pipeline* p, const Command& c)
 {
+    if (c.kind == Command::POST) return post_process(p, c, true);
     const uint8_t* src = p->colour + ((size_t)(p->devH - c.copyY - c.copyH) * p->devW + c.copyX) * 4;
     int rc = before_read(p, p->stream, p->colour);
     if (rc) return rc;
@@ -1553,6 +1608,40 @@ int ps3d_copy_colour_rect(ps3d_pipeline* p, int x, int y, int width, int height,
     c.copyW = width;
     c.copyH = height;
     c.copyPitch = dstPitch;
+    (p->recording ? p->recording->cmds : p->pending).push_back(c);
+    return 0;
+}
+
+int ps3d_post_process(ps3d_pipeline* p, int postProcessorId, const void* params, size_t bytes)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    Command c;
+    memset(&c, 0, sizeof c);
+    c.kind = Command::POST;
+    c.depthTarget = p->depthTarget;
+    c.postId = postProcessorId;
+    switch (postProcessorId) {
+    case PP_ADD8:
+        c.postColour = 0x32323232u;  // the demo's eight bytes of 50 (test2/testpost.cpp:16)
+        if (params) {
+            if (bytes < 4) return fail(PS3D_ERR_INVALID, "PS3D_PP_ADD8 takes 4 bytes (B, G, R, A addends)");
+            memcpy(&c.postColour, params, 4);
+        }
+        break;
+    case PP_FOG: {
+        if (!params || bytes < 12) return fail(PS3D_ERR_INVALID, "PS3D_PP_FOG takes {uint32 BGRA, float near, float far}");
+        memcpy(&c.postColour, params, 4);
+        memcpy(&c.postNear, (const uint8_t*)params + 4, 4);
+        memcpy(&c.postFar, (const uint8_t*)params + 8, 4);
+        Target t;
+        int rc = depth_target(p, c.depthTarget, t);
+        if (rc) return rc;
+        if (t.w < p->devW || t.h < p->devH || t.scan < p->devW)
+            return fail(PS3D_ERR_INVALID, "the fog post-process needs a depth buffer of at least %dx%d", p->devW, p->devH);
+        break;
+    }
+    default: return fail(PS3D_ERR_INVALID, "unknown post-processor 0x%04x", postProcessorId);
+    }
     (p->recording ? p->recording->cmds : p->pending).push_back(c);
     return 0;
 }

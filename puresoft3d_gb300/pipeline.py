@@ -33,6 +33,7 @@ _SIGS = {
     "ps3d_texture_create_device": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p, _c_int],
     "ps3d_texture_destroy": [_c_void_p, _c_int],
     "ps3d_texture_read": [_c_void_p, _c_int, _c_void_p, _c_size_t],
+    "ps3d_post_process": [_c_void_p, _c_int, _c_void_p, _c_size_t],
     "ps3d_texture_create_layers": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p, _c_int, _c_int],
     "ps3d_texture_write_layer": [_c_void_p, _c_int, _c_int, _c_void_p, _c_size_t],
     "ps3d_texture_read_layer": [_c_void_p, _c_int, _c_int, _c_void_p, _c_size_t],
@@ -300,6 +301,13 @@ class PuresoftPipeline:
         """Records a read-out of the colour rectangle (x, y, w, h) to dst_ptr
         (device or pinned host memory), rows top-down, `pitch` bytes apart."""
         self._check(self.lib.ps3d_copy_colour_rect(self.h, x, y, w, h, dst_ptr, pitch))
+
+    def postProcess(self, pp_id: int, params: bytes = None):
+        """postProcess(processor): records a built-in post-processor
+        (PS3D_PP_*) over the colour buffer, in order with the draws; `params`
+        are its parameter bytes (see scenes.fog_params)."""
+        buf = None if params is None else ctypes.create_string_buffer(bytes(params), len(params))
+        self._check(self.lib.ps3d_post_process(self.h, pp_id, buf, 0 if params is None else len(params)))
 
     def query(self) -> bool:
         """True when all launched work has completed (no wait)."""

@@ -45,6 +45,18 @@ FP_LIT1, FP_LIT1A, FP_LIT3 = 0x1103, 0x1403, 0x1303
 VP_LIT2, IP_LIT2, FP_LIT2 = 0x1201, 0x1202, 0x1203
 
 UPDATE_DEPTH, TEST_DEPTH, FACE_CULLING, ALPHABLEND = 1, 2, 4, 8
+PP_ADD8, PP_FOG = 0x7001, 0x7002  # built-in post-processors
+
+
+def add8_params(b: int, g: int, r: int, a: int) -> bytes:
+    """PP_ADD8's parameter: the per-byte addends of a BGRA pixel."""
+    return bytes([b & 255, g & 255, r & 255, a & 255])
+
+
+def fog_params(bgra: int, near: float, far: float) -> bytes:
+    """PP_FOG's parameter: fog colour (BGRA word) and the depth range."""
+    import struct
+    return struct.pack("<Iff", bgra & 0xFFFFFFFF, near, far)
 
 
 @dataclasses.dataclass

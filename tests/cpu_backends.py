@@ -44,6 +44,7 @@ _API = [
     ("clear_colour", [ctypes.c_uint32]),
     ("draw", [ctypes.c_int]),
     ("read_colour", [ctypes.c_void_p]),
+    ("post_process", [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]),
 ]
 
 
@@ -140,6 +141,10 @@ class _CPipeline:
 
     def drawVAO(self, vao):
         self._call("draw", vao)
+
+    def postProcess(self, pp_id, params=None):
+        buf = None if params is None else ctypes.create_string_buffer(bytes(params), len(params))
+        self._call("post_process", pp_id, buf, 0 if params is None else len(params))
 
     def readColour(self) -> np.ndarray:
         out = np.empty((self.height, self.width, 4), dtype=np.uint8)

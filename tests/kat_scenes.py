@@ -167,6 +167,35 @@ def _skybox_scene(name, w, h, view, face_size, wrap, soup_seed=None, blend=False
     return S.Scene(name, w, h, b.setup, b.frame, {"triangles": tris, "depth_texture": depth})
 
 
+def _post_scene(name, w, h, seed):
+    """The post-processing hook (post.cpp:3-19) between passes: a DEF01
+    soup, the demo's per-byte add with wrap-around, a second soup over it,
+    depth fog, and the add again with the demo's default addend."""
+    b = S._Builder()
+    rng = np.random.default_rng(seed)
+    tex = b.texture(S.checker_noise_bgra(16, 4, rng))
+    depth = b.empty_texture(w, h)
+    m1, m2 = _tri_mesh(random_soup(150, seed)), _tri_mesh(random_soup(150, seed + 1))
+    prog = b.programme(S.VP_DEF01, S.IP_DEF01, S.FP_LIT1)
+    v1, v2 = b.vao(m1, slots=(0, 3, 4)), b.vao(m2, slots=(0, 3, 4))
+    eye = np.eye(4)
+    b.f("setDepth", depth)
+    b.f("clearDepth", 1.0)
+    b.f("clearColour", 0xFF101010)
+    b.f("useProgramme", prog)
+    for slot in (3, 4, 5):
+        b.f("setUniform", slot, S.col_major(eye))
+    b.f("setUniform", 7, S.vec4(0.3, 0.5, 0.81))
+    b.f("setUniform", 8, S.vec4(0, 0, 2, 1))
+    b.f("setUniform", 9, np.array([tex], dtype=np.int32))
+    b.f("drawVAO", v1)
+    b.f("postProcess", S.PP_ADD8, S.add8_params(10, 200, 77, 5))
+    b.f("drawVAO", v2)
+    b.f("postProcess", S.PP_FOG, S.fog_params(0xFF8040C0, -0.2, 0.9))
+    b.f("postProcess", S.PP_ADD8, None)
+    return S.Scene(name, w, h, b.setup, b.frame, {"triangles": 300, "depth_texture": depth})
+
+
 def _v(x, y, z=0.0, w=1.0):
     return [x * w, y * w, z * w, w]
 
@@ -251,4 +280,6 @@ def kat_scenes():
                                                             17, True)))
     out.append(("kat_def04_sky_down_blend_72x56", _skybox_scene("kat_def04_sky_down_blend", 72, 56,
                                                                _rot(-2.6, 1.05, -0.5), 32, False, blend=True)))
+    # the post-processing hook between passes
+    out.append(("kat_post_add_fog_96x64", _post_scene("kat_post_add_fog", 96, 64, 22)))
     return out

@@ -41,12 +41,14 @@ def test_fragment_counts_match_oracle(gpu_lib):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", ["c3_small", "c2_small"])
+@pytest.mark.parametrize("case", ["c3_small", "c2_small", "kat_post_add_fog"])
 def test_bin_capacity_replay(gpu_lib, monkeypatch, case):
     """A pass whose bin lists overflow the preallocated room is re-run
     transparently with larger buffers; the result is unchanged.  In the
     two-pass case (shadow pass, then the lit pass sampling it, on the two pass
-    streams) the first pass overflows while the second may already run."""
+    streams) the first pass overflows while the second may already run.  In
+    the post-process case (pass, add, pass, fog, add) every post-process runs
+    exactly once although the passes around them replay."""
     from puresoft3d_gb300.pipeline import PuresoftPipeline
     name, scene = [c for c in CASES if c[0].startswith(case)][0]
     monkeypatch.setenv("PS3D_PAIR_CAP", "64")
@@ -200,4 +202,31 @@ def test_layered_texture_gpu(gpu_lib):
     p.setUniform(2, np.array([idx], dtype=np.int32))
     p.drawVAO(vao)
     p.finish()
+    p.close()
+
+
+@pytest.mark.gpu
+def test_post_process_arguments(gpu_lib):
+    """Unknown post-processors and short parameters are refused at record
+    time; the fog needs a depth buffer covering the colour buffer."""
+    from puresoft3d_gb300 import scenes as S
+    from puresoft3d_gb300.pipeline import PuresoftPipeline
+    p = PuresoftPipeline(32, 16)
+    with pytest.raises(ValueError):
+        p.postProcess(0x7777)
+    with pytest.raises(ValueError):
+        p.postProcess(S.PP_ADD8, b"\x01")
+    with pytest.raises(ValueError):
+        p.postProcess(S.PP_FOG, None)
+    small = p.createTexture(16, 16, 64, 4, None, 0)
+    p.setDepth(small)
+    with pytest.raises(ValueError):
+        p.postProcess(S.PP_FOG, S.fog_params(0, 0.0, 1.0))
+    p.setDepth(-1)
+    p.clearDepth(1.0)
+    p.clearColour(0x01020304)
+    p.postProcess(S.PP_FOG, S.fog_params(0xFFFFFFFF, 0.0, 1.0))  # depth cleared to 1.0: full fog
+    p.postProcess(S.PP_ADD8, S.add8_params(1, 1, 1, 1))
+    img = p.readColour()
+    assert (img.reshape(-1, 4) == np.array([0, 0, 0, 2], dtype=np.uint8)).all()  # 255 + 1 wraps; alpha 1 + 1
     p.close()

@@ -13,7 +13,7 @@ from kat_scenes import _scene, _tri_mesh
 
 COLOUR_TOL = 1  # LSB per channel
 CASES = [c for c in golden_cases() if c[0].split("_")[0] in ("c1", "c2") or c[0].startswith("kat_soup_lit")
-         or c[0].startswith("kat_alphatest_blend")]
+         or c[0].startswith("kat_alphatest_blend") or c[0].startswith("kat_post")]
 
 
 def _outputs(pipe, scene):
