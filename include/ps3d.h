@@ -328,6 +328,52 @@ int ps3d_cmdbuf_destroy(ps3d_pipeline* p, ps3d_cmdbuf* cb);
 /* Bytes a submission with uploadInputs copies host -> device. */
 int ps3d_cmdbuf_input_bytes(ps3d_pipeline* p, ps3d_cmdbuf* cb, size_t* out);
 
+/* ---- OBJX mesh files (the reference's objcvt/objxio.h:42-52, objxio.cpp).
+ * Little-endian, packed as the reference writes them: a file header
+ * (version 0x010003, camera, four lights) and per mesh a 1627-byte header,
+ * float4 positions, float4 normals, float4 tangents, float2 texture
+ * coordinates (each as the header says) and int32 indices.  Host-only calls
+ * (no device needed) except ps3d_objx_load_vao. */
+typedef struct ps3d_objx ps3d_objx;
+typedef struct {                 /* scene_desc (objxio.h:29-36) */
+    float camera_pos[4], camera_ypr[4];
+    float light_pos[4][4], light_dir[4][4];
+    int light_types[4];          /* 0 omni (direction shorter than 1e-7), 1 directional */
+} ps3d_objx_scene;
+typedef struct {                 /* mesh_info (objxio.h:5-27) without the arrays */
+    char name[260];
+    unsigned num_vertices, num_indices;
+    int has_texcoords, has_normals, has_tangents;
+    float ambient[4], diffuse[4], specular[4];  /* r, g, b, a; clamped to [0, 1] when read */
+    float specular_exponent;
+    char diffuse_file[260], bump_file[260], spc_file[260], spe_file[260], programme[260];
+} ps3d_objx_mesh_info;
+/* create_objxA / write_mesh: arrays may be NULL (absent) except vertices;
+ * indices iff num_indices.  close writes the mesh count. */
+int ps3d_objx_create(const char* path, const ps3d_objx_scene* scene, ps3d_objx** out);
+int ps3d_objx_write_mesh(ps3d_objx* h, const ps3d_objx_mesh_info* info, const float* vertices, const float* normals,
+                         const float* tangents, const float* texcoords, const int* indices);
+/* open_objxA / get_mesh_count / read_mesh_header / read_mesh / close_objx.
+ * read_mesh fills the arrays that are not NULL (num_vertices float4 / float2
+ * elements, num_indices ints) and skips the rest; tangents asked for but
+ * absent are derived from the texture coordinates (the reference's
+ * generate_tangents reads an uninitialised vector and, for indexed meshes,
+ * clears the positions; here the evident intent: per-triangle
+ * ((c-a)*dv2 - (b-a)*dv1) / (du1*dv2 - dv1*du2), summed per vertex and
+ * normalised when indexed). */
+int ps3d_objx_open(const char* path, ps3d_objx_scene* scene, ps3d_objx** out);
+int ps3d_objx_mesh_count(ps3d_objx* h);
+int ps3d_objx_read_mesh_header(ps3d_objx* h, ps3d_objx_mesh_info* info);
+int ps3d_objx_read_mesh(ps3d_objx* h, float* vertices, float* normals, float* tangents, float* texcoords,
+                        int* indices);
+int ps3d_objx_close(ps3d_objx* h);
+/* The reference demo's SceneObject::findOrCreateVao (test/scenobj.cpp:88-162)
+ * for mesh `meshIndex` of an OBJX file: a new VAO with slot 0 positions
+ * (w = 1), and with texture coordinates slot 1 tangents, 2 binormals =
+ * normalise(cross(normal, tangent)), 4 texture coordinates, and slot 3
+ * normals -- the DEF03 layout.  Non-indexed meshes only. */
+int ps3d_objx_load_vao(ps3d_pipeline* p, const char* path, int meshIndex, int* vao);
+
 /* ---- timing on the pipeline's stream (CUDA events) */
 int ps3d_timer_begin(ps3d_pipeline* p);
 int ps3d_timer_end(ps3d_pipeline* p, float* ms);

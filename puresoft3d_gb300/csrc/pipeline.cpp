@@ -64,6 +64,17 @@ int fail(int code, const char* fmt, ...)
     return code;
 }
 
+}  // namespace
+
+// The same message slot for the other translation units (objx.cpp).
+int ps3d::report_error(int code, const char* msg)
+{
+    g_err = msg;
+    return code;
+}
+
+namespace {
+
 #define CU(call)                                                                                 \
     do {                                                                                         \
         cudaError_t e_ = (call);                                                                 \

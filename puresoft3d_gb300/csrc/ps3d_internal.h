@@ -30,6 +30,9 @@ enum : int {
     VP_LIT2 = 0x1201, IP_LIT2 = 0x1202, FP_LIT2 = 0x1203,
 };
 
+// Sets the calling thread's last-error message (ps3d_last_error); returns code.
+int report_error(int code, const char* msg);
+
 // built-in post-processors (include/ps3d.h)
 enum : int { PP_ADD8 = 0x7001, PP_FOG = 0x7002 };
 

@@ -119,7 +119,8 @@ def selftest_division(pairs: int = 1 << 28):
 
 
 def exported_symbols() -> list:
-    return sorted(list(_SIGS) + ["ps3d_last_error"])
+    from . import objx
+    return sorted(list(_SIGS) + list(objx._SIGS) + ["ps3d_last_error"])
 
 
 class PuresoftPipeline:
@@ -301,6 +302,12 @@ class PuresoftPipeline:
         """Records a read-out of the colour rectangle (x, y, w, h) to dst_ptr
         (device or pinned host memory), rows top-down, `pitch` bytes apart."""
         self._check(self.lib.ps3d_copy_colour_rect(self.h, x, y, w, h, dst_ptr, pitch))
+
+    def loadObjxVao(self, path: str, mesh: int = 0) -> int:
+        """A VAO from an OBJX mesh, laid out as the reference demo does
+        (positions, tangents, binormals, normals, texture coordinates)."""
+        from .objx import load_vao
+        return load_vao(self, path, mesh)
 
     def postProcess(self, pp_id: int, params: bytes = None):
         """postProcess(processor): records a built-in post-processor
