@@ -213,9 +213,11 @@ def autotune(pipe, record, key, args):
     if args.bin_width:
         pipe.setBinWidth(args.bin_width)
         pipe.setRasterOccupancy(args.raster_occupancy)
-        return {"bin_width": args.bin_width, "raster_occupancy": args.raster_occupancy, "source": "flags"}
+        pipe.setSpanCulling(args.span_culling)
+        return {"bin_width": args.bin_width, "raster_occupancy": args.raster_occupancy,
+                "span_culling": args.span_culling, "source": "flags"}
     best, ms = Autotuner().tune(pipe, record, key, reps=3)
-    return {"bin_width": best[0], "raster_occupancy": best[1], "source": "autotuner",
+    return {"bin_width": best[0], "raster_occupancy": best[1], "span_culling": best[2], "source": "autotuner",
             "candidate_ms": {k: round(v, 4) for k, v in ms.items()}}
 
 
@@ -469,6 +471,7 @@ def run_frames_only(args):
     if args.bin_width:
         pipe.setBinWidth(args.bin_width)
         pipe.setRasterOccupancy(args.raster_occupancy)
+        pipe.setSpanCulling(args.span_culling)
     for _ in range(args.ncu_frames):
         S.replay_frame(scene, pipe)
         pipe.finish()
@@ -786,6 +789,8 @@ def main():
     ap.add_argument("--bin-width", type=int, default=0, choices=[0, 8, 16, 32],
                     help="fix the schedule (with --raster-occupancy) instead of autotuning it")
     ap.add_argument("--raster-occupancy", type=int, default=0, choices=[0, 8])
+    ap.add_argument("--span-culling", type=int, default=1, choices=[0, 1],
+                    help="with --bin-width: raster variant with (1) or without (0) the span occlusion test")
     args = ap.parse_args()
     if args.ncu_frames:
         run_frames_only(args)

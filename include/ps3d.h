@@ -231,6 +231,12 @@ int ps3d_finish(ps3d_pipeline* p);
  * workload.  Default 32 (or PS3D_BIN_W). */
 int ps3d_set_bin_width(ps3d_pipeline* p, int columns);
 int ps3d_get_bin_width(ps3d_pipeline* p, int* columns);
+/* Raster variant: on (the default), a span whose every pixel would fail the
+ * depth test against its row's current depths is dropped before its depths
+ * are computed, in bins with more than 128 triangles (a conservative test,
+ * so results are unchanged); off leaves the test out of the kernel.  The
+ * autotuner times both. */
+int ps3d_set_span_culling(ps3d_pipeline* p, int on);
 /* Second schedule knob: the raster kernel variant.  0 lets each thread use
  * the registers it wants (fewer resident blocks); 8 caps registers so that
  * 8 blocks fit per SM where shared memory allows (more warps to hide
@@ -399,6 +405,12 @@ int ps3d_selftest_wait(ps3d_pipeline* p, int spins, float* ms);
  * exponents -100..100 for the reciprocal, `pairs` hashed pairs for the
  * quotient.  Both counts must be 0. */
 int ps3d_selftest_division(uint64_t pairs, uint64_t* rcpMismatches, uint64_t* divMismatches);
+/* Checks the raster's span occlusion test (a span is dropped before its
+ * per-pixel depths are computed when no pixel can pass the depth test)
+ * against the per-pixel loop it replaces, on `cases` random spans with depth
+ * bounds around the pass/fail boundary: *wrong must be 0; *occluded is how
+ * many spans it dropped. */
+int ps3d_selftest_occlusion(uint64_t cases, uint64_t* wrong, uint64_t* occluded);
 /* Overwrites `bytes` of an internal device buffer on the pipeline's stream
  * (benchmarking aid: evicts the 126 MB L2 between timed frames). */
 int ps3d_l2_scrub(ps3d_pipeline* p, size_t bytes);

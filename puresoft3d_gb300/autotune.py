@@ -1,6 +1,7 @@
 """Schedule autotuner for the device passes.
 
-A schedule is a pair (bin width, raster occupancy).  The bin width (8, 16 or
+A schedule is a triple (bin width, raster occupancy, span culling).  The bin
+width (8, 16 or
 32 columns; bins are always 32 rows) sets how the raster kernel's work is
 cut:
 
@@ -14,7 +15,10 @@ cut:
 
 The raster occupancy picks the raster kernel variant: 0 lets each thread use
 the registers it wants, 8 caps them so that up to 8 blocks are resident per
-SM (more warps to hide latency, less room per thread).
+SM (more warps to hide latency, less room per thread).  Span culling (1)
+drops spans that cannot pass the depth test before their depths are
+computed, in crowded bins: it pays off with depth complexity and costs a
+little elsewhere.
 
 Which schedule wins depends on the workload (triangle sizes, depth complexity,
 target size), so the tuner times every candidate on the caller's own frame:
@@ -33,23 +37,28 @@ import os
 import statistics
 from typing import Callable, Dict, Optional, Sequence, Tuple
 
-CANDIDATES = tuple((bw, occ) for bw in (8, 16, 32) for occ in (0, 8))
+CANDIDATES = tuple((bw, occ, cull) for bw in (8, 16, 32) for occ in (0, 8) for cull in (1, 0))
 
 
-def _pair(c):
-    return (int(c[0]), int(c[1])) if isinstance(c, (tuple, list)) else (int(c), 0)
+def _sched(c):
+    """(bin width, occupancy, span culling) of a candidate given as a bare
+    width, a pair or a triple (occupancy 0 and culling on by default)."""
+    if not isinstance(c, (tuple, list)):
+        return (int(c), 0, 1)
+    return (int(c[0]), int(c[1]) if len(c) > 1 else 0, int(c[2]) if len(c) > 2 else 1)
 
 
 def _name(c) -> str:
-    bw, occ = _pair(c)
-    return "%d/%d" % (bw, occ)
+    return "%d/%d/%d" % _sched(c)
 
 
 def apply(pipe, c) -> None:
-    bw, occ = _pair(c)
+    bw, occ, cull = _sched(c)
     pipe.setBinWidth(bw)
     if hasattr(pipe, "setRasterOccupancy"):
         pipe.setRasterOccupancy(occ)
+    if hasattr(pipe, "setSpanCulling"):
+        pipe.setSpanCulling(cull)
 
 
 def _default_cache() -> str:
@@ -116,23 +125,23 @@ class Autotuner:
 
     def tune(self, pipe, record: Callable[[object], None], key: str,
              candidates: Sequence = CANDIDATES, reps: int = 5, warmup: int = 2,
-             retune: bool = False) -> Tuple[Tuple[int, int], Dict[str, float]]:
+             retune: bool = False) -> Tuple[Tuple[int, int, int], Dict[str, float]]:
         """Sets `pipe`'s schedule to the fastest candidate for `record`'s
-        frame and returns ((bin width, raster occupancy), {"bw/occ": median
-        ms}).  A candidate is a (bin width, occupancy) pair or a bare bin
-        width.  A cached result for (key, device, candidates) is reused
-        unless `retune`."""
+        frame and returns ((bin width, raster occupancy, span culling),
+        {"bw/occ/cull": median ms}).  A candidate is such a triple, a (bin
+        width, occupancy) pair or a bare bin width.  A cached result for
+        (key, device, candidates) is reused unless `retune`."""
         full = "%s|%s|%s" % (key, device_name(), ",".join(_name(c) for c in candidates))
         hit = self.table.get(full)
         if hit and not retune:
-            best = _pair(hit["best"])
+            best = _sched(hit["best"])
             apply(pipe, best)
             return best, dict(hit["ms"])
         ms: Dict[str, float] = {}
         for c in candidates:
             apply(pipe, c)
             ms[_name(c)] = self.time_frame(pipe, record, reps=reps, warmup=warmup)
-        best = _pair(min(candidates, key=lambda c: ms[_name(c)]))
+        best = _sched(min(candidates, key=lambda c: ms[_name(c)]))
         apply(pipe, best)
         self.table[full] = {"best": list(best), "ms": {k: round(v, 5) for k, v in ms.items()}}
         self._save()

@@ -36,6 +36,7 @@ int radix_passes(int nBins);
 int sort_desc_offset(int nTris);
 size_t radix_scratch_ints(int sortBlocks, int passes, int nTris);
 int selftest_division(unsigned long long pairs, unsigned long long* rcpBad, unsigned long long* divBad);
+int selftest_occlusion(unsigned long long cases, unsigned long long* wrong, unsigned long long* occluded);
 void launch_raster(const PassParams& P, cudaStream_t s, int& launches, Prof* pr);
 void launch_selftest_wait(int* status, const int* flag, int spins, cudaStream_t s);
 void launch_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr);
@@ -222,6 +223,7 @@ struct ps3d_pipeline {
     int depthTarget = -1;
     int binW = 32;
     int rasterBlocks = 0;
+    int cullSpans = 1;
     bool countFrags = false;
     cudaStream_t stream = nullptr;
     bool ownStream = false;
@@ -747,6 +749,7 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     P.H = H;
     P.binW = binW;
     P.rasterBlocks = p->rasterBlocks;
+    P.cullSpans = p->cullSpans;
     P.passFp = pass_fp(dd.data(), dd.size());
     P.forward = forward;
     P.binsX = binsX;
@@ -1539,6 +1542,13 @@ int ps3d_set_bin_width(ps3d_pipeline* p, int columns)
     return 0;
 }
 
+int ps3d_set_span_culling(ps3d_pipeline* p, int on)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    p->cullSpans = on ? 1 : 0;
+    return 0;
+}
+
 int ps3d_set_raster_occupancy(ps3d_pipeline* p, int blocksPerSM)
 {
     if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
@@ -1870,6 +1880,16 @@ int ps3d_selftest_division(uint64_t pairs, uint64_t* rcpMismatches, uint64_t* di
     return 0;
 }
 
+int ps3d_selftest_occlusion(uint64_t cases, uint64_t* wrong, uint64_t* occluded)
+{
+    if (!wrong || !occluded) return fail(PS3D_ERR_INVALID, "null argument");
+    unsigned long long a = 0, b = 0;
+    if (selftest_occlusion(cases, &a, &b)) return fail(PS3D_ERR_DEVICE, "self-test launch failed");
+    *wrong = a;
+    *occluded = b;
+    return 0;
+}
+
 int ps3d_selftest_wait(ps3d_pipeline* p, int spins, float* ms)
 {
     if (!p || !ms || spins < 1) return fail(PS3D_ERR_INVALID, "bad argument");
@@ -2085,6 +2105,7 @@ int noalloc_run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const P
     P.H = H;
     P.binW = s.binW;
     P.rasterBlocks = p->rasterBlocks;
+    P.cullSpans = p->cullSpans;
     P.passFp = pass_fp(g_noallocDraws, (size_t)s.nd);
     P.forward = s.forward;
     P.binsX = s.binsX;

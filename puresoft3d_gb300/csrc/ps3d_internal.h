@@ -92,6 +92,7 @@ struct PassParams {
     int W, H;                 // target (depth buffer) size; each draw has its own viewport rectangle
     int binW, binsX, binsY;   // bins of kBinH x binW pixels
     int rasterBlocks;         // raster variant: 0 = registers as needed, 8 = capped for 8 blocks per SM
+    int cullSpans;            // raster variant: 1 = occluded spans dropped in crowded bins
     int passFp;               // the fragment processor every colour draw of the pass uses, else 0
     int forward;              // some draw blends or may discard: shade every passing fragment in order
     int nTris, nDraws;

@@ -151,6 +151,38 @@ __device__ __forceinline__ int shade_fragment(const DrawDesc& d, const DrawUnifo
     }
 }
 
+// True when no pixel kA..kB (steps from leftClamped) of a span can pass a
+// depth test against depths <= curMax -- i.e. every z the per-pixel loop
+// would compute satisfies z - cur >= -0.0001f -- decided without running the
+// loop.  The loop's values are z_k = fl(S_k * rcp(C_k)) with S_k, C_k the
+// sequential float sums S0 + dS + ... and C0 + dC + ...  Against the exact
+// T(k) = S0 + k dS and U(k) = C0 + k dC: each of the k additions errs by at
+// most 2^-24 |S_i| <= 2^-23 max|T| (likewise C), so |S_k - T(k)| <= eS =
+// k 2^-23 AS; with U > 0 on the span, T/U is monotonic, so its minimum is at
+// an end point, and |z_k - T/U| <= (eS + Tmax eC / Umin) / Umin plus two
+// roundings.  Every bound below is taken at least twice as loose as this
+// derivation needs (evaluation errors of the bounds themselves included),
+// and anything non-finite or a U near zero keeps the span.
+__device__ __forceinline__ bool span_occluded(const SpanZ& z, int kA, int kB, float curMax)
+{
+    const float S0 = z.pz, C0 = z.cf2, dS = z.pzStep, dC = z.cf2Step;
+    const float fA = (float)kA, fB = (float)kB;
+    const float TA = S0 + fA * dS, TB = S0 + fB * dS, UA = C0 + fA * dC, UB = C0 + fB * dC;
+    const float evT = 0x1p-21f * (fabsf(S0) + fB * fabsf(dS)), evU = 0x1p-21f * (fabsf(C0) + fB * fabsf(dC));
+    const float AS = fmaxf(fabsf(S0), fabsf(TB)) + evT, AC = fmaxf(fabsf(C0), fabsf(UB)) + evU;
+    const float eS = fB * 0x1p-22f * AS + 1e-37f, eC = fB * 0x1p-22f * AC + 1e-37f;
+    const float Umin = fminf(UA, UB) - evU - eC;
+    if (!(Umin > 1e-30f) || !(Umin < 1e30f)) return false;
+    const float Tmax = fmaxf(fabsf(TA), fabsf(TB)) + evT + eS;
+    // fast quotients (2 ulp for divisors in [2^-126, 2^126]): the bound's slack covers them
+    const float fmin = fminf(__fdividef(TA, UA), __fdividef(TB, UB));
+    const float rU = __fdividef(1.0f, Umin);
+    const float delta = 2.0f * ((eS + evT + Tmax * (eC + evU) * rU) * rU) + (Tmax * rU) * 0x1p-19f;
+    const float lhs = fmin - delta - curMax;
+    const float slack = (fabsf(fmin) + fabsf(curMax) + delta) * 1e-6f;
+    return lhs - slack >= -0.0001f;  // false for NaN
+}
+
 constexpr int kRasterThreads = 128;  // 4 warps: warp = column quarter, lane = bin row
 constexpr int kChunk = 128;          // triangles per chunk (one per thread)
 constexpr int kSlots = 128;          // (triangle, row) spans per round (one per thread)
@@ -160,7 +192,10 @@ constexpr int kSlots = 128;          // (triangle, row) spans per round (one per
 // in order, into the bin's colour tile (blend4 under ALPHABLEND; a discard
 // skips the colour and the depth write) -- the reference's per-fragment
 // order (fragthrd.cpp:208-252); no shade list.
-template <int BW, int MINB, int FWD = 0>
+// CULL: spans are tested for occlusion before their depths are computed
+// (span_occluded) in crowded bins; the variant without it keeps the
+// registers and instructions of the test out of passes that gain nothing.
+template <int BW, int MINB, int FWD = 0, bool CULL = true>
 __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
 {
     constexpr int S = BW + 1;   // padded strides: threads at one column hit distinct banks
@@ -178,6 +213,7 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
     __shared__ SpanRec sRec[kSlots];
     __shared__ unsigned sMask[2][4][kBinH][kSlots / 32];  // by round parity: rounds alternate buffers
     __shared__ int sWarpSum[kRasterThreads / 32];
+    __shared__ float sQMax[4][kBinH];            // per quarter and row: an upper bound of its depths
     __shared__ int sListBase;
     if (pass_failed(P.status, P.passSeq)) return;
 
@@ -225,6 +261,22 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
         }
     }
     for (int i = tid; i < 2 * 4 * kBinH * (kSlots / 32); i += kRasterThreads) (&sMask[0][0][0][0])[i] = 0u;
+    // Spans are tested for occlusion (span_occluded) in bins of more than
+    // one chunk of triangles, where layers overlap; each thread keeps an
+    // upper bound of its quarter of its row in sQMax.
+    const bool cull = CULL && end - start > kChunk;
+    if (cull) {
+        if (P.clearDepth) {
+            sQMax[warp][lane] = P.depthClearValue;
+        } else {
+            __syncthreads();  // the depth tile is complete
+            const float* dr = sDepth + lane * S + warp * (BW / 4);
+            float m = dr[0];
+#pragma unroll
+            for (int c = 1; c < BW / 4; c++) m = fmaxf(m, dr[c]);
+            sQMax[warp][lane] = m;
+        }
+    }
     int par = 0;  // mask buffer of the current round
 
     unsigned long long tested = 0, passed = 0;
@@ -295,9 +347,22 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
                 Span sp;
                 if (span_row(t, yl, sLw[j], sp)) {
                     int xs = max(sp.leftClamped + ox, x0), xe = min(sp.rightClamped + ox, x0 + cols - 1);
+                    const int sflags = t.edges >> 16;
+                    SpanZ z;
+                    if (xs <= xe) span_z(t, sp, yl, z);
+                    // a span that no depth test can pass is dropped here: no
+                    // per-pixel z, no walk (counted as tested, as the walk would)
+                    if (cull && xs <= xe && (sflags & B_TEST_DEPTH)) {
+                        const int qa = (xs - x0) / Q, qb = (xe - x0) / Q;
+                        float bound = sQMax[qa][r];
+                        for (int q = qa + 1; q <= qb; q++) bound = fmaxf(bound, sQMax[q][r]);
+                        const int k0 = sp.leftClamped + ox;
+                        if (span_occluded(z, xs - k0, xe - k0, bound)) {
+                            tested += (unsigned long long)(xe - xs + 1);
+                            xe = xs - 1;
+                        }
+                    }
                     if (xs <= xe) {
-                        SpanZ z;
-                        span_z(t, sp, yl, z);
                         float cf2 = z.cf2, pz = z.pz;
                         for (int x = sp.leftClamped + ox; x < xs; x++) {
                             cf2 = fadd(cf2, z.cf2Step);
@@ -329,7 +394,7 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
                         R.xs = (short)(xs - x0);
                         R.xe = (short)(xe - x0);
                         R.j = (short)j;
-                        R.flags = (short)(t.edges >> 16);
+                        R.flags = (short)sflags;
                     }
                 }
             }
@@ -415,6 +480,7 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
                         }
                     }
                 }
+                if (cull) sQMax[warp][lane] = curMax;  // for the next round's set-up
             }
             __syncthreads();
             par ^= 1;
@@ -583,16 +649,26 @@ static inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) 
 
 template <int BW> void launch_raster(const PassParams& P, int nBins, cudaStream_t s)
 {
-    if (P.rasterBlocks == 8) k_raster<BW, 8><<<nBins, kRasterThreads, 0, s>>>(P);
-    else k_raster<BW, 1><<<nBins, kRasterThreads, 0, s>>>(P);
+    if (P.rasterBlocks == 8) {
+        if (P.cullSpans) k_raster<BW, 8, 0, true><<<nBins, kRasterThreads, 0, s>>>(P);
+        else k_raster<BW, 8, 0, false><<<nBins, kRasterThreads, 0, s>>>(P);
+    } else {
+        if (P.cullSpans) k_raster<BW, 1, 0, true><<<nBins, kRasterThreads, 0, s>>>(P);
+        else k_raster<BW, 1, 0, false><<<nBins, kRasterThreads, 0, s>>>(P);
+    }
 }
 
 // Forward passes (blending or discarding draws) run with 16-column bins.
 void launch_raster_forward(const PassParams& P, int nBins, cudaStream_t s)
 {
     // the host lays a forward pass's varyings out with stride forward_vary()
-    if (P.nvMax == forward_vary(9)) k_raster<16, 1, 9><<<nBins, kRasterThreads, 0, s>>>(P);
-    else k_raster<16, 1, kMaxVary><<<nBins, kRasterThreads, 0, s>>>(P);
+    if (P.nvMax == forward_vary(9)) {
+        if (P.cullSpans) k_raster<16, 1, 9, true><<<nBins, kRasterThreads, 0, s>>>(P);
+        else k_raster<16, 1, 9, false><<<nBins, kRasterThreads, 0, s>>>(P);
+    } else {
+        if (P.cullSpans) k_raster<16, 1, kMaxVary, true><<<nBins, kRasterThreads, 0, s>>>(P);
+        else k_raster<16, 1, kMaxVary, false><<<nBins, kRasterThreads, 0, s>>>(P);
+    }
 }
 
 void launch_raster(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
@@ -700,6 +776,73 @@ __global__ void k_selftest_wait(int* status, const int* flag, int spins)
         }
         __nanosleep(64);
     }
+}
+
+// Self-test of span_occluded against the per-pixel loop it stands in for:
+// random spans (1/w in [1e-3, 10], z in [-1.2, 1.2] at both ends, up to 4095
+// steps, sometimes a 1/w that crosses zero) and depth bounds placed around
+// the exact pass/fail boundary.  bad[0] counts spans declared occluded that
+// have a pixel passing the depth test (must be 0), bad[1] the spans
+// declared occluded.
+__global__ void k_selftest_occlusion(unsigned seed, unsigned long long n, unsigned long long* bad)
+{
+    const unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    unsigned h = st_hash((unsigned)i * 2654435761u ^ seed);
+    auto uni = [&]() {  // [0, 1)
+        h = st_hash(h + 0x9e3779b9u);
+        return (float)(h >> 8) * 0x1p-24f;
+    };
+    const int kB = 1 + (int)(uni() * uni() * 4094.0f);
+    const int kA = (int)(uni() * (float)(kB + 1)) % (kB + 1);
+    const float C0 = exp2f(-10.0f + 13.3f * uni());
+    float C1 = exp2f(-10.0f + 13.3f * uni());
+    if (uni() < 0.05f) C1 = -C1;  // 1/w through zero: must never be declared occluded wrongly
+    const float z0 = -1.2f + 2.4f * uni(), z1 = uni() < 0.3f ? z0 + (uni() - 0.5f) * 1e-3f : -1.2f + 2.4f * uni();
+    SpanZ z;
+    z.cf2 = C0;
+    z.pz = fmul(z0, C0);
+    z.cf2Step = fdiv(fsub(C1, C0), (float)kB);
+    z.pzStep = fdiv(fsub(fmul(z1, C1), z.pz), (float)kB);
+    // the loop's z values and their minimum over kA..kB
+    float cf2 = z.cf2, pz = z.pz, zmin = INFINITY;
+    for (int k = 0; k <= kB; k++) {
+        float zz = fmul(pz, frcp(cf2));
+        if (k >= kA) zmin = fminf(zmin, zz);
+        cf2 = fadd(cf2, z.cf2Step);
+        pz = fadd(pz, z.pzStep);
+    }
+    if (!isfinite(zmin)) return;
+    // a bound at the boundary (zmin + 1e-4) moved by up to 1e-3 relative, or anywhere
+    float curMax = uni() < 0.7f ? zmin + 0.0001f * (1.0f + (uni() - 0.5f) * 0.002f) : -1.0f + 2.0f * uni();
+    if (!span_occluded(z, kA, kB, curMax)) return;
+    atomicAdd(bad + 1, 1ull);
+    cf2 = z.cf2;
+    pz = z.pz;
+    for (int k = 0; k <= kB; k++) {
+        float zz = fmul(pz, frcp(cf2));
+        if (k >= kA && fsub(zz, curMax) < -0.0001f) {
+            atomicAdd(bad, 1ull);
+            return;
+        }
+        cf2 = fadd(cf2, z.cf2Step);
+        pz = fadd(pz, z.pzStep);
+    }
+}
+
+int selftest_occlusion(unsigned long long cases, unsigned long long* wrong, unsigned long long* occluded)
+{
+    unsigned long long* d = nullptr;
+    if (cudaMalloc(&d, 16) != cudaSuccess) return -1;
+    cudaMemset(d, 0, 16);
+    if (cases) k_selftest_occlusion<<<(unsigned)((cases + 255) / 256), 256>>>(777u, cases, d);
+    unsigned long long h[2];
+    cudaError_t e = cudaMemcpy(h, d, 16, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return -1;
+    *wrong = h[0];
+    *occluded = h[1];
+    return 0;
 }
 
 void launch_selftest_wait(int* status, const int* flag, int spins, cudaStream_t s)

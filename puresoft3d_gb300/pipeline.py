@@ -33,6 +33,8 @@ _SIGS = {
     "ps3d_texture_create_device": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p, _c_int],
     "ps3d_texture_destroy": [_c_void_p, _c_int],
     "ps3d_texture_read": [_c_void_p, _c_int, _c_void_p, _c_size_t],
+    "ps3d_selftest_occlusion": [ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)],
+    "ps3d_set_span_culling": [_c_void_p, _c_int],
     "ps3d_post_process": [_c_void_p, _c_int, _c_void_p, _c_size_t],
     "ps3d_texture_create_layers": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p, _c_int, _c_int],
     "ps3d_texture_write_layer": [_c_void_p, _c_int, _c_int, _c_void_p, _c_size_t],
@@ -113,6 +115,17 @@ def selftest_division(pairs: int = 1 << 28):
     lib = library()
     a, b = ctypes.c_uint64(), ctypes.c_uint64()
     rc = lib.ps3d_selftest_division(pairs, ctypes.byref(a), ctypes.byref(b))
+    if rc < 0:
+        raise RuntimeError(lib.ps3d_last_error().decode())
+    return int(a.value), int(b.value)
+
+
+def selftest_occlusion(cases: int = 1 << 22):
+    """(spans wrongly declared occluded, spans declared occluded) of the
+    raster's span occlusion test against the per-pixel loop."""
+    lib = library()
+    a, b = ctypes.c_uint64(), ctypes.c_uint64()
+    rc = lib.ps3d_selftest_occlusion(cases, ctypes.byref(a), ctypes.byref(b))
     if rc < 0:
         raise RuntimeError(lib.ps3d_last_error().decode())
     return int(a.value), int(b.value)
@@ -263,6 +276,11 @@ class PuresoftPipeline:
     def setRasterOccupancy(self, blocks_per_sm: int):
         """Raster kernel variant: 0 (registers as needed) or 8 blocks per SM."""
         self._check(self.lib.ps3d_set_raster_occupancy(self.h, blocks_per_sm))
+
+    def setSpanCulling(self, on: bool):
+        """Raster kernel variant: drop occluded spans before their depths are
+        computed (on, the default) or not."""
+        self._check(self.lib.ps3d_set_span_culling(self.h, int(bool(on))))
 
     def selftestWait(self, spins: int) -> float:
         """Runs a bounded wait that must run out; raises TimeoutError (with

@@ -1,5 +1,5 @@
 """The schedule autotuner's selection and cache logic, on a fake pipeline
-whose frame time depends on the bin width (no GPU)."""
+whose frame time depends on the schedule (no GPU)."""
 import json
 
 from puresoft3d_gb300.autotune import Autotuner
@@ -22,6 +22,7 @@ class _FakePipe:
     def __init__(self):
         self.bw = 32
         self.occ = 0
+        self.cull = 1
         self.submits = 0
         self.recorded = 0
 
@@ -32,6 +33,9 @@ class _FakePipe:
     def setRasterOccupancy(self, o):
         assert o in (0, 8)
         self.occ = o
+
+    def setSpanCulling(self, on):
+        self.cull = int(on)
 
     def beginCommands(self):
         pass
@@ -49,7 +53,7 @@ class _FakePipe:
         pass
 
     def timerEnd(self):
-        return self.COST[self.bw] - (0.25 if self.occ == 8 else 0.0)
+        return self.COST[self.bw] - (0.25 if self.occ == 8 else 0.0) - (0.125 if self.cull == 0 else 0.0)
 
 
 def _record(pipe):
@@ -60,27 +64,27 @@ def test_picks_fastest_and_sets_it(tmp_path):
     t = Autotuner(cache_path=str(tmp_path / "tune.json"))
     p = _FakePipe()
     best, ms = t.tune(p, _record, key="w1", candidates=(8, 16, 32))
-    assert best == (16, 0) and p.bw == 16
-    assert ms == {"8/0": 3.0, "16/0": 1.5, "32/0": 2.0}
+    assert best == (16, 0, 1) and p.bw == 16
+    assert ms == {"8/0/1": 3.0, "16/0/1": 1.5, "32/0/1": 2.0}
     assert p.recorded == 3
 
 
-def test_pairs_of_width_and_occupancy(tmp_path):
+def test_triples_of_width_occupancy_and_culling(tmp_path):
     t = Autotuner(cache_path=str(tmp_path / "tune.json"))
     p = _FakePipe()
     best, ms = t.tune(p, _record, key="w1")
-    assert best == (16, 8) and (p.bw, p.occ) == (16, 8)
-    assert len(ms) == 6 and p.recorded == 6
+    assert best == (16, 8, 0) and (p.bw, p.occ, p.cull) == (16, 8, 0)
+    assert len(ms) == 12 and p.recorded == 12
 
 
 def test_cache_is_reused_and_keyed(tmp_path):
     path = str(tmp_path / "tune.json")
     Autotuner(cache_path=path).tune(_FakePipe(), _record, key="w1")
     table = json.load(open(path))
-    assert len(table) == 1 and list(table.values())[0]["best"] == [16, 8]
+    assert len(table) == 1 and list(table.values())[0]["best"] == [16, 8, 0]
     p = _FakePipe()
     best, _ = Autotuner(cache_path=path).tune(p, _record, key="w1")
-    assert best == (16, 8) and p.bw == 16 and p.recorded == 0  # from the cache, nothing timed
+    assert best == (16, 8, 0) and p.bw == 16 and p.cull == 0 and p.recorded == 0  # from the cache, nothing timed
     p2 = _FakePipe()
     Autotuner(cache_path=path).tune(p2, _record, key="w2", candidates=(8, 32))
     assert p2.bw == 32 and p2.recorded == 2
@@ -92,4 +96,4 @@ def test_retune_ignores_cache(tmp_path):
     Autotuner(cache_path=path).tune(_FakePipe(), _record, key="w1")
     p = _FakePipe()
     Autotuner(cache_path=path).tune(p, _record, key="w1", retune=True)
-    assert p.recorded == 6
+    assert p.recorded == 12

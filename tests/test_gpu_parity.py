@@ -63,17 +63,19 @@ def test_bin_capacity_replay(gpu_lib, monkeypatch, case):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("cull", [1, 0])
 @pytest.mark.parametrize("occupancy", [0, 8])
 @pytest.mark.parametrize("bin_w", [8, 16, 32])
-@pytest.mark.parametrize("case", ["kat_soup_depth", "c3_small"])
-def test_schedules_agree(gpu_lib, bin_w, occupancy, case):
-    """Every schedule (bin width x raster kernel variant) gives the oracle's
-    result."""
+@pytest.mark.parametrize("case", ["kat_soup_depth", "c3_small", "kat_post_add_fog"])
+def test_schedules_agree(gpu_lib, bin_w, occupancy, cull, case):
+    """Every schedule (bin width x raster kernel variants: occupancy, span
+    culling) gives the oracle's result."""
     from puresoft3d_gb300.pipeline import PuresoftPipeline
     name, scene = [c for c in CASES if c[0].startswith(case)][0]
     g = PuresoftPipeline(scene.width, scene.height)
     g.setBinWidth(bin_w)
     g.setRasterOccupancy(occupancy)
+    g.setSpanCulling(cull)
     assert g.binWidth() == bin_w
     out = render(g, scene)
     ref = render(OraclePipeline(scene.width, scene.height), scene)
@@ -230,3 +232,15 @@ def test_post_process_arguments(gpu_lib):
     img = p.readColour()
     assert (img.reshape(-1, 4) == np.array([0, 0, 0, 2], dtype=np.uint8)).all()  # 255 + 1 wraps; alpha 1 + 1
     p.close()
+
+
+@pytest.mark.gpu
+def test_span_occlusion_is_conservative(gpu_lib):
+    """The raster drops a span before computing its depths when no pixel
+    can pass the depth test; on random spans with depth bounds at the
+    pass/fail boundary it never drops one with a passing pixel, and does
+    drop many."""
+    from puresoft3d_gb300.pipeline import selftest_occlusion
+    wrong, dropped = selftest_occlusion(1 << 22)
+    assert wrong == 0
+    assert dropped > (1 << 22) // 20
