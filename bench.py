@@ -214,11 +214,12 @@ def autotune(pipe, record, key, args):
         pipe.setBinWidth(args.bin_width)
         pipe.setRasterOccupancy(args.raster_occupancy)
         pipe.setSpanCulling(args.span_culling)
+        pipe.setRowSplit(args.row_split)
         return {"bin_width": args.bin_width, "raster_occupancy": args.raster_occupancy,
-                "span_culling": args.span_culling, "source": "flags"}
+                "span_culling": args.span_culling, "row_split": args.row_split, "source": "flags"}
     best, ms = Autotuner().tune(pipe, record, key, reps=3)
-    return {"bin_width": best[0], "raster_occupancy": best[1], "span_culling": best[2], "source": "autotuner",
-            "candidate_ms": {k: round(v, 4) for k, v in ms.items()}}
+    return {"bin_width": best[0], "raster_occupancy": best[1], "span_culling": best[2], "row_split": best[3],
+            "source": "autotuner", "candidate_ms": {k: round(v, 4) for k, v in ms.items()}}
 
 
 def run_c4(args):
@@ -472,6 +473,7 @@ def run_frames_only(args):
         pipe.setBinWidth(args.bin_width)
         pipe.setRasterOccupancy(args.raster_occupancy)
         pipe.setSpanCulling(args.span_culling)
+        pipe.setRowSplit(args.row_split)
     for _ in range(args.ncu_frames):
         S.replay_frame(scene, pipe)
         pipe.finish()
@@ -791,6 +793,8 @@ def main():
     ap.add_argument("--raster-occupancy", type=int, default=0, choices=[0, 8])
     ap.add_argument("--span-culling", type=int, default=1, choices=[0, 1],
                     help="with --bin-width: raster variant with (1) or without (0) the span occlusion test")
+    ap.add_argument("--row-split", type=int, default=1, choices=[1, 2, 4, 8],
+                    help="with --bin-width: raster blocks per bin (crowded bins shared out by rows)")
     args = ap.parse_args()
     if args.ncu_frames:
         run_frames_only(args)

@@ -237,6 +237,12 @@ int ps3d_get_bin_width(ps3d_pipeline* p, int* columns);
  * so results are unchanged); off leaves the test out of the kernel.  The
  * autotuner times both. */
 int ps3d_set_span_culling(ps3d_pipeline* p, int on);
+/* Raster blocks per bin: 1 (the default), 2, 4 or 8.  With more than one, a
+ * bin holding more than 256 triangles is shared out by rows between its
+ * blocks (each takes 32 / n rows), so that a few crowded bins do not hold
+ * up the launch; other bins are done whole.  Time only, never results; the
+ * autotuner times 1 and 4. */
+int ps3d_set_row_split(ps3d_pipeline* p, int blocksPerBin);
 /* Second schedule knob: the raster kernel variant.  0 lets each thread use
  * the registers it wants (fewer resident blocks); 8 caps registers so that
  * 8 blocks fit per SM where shared memory allows (more warps to hide

@@ -1,7 +1,7 @@
 """Schedule autotuner for the device passes.
 
-A schedule is a triple (bin width, raster occupancy, span culling).  The bin
-width (8, 16 or
+A schedule is (bin width, raster occupancy, span culling, row split).  The
+bin width (8, 16 or
 32 columns; bins are always 32 rows) sets how the raster kernel's work is
 cut:
 
@@ -18,7 +18,9 @@ the registers it wants, 8 caps them so that up to 8 blocks are resident per
 SM (more warps to hide latency, less room per thread).  Span culling (1)
 drops spans that cannot pass the depth test before their depths are
 computed, in crowded bins: it pays off with depth complexity and costs a
-little elsewhere.
+little elsewhere.  The row split (1 or 4 raster blocks per bin) shares the
+rows of crowded bins out between blocks: it pays off when a few crowded
+bins would otherwise run alone at the end of the launch.
 
 Which schedule wins depends on the workload (triangle sizes, depth complexity,
 target size), so the tuner times every candidate on the caller's own frame:
@@ -37,28 +39,33 @@ import os
 import statistics
 from typing import Callable, Dict, Optional, Sequence, Tuple
 
-CANDIDATES = tuple((bw, occ, cull) for bw in (8, 16, 32) for occ in (0, 8) for cull in (1, 0))
+CANDIDATES = tuple((bw, occ, cull, split) for bw in (8, 16, 32) for occ in (0, 8) for cull in (1, 0)
+                   for split in (1, 4))
 
 
 def _sched(c):
-    """(bin width, occupancy, span culling) of a candidate given as a bare
-    width, a pair or a triple (occupancy 0 and culling on by default)."""
+    """(bin width, occupancy, span culling, row split) of a candidate given
+    as a bare width or a shorter tuple (occupancy 0, culling on and one block
+    per bin by default)."""
     if not isinstance(c, (tuple, list)):
-        return (int(c), 0, 1)
-    return (int(c[0]), int(c[1]) if len(c) > 1 else 0, int(c[2]) if len(c) > 2 else 1)
+        c = (c,)
+    d = (None, 0, 1, 1)
+    return tuple(int(c[i]) if i < len(c) else d[i] for i in range(4))
 
 
 def _name(c) -> str:
-    return "%d/%d/%d" % _sched(c)
+    return "%d/%d/%d/%d" % _sched(c)
 
 
 def apply(pipe, c) -> None:
-    bw, occ, cull = _sched(c)
+    bw, occ, cull, split = _sched(c)
     pipe.setBinWidth(bw)
     if hasattr(pipe, "setRasterOccupancy"):
         pipe.setRasterOccupancy(occ)
     if hasattr(pipe, "setSpanCulling"):
         pipe.setSpanCulling(cull)
+    if hasattr(pipe, "setRowSplit"):
+        pipe.setRowSplit(split)
 
 
 def _default_cache() -> str:
@@ -125,12 +132,12 @@ class Autotuner:
 
     def tune(self, pipe, record: Callable[[object], None], key: str,
              candidates: Sequence = CANDIDATES, reps: int = 5, warmup: int = 2,
-             retune: bool = False) -> Tuple[Tuple[int, int, int], Dict[str, float]]:
+             retune: bool = False) -> Tuple[Tuple[int, int, int, int], Dict[str, float]]:
         """Sets `pipe`'s schedule to the fastest candidate for `record`'s
-        frame and returns ((bin width, raster occupancy, span culling),
-        {"bw/occ/cull": median ms}).  A candidate is such a triple, a (bin
-        width, occupancy) pair or a bare bin width.  A cached result for
-        (key, device, candidates) is reused unless `retune`."""
+        frame and returns ((bin width, raster occupancy, span culling, row
+        split), {"bw/occ/cull/split": median ms}).  A candidate is such a
+        tuple, a shorter prefix of it or a bare bin width.  A cached result
+        for (key, device, candidates) is reused unless `retune`."""
         full = "%s|%s|%s" % (key, device_name(), ",".join(_name(c) for c in candidates))
         hit = self.table.get(full)
         if hit and not retune:

@@ -224,6 +224,7 @@ struct ps3d_pipeline {
     int binW = 32;
     int rasterBlocks = 0;
     int cullSpans = 1;
+    int rowSplit = 1;
     bool countFrags = false;
     cudaStream_t stream = nullptr;
     bool ownStream = false;
@@ -750,6 +751,7 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     P.binW = binW;
     P.rasterBlocks = p->rasterBlocks;
     P.cullSpans = p->cullSpans;
+    P.rowSplit = p->rowSplit;
     P.passFp = pass_fp(dd.data(), dd.size());
     P.forward = forward;
     P.binsX = binsX;
@@ -1542,6 +1544,15 @@ int ps3d_set_bin_width(ps3d_pipeline* p, int columns)
     return 0;
 }
 
+int ps3d_set_row_split(ps3d_pipeline* p, int blocksPerBin)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    if (blocksPerBin != 1 && blocksPerBin != 2 && blocksPerBin != 4 && blocksPerBin != 8)
+        return fail(PS3D_ERR_INVALID, "blocks per bin must be 1, 2, 4 or 8");
+    p->rowSplit = blocksPerBin;
+    return 0;
+}
+
 int ps3d_set_span_culling(ps3d_pipeline* p, int on)
 {
     if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
@@ -2106,6 +2117,7 @@ int noalloc_run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const P
     P.binW = s.binW;
     P.rasterBlocks = p->rasterBlocks;
     P.cullSpans = p->cullSpans;
+    P.rowSplit = p->rowSplit;
     P.passFp = pass_fp(g_noallocDraws, (size_t)s.nd);
     P.forward = s.forward;
     P.binsX = s.binsX;

@@ -93,6 +93,7 @@ struct PassParams {
     int binW, binsX, binsY;   // bins of kBinH x binW pixels
     int rasterBlocks;         // raster variant: 0 = registers as needed, 8 = capped for 8 blocks per SM
     int cullSpans;            // raster variant: 1 = occluded spans dropped in crowded bins
+    int rowSplit;             // raster blocks per bin (1, 2, 4 or 8): crowded bins shared out by rows
     int passFp;               // the fragment processor every colour draw of the pass uses, else 0
     int forward;              // some draw blends or may discard: shade every passing fragment in order
     int nTris, nDraws;

@@ -186,6 +186,7 @@ __device__ __forceinline__ bool span_occluded(const SpanZ& z, int kA, int kB, fl
 constexpr int kRasterThreads = 128;  // 4 warps: warp = column quarter, lane = bin row
 constexpr int kChunk = 128;          // triangles per chunk (one per thread)
 constexpr int kSlots = 128;          // (triangle, row) spans per round (one per thread)
+constexpr int kSplitMin = 2 * kChunk;  // triangles above which a bin is shared out by rows
 
 // FWD (forward mode, 9 or 16 varyings): for passes that blend or may
 // discard, every fragment that passes the depth test is shaded in the walk,
@@ -217,7 +218,13 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
     __shared__ int sListBase;
     if (pass_failed(P.status, P.passSeq)) return;
 
-    const int bin = blockIdx.x;
+    // Row slices: with P.rowSplit > 1, each bin has that many blocks; a bin
+    // with more than kSplitMin triangles is shared out by rows (block s takes
+    // rows [s R, s R + R), R = 32 / rowSplit: fewer spans per block, so a
+    // crowded bin no longer holds up the launch alone); other bins are done
+    // whole by their first block.
+    const int split = P.rowSplit;
+    const int bin = blockIdx.x / split, slice = blockIdx.x - bin * split;
     const int bx = bin % P.binsX, by = bin / P.binsX;
     const int x0 = bx * BW, y0 = by * kBinH;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -225,6 +232,17 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
     const int rows = min(kBinH, P.H - y0);
     int start, end;
     bin_range(P, bin, start, end);
+    int rowBeg = 0, rowEnd = rows;
+    if (split > 1) {
+        if (end - start > kSplitMin) {
+            const int R = kBinH / split;
+            rowBeg = slice * R;
+            rowEnd = min(rowBeg + R, rows);
+            if (rowBeg >= rowEnd) return;
+        } else if (slice) {
+            return;
+        }
+    }
 
     if (start == end) {
         if (P.clearDepth || P.clearColour)
@@ -249,13 +267,13 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
     for (int i = tid; i < kBinH * BW; i += kRasterThreads) {
         int r = i / BW, c = i - r * BW;
         float d = P.depthClearValue;
-        if (!P.clearDepth && r < rows && c < cols) d = P.depth[(size_t)(y0 + r) * P.depthScan + x0 + c];
+        if (!P.clearDepth && r >= rowBeg && r < rowEnd && c < cols) d = P.depth[(size_t)(y0 + r) * P.depthScan + x0 + c];
         sDepth[r * S + c] = d;
         sWin[r * S + c] = -1;
         if constexpr (FWD > 0) {
             uint32_t col = P.colourClearValue;
             int x = x0 + c, y = y0 + r;
-            if (!P.clearColour && r < rows && c < cols && x < P.colourW && y < P.colourH)
+            if (!P.clearColour && r >= rowBeg && r < rowEnd && c < cols && x < P.colourW && y < P.colourH)
                 col = ((const uint32_t*)P.colour)[(size_t)(P.colourH - 1 - y) * P.colourW + x];
             sCol[r * S + c] = col;
         }
@@ -296,8 +314,8 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
             sOx[tid] = (short)dd.vpX;
             sOy[tid] = (short)oy;
             sLw[tid] = (short)dd.vpW;
-            r0 = max((int)sTri[tid].firstRow + oy - y0, 0);
-            int r1 = min((int)sTri[tid].lastRow + oy - y0, rows - 1);
+            r0 = max((int)sTri[tid].firstRow + oy - y0, rowBeg);
+            int r1 = min((int)sTri[tid].lastRow + oy - y0, rowEnd - 1);
             if (r0 <= r1) cnt = r1 - r0 + 1;
         }
         recTid = nextIdx;  // prefetch the next chunk while this one is processed
@@ -405,7 +423,7 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
             // pass (z >= zmin >= every current depth here + epsilon) is skipped:
             // with TEST_DEPTH on, depth only decreases, so curMax stays an
             // upper bound and the skip never changes a result.
-            if (lane < rows) {
+            if (lane >= rowBeg && lane < rowEnd) {
                 float curMax = dRow[qs];
 #pragma unroll
                 for (int c = 1; c < Q; c++) curMax = fmaxf(curMax, dRow[qs + c]);
@@ -488,15 +506,16 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
     }
     // depth write-back; count of covered pixels per thread
     int covered = 0;
-    for (int i = tid; i < rows * cols; i += kRasterThreads) {
-        int r = i / cols, c = i - r * cols;
+    const int nr = rowEnd - rowBeg;
+    for (int i = tid; i < nr * cols; i += kRasterThreads) {
+        int r = rowBeg + i / cols, c = i - (r - rowBeg) * cols;
         P.depth[(size_t)(y0 + r) * P.depthScan + x0 + c] = sDepth[r * S + c];
         covered += sWin[r * S + c] >= 0;
     }
     if constexpr (FWD > 0) {
         if (P.anyColour || P.clearColour)
-            for (int i = tid; i < rows * cols; i += kRasterThreads) {
-                int r = i / cols, c = i - r * cols, x = x0 + c, y = y0 + r;
+            for (int i = tid; i < nr * cols; i += kRasterThreads) {
+                int r = rowBeg + i / cols, c = i - (r - rowBeg) * cols, x = x0 + c, y = y0 + r;
                 if (x < P.colourW && y < P.colourH)
                     ((uint32_t*)P.colour)[(size_t)(P.colourH - 1 - y) * P.colourW + x] = sCol[r * S + c];
             }
@@ -524,8 +543,8 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
         }
         __syncthreads();
         int pos = sListBase + sWarpSum[warp] + inc - covered;
-        for (int i = tid; i < rows * cols; i += kRasterThreads) {
-            int r = i / cols, c = i - r * cols;
+        for (int i = tid; i < nr * cols; i += kRasterThreads) {
+            int r = rowBeg + i / cols, c = i - (r - rowBeg) * cols;
             int w = sWin[r * S + c];
             if (w >= 0) {
                 if (P.anyColour) P.shadeList[pos++] = make_int2((y0 + r) * P.W + x0 + c, w);
@@ -650,11 +669,11 @@ static inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) 
 template <int BW> void launch_raster(const PassParams& P, int nBins, cudaStream_t s)
 {
     if (P.rasterBlocks == 8) {
-        if (P.cullSpans) k_raster<BW, 8, 0, true><<<nBins, kRasterThreads, 0, s>>>(P);
-        else k_raster<BW, 8, 0, false><<<nBins, kRasterThreads, 0, s>>>(P);
+        if (P.cullSpans) k_raster<BW, 8, 0, true><<<nBins * P.rowSplit, kRasterThreads, 0, s>>>(P);
+        else k_raster<BW, 8, 0, false><<<nBins * P.rowSplit, kRasterThreads, 0, s>>>(P);
     } else {
-        if (P.cullSpans) k_raster<BW, 1, 0, true><<<nBins, kRasterThreads, 0, s>>>(P);
-        else k_raster<BW, 1, 0, false><<<nBins, kRasterThreads, 0, s>>>(P);
+        if (P.cullSpans) k_raster<BW, 1, 0, true><<<nBins * P.rowSplit, kRasterThreads, 0, s>>>(P);
+        else k_raster<BW, 1, 0, false><<<nBins * P.rowSplit, kRasterThreads, 0, s>>>(P);
     }
 }
 
@@ -663,11 +682,11 @@ void launch_raster_forward(const PassParams& P, int nBins, cudaStream_t s)
 {
     // the host lays a forward pass's varyings out with stride forward_vary()
     if (P.nvMax == forward_vary(9)) {
-        if (P.cullSpans) k_raster<16, 1, 9, true><<<nBins, kRasterThreads, 0, s>>>(P);
-        else k_raster<16, 1, 9, false><<<nBins, kRasterThreads, 0, s>>>(P);
+        if (P.cullSpans) k_raster<16, 1, 9, true><<<nBins * P.rowSplit, kRasterThreads, 0, s>>>(P);
+        else k_raster<16, 1, 9, false><<<nBins * P.rowSplit, kRasterThreads, 0, s>>>(P);
     } else {
-        if (P.cullSpans) k_raster<16, 1, kMaxVary, true><<<nBins, kRasterThreads, 0, s>>>(P);
-        else k_raster<16, 1, kMaxVary, false><<<nBins, kRasterThreads, 0, s>>>(P);
+        if (P.cullSpans) k_raster<16, 1, kMaxVary, true><<<nBins * P.rowSplit, kRasterThreads, 0, s>>>(P);
+        else k_raster<16, 1, kMaxVary, false><<<nBins * P.rowSplit, kRasterThreads, 0, s>>>(P);
     }
 }
 

@@ -35,6 +35,7 @@ _SIGS = {
     "ps3d_texture_read": [_c_void_p, _c_int, _c_void_p, _c_size_t],
     "ps3d_selftest_occlusion": [ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)],
     "ps3d_set_span_culling": [_c_void_p, _c_int],
+    "ps3d_set_row_split": [_c_void_p, _c_int],
     "ps3d_post_process": [_c_void_p, _c_int, _c_void_p, _c_size_t],
     "ps3d_texture_create_layers": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p, _c_int, _c_int],
     "ps3d_texture_write_layer": [_c_void_p, _c_int, _c_int, _c_void_p, _c_size_t],
@@ -276,6 +277,10 @@ class PuresoftPipeline:
     def setRasterOccupancy(self, blocks_per_sm: int):
         """Raster kernel variant: 0 (registers as needed) or 8 blocks per SM."""
         self._check(self.lib.ps3d_set_raster_occupancy(self.h, blocks_per_sm))
+
+    def setRowSplit(self, blocks_per_bin: int):
+        """Raster blocks per bin (1, 2, 4 or 8): crowded bins shared out by rows."""
+        self._check(self.lib.ps3d_set_row_split(self.h, blocks_per_bin))
 
     def setSpanCulling(self, on: bool):
         """Raster kernel variant: drop occluded spans before their depths are

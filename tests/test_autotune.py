@@ -23,6 +23,7 @@ class _FakePipe:
         self.bw = 32
         self.occ = 0
         self.cull = 1
+        self.split = 1
         self.submits = 0
         self.recorded = 0
 
@@ -36,6 +37,10 @@ class _FakePipe:
 
     def setSpanCulling(self, on):
         self.cull = int(on)
+
+    def setRowSplit(self, n):
+        assert n in (1, 2, 4, 8)
+        self.split = n
 
     def beginCommands(self):
         pass
@@ -53,7 +58,8 @@ class _FakePipe:
         pass
 
     def timerEnd(self):
-        return self.COST[self.bw] - (0.25 if self.occ == 8 else 0.0) - (0.125 if self.cull == 0 else 0.0)
+        return (self.COST[self.bw] - (0.25 if self.occ == 8 else 0.0) - (0.125 if self.cull == 0 else 0.0)
+                - (0.0625 if self.split == 4 else 0.0))
 
 
 def _record(pipe):
@@ -64,27 +70,27 @@ def test_picks_fastest_and_sets_it(tmp_path):
     t = Autotuner(cache_path=str(tmp_path / "tune.json"))
     p = _FakePipe()
     best, ms = t.tune(p, _record, key="w1", candidates=(8, 16, 32))
-    assert best == (16, 0, 1) and p.bw == 16
-    assert ms == {"8/0/1": 3.0, "16/0/1": 1.5, "32/0/1": 2.0}
+    assert best == (16, 0, 1, 1) and p.bw == 16
+    assert ms == {"8/0/1/1": 3.0, "16/0/1/1": 1.5, "32/0/1/1": 2.0}
     assert p.recorded == 3
 
 
-def test_triples_of_width_occupancy_and_culling(tmp_path):
+def test_width_occupancy_culling_and_split(tmp_path):
     t = Autotuner(cache_path=str(tmp_path / "tune.json"))
     p = _FakePipe()
     best, ms = t.tune(p, _record, key="w1")
-    assert best == (16, 8, 0) and (p.bw, p.occ, p.cull) == (16, 8, 0)
-    assert len(ms) == 12 and p.recorded == 12
+    assert best == (16, 8, 0, 4) and (p.bw, p.occ, p.cull, p.split) == (16, 8, 0, 4)
+    assert len(ms) == 24 and p.recorded == 24
 
 
 def test_cache_is_reused_and_keyed(tmp_path):
     path = str(tmp_path / "tune.json")
     Autotuner(cache_path=path).tune(_FakePipe(), _record, key="w1")
     table = json.load(open(path))
-    assert len(table) == 1 and list(table.values())[0]["best"] == [16, 8, 0]
+    assert len(table) == 1 and list(table.values())[0]["best"] == [16, 8, 0, 4]
     p = _FakePipe()
     best, _ = Autotuner(cache_path=path).tune(p, _record, key="w1")
-    assert best == (16, 8, 0) and p.bw == 16 and p.cull == 0 and p.recorded == 0  # from the cache, nothing timed
+    assert best == (16, 8, 0, 4) and p.bw == 16 and p.cull == 0 and p.split == 4 and p.recorded == 0  # from the cache
     p2 = _FakePipe()
     Autotuner(cache_path=path).tune(p2, _record, key="w2", candidates=(8, 32))
     assert p2.bw == 32 and p2.recorded == 2
@@ -96,4 +102,4 @@ def test_retune_ignores_cache(tmp_path):
     Autotuner(cache_path=path).tune(_FakePipe(), _record, key="w1")
     p = _FakePipe()
     Autotuner(cache_path=path).tune(p, _record, key="w1", retune=True)
-    assert p.recorded == 12
+    assert p.recorded == 24

@@ -63,19 +63,21 @@ def test_bin_capacity_replay(gpu_lib, monkeypatch, case):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("split", [1, 2, 4, 8])
 @pytest.mark.parametrize("cull", [1, 0])
 @pytest.mark.parametrize("occupancy", [0, 8])
 @pytest.mark.parametrize("bin_w", [8, 16, 32])
-@pytest.mark.parametrize("case", ["kat_soup_depth", "c3_small", "kat_post_add_fog"])
-def test_schedules_agree(gpu_lib, bin_w, occupancy, cull, case):
+@pytest.mark.parametrize("case", ["kat_soup_depth", "c3_small", "kat_post_add_fog", "kat_alphatest_blend"])
+def test_schedules_agree(gpu_lib, bin_w, occupancy, cull, split, case):
     """Every schedule (bin width x raster kernel variants: occupancy, span
-    culling) gives the oracle's result."""
+    culling, row split) gives the oracle's result."""
     from puresoft3d_gb300.pipeline import PuresoftPipeline
     name, scene = [c for c in CASES if c[0].startswith(case)][0]
     g = PuresoftPipeline(scene.width, scene.height)
     g.setBinWidth(bin_w)
     g.setRasterOccupancy(occupancy)
     g.setSpanCulling(cull)
+    g.setRowSplit(split)
     assert g.binWidth() == bin_w
     out = render(g, scene)
     ref = render(OraclePipeline(scene.width, scene.height), scene)
