@@ -85,6 +85,17 @@ extern "C" {
 #define PS3D_VP_DEF04 0x0401
 #define PS3D_IP_DEF04 0x0402
 #define PS3D_FP_DEF04 0x0403
+/* The reference demo's planet processors (src/test/testproc.cpp): VBO slots
+ * as DEF03; uniforms 3-5 as DEF01, 16 the shadow projection (world -> the
+ * shadow map's [0, 1] texture space, z compared with the stored depth), 7
+ * light, 8 camera; textures by index at 9 diffuse, 10 bump, 15 shadow map
+ * (FP32) and, for Earth, 11 specular (red scales the highlight) and 12
+ * night (added where lambert < 0.2).  The shadow factor is the reference's
+ * 4-tap Poisson projective lookup (samplrproj.cpp:20-38). */
+#define PS3D_VP_PLANET 0x0701
+#define PS3D_IP_PLANET 0x0702
+#define PS3D_FP_EARTH 0x0703
+#define PS3D_FP_SATELLITE 0x0713
 #define PS3D_VP_DEF05 0x0501
 #define PS3D_IP_DEF05 0x0502
 #define PS3D_FP_DEF05 0x0503

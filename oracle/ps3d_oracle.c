@@ -58,6 +58,7 @@ enum {
     VP_DEF04 = 0x0401, IP_DEF04 = 0x0402, FP_DEF04 = 0x0403,
     VP_DEF05 = 0x0501, IP_DEF05 = 0x0502, FP_DEF05 = 0x0503,
     VP_SHADOW = 0x0601,
+    VP_PLANET = 0x0701, IP_PLANET = 0x0702, FP_EARTH = 0x0703, FP_SATELLITE = 0x0713,
     FP_LIT1 = 0x1103, FP_LIT1A = 0x1403, FP_LIT3 = 0x1303,
     VP_LIT2 = 0x1201, IP_LIT2 = 0x1202, FP_LIT2 = 0x1203
 };
@@ -303,6 +304,7 @@ static int known_processor(int id)
     case VP_DEF01: case IP_DEF01: case FP_DEF01: case VP_DEF05: case IP_DEF05: case FP_DEF05:
     case VP_DEF02: case IP_DEF02: case FP_DEF02: case VP_DEF03: case IP_DEF03: case FP_DEF03:
     case VP_DEF04: case IP_DEF04: case FP_DEF04:
+    case VP_PLANET: case IP_PLANET: case FP_EARTH: case FP_SATELLITE:
     case VP_SHADOW: case FP_LIT1: case FP_LIT1A: case FP_LIT3: case VP_LIT2: case IP_LIT2: case FP_LIT2:
         return 1;
     }
@@ -509,6 +511,8 @@ static int ip_vecs(int ip)
     case IP_DEF02: return 3; /* PROCDATA_DEF02: normal, worldPos, colour (colr1light1.h:3-9) */
     case IP_DEF03: return 5; /* PROCDATA_DEF03: tangent, binormal, normal, worldPos, texcoord (tex1bump1light1.h:4-11) */
     case IP_DEF04: return 1; /* PROCDATA_DEF04: direction (skybox.h:3-7) */
+    case IP_PLANET: return 6; /* PROCDATA_PLANET: tangent, binormal, normal, worldPos, texcoord, shadowcoord
+                                 (test/testproc.h:5-14) */
     default: return 0;       /* IP_DEF05: no varyings (shadow.h) */
     }
 }
@@ -561,6 +565,23 @@ static void run_vp(const ps3do* p, const void* const* in, float* pos, float* use
         for (int k = 12; k < 16; k++) inv[k] = 0.0f;
         m4v4(user, inv, d);
         memcpy(pos, v, 16);
+        break;
+    }
+    case VP_PLANET: { /* test/testproc.cpp:37-71: DEF03's outputs plus the world
+                         position through the shadow projection (uniform 16) */
+        float* tan = user, * bin = user + 4, * nrm = user + 8, * wp = user + 12, * tc = user + 16, * sc = user + 20;
+        const float* uv = (const float*)in[4];
+        m4v4(wp, ufl(p, 4), (const float*)in[0]);
+        m4v4(sc, ufl(p, 16), wp);
+        memcpy(pos, wp, 16);
+        m4v4(pos, ufl(p, 3), pos);
+        wp[3] = 0;
+        m4v4(tan, ufl(p, 5), (const float*)in[1]);
+        m4v4(bin, ufl(p, 5), (const float*)in[2]);
+        m4v4(nrm, ufl(p, 5), (const float*)in[3]);
+        tc[0] = uv[0];
+        tc[1] = uv[1];
+        tc[2] = tc[3] = 0.0f; /* left unset by the reference; never read */
         break;
     }
     case VP_DEF03: { /* tex1bump1light1.cpp:22-46 */
@@ -633,13 +654,20 @@ static void ip_calc_step(int nv, float* step, const float* start, const float* e
     for (int i = 0; i < 4 * nv; i++) step[i] = (end[i] - start[i]) * r;
 }
 
-static void ip_step_forward(int nv, float* start, const float* step, int n)
+/* The step vector stepForward adds to vector k: its own, except in the
+   demo's IP_Planet, which steps the tangent and the binormal by the normal's
+   step (test/testproc.cpp:171-195). */
+static int step_src(int ip, int k) { return (ip == IP_PLANET && k < 2) ? 2 : k; }
+
+static void ip_step_forward(int ip, int nv, float* start, const float* step, int n)
 {
-    if (1 == n)
-        for (int i = 0; i < 4 * nv; i++) start[i] = start[i] + step[i];
-    else {
+    if (1 == n) {
+        for (int k = 0; k < nv; k++)
+            for (int l = 0; l < 4; l++) start[4 * k + l] = start[4 * k + l] + step[4 * step_src(ip, k) + l];
+    } else {
         float fn = (float)n;
-        for (int i = 0; i < 4 * nv; i++) start[i] = start[i] + step[i] * fn;
+        for (int k = 0; k < nv; k++)
+            for (int l = 0; l < 4; l++) start[4 * k + l] = start[4 * k + l] + step[4 * step_src(ip, k) + l] * fn;
     }
 }
 
@@ -660,6 +688,7 @@ typedef struct {
     const o_fbo* tex;
     const o_fbo* tex2;  /* DEF03's bump map */
     const o_fbo* cube;  /* DEF04's cube map */
+    const o_fbo* spec, * night, * proj; /* the planet set's specular, night and shadow maps */
     sr_level chainA[MAX_LEVELS], chainN[MAX_LEVELS];
     int levelsA, levelsN;
     const float* shadow;
@@ -679,6 +708,31 @@ static int fp_prepare(const ps3do* p, fp_state* s)
         s->light = ufl(p, 7);
         s->cam = ufl(p, 8);
         s->tex = p->tex[t];
+        break;
+    }
+    case FP_EARTH:     /* test/testproc.cpp:197-206 */
+    case FP_SATELLITE: { /* test/testproc.cpp:290-297 */
+        const int slots[5] = {9, 10, 11, 12, 15};
+        const o_fbo* t[5];
+        int n = p->fp == FP_EARTH ? 5 : 3;
+        for (int i = 0; i < 5; i++) {
+            int slot = (p->fp == FP_SATELLITE && i >= 2) ? 15 : slots[i];
+            int k = *uin(p, slot);
+            if (i >= n && p->fp == FP_SATELLITE) { t[i] = NULL; continue; }
+            if (k < 0 || k >= p->ntex || !p->tex[k] || p->tex[k]->elemLen != 4) return -1;
+            t[i] = p->tex[k];
+        }
+        s->light = ufl(p, 7);
+        s->cam = ufl(p, 8);
+        s->tex = t[0];
+        s->tex2 = t[1];
+        if (p->fp == FP_EARTH) {
+            s->spec = t[2];
+            s->night = t[3];
+            s->proj = t[4];
+        } else {
+            s->proj = t[2];
+        }
         break;
     }
     case FP_DEF02: /* colr1light1.cpp:144-148 */
@@ -865,6 +919,111 @@ static void sample_cube(const o_fbo* t, const float* d, uint8_t* bgra)
     memcpy(bgra, t->buf + (size_t)t->scanline * t->height * layer + (size_t)row * t->scanline + 4 * col, 4);
 }
 
+/* PuresoftSamplerProjection::get (samplrproj.cpp:20-38): the projected
+   coordinate divided by its w (mcemaths_div_3_4: times 1/w, IEEE here in
+   place of rcpps), then four Poisson taps -- row from t plus the disk's x,
+   column from s plus the disk's y, each / 500 -- each lowering the factor
+   by 0.2 when the stored depth is below the coordinate's z. */
+static float sample_proj(const o_fbo* t, const float* proj)
+{
+    static const float PX[4] = {-0.94201624f, 0.94558609f, -0.094184101f, 0.34495938f};
+    static const float PY[4] = {-0.39906216f, -0.76890725f, -0.92938870f, 0.29387760f};
+    float tc[4], r = 1.0f / proj[3], factor = 1.0f;
+    for (int k = 0; k < 4; k++) tc[k] = proj[k] * r;
+    for (int i = 0; i < 4; i++) {
+        int y = (int)sr_f2u((float)t->height * (tc[1] + PX[i] / 500.0f));
+        int x = (int)sr_f2u((float)t->width * (tc[0] + PY[i] / 500.0f));
+        float depth;
+        if (t->wrap) {
+            y = sr_wrap(y, t->height);
+            x = sr_wrap(x, t->width);
+        } else {
+            y = sr_clampi(y, t->height);
+            x = sr_clampi(x, t->width);
+        }
+        memcpy(&depth, t->buf + (size_t)y * t->scanline + 4 * x, 4);
+        if (depth < tc[2]) factor -= 0.2f;
+    }
+    return factor;
+}
+
+/* The demo's planet fragment processors (test/testproc.cpp:208-288 FP_Earth,
+   299-363 FP_Satellite): DEF03's bump-mapped normal and lighting, the
+   specular term scaled by the specular map's red / 255 (Earth), the night
+   texel added where lambert < 0.2 (Earth), then the colour times the
+   projective shadow factor; IEEE 1/x and 1/sqrt in place of rcpps /
+   rsqrtss. */
+static void fp_planet(const ps3do* p, const fp_state* s, const float* in, uint8_t* bgra)
+{
+    const float* tan = in, * bin = in + 4, * nrm = in + 8, * wp = in + 12, * tc = in + 16, * sc = in + 20;
+    const int earth = p->fp == FP_EARTH;
+    float c[4], night[4] = {0, 0, 0, 0}, bt[4], bn[4], tbn[16], r, shadow, control = 1.0f;
+    float L[4], E[4], Hv[4], dist, lambert, spec;
+    sample_nearest(s->tex, tc, c);
+    if (earth) sample_nearest(s->night, tc, night);
+    sample_nearest(s->tex2, tc, bt);
+    bn[0] = bt[2];
+    bn[1] = bt[1];
+    bn[2] = bt[0];
+    bn[3] = 0.0f;
+    shadow = sample_proj(s->proj, sc);
+    if (earth) {
+        float st[4];
+        sample_nearest(s->spec, tc, st);
+        control = st[2] / 255.0f;
+    }
+    r = 1.0f / 255.0f;
+    for (int k = 0; k < 4; k++) bn[k] = bn[k] * r;
+    for (int k = 0; k < 4; k++) bn[k] = bn[k] * 2.0f;
+    for (int k = 0; k < 4; k++) bn[k] = bn[k] - 1.0f;
+    memcpy(tbn, tan, 16);
+    memcpy(tbn + 4, bin, 16);
+    memcpy(tbn + 8, nrm, 16);
+    memset(tbn + 12, 0, 16);
+    m4v4(bn, tbn, bn);
+    r = 1.0f / sqrtf((bn[0] * bn[0] + bn[1] * bn[1]) + (bn[2] * bn[2] + bn[3] * bn[3]));
+    for (int k = 0; k < 4; k++) bn[k] = bn[k] * r;
+    for (int k = 0; k < 4; k++) L[k] = s->light[k] - wp[k];
+    dist = sqrtf((L[0] * L[0] + L[1] * L[1]) + (L[2] * L[2] + L[3] * L[3]));
+    r = 1.0f / dist;
+    for (int k = 0; k < 4; k++) L[k] = L[k] * r;
+    for (int k = 0; k < 4; k++) E[k] = s->cam[k] - wp[k];
+    r = 1.0f / sqrtf((E[0] * E[0] + E[1] * E[1]) + (E[2] * E[2] + E[3] * E[3]));
+    for (int k = 0; k < 4; k++) E[k] = E[k] * r;
+    for (int k = 0; k < 4; k++) Hv[k] = E[k] + L[k];
+    r = 1.0f / sqrtf((Hv[0] * Hv[0] + Hv[1] * Hv[1]) + (Hv[2] * Hv[2] + Hv[3] * Hv[3]));
+    for (int k = 0; k < 4; k++) Hv[k] = Hv[k] * r;
+    lambert = (L[0] * bn[0] + L[1] * bn[1]) + (L[2] * bn[2] + L[3] * bn[3]);
+    spec = (Hv[0] * bn[0] + Hv[1] * bn[1]) + (Hv[2] * bn[2] + Hv[3] * bn[3]);
+    spec = spec < 0 ? 0 : spec;
+    { /* opt_pow(spec, 50) (proc.h:73-86) */
+        float pw = 1.0f, x = spec;
+        unsigned n = 50;
+        while (n > 0) {
+            if (n & 1) pw *= x;
+            x *= x;
+            n >>= 1;
+        }
+        spec = pw;
+    }
+    if (earth) spec *= control;
+    for (int k = 0; k < 4; k++) c[k] = c[k] + 255.0f * spec;
+    for (int k = 0; k < 4; k++) c[k] = c[k] * lambert;
+    if (earth && lambert < 0.2f)
+        for (int k = 0; k < 4; k++) c[k] = c[k] + night[k];
+    for (int k = 0; k < 4; k++) c[k] = c[k] * shadow;
+    for (int k = 0; k < 4; k++) { /* clamp_3_4: maxps then minps */
+        float v = c[k];
+        v = v > 0.0f ? v : 0.0f;
+        v = v < 255.0f ? v : 255.0f;
+        c[k] = v;
+    }
+    bgra[0] = (uint8_t)(int)c[0];
+    bgra[1] = (uint8_t)(int)c[1];
+    bgra[2] = (uint8_t)(int)c[2];
+    bgra[3] = 0;
+}
+
 /* FragmentProcessorDEF03::process (tex1bump1light1.cpp:180-239): the bump
    texel's (r, g, b, 0) / 255 * 2 - 1 on four lanes, through the matrix whose
    columns are the tangent, binormal, normal and 0 (mcemaths_make_tbn,
@@ -943,6 +1102,8 @@ static int run_fp(const ps3do* p, const fp_state* s, const float* in, uint8_t* b
     case FP_DEF02: fp_def02(s, in, bgra); return 1;
     case FP_DEF03: fp_def03(s, in, bgra); return 1;
     case FP_DEF04: sample_cube(s->cube, in, bgra); return 1; /* skybox.cpp:127-134 */
+    case FP_EARTH:
+    case FP_SATELLITE: fp_planet(p, s, in, bgra); return 1;
     case FP_LIT1: {
         sr_level t = level_of(s->tex);
         sr_shade_lit1(&t, s->light, s->cam, in, in + 4, in + 8, bgra);
@@ -1100,7 +1261,7 @@ static void line_contrib(const v2f* v, int v1, int v2, float x, float y, float* 
 }
 
 /* interpolateStartAndStep (interp.cpp:26-80) */
-static void span_setup(const o_raster* r, const o_row* row, int y, const float* rw, const float* pz, int nv,
+static void span_setup(const o_raster* r, const o_row* row, int y, const float* rw, const float* pz, int ip, int nv,
                        const float* const* vuser, o_task* t)
 {
     float cl[4], cr[4], ccl[4], ccr[4], recip;
@@ -1133,7 +1294,7 @@ static void span_setup(const o_raster* r, const o_row* row, int y, const float* 
     if (skip > 0) {
         t->cf2Start += t->cf2Step * (float)skip;
         t->pzStart += t->pzStep * (float)skip;
-        ip_step_forward(nv, start, step, skip);
+        ip_step_forward(ip, nv, start, step, skip);
     }
     t->x1 = row->leftClamped;
     t->x2 = row->rightClamped;
@@ -1202,7 +1363,7 @@ static void run_task(draw_ctx* d, const o_task* t, long long* tested, long long*
         float inv = 1.0f / cf2, z, cur;
         cf2 += t->cf2Step;
         for (int i = 0; i < 4 * nv; i++) frag[i] = start[i] * inv;
-        for (int i = 0; i < 4 * nv; i++) start[i] = start[i] + step[i];
+        ip_step_forward(p->ip, nv, start, step, 1);
         z = pz * inv;
         pz += t->pzStep;
         (*tested)++;
@@ -1328,7 +1489,7 @@ int ps3do_draw(ps3do* p, int vao)
             const o_row* row = &r.rows[y];
             o_task t;
             if (row->left == row->right) continue; /* drawvao.cpp:72-75 */
-            span_setup(&r, row, y, rw, pz, nv, vu, &t);
+            span_setup(&r, row, y, rw, pz, p->ip, nv, vu, &t);
             if (t.x2 >= t.x1) {
                 int len = t.x2 - t.x1 + 1, b = 0;
                 while (len >>= 1) b++;

@@ -1,23 +1,29 @@
-"""Generate asm-free copies of two reference translation units for the Linux
-build of the reference pipeline core (oracle/_ref).  TEST INFRASTRUCTURE ONLY.
+"""Generate asm-free copies of three reference translation units for the
+Linux build of the reference pipeline core (oracle/_ref).  TEST
+INFRASTRUCTURE ONLY.
 
-The reference's interp.cpp and fbo.cpp each contain MSVC 32-bit ``__asm{}``
-blocks, which GCC cannot compile.  This script reads the two files from the
-read-only reference tree and writes copies into the build output directory
-(never into the repository) in which each ``__asm{...}`` block is replaced by
-SSE intrinsics issuing the same operations:
+The reference's interp.cpp and fbo.cpp, and its demo's processors
+(src/test/testproc.cpp), contain MSVC 32-bit ``__asm{}`` blocks, which GCC
+cannot compile.  This script reads the files from the read-only reference
+tree and writes copies into the build output directory (never into the
+repository) in which each ``__asm{...}`` block is replaced by SSE
+intrinsics (or a plain copy) issuing the same operations:
 
 * interp.cpp ``interpolateStartAndStep`` (reference interp.cpp:55-66): two
   haddps reductions of the left/right corrected contributions; lane 0 of the
   left and lane 2 of the right are stored to ``temp``.
 * fbo.cpp ``clear16`` / ``clearToZero`` (reference fbo.cpp:348-393): fill
   m_bytes/16 16-byte slots of m_buffer with the given vector / zero.
+* test/testproc.cpp: the three ``copyUserData`` helpers (6, 4 and 1 aligned
+  16-byte moves, testproc.cpp:8-27, 367-381, 578-587) become memcpy of the
+  same bytes; FP_Cloud's colour packing (testproc.cpp:565-571: cvtps2dq,
+  packusdw, packuswb, movss) becomes the same four intrinsics.
 
 Everything else in both files is left byte-for-byte unchanged.  Each block is
 matched by its own instruction text so that a different reference revision
 fails loudly instead of silently compiling something else.
 
-Usage: python patch_asm.py <reference src/puresoft3d dir> <output dir>
+Usage: python patch_asm.py <reference src/puresoft3d dir> <output dir> [<reference src/test dir>]
 """
 import os
 import re
@@ -71,7 +77,19 @@ def _patch(text, expect):
     return "".join(out)
 
 
-def main(src_dir, out_dir):
+COPY_REPL = """{
+\t\tmemcpy(dest, src, %d);
+\t}"""
+
+PACK_REPL = """{
+\t\t__m128i v_ = _mm_cvtps_epi32(_mm_load_ps(cloudColour));
+\t\tv_ = _mm_packus_epi32(v_, v_);
+\t\tv_ = _mm_packus_epi16(v_, v_);
+\t\t_mm_store_ss(cloudColour, _mm_castsi128_ps(v_));
+\t}"""
+
+
+def main(src_dir, out_dir, test_dir=None):
     os.makedirs(out_dir, exist_ok=True)
     with open(os.path.join(src_dir, "interp.cpp"), encoding="latin-1") as f:
         interp = f.read()
@@ -88,6 +106,17 @@ def main(src_dir, out_dir):
     with open(os.path.join(out_dir, "fbo.cpp"), "w", encoding="latin-1") as f:
         f.write(fbo)
 
+    if test_dir:
+        with open(os.path.join(test_dir, "testproc.cpp"), encoding="latin-1") as f:
+            tp = f.read()
+        tp = _patch(tp, [(["[eax + 80]", "movaps\t[eax + 80]"], COPY_REPL % 96),
+                         (["[eax + 48]", "movaps\t[eax + 48],\txmm3"], COPY_REPL % 64),
+                         (["cvtps2dq", "packusdw", "packuswb", "movss"], PACK_REPL),
+                         (["movaps\txmm0,\t\t[eax]", "movaps\t[eax],\t\txmm0"], COPY_REPL % 16)])
+        tp = "#include <smmintrin.h>\n#include <string.h>\n" + tp
+        with open(os.path.join(out_dir, "testproc.cpp"), "w", encoding="latin-1") as f:
+            f.write(tp)
+
 
 if __name__ == "__main__":
-    main(sys.argv[1], sys.argv[2])
+    main(sys.argv[1], sys.argv[2], sys.argv[3] if len(sys.argv) > 3 else None)

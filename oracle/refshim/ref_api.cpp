@@ -22,6 +22,7 @@
 #include "pipeline.h"
 #include "defproc.h"
 #include "cfgproc.h"
+#include "testproc.h"
 
 int logicCPUs(void); /* refshim/win32_runtime.cpp */
 
@@ -91,6 +92,10 @@ PuresoftProcessor* make_processor(int id)
     case 0x0401: return new VertexProcesserDEF04;
     case 0x0402: return new InterpolationProcessorDEF04;
     case 0x0403: return new FragmentProcessorDEF04;
+    case 0x0701: return new VP_Planet;   /* the reference demo's planet set (test/testproc.cpp) */
+    case 0x0702: return new IP_Planet;
+    case 0x0703: return new FP_Earth;
+    case 0x0713: return new FP_Satellite;
     case 0x0501: return new VertexProcesserDEF05;
     case 0x0502: return new InterpolationProcessorDEF05;
     case 0x0503: return new FragmentProcessorDEF05;

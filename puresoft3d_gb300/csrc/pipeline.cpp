@@ -299,6 +299,7 @@ int required_vary(int ip)
     case IP_DEF02: return 11;  // normal xyzw, worldPos xyz, colour xyzw
     case IP_DEF03: return 17;
     case IP_DEF04: return 3;   // direction xyz
+    case IP_PLANET: return 21; // tangent, binormal, normal xyzw, worldPos xyz, uv, shadow coordinate xyzw
     case IP_LIT2: return 16;
     default: return 0;
     }
@@ -312,6 +313,7 @@ int fp_needs(int fp)
     case FP_DEF02: return IP_DEF02;
     case FP_DEF03: return IP_DEF03;
     case FP_DEF04: return IP_DEF04;
+    case FP_EARTH: case FP_SATELLITE: return IP_PLANET;
     default: return 0;
     }
 }
@@ -324,6 +326,7 @@ int vp_gives(int vp)
     case VP_DEF02: return IP_DEF02;
     case VP_DEF03: return IP_DEF03;
     case VP_DEF04: return IP_DEF04;
+    case VP_PLANET: return IP_PLANET;
     default: return 0;
     }
 }
@@ -335,6 +338,7 @@ bool known_processor(int id)
     case VP_SHADOW: case FP_LIT1: case FP_LIT1A: case FP_LIT3: case VP_LIT2: case IP_LIT2: case FP_LIT2:
     case VP_DEF02: case IP_DEF02: case FP_DEF02: case VP_DEF03: case IP_DEF03: case FP_DEF03:
     case VP_DEF04: case IP_DEF04: case FP_DEF04:
+    case VP_PLANET: case IP_PLANET: case FP_EARTH: case FP_SATELLITE:
         return true;
     }
     return false;
@@ -397,6 +401,11 @@ int snapshot_uniforms(const ps3d_pipeline* p, DrawUniforms& U)
     case VP_DEF03:  // tex1bump1light1.cpp:15-20
         if ((rc = need(3, U.PV, 16)) || (rc = need(4, U.M, 16)) || (rc = need(5, U.Mrot, 16))) return rc;
         break;
+    case VP_PLANET:  // test/testproc.cpp:29-35: DEF03's matrices and the shadow projection at 16
+        if ((rc = need(3, U.PV, 16)) || (rc = need(4, U.M, 16)) || (rc = need(5, U.Mrot, 16)) ||
+            (rc = need(16, U.LPV, 16)))
+            return rc;
+        break;
     case VP_DEF04: {  // skybox.cpp:17-21, 34-37: the view's inverse rotation, the
                       // transposed view matrix with its last column zeroed
         float V[16];
@@ -420,6 +429,25 @@ int snapshot_uniforms(const ps3d_pipeline* p, DrawUniforms& U)
     case FP_DEF02:  // colr1light1.cpp:144-148
         if ((rc = need(7, U.light, 4)) || (rc = need(8, U.cam, 4))) return rc;
         break;
+    case FP_EARTH:       // test/testproc.cpp:197-206: diffuse 9, bump 10, specular 11, night 12, shadow 15
+    case FP_SATELLITE: {  // test/testproc.cpp:290-297: diffuse 9, bump 10, shadow 15
+        if ((rc = need(7, U.light, 4)) || (rc = need(8, U.cam, 4))) return rc;
+        const int earthSlots[5] = {9, 10, 11, 12, 15}, satSlots[3] = {9, 10, 15};
+        const int* slots = p->fp == FP_EARTH ? earthSlots : satSlots;
+        const int n = p->fp == FP_EARTH ? 5 : 3;
+        TexLevel lv[5];
+        for (int i = 0; i < n; i++) {
+            const int* t = uint_(p, slots[i], 1);
+            if (!t) return fail(PS3D_ERR_INVALID, "uniform %d (texture index) is not set", slots[i]);
+            if (!tex_ok(p, *t)) return fail(PS3D_ERR_RANGE, "uniform %d: texture %d", slots[i], *t);
+            if (p->tex[*t].elemLen != 4) return fail(PS3D_ERR_INVALID, "texture %d: 4-byte texels expected", *t);
+            lv[i] = level_of(p->tex[*t]);
+        }
+        U.tex = lv[0];
+        U.tex2 = lv[1];
+        for (int i = 2; i < n; i++) U.ptex[i - 2] = lv[i];
+        break;
+    }
     case FP_DEF04: {  // skybox.cpp:122-125: the cube map's index at uniform 2
         const int* t = uint_(p, 2, 1);
         if (!t) return fail(PS3D_ERR_INVALID, "uniform 2 (cube map index) is not set");
@@ -681,6 +709,8 @@ void sampled_targets(const ps3d_pipeline* p, const std::vector<DrawUniforms>& uu
     };
     for (const DrawUniforms& u : uu) {
         add(u.tex.base);
+        add(u.tex2.base);
+        for (int k = 0; k < 3; k++) add(u.ptex[k].base);
         for (int k = 0; k < u.albedoLevels && k < kMaxLevels; k++) add(u.albedo[k].base);
         for (int k = 0; k < u.normalLevels && k < kMaxLevels; k++) add(u.normal[k].base);
         add(u.shadow);
@@ -801,15 +831,23 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     if ((rc = wait_event(s, p->trk.lastEmit))) return rc;
     if ((rc = mark(p, s, e))) return rc;
     p->trk.lastEmit = e;
+    // a forward pass shades in the raster: it reads and writes the colour
+    // buffer and samples its textures there
+    const bool rasterColour = fuseColour || (forward && anyColour);
+    std::vector<const void*> sampled;
+    if (anyColour) sampled_targets(p, uu, sampled);
     if ((rc = before_write(p, s, tg.depth))) return rc;
-    if (fuseColour && (rc = before_write(p, s, p->colour))) return rc;
+    if (rasterColour && (rc = before_write(p, s, p->colour))) return rc;
+    if (forward)
+        for (const void* t : sampled)
+            if ((rc = before_read(p, s, t))) return rc;
     launch_raster(P, s, launches, &p->prof);
     if ((rc = mark(p, s, e))) return rc;
     wrote(p, tg.depth, e);
-    if (fuseColour) wrote(p, p->colour, e);
-    if (anyColour) {
-        std::vector<const void*> sampled;
-        sampled_targets(p, uu, sampled);
+    if (rasterColour) wrote(p, p->colour, e);
+    if (forward)
+        for (const void* t : sampled) read_by(p, t, e);
+    if (anyColour && !forward) {
         if ((rc = before_write(p, s, p->colour))) return rc;
         for (const void* t : sampled)
             if ((rc = before_read(p, s, t))) return rc;
@@ -1507,6 +1545,7 @@ int ps3d_draw(ps3d_pipeline* p, int vao)
     if (p->vp == VP_LIT2 && d.nv) reqSlots[1] = reqSlots[3] = reqSlots[4] = 1;
     if (p->vp == VP_DEF03 && d.nv) reqSlots[1] = reqSlots[2] = reqSlots[3] = reqSlots[4] = 1;
     if (p->vp == VP_DEF02 && d.nv) reqSlots[1] = reqSlots[2] = 1;
+    if (p->vp == VP_PLANET && d.nv) reqSlots[1] = reqSlots[2] = reqSlots[3] = reqSlots[4] = 1;
     for (int s = 0; s < kVboSlots; s++) {
         if (reqSlots[s] && !va.vbo[s]) return fail(PS3D_ERR_INVALID, "the vertex processor reads VBO slot %d", s);
         if (va.vbo[s]) {

@@ -8,7 +8,8 @@
 namespace ps3d {
 
 constexpr int kMaxLevels = 16;
-constexpr int kMaxVary = 17;   // varying floats per vertex (DEF03: tangent, binormal, normal xyzw, worldPos xyz, uv)
+constexpr int kMaxVary = 21;   // varying floats per vertex (the planet set: tangent, binormal, normal xyzw,
+                               // worldPos xyz, uv, shadow coordinate xyzw)
 // Varyings per vertex of the forward raster variant that serves a pass
 // whose draws carry at most nv (the variants are compiled for 9 and 17); a
 // forward pass lays its varyings out with this stride, so that the variant's
@@ -26,6 +27,7 @@ enum : int {
     VP_DEF04 = 0x0401, IP_DEF04 = 0x0402, FP_DEF04 = 0x0403,
     VP_DEF05 = 0x0501, IP_DEF05 = 0x0502, FP_DEF05 = 0x0503,
     VP_SHADOW = 0x0601,
+    VP_PLANET = 0x0701, IP_PLANET = 0x0702, FP_EARTH = 0x0703, FP_SATELLITE = 0x0713,
     FP_LIT1 = 0x1103, FP_LIT1A = 0x1403, FP_LIT3 = 0x1303,
     VP_LIT2 = 0x1201, IP_LIT2 = 0x1202, FP_LIT2 = 0x1203,
 };
@@ -57,7 +59,8 @@ struct DrawUniforms {
     float Vrot[16];                 // DEF04: transposed view matrix, last column zeroed
     TexLevel tex;                   // DEF01 / DEF03 / LIT1 texture; DEF04 cube map face 0
     long long layerBytes;           // DEF04: bytes from one cube face to the next
-    TexLevel tex2;                  // DEF03 bump map
+    TexLevel tex2;                  // DEF03 / planet bump map
+    TexLevel ptex[3];               // planet set: specular, night and shadow maps
     TexLevel albedo[kMaxLevels];    // LIT2 / LIT3 albedo chain
     TexLevel normal[kMaxLevels];    // LIT2 normal-map chain (RGBA16F)
     int albedoLevels, normalLevels;

@@ -62,9 +62,12 @@ template <int NV> struct VaryState {
     int x;  // the pixel the state is at
 };
 
+// nstep: the interpolation stage steps the first two float4 varyings by the
+// third's step (the reference demo's IP_Planet, test/testproc.cpp:171-195,
+// adds the normal's step to the tangent and the binormal).
 template <int NV>
 __device__ __forceinline__ void vary_begin(const TriRaster& t, const float* vary, int nvMax, const Span& s,
-                                           const SpanZ& z, VaryState<NV>& v)
+                                           const SpanZ& z, VaryState<NV>& v, bool nstep = false)
 {
     const float* a = vary;
     const float* b = vary + nvMax;
@@ -76,6 +79,12 @@ __device__ __forceinline__ void vary_begin(const TriRaster& t, const float* vary
         float e0 = fadd(fadd(fmul(va, z.cr[0]), fmul(vb, z.cr[1])), fmul(vc, z.cr[2]));
         v.st[k] = s0;
         v.sp[k] = fmul(fsub(e0, s0), z.recip);  // calcStep: stepCount != 0 here
+    }
+    if constexpr (NV >= 12) {
+        if (nstep) {
+#pragma unroll
+            for (int k = 0; k < 8; k++) v.sp[k] = v.sp[8 + (k & 3)];
+        }
     }
     if (z.skip == 1) {
 #pragma unroll
@@ -109,10 +118,10 @@ template <int NV> __device__ __forceinline__ void vary_out(const VaryState<NV>& 
 // Varyings of the fragment at x on row y of triangle t.
 template <int NV>
 __device__ __forceinline__ void fragment_varyings(const TriRaster& t, const float* vary, int nvMax, const Span& s,
-                                                  const SpanZ& z, int x, float out[NV])
+                                                  const SpanZ& z, int x, float out[NV], bool nstep = false)
 {
     VaryState<NV> v;
-    vary_begin<NV>(t, vary, nvMax, s, z, v);
+    vary_begin<NV>(t, vary, nvMax, s, z, v, nstep);
     vary_advance<NV>(v, x);
     vary_out<NV>(v, out);
 }
@@ -144,6 +153,13 @@ __device__ __forceinline__ int shade_fragment(const DrawDesc& d, const DrawUnifo
     case FP_DEF03:
         if constexpr (NV >= 17) {
             bgra = shade_def03(U, in);
+            return 1;
+        }
+        return 0;
+    case FP_EARTH:
+    case FP_SATELLITE:
+        if constexpr (NV >= 21) {
+            bgra = shade_planet(U, in, d.fp == FP_EARTH);
             return 1;
         }
         return 0;
@@ -461,7 +477,8 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
                                         span_row(t, yl, sLw[j], sp);
                                         SpanZ zs;
                                         span_z(t, sp, yl, zs);
-                                        vary_begin<FWD>(t, P.vary + (size_t)triId * 3 * P.nvMax, P.nvMax, sp, zs, vs);
+                                        vary_begin<FWD>(t, P.vary + (size_t)triId * 3 * P.nvMax, P.nvMax, sp, zs, vs,
+                                                        dd.fp == FP_EARTH || dd.fp == FP_SATELLITE);
                                         begun = true;
                                     }
                                     vary_advance<FWD>(vs, x0 + x - ox);
@@ -598,6 +615,13 @@ __device__ __forceinline__ void shade_entry(const PassParams& P, int2 e)
     const float* vary = P.vary + (size_t)w * 3 * P.nvMax;
     uint32_t bgra;
     switch (FPK ? FPK : d.fp) {
+    case FP_EARTH:
+    case FP_SATELLITE: {
+        float in[21];
+        fragment_varyings<21>(t, vary, P.nvMax, s, z, xl, in, true);
+        bgra = shade_planet(U, in, (FPK ? FPK : d.fp) == FP_EARTH);
+        break;
+    }
     case FP_DEF03: {
         float in[17];
         fragment_varyings<17>(t, vary, P.nvMax, s, z, xl, in);
@@ -720,6 +744,8 @@ void launch_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
     case FP_DEF03: kern = k_shade<FP_DEF03>; break;
     case FP_DEF02: kern = k_shade<FP_DEF02>; break;
     case FP_DEF04: kern = k_shade<FP_DEF04>; break;
+    case FP_EARTH: kern = k_shade<FP_EARTH>; break;
+    case FP_SATELLITE: kern = k_shade<FP_SATELLITE>; break;
     default: break;
     }
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, 256, 0);

@@ -80,6 +80,26 @@ __device__ __forceinline__ void run_vp(const DrawDesc& d, const DrawUniforms& U,
         }
         break;
     }
+    case VP_PLANET: {  // the reference demo's VP_Planet (test/testproc.cpp:37-71): DEF03's
+                       // outputs plus the world position through the shadow projection
+        float wp[4], v[4], o[4], sc[4];
+        m4v4(wp, U.M, p);
+        m4v4(pos, U.PV, wp);
+        if (d.nv) {
+            m4v4(sc, U.LPV, wp);
+#pragma unroll
+            for (int k = 0; k < 3; k++) {  // tangent, binormal, normal: Mrot on all four lanes
+                ld4(d.vbo[1 + k] + (size_t)idx * d.stride[1 + k], v);
+                m4v4(o, U.Mrot, v);
+                vary[4 * k] = o[0]; vary[4 * k + 1] = o[1]; vary[4 * k + 2] = o[2]; vary[4 * k + 3] = o[3];
+            }
+            const float* uv = (const float*)(d.vbo[4] + (size_t)idx * d.stride[4]);
+            vary[12] = wp[0]; vary[13] = wp[1]; vary[14] = wp[2];
+            vary[15] = __ldg(uv); vary[16] = __ldg(uv + 1);
+            vary[17] = sc[0]; vary[18] = sc[1]; vary[19] = sc[2]; vary[20] = sc[3];
+        }
+        break;
+    }
     case VP_DEF03: {  // tex1bump1light1.cpp:22-46
         float wp[4], v[4], o[4];
         m4v4(wp, U.M, p);
@@ -195,6 +215,10 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float
         case 17:
 #pragma unroll
             for (int k = 0; k < 17; k++) vout[v * P.nvMax + k] = vary[k];
+            break;
+        case 21:
+#pragma unroll
+            for (int k = 0; k < 21; k++) vout[v * P.nvMax + k] = vary[k];
             break;
         }
         float r = frcp(pos[v][3]);  // vertthrd.cpp:37-47: 1/w, then a 4-wide multiply
@@ -330,7 +354,7 @@ constexpr unsigned long long kDescAgg = 1ull << 62, kDescPrefix = 2ull << 62, kD
 
 __global__ void __launch_bounds__(kSetupThreads) k_setup_emit(PassParams P)
 {
-    __shared__ float sVary[kSetupThreads * 3 * kMaxVary];
+    extern __shared__ float sVary[];  // kSetupThreads * 3 * nvMax floats (dynamic: sized by the pass)
     __shared__ int sHist[kRadixMaxPasses][kRadixDigits];
     __shared__ int sWarp[kSetupThreads / 32];
     __shared__ int sTicket, sPrefix;
@@ -612,7 +636,8 @@ int launch_setup(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
     size_t ints = radix_scratch_ints(P.sortBlocks, P.radixPasses, P.nTris);
     if (cudaMemsetAsync(P.radix, 0, ints * sizeof(int), s) != cudaSuccess) return -1;
     pr->begin(K_SETUP, s);
-    k_setup_emit<<<ceil_div(P.nTris, kSetupThreads), kSetupThreads, 0, s>>>(P);
+    const size_t varyBytes = (size_t)kSetupThreads * 3 * P.nvMax * sizeof(float);  // nvMax <= kMaxVary: < 48 KB
+    k_setup_emit<<<ceil_div(P.nTris, kSetupThreads), kSetupThreads, varyBytes, s>>>(P);
     pr->end(s);
     launches++;
     return 0;

