@@ -77,7 +77,7 @@ CONFIGS = {
 # metrics dram__bytes_read.sum / dram__bytes_write.sum; the command and the
 # per-launch figures are in profiles/raster_dram_traffic.md).  Averages over
 # the captured launches that ran to completion.
-RASTER_TRAFFIC = {"c1": 89344, "c2": 7052864, "c3": 114543000, "c4": 784941000}
+RASTER_TRAFFIC = {"c1": 94848, "c2": 6698240, "c3": 114982784, "c4": 785054976}
 
 
 def peaks():

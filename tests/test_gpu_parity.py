@@ -246,3 +246,48 @@ def test_span_occlusion_is_conservative(gpu_lib):
     wrong, dropped = selftest_occlusion(1 << 22)
     assert wrong == 0
     assert dropped > (1 << 22) // 20
+
+
+@pytest.mark.gpu
+def test_forward_pass_waits_for_earlier_colour_pass(gpu_lib):
+    """Two passes on the two pass streams: a lit pass into one depth target,
+    then a blended (forward) pass into another, which reads the colour the
+    first pass's shade wrote; repeated frames match the oracle every time."""
+    from kat_scenes import _alpha_texture, _tri_mesh, random_soup
+    from puresoft3d_gb300 import scenes as S
+    from puresoft3d_gb300.pipeline import PuresoftPipeline
+    b = S._Builder()
+    opaque = b.texture(S.checker_noise_bgra(16, 4, np.random.default_rng(5)))
+    alpha = b.texture(_alpha_texture(6))
+    d1, d2 = b.empty_texture(96, 64), b.empty_texture(96, 64)
+    prog = b.programme(S.VP_DEF01, S.IP_DEF01, S.FP_LIT1)
+    va = b.vao(_tri_mesh(random_soup(400, 31)), slots=(0, 3, 4))
+    vb = b.vao(_tri_mesh(random_soup(200, 32)), slots=(0, 3, 4))
+    eye = np.eye(4)
+    b.f("clearColour", 0xFF000000)
+    b.f("useProgramme", prog)
+    for slot in (3, 4, 5):
+        b.f("setUniform", slot, S.col_major(eye))
+    b.f("setUniform", 7, S.vec4(0.3, 0.5, 0.81))
+    b.f("setUniform", 8, S.vec4(0, 0, 2, 1))
+    b.f("setDepth", d1)
+    b.f("clearDepth", 1.0)
+    b.f("setUniform", 9, np.array([opaque], dtype=np.int32))
+    b.f("drawVAO", va)
+    b.f("setDepth", d2)
+    b.f("clearDepth", 1.0)
+    b.f("enable", S.ALPHABLEND)
+    b.f("setUniform", 9, np.array([alpha], dtype=np.int32))
+    b.f("drawVAO", vb)
+    b.f("disable", S.ALPHABLEND)
+    scene = S.Scene("fwd_after_colour", 96, 64, b.setup, b.frame, {"triangles": 600, "depth_texture": d2})
+    o = OraclePipeline(96, 64)
+    S.replay_setup(scene, o)
+    S.replay_frame(scene, o)
+    want = o.readColour()
+    g = PuresoftPipeline(96, 64)
+    S.replay_setup(scene, g)
+    for _ in range(20):
+        S.replay_frame(scene, g)
+        got = g.readColour()
+        assert colour_diff(got, want)[0] <= COLOUR_TOL
