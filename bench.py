@@ -450,7 +450,11 @@ def run_c5(args):
 
     clocks = ClockSampler()
     clocks.start()
+    up0 = sum(p.stats()["upload_bytes"] for p in srv.pipes)
+    kl0 = sum(p.stats()["kernel_launches"] for p in srv.pipes)
     cap_b = summarize(srv.serve(base, realtime=False), realtime=False)
+    h2d = (sum(p.stats()["upload_bytes"] for p in srv.pipes) - up0) / len(base)
+    launches_b = sum(p.stats()["kernel_launches"] for p in srv.pipes) - kl0
     cap_p = summarize(plain.serve(base, realtime=False), realtime=False)
     loads = {}
     for name, cap in (("batched_capacity", cap_b["images_per_s"]), ("plain_capacity", cap_p["images_per_s"])):
@@ -476,9 +480,9 @@ def run_c5(args):
                         "plain": {k: round(v, 3) for k, v in cap_p.items()}},
         "open_loop": loads,
         "batched_over_plain": round(cap_b["images_per_s"] / cap_p["images_per_s"], 2),
-        "gpu_launches": None,
+        "gpu_launches": int(launches_b),
         "e2e": {"value": round(cap_b["images_per_s"], 2), "unit": "images/s",
-                "h2d_bytes_per_step": None, "d2h_bytes_per_step": int(d2h),
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "note": "the serving loop is end to end: jobs enter from the host, images land in pinned host memory"},
         "roofline": None,
         "clocks": clk,

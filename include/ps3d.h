@@ -129,6 +129,7 @@ typedef struct {
     uint64_t replays;         /* passes re-run after a bin-list capacity miss */
     uint64_t bin_pairs;       /* (bin, triangle) pairs written by the binning passes */
     uint64_t shaded;          /* pixels shaded once: covered at the end of a colour pass (when counting is on) */
+    uint64_t upload_bytes;    /* host -> device bytes of draw descriptors and uniforms uploaded for passes */
 } ps3d_stats_t;
 
 /* PuresoftPipeline::PuresoftPipeline(canvas, w, h, rndr) (pipeline.cpp:24-61).

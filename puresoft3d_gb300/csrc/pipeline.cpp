@@ -764,6 +764,7 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
         // pageable sources: each copy returns once its source has been read
         CU(cudaMemcpyAsync(x.draws, dd.data(), dd.size() * sizeof(DrawDesc), cudaMemcpyHostToDevice, s));
         CU(cudaMemcpyAsync(x.unis, uu.data(), uu.size() * sizeof(DrawUniforms), cudaMemcpyHostToDevice, s));
+        p->stats.upload_bytes += dd.size() * sizeof(DrawDesc) + uu.size() * sizeof(DrawUniforms);
         devDraws = x.draws;
         devUnis = x.unis;
     }
@@ -1871,6 +1872,7 @@ int ps3d_cmdbuf_submit(ps3d_pipeline* p, ps3d_cmdbuf* cb, int uploadInputs)
                            p->stream));
         CU(cudaMemcpyAsync(cb->dUnis, cb->pinUnis, cb->hUnis.size() * sizeof(DrawUniforms), cudaMemcpyHostToDevice,
                            p->stream));
+        p->stats.upload_bytes += cb->hDraws.size() * sizeof(DrawDesc) + cb->hUnis.size() * sizeof(DrawUniforms);
     }
     CU(cudaGraphLaunch(cb->exec, p->stream));
     p->graphUnverified = cb;
@@ -2143,6 +2145,7 @@ int noalloc_run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const P
     CU(cudaMemcpyAsync(base + L.draws, g_noallocDraws, s.nd * sizeof(DrawDesc), cudaMemcpyHostToDevice, p->stream));
     CU(cudaMemcpyAsync(base + L.unis, g_noallocUnis, s.nd * sizeof(DrawUniforms), cudaMemcpyHostToDevice,
                        p->stream));
+    p->stats.upload_bytes += s.nd * (sizeof(DrawDesc) + sizeof(DrawUniforms));
 
     bool fuseDepth = ps.clearDepth && s.tg.scan == W;
     bool fuseColour = ps.clearColour && p->devW == W && p->devH == H;

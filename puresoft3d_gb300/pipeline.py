@@ -21,7 +21,7 @@ ERRORS = {-1: IndexError, -2: ValueError, -3: MemoryError, -4: RuntimeError, -5:
 
 class Stats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in ("draws", "batches", "kernel_launches", "triangles", "fragments",
-                                                "fragments_passed", "replays", "bin_pairs", "shaded")]
+                                                "fragments_passed", "replays", "bin_pairs", "shaded", "upload_bytes")]
 
 
 _lib = None
