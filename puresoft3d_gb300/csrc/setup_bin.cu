@@ -30,93 +30,29 @@ __device__ __forceinline__ void ld4(const uint8_t* p, float v[4])
     v[3] = __ldg(f + 3);
 }
 
-// Runs the draw's vertex processor on vertex `idx`; writes the clip position
-// and the varyings its interpolation stage carries.
-__device__ __forceinline__ void run_vp(const DrawDesc& d, const DrawUniforms& U, int idx, float pos[4], float* vary)
+// The draw's vertex processor on vertex `idx`, in two halves: the clip
+// position, needed by every triangle for its cull and set-up, and the
+// varyings its interpolation stage carries, computed only for triangles that
+// reach a bin (the same operations in the same order as one call would do;
+// the world position both halves need is computed in each).
+__device__ __forceinline__ void vp_position(const DrawDesc& d, const DrawUniforms& U, int idx, float pos[4])
 {
     float p[4];
     ld4(d.vbo[0] + (size_t)idx * d.stride[0], p);
     switch (d.vp) {
-    case VP_DEF01: {  // tex1light1.cpp:22-41
-        float wp[4], n[4], nrm[4];
+    case VP_DEF01:   // tex1light1.cpp:22-41
+    case VP_DEF02:   // colr1light1.cpp:22-40
+    case VP_DEF03:   // tex1bump1light1.cpp:22-46
+    case VP_LIT2:
+    case VP_PLANET: {  // test/testproc.cpp:37-71
+        float wp[4];
         m4v4(wp, U.M, p);
         m4v4(pos, U.PV, wp);
-        if (d.nv) {
-            ld4(d.vbo[3] + (size_t)idx * d.stride[3], n);
-            m4v4(nrm, U.Mrot, n);
-            const float* uv = (const float*)(d.vbo[4] + (size_t)idx * d.stride[4]);
-            vary[0] = nrm[0]; vary[1] = nrm[1]; vary[2] = nrm[2]; vary[3] = nrm[3];
-            vary[4] = wp[0]; vary[5] = wp[1]; vary[6] = wp[2];
-            vary[7] = __ldg(uv); vary[8] = __ldg(uv + 1);
-        }
         break;
     }
-    case VP_DEF02: {  // colr1light1.cpp:22-40: normal in VBO 1, colour in VBO 2
-        float wp[4], n[4], nrm[4], c[4];
-        m4v4(wp, U.M, p);
-        m4v4(pos, U.PV, wp);
-        if (d.nv) {
-            ld4(d.vbo[1] + (size_t)idx * d.stride[1], n);
-            ld4(d.vbo[2] + (size_t)idx * d.stride[2], c);
-            m4v4(nrm, U.Mrot, n);
-            vary[0] = nrm[0]; vary[1] = nrm[1]; vary[2] = nrm[2]; vary[3] = nrm[3];
-            vary[4] = wp[0]; vary[5] = wp[1]; vary[6] = wp[2];
-            vary[7] = c[0]; vary[8] = c[1]; vary[9] = c[2]; vary[10] = c[3];
-        }
-        break;
-    }
-    case VP_DEF04: {  // skybox.cpp:23-44: the position passes through; the
-                      // direction is Vrot times the normalised vector from
-                      // the observer (0, 0, 1) to the vertex
+    case VP_DEF04:  // skybox.cpp:23-44: the position passes through
         pos[0] = p[0]; pos[1] = p[1]; pos[2] = p[2]; pos[3] = p[3];
-        if (d.nv) {
-            float v[4] = {fsub(p[0], 0.0f), fsub(p[1], 0.0f), fsub(p[2], 1.0f), 0.0f}, dir[4];
-            float r = fdiv(1.0f, fsqrt(fadd(fadd(fmul(v[0], v[0]), fmul(v[1], v[1])),
-                                           fadd(fmul(v[2], v[2]), fmul(v[3], v[3])))));
-#pragma unroll
-            for (int k = 0; k < 4; k++) v[k] = fmul(v[k], r);
-            m4v4(dir, U.Vrot, v);
-            vary[0] = dir[0]; vary[1] = dir[1]; vary[2] = dir[2];
-        }
         break;
-    }
-    case VP_PLANET: {  // the reference demo's VP_Planet (test/testproc.cpp:37-71): DEF03's
-                       // outputs plus the world position through the shadow projection
-        float wp[4], v[4], o[4], sc[4];
-        m4v4(wp, U.M, p);
-        m4v4(pos, U.PV, wp);
-        if (d.nv) {
-            m4v4(sc, U.LPV, wp);
-#pragma unroll
-            for (int k = 0; k < 3; k++) {  // tangent, binormal, normal: Mrot on all four lanes
-                ld4(d.vbo[1 + k] + (size_t)idx * d.stride[1 + k], v);
-                m4v4(o, U.Mrot, v);
-                vary[4 * k] = o[0]; vary[4 * k + 1] = o[1]; vary[4 * k + 2] = o[2]; vary[4 * k + 3] = o[3];
-            }
-            const float* uv = (const float*)(d.vbo[4] + (size_t)idx * d.stride[4]);
-            vary[12] = wp[0]; vary[13] = wp[1]; vary[14] = wp[2];
-            vary[15] = __ldg(uv); vary[16] = __ldg(uv + 1);
-            vary[17] = sc[0]; vary[18] = sc[1]; vary[19] = sc[2]; vary[20] = sc[3];
-        }
-        break;
-    }
-    case VP_DEF03: {  // tex1bump1light1.cpp:22-46
-        float wp[4], v[4], o[4];
-        m4v4(wp, U.M, p);
-        m4v4(pos, U.PV, wp);
-        if (d.nv) {
-#pragma unroll
-            for (int k = 0; k < 3; k++) {  // tangent, binormal, normal: Mrot on all four lanes
-                ld4(d.vbo[1 + k] + (size_t)idx * d.stride[1 + k], v);
-                m4v4(o, U.Mrot, v);
-                vary[4 * k] = o[0]; vary[4 * k + 1] = o[1]; vary[4 * k + 2] = o[2]; vary[4 * k + 3] = o[3];
-            }
-            const float* uv = (const float*)(d.vbo[4] + (size_t)idx * d.stride[4]);
-            vary[12] = wp[0]; vary[13] = wp[1]; vary[14] = wp[2];
-            vary[15] = __ldg(uv); vary[16] = __ldg(uv + 1);
-        }
-        break;
-    }
     case VP_DEF05: {  // shadow.cpp:21-29: positions x0.9 (mcemaths_mul_3), then (PV*M) * p
         float a[4] = {fmul(p[0], 0.9f), fmul(p[1], 0.9f), fmul(p[2], 0.9f), p[3]};
         m4v4(pos, U.PVM, a);
@@ -125,28 +61,99 @@ __device__ __forceinline__ void run_vp(const DrawDesc& d, const DrawUniforms& U,
     case VP_SHADOW:
         m4v4(pos, U.PVM, p);
         break;
+    default:
+        pos[0] = pos[1] = pos[2] = pos[3] = 0.0f;
+    }
+}
+
+__device__ __forceinline__ void vp_varyings(const DrawDesc& d, const DrawUniforms& U, int idx, float* vary)
+{
+    float p[4];
+    ld4(d.vbo[0] + (size_t)idx * d.stride[0], p);
+    switch (d.vp) {
+    case VP_DEF01: {  // tex1light1.cpp:22-41
+        float wp[4], n[4], nrm[4];
+        m4v4(wp, U.M, p);
+        ld4(d.vbo[3] + (size_t)idx * d.stride[3], n);
+        m4v4(nrm, U.Mrot, n);
+        const float* uv = (const float*)(d.vbo[4] + (size_t)idx * d.stride[4]);
+        vary[0] = nrm[0]; vary[1] = nrm[1]; vary[2] = nrm[2]; vary[3] = nrm[3];
+        vary[4] = wp[0]; vary[5] = wp[1]; vary[6] = wp[2];
+        vary[7] = __ldg(uv); vary[8] = __ldg(uv + 1);
+        break;
+    }
+    case VP_DEF02: {  // colr1light1.cpp:22-40: normal in VBO 1, colour in VBO 2
+        float wp[4], n[4], nrm[4], c[4];
+        m4v4(wp, U.M, p);
+        ld4(d.vbo[1] + (size_t)idx * d.stride[1], n);
+        ld4(d.vbo[2] + (size_t)idx * d.stride[2], c);
+        m4v4(nrm, U.Mrot, n);
+        vary[0] = nrm[0]; vary[1] = nrm[1]; vary[2] = nrm[2]; vary[3] = nrm[3];
+        vary[4] = wp[0]; vary[5] = wp[1]; vary[6] = wp[2];
+        vary[7] = c[0]; vary[8] = c[1]; vary[9] = c[2]; vary[10] = c[3];
+        break;
+    }
+    case VP_DEF04: {  // skybox.cpp:23-44: the direction is Vrot times the
+                      // normalised vector from the observer (0, 0, 1) to the vertex
+        float v[4] = {fsub(p[0], 0.0f), fsub(p[1], 0.0f), fsub(p[2], 1.0f), 0.0f}, dir[4];
+        float r = fdiv(1.0f, fsqrt(fadd(fadd(fmul(v[0], v[0]), fmul(v[1], v[1])),
+                                       fadd(fmul(v[2], v[2]), fmul(v[3], v[3])))));
+#pragma unroll
+        for (int k = 0; k < 4; k++) v[k] = fmul(v[k], r);
+        m4v4(dir, U.Vrot, v);
+        vary[0] = dir[0]; vary[1] = dir[1]; vary[2] = dir[2];
+        break;
+    }
+    case VP_PLANET: {  // test/testproc.cpp:37-71: DEF03's outputs plus the world
+                       // position through the shadow projection
+        float wp[4], v[4], o[4], sc[4];
+        m4v4(wp, U.M, p);
+        m4v4(sc, U.LPV, wp);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {  // tangent, binormal, normal: Mrot on all four lanes
+            ld4(d.vbo[1 + k] + (size_t)idx * d.stride[1 + k], v);
+            m4v4(o, U.Mrot, v);
+            vary[4 * k] = o[0]; vary[4 * k + 1] = o[1]; vary[4 * k + 2] = o[2]; vary[4 * k + 3] = o[3];
+        }
+        const float* uv = (const float*)(d.vbo[4] + (size_t)idx * d.stride[4]);
+        vary[12] = wp[0]; vary[13] = wp[1]; vary[14] = wp[2];
+        vary[15] = __ldg(uv); vary[16] = __ldg(uv + 1);
+        vary[17] = sc[0]; vary[18] = sc[1]; vary[19] = sc[2]; vary[20] = sc[3];
+        break;
+    }
+    case VP_DEF03: {  // tex1bump1light1.cpp:22-46
+        float wp[4], v[4], o[4];
+        m4v4(wp, U.M, p);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {  // tangent, binormal, normal: Mrot on all four lanes
+            ld4(d.vbo[1 + k] + (size_t)idx * d.stride[1 + k], v);
+            m4v4(o, U.Mrot, v);
+            vary[4 * k] = o[0]; vary[4 * k + 1] = o[1]; vary[4 * k + 2] = o[2]; vary[4 * k + 3] = o[3];
+        }
+        const float* uv = (const float*)(d.vbo[4] + (size_t)idx * d.stride[4]);
+        vary[12] = wp[0]; vary[13] = wp[1]; vary[14] = wp[2];
+        vary[15] = __ldg(uv); vary[16] = __ldg(uv + 1);
+        break;
+    }
     case VP_LIT2: {
         float wp[4], sp[4], n[4], nrm[4], t[4], tan[4];
         m4v4(wp, U.M, p);
         m4v4(sp, U.LPV, wp);
-        m4v4(pos, U.PV, wp);
-        if (d.nv) {
-            ld4(d.vbo[3] + (size_t)idx * d.stride[3], n);
-            ld4(d.vbo[1] + (size_t)idx * d.stride[1], t);
-            float t3[4] = {t[0], t[1], t[2], 0.0f};
-            m4v4(nrm, U.Mrot, n);
-            m4v4(tan, U.Mrot, t3);
-            const float* uv = (const float*)(d.vbo[4] + (size_t)idx * d.stride[4]);
-            vary[0] = nrm[0]; vary[1] = nrm[1]; vary[2] = nrm[2];
-            vary[3] = tan[0]; vary[4] = tan[1]; vary[5] = tan[2]; vary[6] = t[3];
-            vary[7] = wp[0]; vary[8] = wp[1]; vary[9] = wp[2];
-            vary[10] = __ldg(uv); vary[11] = __ldg(uv + 1);
-            vary[12] = sp[0]; vary[13] = sp[1]; vary[14] = sp[2]; vary[15] = sp[3];
-        }
+        ld4(d.vbo[3] + (size_t)idx * d.stride[3], n);
+        ld4(d.vbo[1] + (size_t)idx * d.stride[1], t);
+        float t3[4] = {t[0], t[1], t[2], 0.0f};
+        m4v4(nrm, U.Mrot, n);
+        m4v4(tan, U.Mrot, t3);
+        const float* uv = (const float*)(d.vbo[4] + (size_t)idx * d.stride[4]);
+        vary[0] = nrm[0]; vary[1] = nrm[1]; vary[2] = nrm[2];
+        vary[3] = tan[0]; vary[4] = tan[1]; vary[5] = tan[2]; vary[6] = t[3];
+        vary[7] = wp[0]; vary[8] = wp[1]; vary[9] = wp[2];
+        vary[10] = __ldg(uv); vary[11] = __ldg(uv + 1);
+        vary[12] = sp[0]; vary[13] = sp[1]; vary[14] = sp[2]; vary[15] = sp[3];
         break;
     }
     default:
-        pos[0] = pos[1] = pos[2] = pos[3] = 0.0f;
+        break;
     }
 }
 
@@ -189,38 +196,9 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float
     int lt = t - d.triBase;
 
     float pos[3][4], rw[3], pz[3];
-    float* vout = sVary + threadIdx.x * 3 * P.nvMax;
 #pragma unroll
     for (int v = 0; v < 3; v++) {
-        float vary[kMaxVary];
-        run_vp(d, U, 3 * lt + v, pos[v], vary);
-        // constant trip counts keep `vary` in registers
-        switch (d.nv) {
-        case 3:
-#pragma unroll
-            for (int k = 0; k < 3; k++) vout[v * P.nvMax + k] = vary[k];
-            break;
-        case 9:
-#pragma unroll
-            for (int k = 0; k < 9; k++) vout[v * P.nvMax + k] = vary[k];
-            break;
-        case 11:
-#pragma unroll
-            for (int k = 0; k < 11; k++) vout[v * P.nvMax + k] = vary[k];
-            break;
-        case 16:
-#pragma unroll
-            for (int k = 0; k < 16; k++) vout[v * P.nvMax + k] = vary[k];
-            break;
-        case 17:
-#pragma unroll
-            for (int k = 0; k < 17; k++) vout[v * P.nvMax + k] = vary[k];
-            break;
-        case 21:
-#pragma unroll
-            for (int k = 0; k < 21; k++) vout[v * P.nvMax + k] = vary[k];
-            break;
-        }
+        vp_position(d, U, 3 * lt + v, pos[v]);
         float r = frcp(pos[v][3]);  // vertthrd.cpp:37-47: 1/w, then a 4-wide multiply
 #pragma unroll
         for (int k = 0; k < 4; k++) pos[v][k] = fmul(pos[v][k], r);
@@ -333,6 +311,42 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float
     for (int k = 0; k < 4; k++) dst[k] = src[k];
     pairs = count;
     rect = make_int4(bx0, bx1, by0, by1);
+    if (count > 0 && d.nv) {
+        // the varyings of a triangle that reaches a bin (no other is ever read)
+        float* vout = sVary + threadIdx.x * 3 * P.nvMax;
+#pragma unroll 1
+        for (int v = 0; v < 3; v++) {
+            float vary[kMaxVary];
+            vp_varyings(d, U, 3 * lt + v, vary);
+            // constant trip counts keep `vary` in registers
+            switch (d.nv) {
+            case 3:
+#pragma unroll
+                for (int k = 0; k < 3; k++) vout[v * P.nvMax + k] = vary[k];
+                break;
+            case 9:
+#pragma unroll
+                for (int k = 0; k < 9; k++) vout[v * P.nvMax + k] = vary[k];
+                break;
+            case 11:
+#pragma unroll
+                for (int k = 0; k < 11; k++) vout[v * P.nvMax + k] = vary[k];
+                break;
+            case 16:
+#pragma unroll
+                for (int k = 0; k < 16; k++) vout[v * P.nvMax + k] = vary[k];
+                break;
+            case 17:
+#pragma unroll
+                for (int k = 0; k < 17; k++) vout[v * P.nvMax + k] = vary[k];
+                break;
+            case 21:
+#pragma unroll
+                for (int k = 0; k < 21; k++) vout[v * P.nvMax + k] = vary[k];
+                break;
+            }
+        }
+    }
 }
 
 // Set-up, pair offsets and pair emission in one kernel.  Block b (numbered
@@ -352,7 +366,7 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float
 constexpr int kLookbackSpins = 1 << 22;  // bounded waits: ~0.1 s and more, then the pass fails
 constexpr unsigned long long kDescAgg = 1ull << 62, kDescPrefix = 2ull << 62, kDescValue = (1ull << 62) - 1;
 
-__global__ void __launch_bounds__(kSetupThreads) k_setup_emit(PassParams P)
+__global__ void __launch_bounds__(kSetupThreads, 8) k_setup_emit(PassParams P)
 {
     extern __shared__ float sVary[];  // kSetupThreads * 3 * nvMax floats (dynamic: sized by the pass)
     __shared__ int sHist[kRadixMaxPasses][kRadixDigits];
