@@ -43,14 +43,22 @@ public:
     PuresoftPipeline(const PuresoftPipeline&) = delete;
     PuresoftPipeline& operator=(const PuresoftPipeline&) = delete;
 
-    // texture api
-    int createTexture(const ImageBuffer* image, bool wrap = false)
+    // texture api (createTexture(image, extraLayers, mode), tex.cpp:3-25: 5 extra layers make a cube map)
+    int createTexture(const ImageBuffer* image, int extraLayers = 0, bool wrap = false)
     {
-        return check(ps3d_texture_create(m_p, (int)image->width, (int)image->height, (int)image->scanline,
-                                         (int)image->elemLen, image->pixels, wrap ? 1 : 0));
+        return check(ps3d_texture_create_layers(m_p, (int)image->width, (int)image->height, (int)image->scanline,
+                                                (int)image->elemLen, image->pixels, wrap ? 1 : 0, extraLayers));
     }
     void destroyTexture(int idx) { check(ps3d_texture_destroy(m_p, idx)); }
-    void readTexture(int idx, void* out, size_t bytes) { check(ps3d_texture_read(m_p, idx, out, bytes)); }
+    void readTexture(int idx, void* out, size_t bytes, int layer = 0)
+    {
+        check(ps3d_texture_read_layer(m_p, idx, layer, out, bytes));
+    }
+    // getTexture(idx, image, layer) then filling image.pixels (tex.cpp:27-37)
+    void writeTexture(int idx, const void* pixels, size_t bytes, int layer = 0)
+    {
+        check(ps3d_texture_write_layer(m_p, idx, layer, pixels, bytes));
+    }
 
     // processor api (processor classes are ids: PS3D_VP_* / PS3D_IP_* / PS3D_FP_*)
     int addProcessor(int processorClass) { return check(ps3d_processor_add(m_p, processorClass)); }
@@ -78,6 +86,18 @@ public:
     void clearDepth(float furthest = 1.0f) { check(ps3d_clear_depth(m_p, furthest)); }
     void clearColour(uint32_t bgra = 0) { check(ps3d_clear_colour(m_p, bgra)); }
     void finish(void) { check(ps3d_finish(m_p)); }
+    // postProcess(processor) (post.cpp:3-19) with a built-in post-processor (PS3D_PP_*)
+    void postProcess(int postProcessorClass, const void* params = nullptr, size_t bytes = 0)
+    {
+        check(ps3d_post_process(m_p, postProcessorClass, params, bytes));
+    }
+    // the demo's SceneObject::findOrCreateVao(objx) (test/scenobj.cpp:88-162)
+    int createVAOFromObjx(const char* path, int mesh = 0)
+    {
+        int vao = -1;
+        check(ps3d_objx_load_vao(m_p, path, mesh, &vao));
+        return vao;
+    }
     // in place of swapBuffers(): the frame, BGRA8 top-down
     void readColour(void* out) { check(ps3d_read_colour(m_p, out)); }
     ps3d_pipeline* handle(void) { return m_p; }

@@ -37,3 +37,33 @@ def test_python_binding_covers_header():
 def test_library_loads():
     lib = pipeline.library()
     assert lib.ps3d_last_error() is not None
+
+
+def test_cpp_adapter_compiles(tmp_path):
+    """include/ps3d.hpp (the reference's class and method names over the C
+    ABI) compiles and links against the library (no device calls)."""
+    src = tmp_path / "use_adapter.cpp"
+    src.write_text('''
+#include "ps3d.hpp"
+int main(int argc, char**) {
+    if (argc > 5) {  // never taken: only the calls' types are checked
+        ps3d_gpu::PuresoftPipeline pipe(64, 48);
+        ps3d_gpu::ImageBuffer img = {4, 16, 4, 4, nullptr};
+        int cube = pipe.createTexture(&img, 5);
+        pipe.writeTexture(cube, nullptr, 0, 3);
+        int prog = pipe.createProgramme(pipe.addProcessor(PS3D_VP_DEF04), pipe.addProcessor(PS3D_IP_DEF04),
+                                        pipe.addProcessor(PS3D_FP_DEF04));
+        pipe.useProgramme(prog);
+        pipe.drawVAO(pipe.createVAOFromObjx("sphere.objx"));
+        pipe.postProcess(PS3D_PP_ADD8);
+        unsigned char frame[64 * 48 * 4];
+        pipe.readColour(frame);
+    }
+    return 0;
+}
+''')
+    lib = build.build()
+    out = tmp_path / "use_adapter"
+    subprocess.run(["g++", "-std=c++17", "-I", os.path.join(ROOT, "include"), str(src), lib, "-o", str(out)],
+                   check=True, capture_output=True, text=True)
+    assert out.exists()
