@@ -249,11 +249,12 @@ int ps3d_get_bin_width(ps3d_pipeline* p, int* columns);
  * so results are unchanged); off leaves the test out of the kernel.  The
  * autotuner times both. */
 int ps3d_set_span_culling(ps3d_pipeline* p, int on);
-/* Raster blocks per bin: 1 (the default), 2, 4 or 8.  With more than one, a
- * bin holding more than 256 triangles is shared out by rows between its
- * blocks (each takes 32 / n rows), so that a few crowded bins do not hold
- * up the launch; other bins are done whole.  Time only, never results; the
- * autotuner times 1 and 4. */
+/* Row split of the raster: 1 (the default: one block per bin), 2, 4 or 8.
+ * With n > 1, a bin of t triangles is cut into min(n, the largest power of
+ * two <= t / 128) row slices, and a persistent grid takes the slices of the
+ * most-cut bins first, then the other bins, so that a few crowded bins do
+ * not hold up the launch.  Time only, never results; the autotuner times 1
+ * and 4. */
 int ps3d_set_row_split(ps3d_pipeline* p, int blocksPerBin);
 /* Second schedule knob: the raster kernel variant.  0 lets each thread use
  * the registers it wants (fewer resident blocks); 8 caps registers so that

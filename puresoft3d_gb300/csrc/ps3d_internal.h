@@ -117,6 +117,7 @@ struct PassParams {
     int sortDescOff;
     int* keyB;                // the sort's second key buffer
     int* binStart;            // first position of each bin's list; [nBins] = total
+    int* binItems;            // the raster's work list (kItemsPerBin x nBins ints)
     int* binTri;              // the sort's second triangle buffer
     const int* sortedTri;     // triangles of each bin, in submission order (binTri or pairTri)
     int* status;              // the pipeline's: [0] bit 1 = a pass overflowed, bit 2 = a wait
@@ -140,6 +141,20 @@ constexpr int kSortChunk = 4096;   // pairs per sort tile
 constexpr int kFirstFailed = 3;    // status word: the first pass that overflowed or timed out
 constexpr int kNoPass = 0x7f7f7f7f; // its value when none did (a byte-wise memset)
 constexpr int kSlotTiles = 0, kSlotShade = 1, kSlotTotal = 2;  // slot status words: sort tiles, shade list, pairs
+// The raster's work list (k_bin_bounds -> k_raster): items in five buckets,
+// bins cut into 8, 4, 2 row slices, whole bins with triangles, empty bins;
+// bucket b's count in slot status word kSlotBucket + b, the raster's cursor
+// in kSlotCursor.  An item is bin | slice << 24 | log2(slices) << 28.
+constexpr int kItemBuckets = 5;
+constexpr int kSlotBucket = 3, kSlotCursor = kSlotBucket + kItemBuckets;
+constexpr int kItemSliceShift = 24, kItemLog2Shift = 28, kItemBinMask = (1 << kItemSliceShift) - 1;
+constexpr int kSliceTris = 128;  // a bin gets the most slices (up to rowSplit) that leave this many triangles each
+// First item of bucket b in a list for nBins bins (capacities 8, 4, 2, 1, 1 x nBins).
+__host__ __device__ constexpr long long bucket_base(int b, int nBins)
+{
+    return b == 0 ? 0 : b == 1 ? 8LL * nBins : b == 2 ? 12LL * nBins : b == 3 ? 14LL * nBins : 15LL * nBins;
+}
+constexpr int kItemsPerBin = 16;
 
 // A pass's kernels do nothing once this pass or an earlier one has failed;
 // the host then re-runs the commands from the first failed pass.  Passes run

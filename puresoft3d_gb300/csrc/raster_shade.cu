@@ -199,6 +199,20 @@ __device__ __forceinline__ bool span_occluded(const SpanZ& z, int kA, int kB, fl
     return lhs - slack >= -0.0001f;  // false for NaN
 }
 
+// The next work item of the pass's list (k_bin_bounds): the crowded bins'
+// row slices, then the other bins, then the empty ones; -1 when done.
+__device__ __forceinline__ int next_bin_item(const PassParams& P)
+{
+    int i = atomicAdd(P.slotStatus + kSlotCursor, 1);
+    const int nBins = P.binsX * P.binsY;
+    for (int b = 0; b < kItemBuckets; b++) {
+        const int n = *(volatile const int*)(P.slotStatus + kSlotBucket + b);
+        if (i < n) return P.binItems[bucket_base(b, nBins) + i];
+        i -= n;
+    }
+    return -1;
+}
+
 constexpr int kRasterThreads = 128;  // 4 warps: warp = column quarter, lane = bin row
 constexpr int kChunk = 128;          // triangles per chunk (one per thread)
 constexpr int kSlots = 128;          // (triangle, row) spans per round (one per thread)
@@ -232,32 +246,39 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
     __shared__ int sWarpSum[kRasterThreads / 32];
     __shared__ float sQMax[4][kBinH];            // per quarter and row: an upper bound of its depths
     __shared__ int sListBase;
+    __shared__ int sItem;
     if (pass_failed(P.status, P.passSeq)) return;
 
-    // Row slices: with P.rowSplit > 1, each bin has that many blocks; a bin
-    // with more than kSplitMin triangles is shared out by rows (block s takes
-    // rows [s R, s R + R), R = 32 / rowSplit: fewer spans per block, so a
-    // crowded bin no longer holds up the launch alone); other bins are done
-    // whole by their first block.
-    const int split = P.rowSplit;
-    const int bin = blockIdx.x / split, slice = blockIdx.x - bin * split;
+    // One block per bin (P.rowSplit == 1), or a persistent grid whose blocks
+    // take work items from the pass's list (k_bin_bounds: crowded bins first,
+    // each as 1 << log2 row slices of 32 >> log2 rows -- fewer spans per
+    // block, so a crowded bin no longer holds up the launch alone -- then the
+    // other bins, the empty ones last) until it is exhausted.  An item is
+    // taken only when the block is free for it (taking the next one early
+    // would hold a crowded slice back behind the current item).
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const bool listed = P.rowSplit > 1;
+    unsigned long long tested = 0, passed = 0, coveredAll = 0;
+    for (int iter = 0;; iter++) {
+    if (listed && tid == 0) sItem = next_bin_item(P);
+    __syncthreads();  // sItem is ready; the previous item's shared data are no longer read
+    const int item = listed ? sItem : (iter ? -1 : blockIdx.x);
+    __syncthreads();  // sItem is written again only after every thread has read it
+    if (item < 0) break;
+    const int bin = item & kItemBinMask, slice = (item >> kItemSliceShift) & 15;
+    const int nSlices = 1 << (item >> kItemLog2Shift);
     const int bx = bin % P.binsX, by = bin / P.binsX;
     const int x0 = bx * BW, y0 = by * kBinH;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int cols = min(BW, P.W - x0);
     const int rows = min(kBinH, P.H - y0);
     int start, end;
     bin_range(P, bin, start, end);
     int rowBeg = 0, rowEnd = rows;
-    if (split > 1) {
-        if (end - start > kSplitMin) {
-            const int R = kBinH / split;
-            rowBeg = slice * R;
-            rowEnd = min(rowBeg + R, rows);
-            if (rowBeg >= rowEnd) return;
-        } else if (slice) {
-            return;
-        }
+    if (nSlices > 1) {
+        const int R = kBinH / nSlices;
+        rowBeg = slice * R;
+        rowEnd = min(rowBeg + R, rows);
+        if (rowBeg >= rowEnd) continue;
     }
 
     if (start == end) {
@@ -267,7 +288,7 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
                 if (P.clearDepth) P.depth[(size_t)(y0 + r) * P.depthScan + x0 + c] = P.depthClearValue;
                 if (P.clearColour) clear_colour_px(P, x0 + c, y0 + r);
             }
-        return;
+        continue;
     }
     // prefetch (record of the first chunk, index of the second), in flight
     // while the bin's depth is loaded
@@ -313,7 +334,6 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
     }
     int par = 0;  // mask buffer of the current round
 
-    unsigned long long tested = 0, passed = 0;
     const int qs = warp * Q, qe = qs + Q - 1;  // this thread's columns (bin-relative)
     float* dRow = sDepth + lane * S;
     int* wRow = sWin + lane * S;
@@ -570,8 +590,10 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
             }
         }
     }
+    coveredAll += (unsigned long long)covered;
+    }
     if (P.countFrags) {
-        unsigned long long cov = P.anyColour ? (unsigned long long)covered : 0ull;
+        unsigned long long cov = P.anyColour ? coveredAll : 0ull;
 #pragma unroll
         for (int o = 16; o; o >>= 1) {
             tested += __shfl_xor_sync(0xffffffffu, tested, o);
@@ -690,14 +712,27 @@ __global__ void k_fill_u32(uint32_t* base, int width, int height, int pitchElems
 
 static inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
+// The persistent raster grid: as many blocks as fit on the device at once
+// (more would only find the list empty), at most one per work item.
+static int raster_grid(const void* kern, int nBins, int rowSplit)
+{
+    if (rowSplit <= 1) return nBins;  // one block per bin
+    int dev = 0, sms = 0, perSM = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, kRasterThreads, 0);
+    long long items = (long long)nBins * rowSplit;
+    return (int)std::max<long long>(1, std::min<long long>(items, (long long)std::max(sms, 1) * std::max(perSM, 1)));
+}
+
 template <int BW> void launch_raster(const PassParams& P, int nBins, cudaStream_t s)
 {
     if (P.rasterBlocks == 8) {
-        if (P.cullSpans) k_raster<BW, 8, 0, true><<<nBins * P.rowSplit, kRasterThreads, 0, s>>>(P);
-        else k_raster<BW, 8, 0, false><<<nBins * P.rowSplit, kRasterThreads, 0, s>>>(P);
+        if (P.cullSpans) { auto* k_ = k_raster<BW, 8, 0, true>; k_<<<raster_grid((const void*)k_, nBins, P.rowSplit), kRasterThreads, 0, s>>>(P); }
+        else { auto* k_ = k_raster<BW, 8, 0, false>; k_<<<raster_grid((const void*)k_, nBins, P.rowSplit), kRasterThreads, 0, s>>>(P); }
     } else {
-        if (P.cullSpans) k_raster<BW, 1, 0, true><<<nBins * P.rowSplit, kRasterThreads, 0, s>>>(P);
-        else k_raster<BW, 1, 0, false><<<nBins * P.rowSplit, kRasterThreads, 0, s>>>(P);
+        if (P.cullSpans) { auto* k_ = k_raster<BW, 5, 0, true>; k_<<<raster_grid((const void*)k_, nBins, P.rowSplit), kRasterThreads, 0, s>>>(P); }
+        else { auto* k_ = k_raster<BW, 5, 0, false>; k_<<<raster_grid((const void*)k_, nBins, P.rowSplit), kRasterThreads, 0, s>>>(P); }
     }
 }
 
@@ -706,11 +741,11 @@ void launch_raster_forward(const PassParams& P, int nBins, cudaStream_t s)
 {
     // the host lays a forward pass's varyings out with stride forward_vary()
     if (P.nvMax == forward_vary(9)) {
-        if (P.cullSpans) k_raster<16, 1, 9, true><<<nBins * P.rowSplit, kRasterThreads, 0, s>>>(P);
-        else k_raster<16, 1, 9, false><<<nBins * P.rowSplit, kRasterThreads, 0, s>>>(P);
+        if (P.cullSpans) { auto* k_ = k_raster<16, 1, 9, true>; k_<<<raster_grid((const void*)k_, nBins, P.rowSplit), kRasterThreads, 0, s>>>(P); }
+        else { auto* k_ = k_raster<16, 1, 9, false>; k_<<<raster_grid((const void*)k_, nBins, P.rowSplit), kRasterThreads, 0, s>>>(P); }
     } else {
-        if (P.cullSpans) k_raster<16, 1, kMaxVary, true><<<nBins * P.rowSplit, kRasterThreads, 0, s>>>(P);
-        else k_raster<16, 1, kMaxVary, false><<<nBins * P.rowSplit, kRasterThreads, 0, s>>>(P);
+        if (P.cullSpans) { auto* k_ = k_raster<16, 1, kMaxVary, true>; k_<<<raster_grid((const void*)k_, nBins, P.rowSplit), kRasterThreads, 0, s>>>(P); }
+        else { auto* k_ = k_raster<16, 1, kMaxVary, false>; k_<<<raster_grid((const void*)k_, nBins, P.rowSplit), kRasterThreads, 0, s>>>(P); }
     }
 }
 

@@ -382,6 +382,7 @@ __global__ void __launch_bounds__(kSetupThreads, 8) k_setup_emit(PassParams P)
     int4 rect = make_int4(0, -1, 0, -1);
     if (t < P.nTris) setup_triangle(P, t, sVary, count, rect);
     if (b == 0 && tid == 0) P.slotStatus[kSlotShade] = 0;  // the shade list starts empty
+    if (b == 0 && tid < kItemBuckets + 1) P.slotStatus[kSlotBucket + tid] = 0;  // the raster's work list too
 
     // block scan of the pair counts
     int inc = count;
@@ -604,21 +605,39 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(PassParams P, int pas
 
 // binStart[b] = first position of bin b in the sorted keys (a lower bound by
 // binary search, one thread per bin); binStart[nBins] = total.
+__device__ __forceinline__ int first_key_at_least(const int* __restrict__ keys, int total, int b)
+{
+    int lo = 0, hi = total;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (__ldg(keys + mid) < b) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Each bin's first position in the sorted list, and the raster's work list:
+// a bin with n triangles becomes s = min(rowSplit, the largest power of two
+// <= n / kSliceTris) items (row slices when s > 1), in buckets by s, crowded
+// first; empty bins last (they still clear their pixels).
 __global__ void k_bin_bounds(PassParams P, const int* __restrict__ keys)
 {
     if (pass_failed(P.status, P.passSeq)) return;
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     int nBins = P.binsX * P.binsY;
     if (b > nBins) return;
-    int total = P.slotStatus[kSlotTotal];
-    int lo = 0, hi = total;
-    if (b == nBins) lo = total;
-    while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if (__ldg(keys + mid) < b) lo = mid + 1;
-        else hi = mid;
-    }
-    P.binStart[b] = lo;
+    int total = P.slotStatus[kSlotTiles] ? P.slotStatus[kSlotTotal] : 0;
+    int start = b == nBins ? total : first_key_at_least(keys, total, b);
+    P.binStart[b] = start;
+    if (b == nBins) return;
+    const int n = first_key_at_least(keys, total, b + 1) - start;
+    int lg = 0;
+    while (lg < 3 && (1 << (lg + 1)) <= P.rowSplit && n >= (kSliceTris << (lg + 1))) lg++;
+    const int bucket = n == 0 ? 4 : 3 - lg;
+    const int k = 1 << lg;
+    const int at = atomicAdd(P.slotStatus + kSlotBucket + bucket, k);
+    int* out = P.binItems + bucket_base(bucket, nBins) + at;
+    for (int s = 0; s < k; s++) out[s] = b | (s << kItemSliceShift) | (lg << kItemLog2Shift);
 }
 
 // ------------------------------------------------------------------ launches
