@@ -216,7 +216,6 @@ __device__ __forceinline__ int next_bin_item(const PassParams& P)
 constexpr int kRasterThreads = 128;  // 4 warps: warp = column quarter, lane = bin row
 constexpr int kChunk = 128;          // triangles per chunk (one per thread)
 constexpr int kSlots = 128;          // (triangle, row) spans per round (one per thread)
-constexpr int kSplitMin = 2 * kChunk;  // triangles above which a bin is shared out by rows
 
 // FWD (forward mode, 9 or 16 varyings): for passes that blend or may
 // discard, every fragment that passes the depth test is shaded in the walk,
