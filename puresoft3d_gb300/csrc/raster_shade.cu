@@ -25,6 +25,7 @@
 //           the reference's framebuffer bit for bit.
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <vector>
 #include "device_common.cuh"
 
 namespace ps3d {
@@ -711,17 +712,30 @@ __global__ void k_fill_u32(uint32_t* base, int width, int height, int pitchElems
 
 static inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
+// Blocks of `threads` threads of kernel `kern` resident on the current
+// device at once (queried once per kernel and device).
+static int resident_blocks(const void* kern, int threads)
+{
+    thread_local std::vector<std::pair<std::pair<const void*, int>, int>> cache;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    for (const auto& e : cache)
+        if (e.first.first == kern && e.first.second == dev) return e.second;
+    int sms = 0, perSM = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, threads, 0);
+    const int resident = std::max(sms, 1) * std::max(perSM, 1);
+    cache.push_back({{kern, dev}, resident});
+    return resident;
+}
+
 // The persistent raster grid: as many blocks as fit on the device at once
 // (more would only find the list empty), at most one per work item.
 static int raster_grid(const void* kern, int nBins, int rowSplit)
 {
     if (rowSplit <= 1) return nBins;  // one block per bin
-    int dev = 0, sms = 0, perSM = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, kRasterThreads, 0);
     long long items = (long long)nBins * rowSplit;
-    return (int)std::max<long long>(1, std::min<long long>(items, (long long)std::max(sms, 1) * std::max(perSM, 1)));
+    return (int)std::max<long long>(1, std::min<long long>(items, resident_blocks(kern, kRasterThreads)));
 }
 
 template <int BW> void launch_raster(const PassParams& P, int nBins, cudaStream_t s)
@@ -766,9 +780,6 @@ void launch_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
 {
     if (!P.anyColour || P.forward) return;  // a forward pass shaded in the raster
     // a grid that fills the GPU, striding over the shade list
-    int dev = 0, sms = 0, perSM = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     void (*kern)(PassParams) = k_shade<0>;
     switch (P.passFp) {
     case FP_LIT1: kern = k_shade<FP_LIT1>; break;
@@ -782,9 +793,8 @@ void launch_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
     case FP_SATELLITE: kern = k_shade<FP_SATELLITE>; break;
     default: break;
     }
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, 256, 0);
     long long need = ((long long)P.W * P.H + 255) / 256;
-    int grid = (int)std::min<long long>(need, (long long)std::max(sms, 1) * std::max(perSM, 1));
+    int grid = (int)std::min<long long>(need, resident_blocks((const void*)kern, 256));
     pr->begin(K_SHADE, s);
     kern<<<std::max(grid, 1), 256, 0, s>>>(P);
     pr->end(s);
