@@ -405,15 +405,27 @@ __global__ void __launch_bounds__(kSetupThreads, 8) k_setup_emit(PassParams P)
         if (w < warp) wbase += v;
         blockTotal += v;
     }
+    if (tid == 0) {  // publish this block's total first: later blocks' look-backs wait on it
+        volatile unsigned long long* desc = (volatile unsigned long long*)(P.radix + kRadixHdr);
+        desc[b] = (b == 0 ? kDescPrefix : kDescAgg) | (unsigned long long)blockTotal;
+    }
+    {
+        // the radix passes' digit histograms of this block's pairs: they need
+        // no offsets, so they are counted while warp 0 looks back (when the
+        // pairs overflow the room the pass fails and the counts go unused)
+        const int passes = P.radixPasses;
+        for (int by = rect.z; by <= rect.w; by++)
+            for (int bx = rect.x; bx <= rect.y; bx++) {
+                const int key = by * P.binsX + bx;
+                for (int ps = 0; ps < passes; ps++) atomicAdd(&sHist[ps][(key >> (8 * ps)) & 255], 1);
+            }
+    }
     if (warp == 0) {
         // warp-wide look-back: 32 earlier blocks' descriptors per step, up to
         // and including the nearest one that holds an inclusive prefix
         volatile unsigned long long* desc = (volatile unsigned long long*)(P.radix + kRadixHdr);
         long long prefix = 0;
-        if (b == 0) {
-            if (lane == 0) desc[0] = kDescPrefix | (unsigned long long)blockTotal;
-        } else {
-            if (lane == 0) desc[b] = kDescAgg | (unsigned long long)blockTotal;
+        if (b != 0) {
             int top = b - 1, spins = 0;
             while (true) {
                 const int idx = top - lane;
@@ -463,7 +475,6 @@ __global__ void __launch_bounds__(kSetupThreads, 8) k_setup_emit(PassParams P)
         }
     }
     __syncthreads();
-    const int passes = P.radixPasses;
     long long o = (long long)sPrefix + wbase + inc - count;
     for (int by = rect.z; by <= rect.w; by++)
         for (int bx = rect.x; bx <= rect.y; bx++, o++) {
@@ -471,10 +482,9 @@ __global__ void __launch_bounds__(kSetupThreads, 8) k_setup_emit(PassParams P)
             int key = by * P.binsX + bx;
             P.pairKey[o] = key;
             P.pairTri[o] = t;
-            for (int ps = 0; ps < passes; ps++) atomicAdd(&sHist[ps][(key >> (8 * ps)) & 255], 1);
         }
     __syncthreads();
-    for (int i = tid; i < passes * kRadixDigits; i += kSetupThreads) {
+    for (int i = tid; i < P.radixPasses * kRadixDigits; i += kSetupThreads) {
         int v = (&sHist[0][0])[i];
         if (v) atomicAdd(P.radix + i, v);
     }
