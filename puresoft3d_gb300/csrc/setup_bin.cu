@@ -615,17 +615,6 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(PassParams P, int pas
 
 // binStart[b] = first position of bin b in the sorted keys (a lower bound by
 // binary search, one thread per bin); binStart[nBins] = total.
-__device__ __forceinline__ int first_key_at_least(const int* __restrict__ keys, int total, int b)
-{
-    int lo = 0, hi = total;
-    while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if (__ldg(keys + mid) < b) lo = mid + 1;
-        else hi = mid;
-    }
-    return lo;
-}
-
 // Each bin's first position in the sorted list, and the raster's work list:
 // a bin with n triangles becomes s = min(rowSplit, the largest power of two
 // <= n / kSliceTris) items (row slices when s > 1), in buckets by s, crowded
@@ -637,10 +626,28 @@ __global__ void k_bin_bounds(PassParams P, const int* __restrict__ keys)
     int nBins = P.binsX * P.binsY;
     if (b > nBins) return;
     int total = P.slotStatus[kSlotTiles] ? P.slotStatus[kSlotTotal] : 0;
-    int start = b == nBins ? total : first_key_at_least(keys, total, b);
+    if (b == nBins) {
+        P.binStart[b] = total;
+        return;
+    }
+    // the first positions of keys b and b + 1, searched side by side (two
+    // independent loads per step)
+    int lo0 = 0, hi0 = total, lo1 = 0, hi1 = total;
+    while (lo0 < hi0 || lo1 < hi1) {
+        const int m0 = (lo0 + hi0) >> 1, m1 = (lo1 + hi1) >> 1;
+        const int k0 = lo0 < hi0 ? __ldg(keys + m0) : 0, k1 = lo1 < hi1 ? __ldg(keys + m1) : 0;
+        if (lo0 < hi0) {
+            if (k0 < b) lo0 = m0 + 1;
+            else hi0 = m0;
+        }
+        if (lo1 < hi1) {
+            if (k1 < b + 1) lo1 = m1 + 1;
+            else hi1 = m1;
+        }
+    }
+    const int start = lo0;
     P.binStart[b] = start;
-    if (b == nBins) return;
-    const int n = first_key_at_least(keys, total, b + 1) - start;
+    const int n = lo1 - start;
     int lg = 0;
     while (lg < 3 && (1 << (lg + 1)) <= P.rowSplit && n >= (kSliceTris << (lg + 1))) lg++;
     const int bucket = n == 0 ? 4 : 3 - lg;
