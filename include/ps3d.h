@@ -96,6 +96,19 @@ extern "C" {
 #define PS3D_IP_PLANET 0x0702
 #define PS3D_FP_EARTH 0x0703
 #define PS3D_FP_SATELLITE 0x0713
+/* The reference demo's cloud processors (src/test/testproc.cpp).  Cloud:
+ * VBO 0 position, 3 normal, 4 uv; uniforms as the planet's plus textures 9
+ * (the cloud, alpha = its red) and 15 (shadow map); writes white times
+ * 2 * lambert * shadow through write4, so it blends under ALPHABLEND.
+ * CloudShadow: positions x0.95 through (3 * 4), uv from VBO 4, texture 9;
+ * writes no colour and discards where the texel's red is below 150 (an
+ * alpha-tested depth-only pass). */
+#define PS3D_VP_CLOUD 0x0801
+#define PS3D_IP_CLOUD 0x0802
+#define PS3D_FP_CLOUD 0x0803
+#define PS3D_VP_CLOUDSHADOW 0x0901
+#define PS3D_IP_CLOUDSHADOW 0x0902
+#define PS3D_FP_CLOUDSHADOW 0x0903
 #define PS3D_VP_DEF05 0x0501
 #define PS3D_IP_DEF05 0x0502
 #define PS3D_FP_DEF05 0x0503

@@ -59,6 +59,8 @@ enum {
     VP_DEF05 = 0x0501, IP_DEF05 = 0x0502, FP_DEF05 = 0x0503,
     VP_SHADOW = 0x0601,
     VP_PLANET = 0x0701, IP_PLANET = 0x0702, FP_EARTH = 0x0703, FP_SATELLITE = 0x0713,
+    VP_CLOUD = 0x0801, IP_CLOUD = 0x0802, FP_CLOUD = 0x0803,
+    VP_CLOUDSHADOW = 0x0901, IP_CLOUDSHADOW = 0x0902, FP_CLOUDSHADOW = 0x0903,
     FP_LIT1 = 0x1103, FP_LIT1A = 0x1403, FP_LIT3 = 0x1303,
     VP_LIT2 = 0x1201, IP_LIT2 = 0x1202, FP_LIT2 = 0x1203
 };
@@ -305,6 +307,7 @@ static int known_processor(int id)
     case VP_DEF02: case IP_DEF02: case FP_DEF02: case VP_DEF03: case IP_DEF03: case FP_DEF03:
     case VP_DEF04: case IP_DEF04: case FP_DEF04:
     case VP_PLANET: case IP_PLANET: case FP_EARTH: case FP_SATELLITE:
+    case VP_CLOUD: case IP_CLOUD: case FP_CLOUD: case VP_CLOUDSHADOW: case IP_CLOUDSHADOW: case FP_CLOUDSHADOW:
     case VP_SHADOW: case FP_LIT1: case FP_LIT1A: case FP_LIT3: case VP_LIT2: case IP_LIT2: case FP_LIT2:
         return 1;
     }
@@ -513,6 +516,8 @@ static int ip_vecs(int ip)
     case IP_DEF04: return 1; /* PROCDATA_DEF04: direction (skybox.h:3-7) */
     case IP_PLANET: return 6; /* PROCDATA_PLANET: tangent, binormal, normal, worldPos, texcoord, shadowcoord
                                  (test/testproc.h:5-14) */
+    case IP_CLOUD: return 4;  /* PROCDATA_CLOUD: normal, worldPos, texcoord, shadowcoord (test/testproc.h:73-80) */
+    case IP_CLOUDSHADOW: return 1; /* PROCDATA_CLOUDSHADOW: texcoord (test/testproc.h:120-124) */
     default: return 0;       /* IP_DEF05: no varyings (shadow.h) */
     }
 }
@@ -582,6 +587,34 @@ static void run_vp(const ps3do* p, const void* const* in, float* pos, float* use
         tc[0] = uv[0];
         tc[1] = uv[1];
         tc[2] = tc[3] = 0.0f; /* left unset by the reference; never read */
+        break;
+    }
+    case VP_CLOUD: { /* test/testproc.cpp:392-425 */
+        float* nrm = user, * wp = user + 4, * tc = user + 8, * sc = user + 12;
+        const float* uv = (const float*)in[4];
+        m4v4(wp, ufl(p, 4), (const float*)in[0]);
+        m4v4(sc, ufl(p, 16), wp);
+        memcpy(pos, wp, 16);
+        m4v4(pos, ufl(p, 3), pos);
+        wp[3] = 0;
+        m4v4(nrm, ufl(p, 5), (const float*)in[3]);
+        tc[0] = uv[0];
+        tc[1] = uv[1];
+        tc[2] = tc[3] = 0.0f; /* left unset by the reference; never read */
+        break;
+    }
+    case VP_CLOUDSHADOW: { /* test/testproc.cpp:595-610: positions x0.95 (mcemaths_mul_3), (PV*M) * p */
+        float adj[4], pvm[16];
+        const float* uv = (const float*)in[4];
+        memcpy(adj, in[0], 16);
+        adj[0] = adj[0] * 0.95f;
+        adj[1] = adj[1] * 0.95f;
+        adj[2] = adj[2] * 0.95f;
+        m4m4(pvm, ufl(p, 3), ufl(p, 4));
+        m4v4(pos, pvm, adj);
+        user[0] = uv[0];
+        user[1] = uv[1];
+        user[2] = user[3] = 0.0f;
         break;
     }
     case VP_DEF03: { /* tex1bump1light1.cpp:22-46 */
@@ -707,6 +740,22 @@ static int fp_prepare(const ps3do* p, fp_state* s)
         if (t < 0 || t >= p->ntex || !p->tex[t]) return -1;
         s->light = ufl(p, 7);
         s->cam = ufl(p, 8);
+        s->tex = p->tex[t];
+        break;
+    }
+    case FP_CLOUD: { /* test/testproc.cpp:526-532: diffuse 9, shadow 15 */
+        int t = *uin(p, 9), sm = *uin(p, 15);
+        if (t < 0 || t >= p->ntex || !p->tex[t] || p->tex[t]->elemLen != 4) return -1;
+        if (sm < 0 || sm >= p->ntex || !p->tex[sm] || p->tex[sm]->elemLen != 4) return -1;
+        s->light = ufl(p, 7);
+        s->cam = ufl(p, 8);
+        s->tex = p->tex[t];
+        s->proj = p->tex[sm];
+        break;
+    }
+    case FP_CLOUDSHADOW: { /* test/testproc.cpp:672-675: the cloud texture at 9 */
+        int t = *uin(p, 9);
+        if (t < 0 || t >= p->ntex || !p->tex[t] || p->tex[t]->elemLen != 4) return -1;
         s->tex = p->tex[t];
         break;
     }
@@ -1024,6 +1073,51 @@ static void fp_planet(const ps3do* p, const fp_state* s, const float* in, uint8_
     bgra[3] = 0;
 }
 
+/* cvtps2dq (round to nearest even; NaN and |x| >= 2^31 give INT_MIN), then
+   packusdw (int32 -> uint16, saturating) and packuswb (the words read as
+   int16 -> uint8, saturating): the byte FP_Cloud writes for lane value x
+   (test/testproc.cpp:565-571). */
+static uint8_t pack_sse(float x)
+{
+    int i;
+    int w;
+    if (x >= -2147483648.0f && x < 2147483648.0f) {
+        float r = nearbyintf(x); /* the default rounding mode: to nearest even */
+        i = (int)r;
+    } else {
+        i = INT_MIN;
+    }
+    w = i < 0 ? 0 : (i > 65535 ? 65535 : i);
+    if (w >= 32768) return 0; /* a negative int16 */
+    return (uint8_t)(w > 255 ? 255 : w);
+}
+
+/* FP_Cloud::process (test/testproc.cpp:534-574): white, alpha the texel's
+   red; the three colour lanes times 2 lambert x the projective shadow
+   factor (mcemaths_mul_3); packed as above; written through write4. */
+static void fp_cloud(const fp_state* s, const float* in, uint8_t* bgra)
+{
+    const float* nrm = in, * wp = in + 4, * tc = in + 8, * sc = in + 12;
+    float t[4], c[4], L[4], dist, r, lambert, f;
+    sample_nearest(s->tex, tc, t);
+    c[0] = 255.0f;
+    c[1] = 255.0f;
+    c[2] = 255.0f;
+    c[3] = t[2];
+    f = sample_proj(s->proj, sc);
+    for (int k = 0; k < 4; k++) L[k] = s->light[k] - wp[k];
+    dist = sqrtf((L[0] * L[0] + L[1] * L[1]) + (L[2] * L[2] + L[3] * L[3]));
+    r = 1.0f / dist;
+    for (int k = 0; k < 4; k++) L[k] = L[k] * r;
+    /* E and H are computed by the reference but unused */
+    lambert = 2.0f * ((L[0] * nrm[0] + L[1] * nrm[1]) + (L[2] * nrm[2] + L[3] * nrm[3]));
+    f = lambert * f;
+    c[0] = c[0] * f;
+    c[1] = c[1] * f;
+    c[2] = c[2] * f;
+    for (int k = 0; k < 4; k++) bgra[k] = pack_sse(c[k]);
+}
+
 /* FragmentProcessorDEF03::process (tex1bump1light1.cpp:180-239): the bump
    texel's (r, g, b, 0) / 255 * 2 - 1 on four lanes, through the matrix whose
    columns are the tangent, binormal, normal and 0 (mcemaths_make_tbn,
@@ -1104,6 +1198,12 @@ static int run_fp(const ps3do* p, const fp_state* s, const float* in, uint8_t* b
     case FP_DEF04: sample_cube(s->cube, in, bgra); return 1; /* skybox.cpp:127-134 */
     case FP_EARTH:
     case FP_SATELLITE: fp_planet(p, s, in, bgra); return 1;
+    case FP_CLOUD: fp_cloud(s, in, bgra); return 1;
+    case FP_CLOUDSHADOW: { /* test/testproc.cpp:677-686: discard where the texel's red is below 150 */
+        float t[4];
+        sample_nearest(s->tex, in, t);
+        return t[2] < 150.0f ? 2 : 0;
+    }
     case FP_LIT1: {
         sr_level t = level_of(s->tex);
         sr_shade_lit1(&t, s->light, s->cam, in, in + 4, in + 8, bgra);

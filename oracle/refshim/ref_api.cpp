@@ -96,6 +96,12 @@ PuresoftProcessor* make_processor(int id)
     case 0x0702: return new IP_Planet;
     case 0x0703: return new FP_Earth;
     case 0x0713: return new FP_Satellite;
+    case 0x0801: return new VP_Cloud;   /* the demo's cloud sets (test/testproc.cpp) */
+    case 0x0802: return new IP_Cloud;
+    case 0x0803: return new FP_Cloud;
+    case 0x0901: return new VP_CloudShadow;
+    case 0x0902: return new IP_CloudShadow;
+    case 0x0903: return new FP_CloudShadow;
     case 0x0501: return new VertexProcesserDEF05;
     case 0x0502: return new InterpolationProcessorDEF05;
     case 0x0503: return new FragmentProcessorDEF05;

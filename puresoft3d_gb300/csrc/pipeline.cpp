@@ -300,6 +300,8 @@ int required_vary(int ip)
     case IP_DEF03: return 17;
     case IP_DEF04: return 3;   // direction xyz
     case IP_PLANET: return 21; // tangent, binormal, normal xyzw, worldPos xyz, uv, shadow coordinate xyzw
+    case IP_CLOUD: return 13;  // normal xyzw, worldPos xyz, uv, shadow coordinate xyzw
+    case IP_CLOUDSHADOW: return 2;  // uv
     case IP_LIT2: return 16;
     default: return 0;
     }
@@ -314,6 +316,8 @@ int fp_needs(int fp)
     case FP_DEF03: return IP_DEF03;
     case FP_DEF04: return IP_DEF04;
     case FP_EARTH: case FP_SATELLITE: return IP_PLANET;
+    case FP_CLOUD: return IP_CLOUD;
+    case FP_CLOUDSHADOW: return IP_CLOUDSHADOW;
     default: return 0;
     }
 }
@@ -327,6 +331,8 @@ int vp_gives(int vp)
     case VP_DEF03: return IP_DEF03;
     case VP_DEF04: return IP_DEF04;
     case VP_PLANET: return IP_PLANET;
+    case VP_CLOUD: return IP_CLOUD;
+    case VP_CLOUDSHADOW: return IP_CLOUDSHADOW;
     default: return 0;
     }
 }
@@ -339,6 +345,7 @@ bool known_processor(int id)
     case VP_DEF02: case IP_DEF02: case FP_DEF02: case VP_DEF03: case IP_DEF03: case FP_DEF03:
     case VP_DEF04: case IP_DEF04: case FP_DEF04:
     case VP_PLANET: case IP_PLANET: case FP_EARTH: case FP_SATELLITE:
+    case VP_CLOUD: case IP_CLOUD: case FP_CLOUD: case VP_CLOUDSHADOW: case IP_CLOUDSHADOW: case FP_CLOUDSHADOW:
         return true;
     }
     return false;
@@ -402,6 +409,7 @@ int snapshot_uniforms(const ps3d_pipeline* p, DrawUniforms& U)
         if ((rc = need(3, U.PV, 16)) || (rc = need(4, U.M, 16)) || (rc = need(5, U.Mrot, 16))) return rc;
         break;
     case VP_PLANET:  // test/testproc.cpp:29-35: DEF03's matrices and the shadow projection at 16
+    case VP_CLOUD:   // test/testproc.cpp:384-390: the same four
         if ((rc = need(3, U.PV, 16)) || (rc = need(4, U.M, 16)) || (rc = need(5, U.Mrot, 16)) ||
             (rc = need(16, U.LPV, 16)))
             return rc;
@@ -415,6 +423,7 @@ int snapshot_uniforms(const ps3d_pipeline* p, DrawUniforms& U)
         break;
     }
     case VP_DEF05:
+    case VP_CLOUDSHADOW:  // test/testproc.cpp:588-593
     case VP_SHADOW:
         if ((rc = need(3, U.PV, 16)) || (rc = need(4, U.M, 16))) return rc;
         m4m4(U.PVM, U.PV, U.M);
@@ -446,6 +455,19 @@ int snapshot_uniforms(const ps3d_pipeline* p, DrawUniforms& U)
         U.tex = lv[0];
         U.tex2 = lv[1];
         for (int i = 2; i < n; i++) U.ptex[i - 2] = lv[i];
+        break;
+    }
+    case FP_CLOUD:          // test/testproc.cpp:526-532: diffuse 9, shadow 15
+    case FP_CLOUDSHADOW: {  // test/testproc.cpp:672-675: the cloud texture at 9
+        if (p->fp == FP_CLOUD && ((rc = need(7, U.light, 4)) || (rc = need(8, U.cam, 4)))) return rc;
+        const int slots[2] = {9, 15};
+        for (int i = 0; i < (p->fp == FP_CLOUD ? 2 : 1); i++) {
+            const int* t = uint_(p, slots[i], 1);
+            if (!t) return fail(PS3D_ERR_INVALID, "uniform %d (texture index) is not set", slots[i]);
+            if (!tex_ok(p, *t)) return fail(PS3D_ERR_RANGE, "uniform %d: texture %d", slots[i], *t);
+            if (p->tex[*t].elemLen != 4) return fail(PS3D_ERR_INVALID, "texture %d: 4-byte texels expected", *t);
+            (i ? U.ptex[0] : U.tex) = level_of(p->tex[*t]);
+        }
         break;
     }
     case FP_DEF04: {  // skybox.cpp:122-125: the cube map's index at uniform 2
@@ -660,11 +682,14 @@ int copy_colour_plain(ps3d_pipeline* p, const Command& c)
 // The draws of a pass as device descriptors: triangle bases are running
 // sums, so a pass's triangles are numbered in submission order.
 // A pass is shaded forward (every passing fragment, in order, in the raster)
-// when a draw blends or its fragment processor may discard.
+// when a draw blends or its fragment processor may discard (a depth-only
+// draw whose processor discards included).
 bool pass_forward(const DrawDesc* dd, size_t n)
 {
     for (size_t i = 0; i < n; i++)
-        if ((dd[i].flags & F_COLOUR) && ((dd[i].flags & B_ALPHABLEND) || dd[i].fp == FP_LIT1A)) return true;
+        if (((dd[i].flags & F_COLOUR) && ((dd[i].flags & B_ALPHABLEND) || dd[i].fp == FP_LIT1A)) ||
+            (dd[i].flags & F_FRAGMENT))
+            return true;
     return false;
 }
 
@@ -837,7 +862,7 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     // buffer and samples its textures there
     const bool rasterColour = fuseColour || (forward && anyColour);
     std::vector<const void*> sampled;
-    if (anyColour) sampled_targets(p, uu, sampled);
+    if (anyColour || forward) sampled_targets(p, uu, sampled);
     if ((rc = before_write(p, s, tg.depth))) return rc;
     if (rasterColour && (rc = before_write(p, s, p->colour))) return rc;
     if (forward)
@@ -1536,7 +1561,9 @@ int ps3d_draw(ps3d_pipeline* p, int vao)
     d.fp = p->fp;
     int need = fp_needs(p->fp);
     d.nv = need ? required_vary(need) : 0;
-    d.flags = (p->behavior & 0xf) | (p->fp != FP_DEF05 ? F_COLOUR : 0);
+    // DEF05 writes nothing; CloudShadow only discards (its depth-only pass)
+    d.flags = (p->behavior & 0xf) |
+              (p->fp == FP_CLOUDSHADOW ? F_FRAGMENT : p->fp != FP_DEF05 ? F_COLOUR : 0);
     // processVertices stops at the first VBO that runs out (vertthrd.cpp:18-31)
     long long minCount = -1;
     for (int s = 0; s < PS3D_MAX_VBOS; s++)
@@ -1548,6 +1575,8 @@ int ps3d_draw(ps3d_pipeline* p, int vao)
     if (p->vp == VP_DEF03 && d.nv) reqSlots[1] = reqSlots[2] = reqSlots[3] = reqSlots[4] = 1;
     if (p->vp == VP_DEF02 && d.nv) reqSlots[1] = reqSlots[2] = 1;
     if (p->vp == VP_PLANET && d.nv) reqSlots[1] = reqSlots[2] = reqSlots[3] = reqSlots[4] = 1;
+    if (p->vp == VP_CLOUD && d.nv) reqSlots[3] = reqSlots[4] = 1;
+    if (p->vp == VP_CLOUDSHADOW && d.nv) reqSlots[4] = 1;
     for (int s = 0; s < kVboSlots; s++) {
         if (reqSlots[s] && !va.vbo[s]) return fail(PS3D_ERR_INVALID, "the vertex processor reads VBO slot %d", s);
         if (va.vbo[s]) {

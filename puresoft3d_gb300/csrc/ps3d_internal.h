@@ -28,6 +28,8 @@ enum : int {
     VP_DEF05 = 0x0501, IP_DEF05 = 0x0502, FP_DEF05 = 0x0503,
     VP_SHADOW = 0x0601,
     VP_PLANET = 0x0701, IP_PLANET = 0x0702, FP_EARTH = 0x0703, FP_SATELLITE = 0x0713,
+    VP_CLOUD = 0x0801, IP_CLOUD = 0x0802, FP_CLOUD = 0x0803,
+    VP_CLOUDSHADOW = 0x0901, IP_CLOUDSHADOW = 0x0902, FP_CLOUDSHADOW = 0x0903,
     FP_LIT1 = 0x1103, FP_LIT1A = 0x1403, FP_LIT3 = 0x1303,
     VP_LIT2 = 0x1201, IP_LIT2 = 0x1202, FP_LIT2 = 0x1203,
 };
@@ -42,6 +44,7 @@ enum : int { PP_ADD8 = 0x7001, PP_FOG = 0x7002 };
 enum : int {
     B_UPDATE_DEPTH = 1, B_TEST_DEPTH = 2, B_FACE_CULLING = 4, B_ALPHABLEND = 8,
     F_COLOUR = 16,   // the fragment stage writes colour
+    F_FRAGMENT = 32, // the fragment stage runs without writing colour (it may discard)
 };
 
 // One 2D texture level in device memory; row r starts at base + r*scanline

@@ -157,6 +157,14 @@ __device__ __forceinline__ int shade_fragment(const DrawDesc& d, const DrawUnifo
             return 1;
         }
         return 0;
+    case FP_CLOUD:
+        if constexpr (NV >= 13) {
+            bgra = shade_cloud(U, in);
+            return 1;
+        }
+        return 0;
+    case FP_CLOUDSHADOW:  // test/testproc.cpp:677-686: discards where the texel's red is below 150
+        return ((nearest_texel(U.tex, in[0], in[1]) >> 16) & 0xff) < 150u ? 2 : 0;
     case FP_EARTH:
     case FP_SATELLITE:
         if constexpr (NV >= 21) {
@@ -490,7 +498,7 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
                                 passed++;
                                 int w = 0;
                                 uint32_t bgra = 0;
-                                if (flags & F_COLOUR) {
+                                if (flags & (F_COLOUR | F_FRAGMENT)) {
                                     const TriRaster& t = sTri[j];
                                     if (!begun) {
                                         Span sp;
@@ -644,6 +652,12 @@ __device__ __forceinline__ void shade_entry(const PassParams& P, int2 e)
         bgra = shade_planet(U, in, (FPK ? FPK : d.fp) == FP_EARTH);
         break;
     }
+    case FP_CLOUD: {
+        float in[13];
+        fragment_varyings<13>(t, vary, P.nvMax, s, z, xl, in);
+        bgra = shade_cloud(U, in);
+        break;
+    }
     case FP_DEF03: {
         float in[17];
         fragment_varyings<17>(t, vary, P.nvMax, s, z, xl, in);
@@ -791,6 +805,7 @@ void launch_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
     case FP_DEF04: kern = k_shade<FP_DEF04>; break;
     case FP_EARTH: kern = k_shade<FP_EARTH>; break;
     case FP_SATELLITE: kern = k_shade<FP_SATELLITE>; break;
+    case FP_CLOUD: kern = k_shade<FP_CLOUD>; break;
     default: break;
     }
     long long need = ((long long)P.W * P.H + 255) / 256;

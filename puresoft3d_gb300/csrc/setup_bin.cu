@@ -44,6 +44,7 @@ __device__ __forceinline__ void vp_position(const DrawDesc& d, const DrawUniform
     case VP_DEF02:   // colr1light1.cpp:22-40
     case VP_DEF03:   // tex1bump1light1.cpp:22-46
     case VP_LIT2:
+    case VP_CLOUD:     // test/testproc.cpp:392-425
     case VP_PLANET: {  // test/testproc.cpp:37-71
         float wp[4];
         m4v4(wp, U.M, p);
@@ -55,6 +56,11 @@ __device__ __forceinline__ void vp_position(const DrawDesc& d, const DrawUniform
         break;
     case VP_DEF05: {  // shadow.cpp:21-29: positions x0.9 (mcemaths_mul_3), then (PV*M) * p
         float a[4] = {fmul(p[0], 0.9f), fmul(p[1], 0.9f), fmul(p[2], 0.9f), p[3]};
+        m4v4(pos, U.PVM, a);
+        break;
+    }
+    case VP_CLOUDSHADOW: {  // test/testproc.cpp:595-610: positions x0.95, then (PV*M) * p
+        float a[4] = {fmul(p[0], 0.95f), fmul(p[1], 0.95f), fmul(p[2], 0.95f), p[3]};
         m4v4(pos, U.PVM, a);
         break;
     }
@@ -119,6 +125,25 @@ __device__ __forceinline__ void vp_varyings(const DrawDesc& d, const DrawUniform
         vary[12] = wp[0]; vary[13] = wp[1]; vary[14] = wp[2];
         vary[15] = __ldg(uv); vary[16] = __ldg(uv + 1);
         vary[17] = sc[0]; vary[18] = sc[1]; vary[19] = sc[2]; vary[20] = sc[3];
+        break;
+    }
+    case VP_CLOUD: {  // test/testproc.cpp:392-425: normal (Mrot, four lanes), world
+                      // position xyz, uv, the world position through the shadow projection
+        float wp[4], n[4], nrm[4], sc[4];
+        m4v4(wp, U.M, p);
+        m4v4(sc, U.LPV, wp);
+        ld4(d.vbo[3] + (size_t)idx * d.stride[3], n);
+        m4v4(nrm, U.Mrot, n);
+        const float* uv = (const float*)(d.vbo[4] + (size_t)idx * d.stride[4]);
+        vary[0] = nrm[0]; vary[1] = nrm[1]; vary[2] = nrm[2]; vary[3] = nrm[3];
+        vary[4] = wp[0]; vary[5] = wp[1]; vary[6] = wp[2];
+        vary[7] = __ldg(uv); vary[8] = __ldg(uv + 1);
+        vary[9] = sc[0]; vary[10] = sc[1]; vary[11] = sc[2]; vary[12] = sc[3];
+        break;
+    }
+    case VP_CLOUDSHADOW: {  // test/testproc.cpp:595-610: uv only
+        const float* uv = (const float*)(d.vbo[4] + (size_t)idx * d.stride[4]);
+        vary[0] = __ldg(uv); vary[1] = __ldg(uv + 1);
         break;
     }
     case VP_DEF03: {  // tex1bump1light1.cpp:22-46
@@ -320,6 +345,10 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float
             vp_varyings(d, U, 3 * lt + v, vary);
             // constant trip counts keep `vary` in registers
             switch (d.nv) {
+            case 2:
+                vout[v * P.nvMax] = vary[0];
+                vout[v * P.nvMax + 1] = vary[1];
+                break;
             case 3:
 #pragma unroll
                 for (int k = 0; k < 3; k++) vout[v * P.nvMax + k] = vary[k];
@@ -331,6 +360,10 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float
             case 11:
 #pragma unroll
                 for (int k = 0; k < 11; k++) vout[v * P.nvMax + k] = vary[k];
+                break;
+            case 13:
+#pragma unroll
+                for (int k = 0; k < 13; k++) vout[v * P.nvMax + k] = vary[k];
                 break;
             case 16:
 #pragma unroll

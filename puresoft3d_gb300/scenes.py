@@ -43,6 +43,8 @@ VP_DEF05, IP_DEF05, FP_DEF05 = 0x0501, 0x0502, 0x0503
 VP_SHADOW = 0x0601
 # the reference demo's planet set (src/test/testproc.cpp)
 VP_PLANET, IP_PLANET, FP_EARTH, FP_SATELLITE = 0x0701, 0x0702, 0x0703, 0x0713
+VP_CLOUD, IP_CLOUD, FP_CLOUD = 0x0801, 0x0802, 0x0803
+VP_CLOUDSHADOW, IP_CLOUDSHADOW, FP_CLOUDSHADOW = 0x0901, 0x0902, 0x0903
 FP_LIT1, FP_LIT1A, FP_LIT3 = 0x1103, 0x1403, 0x1303
 VP_LIT2, IP_LIT2, FP_LIT2 = 0x1201, 0x1202, 0x1203
 

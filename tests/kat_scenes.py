@@ -246,6 +246,53 @@ def _planet_scene(name, w, h, seed, fp, blend=False):
                                                    "shadow_texture": shadow})
 
 
+def _cloud_scene(name, w, h, seed):
+    """The reference demo's cloud processors (test/testproc.cpp): an
+    alpha-tested depth-only pass (VP_CloudShadow / FP_CloudShadow: texels
+    whose red is below 150 discard) into a 64x64 shadow map, then the
+    clouds blended over the frame (VP_Cloud / FP_Cloud: alpha = the texel's
+    red, lambert x the projective shadow factor, packed with the SSE
+    saturating conversions)."""
+    b = S._Builder()
+    rng = np.random.default_rng(seed)
+    cloud = b.texture(S.checker_noise_bgra(16, 4, rng, noise=90, lo=60, hi=230), wrap=True)
+    shadow = b.empty_texture(64, 64)
+    depth = b.empty_texture(w, h)
+    mesh = _tri_mesh(random_soup(220, seed))
+    shadow_prog = b.programme(S.VP_CLOUDSHADOW, S.IP_CLOUDSHADOW, S.FP_CLOUDSHADOW)
+    cloud_prog = b.programme(S.VP_CLOUD, S.IP_CLOUD, S.FP_CLOUD)
+    vao = b.vao(mesh, slots=(0, 3, 4))
+    c, s_ = np.cos(0.5), np.sin(0.5)
+    light = np.array([[0.8 * c, 0.1, 0.5 * s_, 0.05], [0.0, 0.8, 0.1, -0.05], [-0.4 * s_, 0.0, 0.4 * c, 0.0],
+                      [0.0, 0.0, 0.0, 1.0]])
+    bias = np.array([[0.5, 0, 0, 0.5], [0, 0.5, 0, 0.5], [0, 0, 1, 0], [0, 0, 0, 1]])
+    eye = np.eye(4)
+    b.f("setViewport", 64, 64)
+    b.f("setDepth", shadow)
+    b.f("clearDepth", 1.0)
+    b.f("useProgramme", shadow_prog)
+    b.f("setUniform", 3, S.col_major(light))
+    b.f("setUniform", 4, S.col_major(eye))
+    b.f("setUniform", 9, np.array([cloud], dtype=np.int32))
+    b.f("drawVAO", vao)
+    b.f("setViewport", w, h)
+    b.f("setDepth", depth)
+    b.f("clearDepth", 1.0)
+    b.f("clearColour", 0xFF402010)
+    b.f("enable", S.ALPHABLEND)
+    b.f("useProgramme", cloud_prog)
+    for slot in (3, 4, 5):
+        b.f("setUniform", slot, S.col_major(eye))
+    b.f("setUniform", 16, S.col_major(bias @ light))
+    b.f("setUniform", 7, S.vec4(0.3, 0.9, 1.6))
+    b.f("setUniform", 8, S.vec4(0, 0, 2, 1))
+    b.f("setUniform", 15, np.array([shadow], dtype=np.int32))
+    b.f("drawVAO", vao)
+    b.f("disable", S.ALPHABLEND)
+    return S.Scene(name, w, h, b.setup, b.frame, {"triangles": 440, "depth_texture": depth,
+                                                   "shadow_texture": shadow})
+
+
 def _v(x, y, z=0.0, w=1.0):
     return [x * w, y * w, z * w, w]
 
@@ -335,4 +382,5 @@ def kat_scenes():
     # the reference demo's planet processors with the projective shadow lookup
     out.append(("kat_def0_planet_earth_96x64", _planet_scene("kat_planet_earth", 96, 64, 23, S.FP_EARTH)))
     out.append(("kat_def0_planet_satellite_80x60", _planet_scene("kat_planet_satellite", 80, 60, 24, S.FP_SATELLITE)))
+    out.append(("kat_def0_planet_cloud_88x64", _cloud_scene("kat_cloud", 88, 64, 25)))
     return out

@@ -67,7 +67,8 @@ def test_bin_capacity_replay(gpu_lib, monkeypatch, case):
 @pytest.mark.parametrize("cull", [1, 0])
 @pytest.mark.parametrize("occupancy", [0, 8])
 @pytest.mark.parametrize("bin_w", [8, 16, 32])
-@pytest.mark.parametrize("case", ["kat_soup_depth", "c3_small", "kat_post_add_fog", "kat_alphatest_blend"])
+@pytest.mark.parametrize("case", ["kat_soup_depth", "c3_small", "kat_post_add_fog", "kat_alphatest_blend",
+                                  "kat_def0_planet_cloud"])
 def test_schedules_agree(gpu_lib, bin_w, occupancy, cull, split, case):
     """Every schedule (bin width x raster kernel variants: occupancy, span
     culling, row split) gives the oracle's result."""
