@@ -109,6 +109,26 @@ extern "C" {
 #define PS3D_VP_CLOUDSHADOW 0x0901
 #define PS3D_IP_CLOUDSHADOW 0x0902
 #define PS3D_FP_CLOUDSHADOW 0x0903
+/* The scene viewer demo's processors (src/test2/testproc.cpp), with its
+ * uniform slots: 0 model, 1 model rotation, 5 PVM, 6 shadow projection;
+ * 20 light position, 21 light direction, 22 camera, 23 shadow map (texture
+ * index); 30 ambient, 31 diffuse colour, 32 specular colour, 33 specular
+ * exponent (one float); 40 diffuse texture (index).  VBO 0 position, 3
+ * normal, 4 uv.  Lighting is a 25-degree spotlight (cos^150 fall-off
+ * outside the cone) with the 4-tap projective shadow lookup.  PositionOnly +
+ * Null + SingleColourNoLighting draws the flat diffuse colour; Shadow (x0.9)
+ * + Null + FP Null is the depth-only shadow pass. */
+#define PS3D_VP_POSITIONONLY 0x0A01
+#define PS3D_IP_NULL 0x0A02
+#define PS3D_FP_SINGLECOLOURNOLIGHTING 0x0A03
+#define PS3D_VP_SINGLECOLOUR 0x0B01
+#define PS3D_IP_SINGLECOLOUR 0x0B02
+#define PS3D_FP_SINGLECOLOUR 0x0B03
+#define PS3D_VP_DIFFUSEONLY 0x0C01
+#define PS3D_IP_DIFFUSEONLY 0x0C02
+#define PS3D_FP_DIFFUSEONLY 0x0C03
+#define PS3D_VP_VIEWERSHADOW 0x0D01
+#define PS3D_FP_NULL 0x0D03
 #define PS3D_VP_DEF05 0x0501
 #define PS3D_IP_DEF05 0x0502
 #define PS3D_FP_DEF05 0x0503

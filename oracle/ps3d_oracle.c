@@ -61,6 +61,11 @@ enum {
     VP_PLANET = 0x0701, IP_PLANET = 0x0702, FP_EARTH = 0x0703, FP_SATELLITE = 0x0713,
     VP_CLOUD = 0x0801, IP_CLOUD = 0x0802, FP_CLOUD = 0x0803,
     VP_CLOUDSHADOW = 0x0901, IP_CLOUDSHADOW = 0x0902, FP_CLOUDSHADOW = 0x0903,
+    /* the scene viewer demo's sets (test2/testproc.h) */
+    VP_POSITIONONLY = 0x0A01, IP_NULL = 0x0A02, FP_SINGLECOLOURNL = 0x0A03,
+    VP_SINGLECOLOUR = 0x0B01, IP_SINGLECOLOUR = 0x0B02, FP_SINGLECOLOUR = 0x0B03,
+    VP_DIFFUSEONLY = 0x0C01, IP_DIFFUSEONLY = 0x0C02, FP_DIFFUSEONLY = 0x0C03,
+    VP_SHADOW2 = 0x0D01, FP_NULL = 0x0D03,
     FP_LIT1 = 0x1103, FP_LIT1A = 0x1403, FP_LIT3 = 0x1303,
     VP_LIT2 = 0x1201, IP_LIT2 = 0x1202, FP_LIT2 = 0x1203
 };
@@ -308,6 +313,8 @@ static int known_processor(int id)
     case VP_DEF04: case IP_DEF04: case FP_DEF04:
     case VP_PLANET: case IP_PLANET: case FP_EARTH: case FP_SATELLITE:
     case VP_CLOUD: case IP_CLOUD: case FP_CLOUD: case VP_CLOUDSHADOW: case IP_CLOUDSHADOW: case FP_CLOUDSHADOW:
+    case VP_POSITIONONLY: case IP_NULL: case FP_SINGLECOLOURNL: case VP_SINGLECOLOUR: case IP_SINGLECOLOUR:
+    case FP_SINGLECOLOUR: case VP_DIFFUSEONLY: case IP_DIFFUSEONLY: case FP_DIFFUSEONLY: case VP_SHADOW2: case FP_NULL:
     case VP_SHADOW: case FP_LIT1: case FP_LIT1A: case FP_LIT3: case VP_LIT2: case IP_LIT2: case FP_LIT2:
         return 1;
     }
@@ -518,6 +525,9 @@ static int ip_vecs(int ip)
                                  (test/testproc.h:5-14) */
     case IP_CLOUD: return 4;  /* PROCDATA_CLOUD: normal, worldPos, texcoord, shadowcoord (test/testproc.h:73-80) */
     case IP_CLOUDSHADOW: return 1; /* PROCDATA_CLOUDSHADOW: texcoord (test/testproc.h:120-124) */
+    case IP_SINGLECOLOUR: return 3; /* PROCDATA_SINGLECOLOUR: normal, worldPos, shadowcoord (test2/testproc.h:83-90) */
+    case IP_DIFFUSEONLY: return 4;  /* PROCDATA_DIFFUSEONLY: normal, worldPos, texcoord, shadowcoord
+                                       (test2/testproc.h:136-144) */
     default: return 0;       /* IP_DEF05: no varyings (shadow.h) */
     }
 }
@@ -601,6 +611,37 @@ static void run_vp(const ps3do* p, const void* const* in, float* pos, float* use
         tc[0] = uv[0];
         tc[1] = uv[1];
         tc[2] = tc[3] = 0.0f; /* left unset by the reference; never read */
+        break;
+    }
+    case VP_POSITIONONLY: /* test2/testproc.cpp:13-23: PVM (uniform 5) * p */
+        m4v4(pos, ufl(p, 5), (const float*)in[0]);
+        break;
+    case VP_SHADOW2: { /* test2/testproc.cpp:507-518: positions x0.9 (mcemaths_mul_3), then PVM (5) * p */
+        float adj[4];
+        memcpy(adj, in[0], 16);
+        adj[0] = adj[0] * 0.9f;
+        adj[1] = adj[1] * 0.9f;
+        adj[2] = adj[2] * 0.9f;
+        m4v4(pos, ufl(p, 5), adj);
+        break;
+    }
+    case VP_SINGLECOLOUR:   /* test2/testproc.cpp:88-116 */
+    case VP_DIFFUSEONLY: {  /* test2/testproc.cpp:304-336: world position M (0) * p, its
+                               shadow projection (6), PVM (5) * p, normal MR (1) * n */
+        const int diffuse = p->vp == VP_DIFFUSEONLY;
+        float* nrm = user, * wp = user + 4, * sc = user + (diffuse ? 12 : 8);
+        m4v4(wp, ufl(p, 0), (const float*)in[0]);
+        m4v4(sc, ufl(p, 6), wp);
+        if (!diffuse) wp[3] = 0;
+        m4v4(pos, ufl(p, 5), (const float*)in[0]);
+        if (diffuse) wp[3] = 0;
+        m4v4(nrm, ufl(p, 1), (const float*)in[3]);
+        if (diffuse) {
+            const float* uv = (const float*)in[4];
+            user[8] = uv[0];
+            user[9] = uv[1];
+            user[10] = user[11] = 0.0f; /* left unset by the reference; never read */
+        }
         break;
     }
     case VP_CLOUDSHADOW: { /* test/testproc.cpp:595-610: positions x0.95 (mcemaths_mul_3), (PV*M) * p */
@@ -727,6 +768,11 @@ typedef struct {
     const float* shadow;
     int shadowSize, shadowScan;
     float lodScale, bias;
+    /* the scene viewer demo's lighting (test2/testproc.h:1-30: uniforms 21
+       light direction, 30 ambient, 31 diffuse, 32 specular colour, 33
+       specular exponent) */
+    const float* ldir, * amb, * dif, * scol;
+    unsigned sexp;
 } fp_state;
 
 static int fp_prepare(const ps3do* p, fp_state* s)
@@ -751,6 +797,29 @@ static int fp_prepare(const ps3do* p, fp_state* s)
         s->cam = ufl(p, 8);
         s->tex = p->tex[t];
         s->proj = p->tex[sm];
+        break;
+    }
+    case FP_SINGLECOLOURNL: /* test2/testproc.cpp:49-53 */
+        s->dif = ufl(p, 31);
+        break;
+    case FP_SINGLECOLOUR:   /* test2/testproc.cpp:199-209 */
+    case FP_DIFFUSEONLY: {  /* test2/testproc.cpp:447-456: shadow map 23, diffuse texture 40 */
+        int sm = *uin(p, 23);
+        if (sm < 0 || sm >= p->ntex || !p->tex[sm] || p->tex[sm]->elemLen != 4) return -1;
+        s->proj = p->tex[sm];
+        if (p->fp == FP_DIFFUSEONLY) {
+            int t = *uin(p, 40);
+            if (t < 0 || t >= p->ntex || !p->tex[t] || p->tex[t]->elemLen != 4) return -1;
+            s->tex = p->tex[t];
+        } else {
+            s->dif = ufl(p, 31);
+            s->scol = ufl(p, 32);
+        }
+        s->light = ufl(p, 20);
+        s->ldir = ufl(p, 21);
+        s->cam = ufl(p, 22);
+        s->amb = ufl(p, 30);
+        s->sexp = (unsigned)*ufl(p, 33);
         break;
     }
     case FP_CLOUDSHADOW: { /* test/testproc.cpp:672-675: the cloud texture at 9 */
@@ -1118,6 +1187,93 @@ static void fp_cloud(const fp_state* s, const float* in, uint8_t* bgra)
     for (int k = 0; k < 4; k++) bgra[k] = pack_sse(c[k]);
 }
 
+/* The scene viewer's spotlight terms (test2/testproc.cpp:220-238 and
+   470-488): L, E, H normalised (IEEE 1/sqrt in place of rsqrtss), lambert =
+   L.n scaled outside the 25-degree cone by cos(yaw - cone)^150, specular =
+   (H.n)^exponent (no clamp before the power), both clamped to [0, 1] by
+   clamp_3_4 (NaN -> 0).  f[0] lambert, f[1] specular. */
+static float norm_rcp(const float* v) { return 1.0f / sqrtf((v[0] * v[0] + v[1] * v[1]) + (v[2] * v[2] + v[3] * v[3])); }
+
+static float opt_powf(float x, unsigned n) /* proc.h:73-86 */
+{
+    float pw = 1.0f;
+    while (n > 0) {
+        if (n & 1) pw *= x;
+        x *= x;
+        n >>= 1;
+    }
+    return pw;
+}
+
+static float clamp01(float v)
+{
+    v = v > 0.0f ? v : 0.0f; /* maxps: NaN -> the bound */
+    return v < 1.0f ? v : 1.0f;
+}
+
+static void spot_factors(const fp_state* s, const float* nrm, const float* wp, float f[2])
+{
+    const float fieldOfLight = 6.283185f * (25.0f / 360.0f); /* test2/testproc.cpp:9 */
+    float L[4], E[4], Hv[4], r, yaw;
+    for (int k = 0; k < 4; k++) L[k] = s->light[k] - wp[k];
+    r = norm_rcp(L);
+    for (int k = 0; k < 4; k++) L[k] = L[k] * r;
+    for (int k = 0; k < 4; k++) E[k] = s->cam[k] - wp[k];
+    r = norm_rcp(E);
+    for (int k = 0; k < 4; k++) E[k] = E[k] * r;
+    for (int k = 0; k < 4; k++) Hv[k] = E[k] + L[k];
+    r = norm_rcp(Hv);
+    for (int k = 0; k < 4; k++) Hv[k] = Hv[k] * r;
+    f[0] = (L[0] * nrm[0] + L[1] * nrm[1]) + (L[2] * nrm[2] + L[3] * nrm[3]);
+    yaw = acosf((L[0] * s->ldir[0] + L[1] * s->ldir[1]) + (L[2] * s->ldir[2] + L[3] * s->ldir[3]));
+    f[0] = f[0] * (yaw < fieldOfLight ? 1.0f : opt_powf(cosf(yaw - fieldOfLight), 150));
+    f[1] = opt_powf((Hv[0] * nrm[0] + Hv[1] * nrm[1]) + (Hv[2] * nrm[2] + Hv[3] * nrm[3]), s->sexp);
+    f[0] = clamp01(f[0]);
+    f[1] = clamp01(f[1]);
+}
+
+/* FP_SingleColour::process (test2/testproc.cpp:211-261) over (normal, world
+   position, shadow coordinate). */
+static void fp_single_colour(const fp_state* s, const float* in, uint8_t* bgra)
+{
+    const float* nrm = in, * wp = in + 4, * sc = in + 8;
+    const float shadow = sample_proj(s->proj, sc);
+    float f[2], o[4];
+    spot_factors(s, nrm, wp, f);
+    for (int k = 0; k < 4; k++) {
+        float sp = (s->dif[k] * s->scol[k]) * f[1];
+        float am = s->dif[k] * s->amb[k];
+        o[k] = ((s->dif[k] * f[0] + sp) * shadow + am);
+        o[k] = clamp01(o[k]) * 255.0f;
+    }
+    bgra[0] = (uint8_t)(int)o[0];
+    bgra[1] = (uint8_t)(int)o[1];
+    bgra[2] = (uint8_t)(int)o[2];
+    bgra[3] = 0;
+}
+
+/* FP_DiffuseOnly::process (test2/testproc.cpp:458-499) over (normal, world
+   position, uv, shadow coordinate). */
+static void fp_diffuse_only(const fp_state* s, const float* in, uint8_t* bgra)
+{
+    const float* nrm = in, * wp = in + 4, * tc = in + 8, * sc = in + 12;
+    const float shadow = sample_proj(s->proj, sc);
+    float c[4], am[4], f[2], g;
+    sample_nearest(s->tex, tc, c);
+    for (int k = 0; k < 4; k++) am[k] = c[k] * s->amb[k];
+    spot_factors(s, nrm, wp, f);
+    g = (f[0] + f[1]) * shadow;
+    for (int k = 0; k < 4; k++) {
+        float v = c[k] * g + am[k];
+        v = v > 0.0f ? v : 0.0f;
+        c[k] = v < 255.0f ? v : 255.0f;
+    }
+    bgra[0] = (uint8_t)(int)c[0];
+    bgra[1] = (uint8_t)(int)c[1];
+    bgra[2] = (uint8_t)(int)c[2];
+    bgra[3] = 0;
+}
+
 /* FragmentProcessorDEF03::process (tex1bump1light1.cpp:180-239): the bump
    texel's (r, g, b, 0) / 255 * 2 - 1 on four lanes, through the matrix whose
    columns are the tangent, binormal, normal and 0 (mcemaths_make_tbn,
@@ -1199,6 +1355,17 @@ static int run_fp(const ps3do* p, const fp_state* s, const float* in, uint8_t* b
     case FP_EARTH:
     case FP_SATELLITE: fp_planet(p, s, in, bgra); return 1;
     case FP_CLOUD: fp_cloud(s, in, bgra); return 1;
+    case FP_SINGLECOLOURNL: { /* test2/testproc.cpp:55-70: the diffuse colour x 255, truncated */
+        float o[4];
+        for (int k = 0; k < 4; k++) o[k] = s->dif[k] * 255.0f;
+        bgra[0] = (uint8_t)(int)o[0];
+        bgra[1] = (uint8_t)(int)o[1];
+        bgra[2] = (uint8_t)(int)o[2];
+        bgra[3] = 0;
+        return 1;
+    }
+    case FP_SINGLECOLOUR: fp_single_colour(s, in, bgra); return 1;
+    case FP_DIFFUSEONLY: fp_diffuse_only(s, in, bgra); return 1;
     case FP_CLOUDSHADOW: { /* test/testproc.cpp:677-686: discard where the texel's red is below 150 */
         float t[4];
         sample_nearest(s->tex, in, t);

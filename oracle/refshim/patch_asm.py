@@ -1,4 +1,4 @@
-"""Generate asm-free copies of three reference translation units for the
+"""Generate asm-free copies of four reference translation units for the
 Linux build of the reference pipeline core (oracle/_ref).  TEST
 INFRASTRUCTURE ONLY.
 
@@ -18,12 +18,16 @@ intrinsics (or a plain copy) issuing the same operations:
   16-byte moves, testproc.cpp:8-27, 367-381, 578-587) become memcpy of the
   same bytes; FP_Cloud's colour packing (testproc.cpp:565-571: cvtps2dq,
   packusdw, packuswb, movss) becomes the same four intrinsics.
+* test2/testproc.cpp (the scene viewer's processors, written as
+  testproc2.cpp): ``copyUserDataSingleColour`` and ``copyUserDataDiffuseOnly``
+  (3 and 4 aligned 16-byte moves, testproc.cpp:73-86, 287-300) become memcpy.
 
 Everything else in both files is left byte-for-byte unchanged.  Each block is
 matched by its own instruction text so that a different reference revision
 fails loudly instead of silently compiling something else.
 
-Usage: python patch_asm.py <reference src/puresoft3d dir> <output dir> [<reference src/test dir>]
+Usage: python patch_asm.py <reference src/puresoft3d dir> <output dir> [<reference src/test dir>
+       [<reference src/test2 dir>]]
 """
 import os
 import re
@@ -89,7 +93,7 @@ PACK_REPL = """{
 \t}"""
 
 
-def main(src_dir, out_dir, test_dir=None):
+def main(src_dir, out_dir, test_dir=None, test2_dir=None):
     os.makedirs(out_dir, exist_ok=True)
     with open(os.path.join(src_dir, "interp.cpp"), encoding="latin-1") as f:
         interp = f.read()
@@ -117,6 +121,16 @@ def main(src_dir, out_dir, test_dir=None):
         with open(os.path.join(out_dir, "testproc.cpp"), "w", encoding="latin-1") as f:
             f.write(tp)
 
+    if test2_dir:
+        with open(os.path.join(test2_dir, "testproc.cpp"), encoding="latin-1") as f:
+            tp = f.read()
+        tp = _patch(tp, [(["[eax + 32]", "movaps\t[eax + 32],\txmm2"], COPY_REPL % 48),
+                         (["[eax + 48]", "movaps\t[eax + 48],\txmm3"], COPY_REPL % 64)])
+        tp = "#include <string.h>\n" + tp
+        with open(os.path.join(out_dir, "testproc2.cpp"), "w", encoding="latin-1") as f:
+            f.write(tp)
+
 
 if __name__ == "__main__":
-    main(sys.argv[1], sys.argv[2], sys.argv[3] if len(sys.argv) > 3 else None)
+    main(sys.argv[1], sys.argv[2], sys.argv[3] if len(sys.argv) > 3 else None,
+         sys.argv[4] if len(sys.argv) > 4 else None)

@@ -23,6 +23,7 @@
 #include "defproc.h"
 #include "cfgproc.h"
 #include "testproc.h"
+#include "../test2/testproc.h"  /* the scene viewer's processors (src/test2) */
 
 int logicCPUs(void); /* refshim/win32_runtime.cpp */
 
@@ -102,6 +103,17 @@ PuresoftProcessor* make_processor(int id)
     case 0x0901: return new VP_CloudShadow;
     case 0x0902: return new IP_CloudShadow;
     case 0x0903: return new FP_CloudShadow;
+    case 0x0A01: return new VP_PositionOnly;  /* the scene viewer's sets (test2/testproc.cpp) */
+    case 0x0A02: return new IP_Null;
+    case 0x0A03: return new FP_SingleColourNoLighting;
+    case 0x0B01: return new VP_SingleColour;
+    case 0x0B02: return new IP_SingleColour;
+    case 0x0B03: return new FP_SingleColour;
+    case 0x0C01: return new VP_DiffuseOnly;
+    case 0x0C02: return new IP_DiffuseOnly;
+    case 0x0C03: return new FP_DiffuseOnly;
+    case 0x0D01: return new VP_Shadow;
+    case 0x0D03: return new FP_Null;
     case 0x0501: return new VertexProcesserDEF05;
     case 0x0502: return new InterpolationProcessorDEF05;
     case 0x0503: return new FragmentProcessorDEF05;

@@ -302,6 +302,8 @@ int required_vary(int ip)
     case IP_PLANET: return 21; // tangent, binormal, normal xyzw, worldPos xyz, uv, shadow coordinate xyzw
     case IP_CLOUD: return 13;  // normal xyzw, worldPos xyz, uv, shadow coordinate xyzw
     case IP_CLOUDSHADOW: return 2;  // uv
+    case IP_SINGLECOLOUR: return 11;  // normal xyzw, worldPos xyz, shadow coordinate xyzw
+    case IP_DIFFUSEONLY: return 13;   // normal xyzw, worldPos xyz, uv, shadow coordinate xyzw
     case IP_LIT2: return 16;
     default: return 0;
     }
@@ -318,6 +320,8 @@ int fp_needs(int fp)
     case FP_EARTH: case FP_SATELLITE: return IP_PLANET;
     case FP_CLOUD: return IP_CLOUD;
     case FP_CLOUDSHADOW: return IP_CLOUDSHADOW;
+    case FP_SINGLECOLOUR: return IP_SINGLECOLOUR;
+    case FP_DIFFUSEONLY: return IP_DIFFUSEONLY;
     default: return 0;
     }
 }
@@ -333,6 +337,8 @@ int vp_gives(int vp)
     case VP_PLANET: return IP_PLANET;
     case VP_CLOUD: return IP_CLOUD;
     case VP_CLOUDSHADOW: return IP_CLOUDSHADOW;
+    case VP_SINGLECOLOUR: return IP_SINGLECOLOUR;
+    case VP_DIFFUSEONLY: return IP_DIFFUSEONLY;
     default: return 0;
     }
 }
@@ -346,6 +352,8 @@ bool known_processor(int id)
     case VP_DEF04: case IP_DEF04: case FP_DEF04:
     case VP_PLANET: case IP_PLANET: case FP_EARTH: case FP_SATELLITE:
     case VP_CLOUD: case IP_CLOUD: case FP_CLOUD: case VP_CLOUDSHADOW: case IP_CLOUDSHADOW: case FP_CLOUDSHADOW:
+    case VP_POSITIONONLY: case IP_NULL: case FP_SINGLECOLOURNL: case VP_SINGLECOLOUR: case IP_SINGLECOLOUR:
+    case FP_SINGLECOLOUR: case VP_DIFFUSEONLY: case IP_DIFFUSEONLY: case FP_DIFFUSEONLY: case VP_SHADOW2: case FP_NULL:
         return true;
     }
     return false;
@@ -422,6 +430,16 @@ int snapshot_uniforms(const ps3d_pipeline* p, DrawUniforms& U)
             for (int r = 0; r < 4; r++) U.Vrot[4 * c + r] = c < 3 ? V[4 * r + c] : 0.0f;
         break;
     }
+    case VP_POSITIONONLY:  // test2/testproc.cpp:13-16: PVM at 5
+    case VP_SHADOW2:       // test2/testproc.cpp:502-505
+        if ((rc = need(5, U.PVM, 16))) return rc;
+        break;
+    case VP_SINGLECOLOUR:  // test2/testproc.cpp:80-86: M 0, MR 1, PVM 5, shadow projection 6
+    case VP_DIFFUSEONLY:   // test2/testproc.cpp:294-301 (its PV at 4 is read by nothing)
+        if ((rc = need(0, U.M, 16)) || (rc = need(1, U.Mrot, 16)) || (rc = need(5, U.PVM, 16)) ||
+            (rc = need(6, U.LPV, 16)))
+            return rc;
+        break;
     case VP_DEF05:
     case VP_CLOUDSHADOW:  // test/testproc.cpp:588-593
     case VP_SHADOW:
@@ -455,6 +473,27 @@ int snapshot_uniforms(const ps3d_pipeline* p, DrawUniforms& U)
         U.tex = lv[0];
         U.tex2 = lv[1];
         for (int i = 2; i < n; i++) U.ptex[i - 2] = lv[i];
+        break;
+    }
+    case FP_SINGLECOLOURNL:  // test2/testproc.cpp:49-53
+        if ((rc = need(31, U.dif, 4))) return rc;
+        break;
+    case FP_SINGLECOLOUR:  // test2/testproc.cpp:199-209: lights 20-22, shadow map 23, colours 30-33
+    case FP_DIFFUSEONLY: {  // test2/testproc.cpp:447-456: the same without 31 / 32; diffuse texture 40
+        float e;
+        if ((rc = need(20, U.light, 4)) || (rc = need(21, U.ldir, 4)) || (rc = need(22, U.cam, 4)) ||
+            (rc = need(30, U.amb, 4)) || (rc = need(33, &e, 1)))
+            return rc;
+        if (p->fp == FP_SINGLECOLOUR && ((rc = need(31, U.dif, 4)) || (rc = need(32, U.scol, 4)))) return rc;
+        U.sexp = (unsigned)e;  // (unsigned int)*m_specularExponent
+        const int slots[2] = {23, 40};
+        for (int i = 0; i < (p->fp == FP_DIFFUSEONLY ? 2 : 1); i++) {
+            const int* t = uint_(p, slots[i], 1);
+            if (!t) return fail(PS3D_ERR_INVALID, "uniform %d (texture index) is not set", slots[i]);
+            if (!tex_ok(p, *t)) return fail(PS3D_ERR_RANGE, "uniform %d: texture %d", slots[i], *t);
+            if (p->tex[*t].elemLen != 4) return fail(PS3D_ERR_INVALID, "texture %d: 4-byte texels expected", *t);
+            (i ? U.tex : U.ptex[0]) = level_of(p->tex[*t]);
+        }
         break;
     }
     case FP_CLOUD:          // test/testproc.cpp:526-532: diffuse 9, shadow 15
@@ -1561,9 +1600,9 @@ int ps3d_draw(ps3d_pipeline* p, int vao)
     d.fp = p->fp;
     int need = fp_needs(p->fp);
     d.nv = need ? required_vary(need) : 0;
-    // DEF05 writes nothing; CloudShadow only discards (its depth-only pass)
+    // DEF05 and FP_Null write nothing; CloudShadow only discards (its depth-only pass)
     d.flags = (p->behavior & 0xf) |
-              (p->fp == FP_CLOUDSHADOW ? F_FRAGMENT : p->fp != FP_DEF05 ? F_COLOUR : 0);
+              (p->fp == FP_CLOUDSHADOW ? F_FRAGMENT : (p->fp != FP_DEF05 && p->fp != FP_NULL) ? F_COLOUR : 0);
     // processVertices stops at the first VBO that runs out (vertthrd.cpp:18-31)
     long long minCount = -1;
     for (int s = 0; s < PS3D_MAX_VBOS; s++)
@@ -1577,6 +1616,8 @@ int ps3d_draw(ps3d_pipeline* p, int vao)
     if (p->vp == VP_PLANET && d.nv) reqSlots[1] = reqSlots[2] = reqSlots[3] = reqSlots[4] = 1;
     if (p->vp == VP_CLOUD && d.nv) reqSlots[3] = reqSlots[4] = 1;
     if (p->vp == VP_CLOUDSHADOW && d.nv) reqSlots[4] = 1;
+    if (p->vp == VP_SINGLECOLOUR && d.nv) reqSlots[3] = 1;
+    if (p->vp == VP_DIFFUSEONLY && d.nv) reqSlots[3] = reqSlots[4] = 1;
     for (int s = 0; s < kVboSlots; s++) {
         if (reqSlots[s] && !va.vbo[s]) return fail(PS3D_ERR_INVALID, "the vertex processor reads VBO slot %d", s);
         if (va.vbo[s]) {

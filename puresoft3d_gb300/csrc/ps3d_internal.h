@@ -30,6 +30,11 @@ enum : int {
     VP_PLANET = 0x0701, IP_PLANET = 0x0702, FP_EARTH = 0x0703, FP_SATELLITE = 0x0713,
     VP_CLOUD = 0x0801, IP_CLOUD = 0x0802, FP_CLOUD = 0x0803,
     VP_CLOUDSHADOW = 0x0901, IP_CLOUDSHADOW = 0x0902, FP_CLOUDSHADOW = 0x0903,
+    // the scene viewer demo's sets (test2/testproc.h)
+    VP_POSITIONONLY = 0x0A01, IP_NULL = 0x0A02, FP_SINGLECOLOURNL = 0x0A03,
+    VP_SINGLECOLOUR = 0x0B01, IP_SINGLECOLOUR = 0x0B02, FP_SINGLECOLOUR = 0x0B03,
+    VP_DIFFUSEONLY = 0x0C01, IP_DIFFUSEONLY = 0x0C02, FP_DIFFUSEONLY = 0x0C03,
+    VP_SHADOW2 = 0x0D01, FP_NULL = 0x0D03,
     FP_LIT1 = 0x1103, FP_LIT1A = 0x1403, FP_LIT3 = 0x1303,
     VP_LIT2 = 0x1201, IP_LIT2 = 0x1202, FP_LIT2 = 0x1203,
 };
@@ -69,6 +74,10 @@ struct DrawUniforms {
     int albedoLevels, normalLevels;
     const float* shadow;            // LIT2 shadow map (FP32, CLAMP)
     int shadowSize, shadowScan;     // size and scanline in floats
+    // scene viewer lighting (test2/testproc.h:4-30): light direction (21),
+    // ambient (30), diffuse (31), specular colour (32), specular exponent (33)
+    float ldir[4], amb[4], dif[4], scol[4];
+    unsigned sexp;
 };
 
 struct DrawDesc {

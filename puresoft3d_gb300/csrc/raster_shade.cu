@@ -163,6 +163,19 @@ __device__ __forceinline__ int shade_fragment(const DrawDesc& d, const DrawUnifo
             return 1;
         }
         return 0;
+    case FP_SINGLECOLOURNL: bgra = shade_single_colour_nl(U); return 1;
+    case FP_SINGLECOLOUR:
+        if constexpr (NV >= 11) {
+            bgra = shade_single_colour(U, in);
+            return 1;
+        }
+        return 0;
+    case FP_DIFFUSEONLY:
+        if constexpr (NV >= 13) {
+            bgra = shade_diffuse_only(U, in);
+            return 1;
+        }
+        return 0;
     case FP_CLOUDSHADOW:  // test/testproc.cpp:677-686: discards where the texel's red is below 150
         return ((nearest_texel(U.tex, in[0], in[1]) >> 16) & 0xff) < 150u ? 2 : 0;
     case FP_EARTH:
@@ -658,6 +671,21 @@ __device__ __forceinline__ void shade_entry(const PassParams& P, int2 e)
         bgra = shade_cloud(U, in);
         break;
     }
+    case FP_DIFFUSEONLY: {
+        float in[13];
+        fragment_varyings<13>(t, vary, P.nvMax, s, z, xl, in);
+        bgra = shade_diffuse_only(U, in);
+        break;
+    }
+    case FP_SINGLECOLOUR: {
+        float in[11];
+        fragment_varyings<11>(t, vary, P.nvMax, s, z, xl, in);
+        bgra = shade_single_colour(U, in);
+        break;
+    }
+    case FP_SINGLECOLOURNL:
+        bgra = shade_single_colour_nl(U);
+        break;
     case FP_DEF03: {
         float in[17];
         fragment_varyings<17>(t, vary, P.nvMax, s, z, xl, in);
@@ -806,6 +834,8 @@ void launch_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
     case FP_EARTH: kern = k_shade<FP_EARTH>; break;
     case FP_SATELLITE: kern = k_shade<FP_SATELLITE>; break;
     case FP_CLOUD: kern = k_shade<FP_CLOUD>; break;
+    case FP_SINGLECOLOUR: kern = k_shade<FP_SINGLECOLOUR>; break;
+    case FP_DIFFUSEONLY: kern = k_shade<FP_DIFFUSEONLY>; break;
     default: break;
     }
     long long need = ((long long)P.W * P.H + 255) / 256;

@@ -64,6 +64,14 @@ __device__ __forceinline__ void vp_position(const DrawDesc& d, const DrawUniform
         m4v4(pos, U.PVM, a);
         break;
     }
+    case VP_SHADOW2: {  // test2/testproc.cpp:507-518: positions x0.9, then PVM (uniform 5) * p
+        float a[4] = {fmul(p[0], 0.9f), fmul(p[1], 0.9f), fmul(p[2], 0.9f), p[3]};
+        m4v4(pos, U.PVM, a);
+        break;
+    }
+    case VP_POSITIONONLY:  // test2/testproc.cpp:13-23
+    case VP_SINGLECOLOUR:  // test2/testproc.cpp:88-116
+    case VP_DIFFUSEONLY:   // test2/testproc.cpp:304-336: PVM (uniform 5) * the model position
     case VP_SHADOW:
         m4v4(pos, U.PVM, p);
         break;
@@ -139,6 +147,25 @@ __device__ __forceinline__ void vp_varyings(const DrawDesc& d, const DrawUniform
         vary[4] = wp[0]; vary[5] = wp[1]; vary[6] = wp[2];
         vary[7] = __ldg(uv); vary[8] = __ldg(uv + 1);
         vary[9] = sc[0]; vary[10] = sc[1]; vary[11] = sc[2]; vary[12] = sc[3];
+        break;
+    }
+    case VP_SINGLECOLOUR:   // test2/testproc.cpp:88-116: normal (MR, four lanes), world
+                            // position xyz, the world position through the shadow projection
+    case VP_DIFFUSEONLY: {  // test2/testproc.cpp:304-336: the same with the uv before the shadow coordinate
+        float wp[4], n[4], nrm[4], sc[4];
+        m4v4(wp, U.M, p);
+        m4v4(sc, U.LPV, wp);
+        ld4(d.vbo[3] + (size_t)idx * d.stride[3], n);
+        m4v4(nrm, U.Mrot, n);
+        vary[0] = nrm[0]; vary[1] = nrm[1]; vary[2] = nrm[2]; vary[3] = nrm[3];
+        vary[4] = wp[0]; vary[5] = wp[1]; vary[6] = wp[2];
+        int o = 7;
+        if (d.vp == VP_DIFFUSEONLY) {
+            const float* uv = (const float*)(d.vbo[4] + (size_t)idx * d.stride[4]);
+            vary[7] = __ldg(uv); vary[8] = __ldg(uv + 1);
+            o = 9;
+        }
+        vary[o] = sc[0]; vary[o + 1] = sc[1]; vary[o + 2] = sc[2]; vary[o + 3] = sc[3];
         break;
     }
     case VP_CLOUDSHADOW: {  // test/testproc.cpp:595-610: uv only

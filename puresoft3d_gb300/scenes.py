@@ -45,6 +45,11 @@ VP_SHADOW = 0x0601
 VP_PLANET, IP_PLANET, FP_EARTH, FP_SATELLITE = 0x0701, 0x0702, 0x0703, 0x0713
 VP_CLOUD, IP_CLOUD, FP_CLOUD = 0x0801, 0x0802, 0x0803
 VP_CLOUDSHADOW, IP_CLOUDSHADOW, FP_CLOUDSHADOW = 0x0901, 0x0902, 0x0903
+# the scene viewer demo's sets (test2/testproc.h)
+VP_POSITIONONLY, IP_NULL, FP_SINGLECOLOURNL = 0x0A01, 0x0A02, 0x0A03
+VP_SINGLECOLOUR, IP_SINGLECOLOUR, FP_SINGLECOLOUR = 0x0B01, 0x0B02, 0x0B03
+VP_DIFFUSEONLY, IP_DIFFUSEONLY, FP_DIFFUSEONLY = 0x0C01, 0x0C02, 0x0C03
+VP_SHADOW2, FP_NULL = 0x0D01, 0x0D03
 FP_LIT1, FP_LIT1A, FP_LIT3 = 0x1103, 0x1403, 0x1303
 VP_LIT2, IP_LIT2, FP_LIT2 = 0x1201, 0x1202, 0x1203
 

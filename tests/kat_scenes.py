@@ -293,6 +293,61 @@ def _cloud_scene(name, w, h, seed):
                                                    "shadow_texture": shadow})
 
 
+def _viewer_scene(name, w, h, seed):
+    """The scene viewer demo's processors (test2/testproc.cpp, uniform slots
+    test2/testproc.h:4-30): a depth-only pass (VP_Shadow: positions x0.9,
+    IP_Null, FP_Null) into a 64x64 shadow map, then an unlit single-colour
+    draw, a lit single-colour draw and a textured draw under a spotlight
+    whose 25-degree cone covers part of the frame (cos^150 fall-off outside
+    it), each with the 4-tap projective shadow lookup."""
+    b = S._Builder()
+    rng = np.random.default_rng(seed)
+    tex = b.texture(S.checker_noise_bgra(32, 8, rng, noise=24, lo=50, hi=210), wrap=True)
+    shadow = b.empty_texture(64, 64)
+    depth = b.empty_texture(w, h)
+    vaos = [b.vao(_tri_mesh(random_soup(n, seed + k)), slots=(0, 3, 4)) for k, n in enumerate((60, 140, 140))]
+    shadow_prog = b.programme(S.VP_SHADOW2, S.IP_NULL, S.FP_NULL)
+    progs = [b.programme(S.VP_POSITIONONLY, S.IP_NULL, S.FP_SINGLECOLOURNL),
+             b.programme(S.VP_SINGLECOLOUR, S.IP_SINGLECOLOUR, S.FP_SINGLECOLOUR),
+             b.programme(S.VP_DIFFUSEONLY, S.IP_DIFFUSEONLY, S.FP_DIFFUSEONLY)]
+    c, s_ = np.cos(0.4), np.sin(0.4)
+    light = np.array([[0.85 * c, 0.0, 0.45 * s_, 0.02], [0.05, 0.85, 0.0, -0.03], [-0.4 * s_, 0.0, 0.4 * c, 0.0],
+                      [0.0, 0.0, 0.0, 1.0]])
+    bias = np.array([[0.5, 0, 0, 0.5], [0, 0.5, 0, 0.5], [0, 0, 1, 0], [0, 0, 0, 1]])
+    eye = np.eye(4)
+    lpos = np.array([0.4, 0.3, 2.2])
+    ldir = lpos - np.array([0.1, 0.0, 0.0])
+    ldir /= np.linalg.norm(ldir)
+    b.f("setViewport", 64, 64)
+    b.f("setDepth", shadow)
+    b.f("clearDepth", 1.0)
+    b.f("useProgramme", shadow_prog)
+    b.f("setUniform", 5, S.col_major(light))
+    for v in vaos:
+        b.f("drawVAO", v)
+    b.f("setViewport", w, h)
+    b.f("setDepth", depth)
+    b.f("clearDepth", 1.0)
+    b.f("clearColour", 0xFF203040)
+    for slot in (0, 1, 5):
+        b.f("setUniform", slot, S.col_major(eye))
+    b.f("setUniform", 6, S.col_major(bias @ light))
+    b.f("setUniform", 20, S.vec4(*lpos))
+    b.f("setUniform", 21, S.vec4(*ldir))
+    b.f("setUniform", 22, S.vec4(0, 0, 2))
+    b.f("setUniform", 23, np.array([shadow], dtype=np.int32))
+    b.f("setUniform", 30, S.vec4(0.25, 0.2, 0.15, 0.0))
+    b.f("setUniform", 31, S.vec4(0.8, 0.55, 0.3, 1.0))
+    b.f("setUniform", 32, S.vec4(0.9, 0.9, 1.0, 1.0))
+    b.f("setUniform", 33, np.array([20.0], dtype=np.float32))
+    b.f("setUniform", 40, np.array([tex], dtype=np.int32))
+    for prog, v in zip(progs, vaos):
+        b.f("useProgramme", prog)
+        b.f("drawVAO", v)
+    return S.Scene(name, w, h, b.setup, b.frame, {"triangles": 340, "depth_texture": depth,
+                                                   "shadow_texture": shadow})
+
+
 def _v(x, y, z=0.0, w=1.0):
     return [x * w, y * w, z * w, w]
 
@@ -383,4 +438,6 @@ def kat_scenes():
     out.append(("kat_def0_planet_earth_96x64", _planet_scene("kat_planet_earth", 96, 64, 23, S.FP_EARTH)))
     out.append(("kat_def0_planet_satellite_80x60", _planet_scene("kat_planet_satellite", 80, 60, 24, S.FP_SATELLITE)))
     out.append(("kat_def0_planet_cloud_88x64", _cloud_scene("kat_cloud", 88, 64, 25)))
+    out.append(("kat_def0_viewer_spot_96x72", _viewer_scene("kat_viewer_spot", 96, 72, 26)))
+    out.append(("kat_def0_viewer_spot_80x64", _viewer_scene("kat_viewer_spot_b", 80, 64, 27)))
     return out
