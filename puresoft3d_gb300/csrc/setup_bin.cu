@@ -19,6 +19,10 @@
 
 namespace ps3d {
 
+// Triangles of at most this many rows get exact bin bounds from their spans
+// in the set-up (and none when no row has a pixel).
+constexpr int kExactRows = 4;
+
 // ----------------------------------------------------------------- vertex stage
 
 __device__ __forceinline__ void ld4(const uint8_t* p, float v[4])
@@ -344,11 +348,33 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float
             float xmax = fmaxf(vx[0], fmaxf(vx[1], vx[2])) + ext + 2.0f;
             int colLo = xmin < 0.0f ? 0 : (xmin > (float)W ? W : (int)xmin);
             int colHi = xmax > (float)(W - 1) ? W - 1 : (xmax < 0.0f ? -1 : (int)xmax);
+            int rowLo = firstRow, rowHi = lastRow;
+            if (lastRow - firstRow < kExactRows) {
+                // a short triangle: its rows' spans exactly, as the raster will
+                // find them (drawvao.cpp:72-75 skips left == right; the fragment
+                // loop covers [leftClamped, rightClamped]); one with no pixel
+                // reaches no bin, the others only the bins their spans touch
+                int lo = W, hi = -1, yLo = lastRow, yHi = firstRow;
+#pragma unroll 1
+                for (int y = firstRow; y <= lastRow; y++) {
+                    Span sp;
+                    if (span_row<true>(tr, y, W, sp) && sp.leftClamped <= sp.rightClamped) {
+                        lo = min(lo, sp.leftClamped);
+                        hi = max(hi, sp.rightClamped);
+                        yLo = min(yLo, y);
+                        yHi = max(yHi, y);
+                    }
+                }
+                colLo = lo;
+                colHi = hi;
+                rowLo = yLo;
+                rowHi = yHi;
+            }
             if (colLo <= colHi) {  // bins are in target pixels: offset by the viewport origin
                 bx0 = (colLo + d.vpX) / P.binW;
                 bx1 = (colHi + d.vpX) / P.binW;
-                by0 = (firstRow + d.vpY) / kBinH;
-                by1 = (lastRow + d.vpY) / kBinH;
+                by0 = (rowLo + d.vpY) / kBinH;
+                by1 = (rowHi + d.vpY) / kBinH;
                 count = (bx1 - bx0 + 1) * (by1 - by0 + 1);
             }
         }
