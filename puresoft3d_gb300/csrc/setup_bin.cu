@@ -19,9 +19,9 @@
 
 namespace ps3d {
 
-// Triangles of at most this many rows get exact bin bounds from their spans
-// in the set-up (and none when no row has a pixel).
-constexpr int kExactRows = 4;
+// Triangles of at most this many rows get exact bin bounds and row range from
+// their spans in the set-up (and none when no row has a pixel).
+constexpr int kExactRows = 32;
 
 // ----------------------------------------------------------------- vertex stage
 
@@ -369,6 +369,10 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float
                 colHi = hi;
                 rowLo = yLo;
                 rowHi = yHi;
+                if (lo <= hi) {  // the raster's row range: only rows with pixels
+                    tr.firstRow = (short)yLo;
+                    tr.lastRow = (short)yHi;
+                }
             }
             if (colLo <= colHi) {  // bins are in target pixels: offset by the viewport origin
                 bx0 = (colLo + d.vpX) / P.binW;
