@@ -77,7 +77,7 @@ CONFIGS = {
 # metrics dram__bytes_read.sum / dram__bytes_write.sum; the command and the
 # per-launch figures are in profiles/raster_dram_traffic.md).  Averages over
 # the captured launches that ran to completion.
-RASTER_TRAFFIC = {"c1": 94848, "c2": 6698240, "c3": 114982784, "c4": 785054976}
+RASTER_TRAFFIC = {"c1": 70272, "c2": 5081664, "c3": 105983872, "c4": 777167744}
 
 
 def peaks():
@@ -388,13 +388,8 @@ def run_c4(args):
     plain_ips = views / (plain_ms / 1e3)
     plain_graph_ips = views / (statistics.median(pg_ms) / 1e3)
 
-    ab = algorithmic_bytes(batched, counts)
-    dom = max(prof, key=lambda k: prof[k][1])
-    n_launch, ms = prof[dom]
-    avg_ms = ms / max(n_launch, 1)
-    peak, peak_kind = peaks()
-    bytes_per_launch = ab["raster_per_frame"] if dom == "raster" else None
-    achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9 if bytes_per_launch else None
+    roof = dominant_roofline(prof, prof_frames, batched, counts, tune["bin_width"],
+                             RASTER_TRAFFIC.get("c4") if views == 4096 else None)
     line = {
         "metric": "images/s", "value": round(ips, 2), "unit": "images/s", "n_gpus": WORLD,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4),
@@ -416,11 +411,7 @@ def run_c4(args):
                         "copies its atlas to pinned host memory",
                 "one_at_a_time": round(WORLD * views * e2e_steps / e2e_sync_s, 2),
                 "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": batched.width * batched.height * 4},
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2) if achieved else None,
-                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5) if achieved else None,
-                     "peak_source": peak_kind, "avg_launch_ms": round(avg_ms, 5),
-                     "bytes_per_launch": bytes_per_launch,
-                     "traffic": RASTER_TRAFFIC.get("c4") if dom == "raster" and views == 4096 else None},
+        "roofline": roof,
         "kernel_ms_per_step": {k: round(prof[k][1] / prof_frames, 5) for k in KERNELS if prof[k][0]},
         "clocks": clk,
     }
@@ -563,6 +554,59 @@ def algorithmic_bytes(scene, counts):
     return {"raster_per_frame": per_frame, "raster_launches_per_frame": launches}
 
 
+def _targets(scene):
+    """(width, height) of each pass's target in a frame of `scene`."""
+    t = [(scene.width, scene.height)]
+    if scene.name == "c2":
+        t.append((scene.info["shadow_size"], scene.info["shadow_size"]))
+    return t
+
+
+def _radix_passes(w, h, bin_w):
+    """The bin sort's LSD passes for one target: 8 bits of bin index each."""
+    bins = -(-w // bin_w) * -(-h // 32)
+    return ((bins - 1).bit_length() + 7) // 8 if bins > 1 else 0
+
+
+def kernel_bytes_per_frame(kind, scene, counts, bin_w):
+    """Algorithmic bytes per frame of each timed kernel class -- what its work
+    must move at least once: raster as in algorithmic_bytes; the set-up reads
+    each triangle's three positions (48 B) and writes its record (64 B) and
+    its (bin, triangle) pairs (8 B each); each radix pass reads and writes
+    every pair (16 B); the bin bounds write each bin's start and work item
+    (8 B); the shade reads a shade-list entry and writes a pixel (12 B)."""
+    if kind == "raster":
+        return algorithmic_bytes(scene, counts)["raster_per_frame"]
+    if kind == "setup":
+        return counts["triangles"] * (48 + 64) + counts["pairs"] * 8
+    if kind == "sort":
+        passes = max(_radix_passes(w, h, bin_w) for w, h in _targets(scene))
+        return counts["pairs"] * 16 * passes
+    if kind == "bounds":
+        return sum(-(-w // bin_w) * -(-h // 32) * 8 for w, h in _targets(scene))
+    if kind == "shade":
+        return counts["shaded"] * 12
+    return None
+
+
+def dominant_roofline(prof, prof_frames, scene, counts, bin_w, traffic):
+    """The roofline object for the kernel class with the largest event-timed
+    share: achieved = its algorithmic bytes per launch / its mean launch
+    time, against the measured HBM copy bandwidth."""
+    dom = max(prof, key=lambda k: prof[k][1])
+    n_launch, ms = prof[dom]
+    avg_ms = ms / max(n_launch, 1)
+    peak, peak_kind = peaks()
+    per_frame = kernel_bytes_per_frame(dom, scene, counts, bin_w)
+    bytes_per_launch = per_frame / (n_launch / prof_frames) if per_frame and n_launch else None
+    achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9 if bytes_per_launch else None
+    return {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2) if achieved else None,
+            "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5) if achieved else None,
+            "peak_source": peak_kind, "avg_launch_ms": round(avg_ms, 5),
+            "bytes_per_launch": round(bytes_per_launch) if bytes_per_launch else None,
+            "traffic": traffic if dom == "raster" else None}
+
+
 def run_ours(args):
     from puresoft3d_gb300 import scenes as S
     from puresoft3d_gb300.pipeline import PuresoftPipeline, KERNELS
@@ -644,17 +688,7 @@ def run_ours(args):
 
     fps = aggregate(args.steps, total_ms / 1e3)
     fps_e2e = aggregate(args.steps, e2e_s)
-    ab = algorithmic_bytes(scene, counts)
-    # dominant kernel by event time share
-    dom = max(prof, key=lambda k: prof[k][1])
-    n_launch, ms = prof[dom]
-    avg_ms = ms / max(n_launch, 1)
-    peak, peak_kind = peaks()
-    if dom == "raster":
-        bytes_per_launch = ab["raster_per_frame"] / ab["raster_launches_per_frame"]
-    else:
-        bytes_per_launch = None
-    achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9 if bytes_per_launch else None
+    roof = dominant_roofline(prof, prof_frames, scene, counts, tune["bin_width"], RASTER_TRAFFIC.get(args.config))
     line = {
         "metric": "frames/s", "value": round(fps, 3), "unit": "frames/s", "n_gpus": WORLD,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4),
@@ -671,11 +705,7 @@ def run_ours(args):
                 "mode": "steps back to back on two pipelines (double-buffered): each uploads its inputs and "
                         "copies its frame to pinned host memory",
                 "one_at_a_time": round(aggregate(args.steps, e2e_sync_s), 3)},
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2) if achieved else None,
-                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5) if achieved else None,
-                     "peak_source": peak_kind, "avg_launch_ms": round(avg_ms, 5),
-                     "bytes_per_launch": bytes_per_launch,
-                     "traffic": RASTER_TRAFFIC.get(args.config) if dom == "raster" else None},
+        "roofline": roof,
         "kernel_ms_per_frame": {k: round(prof[k][1] / prof_frames, 5) for k in KERNELS if prof[k][0]},
         "clocks": clk,
     }
