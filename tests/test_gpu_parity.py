@@ -292,3 +292,59 @@ def test_forward_pass_waits_for_earlier_colour_pass(gpu_lib):
         S.replay_frame(scene, g)
         got = g.readColour()
         assert colour_diff(got, want)[0] <= COLOUR_TOL
+
+
+def _tiny_thin_clip(w, h, seed):
+    """Triangles in pixel units turned into clip space: sub-pixel ones, slivers
+    whose every row is empty, spans clamped away at the left and right
+    edges, and thin triangles 30-35 rows tall (around the set-up's exact-span
+    limit of 32 rows), in both orientations."""
+    rng = np.random.default_rng(seed)
+    tris = []
+    for _ in range(300):  # sub-pixel and few-pixel
+        c = rng.uniform([-2, -2], [w + 2, h + 2])
+        tris.append(c + rng.normal(size=(3, 2)) * rng.uniform(0.2, 2.0))
+    for _ in range(80):  # horizontal slivers across a row boundary
+        y = rng.integers(1, h - 1) + rng.uniform(-0.3, 0.3)
+        x = rng.uniform(0, w)
+        tris.append(np.array([[x, y], [x + rng.uniform(2, 20), y + rng.uniform(-0.4, 0.4)], [x + 1, y + 0.45]]))
+    for _ in range(80):  # vertical needles, under a pixel wide
+        x, y = rng.uniform(-1, w + 1), rng.uniform(0, h)
+        tris.append(np.array([[x, y], [x + rng.uniform(0.05, 0.9), y], [x + rng.uniform(0, 0.9), y + rng.uniform(3, 40)]]))
+    for rows in (30, 31, 32, 33, 34, 35):  # around the exact-span limit
+        for _ in range(6):
+            x, y = rng.uniform(0, w), rng.uniform(0, h - rows - 1)
+            tris.append(np.array([[x, y], [x + rng.uniform(0.5, 6), y + 0.2], [x + rng.uniform(-3, 3), y + rows + 0.5]]))
+    out = []
+    for t in tris:
+        if rng.random() < 0.5:
+            t = t[::-1]  # either winding
+        z = rng.uniform(-0.9, 0.9)
+        for px, py in t:
+            wc = rng.uniform(0.7, 1.6)
+            out.append([(2 * px / w - 1) * wc, (2 * py / h - 1) * wc, (z + rng.normal() * 0.02) * wc, wc])
+    return np.array(out, dtype=np.float32)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("bin_w", [8, 16, 32])
+def test_tiny_and_thin_triangles(gpu_lib, bin_w):
+    """The set-up's exact spans drop triangles with no pixel and trim bins and
+    rows to the spans: on triangles built to hit those cases the GPU gives
+    the oracle's depth bit for bit, its colour within 1 LSB and the same
+    fragment counts."""
+    import kat_scenes as K
+    from puresoft3d_gb300.pipeline import PuresoftPipeline
+    w, h = 96, 80
+    scene = K._scene("tiny_thin", w, h, _tiny_thin_clip(w, h, 5), lit=True)
+    g = PuresoftPipeline(w, h)
+    g.setBinWidth(bin_w)
+    g.setFragmentCounting(True)
+    out = render(g, scene)
+    o = OraclePipeline(w, h)
+    ref = render(o, scene)
+    assert_depth_exact(out["depth"], ref["depth"], "tiny_thin")
+    assert colour_diff(out["colour"], ref["colour"])[0] <= COLOUR_TOL
+    st = g.stats()
+    assert (st["fragments"], st["fragments_passed"]) == o.fragments()
+    assert int((ref["depth"] < 1.0).sum()) > 500  # the scene covers something
