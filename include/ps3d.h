@@ -319,7 +319,11 @@ int ps3d_set_raster_occupancy(ps3d_pipeline* p, int blocksPerSM);
  * nothing recorded, before any stream capture starts, to do this set-up.
  * Overlap: every pipeline of the process shares the array, so two calls
  * whose work overlapped on the device would race; calls are serialised by a
- * process-wide lock and each returns only after its work has completed.
+ * process-wide lock and each returns only after its work has completed (on
+ * an error too: work already queued is waited for, and the frame's
+ * commands are then dropped, except after PS3D_ERR_RANGE / PS3D_ERR_NOMEM
+ * as above).  The device current at the call must be the one the pipeline
+ * was created on (else PS3D_ERR_DEVICE).
  * Flushed work (ps3d_flush) must be finished with ps3d_finish first. */
 int ps3d_finish_noalloc(ps3d_pipeline* p);
 
@@ -369,6 +373,10 @@ int ps3d_get_stream(ps3d_pipeline* p, void** out);
  * adds one atomic per warp-span). */
 int ps3d_set_fragment_counting(ps3d_pipeline* p, int on);
 int ps3d_stats(ps3d_pipeline* p, ps3d_stats_t* out);
+/* Device and pinned-host allocations (cudaMalloc / cudaMallocHost calls)
+ * made so far by every pipeline of the process: a caller can check that a
+ * stretch of calls allocated nothing (no counterpart in the reference). */
+unsigned long long ps3d_allocation_count(void);
 
 /* ---- command buffers (no counterpart in the reference, whose drawVAO runs
  * immediately).  Between ps3d_cmdbuf_begin and ps3d_cmdbuf_end, clears and

@@ -22,6 +22,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <new>
 #include <string>
@@ -132,6 +133,22 @@ struct Pass {
     uint32_t colourValue = 0;
 };
 
+// Every device or pinned-host allocation this runtime makes goes through
+// dev_malloc / host_malloc and is counted (ps3d_allocation_count).
+std::atomic<unsigned long long> g_allocCount{0};
+
+cudaError_t dev_malloc(void** p, size_t bytes)
+{
+    g_allocCount.fetch_add(1, std::memory_order_relaxed);
+    return cudaMalloc(p, bytes);
+}
+
+cudaError_t host_malloc(void** p, size_t bytes)
+{
+    g_allocCount.fetch_add(1, std::memory_order_relaxed);
+    return cudaMallocHost(p, bytes);
+}
+
 // Device buffers that grow.  While a captured graph exists its kernels hold
 // the old addresses, so a buffer being replaced is retired (freed when the
 // last graph goes) instead of freed.
@@ -147,7 +164,7 @@ template <class T> bool dev_alloc(T*& p, size_t& cap, size_t need)
     }
     p = nullptr;
     cap = 0;
-    if (cudaMalloc((void**)&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return false;
+    if (dev_malloc((void**)&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return false;
     cap = n;
     return true;
 }
@@ -216,6 +233,7 @@ struct Tracker {
 }  // namespace
 
 struct ps3d_pipeline {
+    int device = -1;     // the CUDA device current when the pipeline was created
     int devW, devH;      // device size (colour buffer, default depth)
     int W, H;            // viewport size
     int vpX = 0, vpY = 0;  // viewport origin in the targets (ps3d_set_viewport_rect)
@@ -1155,6 +1173,10 @@ int ps3d_pipeline_create(int width, int height, void* stream, ps3d_pipeline** ou
     if (!p) return fail(PS3D_ERR_NOMEM, "host allocation failed");
     p->devW = p->W = width;
     p->devH = p->H = height;
+    if (cudaGetDevice(&p->device) != cudaSuccess) {
+        delete p;
+        return fail(PS3D_ERR_DEVICE, "cudaGetDevice failed");
+    }
     if (const char* cap = getenv("PS3D_PAIR_CAP")) {
         long v = atol(cap);
         if (v >= 32 && v <= kMaxPairs) p->pairCap = (int)v;
@@ -1173,9 +1195,9 @@ int ps3d_pipeline_create(int width, int height, void* stream, ps3d_pipeline** ou
     }
     p->defDepthScan = (int)(width / 4.0f + 0.5f) * 4;  // pipeline.cpp:31
     if (p->defDepthScan < width) p->defDepthScan = (width + 3) / 4 * 4;
-    bool ok = cudaMalloc((void**)&p->colour, (size_t)width * 4 * height) == cudaSuccess &&
-              cudaMalloc((void**)&p->defDepth, (size_t)p->defDepthScan * 4 * height) == cudaSuccess &&
-              cudaMalloc((void**)&p->status, 64 * sizeof(int)) == cudaSuccess;
+    bool ok = dev_malloc((void**)&p->colour, (size_t)width * 4 * height) == cudaSuccess &&
+              dev_malloc((void**)&p->defDepth, (size_t)p->defDepthScan * 4 * height) == cudaSuccess &&
+              dev_malloc((void**)&p->status, 64 * sizeof(int)) == cudaSuccess;
     for (int k = 0; k < kSlots && ok; k++) {
         p->scr[k].slotStatus = p->status + 16 * (k + 1);
         ok = cudaStreamCreateWithFlags(&p->gs[k], cudaStreamNonBlocking) == cudaSuccess;
@@ -1256,7 +1278,7 @@ static int texture_create(ps3d_pipeline* p, int width, int height, int scanline,
     t.layers = 1 + extraLayers;
     size_t bytes = (size_t)scanline * height;
     size_t all = bytes * t.layers;
-    if (cudaMalloc((void**)&t.dev, (all + 15) / 16 * 16) != cudaSuccess)
+    if (dev_malloc((void**)&t.dev, (all + 15) / 16 * 16) != cudaSuccess)
         return fail(PS3D_ERR_NOMEM, "texture allocation of %zu bytes failed", all);
     // tex.cpp:20-23: the pixels fill the default layer; extra layers start zeroed
     if (pixels) {
@@ -1467,7 +1489,7 @@ static int vbo_attach(ps3d_pipeline* p, int vao, int slot, int unitBytes, int co
     b->unitBytes = unitBytes;
     b->count = count;
     size_t bytes = (size_t)unitBytes * count;
-    if (cudaMalloc((void**)&b->dev, std::max<size_t>(bytes, 16)) != cudaSuccess) {
+    if (dev_malloc((void**)&b->dev, std::max<size_t>(bytes, 16)) != cudaSuccess) {
         delete b;
         return fail(PS3D_ERR_NOMEM, "VBO allocation failed");
     }
@@ -1819,6 +1841,8 @@ int ps3d_set_fragment_counting(ps3d_pipeline* p, int on)
     return 0;
 }
 
+unsigned long long ps3d_allocation_count(void) { return g_allocCount.load(std::memory_order_relaxed); }
+
 int ps3d_stats(ps3d_pipeline* p, ps3d_stats_t* out)
 {
     if (!p || !out) return fail(PS3D_ERR_INVALID, "null argument");
@@ -1865,10 +1889,10 @@ int ps3d_cmdbuf_end(ps3d_pipeline* p, ps3d_cmdbuf** out)
         },
         [&](int, float, uint32_t) { return 0; }, [&](const Command&) { return 0; });
     size_t n = std::max<size_t>(cb->hDraws.size(), 1);
-    bool ok = cudaMalloc((void**)&cb->dDraws, n * sizeof(DrawDesc)) == cudaSuccess &&
-              cudaMalloc((void**)&cb->dUnis, n * sizeof(DrawUniforms)) == cudaSuccess &&
-              cudaMallocHost((void**)&cb->pinDraws, n * sizeof(DrawDesc)) == cudaSuccess &&
-              cudaMallocHost((void**)&cb->pinUnis, n * sizeof(DrawUniforms)) == cudaSuccess;
+    bool ok = dev_malloc((void**)&cb->dDraws, n * sizeof(DrawDesc)) == cudaSuccess &&
+              dev_malloc((void**)&cb->dUnis, n * sizeof(DrawUniforms)) == cudaSuccess &&
+              host_malloc((void**)&cb->pinDraws, n * sizeof(DrawDesc)) == cudaSuccess &&
+              host_malloc((void**)&cb->pinUnis, n * sizeof(DrawUniforms)) == cudaSuccess;
     if (!ok) {
         p->cmdbufs.push_back(cb);
         ps3d_cmdbuf_destroy(p, cb);
@@ -2039,7 +2063,7 @@ int ps3d_l2_scrub(ps3d_pipeline* p, size_t bytes)
         if (p->scrub) cudaFree(p->scrub);
         p->scrub = nullptr;
         p->scrubBytes = 0;
-        CU(cudaMalloc(&p->scrub, bytes));
+        CU(dev_malloc(&p->scrub, bytes));
         p->scrubBytes = bytes;
     }
     static unsigned char v = 0;
@@ -2173,6 +2197,9 @@ int noalloc_shape(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass
     s.binsX = (s.tg.w + s.binW - 1) / s.binW;
     s.binsY = (s.tg.h + kBinH - 1) / kBinH;
     s.nBins = (size_t)s.binsX * s.binsY;
+    if (s.nBins > 0x7fffffff || radix_passes((int)s.nBins) > kRadixMaxPasses)
+        return fail(PS3D_ERR_RANGE, "ps3d_finish_noalloc: a %dx%d target has too many bins to sort", s.tg.w,
+                    s.tg.h);
     NoAllocLayout L;
     size_t base = noalloc_layout(L, s.nd, s.nTris, s.nvMax, s.tg.w, s.tg.h, s.anyColour, s.nBins, kSortChunk);
     if (base > kNoAllocBytes) {
@@ -2296,6 +2323,10 @@ extern "C" int ps3d_finish_noalloc(ps3d_pipeline* p)
     std::lock_guard<std::mutex> lock(g_noallocLock);
     int dev = -1;
     CU(cudaGetDevice(&dev));
+    // the array's address is per device: it must be the device the pipeline's streams belong to
+    if (dev != p->device)
+        return fail(PS3D_ERR_DEVICE, "ps3d_finish_noalloc: device %d is current, the pipeline was created on %d",
+                    dev, p->device);
     if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(PS3D_ERR_DEVICE, "device %d out of range", dev);
     if (!g_noallocPtr[dev]) {
         void* ptr = nullptr;
@@ -2329,7 +2360,15 @@ extern "C" int ps3d_finish_noalloc(ps3d_pipeline* p)
             return target == -3 ? fill_colour_plain(p, c) : fill_depth_plain(p, target, v);
         },
         [&](const Command& c) { return copy_colour_plain(p, c); });
-    if (rc) return rc;
+    if (rc) {
+        // Work already queued on the shared array must finish before the
+        // lock is released; the frame's commands are dropped (incomplete).
+        cudaStreamSynchronize(p->stream);
+        cudaGetLastError();
+        p->launched.clear();
+        p->passStart.clear();
+        return rc;
+    }
     CU(cudaStreamSynchronize(p->stream));
     int st[4];
     CU(cudaMemcpy(st, p->status, sizeof st, cudaMemcpyDeviceToHost));

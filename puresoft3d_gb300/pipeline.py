@@ -63,6 +63,7 @@ _SIGS = {
     "ps3d_flush": [_c_void_p],
     "ps3d_finish": [_c_void_p],
     "ps3d_finish_noalloc": [_c_void_p],
+    "ps3d_allocation_count": [],
     "ps3d_set_bin_width": [_c_void_p, _c_int],
     "ps3d_get_bin_width": [_c_void_p, ctypes.POINTER(_c_int)],
     "ps3d_set_raster_occupancy": [_c_void_p, _c_int],
@@ -106,6 +107,7 @@ def library(path: str | None = None) -> ctypes.CDLL:
             f.restype = ctypes.c_int
         lib.ps3d_last_error.restype = ctypes.c_char_p
         lib.ps3d_last_error.argtypes = []
+        lib.ps3d_allocation_count.restype = ctypes.c_ulonglong
         _lib = lib
     return _lib
 
@@ -130,6 +132,12 @@ def selftest_occlusion(cases: int = 1 << 22):
     if rc < 0:
         raise RuntimeError(lib.ps3d_last_error().decode())
     return int(a.value), int(b.value)
+
+
+def allocation_count() -> int:
+    """Device and pinned-host allocations the library's pipelines have made
+    so far (ps3d_allocation_count)."""
+    return int(library().ps3d_allocation_count())
 
 
 def exported_symbols() -> list:

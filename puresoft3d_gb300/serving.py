@@ -135,6 +135,12 @@ def _clear_ops():
     return [("clearDepth", 1.0), ("clearColour", 0xFF000000)]
 
 
+def job_ops(pool: S.Scene, job: S.Job) -> list:
+    """The calls that render `job` alone in a pipeline of its own size (with
+    `pool`'s resources): clears, the pool's common state, the job's draws."""
+    return _clear_ops() + pool.info["common"] + job.ops
+
+
 class RenderServer:
     def __init__(self, pool: S.Scene, atlas: Tuple[int, int] = (4096, 4096), slots: int = 2,
                  hbm_budget: Optional[int] = None, arena_bytes: int = 1 << 30, bin_width: Optional[int] = None,
@@ -282,7 +288,7 @@ class PlainLoop:
 
     def render(self, job: S.Job, out_off: int = 0) -> None:
         p = self.pipes[(job.width, job.height)]
-        S.replay_ops(_clear_ops() + self.pool.info["common"] + job.ops, p)
+        S.replay_ops(job_ops(self.pool, job), p)
         p.copyColourRect(0, 0, job.width, job.height, self.arena.base + out_off, job.width * 4)
         p.finish()
 

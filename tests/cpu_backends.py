@@ -21,7 +21,9 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ORACLE_SO = os.path.join(ROOT, "oracle", "_build", "libps3d_oracle.so")
 REF_SO = os.path.join(ROOT, "oracle", "_ref", "libps3dref.so")
-REF_SRC = "/root/reference/src/puresoft3d"
+# the reference tree (read-only): PS3D_REFERENCE, else its checkout in the build container
+REF_ROOT = os.environ.get("PS3D_REFERENCE", "/root/reference")
+REF_SRC = os.path.join(REF_ROOT, "src", "puresoft3d")
 
 _API = [
     ("texture_create", [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]),
@@ -180,6 +182,15 @@ class OraclePipeline(_CPipeline):
 
     def fragments(self):
         return self.lib.ps3do_fragments_tested(self.h), self.lib.ps3do_fragments_passed(self.h)
+
+    def readDepth(self) -> np.ndarray:
+        """The default depth buffer, (height, scanline floats): the
+        reference's scanline of round(width / 4) * 4 floats (pipeline.cpp:31)."""
+        scan = int(self.width / 4.0 + 0.5) * 4
+        out = np.empty((self.height, scan), dtype=np.float32)
+        self.lib.ps3do_read_depth.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        self.lib.ps3do_read_depth(self.h, out.ctypes.data)
+        return out
 
     def measureColourError(self, on=True):
         """Compare every shaded fragment's FP32 colour with an FP64 re-shade."""

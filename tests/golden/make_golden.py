@@ -9,9 +9,12 @@ Each fixture records
   * for the small known-answer scenes, the buffers themselves;
   * ``covered``    -- pixels whose depth is below the clear value.
 
+The full-size cases (``full_cases``: configs 2 and 3 exactly as the benchmark
+renders them) keep hashes only.
+
 Run from the repository root on an x86-64 host with the reference tree:
     python tests/golden/make_golden.py [case name ...]
-(no names: every case).
+(no names: every case, the full-size ones included).
 """
 from __future__ import annotations
 
@@ -63,6 +66,12 @@ def golden_cases():
     return cases
 
 
+def full_cases():
+    """Configs 2 and 3 at the size the benchmark renders them (the same
+    generator calls as bench.py's workloads): hash-only fixtures."""
+    return [("c2_1920x1080", S.scene_c2()), ("c3_3840x2160", S.scene_c3())]
+
+
 def render(pipe_cls, scene):
     p = pipe_cls(scene.width, scene.height)
     S.replay_setup(scene, p)
@@ -79,9 +88,11 @@ def main():
     if not ref_available():
         raise SystemExit("the reference sources are needed to make golden fixtures")
     only = set(sys.argv[1:])
-    for name, scene in golden_cases():
+    for name, make in [(n, (lambda s=s: s)) for n, s in golden_cases()] + [
+            ("c2_1920x1080", S.scene_c2), ("c3_3840x2160", S.scene_c3)]:
         if only and name not in only:
             continue
+        scene = make()
         out = render(RefPipeline, scene)
         rec = {"digest": scene_digest(scene), "colour_sha": sha(out["colour"]), "depth_sha": sha(out["depth"]),
                "covered": int((out["depth"] < 1.0).sum())}

@@ -1,7 +1,7 @@
 """Batched views: many independent views rendered in one pass, each into its
 own tile of an atlas (ps3d_set_viewport_rect), give per tile exactly what the
 view gives rendered alone in a pipeline of the view's size; the view alone
-matches the oracle (colour within 1 LSB, bit-exact so far)."""
+matches the oracle (depth bit-exact, colour within 1 LSB)."""
 import numpy as np
 import pytest
 
@@ -54,6 +54,9 @@ def test_atlas_tiles_equal_views_alone(gpu_lib):
 
 @pytest.mark.gpu
 def test_views_alone_match_oracle(gpu_lib):
+    """Every view alone against the oracle: depth bit-exact, colour within
+    1 LSB."""
+    from common import assert_depth_exact
     from puresoft3d_gb300 import scenes as S
     from puresoft3d_gb300.pipeline import PuresoftPipeline
     _, plain = _scenes()
@@ -61,12 +64,14 @@ def test_views_alone_match_oracle(gpu_lib):
     o = OraclePipeline(SIZE, SIZE)
     S.replay_setup(plain, g)
     S.replay_setup(plain, o)
-    for v in range(0, VIEWS, 3):
+    for v in range(VIEWS):
         S.replay_ops(plain.info["view_frames"][v], g)
         S.replay_ops(plain.info["view_frames"][v], o)
+        assert_depth_exact(g.readDepth()[:, :SIZE], o.readDepth()[:, :SIZE], "view %d" % v)
         mx, mean = colour_diff(g.readColour(), o.readColour())
         assert mx <= 1, "view %d: colour differs by up to %d LSB (mean %.4f)" % (v, mx, mean)
     g.close()
+    o.close()
 
 
 @pytest.mark.gpu

@@ -1,0 +1,131 @@
+"""Full-size parity: the frames bench.py times, rendered through the C ABI
+on the GPU, against the oracle (the C restatement, on all host cores) and
+against the hashes of the reference build's own render of the same inputs
+(tests/golden/c2_1920x1080.npz, c3_3840x2160.npz).
+
+Configs 2 and 3 at their full size (2048^2 shadow pass + 1920x1080 LIT2
+pass over 200k triangles; 3840x2160 LIT3 over 2M triangles in four depth
+layers) at the schedule the benchmark pins and at the default schedule;
+config 4 as the benchmark batches it (4096 views of 128x128 in one pass over
+an 8192^2 atlas) against each view rendered alone by the oracle.  Depth and
+shadow maps bit-exact, colour within 1 LSB, fragment counts equal."""
+import os
+
+import numpy as np
+import pytest
+
+from common import assert_depth_exact, colour_diff, load_golden, render, sha
+from cpu_backends import OraclePipeline
+from golden.make_golden import scene_digest
+
+COLOUR_TOL = 1  # LSB per channel
+FULL = {"c2_1920x1080": ("c2", "scene_c2"), "c3_3840x2160": ("c3", "scene_c3")}
+_cache = {}
+
+
+def _oracle(name):
+    """The scene and the oracle's render of it (with fragment counts), once per session."""
+    if name not in _cache:
+        from puresoft3d_gb300 import scenes as S
+        scene = getattr(S, FULL[name][1])()
+        g = load_golden(name)
+        # the scene's inputs must be the ones the reference build rendered
+        assert scene_digest(scene) == str(g["digest"]), "%s: scene inputs differ from the fixture's" % name
+        o = OraclePipeline(scene.width, scene.height, os.cpu_count() or 1)
+        out = render(o, scene)
+        out["fragments"] = o.fragments()
+        o.close()
+        _cache[name] = (scene, out, g)
+    return _cache[name]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("sched", ["pinned", "default"])
+@pytest.mark.parametrize("name", sorted(FULL))
+def test_full_size_frame_matches_oracle_and_reference(gpu_lib, name, sched):
+    from puresoft3d_gb300.autotune import PINNED, apply
+    from puresoft3d_gb300.pipeline import PuresoftPipeline
+    scene, ora, g = _oracle(name)
+    # the oracle is pinned to the reference build at this size
+    assert sha(ora["depth"]) == str(g["depth_sha"]) and sha(ora["colour"]) == str(g["colour_sha"]), name
+    p = PuresoftPipeline(scene.width, scene.height)
+    if sched == "pinned":
+        apply(p, PINNED[FULL[name][0]])
+    p.setFragmentCounting(True)
+    gpu = render(p, scene)
+    st = p.stats()
+    p.close()
+    assert_depth_exact(gpu["depth"], ora["depth"], name)
+    assert sha(gpu["depth"]) == str(g["depth_sha"]), name
+    if "shadow" in ora:
+        assert_depth_exact(gpu["shadow"], ora["shadow"], name + " shadow map")
+        assert sha(gpu["shadow"]) == str(g["shadow_sha"]), name
+    mx, mean = colour_diff(gpu["colour"], ora["colour"])
+    assert mx <= COLOUR_TOL, "%s: colour differs by up to %d LSB (mean %.4f)" % (name, mx, mean)
+    assert (st["fragments"], st["fragments_passed"]) == ora["fragments"], name
+    assert int((gpu["depth"] < 1.0).sum()) == int(g["covered"])
+
+
+@pytest.mark.gpu
+def test_full_size_command_buffer_replay(gpu_lib):
+    """Config 2 recorded once and replayed as a CUDA graph (the benchmark's
+    timed step) gives the oracle's frame on every replay."""
+    from puresoft3d_gb300 import scenes as S
+    from puresoft3d_gb300.autotune import PINNED, apply
+    from puresoft3d_gb300.pipeline import PuresoftPipeline
+    scene, ora, _ = _oracle("c2_1920x1080")
+    p = PuresoftPipeline(scene.width, scene.height)
+    S.replay_setup(scene, p)
+    apply(p, PINNED["c2"])
+    p.beginCommands()
+    S.replay_frame(scene, p)
+    cb = p.endCommands()
+    for _ in range(3):
+        p.clearColour(0)
+        p.finish()
+        cb.submit()
+        p.finish()
+        assert_depth_exact(p.readDepthTexture(scene.info["depth_texture"]), ora["depth"], "c2 replay")
+        assert_depth_exact(p.readDepthTexture(scene.info["shadow_texture"]), ora["shadow"], "c2 replay shadow")
+        assert colour_diff(p.readColour(), ora["colour"])[0] <= COLOUR_TOL
+    cb.destroy()
+    p.close()
+
+
+def _tile(atlas_colour, atlas_depth, ox, oy, size):
+    h = atlas_colour.shape[0]  # colour memory is top-down: pixel row y is memory row h-1-y
+    return atlas_colour[h - oy - size:h - oy, ox:ox + size], atlas_depth[oy:oy + size, ox:ox + size]
+
+
+@pytest.mark.gpu
+def test_full_size_atlas_matches_oracle_views(gpu_lib):
+    """Config 4 as the benchmark renders it: 4096 views in one pass over an
+    8192^2 atlas at the pinned schedule; every tile against the oracle's
+    render of its view alone in a 128x128 pipeline (colour and depth)."""
+    from puresoft3d_gb300 import scenes as S
+    from puresoft3d_gb300.autotune import PINNED, apply
+    from puresoft3d_gb300.pipeline import PuresoftPipeline
+    batched, plain = S.scene_c4(views=4096)
+    size = batched.info["view_size"]
+    atlas = PuresoftPipeline(batched.width, batched.height)
+    S.replay_setup(batched, atlas)
+    apply(atlas, PINNED["c4"])
+    S.replay_frame(batched, atlas)
+    colour = atlas.readColour()
+    depth = atlas.readDepth()[:, :batched.width]
+    atlas.close()
+    o = OraclePipeline(size, size, os.cpu_count() or 1)
+    S.replay_setup(plain, o)
+    covered, worst = 0, 0
+    for v, (ox, oy) in enumerate(batched.info["origins"]):
+        S.replay_ops(plain.info["view_frames"][v], o)
+        oc = o.readColour()
+        od = o.readDepth()[:, :size]
+        tc, td = _tile(colour, depth, ox, oy, size)
+        assert_depth_exact(td, od, "view %d" % v)
+        mx, _ = colour_diff(tc, oc)
+        assert mx <= COLOUR_TOL, "view %d: colour differs by up to %d LSB" % (v, mx)
+        worst = max(worst, mx)
+        covered += int((od < 1.0).sum())
+    o.close()
+    assert covered > 4096 * 500, "views cover too little to test anything"

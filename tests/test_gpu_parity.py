@@ -22,9 +22,13 @@ def test_gpu_matches_oracle(name, scene, gpu_lib):
         assert_depth_exact(gpu["shadow"], ora["shadow"], name + " shadow map")
     mx, mean = colour_diff(gpu["colour"], ora["colour"])
     assert mx <= COLOUR_TOL, "%s: colour differs by up to %d LSB (mean %.4f)" % (name, mx, mean)
+    # pinned to the reference build's own render of the same inputs: the
+    # inputs generated on this host must be the fixture's
     g = load_golden(name)
-    if scene_digest(scene) == str(g["digest"]):
-        assert sha(gpu["depth"]) == str(g["depth_sha"]), name
+    assert scene_digest(scene) == str(g["digest"]), "%s: scene inputs differ from the fixture's" % name
+    assert sha(gpu["depth"]) == str(g["depth_sha"]), name
+    if "shadow_sha" in g:
+        assert sha(gpu["shadow"]) == str(g["shadow_sha"]), name
 
 
 @pytest.mark.gpu

@@ -12,7 +12,7 @@ import pytest
 from puresoft3d_gb300 import objx
 from puresoft3d_gb300 import scenes as S
 
-REF_SPHERE = "/root/reference/src/test/sphere.objx"
+REF_SPHERE = os.path.join(os.environ.get("PS3D_REFERENCE", "/root/reference"), "src", "test", "sphere.objx")
 
 
 def parse(path):

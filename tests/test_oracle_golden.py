@@ -1,6 +1,8 @@
 """The oracle (C restatement of the reference pipeline) against golden
 fixtures rendered by the reference's own pipeline core, and -- where the
 reference sources are present -- against that build directly."""
+import os
+
 import numpy as np
 import pytest
 
@@ -53,6 +55,26 @@ def test_oracle_matches_golden(name, scene):
     assert sha(out["depth"]) == str(g["depth_sha"]), name
     if not approx:
         assert sha(out["colour"]) == str(g["colour_sha"]), name
+    if "shadow_sha" in g:
+        assert sha(out["shadow"]) == str(g["shadow_sha"]), name
+    assert int((out["depth"] < 1.0).sum()) == int(g["covered"])
+
+
+FULL = {"c2_1920x1080": "scene_c2", "c3_3840x2160": "scene_c3"}
+
+
+@pytest.mark.parametrize("name", sorted(FULL))
+def test_oracle_matches_golden_full_size(name):
+    """Configs 2 and 3 at the size the benchmark renders them: the oracle's
+    colour, depth and shadow map hash to what the reference build rendered.
+    The scene inputs must be the fixture's: a digest mismatch fails."""
+    from puresoft3d_gb300 import scenes as S
+    g = load_golden(name)
+    scene = getattr(S, FULL[name])()
+    assert scene_digest(scene) == str(g["digest"]), "%s: scene inputs differ from the fixture's" % name
+    out = render(OraclePipeline(scene.width, scene.height, os.cpu_count() or 1), scene)
+    assert sha(out["depth"]) == str(g["depth_sha"]), name
+    assert sha(out["colour"]) == str(g["colour_sha"]), name
     if "shadow_sha" in g:
         assert sha(out["shadow"]) == str(g["shadow_sha"]), name
     assert int((out["depth"] < 1.0).sum()) == int(g["covered"])

@@ -89,6 +89,20 @@ def test_served_images_equal_alone(gpu_lib, monkeypatch):
         assert np.array_equal(d.image, alone[d.job.id]), "job %d differs in the mix" % d.job.id
         covered += int((d.image[..., :3].max(axis=2) > 0).sum())
     assert covered > 5000
+    # and each served image is the oracle's render of the job (within 1 LSB)
+    from cpu_backends import OraclePipeline
+    from puresoft3d_gb300.serving import job_ops
+    oracles = {}
+    for wh in RES:
+        oracles[wh] = OraclePipeline(wh[0], wh[1])
+        S.replay_setup(pool, oracles[wh])
+    for d in done:
+        o = oracles[(d.job.width, d.job.height)]
+        S.replay_ops(job_ops(pool, d.job), o)
+        diff = np.abs(d.image.astype(np.int32) - o.readColour().astype(np.int32)).max()
+        assert diff <= 1, "job %d: served image differs from the oracle by %d LSB" % (d.job.id, diff)
+    for o in oracles.values():
+        o.close()
     s = summarize(done)
     assert s["p99_ms"] >= s["p50_ms"] > 0
     srv.close()

@@ -49,15 +49,18 @@ def _same(a, b, what):
 @pytest.mark.parametrize("name,scene", CASES, ids=[c[0] for c in CASES])
 def test_noalloc_matches_finish(name, scene, gpu_lib):
     from puresoft3d_gb300 import scenes as S
-    from puresoft3d_gb300.pipeline import PuresoftPipeline
+    from puresoft3d_gb300.pipeline import PuresoftPipeline, allocation_count
     ref = _reference(scene)
     p = PuresoftPipeline(scene.width, scene.height)
     S.replay_setup(scene, p)
     p.finish()
     p.finishNoAlloc()  # first call: looks the scratch address up
+    allocs = allocation_count()
     for call in range(2):
         S.replay_frame(scene, p)
         p.finishNoAlloc()
+        # the defining property: no device or pinned allocation was made
+        assert allocation_count() == allocs, "%s call %d allocated" % (name, call + 1)
         _same(ref, _outputs(p, scene), "%s call %d" % (name, call + 1))
     p.close()
 
