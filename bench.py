@@ -211,20 +211,31 @@ def make_scene(cfg, views=4096):
     return {"c1": S.scene_c1, "c2": S.scene_c2, "c3": S.scene_c3}[cfg]()
 
 
-def autotune(pipe, record, key, args):
-    """Bin width for this workload, picked by timing each candidate on the
-    frame itself (puresoft3d_gb300.autotune); untimed."""
-    from puresoft3d_gb300.autotune import Autotuner
+def _sched_dict(s, source, span_items=0):
+    return {"bin_width": s[0], "raster_occupancy": s[1], "span_culling": s[2], "row_split": s[3],
+            "warp_bins": s[4], "span_items": span_items, "source": source}
+
+
+def autotune(pipe, record, key, args, pinned=None):
+    """The schedule the workload is timed at, applied to `pipe`: the flags'
+    (--bin-width ...) when given; else, with --autotune, the fastest
+    candidate timed on the frame itself (puresoft3d_gb300.autotune;
+    untimed); else the schedule pinned for the workload
+    (puresoft3d_gb300.autotune.PINNED), so that its profiles under profiles/
+    describe the same kernels."""
+    from puresoft3d_gb300.autotune import Autotuner, apply
+    pipe.setSpanItems(args.span_items)
     if args.bin_width:
-        pipe.setBinWidth(args.bin_width)
-        pipe.setRasterOccupancy(args.raster_occupancy)
-        pipe.setSpanCulling(args.span_culling)
-        pipe.setRowSplit(args.row_split)
-        return {"bin_width": args.bin_width, "raster_occupancy": args.raster_occupancy,
-                "span_culling": args.span_culling, "row_split": args.row_split, "source": "flags"}
+        s = (args.bin_width, args.raster_occupancy, args.span_culling, args.row_split, args.warp_bins)
+        apply(pipe, s)
+        return _sched_dict(s, "flags", args.span_items)
+    if pinned is not None and not args.autotune:
+        apply(pipe, pinned)
+        return _sched_dict(tuple(pinned) + (0,) * (5 - len(pinned)), "pinned", args.span_items)
     best, ms = Autotuner().tune(pipe, record, key, reps=3)
-    return {"bin_width": best[0], "raster_occupancy": best[1], "span_culling": best[2], "row_split": best[3],
-            "source": "autotuner", "candidate_ms": {k: round(v, 4) for k, v in ms.items()}}
+    d = _sched_dict(best, "autotuner", args.span_items)
+    d["candidate_ms"] = {k: round(v, 4) for k, v in ms.items()}
+    return d
 
 
 def twin(scene, tune):
@@ -234,7 +245,9 @@ def twin(scene, tune):
     from puresoft3d_gb300.pipeline import PuresoftPipeline
     p = PuresoftPipeline(scene.width, scene.height)
     S.replay_setup(scene, p)
-    apply(p, (tune["bin_width"], tune["raster_occupancy"], tune["span_culling"], tune["row_split"]))
+    apply(p, (tune["bin_width"], tune["raster_occupancy"], tune["span_culling"], tune["row_split"],
+              tune.get("warp_bins", 0)))
+    p.setSpanItems(tune.get("span_items", 0))
     p.finish()
     return p
 
@@ -287,8 +300,9 @@ def run_c4(args):
     pipe = PuresoftPipeline(batched.width, batched.height)
     S.replay_setup(batched, pipe)
     pipe.finish()
+    from puresoft3d_gb300.autotune import PINNED
     tune = autotune(pipe, lambda p: S.replay_frame(batched, p), "c4:%d:%dx%d" % (views, batched.width, batched.height),
-                    args)
+                    args, PINNED["c4"] if views == 4096 else None)
     pipe.setFragmentCounting(True)
     st0 = pipe.stats()
     S.replay_frame(batched, pipe)
@@ -524,11 +538,12 @@ def run_frames_only(args):
     scene = make_scene(args.config, args.views)
     pipe = PuresoftPipeline(scene.width, scene.height)
     S.replay_setup(scene, pipe)
+    from puresoft3d_gb300.autotune import PINNED, apply
+    pipe.setSpanItems(args.span_items)
     if args.bin_width:
-        pipe.setBinWidth(args.bin_width)
-        pipe.setRasterOccupancy(args.raster_occupancy)
-        pipe.setSpanCulling(args.span_culling)
-        pipe.setRowSplit(args.row_split)
+        apply(pipe, (args.bin_width, args.raster_occupancy, args.span_culling, args.row_split, args.warp_bins))
+    elif args.config in PINNED:
+        apply(pipe, PINNED[args.config])
     for _ in range(args.ncu_frames):
         S.replay_frame(scene, pipe)
         pipe.finish()
@@ -614,8 +629,9 @@ def run_ours(args):
     pipe = PuresoftPipeline(scene.width, scene.height)
     S.replay_setup(scene, pipe)
     pipe.finish()
+    from puresoft3d_gb300.autotune import PINNED
     tune = autotune(pipe, lambda p: S.replay_frame(scene, p), "%s:%dx%d:%d" % (
-        args.config, scene.width, scene.height, scene.triangles()), args)
+        args.config, scene.width, scene.height, scene.triangles()), args, PINNED.get(args.config))
 
     # fragments and pairs per frame (counting run, untimed)
     pipe.setFragmentCounting(True)
@@ -901,6 +917,12 @@ def main():
                     help="with --bin-width: raster variant with (1) or without (0) the span occlusion test")
     ap.add_argument("--row-split", type=int, default=1, choices=[1, 2, 4, 8],
                     help="with --bin-width: raster blocks per bin (crowded bins shared out by rows)")
+    ap.add_argument("--warp-bins", type=int, default=0, choices=[0, 1],
+                    help="with --bin-width 8 or 16: one raster warp per bin (1) or four sharing it (0)")
+    ap.add_argument("--span-items", type=int, default=0, choices=[0, 1],
+                    help="bin short triangles' row spans as set-up items (1) or whole triangles (0)")
+    ap.add_argument("--autotune", action="store_true",
+                    help="time every schedule candidate on the frame and use the fastest (default: the pinned one)")
     args = ap.parse_args()
     if args.ncu_frames:
         run_frames_only(args)

@@ -294,6 +294,19 @@ int ps3d_set_row_split(ps3d_pipeline* p, int blocksPerBin);
  * 8 blocks fit per SM where shared memory allows (more warps to hide
  * latency).  Time only, never results. */
 int ps3d_set_raster_occupancy(ps3d_pipeline* p, int blocksPerSM);
+/* Raster shape: 0 (the default) four warps share each bin and meet at
+ * block barriers; 1 each warp owns a bin of 8 or 16 columns and works
+ * through it alone (no block barrier; bins of 32 columns and passes that
+ * blend or discard keep the shared shape).  Time only, never results. */
+int ps3d_set_raster_warp_bins(ps3d_pipeline* p, int on);
+/* Span items: 1 bins each row span of a triangle up to 32 rows tall as its
+ * own item, set up (row result, span set-up and the sequential steps to its
+ * first pixel in the bin) in the set-up kernel, where all triangles run in
+ * parallel, instead of in the raster, where a crowded bin's spans are set up
+ * by one block; 0 (the default) bins whole triangles and sets their spans up
+ * in the raster.  Passes that blend or discard bin whole triangles either
+ * way.  Time only, never results. */
+int ps3d_set_span_items(ps3d_pipeline* p, int on);
 
 /* ps3d_finish for callers that must not allocate device memory; it has no
  * counterpart in the reference, whose CPU pipeline allocates no device memory

@@ -1,9 +1,8 @@
 """Schedule autotuner for the device passes.
 
-A schedule is (bin width, raster occupancy, span culling, row split).  The
-bin width (8, 16 or
-32 columns; bins are always 32 rows) sets how the raster kernel's work is
-cut:
+A schedule is (bin width, raster occupancy, span culling, row split, warp
+bins).  The bin width (8, 16 or 32 columns; bins are always 32 rows) sets
+how the raster kernel's work is cut:
 
 * the number of bins, hence blocks, a pass launches (more, smaller bins give
   small views and thin targets more parallelism);
@@ -20,7 +19,10 @@ drops spans that cannot pass the depth test before their depths are
 computed, in crowded bins: it pays off with depth complexity and costs a
 little elsewhere.  The row split (1 or 4 raster blocks per bin) shares the
 rows of crowded bins out between blocks: it pays off when a few crowded
-bins would otherwise run alone at the end of the launch.
+bins would otherwise run alone at the end of the launch.  Warp bins (1)
+switch the raster to one warp per bin of 8 or 16 columns that works through
+it alone, with no block-wide barrier between its span set-up and its walk
+(0: four warps share a bin; 32-column bins always do).
 
 Which schedule wins depends on the workload (triangle sizes, depth complexity,
 target size), so the tuner times every candidate on the caller's own frame:
@@ -39,8 +41,9 @@ import os
 import statistics
 from typing import Callable, Dict, Optional, Sequence, Tuple
 
-CANDIDATES = tuple((bw, occ, cull, split) for bw in (8, 16, 32) for occ in (0, 8) for cull in (1, 0)
-                   for split in (1, 4))
+CANDIDATES = tuple((bw, occ, cull, split, 0) for bw in (8, 16, 32) for occ in (0, 8) for cull in (1, 0)
+                   for split in (1, 4)) + tuple((bw, 0, cull, split, 1) for bw in (8, 16) for cull in (1, 0)
+                                                for split in (1, 4))
 
 
 # The schedule bench.py renders each workload with unless asked to tune:
@@ -57,22 +60,24 @@ PINNED = {
 
 
 def _sched(c):
-    """(bin width, occupancy, span culling, row split) of a candidate given
-    as a bare width or a shorter tuple (occupancy 0, culling on and one block
-    per bin by default)."""
+    """(bin width, occupancy, span culling, row split, warp bins) of a
+    candidate given as a bare width or a shorter tuple (occupancy 0, culling
+    on, one block per bin and shared bins by default)."""
     if not isinstance(c, (tuple, list)):
         c = (c,)
-    d = (None, 0, 1, 1)
-    return tuple(int(c[i]) if i < len(c) else d[i] for i in range(4))
+    d = (None, 0, 1, 1, 0)
+    return tuple(int(c[i]) if i < len(c) else d[i] for i in range(5))
 
 
 def _name(c) -> str:
-    return "%d/%d/%d/%d" % _sched(c)
+    return "%d/%d/%d/%d/%d" % _sched(c)
 
 
 def apply(pipe, c) -> None:
-    bw, occ, cull, split = _sched(c)
+    bw, occ, cull, split, warp = _sched(c)
     pipe.setBinWidth(bw)
+    if hasattr(pipe, "setWarpBins"):
+        pipe.setWarpBins(warp)
     if hasattr(pipe, "setRasterOccupancy"):
         pipe.setRasterOccupancy(occ)
     if hasattr(pipe, "setSpanCulling"):
@@ -145,10 +150,10 @@ class Autotuner:
 
     def tune(self, pipe, record: Callable[[object], None], key: str,
              candidates: Sequence = CANDIDATES, reps: int = 5, warmup: int = 2,
-             retune: bool = False) -> Tuple[Tuple[int, int, int, int], Dict[str, float]]:
+             retune: bool = False) -> Tuple[Tuple[int, int, int, int, int], Dict[str, float]]:
         """Sets `pipe`'s schedule to the fastest candidate for `record`'s
         frame and returns ((bin width, raster occupancy, span culling, row
-        split), {"bw/occ/cull/split": median ms}).  A candidate is such a
+        split, warp bins), {"bw/occ/cull/split/warp": median ms}).  A candidate is such a
         tuple, a shorter prefix of it or a bare bin width.  A cached result
         for (key, device, candidates) is reused unless `retune`."""
         full = "%s|%s|%s" % (key, device_name(), ",".join(_name(c) for c in candidates))

@@ -17,7 +17,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libps3d.so")
-SOURCES = ["setup_bin.cu", "raster_shade.cu", "post.cu", "pipeline.cpp", "objx.cpp"]
+SOURCES = ["setup_bin.cu", "raster_shade.cu", "raster_warp.cu", "post.cu", "pipeline.cpp", "objx.cpp"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc")
 FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17", "--fmad=false",
          "-prec-div=true", "-prec-sqrt=true", "-ftz=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",

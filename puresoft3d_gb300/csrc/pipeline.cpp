@@ -201,6 +201,7 @@ struct Scratch {
     int* keyB = nullptr; size_t keyBCap = 0;
     int* binStart = nullptr; size_t binStartCap = 0;
     int2* shadeList = nullptr; size_t shadeListCap = 0;
+    SpanItem* spans = nullptr; size_t spansCap = 0;
     DrawDesc* draws = nullptr; size_t drawsCap = 0;
     DrawUniforms* unis = nullptr; size_t unisCap = 0;
     int* slotStatus = nullptr;  // 16 ints, allocated with the pipeline
@@ -243,6 +244,8 @@ struct ps3d_pipeline {
     int rasterBlocks = 0;
     int cullSpans = 1;
     int rowSplit = 1;
+    int warpBins = 0;
+    int spanItems = 0;
     bool countFrags = false;
     cudaStream_t stream = nullptr;
     bool ownStream = false;
@@ -580,7 +583,7 @@ int snapshot_uniforms(const ps3d_pipeline* p, DrawUniforms& U)
 }
 
 int ensure_scratch(ps3d_pipeline* p, Scratch& x, int nTris, int nvMax, int W, int H, int binsX, int binsY,
-                   bool colour)
+                   bool colour, bool spanItems)
 {
     size_t nBins = (size_t)binsX * binsY;
     int sortBlocks = (p->pairCap + kSortChunk - 1) / kSortChunk;
@@ -590,6 +593,7 @@ int ensure_scratch(ps3d_pipeline* p, Scratch& x, int nTris, int nvMax, int W, in
               dev_alloc(x.radix, x.radixCap, radix_scratch_ints(sortBlocks, radix_passes((int)nBins), nTris)) &&
               dev_alloc(x.binStart, x.binStartCap, nBins + 1 + (size_t)kItemsPerBin * nBins);
     if (ok && colour) ok = dev_alloc(x.shadeList, x.shadeListCap, (size_t)W * H);
+    if (ok && spanItems) ok = dev_alloc(x.spans, x.spansCap, p->pairCap);
     if (!ok) return fail(PS3D_ERR_NOMEM, "device scratch allocation failed");
     return 0;
 }
@@ -833,7 +837,8 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     int binW = forward ? 16 : p->binW;  // forward passes run with 16-column bins
     int binsX = (W + binW - 1) / binW, binsY = (H + kBinH - 1) / kBinH;
     if (radix_passes(binsX * binsY) > kRadixMaxPasses) return fail(PS3D_ERR_RANGE, "target too large for the bin sort");
-    if ((rc = ensure_scratch(p, x, nTris, nvMax, W, H, binsX, binsY, anyColour))) return rc;
+    const bool spanItems = p->spanItems && !forward;  // a forward pass shades from its triangles' records
+    if ((rc = ensure_scratch(p, x, nTris, nvMax, W, H, binsX, binsY, anyColour, spanItems))) return rc;
     const DrawDesc* devDraws;
     const DrawUniforms* devUnis;
     if (p->cbOffsets) {  // capturing a command buffer: its descriptors are already on the device
@@ -865,6 +870,9 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     P.rasterBlocks = p->rasterBlocks;
     P.cullSpans = p->cullSpans;
     P.rowSplit = p->rowSplit;
+    P.warpBins = p->warpBins;
+    P.spanItems = spanItems;
+    P.spans = spanItems ? x.spans : nullptr;
     P.passFp = pass_fp(dd.data(), dd.size());
     P.forward = forward;
     P.binsX = binsX;
@@ -1239,7 +1247,7 @@ int ps3d_pipeline_destroy(ps3d_pipeline* p)
     for (int k = 0; k < kSlots; k++) {
         Scratch& x = p->scr[k];
         void* sb[] = {x.tris, x.vary, x.pairKey, x.pairTri, x.keyB, x.binTri, x.radix, x.binStart, x.shadeList,
-                      x.draws, x.unis};
+                      x.spans, x.draws, x.unis};
         for (void* b : sb)
             if (b) cudaFree(b);
         if (p->gs[k]) {
@@ -1683,6 +1691,20 @@ int ps3d_set_row_split(ps3d_pipeline* p, int blocksPerBin)
     if (blocksPerBin != 1 && blocksPerBin != 2 && blocksPerBin != 4 && blocksPerBin != 8)
         return fail(PS3D_ERR_INVALID, "blocks per bin must be 1, 2, 4 or 8");
     p->rowSplit = blocksPerBin;
+    return 0;
+}
+
+int ps3d_set_span_items(ps3d_pipeline* p, int on)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    p->spanItems = on ? 1 : 0;
+    return 0;
+}
+
+int ps3d_set_raster_warp_bins(ps3d_pipeline* p, int on)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    p->warpBins = on ? 1 : 0;
     return 0;
 }
 
@@ -2130,11 +2152,11 @@ DrawUniforms g_noallocUnis[kNoAllocMaxDraws];
 // Byte offsets of one pass's buffers in the array, each 256-byte aligned.
 struct NoAllocLayout {
     size_t draws, unis, tris, vary, shadeList, binStart, radix, pairKey,
-        pairTri, keyB, binTri;
+        pairTri, keyB, binTri, spans;
 };
 
 size_t noalloc_layout(NoAllocLayout& L, int nd, int nTris, int nv, int W, int H, bool colour, size_t nBins,
-                      int pairCap)
+                      int pairCap, bool spanItems)
 {
     size_t off = 0;
     auto take = [&](size_t bytes) {
@@ -2155,6 +2177,7 @@ size_t noalloc_layout(NoAllocLayout& L, int nd, int nTris, int nv, int W, int H,
     L.pairTri = take((size_t)pairCap * sizeof(int));
     L.keyB = take((size_t)pairCap * sizeof(int));
     L.binTri = take((size_t)pairCap * sizeof(int));
+    L.spans = spanItems ? take((size_t)pairCap * sizeof(SpanItem)) : 0;
     return off;
 }
 
@@ -2168,6 +2191,7 @@ struct NoAllocPass {
     int pairCap = 0;  // largest multiple of the sort chunk that fits, 0 if none does
     bool forward = false;
     int binW = 0;
+    bool spanItems = false;
 };
 
 int noalloc_shape(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps, NoAllocPass& s, bool stage)
@@ -2194,6 +2218,7 @@ int noalloc_shape(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass
     if (s.nTris == 0) return 0;
     if (s.forward) s.nvMax = forward_vary(s.nvMax);
     s.binW = s.forward ? 16 : p->binW;
+    s.spanItems = p->spanItems && !s.forward;
     s.binsX = (s.tg.w + s.binW - 1) / s.binW;
     s.binsY = (s.tg.h + kBinH - 1) / kBinH;
     s.nBins = (size_t)s.binsX * s.binsY;
@@ -2201,7 +2226,8 @@ int noalloc_shape(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass
         return fail(PS3D_ERR_RANGE, "ps3d_finish_noalloc: a %dx%d target has too many bins to sort", s.tg.w,
                     s.tg.h);
     NoAllocLayout L;
-    size_t base = noalloc_layout(L, s.nd, s.nTris, s.nvMax, s.tg.w, s.tg.h, s.anyColour, s.nBins, kSortChunk);
+    size_t base = noalloc_layout(L, s.nd, s.nTris, s.nvMax, s.tg.w, s.tg.h, s.anyColour, s.nBins, kSortChunk,
+                                 s.spanItems);
     if (base > kNoAllocBytes) {
         if (base == (size_t)-1) base = 0;
         return fail(PS3D_ERR_RANGE,
@@ -2209,13 +2235,14 @@ int noalloc_shape(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass
                     "before its bin lists; the fixed scratch is %zu bytes (ps3d_finish has no such limit)",
                     s.nTris, s.tg.w, s.tg.h, base, kNoAllocBytes);
     }
-    // each further sort tile costs its four pair arrays and its look-back descriptors
-    size_t perChunk = (size_t)kSortChunk * 4 * sizeof(int) + (size_t)kRadixMaxPasses * kRadixDigits * sizeof(int);
+    // each further sort tile costs its four pair arrays (and span items) and its look-back descriptors
+    size_t perChunk = (size_t)kSortChunk * (4 * sizeof(int) + (s.spanItems ? sizeof(SpanItem) : 0)) +
+                      (size_t)kRadixMaxPasses * kRadixDigits * sizeof(int);
     long long chunks = 1 + (long long)((kNoAllocBytes - base) / perChunk);
     chunks = std::min<long long>(chunks, 0x7fffffff / kSortChunk);
     while (chunks > 1 &&
            noalloc_layout(L, s.nd, s.nTris, s.nvMax, s.tg.w, s.tg.h, s.anyColour, s.nBins,
-                          (int)(chunks * kSortChunk)) > kNoAllocBytes)
+                          (int)(chunks * kSortChunk), s.spanItems) > kNoAllocBytes)
         chunks--;
     s.pairCap = (int)(chunks * kSortChunk);
     return 0;
@@ -2237,7 +2264,7 @@ int noalloc_run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const P
     }
     int W = s.tg.w, H = s.tg.h;
     NoAllocLayout L;
-    noalloc_layout(L, s.nd, s.nTris, s.nvMax, W, H, s.anyColour, s.nBins, s.pairCap);
+    noalloc_layout(L, s.nd, s.nTris, s.nvMax, W, H, s.anyColour, s.nBins, s.pairCap, s.spanItems);
     // Pageable-source copies: each returns once the staging arrays are copied
     // out, so the next pass may overwrite them.
     CU(cudaMemcpyAsync(base + L.draws, g_noallocDraws, s.nd * sizeof(DrawDesc), cudaMemcpyHostToDevice, p->stream));
@@ -2258,7 +2285,10 @@ int noalloc_run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const P
     P.rasterBlocks = p->rasterBlocks;
     P.cullSpans = p->cullSpans;
     P.rowSplit = p->rowSplit;
+    P.warpBins = p->warpBins;
     P.passFp = pass_fp(g_noallocDraws, (size_t)s.nd);
+    P.spanItems = s.spanItems;
+    P.spans = s.spanItems ? (SpanItem*)(base + L.spans) : nullptr;
     P.forward = s.forward;
     P.binsX = s.binsX;
     P.binsY = s.binsY;

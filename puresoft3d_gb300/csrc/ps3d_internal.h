@@ -102,6 +102,22 @@ struct TriRaster {
 };
 static_assert(sizeof(TriRaster) == 64, "TriRaster must be 64 bytes");
 
+// A span item: one row span of a short triangle, the part of it that lies in
+// one bin, set up by k_setup_emit so that the raster reads it instead of
+// deriving it (32 bytes).  cf2 / pz are the interpolation state at pixel xs
+// -- the reference's span set-up (interp.cpp:26-80) followed by the
+// sequential per-pixel steps from leftClamped (interp.cpp:82-92) -- and the
+// steps continue it.  In the sorted bin lists a span item appears as ~index
+// (negative); a triangle (non-negative index) is set up by the raster.
+struct SpanItem {
+    float cf2, pz, cf2Step, pzStep;
+    int tri;          // the triangle (the winner id a covered pixel records)
+    short xs, xe;     // target columns, inclusive, inside one bin
+    int y;            // target row
+    int flags;        // the draw's flags (behaviour bits | F_COLOUR | F_FRAGMENT)
+};
+static_assert(sizeof(SpanItem) == 32, "SpanItem must be 32 bytes");
+
 // Kernel parameters of one device pass (a run of draws into one target).
 struct PassParams {
     int W, H;                 // target (depth buffer) size; each draw has its own viewport rectangle
@@ -109,6 +125,9 @@ struct PassParams {
     int rasterBlocks;         // raster variant: 0 = registers as needed, 8 = capped for 8 blocks per SM
     int cullSpans;            // raster variant: 1 = occluded spans dropped in crowded bins
     int rowSplit;             // raster blocks per bin (1, 2, 4 or 8): crowded bins shared out by rows
+    int warpBins;             // raster shape: 1 = one warp per bin (k_raster_warp, 8- or 16-column bins)
+    int spanItems;            // 1 = short triangles are binned as set-up span items (no forward passes)
+    SpanItem* spans;          // span items, by emission index (capacity pairCap)
     int passFp;               // the fragment processor every colour draw of the pass uses, else 0
     int forward;              // some draw blends or may discard: shade every passing fragment in order
     int nTris, nDraws;

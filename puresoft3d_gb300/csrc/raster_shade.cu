@@ -26,25 +26,9 @@
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <vector>
-#include "device_common.cuh"
+#include "raster_common.cuh"
 
 namespace ps3d {
-
-__device__ __forceinline__ void bin_range(const PassParams& P, int bin, int& start, int& end)
-{
-    if (P.slotStatus[kSlotTiles] == 0) {  // no pairs
-        start = end = 0;
-        return;
-    }
-    start = P.binStart[bin];
-    end = P.binStart[bin + 1];
-}
-
-// The pass's clear colour at target pixel (x, y) (colour rows top-down).
-__device__ __forceinline__ void clear_colour_px(const PassParams& P, int x, int y)
-{
-    ((uint32_t*)P.colour)[(size_t)(P.colourH - 1 - y) * P.colourW + x] = P.colourClearValue;
-}
 
 // Per span of a round: its columns in the bin, its triangle slot and flags.
 struct SpanRec {
@@ -189,52 +173,6 @@ __device__ __forceinline__ int shade_fragment(const DrawDesc& d, const DrawUnifo
     }
 }
 
-// True when no pixel kA..kB (steps from leftClamped) of a span can pass a
-// depth test against depths <= curMax -- i.e. every z the per-pixel loop
-// would compute satisfies z - cur >= -0.0001f -- decided without running the
-// loop.  The loop's values are z_k = fl(S_k * rcp(C_k)) with S_k, C_k the
-// sequential float sums S0 + dS + ... and C0 + dC + ...  Against the exact
-// T(k) = S0 + k dS and U(k) = C0 + k dC: each of the k additions errs by at
-// most 2^-24 |S_i| <= 2^-23 max|T| (likewise C), so |S_k - T(k)| <= eS =
-// k 2^-23 AS; with U > 0 on the span, T/U is monotonic, so its minimum is at
-// an end point, and |z_k - T/U| <= (eS + Tmax eC / Umin) / Umin plus two
-// roundings.  Every bound below is taken at least twice as loose as this
-// derivation needs (evaluation errors of the bounds themselves included),
-// and anything non-finite or a U near zero keeps the span.
-__device__ __forceinline__ bool span_occluded(const SpanZ& z, int kA, int kB, float curMax)
-{
-    const float S0 = z.pz, C0 = z.cf2, dS = z.pzStep, dC = z.cf2Step;
-    const float fA = (float)kA, fB = (float)kB;
-    const float TA = S0 + fA * dS, TB = S0 + fB * dS, UA = C0 + fA * dC, UB = C0 + fB * dC;
-    const float evT = 0x1p-21f * (fabsf(S0) + fB * fabsf(dS)), evU = 0x1p-21f * (fabsf(C0) + fB * fabsf(dC));
-    const float AS = fmaxf(fabsf(S0), fabsf(TB)) + evT, AC = fmaxf(fabsf(C0), fabsf(UB)) + evU;
-    const float eS = fB * 0x1p-22f * AS + 1e-37f, eC = fB * 0x1p-22f * AC + 1e-37f;
-    const float Umin = fminf(UA, UB) - evU - eC;
-    if (!(Umin > 1e-30f) || !(Umin < 1e30f)) return false;
-    const float Tmax = fmaxf(fabsf(TA), fabsf(TB)) + evT + eS;
-    // fast quotients (2 ulp for divisors in [2^-126, 2^126]): the bound's slack covers them
-    const float fmin = fminf(__fdividef(TA, UA), __fdividef(TB, UB));
-    const float rU = __fdividef(1.0f, Umin);
-    const float delta = 2.0f * ((eS + evT + Tmax * (eC + evU) * rU) * rU) + (Tmax * rU) * 0x1p-19f;
-    const float lhs = fmin - delta - curMax;
-    const float slack = (fabsf(fmin) + fabsf(curMax) + delta) * 1e-6f;
-    return lhs - slack >= -0.0001f;  // false for NaN
-}
-
-// The next work item of the pass's list (k_bin_bounds): the crowded bins'
-// row slices, then the other bins, then the empty ones; -1 when done.
-__device__ __forceinline__ int next_bin_item(const PassParams& P)
-{
-    int i = atomicAdd(P.slotStatus + kSlotCursor, 1);
-    const int nBins = P.binsX * P.binsY;
-    for (int b = 0; b < kItemBuckets; b++) {
-        const int n = *(volatile const int*)(P.slotStatus + kSlotBucket + b);
-        if (i < n) return P.binItems[bucket_base(b, nBins) + i];
-        i -= n;
-    }
-    return -1;
-}
-
 constexpr int kRasterThreads = 128;  // 4 warps: warp = column quarter, lane = bin row
 constexpr int kChunk = 128;          // triangles per chunk (one per thread)
 constexpr int kSlots = 128;          // (triangle, row) spans per round (one per thread)
@@ -312,16 +250,16 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
         continue;
     }
     // prefetch (record of the first chunk, index of the second), in flight
-    // while the bin's depth is loaded
+    // while the bin's depth is loaded; an item is a triangle (its index) or
+    // a span item (~its index)
     float4 rec[4];
-    int recTid = -1, nextIdx = -1;
-    if (start + tid < end) {
+    bool have = start + tid < end, haveNext = start + kChunk + tid < end;
+    int recTid = 0, nextIdx = 0;
+    if (have) {
         recTid = P.sortedTri[start + tid];
-        const float4* src = (const float4*)(P.tris + recTid);
-#pragma unroll
-        for (int k = 0; k < 4; k++) rec[k] = __ldg(src + k);
+        load_item(P, recTid, rec);
     }
-    if (start + kChunk + tid < end) nextIdx = P.sortedTri[start + kChunk + tid];
+    if (haveNext) nextIdx = P.sortedTri[start + kChunk + tid];
     for (int i = tid; i < kBinH * BW; i += kRasterThreads) {
         int r = i / BW, c = i - r * BW;
         float d = P.depthClearValue;
@@ -361,27 +299,35 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
     for (int chunk = start; chunk < end; chunk += kChunk) {
         // ---- stage the chunk's triangles, count their rows in the bin
         int cnt = 0, r0 = 0;
-        if (recTid >= 0) {
+        if (have) {
             float4* dst = (float4*)(sTri + tid);
+            if (recTid >= 0) {
 #pragma unroll
-            for (int k = 0; k < 4; k++) dst[k] = rec[k];
-            sTid[tid] = recTid;
-            const DrawDesc& dd = P.draws[sTri[tid].draw];
-            int oy = dd.vpY;
-            sOx[tid] = (short)dd.vpX;
-            sOy[tid] = (short)oy;
-            sLw[tid] = (short)dd.vpW;
-            r0 = max((int)sTri[tid].firstRow + oy - y0, rowBeg);
-            int r1 = min((int)sTri[tid].lastRow + oy - y0, rowEnd - 1);
-            if (r0 <= r1) cnt = r1 - r0 + 1;
+                for (int k = 0; k < 4; k++) dst[k] = rec[k];
+                sTid[tid] = recTid;
+                const DrawDesc& dd = P.draws[sTri[tid].draw];
+                int oy = dd.vpY;
+                sOx[tid] = (short)dd.vpX;
+                sOy[tid] = (short)oy;
+                sLw[tid] = (short)dd.vpW;
+                r0 = max((int)sTri[tid].firstRow + oy - y0, rowBeg);
+                int r1 = min((int)sTri[tid].lastRow + oy - y0, rowEnd - 1);
+                if (r0 <= r1) cnt = r1 - r0 + 1;
+            } else {  // a span item: one row, set up already
+                dst[0] = rec[0];
+                dst[1] = rec[1];
+                const SpanItem& si = *(const SpanItem*)(sTri + tid);
+                sTid[tid] = si.tri;
+                sLw[tid] = -1;  // marks the slot as a span item
+                r0 = si.y - y0;
+                if (r0 >= rowBeg && r0 < rowEnd) cnt = 1;
+            }
         }
-        recTid = nextIdx;  // prefetch the next chunk while this one is processed
-        if (recTid >= 0) {
-            const float4* src = (const float4*)(P.tris + recTid);
-#pragma unroll
-            for (int k = 0; k < 4; k++) rec[k] = __ldg(src + k);
-        }
-        nextIdx = (chunk + 2 * kChunk + tid < end) ? P.sortedTri[chunk + 2 * kChunk + tid] : -1;
+        have = haveNext;  // prefetch the next chunk while this one is processed
+        recTid = nextIdx;
+        if (have) load_item(P, recTid, rec);
+        haveNext = chunk + 2 * kChunk + tid < end;
+        if (haveNext) nextIdx = P.sortedTri[chunk + 2 * kChunk + tid];
         int inc = cnt;  // block-wide exclusive scan of the row counts
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -417,21 +363,37 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
                 for (int step = kChunk / 2; step; step >>= 1)
                     if (sBase[j + step] <= g) j += step;
                 const int r = sR0[j] + (g - sBase[j]);
-                const int ox = sOx[j], yl = y0 + r - sOy[j];  // the draw's rasteriser row
-                const TriRaster& t = sTri[j];
-                Span sp;
-                if (span_row(t, yl, sLw[j], sp)) {
-                    int xs = max(sp.leftClamped + ox, x0), xe = min(sp.rightClamped + ox, x0 + cols - 1);
-                    const int sflags = t.edges >> 16;
-                    SpanZ z;
-                    if (xs <= xe) span_z(t, sp, yl, z);
+                // the span's columns in the bin and its interpolation state
+                // at pixel k0: from a span item as set up, or from the
+                // triangle (the row result and span set-up)
+                bool live;
+                int xs, xe, k0, sflags;
+                SpanZ z;
+                if constexpr (FWD == 0) {
+                    if (sLw[j] < 0) {
+                        const SpanItem& si = *(const SpanItem*)(sTri + j);
+                        live = true;
+                        xs = si.xs;
+                        xe = si.xe;
+                        k0 = xs;
+                        sflags = si.flags;
+                        z.cf2 = si.cf2;
+                        z.pz = si.pz;
+                        z.cf2Step = si.cf2Step;
+                        z.pzStep = si.pzStep;
+                    } else {
+                        live = triangle_span(sTri[j], y0 + r - sOy[j], sLw[j], sOx[j], x0, cols, xs, xe, k0, sflags, z);
+                    }
+                } else {
+                    live = triangle_span(sTri[j], y0 + r - sOy[j], sLw[j], sOx[j], x0, cols, xs, xe, k0, sflags, z);
+                }
+                if (live) {
                     // a span that no depth test can pass is dropped here: no
                     // per-pixel z, no walk (counted as tested, as the walk would)
                     if (cull && xs <= xe && (sflags & B_TEST_DEPTH)) {
                         const int qa = (xs - x0) / Q, qb = (xe - x0) / Q;
                         float bound = sQMax[qa][r];
                         for (int q = qa + 1; q <= qb; q++) bound = fmaxf(bound, sQMax[q][r]);
-                        const int k0 = sp.leftClamped + ox;
                         if (span_occluded(z, xs - k0, xe - k0, bound)) {
                             tested += (unsigned long long)(xe - xs + 1);
                             xe = xs - 1;
@@ -439,7 +401,7 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
                     }
                     if (xs <= xe) {
                         float cf2 = z.cf2, pz = z.pz;
-                        for (int x = sp.leftClamped + ox; x < xs; x++) {
+                        for (int x = k0; x < xs; x++) {
                             cf2 = fadd(cf2, z.cf2Step);
                             pz = fadd(pz, z.pzStep);
                         }
@@ -804,11 +766,14 @@ void launch_raster_forward(const PassParams& P, int nBins, cudaStream_t s)
     }
 }
 
+void launch_raster_warp(const PassParams& P, int nBins, cudaStream_t s);  // raster_warp.cu
+
 void launch_raster(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
 {
     int nBins = P.binsX * P.binsY;
     pr->begin(K_RASTER, s);
     if (P.forward) launch_raster_forward(P, nBins, s);
+    else if (P.warpBins && P.binW <= 16) launch_raster_warp(P, nBins, s);
     else switch (P.binW) {
     case 8: launch_raster<8>(P, nBins, s); break;
     case 16: launch_raster<16>(P, nBins, s); break;

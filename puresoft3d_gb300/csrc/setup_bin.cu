@@ -239,7 +239,11 @@ __device__ __forceinline__ int edge_code(int a, int b) { return a | (b << 2); }
 
 constexpr int kSetupThreads = 128;
 
-__device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float* sVary, int& pairs, int4& rect)
+// itemized: the triangle's pairs are span items (one per row span and bin),
+// emitted by emit_span_items after the look-back; otherwise one pair per bin
+// of `rect`.
+__device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float* sVary, int& pairs, int4& rect,
+                                               bool& itemized)
 {
     int lo = 0, hi = P.nDraws - 1;
     while (lo < hi) {
@@ -354,7 +358,7 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float
                 // find them (drawvao.cpp:72-75 skips left == right; the fragment
                 // loop covers [leftClamped, rightClamped]); one with no pixel
                 // reaches no bin, the others only the bins their spans touch
-                int lo = W, hi = -1, yLo = lastRow, yHi = firstRow;
+                int lo = W, hi = -1, yLo = lastRow, yHi = firstRow, items = 0;
 #pragma unroll 1
                 for (int y = firstRow; y <= lastRow; y++) {
                     Span sp;
@@ -363,8 +367,12 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float
                         hi = max(hi, sp.rightClamped);
                         yLo = min(yLo, y);
                         yHi = max(yHi, y);
+                        // span items: one per bin the row's span touches
+                        items += (sp.rightClamped + d.vpX) / P.binW - (sp.leftClamped + d.vpX) / P.binW + 1;
                     }
                 }
+                itemized = P.spanItems && lo <= hi;
+                if (itemized) count = items;
                 colLo = lo;
                 colHi = hi;
                 rowLo = yLo;
@@ -374,7 +382,7 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float
                     tr.lastRow = (short)yHi;
                 }
             }
-            if (colLo <= colHi) {  // bins are in target pixels: offset by the viewport origin
+            if (colLo <= colHi && !itemized) {  // bins are in target pixels: offset by the viewport origin
                 bx0 = (colLo + d.vpX) / P.binW;
                 bx1 = (colHi + d.vpX) / P.binW;
                 by0 = (rowLo + d.vpY) / kBinH;
@@ -386,6 +394,7 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float
     if (count == 0) {
         tr.firstRow = 1;
         tr.lastRow = 0;
+        itemized = false;
     }
     float4* dst = (float4*)(P.tris + t);
     const float4* src = (const float4*)&tr;
@@ -439,6 +448,63 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float
     }
 }
 
+// The span items of an itemized triangle, from pair offset o on, in
+// (row, bin) order: each row's span set-up (interp.cpp:26-80) and, bin by
+// bin, the sequential steps (interp.cpp:82-92) to the span's first pixel in
+// the bin, so that the raster starts there.  The radix digit histograms of
+// the items' bins are counted here too.  Items past the pair capacity are
+// not written (the pass has failed and will be re-run).
+__device__ __forceinline__ void emit_span_items(const PassParams& P, int t, long long o,
+                                                int (*hist)[kRadixDigits])
+{
+    TriRaster tr;
+    {
+        const float4* src = (const float4*)(P.tris + t);
+        float4* d4 = (float4*)&tr;
+#pragma unroll
+        for (int k = 0; k < 4; k++) d4[k] = src[k];
+    }
+    const DrawDesc& d = P.draws[tr.draw];
+    const int W = d.vpW, ox = d.vpX, oy = d.vpY, flags = tr.edges >> 16;
+#pragma unroll 1
+    for (int y = tr.firstRow; y <= tr.lastRow; y++) {
+        Span sp;
+        if (!span_row<true>(tr, y, W, sp) || sp.leftClamped > sp.rightClamped) continue;
+        SpanZ z;
+        span_z(tr, sp, y, z);
+        const int ty = y + oy, by = ty / kBinH;
+        const int xa = sp.leftClamped + ox, xb = sp.rightClamped + ox;
+        float cf2 = z.cf2, pz = z.pz;
+        int x = xa;  // the pixel the state is at
+        for (int bx = xa / P.binW; bx <= xb / P.binW; bx++, o++) {
+            const int a = max(xa, bx * P.binW), b = min(xb, bx * P.binW + P.binW - 1);
+            for (; x < a; x++) {
+                cf2 = fadd(cf2, z.cf2Step);
+                pz = fadd(pz, z.pzStep);
+            }
+            const int key = by * P.binsX + bx;
+            for (int ps = 0; ps < P.radixPasses; ps++) atomicAdd(&hist[ps][(key >> (8 * ps)) & 255], 1);
+            if (o >= P.pairCap) continue;
+            P.pairKey[o] = key;
+            P.pairTri[o] = ~(int)o;
+            SpanItem si;
+            si.cf2 = cf2;
+            si.pz = pz;
+            si.cf2Step = z.cf2Step;
+            si.pzStep = z.pzStep;
+            si.tri = t;
+            si.xs = (short)a;
+            si.xe = (short)b;
+            si.y = ty;
+            si.flags = flags;
+            float4* dst = (float4*)(P.spans + o);
+            const float4* s4 = (const float4*)&si;
+            dst[0] = s4[0];
+            dst[1] = s4[1];
+        }
+    }
+}
+
 // Set-up, pair offsets and pair emission in one kernel.  Block b (numbered
 // by an atomic ticket, so that it only ever waits for blocks already
 // running) sets up triangles [b*128, b*128+128): each thread one triangle
@@ -470,7 +536,8 @@ __global__ void __launch_bounds__(kSetupThreads, 8) k_setup_emit(PassParams P)
     const int first = b * kSetupThreads, t = first + tid;
     int count = 0;
     int4 rect = make_int4(0, -1, 0, -1);
-    if (t < P.nTris) setup_triangle(P, t, sVary, count, rect);
+    bool itemized = false;
+    if (t < P.nTris) setup_triangle(P, t, sVary, count, rect, itemized);
     if (b == 0 && tid == 0) P.slotStatus[kSlotShade] = 0;  // the shade list starts empty
     if (b == 0 && tid < kItemBuckets + 1) P.slotStatus[kSlotBucket + tid] = 0;  // the raster's work list too
 
@@ -566,6 +633,7 @@ __global__ void __launch_bounds__(kSetupThreads, 8) k_setup_emit(PassParams P)
     }
     __syncthreads();
     long long o = (long long)sPrefix + wbase + inc - count;
+    if (itemized) emit_span_items(P, t, o, sHist);
     for (int by = rect.z; by <= rect.w; by++)
         for (int bx = rect.x; bx <= rect.y; bx++, o++) {
             if (o >= P.pairCap) continue;

@@ -67,6 +67,8 @@ _SIGS = {
     "ps3d_set_bin_width": [_c_void_p, _c_int],
     "ps3d_get_bin_width": [_c_void_p, ctypes.POINTER(_c_int)],
     "ps3d_set_raster_occupancy": [_c_void_p, _c_int],
+    "ps3d_set_raster_warp_bins": [_c_void_p, _c_int],
+    "ps3d_set_span_items": [_c_void_p, _c_int],
     "ps3d_selftest_wait": [_c_void_p, _c_int, ctypes.POINTER(ctypes.c_float)],
     "ps3d_read_colour": [_c_void_p, _c_void_p],
     "ps3d_read_depth": [_c_void_p, _c_void_p],
@@ -289,6 +291,16 @@ class PuresoftPipeline:
     def setRowSplit(self, blocks_per_bin: int):
         """Raster blocks per bin (1, 2, 4 or 8): crowded bins shared out by rows."""
         self._check(self.lib.ps3d_set_row_split(self.h, blocks_per_bin))
+
+    def setWarpBins(self, on: bool):
+        """Raster shape: one warp per bin of 8 or 16 columns (on) or four
+        warps sharing each bin (off, the default)."""
+        self._check(self.lib.ps3d_set_raster_warp_bins(self.h, int(bool(on))))
+
+    def setSpanItems(self, on: bool):
+        """Bin short triangles' row spans as set-up items (on) or whole
+        triangles whose spans the raster sets up (off, the default)."""
+        self._check(self.lib.ps3d_set_span_items(self.h, int(bool(on))))
 
     def setSpanCulling(self, on: bool):
         """Raster kernel variant: drop occluded spans before their depths are
