@@ -499,7 +499,7 @@ def run_c5(args):
     return line
 
 
-def cpu_baseline_views(budget_s=15.0, threads=None, sample_views=256):
+def cpu_baseline_views(budget_s=15.0, threads=None, sample_views=256, kind="auto"):
     """Config 4 on the host cores: the reference pipeline (or its oracle
     port) rendering the first views of the same seeded set one at a time in a
     128x128 pipeline."""
@@ -509,7 +509,7 @@ def cpu_baseline_views(budget_s=15.0, threads=None, sample_views=256):
     threads = threads or os.cpu_count() or 1
     _, plain = S.scene_c4(views=sample_views)
     size = plain.info["view_size"]
-    use_ref = os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libps3dref.so")) and os.uname().machine == "x86_64"
+    use_ref = _use_ref(kind)
     if use_ref:
         os.environ["PS3D_REF_THREADS"] = str(threads)
         pipe, kind = RefPipeline(size, size, threads), "reference"
@@ -750,14 +750,23 @@ def shading_error(scene):
             "channels_off_by_1_or_more": e["over_1"]}
 
 
-def cpu_baseline(scene, budget_s=15.0, threads=None):
+def _use_ref(kind):
+    """Whether a CPU timing runs the reference build (kind "reference", or
+    "auto" where it compiled on this host) or the oracle port ("port")."""
+    have = os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libps3dref.so")) and os.uname().machine == "x86_64"
+    if kind == "reference" and not have:
+        raise SystemExit("the reference build is not available on this host")
+    return have if kind == "auto" else kind == "reference"
+
+
+def cpu_baseline(scene, budget_s=15.0, threads=None, kind="auto"):
     """The reference pipeline's CPU path timed on this host's cores: the
     reference build where it compiled here, else the oracle port of it."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from puresoft3d_gb300 import scenes as S
     from cpu_backends import OraclePipeline, RefPipeline
     threads = threads or os.cpu_count() or 1
-    use_ref = os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libps3dref.so")) and os.uname().machine == "x86_64"
+    use_ref = _use_ref(kind)
     if use_ref:
         os.environ["PS3D_REF_THREADS"] = str(threads)
         pipe = RefPipeline(scene.width, scene.height, threads)
@@ -779,7 +788,7 @@ def cpu_baseline(scene, budget_s=15.0, threads=None):
             "sample": "%d frames of the same workload in %.1f s" % (frames, el)}
 
 
-def cpu_baseline_jobs(budget_s=15.0, threads=None, pool=None, jobs=None):
+def cpu_baseline_jobs(budget_s=15.0, threads=None, pool=None, jobs=None, kind="auto"):
     """Config 5 on the host cores: the reference pipeline (or its oracle
     port) rendering the seeded jobs one at a time, one pipeline per
     resolution, for a bounded time."""
@@ -789,7 +798,7 @@ def cpu_baseline_jobs(budget_s=15.0, threads=None, pool=None, jobs=None):
     threads = threads or os.cpu_count() or 1
     pool = pool or S.scene_c5_pool()
     jobs = jobs or S.c5_jobs(pool, n=2000, rate=1.0)
-    use_ref = os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libps3dref.so")) and os.uname().machine == "x86_64"
+    use_ref = _use_ref(kind)
     if use_ref:
         os.environ["PS3D_REF_THREADS"] = str(threads)
     pipes = {}
@@ -810,11 +819,40 @@ def cpu_baseline_jobs(budget_s=15.0, threads=None, pool=None, jobs=None):
     for p in pipes.values():
         p.close()
     return {"value": round(n / el, 3), "unit": "images/s", "cores": threads,
-            "kind": "reference" if use_ref else "port",
+            "kind": "reference" if use_ref else "port", "jobs_done": n,
             "sample": "the first %d jobs of the seeded stream, one at a time, in %.1f s" % (n, el)}
 
 
+def run_calibration(args):
+    """The reference build against the oracle port on this host, same
+    workload, same thread count: how fast the port (the CPU arm on hosts
+    where the reference does not build) runs relative to the reference's own
+    code.  x86-64 hosts with the reference build only."""
+    threads = args.cpu_threads or os.cpu_count() or 1
+    out = {"impl": "reference", "calibration": True, "config": {"workload": CONFIGS[args.config]["desc"]},
+           "threads": threads, "host": os.uname().machine}
+    jobs = None
+    for kind in ("reference", "port"):
+        if args.config == "c4":
+            v = cpu_baseline_views(budget_s=args.cpu_budget, threads=threads, kind=kind)
+        elif args.config == "c5":
+            # the port renders exactly the jobs the reference finished in its budget
+            from puresoft3d_gb300 import scenes as S
+            pool = S.scene_c5_pool()
+            jobs = jobs or S.c5_jobs(pool, n=2000, rate=1.0)
+            v = cpu_baseline_jobs(budget_s=args.cpu_budget if kind == "reference" else 1e9, threads=threads,
+                                  pool=pool, jobs=jobs, kind=kind)
+            jobs = jobs[:v["jobs_done"]]
+        else:
+            v = cpu_baseline(make_scene(args.config), budget_s=args.cpu_budget, threads=threads, kind=kind)
+        out[kind] = v
+    out["port_over_reference"] = round(out["port"]["value"] / out["reference"]["value"], 3)
+    return out
+
+
 def run_reference(args):
+    if args.calibrate:
+        return run_calibration(args)
     if args.config == "c4":
         return run_reference_views(args)
     if args.config == "c5":
@@ -906,6 +944,9 @@ def main():
     ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--cpu-threads", type=int, default=0, help="CPU timings: threads (default: every host core)")
+    ap.add_argument("--calibrate", action="store_true",
+                    help="with --impl reference: time the reference build and the oracle port side by side")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ncu-frames", type=int, default=0, help="render N frames for a profiler and exit")
     ap.add_argument("--views", type=int, default=4096, help="config 4: number of views")

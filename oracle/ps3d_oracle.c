@@ -14,6 +14,14 @@
  * (oracle/_ref, tests/golden).  Citations are file:line in
  * src/puresoft3d/ or src/mcemath/ of the reference.
  *
+ * The reference's shaders normalise and divide with the x86 approximate
+ * reciprocal and reciprocal square root (rcpps / rsqrtss, vector.cpp:158-169
+ * mcemaths_div_3_4, :225-250 mcemaths_norm_3_4), whose results depend on the
+ * host.  Here they are the table restatement of the instructions of the host
+ * the golden fixtures were made on (x86_approx.h, generated from and checked
+ * against the instructions on all 2^32 inputs), so that the colour matches
+ * the reference build bit for bit on every host.
+ *
  * Threads: the reference hands row y to fragment thread y % (N-1)
  * (drawvao.cpp:77-83); each thread walks its rows' spans in submission order.
  * Results depend only on that per-row order, so here each draw first builds
@@ -24,10 +32,6 @@
  *  - TEST_DEPTH without UPDATE_DEPTH: the reference never positions the depth
  *    cursor in that mode (fragthrd.cpp:184-203) and reads a stale pixel; here
  *    the pixel under the fragment is read.
- *  - FragmentProcessorDEF01 uses rcpps/rsqrtss (vector.cpp:158-169,
- *    225-250), whose results depend on the x86 model; here 1/x and 1/sqrt(x)
- *    are IEEE.  Colour of DEF01 may differ by a few LSB; depth and coverage
- *    are unaffected.
  *  - Triangles with non-finite vertex coordinates make the reference index
  *    its row table out of range (rasterizer.cpp:93-118); here they draw nothing.
  */
@@ -38,6 +42,30 @@
 #include <stdlib.h>
 #include <string.h>
 #include "ps3d_oracle.h"
+#include "x86_approx.h"
+
+/* rcpps / rsqrtss of one lane on the reference's host (x86_approx.h). */
+static float x86_rcp(float x)
+{
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    u = x86a_rcp_bits(u);
+    memcpy(&x, &u, 4);
+    return x;
+}
+
+static float x86_rsqrt(float x)
+{
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    u = x86a_rsqrt_bits(u);
+    memcpy(&x, &u, 4);
+    return x;
+}
+
+/* mcemaths_norm_3_4's scale (vector.cpp:225-250): rsqrtss of the haddps sum
+   of the squares. */
+static float norm_scale(const float* v) { return x86_rsqrt((v[0] * v[0] + v[1] * v[1]) + (v[2] * v[2] + v[3] * v[3])); }
 #include "shade_ref.h"
 
 #define MAX_VBOS 16      /* config.h:4 */
@@ -573,7 +601,7 @@ static void run_vp(const ps3do* p, const void* const* in, float* pos, float* use
         d[1] = v[1] - 0.0f;
         d[2] = v[2] - 1.0f;
         d[3] = 0.0f;
-        r = 1.0f / sqrtf((d[0] * d[0] + d[1] * d[1]) + (d[2] * d[2] + d[3] * d[3]));
+        r = norm_scale(d);
         for (int k = 0; k < 4; k++) d[k] = d[k] * r;
         for (int c = 0; c < 4; c++)
             for (int rr = 0; rr < 4; rr++) inv[4 * c + rr] = ufl(p, 1)[4 * rr + c];
@@ -931,20 +959,20 @@ static void sample_nearest(const o_fbo* t, const float* tc, float c[4])
 
 /* The lighting shared by DEF01 and DEF03 (tex1light1.cpp:165-192,
    tex1bump1light1.cpp:212-237) on colour c (BGRA floats), normal n and
-   world position wp (all four lanes, as the 4-wide mcemaths ops use them),
-   with IEEE 1/x and 1/sqrt in place of rcpps / rsqrtss (see the header). */
+   world position wp (all four lanes, as the 4-wide mcemaths ops use them):
+   L divided by its length with rcpps, E and H normalised with rsqrtss. */
 static void def_lighting(const fp_state* s, float c[4], const float* nrm, const float* wp, uint8_t* bgra)
 {
     float L[4], E[4], Hv[4], dist, lambert, spec, r;
     for (int k = 0; k < 4; k++) L[k] = s->light[k] - wp[k];
     dist = sqrtf((L[0] * L[0] + L[1] * L[1]) + (L[2] * L[2] + L[3] * L[3]));
-    r = 1.0f / dist;
+    r = x86_rcp(dist);
     for (int k = 0; k < 4; k++) L[k] = L[k] * r;
     for (int k = 0; k < 4; k++) E[k] = s->cam[k] - wp[k];
-    r = 1.0f / sqrtf((E[0] * E[0] + E[1] * E[1]) + (E[2] * E[2] + E[3] * E[3]));
+    r = norm_scale(E);
     for (int k = 0; k < 4; k++) E[k] = E[k] * r;
     for (int k = 0; k < 4; k++) Hv[k] = E[k] + L[k];
-    r = 1.0f / sqrtf((Hv[0] * Hv[0] + Hv[1] * Hv[1]) + (Hv[2] * Hv[2] + Hv[3] * Hv[3]));
+    r = norm_scale(Hv);
     for (int k = 0; k < 4; k++) Hv[k] = Hv[k] * r;
     lambert = (L[0] * nrm[0] + L[1] * nrm[1]) + (L[2] * nrm[2] + L[3] * nrm[3]);
     spec = (Hv[0] * nrm[0] + Hv[1] * nrm[1]) + (Hv[2] * nrm[2] + Hv[3] * nrm[3]);
@@ -1038,15 +1066,15 @@ static void sample_cube(const o_fbo* t, const float* d, uint8_t* bgra)
 }
 
 /* PuresoftSamplerProjection::get (samplrproj.cpp:20-38): the projected
-   coordinate divided by its w (mcemaths_div_3_4: times 1/w, IEEE here in
-   place of rcpps), then four Poisson taps -- row from t plus the disk's x,
+   coordinate divided by its w (mcemaths_div_3_4: times rcpps(w)), then four
+   Poisson taps -- row from t plus the disk's x,
    column from s plus the disk's y, each / 500 -- each lowering the factor
    by 0.2 when the stored depth is below the coordinate's z. */
 static float sample_proj(const o_fbo* t, const float* proj)
 {
     static const float PX[4] = {-0.94201624f, 0.94558609f, -0.094184101f, 0.34495938f};
     static const float PY[4] = {-0.39906216f, -0.76890725f, -0.92938870f, 0.29387760f};
-    float tc[4], r = 1.0f / proj[3], factor = 1.0f;
+    float tc[4], r = x86_rcp(proj[3]), factor = 1.0f;
     for (int k = 0; k < 4; k++) tc[k] = proj[k] * r;
     for (int i = 0; i < 4; i++) {
         int y = (int)sr_f2u((float)t->height * (tc[1] + PX[i] / 500.0f));
@@ -1069,8 +1097,7 @@ static float sample_proj(const o_fbo* t, const float* proj)
    299-363 FP_Satellite): DEF03's bump-mapped normal and lighting, the
    specular term scaled by the specular map's red / 255 (Earth), the night
    texel added where lambert < 0.2 (Earth), then the colour times the
-   projective shadow factor; IEEE 1/x and 1/sqrt in place of rcpps /
-   rsqrtss. */
+   projective shadow factor. */
 static void fp_planet(const ps3do* p, const fp_state* s, const float* in, uint8_t* bgra)
 {
     const float* tan = in, * bin = in + 4, * nrm = in + 8, * wp = in + 12, * tc = in + 16, * sc = in + 20;
@@ -1090,7 +1117,7 @@ static void fp_planet(const ps3do* p, const fp_state* s, const float* in, uint8_
         sample_nearest(s->spec, tc, st);
         control = st[2] / 255.0f;
     }
-    r = 1.0f / 255.0f;
+    r = x86_rcp(255.0f);  /* mcemaths_div_3_4(bumpNormal, 255.0f) */
     for (int k = 0; k < 4; k++) bn[k] = bn[k] * r;
     for (int k = 0; k < 4; k++) bn[k] = bn[k] * 2.0f;
     for (int k = 0; k < 4; k++) bn[k] = bn[k] - 1.0f;
@@ -1099,17 +1126,17 @@ static void fp_planet(const ps3do* p, const fp_state* s, const float* in, uint8_
     memcpy(tbn + 8, nrm, 16);
     memset(tbn + 12, 0, 16);
     m4v4(bn, tbn, bn);
-    r = 1.0f / sqrtf((bn[0] * bn[0] + bn[1] * bn[1]) + (bn[2] * bn[2] + bn[3] * bn[3]));
+    r = norm_scale(bn);
     for (int k = 0; k < 4; k++) bn[k] = bn[k] * r;
     for (int k = 0; k < 4; k++) L[k] = s->light[k] - wp[k];
     dist = sqrtf((L[0] * L[0] + L[1] * L[1]) + (L[2] * L[2] + L[3] * L[3]));
-    r = 1.0f / dist;
+    r = x86_rcp(dist);
     for (int k = 0; k < 4; k++) L[k] = L[k] * r;
     for (int k = 0; k < 4; k++) E[k] = s->cam[k] - wp[k];
-    r = 1.0f / sqrtf((E[0] * E[0] + E[1] * E[1]) + (E[2] * E[2] + E[3] * E[3]));
+    r = norm_scale(E);
     for (int k = 0; k < 4; k++) E[k] = E[k] * r;
     for (int k = 0; k < 4; k++) Hv[k] = E[k] + L[k];
-    r = 1.0f / sqrtf((Hv[0] * Hv[0] + Hv[1] * Hv[1]) + (Hv[2] * Hv[2] + Hv[3] * Hv[3]));
+    r = norm_scale(Hv);
     for (int k = 0; k < 4; k++) Hv[k] = Hv[k] * r;
     lambert = (L[0] * bn[0] + L[1] * bn[1]) + (L[2] * bn[2] + L[3] * bn[3]);
     spec = (Hv[0] * bn[0] + Hv[1] * bn[1]) + (Hv[2] * bn[2] + Hv[3] * bn[3]);
@@ -1176,7 +1203,7 @@ static void fp_cloud(const fp_state* s, const float* in, uint8_t* bgra)
     f = sample_proj(s->proj, sc);
     for (int k = 0; k < 4; k++) L[k] = s->light[k] - wp[k];
     dist = sqrtf((L[0] * L[0] + L[1] * L[1]) + (L[2] * L[2] + L[3] * L[3]));
-    r = 1.0f / dist;
+    r = x86_rcp(dist);
     for (int k = 0; k < 4; k++) L[k] = L[k] * r;
     /* E and H are computed by the reference but unused */
     lambert = 2.0f * ((L[0] * nrm[0] + L[1] * nrm[1]) + (L[2] * nrm[2] + L[3] * nrm[3]));
@@ -1188,11 +1215,10 @@ static void fp_cloud(const fp_state* s, const float* in, uint8_t* bgra)
 }
 
 /* The scene viewer's spotlight terms (test2/testproc.cpp:220-238 and
-   470-488): L, E, H normalised (IEEE 1/sqrt in place of rsqrtss), lambert =
+   470-488): L, E, H normalised (rsqrtss), lambert =
    L.n scaled outside the 25-degree cone by cos(yaw - cone)^150, specular =
    (H.n)^exponent (no clamp before the power), both clamped to [0, 1] by
    clamp_3_4 (NaN -> 0).  f[0] lambert, f[1] specular. */
-static float norm_rcp(const float* v) { return 1.0f / sqrtf((v[0] * v[0] + v[1] * v[1]) + (v[2] * v[2] + v[3] * v[3])); }
 
 static float opt_powf(float x, unsigned n) /* proc.h:73-86 */
 {
@@ -1216,13 +1242,13 @@ static void spot_factors(const fp_state* s, const float* nrm, const float* wp, f
     const float fieldOfLight = 6.283185f * (25.0f / 360.0f); /* test2/testproc.cpp:9 */
     float L[4], E[4], Hv[4], r, yaw;
     for (int k = 0; k < 4; k++) L[k] = s->light[k] - wp[k];
-    r = norm_rcp(L);
+    r = norm_scale(L);
     for (int k = 0; k < 4; k++) L[k] = L[k] * r;
     for (int k = 0; k < 4; k++) E[k] = s->cam[k] - wp[k];
-    r = norm_rcp(E);
+    r = norm_scale(E);
     for (int k = 0; k < 4; k++) E[k] = E[k] * r;
     for (int k = 0; k < 4; k++) Hv[k] = E[k] + L[k];
-    r = norm_rcp(Hv);
+    r = norm_scale(Hv);
     for (int k = 0; k < 4; k++) Hv[k] = Hv[k] * r;
     f[0] = (L[0] * nrm[0] + L[1] * nrm[1]) + (L[2] * nrm[2] + L[3] * nrm[3]);
     yaw = acosf((L[0] * s->ldir[0] + L[1] * s->ldir[1]) + (L[2] * s->ldir[2] + L[3] * s->ldir[3]));
@@ -1288,7 +1314,7 @@ static void fp_def03(const fp_state* s, const float* in, uint8_t* bgra)
     bn[1] = bt[1];
     bn[2] = bt[0];
     bn[3] = 0.0f;
-    r = 1.0f / 255.0f;
+    r = x86_rcp(255.0f);  /* mcemaths_div_3_4(bumpNormal, 255.0f) */
     for (int k = 0; k < 4; k++) bn[k] = bn[k] * r;
     for (int k = 0; k < 4; k++) bn[k] = bn[k] * 2.0f;
     for (int k = 0; k < 4; k++) bn[k] = bn[k] - 1.0f;
@@ -1297,7 +1323,7 @@ static void fp_def03(const fp_state* s, const float* in, uint8_t* bgra)
     memcpy(tbn + 8, nrm, 16);
     memset(tbn + 12, 0, 16);
     m4v4(bn, tbn, bn);
-    r = 1.0f / sqrtf((bn[0] * bn[0] + bn[1] * bn[1]) + (bn[2] * bn[2] + bn[3] * bn[3]));
+    r = norm_scale(bn);
     for (int k = 0; k < 4; k++) bn[k] = bn[k] * r;
     def_lighting(s, c, bn, wp, bgra);
 }

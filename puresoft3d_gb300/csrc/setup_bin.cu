@@ -114,8 +114,7 @@ __device__ __forceinline__ void vp_varyings(const DrawDesc& d, const DrawUniform
     case VP_DEF04: {  // skybox.cpp:23-44: the direction is Vrot times the
                       // normalised vector from the observer (0, 0, 1) to the vertex
         float v[4] = {fsub(p[0], 0.0f), fsub(p[1], 0.0f), fsub(p[2], 1.0f), 0.0f}, dir[4];
-        float r = fdiv(1.0f, fsqrt(fadd(fadd(fmul(v[0], v[0]), fmul(v[1], v[1])),
-                                       fadd(fmul(v[2], v[2]), fmul(v[3], v[3])))));
+        float r = norm_scale(v);  // mcemaths_norm_3_4: rsqrtss
 #pragma unroll
         for (int k = 0; k < 4; k++) v[k] = fmul(v[k], r);
         m4v4(dir, U.Vrot, v);

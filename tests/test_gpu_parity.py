@@ -29,6 +29,11 @@ def test_gpu_matches_oracle(name, scene, gpu_lib):
     assert sha(gpu["depth"]) == str(g["depth_sha"]), name
     if "shadow_sha" in g:
         assert sha(gpu["shadow"]) == str(g["shadow_sha"]), name
+    # colour is the reference build's bit for bit (the rcpps / rsqrtss
+    # tables included), except that the scene viewer's spotlight uses the
+    # device's acosf / cosf where the reference build has glibc's
+    if "viewer" not in name:
+        assert sha(gpu["colour"]) == str(g["colour_sha"]), name + ": colour differs from the reference build"
 
 
 @pytest.mark.gpu
