@@ -2,8 +2,11 @@
 
 Default workload: config 2 -- 1920x1080 Blinn-Phong pass with trilinear
 albedo, tangent-space normal map and 3x3 PCF, preceded by a 2048^2 FP32
-shadow pass, 64 seeded meshes (~200k triangles).  One step renders one frame
-(both passes).
+shadow pass, 64 seeded meshes (~200k triangles).  One step renders a fixed
+batch of K frames (both passes each; K per workload in FRAMES_PER_STEP, 50 at
+config 2, stated in config.frames_per_step), every frame timed alone after an
+L2 scrub; the workload's schedule is the one pinned for it
+(puresoft3d_gb300.autotune.PINNED) unless --autotune or --bin-width is given.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--config c1|c2|c3]
                   [--impl ours|reference]
@@ -202,6 +205,15 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.samples), "source": "nvml" if self.nvml else "nvidia-smi"}
 
 
+# Frames per timed step, per workload: enough that the timed region (and the
+# clock samples taken during it) lasts a few hundred milliseconds.
+FRAMES_PER_STEP = {"c1": 200, "c2": 50, "c3": 10, "c3s": 20, "c4": 4}
+
+
+def frames_per_step(args):
+    return args.frames_per_step or FRAMES_PER_STEP.get(args.config, 1)
+
+
 def make_scene(cfg, views=4096):
     from puresoft3d_gb300 import scenes as S
     if cfg == "c4":
@@ -331,10 +343,11 @@ def run_c4(args):
     for _ in range(max(3, args.warmup)):
         cb.submit()
     pipe.finish()
+    K = frames_per_step(args)
     clocks = ClockSampler()
     clocks.start()
     frame_ms = []
-    for _ in range(args.steps):
+    for _ in range(args.steps * K):  # a step is K atlas passes, each timed alone after an L2 scrub
         pipe.scrubL2()
         pipe.timerBegin()
         cb.submit()
@@ -342,7 +355,7 @@ def run_c4(args):
     pipe.finish()
     clk = clocks.stop()
     total_ms = allreduce_max(sum(frame_ms))
-    ips = aggregate(views * args.steps, total_ms / 1e3)
+    ips = aggregate(views * args.steps * K, total_ms / 1e3)
 
     host = torch.empty((batched.height, batched.width, 4), dtype=torch.uint8, pin_memory=True).numpy()
     for _ in range(2):
@@ -411,6 +424,7 @@ def run_c4(args):
         "data": "synthetic (seeded meshes, cameras and textures per view)",
         "config": {"workload": CONFIGS["c4"]["desc"], "views": views, "view_size": size,
                    "atlas": [batched.width, batched.height], "triangles": batched.triangles(),
+                   "frames_per_step": K,
                    "l2": "256 MB scrub before each timed step",
                    "parallelism": "replicas" if WORLD > 1 else "single GPU", "schedule": tune},
         "plain_images_per_s": {"immediate": round(plain_ips, 2), "graph": round(plain_graph_ips, 2),
@@ -419,7 +433,7 @@ def run_c4(args):
                                "graph": round(ips / WORLD / plain_graph_ips, 2)},
         "gfrag_per_s": round(frags * ips / views / 1e9, 4),
         "fragments_per_step": frags,
-        "gpu_launches": launches_per_frame * args.steps,
+        "gpu_launches": launches_per_frame * args.steps * K,
         "e2e": {"value": round(WORLD * views * e2e_steps / e2e_s, 2), "unit": "images/s",
                 "mode": "steps back to back on two pipelines (double-buffered): each uploads its inputs and "
                         "copies its atlas to pinned host memory",
@@ -665,11 +679,12 @@ def run_ours(args):
         cb.submit()
     pipe.finish()
 
+    K = frames_per_step(args)
     barrier()
     clocks = ClockSampler()
     clocks.start()
     frame_ms = []
-    for _ in range(args.steps):
+    for _ in range(args.steps * K):  # a step is K frames, each timed alone after an L2 scrub
         pipe.scrubL2()
         pipe.timerBegin()
         cb.submit()
@@ -688,7 +703,7 @@ def run_ours(args):
         cb.submit(upload_inputs=True)
         pipe.readColour(host)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(args.steps * K):
         pipe.scrubL2()
         cb.submit(upload_inputs=True)
         pipe.readColour(host)
@@ -699,11 +714,11 @@ def run_ours(args):
         host2 = torch.empty((scene.height, scene.width, 4), dtype=torch.uint8, pin_memory=True).numpy()
     except Exception:
         host2 = np.empty((scene.height, scene.width, 4), dtype=np.uint8)
-    e2e_s = e2e_pipelined([pipe, pipe2], lambda p: S.replay_frame(scene, p), [host, host2], args.steps)
+    e2e_s = e2e_pipelined([pipe, pipe2], lambda p: S.replay_frame(scene, p), [host, host2], args.steps * K)
     pipe2.close()
 
-    fps = aggregate(args.steps, total_ms / 1e3)
-    fps_e2e = aggregate(args.steps, e2e_s)
+    fps = aggregate(args.steps * K, total_ms / 1e3)
+    fps_e2e = aggregate(args.steps * K, e2e_s)
     roof = dominant_roofline(prof, prof_frames, scene, counts, tune["bin_width"], RASTER_TRAFFIC.get(args.config))
     line = {
         "metric": "frames/s", "value": round(fps, 3), "unit": "frames/s", "n_gpus": WORLD,
@@ -711,16 +726,17 @@ def run_ours(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded meshes and procedural textures)",
         "config": {"workload": CONFIGS[args.config]["desc"], "width": scene.width, "height": scene.height,
-                   "triangles": scene.triangles(), "l2": "256 MB scrub before each timed frame",
+                   "triangles": scene.triangles(), "frames_per_step": K,
+                   "l2": "256 MB scrub before each timed frame",
                    "parallelism": "replicas" if WORLD > 1 else "single GPU", "schedule": tune},
         "gfrag_per_s": round(frags * fps / WORLD / 1e9 * WORLD, 4),
         "fragments_per_frame": frags,
-        "gpu_launches": launches_per_frame * args.steps,
-        "e2e": {"value": round(fps_e2e, 3), "unit": "frames/s", "h2d_bytes_per_step": cb.input_bytes(),
-                "d2h_bytes_per_step": scene.width * scene.height * 4,
+        "gpu_launches": launches_per_frame * args.steps * K,
+        "e2e": {"value": round(fps_e2e, 3), "unit": "frames/s", "h2d_bytes_per_step": cb.input_bytes() * K,
+                "d2h_bytes_per_step": scene.width * scene.height * 4 * K,
                 "mode": "steps back to back on two pipelines (double-buffered): each uploads its inputs and "
                         "copies its frame to pinned host memory",
-                "one_at_a_time": round(aggregate(args.steps, e2e_sync_s), 3)},
+                "one_at_a_time": round(aggregate(args.steps * K, e2e_sync_s), 3)},
         "roofline": roof,
         "kernel_ms_per_frame": {k: round(prof[k][1] / prof_frames, 5) for k in KERNELS if prof[k][0]},
         "clocks": clk,
@@ -876,10 +892,12 @@ def run_reference(args):
         frames += int(cb["sample"].split()[0])
     el = time.perf_counter() - t0
     v = statistics.median(vals)
+    K = frames_per_step(args)
     return {"impl": "reference", "metric": "frames/s", "value": v, "unit": "frames/s", "n_gpus": WORLD,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 / v, 3), "higher_is_better": True,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * K / v, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": CONFIGS[args.config]["desc"]},
+            "config": {"workload": CONFIGS[args.config]["desc"], "frames_per_step": K,
+                       "note": "each step a bounded sample of the workload on the host cores"},
             "cpu_baseline": {"value": v, "unit": "frames/s", "cores": cb["cores"], "kind": cb["kind"],
                              "sample": "%d steps, %d frames in %.1f s" % (args.steps, frames, el)},
             "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -896,10 +914,11 @@ def run_reference_views(args):
         n_total += int(cb["sample"].split()[0])
     el = time.perf_counter() - t0
     v = statistics.median(vals)
+    K = frames_per_step(args)
     return {"impl": "reference", "metric": "images/s", "value": v, "unit": "images/s", "n_gpus": WORLD,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 / v, 3), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": CONFIGS["c4"]["desc"]},
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * 4096 * K / v, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": CONFIGS["c4"]["desc"], "frames_per_step": K},
             "cpu_baseline": {"value": v, "unit": "images/s", "cores": cb["cores"], "kind": cb["kind"],
                              "sample": "%d steps, %d views in %.1f s" % (args.steps, n_total, el)},
             "e2e": {"value": v, "unit": "images/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -945,6 +964,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--cpu-threads", type=int, default=0, help="CPU timings: threads (default: every host core)")
+    ap.add_argument("--frames-per-step", type=int, default=0,
+                    help="frames (c4: atlas passes) per timed step (default: per workload, FRAMES_PER_STEP)")
     ap.add_argument("--calibrate", action="store_true",
                     help="with --impl reference: time the reference build and the oracle port side by side")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -591,7 +591,7 @@ int ensure_scratch(ps3d_pipeline* p, Scratch& x, int nTris, int nvMax, int W, in
               dev_alloc(x.pairKey, x.pairKeyCap, p->pairCap) && dev_alloc(x.pairTri, x.pairTriCap, p->pairCap) &&
               dev_alloc(x.keyB, x.keyBCap, p->pairCap) && dev_alloc(x.binTri, x.binTriCap, p->pairCap) &&
               dev_alloc(x.radix, x.radixCap, radix_scratch_ints(sortBlocks, radix_passes((int)nBins), nTris)) &&
-              dev_alloc(x.binStart, x.binStartCap, nBins + 1 + (size_t)kItemsPerBin * nBins);
+              dev_alloc(x.binStart, x.binStartCap, (2 + (size_t)kItemsPerBin) * nBins);
     if (ok && colour) ok = dev_alloc(x.shadeList, x.shadeListCap, (size_t)W * H);
     if (ok && spanItems) ok = dev_alloc(x.spans, x.spansCap, p->pairCap);
     if (!ok) return fail(PS3D_ERR_NOMEM, "device scratch allocation failed");
@@ -894,7 +894,7 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     P.sortDescOff = sort_desc_offset(nTris);
     P.keyB = x.keyB;
     P.binStart = x.binStart;
-    P.binItems = x.binStart + (size_t)binsX * binsY + 1;
+    P.binItems = x.binStart + 2 * (size_t)binsX * binsY;
     P.binTri = x.binTri;
     P.sortedTri = (P.radixPasses & 1) ? x.binTri : x.pairTri;
     P.status = p->status;
@@ -2171,7 +2171,7 @@ size_t noalloc_layout(NoAllocLayout& L, int nd, int nTris, int nv, int W, int H,
     L.tris = take((size_t)nTris * sizeof(TriRaster));
     L.vary = take((size_t)nTris * 3 * std::max(nv, 1) * sizeof(float));
     L.shadeList = colour ? take((size_t)W * H * sizeof(int2)) : 0;
-    L.binStart = take((nBins + 1 + (size_t)kItemsPerBin * nBins) * sizeof(int));
+    L.binStart = take((2 + (size_t)kItemsPerBin) * nBins * sizeof(int));
     L.radix = take(radix_scratch_ints((int)sortBlocks, radix_passes((int)nBins), nTris) * sizeof(int));
     L.pairKey = take((size_t)pairCap * sizeof(int));
     L.pairTri = take((size_t)pairCap * sizeof(int));
@@ -2309,7 +2309,7 @@ int noalloc_run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const P
     P.sortDescOff = sort_desc_offset(s.nTris);
     P.keyB = (int*)(base + L.keyB);
     P.binStart = (int*)(base + L.binStart);
-    P.binItems = P.binStart + s.nBins + 1;
+    P.binItems = P.binStart + 2 * s.nBins;
     P.binTri = (int*)(base + L.binTri);
     P.sortedTri = (P.radixPasses & 1) ? P.binTri : P.pairTri;
     P.status = p->status;

@@ -147,7 +147,7 @@ struct PassParams {
                               // [pass][tile][256]; zeroed before each pass
     int sortDescOff;
     int* keyB;                // the sort's second key buffer
-    int* binStart;            // first position of each bin's list; [nBins] = total
+    int* binStart;            // per bin (start, end) of its list in the sorted pairs (int2; empty: start >= end)
     int* binItems;            // the raster's work list (kItemsPerBin x nBins ints)
     int* binTri;              // the sort's second triangle buffer
     const int* sortedTri;     // triangles of each bin, in submission order (binTri or pairTri)
@@ -186,6 +186,13 @@ __host__ __device__ constexpr long long bucket_base(int b, int nBins)
     return b == 0 ? 0 : b == 1 ? 8LL * nBins : b == 2 ? 12LL * nBins : b == 3 ? 14LL * nBins : 15LL * nBins;
 }
 constexpr int kItemsPerBin = 16;
+
+// Whether a pass's raster takes its bins from the work list (row slices, or
+// one warp per bin) rather than one block per bin.
+__host__ __device__ inline bool raster_uses_items(const PassParams& P)
+{
+    return P.rowSplit > 1 || (P.warpBins && !P.forward && P.binW <= 16);
+}
 
 // A pass's kernels do nothing once this pass or an earlier one has failed;
 // the host then re-runs the commands from the first failed pass.  Passes run

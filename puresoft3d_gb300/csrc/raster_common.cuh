@@ -11,8 +11,9 @@ __device__ __forceinline__ void bin_range(const PassParams& P, int bin, int& sta
         start = end = 0;
         return;
     }
-    start = P.binStart[bin];
-    end = P.binStart[bin + 1];
+    const int2 r = ((const int2*)P.binStart)[bin];  // (start, end) in the sorted list; start >= end: empty
+    start = r.x < r.y ? r.x : 0;
+    end = r.x < r.y ? r.y : 0;
 }
 
 // The pass's clear colour at target pixel (x, y) (colour rows top-down).

@@ -539,6 +539,11 @@ __global__ void __launch_bounds__(kSetupThreads, 8) k_setup_emit(PassParams P)
     if (t < P.nTris) setup_triangle(P, t, sVary, count, rect, itemized);
     if (b == 0 && tid == 0) P.slotStatus[kSlotShade] = 0;  // the shade list starts empty
     if (b == 0 && tid < kItemBuckets + 1) P.slotStatus[kSlotBucket + tid] = 0;  // the raster's work list too
+    if (P.radixPasses > 0) {  // every bin's (start, end) starts empty: the last radix pass fills them in
+        const int nBins = P.binsX * P.binsY;
+        for (int i = blockIdx.x * kSetupThreads + tid; i < nBins; i += gridDim.x * kSetupThreads)
+            ((int2*)P.binStart)[i] = make_int2(INT_MAX, 0);
+    }
 
     // block scan of the pair counts
     int inc = count;
@@ -626,6 +631,8 @@ __global__ void __launch_bounds__(kSetupThreads, 8) k_setup_emit(PassParams P)
                     P.slotStatus[kSlotTotal] = (int)total;
                     P.slotStatus[kSlotTiles] = (int)((total + kSortChunk - 1) / kSortChunk);
                     atomicAdd((unsigned long long*)(P.status + 8), (unsigned long long)total);
+                    // one bin, no radix pass: its list is the pairs in emission order
+                    if (P.radixPasses == 0) ((int2*)P.binStart)[0] = make_int2(0, (int)total);
                 }
             }
         }
@@ -724,10 +731,31 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(PassParams P, int pas
     } else {
         *mine = kFlagCount | (unsigned)count;
         int j = tile - 1, spins = 0;
-        while (true) {
-            unsigned v = *(volatile unsigned*)(desc + (size_t)j * kRadixDigits + d);
-            unsigned f = v & ~kValueMask;
-            if (f == 0u) {
+        while (j >= 0) {
+            // four predecessors' descriptors per round trip, nearest first:
+            // counts are added until an inclusive prefix ends the walk; a
+            // descriptor not yet published is waited for (bounded)
+            unsigned v[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                v[k] = j - k >= 0 ? *(volatile unsigned*)(desc + (size_t)(j - k) * kRadixDigits + d) : (unsigned)kFlagPrefix;
+            int k = 0;
+            bool stop = false, wait = false;
+            for (; k < 4; k++) {
+                const unsigned f = v[k] & ~kValueMask;
+                if (f == 0u) {
+                    wait = true;
+                    break;
+                }
+                prefix += (int)(v[k] & kValueMask);
+                if (f == kFlagPrefix) {
+                    stop = true;
+                    break;
+                }
+            }
+            if (stop) break;
+            j -= k;  // the counts taken
+            if (wait) {
                 if (++spins > kLookbackSpins) {
                     atomicMin(P.status + kFirstFailed, P.passSeq);
                     atomicOr(P.status, 2);
@@ -735,11 +763,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(PassParams P, int pas
                     break;
                 }
                 __nanosleep(32);
-                continue;
             }
-            prefix += (int)(v & kValueMask);
-            if (f == kFlagPrefix) break;
-            j--;
         }
         *mine = kFlagPrefix | (unsigned)(prefix + count);
     }
@@ -758,53 +782,46 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(PassParams P, int pas
     sBase[d] = wsum + inc - g + prefix;
     __threadfence();
     __syncthreads();
-    if (pass_failed(P.status, P.passSeq)) return;  // a wait expired: prefixes may be wrong
+    // a wait expired: prefixes may be wrong (one read per warp, so that the
+    // whole warp leaves or stays for the collective below)
+    if (__shfl_sync(0xffffffffu, (int)pass_failed(P.status, P.passSeq), 0)) return;
+    const bool last = pass == P.radixPasses - 1;
 #pragma unroll
     for (int gi = 0; gi < kSortGroups; gi++) {
-        if (key[gi] < 0) continue;
-        int dg = (key[gi] >> shift) & 255;
-        int pos = sBase[dg] + sWarpCnt[warp][dg] + rank[gi];
-        if ((unsigned)pos >= (unsigned)total) continue;  // only reachable after an expired wait
-        outKey[pos] = key[gi];
-        outTri[pos] = tri[gi];
+        const bool valid = key[gi] >= 0;
+        const int dg = (key[gi] >> shift) & 255;
+        const int pos = valid ? sBase[dg] + sWarpCnt[warp][dg] + rank[gi] : 0;
+        const bool put = valid && (unsigned)pos < (unsigned)total;  // false only after an expired wait
+        if (put) {
+            outKey[pos] = key[gi];
+            outTri[pos] = tri[gi];
+        }
+        if (last) {
+            // each bin's (start, end) in the sorted list: the group's lanes
+            // with one key hold consecutive positions (ranks follow lane
+            // order), so its lowest lane gives the start and its highest the end
+            const unsigned peers = __match_any_sync(0xffffffffu, put ? key[gi] : -1 - lane);
+            if (put && lane == __ffs(peers) - 1) atomicMin(P.binStart + 2 * key[gi], pos);
+            if (put && lane == 31 - __clz(peers)) atomicMax(P.binStart + 2 * key[gi] + 1, pos + 1);
+        }
     }
 }
 
-// binStart[b] = first position of bin b in the sorted keys (a lower bound by
-// binary search, one thread per bin); binStart[nBins] = total.
-// Each bin's first position in the sorted list, and the raster's work list:
-// a bin with n triangles becomes s = min(rowSplit, the largest power of two
-// <= n / kSliceTris) items (row slices when s > 1), in buckets by s, crowded
-// first; empty bins last (they still clear their pixels).
-__global__ void k_bin_bounds(PassParams P, const int* __restrict__ keys)
+// The raster's work list, from each bin's (start, end) in the sorted list
+// (written by the last radix pass): a bin with n triangles becomes s =
+// min(rowSplit, the largest power of two <= n / kSliceTris) items (row
+// slices when s > 1), in buckets by s, crowded first; empty bins last (they
+// still clear their pixels).  Launched only for rasters that take work items
+// (row split or one warp per bin); a raster with one block per bin reads the
+// ranges directly.
+__global__ void k_bin_bounds(PassParams P)
 {
     if (pass_failed(P.status, P.passSeq)) return;
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     int nBins = P.binsX * P.binsY;
-    if (b > nBins) return;
-    int total = P.slotStatus[kSlotTiles] ? P.slotStatus[kSlotTotal] : 0;
-    if (b == nBins) {
-        P.binStart[b] = total;
-        return;
-    }
-    // the first positions of keys b and b + 1, searched side by side (two
-    // independent loads per step)
-    int lo0 = 0, hi0 = total, lo1 = 0, hi1 = total;
-    while (lo0 < hi0 || lo1 < hi1) {
-        const int m0 = (lo0 + hi0) >> 1, m1 = (lo1 + hi1) >> 1;
-        const int k0 = lo0 < hi0 ? __ldg(keys + m0) : 0, k1 = lo1 < hi1 ? __ldg(keys + m1) : 0;
-        if (lo0 < hi0) {
-            if (k0 < b) lo0 = m0 + 1;
-            else hi0 = m0;
-        }
-        if (lo1 < hi1) {
-            if (k1 < b + 1) lo1 = m1 + 1;
-            else hi1 = m1;
-        }
-    }
-    const int start = lo0;
-    P.binStart[b] = start;
-    const int n = lo1 - start;
+    if (b >= nBins) return;
+    const int2 r = P.slotStatus[kSlotTiles] ? ((const int2*)P.binStart)[b] : make_int2(0, 0);
+    const int n = r.x < r.y ? r.y - r.x : 0;
     int lg = 0;
     while (lg < 3 && (1 << (lg + 1)) <= P.rowSplit && n >= (kSliceTris << (lg + 1))) lg++;
     const int bucket = n == 0 ? 4 : 3 - lg;
@@ -865,10 +882,12 @@ void launch_sort(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
         launches++;
     }
     pr->end(s);
-    pr->begin(K_BOUNDS, s);
-    k_bin_bounds<<<ceil_div(nBins + 1, 256), 256, 0, s>>>(P, key);
-    pr->end(s);
-    launches++;
+    if (raster_uses_items(P)) {
+        pr->begin(K_BOUNDS, s);
+        k_bin_bounds<<<ceil_div(nBins, 256), 256, 0, s>>>(P);
+        pr->end(s);
+        launches++;
+    }
 }
 
 }  // namespace ps3d
