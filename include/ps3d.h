@@ -52,8 +52,9 @@ extern "C" {
  * selected by id.  Low nibble: 1 vertex, 2 interpolation, 3 fragment.
  *   DEF01  VertexProcesserDEF01 / InterpolationProcessorDEF01 /
  *          FragmentProcessorDEF01 (tex1light1.cpp): point light, nearest
- *          texture; the fragment stage uses IEEE 1/x and 1/sqrt where the
- *          reference uses rcpps/rsqrtss.
+ *          texture; its rcpps / rsqrtss normalisations are reproduced bit
+ *          for bit (tables of the instructions as the reference's x86 host
+ *          computes them), as in every reference processor here.
  *   DEF05  the depth-only shadow programme (shadow.cpp), positions x0.9.
  *   SHADOW DEF05's vertex stage without the x0.9 scale.
  *   LIT1   fragment stage over DEF01 varyings: bilinear REPEAT albedo,
@@ -233,6 +234,15 @@ int ps3d_vao_destroy(ps3d_pipeline* p, int vao);
 int ps3d_vbo_attach(ps3d_pipeline* p, int vao, int slot, int unitBytes, int count, const void* data);
 /* Same, from device memory. */
 int ps3d_vbo_attach_device(ps3d_pipeline* p, int vao, int slot, int unitBytes, int count, const void* devData);
+/* PuresoftPipeline::getVBO(vao, idx)->updateContent(src) (pipeline.cpp:168-181,
+ * vbo.cpp:28-31): overwrites the VBO's unitBytes * count bytes with `data`
+ * (host memory) in place.  Draws recorded before the call are rendered with
+ * the old contents first (the reference's drawVAO is synchronous); draws
+ * recorded after it, and command buffers replayed after it, read the new
+ * contents.  PS3D_ERR_RANGE for a bad VAO or slot or an empty slot (where
+ * the reference would dereference a null VBO), PS3D_ERR_INVALID while a
+ * command buffer is being recorded. */
+int ps3d_vbo_update(ps3d_pipeline* p, int vao, int slot, const void* data);
 /* PuresoftPipeline::detachVBO + delete (pipeline.cpp:153-166). */
 int ps3d_vbo_detach(ps3d_pipeline* p, int vao, int slot);
 

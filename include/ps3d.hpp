@@ -31,6 +31,19 @@ struct ImageBuffer {
     const void* pixels;
 };
 
+// A VBO of a pipeline's VAO, as getVBO returns it (pipeline.cpp:168-181):
+// updateContent replaces its contents in place (vbo.cpp:28-31).
+class PuresoftVBO
+{
+public:
+    PuresoftVBO(ps3d_pipeline* p, int vao, int idx) : m_p(p), m_vao(vao), m_idx(idx) {}
+    void updateContent(const void* src) { check(ps3d_vbo_update(m_p, m_vao, m_idx, src)); }
+
+private:
+    ps3d_pipeline* m_p;
+    int m_vao, m_idx;
+};
+
 class PuresoftPipeline
 {
 public:
@@ -74,6 +87,7 @@ public:
         check(ps3d_vbo_attach(m_p, vao, idx, unitBytes, unitCount, data));
     }
     void detachVBO(int vao, int idx) { check(ps3d_vbo_detach(m_p, vao, idx)); }
+    PuresoftVBO getVBO(int vao, int idx) { return PuresoftVBO(m_p, vao, idx); }
     void destroyVAO(int vao) { check(ps3d_vao_destroy(m_p, vao)); }
 
     // rendering api

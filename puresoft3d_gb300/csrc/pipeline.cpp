@@ -1517,6 +1517,29 @@ int ps3d_vbo_attach_device(ps3d_pipeline* p, int vao, int slot, int unitBytes, i
     return vbo_attach(p, vao, slot, unitBytes, count, devData, cudaMemcpyDeviceToDevice);
 }
 
+int ps3d_vbo_update(ps3d_pipeline* p, int vao, int slot, const void* data)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    if (vao < 0 || vao >= (int)p->vaos.size() || !p->vaos[vao].alive) return fail(PS3D_ERR_RANGE, "getVBO vao");
+    if (slot < 0 || slot >= PS3D_MAX_VBOS) return fail(PS3D_ERR_RANGE, "getVBO idx");
+    Vbo* b = p->vaos[vao].vbo[slot];
+    if (!b) return fail(PS3D_ERR_RANGE, "updateContent: no VBO in that slot");
+    if (!data) return fail(PS3D_ERR_INVALID, "updateContent: null source");
+    if (p->recording) return fail(PS3D_ERR_INVALID, "updateContent while a command buffer is being recorded");
+    // Draws recorded before the call read the old contents, as the
+    // reference's synchronous drawVAO did: they are rendered (and, after a
+    // bin-list overflow, re-run) before the buffer changes.  Draws recorded
+    // later, and command buffers replayed later, read the new contents.
+    int rc = do_finish(p);
+    if (rc) return rc;
+    const size_t bytes = (size_t)b->unitBytes * b->count;
+    if (bytes) {
+        CU(cudaMemcpyAsync(b->dev, data, bytes, cudaMemcpyHostToDevice, p->stream));
+        CU(cudaStreamSynchronize(p->stream));
+    }
+    return 0;
+}
+
 int ps3d_vbo_detach(ps3d_pipeline* p, int vao, int slot)
 {
     if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");

@@ -63,6 +63,7 @@ _SIGS = {
     "ps3d_flush": [_c_void_p],
     "ps3d_finish": [_c_void_p],
     "ps3d_finish_noalloc": [_c_void_p],
+    "ps3d_vbo_update": [_c_void_p, _c_int, _c_int, _c_void_p],
     "ps3d_allocation_count": [],
     "ps3d_set_bin_width": [_c_void_p, _c_int],
     "ps3d_get_bin_width": [_c_void_p, ctypes.POINTER(_c_int)],
@@ -238,6 +239,12 @@ class PuresoftPipeline:
         arr = np.ascontiguousarray(arr)
         self._check(self.lib.ps3d_vbo_attach(self.h, vao, slot, arr.nbytes // max(len(arr), 1), len(arr),
                                              arr.ctypes.data))
+
+    def updateVBO(self, vao, slot, arr):
+        """getVBO(vao, slot)->updateContent(arr): the VBO's contents replaced in
+        place (arr must hold exactly its unitBytes * count bytes)."""
+        arr = np.ascontiguousarray(arr)
+        self._check(self.lib.ps3d_vbo_update(self.h, vao, slot, arr.ctypes.data))
 
     def detachVBO(self, vao, slot):
         self._check(self.lib.ps3d_vbo_detach(self.h, vao, slot))

@@ -54,7 +54,9 @@ int main(int argc, char**) {
         int prog = pipe.createProgramme(pipe.addProcessor(PS3D_VP_DEF04), pipe.addProcessor(PS3D_IP_DEF04),
                                         pipe.addProcessor(PS3D_FP_DEF04));
         pipe.useProgramme(prog);
-        pipe.drawVAO(pipe.createVAOFromObjx("sphere.objx"));
+        int vao = pipe.createVAOFromObjx("sphere.objx");
+        pipe.getVBO(vao, 0).updateContent(nullptr);
+        pipe.drawVAO(vao);
         pipe.postProcess(PS3D_PP_ADD8);
         unsigned char frame[64 * 48 * 4];
         pipe.readColour(frame);
