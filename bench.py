@@ -75,12 +75,13 @@ CONFIGS = {
 }
 
 
-# DRAM bytes (read + write) of one raster launch on each workload, from one
-# ncu capture of the same kernel on the same full-size workload (one-pass
-# metrics dram__bytes_read.sum / dram__bytes_write.sum; the command and the
-# per-launch figures are in profiles/raster_dram_traffic.md).  Averages over
-# the captured launches that ran to completion.
-RASTER_TRAFFIC = {"c1": 70272, "c2": 5081664, "c3": 105983872, "c4": 777167744}
+# DRAM bytes (read + write) of one raster launch on each workload at its
+# pinned schedule, from one ncu capture of the same kernel on the same
+# full-size workload (one-pass metrics dram__bytes_read.sum and
+# dram__bytes_write.sum, every raster launch of two immediate-path frames:
+# bench.py --config cN --ncu-frames 2); averages over the launches that ran
+# to completion.
+RASTER_TRAFFIC = {"c1": 77696, "c2": 5204672, "c3": 113905024, "c4": 778335744}
 
 
 def peaks():

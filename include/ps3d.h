@@ -317,6 +317,13 @@ int ps3d_set_raster_warp_bins(ps3d_pipeline* p, int on);
  * in the raster.  Passes that blend or discard bin whole triangles either
  * way.  Time only, never results. */
 int ps3d_set_span_items(ps3d_pipeline* p, int on);
+/* Deferred varyings: 1 the set-up kernel computes only positions, and the
+ * shade kernel runs the vertex processor on the three vertices of each
+ * pixel's winning triangle (less set-up work and traffic, more per shaded
+ * pixel: pays where triangles outnumber shaded pixels); 0 (the default)
+ * the set-up stores every binned triangle's vertex varyings.  Passes that
+ * blend or discard keep stored varyings.  Time only, never results. */
+int ps3d_set_lazy_varyings(ps3d_pipeline* p, int on);
 
 /* ps3d_finish for callers that must not allocate device memory; it has no
  * counterpart in the reference, whose CPU pipeline allocates no device memory
@@ -497,7 +504,9 @@ int ps3d_selftest_occlusion(uint64_t cases, uint64_t* wrong, uint64_t* occluded)
 /* Overwrites `bytes` of an internal device buffer on the pipeline's stream
  * (benchmarking aid: evicts the 126 MB L2 between timed frames). */
 int ps3d_l2_scrub(ps3d_pipeline* p, size_t bytes);
-/* When on, each kernel launch outside graphs is bracketed by CUDA events. */
+/* When on, each kernel launch outside graphs is bracketed by CUDA events,
+ * and a launch's passes run one after another on the pipeline's stream (not
+ * overlapped on two), so that each kernel's events time that kernel alone. */
 int ps3d_profile_enable(ps3d_pipeline* p, int on);
 /* Waits, then returns per family the launches and milliseconds since the
  * last read (arrays of PS3D_K_COUNT). */

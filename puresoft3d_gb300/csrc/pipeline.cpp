@@ -246,6 +246,7 @@ struct ps3d_pipeline {
     int rowSplit = 1;
     int warpBins = 0;
     int spanItems = 0;
+    int lazyVary = 0;
     bool countFrags = false;
     cudaStream_t stream = nullptr;
     bool ownStream = false;
@@ -885,6 +886,7 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     P.vary = x.vary;
     P.nvMax = std::max(nvMax, 1);
     P.anyVary = nvMax > 0;
+    P.lazyVary = p->lazyVary && !forward && nvMax > 0;
     P.pairKey = x.pairKey;
     P.pairTri = x.pairTri;
     P.pairCap = p->pairCap;
@@ -1078,7 +1080,9 @@ int launch_cmds(ps3d_pipeline* p, const std::vector<Command>& cmds, size_t from)
     // Two streams pay off for a few large passes (a shadow pass and a lit
     // pass); for many small passes the events cost more than the overlap
     // gains, and graphs of them instantiate slowly.
-    p->oneStream = passes <= 1 || passes > kMaxOverlapPasses;
+    // while profiling, passes run one after another, so that each kernel's
+    // events time that kernel alone
+    p->oneStream = passes <= 1 || passes > kMaxOverlapPasses || p->prof.on;
     if (p->oneStream) return launch_cmds_inner(p, cmds, from);
     cudaEvent_t fork;
     int rc = mark(p, p->stream, fork);
@@ -1717,6 +1721,13 @@ int ps3d_set_row_split(ps3d_pipeline* p, int blocksPerBin)
     return 0;
 }
 
+int ps3d_set_lazy_varyings(ps3d_pipeline* p, int on)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    p->lazyVary = on ? 1 : 0;
+    return 0;
+}
+
 int ps3d_set_span_items(ps3d_pipeline* p, int on)
 {
     if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
@@ -2323,6 +2334,7 @@ int noalloc_run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const P
     P.vary = (float*)(base + L.vary);
     P.nvMax = std::max(s.nvMax, 1);
     P.anyVary = s.nvMax > 0;
+    P.lazyVary = p->lazyVary && !s.forward && s.nvMax > 0;
     P.pairKey = (int*)(base + L.pairKey);
     P.pairTri = (int*)(base + L.pairTri);
     P.pairCap = s.pairCap;

@@ -137,6 +137,8 @@ struct PassParams {
     float* vary;              // [tri][3][nvMax]
     int nvMax;
     int anyVary;              // some draw of the pass carries varyings
+    int lazyVary;             // 1 = the set-up writes no varyings: the shade computes its winners' vertices'
+                              // (passes shaded after the raster only)
     int* pairKey;             // bin of each (tri, bin) pair, in triangle order
     int* pairTri;
     int pairCap;              // capacity of pairKey / pairTri / keyB / binTri

@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <vector>
 #include "raster_common.cuh"
+#include "vertex_stage.cuh"
 
 namespace ps3d {
 
@@ -47,23 +48,20 @@ template <int NV> struct VaryState {
     int x;  // the pixel the state is at
 };
 
-// nstep: the interpolation stage steps the first two float4 varyings by the
-// third's step (the reference demo's IP_Planet, test/testproc.cpp:171-195,
-// adds the normal's step to the tangent and the binormal).
+// The span's interpolation state from the varyings' values at its two ends
+// (s0, e0: interpolateByContributes at left and right): calcStep, the
+// interpolation stage's step rule, the left-clamp skip.  nstep: the
+// interpolation stage steps the first two float4 varyings by the third's
+// step (the reference demo's IP_Planet, test/testproc.cpp:171-195, adds the
+// normal's step to the tangent and the binormal).
 template <int NV>
-__device__ __forceinline__ void vary_begin(const TriRaster& t, const float* vary, int nvMax, const Span& s,
-                                           const SpanZ& z, VaryState<NV>& v, bool nstep = false)
+__device__ __forceinline__ void vary_steps(const float* s0, const float* e0, const Span& s, const SpanZ& z,
+                                           VaryState<NV>& v, bool nstep)
 {
-    const float* a = vary;
-    const float* b = vary + nvMax;
-    const float* c = vary + 2 * nvMax;
 #pragma unroll
     for (int k = 0; k < NV; k++) {
-        float va = __ldg(a + k), vb = __ldg(b + k), vc = __ldg(c + k);
-        float s0 = fadd(fadd(fmul(va, z.cl[0]), fmul(vb, z.cl[1])), fmul(vc, z.cl[2]));
-        float e0 = fadd(fadd(fmul(va, z.cr[0]), fmul(vb, z.cr[1])), fmul(vc, z.cr[2]));
-        v.st[k] = s0;
-        v.sp[k] = fmul(fsub(e0, s0), z.recip);  // calcStep: stepCount != 0 here
+        v.st[k] = s0[k];
+        v.sp[k] = fmul(fsub(e0[k], s0[k]), z.recip);  // calcStep: stepCount != 0 here
     }
     if constexpr (NV >= 12) {
         if (nstep) {
@@ -84,6 +82,53 @@ __device__ __forceinline__ void vary_begin(const TriRaster& t, const float* vary
     v.x = s.leftClamped;
 }
 
+// Set-up from the triangle's vertex varyings as the set-up kernel stored them.
+template <int NV>
+__device__ __forceinline__ void vary_begin(const TriRaster& t, const float* vary, int nvMax, const Span& s,
+                                           const SpanZ& z, VaryState<NV>& v, bool nstep = false)
+{
+    const float* a = vary;
+    const float* b = vary + nvMax;
+    const float* c = vary + 2 * nvMax;
+    float s0[NV], e0[NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+        float va = __ldg(a + k), vb = __ldg(b + k), vc = __ldg(c + k);
+        s0[k] = fadd(fadd(fmul(va, z.cl[0]), fmul(vb, z.cl[1])), fmul(vc, z.cl[2]));
+        e0[k] = fadd(fadd(fmul(va, z.cr[0]), fmul(vb, z.cr[1])), fmul(vc, z.cr[2]));
+    }
+    vary_steps<NV>(s0, e0, s, z, v, nstep);
+}
+
+// Set-up with the vertex varyings computed here (a pass whose set-up
+// deferred them): the draw's vertex processor on the triangle's three
+// vertices, each product added in vertex order as above.
+template <int NV>
+__device__ __forceinline__ void vary_begin_lazy(const DrawDesc& d, const DrawUniforms& U, int lt, const Span& s,
+                                                const SpanZ& z, VaryState<NV>& v, bool nstep = false)
+{
+    float s0[NV], e0[NV];
+#pragma unroll 1
+    for (int vtx = 0; vtx < 3; vtx++) {
+        float a[kMaxVary];
+        vp_varyings(d, U, 3 * lt + vtx, a);
+        const float cl = vtx == 0 ? z.cl[0] : (vtx == 1 ? z.cl[1] : z.cl[2]);
+        const float cr = vtx == 0 ? z.cr[0] : (vtx == 1 ? z.cr[1] : z.cr[2]);
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            const float ps = fmul(a[k], cl), pe = fmul(a[k], cr);
+            if (vtx == 0) {
+                s0[k] = ps;
+                e0[k] = pe;
+            } else {
+                s0[k] = fadd(s0[k], ps);
+                e0[k] = fadd(e0[k], pe);
+            }
+        }
+    }
+    vary_steps<NV>(s0, e0, s, z, v, nstep);
+}
+
 template <int NV> __device__ __forceinline__ void vary_advance(VaryState<NV>& v, int x)
 {
     for (; v.x < x; v.x++) {
@@ -100,13 +145,16 @@ template <int NV> __device__ __forceinline__ void vary_out(const VaryState<NV>& 
     for (int k = 0; k < NV; k++) out[k] = fmul(v.st[k], inv);
 }
 
-// Varyings of the fragment at x on row y of triangle t.
+// Varyings of the shade-list fragment at x of triangle w (its record t):
+// from the stored vertex varyings, or computed from the vertices.
 template <int NV>
-__device__ __forceinline__ void fragment_varyings(const TriRaster& t, const float* vary, int nvMax, const Span& s,
-                                                  const SpanZ& z, int x, float out[NV], bool nstep = false)
+__device__ __forceinline__ void shade_varyings(const PassParams& P, const DrawDesc& d, const DrawUniforms& U, int w,
+                                               const TriRaster& t, const Span& s, const SpanZ& z, int x, float out[NV],
+                                               bool nstep = false)
 {
     VaryState<NV> v;
-    vary_begin<NV>(t, vary, nvMax, s, z, v, nstep);
+    if (P.lazyVary) vary_begin_lazy<NV>(d, U, w - d.triBase, s, z, v, nstep);
+    else vary_begin<NV>(t, P.vary + (size_t)w * 3 * P.nvMax, P.nvMax, s, z, v, nstep);
     vary_advance<NV>(v, x);
     vary_out<NV>(v, out);
 }
@@ -617,31 +665,30 @@ __device__ __forceinline__ void shade_entry(const PassParams& P, int2 e)
     span_row<true>(t, yl, d.vpW, s);
     SpanZ z;
     span_z(t, s, yl, z);
-    const float* vary = P.vary + (size_t)w * 3 * P.nvMax;
     uint32_t bgra;
     switch (FPK ? FPK : d.fp) {
     case FP_EARTH:
     case FP_SATELLITE: {
         float in[21];
-        fragment_varyings<21>(t, vary, P.nvMax, s, z, xl, in, true);
+        shade_varyings<21>(P, d, U, w, t, s, z, xl, in, true);
         bgra = shade_planet(U, in, (FPK ? FPK : d.fp) == FP_EARTH);
         break;
     }
     case FP_CLOUD: {
         float in[13];
-        fragment_varyings<13>(t, vary, P.nvMax, s, z, xl, in);
+        shade_varyings<13>(P, d, U, w, t, s, z, xl, in);
         bgra = shade_cloud(U, in);
         break;
     }
     case FP_DIFFUSEONLY: {
         float in[13];
-        fragment_varyings<13>(t, vary, P.nvMax, s, z, xl, in);
+        shade_varyings<13>(P, d, U, w, t, s, z, xl, in);
         bgra = shade_diffuse_only(U, in);
         break;
     }
     case FP_SINGLECOLOUR: {
         float in[11];
-        fragment_varyings<11>(t, vary, P.nvMax, s, z, xl, in);
+        shade_varyings<11>(P, d, U, w, t, s, z, xl, in);
         bgra = shade_single_colour(U, in);
         break;
     }
@@ -650,43 +697,43 @@ __device__ __forceinline__ void shade_entry(const PassParams& P, int2 e)
         break;
     case FP_DEF03: {
         float in[17];
-        fragment_varyings<17>(t, vary, P.nvMax, s, z, xl, in);
+        shade_varyings<17>(P, d, U, w, t, s, z, xl, in);
         bgra = shade_def03(U, in);
         break;
     }
     case FP_LIT2: {
         float in[16];
-        fragment_varyings<16>(t, vary, P.nvMax, s, z, xl, in);
+        shade_varyings<16>(P, d, U, w, t, s, z, xl, in);
         bgra = shade_lit2(U, in);
         break;
     }
     case FP_LIT1: {
         float in[9];
-        fragment_varyings<9>(t, vary, P.nvMax, s, z, xl, in);
+        shade_varyings<9>(P, d, U, w, t, s, z, xl, in);
         bgra = shade_lit1(U, in);
         break;
     }
     case FP_DEF02: {
         float in[11];
-        fragment_varyings<11>(t, vary, P.nvMax, s, z, xl, in);
+        shade_varyings<11>(P, d, U, w, t, s, z, xl, in);
         bgra = shade_def02(U, in);
         break;
     }
     case FP_DEF04: {
         float in[3];
-        fragment_varyings<3>(t, vary, P.nvMax, s, z, xl, in);
+        shade_varyings<3>(P, d, U, w, t, s, z, xl, in);
         bgra = shade_def04(U, in);
         break;
     }
     case FP_LIT3: {
         float in[9];
-        fragment_varyings<9>(t, vary, P.nvMax, s, z, xl, in);
+        shade_varyings<9>(P, d, U, w, t, s, z, xl, in);
         bgra = shade_lit3(U, in);
         break;
     }
     default: {  // FP_DEF01
         float in[9];
-        fragment_varyings<9>(t, vary, P.nvMax, s, z, xl, in);
+        shade_varyings<9>(P, d, U, w, t, s, z, xl, in);
         bgra = shade_def01(U, in);
         break;
     }

@@ -70,6 +70,7 @@ _SIGS = {
     "ps3d_set_raster_occupancy": [_c_void_p, _c_int],
     "ps3d_set_raster_warp_bins": [_c_void_p, _c_int],
     "ps3d_set_span_items": [_c_void_p, _c_int],
+    "ps3d_set_lazy_varyings": [_c_void_p, _c_int],
     "ps3d_selftest_wait": [_c_void_p, _c_int, ctypes.POINTER(ctypes.c_float)],
     "ps3d_read_colour": [_c_void_p, _c_void_p],
     "ps3d_read_depth": [_c_void_p, _c_void_p],
@@ -308,6 +309,11 @@ class PuresoftPipeline:
         """Bin short triangles' row spans as set-up items (on) or whole
         triangles whose spans the raster sets up (off, the default)."""
         self._check(self.lib.ps3d_set_span_items(self.h, int(bool(on))))
+
+    def setLazyVaryings(self, on: bool):
+        """The shade computes its winners' vertex varyings (on) or the set-up
+        stores every binned triangle's (off, the default)."""
+        self._check(self.lib.ps3d_set_lazy_varyings(self.h, int(bool(on))))
 
     def setSpanCulling(self, on: bool):
         """Raster kernel variant: drop occluded spans before their depths are

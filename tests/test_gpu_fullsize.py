@@ -40,7 +40,7 @@ def _oracle(name):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("sched", ["pinned", "default"])
+@pytest.mark.parametrize("sched", ["pinned", "default", "lazy"])
 @pytest.mark.parametrize("name", sorted(FULL))
 def test_full_size_frame_matches_oracle_and_reference(gpu_lib, name, sched):
     from puresoft3d_gb300.autotune import PINNED, apply
@@ -51,6 +51,8 @@ def test_full_size_frame_matches_oracle_and_reference(gpu_lib, name, sched):
     p = PuresoftPipeline(scene.width, scene.height)
     if sched == "pinned":
         apply(p, PINNED[FULL[name][0]])
+    if sched == "lazy":  # the shade computes its winners' vertex varyings
+        p.setLazyVaryings(True)
     p.setFragmentCounting(True)
     gpu = render(p, scene)
     st = p.stats()

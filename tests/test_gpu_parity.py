@@ -37,6 +37,22 @@ def test_gpu_matches_oracle(name, scene, gpu_lib):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("name,scene", CASES, ids=[c[0] for c in CASES])
+def test_deferred_varyings_match_oracle(name, scene, gpu_lib):
+    """The shade computing its winners' vertex varyings (the set-up storing
+    none) gives the oracle's frame on every golden case; passes that blend
+    or discard keep stored varyings."""
+    from puresoft3d_gb300.pipeline import PuresoftPipeline
+    g = PuresoftPipeline(scene.width, scene.height)
+    g.setLazyVaryings(True)
+    gpu = render(g, scene)
+    ora = render(OraclePipeline(scene.width, scene.height), scene)
+    assert_depth_exact(gpu["depth"], ora["depth"], name)
+    mx, mean = colour_diff(gpu["colour"], ora["colour"])
+    assert mx <= COLOUR_TOL, "%s: colour differs by up to %d LSB (mean %.4f)" % (name, mx, mean)
+
+
+@pytest.mark.gpu
 def test_fragment_counts_match_oracle(gpu_lib):
     from puresoft3d_gb300.pipeline import PuresoftPipeline
     name, scene = [c for c in CASES if c[0].startswith("kat_soup_lit")][0]
