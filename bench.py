@@ -224,9 +224,20 @@ def make_scene(cfg, views=4096):
     return {"c1": S.scene_c1, "c2": S.scene_c2, "c3": S.scene_c3}[cfg]()
 
 
-def _sched_dict(s, source, span_items=0):
-    return {"bin_width": s[0], "raster_occupancy": s[1], "span_culling": s[2], "row_split": s[3],
-            "warp_bins": s[4], "span_items": span_items, "source": source}
+SCHED_KEYS = ("bin_width", "raster_occupancy", "span_culling", "row_split", "warp_bins", "span_items",
+              "lazy_varyings")
+
+
+def _sched_dict(s, source):
+    from puresoft3d_gb300.autotune import _sched
+    d = dict(zip(SCHED_KEYS, _sched(s)))
+    d["source"] = source
+    return d
+
+
+def _flag_schedule(args):
+    return (args.bin_width, args.raster_occupancy, args.span_culling, args.row_split, args.warp_bins,
+            args.span_items, args.lazy_varyings)
 
 
 def autotune(pipe, record, key, args, pinned=None):
@@ -237,16 +248,15 @@ def autotune(pipe, record, key, args, pinned=None):
     (puresoft3d_gb300.autotune.PINNED), so that its profiles under profiles/
     describe the same kernels."""
     from puresoft3d_gb300.autotune import Autotuner, apply
-    pipe.setSpanItems(args.span_items)
     if args.bin_width:
-        s = (args.bin_width, args.raster_occupancy, args.span_culling, args.row_split, args.warp_bins)
+        s = _flag_schedule(args)
         apply(pipe, s)
-        return _sched_dict(s, "flags", args.span_items)
+        return _sched_dict(s, "flags")
     if pinned is not None and not args.autotune:
         apply(pipe, pinned)
-        return _sched_dict(tuple(pinned) + (0,) * (5 - len(pinned)), "pinned", args.span_items)
+        return _sched_dict(pinned, "pinned")
     best, ms = Autotuner().tune(pipe, record, key, reps=3)
-    d = _sched_dict(best, "autotuner", args.span_items)
+    d = _sched_dict(best, "autotuner")
     d["candidate_ms"] = {k: round(v, 4) for k, v in ms.items()}
     return d
 
@@ -258,9 +268,7 @@ def twin(scene, tune):
     from puresoft3d_gb300.pipeline import PuresoftPipeline
     p = PuresoftPipeline(scene.width, scene.height)
     S.replay_setup(scene, p)
-    apply(p, (tune["bin_width"], tune["raster_occupancy"], tune["span_culling"], tune["row_split"],
-              tune.get("warp_bins", 0)))
-    p.setSpanItems(tune.get("span_items", 0))
+    apply(p, tuple(tune[k] for k in SCHED_KEYS))
     p.finish()
     return p
 
@@ -554,9 +562,8 @@ def run_frames_only(args):
     pipe = PuresoftPipeline(scene.width, scene.height)
     S.replay_setup(scene, pipe)
     from puresoft3d_gb300.autotune import PINNED, apply
-    pipe.setSpanItems(args.span_items)
     if args.bin_width:
-        apply(pipe, (args.bin_width, args.raster_occupancy, args.span_culling, args.row_split, args.warp_bins))
+        apply(pipe, _flag_schedule(args))
     elif args.config in PINNED:
         apply(pipe, PINNED[args.config])
     for _ in range(args.ncu_frames):
@@ -983,7 +990,10 @@ def main():
     ap.add_argument("--warp-bins", type=int, default=0, choices=[0, 1],
                     help="with --bin-width 8 or 16: one raster warp per bin (1) or four sharing it (0)")
     ap.add_argument("--span-items", type=int, default=0, choices=[0, 1],
-                    help="bin short triangles' row spans as set-up items (1) or whole triangles (0)")
+                    help="with --bin-width: bin short triangles' row spans as set-up items (1) or whole triangles (0)")
+    ap.add_argument("--lazy-varyings", type=int, default=0, choices=[0, 1],
+                    help="with --bin-width: the shade computes its winners' vertex varyings (1) or the set-up "
+                         "stores them (0)")
     ap.add_argument("--autotune", action="store_true",
                     help="time every schedule candidate on the frame and use the fastest (default: the pinned one)")
     args = ap.parse_args()

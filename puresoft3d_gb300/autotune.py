@@ -1,8 +1,8 @@
 """Schedule autotuner for the device passes.
 
 A schedule is (bin width, raster occupancy, span culling, row split, warp
-bins).  The bin width (8, 16 or 32 columns; bins are always 32 rows) sets
-how the raster kernel's work is cut:
+bins, span items, deferred varyings).  The bin width (8, 16 or 32 columns;
+bins are always 32 rows) sets how the raster kernel's work is cut:
 
 * the number of bins, hence blocks, a pass launches (more, smaller bins give
   small views and thin targets more parallelism);
@@ -22,7 +22,11 @@ rows of crowded bins out between blocks: it pays off when a few crowded
 bins would otherwise run alone at the end of the launch.  Warp bins (1)
 switch the raster to one warp per bin of 8 or 16 columns that works through
 it alone, with no block-wide barrier between its span set-up and its walk
-(0: four warps share a bin; 32-column bins always do).
+(0: four warps share a bin; 32-column bins always do).  Span items (1) set
+short triangles' spans up in the set-up kernel instead of the raster;
+deferred varyings (1) leave the vertex varyings to the shade, which computes
+them for each pixel's winner only.  These two are tried as a second stage,
+one at a time on top of the best of the other five.
 
 Which schedule wins depends on the workload (triangle sizes, depth complexity,
 target size), so the tuner times every candidate on the caller's own frame:
@@ -59,25 +63,35 @@ PINNED = {
 }
 
 
+SCHEDULE_LEN = 7
+
+
 def _sched(c):
-    """(bin width, occupancy, span culling, row split, warp bins) of a
-    candidate given as a bare width or a shorter tuple (occupancy 0, culling
-    on, one block per bin and shared bins by default)."""
+    """(bin width, occupancy, span culling, row split, warp bins, span items,
+    deferred varyings) of a candidate given as a bare width or a shorter
+    tuple (occupancy 0, culling on, one block per bin, shared bins, whole
+    triangles binned and stored varyings by default)."""
     if not isinstance(c, (tuple, list)):
         c = (c,)
-    d = (None, 0, 1, 1, 0)
-    return tuple(int(c[i]) if i < len(c) else d[i] for i in range(5))
+    d = (None, 0, 1, 1, 0, 0, 0)
+    return tuple(int(c[i]) if i < len(c) else d[i] for i in range(SCHEDULE_LEN))
 
 
 def _name(c) -> str:
-    return "%d/%d/%d/%d/%d" % _sched(c)
+    s = _sched(c)
+    # the first five always; the second-stage switches only when on
+    return "/".join(str(v) for v in (s[:5] if not (s[5] or s[6]) else s))
 
 
 def apply(pipe, c) -> None:
-    bw, occ, cull, split, warp = _sched(c)
+    bw, occ, cull, split, warp, items, lazy = _sched(c)
     pipe.setBinWidth(bw)
     if hasattr(pipe, "setWarpBins"):
         pipe.setWarpBins(warp)
+    if hasattr(pipe, "setSpanItems"):
+        pipe.setSpanItems(items)
+    if hasattr(pipe, "setLazyVaryings"):
+        pipe.setLazyVaryings(lazy)
     if hasattr(pipe, "setRasterOccupancy"):
         pipe.setRasterOccupancy(occ)
     if hasattr(pipe, "setSpanCulling"):
@@ -150,13 +164,15 @@ class Autotuner:
 
     def tune(self, pipe, record: Callable[[object], None], key: str,
              candidates: Sequence = CANDIDATES, reps: int = 5, warmup: int = 2,
-             retune: bool = False) -> Tuple[Tuple[int, int, int, int, int], Dict[str, float]]:
+             retune: bool = False, second_stage: bool = True) -> Tuple[Tuple[int, ...], Dict[str, float]]:
         """Sets `pipe`'s schedule to the fastest candidate for `record`'s
         frame and returns ((bin width, raster occupancy, span culling, row
-        split, warp bins), {"bw/occ/cull/split/warp": median ms}).  A candidate is such a
+        split, warp bins, span items, deferred varyings), {name: median
+        ms}); with second_stage, span items and then deferred varyings are
+        tried on top of the best candidate and kept when faster.  A candidate is such a
         tuple, a shorter prefix of it or a bare bin width.  A cached result
         for (key, device, candidates) is reused unless `retune`."""
-        full = "%s|%s|%s" % (key, device_name(), ",".join(_name(c) for c in candidates))
+        full = "%s|%s|%s%s" % (key, device_name(), ",".join(_name(c) for c in candidates), "+2" if second_stage else "")
         hit = self.table.get(full)
         if hit and not retune:
             best = _sched(hit["best"])
@@ -167,6 +183,13 @@ class Autotuner:
             apply(pipe, c)
             ms[_name(c)] = self.time_frame(pipe, record, reps=reps, warmup=warmup)
         best = _sched(min(candidates, key=lambda c: ms[_name(c)]))
+        if second_stage:
+            for k in (5, 6):  # span items, then deferred varyings
+                trial = tuple(1 if i == k else v for i, v in enumerate(best))
+                apply(pipe, trial)
+                ms[_name(trial)] = self.time_frame(pipe, record, reps=reps, warmup=warmup)
+                if ms[_name(trial)] < ms[_name(best)]:
+                    best = trial
         apply(pipe, best)
         self.table[full] = {"best": list(best), "ms": {k: round(v, 5) for k, v in ms.items()}}
         self._save()

@@ -25,6 +25,8 @@ class _FakePipe:
         self.cull = 1
         self.split = 1
         self.warp = 0
+        self.items = 0
+        self.lazy = 0
         self.submits = 0
         self.recorded = 0
 
@@ -46,6 +48,12 @@ class _FakePipe:
     def setWarpBins(self, on):
         self.warp = int(on)
 
+    def setSpanItems(self, on):
+        self.items = int(on)
+
+    def setLazyVaryings(self, on):
+        self.lazy = int(on)
+
     def beginCommands(self):
         pass
 
@@ -63,7 +71,8 @@ class _FakePipe:
 
     def timerEnd(self):
         return (self.COST[self.bw] - (0.25 if self.occ == 8 else 0.0) - (0.125 if self.cull == 0 else 0.0)
-                - (0.0625 if self.split == 4 else 0.0) - (0.5 if self.warp and self.bw == 8 else 0.0))
+                - (0.0625 if self.split == 4 else 0.0) - (0.5 if self.warp and self.bw == 8 else 0.0)
+                + (0.01 if self.items else 0.0) - (0.03125 if self.lazy else 0.0))
 
 
 def _record(pipe):
@@ -73,8 +82,8 @@ def _record(pipe):
 def test_picks_fastest_and_sets_it(tmp_path):
     t = Autotuner(cache_path=str(tmp_path / "tune.json"))
     p = _FakePipe()
-    best, ms = t.tune(p, _record, key="w1", candidates=(8, 16, 32))
-    assert best == (16, 0, 1, 1, 0) and p.bw == 16
+    best, ms = t.tune(p, _record, key="w1", candidates=(8, 16, 32), second_stage=False)
+    assert best == (16, 0, 1, 1, 0, 0, 0) and p.bw == 16
     assert ms == {"8/0/1/1/0": 3.0, "16/0/1/1/0": 1.5, "32/0/1/1/0": 2.0}
     assert p.recorded == 3
 
@@ -83,22 +92,24 @@ def test_width_occupancy_culling_split_and_warp_bins(tmp_path):
     t = Autotuner(cache_path=str(tmp_path / "tune.json"))
     p = _FakePipe()
     best, ms = t.tune(p, _record, key="w1")
-    assert best == (16, 8, 0, 4, 0) and (p.bw, p.occ, p.cull, p.split, p.warp) == (16, 8, 0, 4, 0)
-    assert len(ms) == 32 and p.recorded == 32
+    # second stage: span items are slower here and dropped, deferred varyings faster and kept
+    assert best == (16, 8, 0, 4, 0, 0, 1) and (p.bw, p.occ, p.cull, p.split, p.warp, p.items, p.lazy) == best
+    assert len(ms) == 34 and p.recorded == 34
     assert ms["8/0/0/4/1"] == 3.0 - 0.125 - 0.0625 - 0.5
+    assert ms["16/8/0/4/0/1/0"] > ms["16/8/0/4/0"] > ms["16/8/0/4/0/0/1"]
 
 
 def test_cache_is_reused_and_keyed(tmp_path):
     path = str(tmp_path / "tune.json")
     Autotuner(cache_path=path).tune(_FakePipe(), _record, key="w1")
     table = json.load(open(path))
-    assert len(table) == 1 and list(table.values())[0]["best"] == [16, 8, 0, 4, 0]
+    assert len(table) == 1 and list(table.values())[0]["best"] == [16, 8, 0, 4, 0, 0, 1]
     p = _FakePipe()
     best, _ = Autotuner(cache_path=path).tune(p, _record, key="w1")
-    assert best == (16, 8, 0, 4, 0) and p.bw == 16 and p.cull == 0 and p.split == 4 and p.recorded == 0  # from the cache
+    assert best == (16, 8, 0, 4, 0, 0, 1) and p.lazy == 1 and p.bw == 16 and p.cull == 0 and p.split == 4 and p.recorded == 0  # from the cache
     p2 = _FakePipe()
     Autotuner(cache_path=path).tune(p2, _record, key="w2", candidates=(8, 32))
-    assert p2.bw == 32 and p2.recorded == 2
+    assert p2.bw == 32 and p2.recorded == 4
     assert len(json.load(open(path))) == 2
 
 
@@ -107,4 +118,4 @@ def test_retune_ignores_cache(tmp_path):
     Autotuner(cache_path=path).tune(_FakePipe(), _record, key="w1")
     p = _FakePipe()
     Autotuner(cache_path=path).tune(p, _record, key="w1", retune=True)
-    assert p.recorded == 32
+    assert p.recorded == 34
