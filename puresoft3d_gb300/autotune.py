@@ -56,10 +56,10 @@ CANDIDATES = tuple((bw, occ, cull, split, 0) for bw in (8, 16, 32) for occ in (0
 # pins one and its profiles are captured at the same one).
 PINNED = {
     "c1": (16, 0, 0, 1, 0),
-    "c2": (8, 8, 0, 1, 0),
+    "c2": (8, 8, 0, 1, 0, 0, 1),
     "c3": (16, 0, 1, 1, 1),
     "c3s": (16, 0, 1, 1, 1),
-    "c4": (32, 0, 0, 1, 0),
+    "c4": (16, 0, 0, 1, 1),
 }
 
 
