@@ -253,6 +253,20 @@ int ps3d_set_uniform(ps3d_pipeline* p, int idx, const void* data, size_t len);
  * a texture must have elemLen 4 and a scanline multiple of 4 (else
  * PS3D_ERR_INVALID).  The depth target must be CLAMP-addressed. */
 int ps3d_set_depth(ps3d_pipeline* p, int idx);
+/* PuresoftPipeline::setFBO(idx, fbo) (pipeline.cpp:260-275) with a texture
+ * of this pipeline as the FBO (borrowed, not copied; -1 = none, and slot 0
+ * back to the display).  The built-in fragment processors write FBO slot 0
+ * (FBOBridge, fragthrd.cpp:55-95), so after ps3d_set_fbo(p, 0, tex) the
+ * draws recorded next colour the texture (BGRA8, its rows bottom-up as the
+ * reference's textures are) and ps3d_post_process works on it (post.cpp:14);
+ * ps3d_clear_colour still clears the display, as clearColour does
+ * (pipeline.cpp:340-343), and the read-backs read the display.  The
+ * texture must have 4-byte elements (PS3D_ERR_INVALID) and cover a
+ * colour-writing draw's viewport (else ps3d_draw returns PS3D_ERR_INVALID,
+ * where the reference would drop the writes outside it).  A texture
+ * destroyed while bound leaves its slots.  PS3D_ERR_RANGE for idx outside
+ * [0, 16) or a bad texture. */
+int ps3d_set_fbo(ps3d_pipeline* p, int idx, int texture);
 /* PuresoftPipeline::setViewport (pipeline.cpp:207-216): rasteriser size. */
 int ps3d_set_viewport(ps3d_pipeline* p, int width, int height);
 /* Extension (no reference counterpart): a viewport of width x height -- the

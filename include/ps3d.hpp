@@ -93,6 +93,8 @@ public:
     // rendering api
     void setViewport(int width, int height) { check(ps3d_set_viewport(m_p, width, height)); }
     void setDepth(int idx = -1) { check(ps3d_set_depth(m_p, idx)); }
+    // setFBO(idx, fbo) with a texture index as the FBO (-1: none / the display)
+    void setFBO(int idx, int texture) { check(ps3d_set_fbo(m_p, idx, texture)); }
     void setUniform(int idx, const void* data, size_t len) { check(ps3d_set_uniform(m_p, idx, data, len)); }
     void drawVAO(int vao) { check(ps3d_draw(m_p, vao)); }
     void enable(int behavior) { check(ps3d_enable(m_p, behavior)); }

@@ -70,6 +70,7 @@ static float norm_scale(const float* v) { return x86_rsqrt((v[0] * v[0] + v[1] *
 
 #define MAX_VBOS 16      /* config.h:4 */
 #define MAX_UNIFORMS 1024 /* config.h:5 */
+#define MAX_FBOS 16      /* config.h:3-9 */
 #define MAX_VECS 8       /* float4 varyings per vertex, enough for every built-in processor */
 #define MAX_LEVELS 16
 
@@ -141,6 +142,7 @@ struct ps3do {
     o_fbo display;    /* BGRA8, topDown (pipeline.cpp:48) */
     o_fbo defDepth;   /* FP32, scanline rounded to 4 floats (pipeline.cpp:31) */
     o_fbo* depth;
+    o_fbo* fbos[MAX_FBOS]; /* setFBO's slots (pipeline.cpp:260-275): 0 = the colour target, the display by default */
     o_fbo** tex;
     int ntex;
     int* procs;
@@ -209,6 +211,7 @@ ps3do* ps3do_create(int width, int height, int threads)
     p->display.elemLen = 4;
     p->display.topDown = 1;
     p->display.buf = (uint8_t*)calloc((size_t)width * 4 * height, 1);
+    p->fbos[0] = &p->display; /* setFBO(0, NULL) in the constructor (pipeline.cpp:49) */
     p->defDepth.width = width;
     p->defDepth.height = height;
     p->defDepth.scanline = ((int)(width / 4.0f + 0.5f) * 4) * 4;
@@ -438,6 +441,23 @@ int ps3do_set_depth(ps3do* p, int idx) /* pipeline.cpp:218-239 */
     return 0;
 }
 
+/* PuresoftPipeline::setFBO (pipeline.cpp:260-275) with a texture as the
+   FBO (-1: none; slot 0 then falls back to the display).  The fragment
+   processors write slot 0 (FBOBridge, fragthrd.cpp:55-95) and postProcess
+   runs on it (post.cpp:14); clearColour still clears the display. */
+int ps3do_set_fbo(ps3do* p, int idx, int tex)
+{
+    if (idx < 0 || idx >= MAX_FBOS) return -1;
+    if (tex == -1) {
+        p->fbos[idx] = idx == 0 ? &p->display : NULL;
+        return 0;
+    }
+    if (tex < 0 || tex >= p->ntex || !p->tex[tex]) return -1;
+    if (p->tex[tex]->elemLen != 4) return -2; /* the processors write 4-byte BGRA */
+    p->fbos[idx] = p->tex[tex];
+    return 0;
+}
+
 int ps3do_set_viewport(ps3do* p, int width, int height)
 {
     if (width <= 0 || height <= 0) return -2;
@@ -467,12 +487,14 @@ int ps3do_clear_colour(ps3do* p, uint32_t bgra)
 }
 
 /* PuresoftPipeline::postProcess (post.cpp:3-19) with the built-in
-   post-processors: 0x7001 the demo's per-byte wrapping add (test2/testpost.cpp:
-   9-43) of a BGRA addend, 0x7002 linear depth fog.  The display buffer's
-   memory row H-1-y holds pixel row y; the depth buffer's row y. */
+   post-processors, over FBO slot 0 (the display unless setFBO moved it):
+   0x7001 the demo's per-byte wrapping add (test2/testpost.cpp:9-43) of a
+   BGRA addend, 0x7002 linear depth fog.  Pixel row y of the display lives at
+   memory row H-1-y, of a texture (and of the depth buffer) at row y. */
 int ps3do_post_process(ps3do* p, int id, const void* params, size_t bytes)
 {
-    int W = p->display.width, H = p->display.height;
+    o_fbo* f = p->fbos[0];
+    int W = f->width, H = f->height;
     if (id == 0x7001) {
         uint8_t add[4] = {50, 50, 50, 50};
         if (params) {
@@ -480,7 +502,7 @@ int ps3do_post_process(ps3do* p, int id, const void* params, size_t bytes)
             memcpy(add, params, 4);
         }
         for (int r = 0; r < H; r++) {
-            uint8_t* row = p->display.buf + (size_t)r * p->display.scanline;
+            uint8_t* row = f->buf + (size_t)r * f->scanline;
             for (int x = 0; x < 4 * W; x++) row[x] = (uint8_t)(row[x] + add[x & 3]);
         }
         return 0;
@@ -497,7 +519,7 @@ int ps3do_post_process(ps3do* p, int id, const void* params, size_t bytes)
         range = farD - nearD;
         for (int y = 0; y < H; y++) {
             const float* drow = (const float*)(d->buf + (size_t)y * d->scanline);
-            uint8_t* crow = p->display.buf + (size_t)(H - 1 - y) * p->display.scanline;
+            uint8_t* crow = f->buf + (size_t)(f->topDown ? H - 1 - y : y) * f->scanline;
             for (int x = 0; x < W; x++) {
                 float t = (drow[x] - nearD) / range;
                 t = t > 0.0f ? t : 0.0f;
@@ -1649,7 +1671,7 @@ static void run_task(draw_ctx* d, const o_task* t, long long* tested, long long*
     o_cursor cc, dc;
     memcpy(start, t->user, sizeof(float) * 4 * nv);
     memcpy(step, t->user + 4 * MAX_VECS, sizeof(float) * 4 * nv);
-    cursor_set(&cc, &p->display, t->y, t->x1);
+    cursor_set(&cc, p->fbos[0], t->y, t->x1);
     cursor_set(&dc, p->depth, t->y, t->x1);
     for (int x = t->x1; x <= t->x2; x++) {
         /* interpolateNextStep (interp.cpp:82-92) */

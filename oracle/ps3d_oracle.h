@@ -39,6 +39,7 @@ int ps3do_vao_create(ps3do* p);
 int ps3do_vbo_attach(ps3do* p, int vao, int slot, int unitBytes, int count, const void* data);
 int ps3do_set_uniform(ps3do* p, int idx, const void* data, size_t len);
 int ps3do_set_depth(ps3do* p, int idx);
+int ps3do_set_fbo(ps3do* p, int idx, int tex);
 int ps3do_set_viewport(ps3do* p, int width, int height);
 int ps3do_enable(ps3do* p, int bits);
 int ps3do_disable(ps3do* p, int bits);

@@ -230,10 +230,12 @@ void PostProcessorADD8::process(int threadIndex, int threadCount, PuresoftFBO* f
     }
 }
 
-PostProcessorFOG::PostProcessorFOG(unsigned int fog, float nearD, float farD) : m_fog(fog), m_near(nearD), m_far(farD) {}
+PostProcessorFOG::PostProcessorFOG(unsigned int fog, float nearD, float farD, bool frameTopDown)
+    : m_fog(fog), m_near(nearD), m_far(farD), m_topDown(frameTopDown) {}
 
-/* The frame (the display FBO) is top-down: pixel row y at memory row H-1-y;
-   the depth buffer's pixel row y at memory row y. */
+/* The frame is the display FBO (top-down: pixel row y at memory row H-1-y)
+   or, after setFBO, a texture (row y at memory row y); the depth buffer's
+   pixel row y is at memory row y. */
 void PostProcessorFOG::process(int threadIndex, int threadCount, PuresoftFBO* frame, PuresoftFBO* depth)
 {
     unsigned char* cbase = (unsigned char*)frame->getBuffer();
@@ -242,7 +244,7 @@ void PostProcessorFOG::process(int threadIndex, int threadCount, PuresoftFBO* fr
     const float range = m_far - m_near;
     for (int y = threadIndex; y < H; y += threadCount) {
         const float* drow = (const float*)(dbase + (size_t)y * depth->getScanline());
-        unsigned char* crow = cbase + (size_t)(H - 1 - y) * frame->getScanline();
+        unsigned char* crow = cbase + (size_t)(m_topDown ? H - 1 - y : y) * frame->getScanline();
         for (int x = 0; x < W; x++) {
             float t = (drow[x] - m_near) / range;
             t = t > 0.0f ? t : 0.0f;

@@ -126,10 +126,11 @@ private:
 class PostProcessorFOG : public PuresoftPostProcessor
 {
 public:
-    PostProcessorFOG(unsigned int fog, float nearD, float farD);
+    PostProcessorFOG(unsigned int fog, float nearD, float farD, bool frameTopDown = true);
     void process(int threadIndex, int threadCount, PuresoftFBO* frame, PuresoftFBO* depth);
 
 private:
     unsigned int m_fog;
     float m_near, m_far;
+    bool m_topDown;
 };

@@ -63,6 +63,9 @@ struct RefCtx {
     PuresoftPipeline* pipe;
     HeadlessRenderer* rndr;
     int width, height;
+    // setFBO with a texture: an FBO over the texture's own memory
+    // (PuresoftFBO's external-buffer form, fbo.cpp:11-45), owned here
+    PuresoftFBO* fboWrap[16] = {};
 };
 
 template <class F> int guarded(F f)
@@ -147,7 +150,30 @@ void ps3dr_destroy(void* h)
 {
     RefCtx* c = (RefCtx*)h;
     delete c->pipe; /* releases the renderer */
+    for (PuresoftFBO* f : c->fboWrap) delete f;
     delete c;
+}
+
+/* PuresoftPipeline::setFBO (pipeline.cpp:260-275) with texture `tex` (its
+   memory, wrapped as an FBO of the texture's layout, rows bottom-up as the
+   pipeline creates textures, tex.cpp:17) or -1 (slot 0: the display). */
+int ps3dr_set_fbo(void* h, int idx, int tex)
+{
+    RefCtx* c = (RefCtx*)h;
+    return guarded([&] {
+        PuresoftFBO* wrap = nullptr;
+        if (tex >= 0) {
+            PURESOFTIMGBUFF32 img;
+            c->pipe->getTexture(tex, &img);
+            wrap = new PuresoftFBO(img.width, img.scanline, img.height, img.elemLen, false, img.pixels);
+        }
+        c->pipe->setFBO(idx, wrap);
+        if (idx >= 0 && idx < 16) {
+            delete c->fboWrap[idx];
+            c->fboWrap[idx] = wrap;
+        }
+        return 0;
+    });
 }
 
 int ps3dr_thread_count(void) { return logicCPUs(); }
@@ -321,7 +347,7 @@ int ps3dr_post_process(void* h, int id, const void* params, size_t bytes)
         memcpy(&fog, params, 4);
         memcpy(&nearD, (const unsigned char*)params + 4, 4);
         memcpy(&farD, (const unsigned char*)params + 8, 4);
-        PostProcessorFOG pp(fog, nearD, farD);
+        PostProcessorFOG pp(fog, nearD, farD, c->fboWrap[0] == nullptr);
         return guarded([&] { c->pipe->postProcess(&pp); return 0; });
     }
     return -2;

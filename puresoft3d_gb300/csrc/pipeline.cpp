@@ -41,10 +41,11 @@ int selftest_occlusion(unsigned long long cases, unsigned long long* wrong, unsi
 void launch_raster(const PassParams& P, cudaStream_t s, int& launches, Prof* pr);
 void launch_selftest_wait(int* status, const int* flag, int spins, cudaStream_t s);
 void launch_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr);
-void launch_post_add8(uint32_t* colour, int width, int height, uint32_t add, const int* status, int seq,
+void launch_post_add8(uint32_t* row0, int pitch, int width, int height, uint32_t add, const int* status, int seq,
                       cudaStream_t s, int& launches, Prof* pr);
-void launch_post_fog(uint32_t* colour, int width, int height, const float* depth, int depthScan, uint32_t fog,
-                     float nearD, float farD, const int* status, int seq, cudaStream_t s, int& launches, Prof* pr);
+void launch_post_fog(uint32_t* row0, int pitch, int width, int height, const float* depth, int depthScan,
+                     uint32_t fog, float nearD, float farD, const int* status, int seq, cudaStream_t s, int& launches,
+                     Prof* pr);
 void launch_fill_u32(void* base, int width, int height, int pitchElems, uint32_t v, const int* status, int seq,
                      cudaStream_t s, int& launches, Prof* pr);
 }  // namespace ps3d
@@ -116,6 +117,7 @@ struct Command {
     int copyX, copyY, copyW, copyH;  // the rectangle, in pixels from the bottom-left corner
     size_t copyPitch;                // destination bytes per row (rows top-down)
     int depthTarget;  // -1 = default buffer
+    int colourTarget; // DRAW, POST: FBO slot 0's texture, -1 = the display (ps3d_set_fbo)
     int vpX, vpY, vpW, vpH;
     float depthValue;
     uint32_t colourValue;
@@ -240,6 +242,7 @@ struct ps3d_pipeline {
     int vpX = 0, vpY = 0;  // viewport origin in the targets (ps3d_set_viewport_rect)
     int behavior = B_UPDATE_DEPTH | B_TEST_DEPTH | B_FACE_CULLING;  // pipeline.cpp:34
     int depthTarget = -1;
+    int fbo[PS3D_MAX_FBOS];  // setFBO's slots: a texture index, -1 = none (slot 0: the display)
     int binW = 32;
     int rasterBlocks = 0;
     int cullSpans = 1;
@@ -622,6 +625,39 @@ int depth_target(ps3d_pipeline* p, int idx, Target& t)
     return 0;
 }
 
+// The colour target a command recorded (FBO slot 0): the display, rows
+// top-down, or a texture, rows bottom-up; `key` is its address for the
+// cross-stream hazards.
+struct ColourTarget {
+    uint32_t* row0;  // pixel row 0
+    int pitch;       // pixels from row y to row y + 1 (negative for the display)
+    int w, h;
+    const void* key;
+    bool display;
+};
+
+int colour_target(ps3d_pipeline* p, int idx, ColourTarget& c)
+{
+    if (idx < 0) {
+        c.row0 = (uint32_t*)p->colour + (size_t)(p->devH - 1) * p->devW;
+        c.pitch = -p->devW;
+        c.w = p->devW;
+        c.h = p->devH;
+        c.key = p->colour;
+        c.display = true;
+        return 0;
+    }
+    if (!tex_ok(p, idx)) return fail(PS3D_ERR_RANGE, "FBO texture %d was destroyed", idx);
+    const Texture& x = p->tex[idx];
+    c.row0 = (uint32_t*)x.dev;
+    c.pitch = x.scanline / 4;
+    c.w = x.width;
+    c.h = x.height;
+    c.key = x.dev;
+    c.display = false;
+    return 0;
+}
+
 // ---- cross-stream ordering (see Tracker)
 cudaEvent_t next_event(ps3d_pipeline* p)
 {
@@ -859,7 +895,11 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
 
     // A clear fuses into the pass when the pass covers the whole buffer.
     bool fuseDepth = ps.clearDepth && tg.w == W && tg.h == H && tg.scan == W;
-    bool fuseColour = ps.clearColour && p->devW == W && p->devH == H;
+    // clearColour clears the display (pipeline.cpp:340-343): fused only into
+    // a pass that draws into the display
+    ColourTarget ct;
+    if ((rc = colour_target(p, c0.colourTarget, ct))) return rc;
+    bool fuseColour = ps.clearColour && ct.display && p->devW == W && p->devH == H;
     if (ps.clearDepth && !fuseDepth && (rc = fill_depth(p, c0.depthTarget, ps.depthValue))) return rc;
     if (ps.clearColour && !fuseColour && (rc = fill_colour(p, ps.colourValue))) return rc;
 
@@ -906,9 +946,10 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     P.depthW = tg.w;
     P.depthH = tg.h;
     P.shadeList = x.shadeList;
-    P.colour = p->colour;
-    P.colourW = p->devW;
-    P.colourH = p->devH;
+    P.colourRow0 = ct.row0;
+    P.colourPitch = ct.pitch;
+    P.colourW = ct.w;
+    P.colourH = ct.h;
     P.clearDepth = fuseDepth;
     P.clearColour = fuseColour;
     P.anyColour = anyColour;
@@ -931,23 +972,23 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     std::vector<const void*> sampled;
     if (anyColour || forward) sampled_targets(p, uu, sampled);
     if ((rc = before_write(p, s, tg.depth))) return rc;
-    if (rasterColour && (rc = before_write(p, s, p->colour))) return rc;
+    if (rasterColour && (rc = before_write(p, s, ct.key))) return rc;
     if (forward)
         for (const void* t : sampled)
             if ((rc = before_read(p, s, t))) return rc;
     launch_raster(P, s, launches, &p->prof);
     if ((rc = mark(p, s, e))) return rc;
     wrote(p, tg.depth, e);
-    if (rasterColour) wrote(p, p->colour, e);
+    if (rasterColour) wrote(p, ct.key, e);
     if (forward)
         for (const void* t : sampled) read_by(p, t, e);
     if (anyColour && !forward) {
-        if ((rc = before_write(p, s, p->colour))) return rc;
+        if ((rc = before_write(p, s, ct.key))) return rc;
         for (const void* t : sampled)
             if ((rc = before_read(p, s, t))) return rc;
         launch_shade(P, s, launches, &p->prof);
         if ((rc = mark(p, s, e))) return rc;
-        wrote(p, p->colour, e);
+        wrote(p, ct.key, e);
         for (const void* t : sampled) read_by(p, t, e);
     }
     CU(cudaGetLastError());
@@ -998,7 +1039,9 @@ int plan_commands(const std::vector<Command>& cmds, size_t from, PassFn onPass, 
             break;
         }
         size_t k = j;
-        while (k < n && cmds[k].kind == Command::DRAW && cmds[k].depthTarget == cmds[j].depthTarget) k++;
+        while (k < n && cmds[k].kind == Command::DRAW && cmds[k].depthTarget == cmds[j].depthTarget &&
+               cmds[k].colourTarget == cmds[j].colourTarget)
+            k++;
         if (ps.clearDepth && depthClearTarget != cmds[j].depthTarget) {
             if ((rc = onFill(depthClearTarget, ps.depthValue, 0u))) return rc;
             ps.clearDepth = false;
@@ -1020,29 +1063,31 @@ int plan_commands(const std::vector<Command>& cmds, size_t from, PassFn onPass, 
 int post_process(ps3d_pipeline* p, const Command& c, bool tracked)
 {
     Target t = {};
-    int rc = 0;
+    ColourTarget ct;
+    int rc = colour_target(p, c.colourTarget, ct);
+    if (rc) return rc;
     if (c.postId == PP_FOG) {
         if ((rc = depth_target(p, c.depthTarget, t))) return rc;
-        if (t.w < p->devW || t.h < p->devH || t.scan < p->devW)
-            return fail(PS3D_ERR_INVALID, "the fog post-process needs a depth buffer of at least %dx%d", p->devW, p->devH);
+        if (t.w < ct.w || t.h < ct.h || t.scan < ct.w)
+            return fail(PS3D_ERR_INVALID, "the fog post-process needs a depth buffer of at least %dx%d", ct.w, ct.h);
     }
     if (tracked) {
-        if ((rc = wait_event(p->stream, p->trk.lastEmit)) || (rc = before_write(p, p->stream, p->colour))) return rc;
+        if ((rc = wait_event(p->stream, p->trk.lastEmit)) || (rc = before_write(p, p->stream, ct.key))) return rc;
         if (t.depth && (rc = before_read(p, p->stream, t.depth))) return rc;
     }
     int launches = 0;
     if (c.postId == PP_ADD8)
-        launch_post_add8((uint32_t*)p->colour, p->devW, p->devH, c.postColour, p->status, gap_seq(p), p->stream,
-                         launches, &p->prof);
+        launch_post_add8(ct.row0, ct.pitch, ct.w, ct.h, c.postColour, p->status, gap_seq(p), p->stream, launches,
+                         &p->prof);
     else
-        launch_post_fog((uint32_t*)p->colour, p->devW, p->devH, t.depth, t.scan, c.postColour, c.postNear, c.postFar,
+        launch_post_fog(ct.row0, ct.pitch, ct.w, ct.h, t.depth, t.scan, c.postColour, c.postNear, c.postFar,
                         p->status, gap_seq(p), p->stream, launches, &p->prof);
     CU(cudaGetLastError());
     p->stats.kernel_launches += launches;
     if (tracked) {
         cudaEvent_t e;
         if ((rc = mark(p, p->stream, e))) return rc;
-        wrote(p, p->colour, e);
+        wrote(p, ct.key, e);
         if (t.depth) read_by(p, t.depth, e);
     }
     return 0;
@@ -1185,6 +1230,7 @@ int ps3d_pipeline_create(int width, int height, void* stream, ps3d_pipeline** ou
     if (!p) return fail(PS3D_ERR_NOMEM, "host allocation failed");
     p->devW = p->W = width;
     p->devH = p->H = height;
+    for (int& f : p->fbo) f = -1;  // setFBO(0, NULL) in the constructor (pipeline.cpp:49)
     if (cudaGetDevice(&p->device) != cudaSuccess) {
         delete p;
         return fail(PS3D_ERR_DEVICE, "cudaGetDevice failed");
@@ -1360,6 +1406,8 @@ int ps3d_texture_destroy(ps3d_pipeline* p, int idx)
     int rc = do_finish(p);
     if (rc) return rc;
     if (p->depthTarget == idx) p->depthTarget = -1;
+    for (int& f : p->fbo)
+        if (f == idx) f = -1;  // slot 0 falls back to the display
     for (auto* cb : p->cmdbufs) cb->stale = true;
     cudaFree(p->tex[idx].dev);
     p->tex[idx] = Texture();
@@ -1620,6 +1668,7 @@ int ps3d_clear_depth(ps3d_pipeline* p, float v)
     Command c;
     memset(&c, 0, sizeof c);
     c.kind = Command::CLEAR_DEPTH;
+    c.colourTarget = -1;
     c.depthTarget = p->depthTarget;
     c.depthValue = v;
     (p->recording ? p->recording->cmds : p->pending).push_back(c);
@@ -1632,6 +1681,7 @@ int ps3d_clear_colour(ps3d_pipeline* p, uint32_t bgra)
     Command c;
     memset(&c, 0, sizeof c);
     c.kind = Command::CLEAR_COLOUR;
+    c.colourTarget = -1;
     c.depthTarget = p->depthTarget;
     c.colourValue = bgra;
     (p->recording ? p->recording->cmds : p->pending).push_back(c);
@@ -1648,6 +1698,7 @@ int ps3d_draw(ps3d_pipeline* p, int vao)
     memset(&c, 0, sizeof c);
     c.kind = Command::DRAW;
     c.depthTarget = p->depthTarget;
+    c.colourTarget = p->fbo[0];
     c.vpX = p->vpX;
     c.vpY = p->vpY;
     c.vpW = p->W;
@@ -1696,8 +1747,12 @@ int ps3d_draw(ps3d_pipeline* p, int vao)
     if ((rc = depth_target(p, p->depthTarget, tg))) return rc;
     if (tg.w < p->vpX + p->W || tg.h < p->vpY + p->H)
         return fail(PS3D_ERR_INVALID, "the viewport rectangle is not inside the depth target");
-    if ((d.flags & F_COLOUR) && (p->devW < p->vpX + p->W || p->devH < p->vpY + p->H))
-        return fail(PS3D_ERR_INVALID, "the viewport rectangle is not inside the colour buffer");
+    if (d.flags & F_COLOUR) {
+        ColourTarget ct;
+        if ((rc = colour_target(p, c.colourTarget, ct))) return rc;
+        if (ct.w < p->vpX + p->W || ct.h < p->vpY + p->H)
+            return fail(PS3D_ERR_INVALID, "the viewport rectangle is not inside the colour target");
+    }
     (p->recording ? p->recording->cmds : p->pending).push_back(c);
     p->stats.draws++;
     return 0;
@@ -1718,6 +1773,20 @@ int ps3d_set_row_split(ps3d_pipeline* p, int blocksPerBin)
     if (blocksPerBin != 1 && blocksPerBin != 2 && blocksPerBin != 4 && blocksPerBin != 8)
         return fail(PS3D_ERR_INVALID, "blocks per bin must be 1, 2, 4 or 8");
     p->rowSplit = blocksPerBin;
+    return 0;
+}
+
+int ps3d_set_fbo(ps3d_pipeline* p, int idx, int texture)
+{
+    if (!p) return fail(PS3D_ERR_INVALID, "null pipeline");
+    if (idx < 0 || idx >= PS3D_MAX_FBOS) return fail(PS3D_ERR_RANGE, "setFBO");
+    if (texture != -1) {
+        if (!tex_ok(p, texture)) return fail(PS3D_ERR_RANGE, "setFBO: texture %d", texture);
+        const Texture& t = p->tex[texture];
+        if (t.elemLen != 4 || t.scanline % 4)
+            return fail(PS3D_ERR_INVALID, "setFBO: the processors write 4-byte BGRA elements");
+    }
+    p->fbo[idx] = texture;
     return 0;
 }
 
@@ -1803,6 +1872,7 @@ int ps3d_read_colour_device(ps3d_pipeline* p, void* devDst)
     Command c;
     memset(&c, 0, sizeof c);
     c.kind = Command::COPY_COLOUR;
+    c.colourTarget = -1;
     c.depthTarget = p->depthTarget;
     c.copyDst = devDst;
     c.copyW = p->devW;
@@ -1822,6 +1892,7 @@ int ps3d_copy_colour_rect(ps3d_pipeline* p, int x, int y, int width, int height,
     Command c;
     memset(&c, 0, sizeof c);
     c.kind = Command::COPY_COLOUR;
+    c.colourTarget = -1;
     c.depthTarget = p->depthTarget;
     c.copyDst = dst;
     c.copyX = x;
@@ -1840,6 +1911,7 @@ int ps3d_post_process(ps3d_pipeline* p, int postProcessorId, const void* params,
     memset(&c, 0, sizeof c);
     c.kind = Command::POST;
     c.depthTarget = p->depthTarget;
+    c.colourTarget = p->fbo[0];
     c.postId = postProcessorId;
     switch (postProcessorId) {
     case PP_ADD8:
@@ -1855,10 +1927,11 @@ int ps3d_post_process(ps3d_pipeline* p, int postProcessorId, const void* params,
         memcpy(&c.postNear, (const uint8_t*)params + 4, 4);
         memcpy(&c.postFar, (const uint8_t*)params + 8, 4);
         Target t;
+        ColourTarget ct;
         int rc = depth_target(p, c.depthTarget, t);
-        if (rc) return rc;
-        if (t.w < p->devW || t.h < p->devH || t.scan < p->devW)
-            return fail(PS3D_ERR_INVALID, "the fog post-process needs a depth buffer of at least %dx%d", p->devW, p->devH);
+        if (rc || (rc = colour_target(p, c.colourTarget, ct))) return rc;
+        if (t.w < ct.w || t.h < ct.h || t.scan < ct.w)
+            return fail(PS3D_ERR_INVALID, "the fog post-process needs a depth buffer of at least %dx%d", ct.w, ct.h);
         break;
     }
     default: return fail(PS3D_ERR_INVALID, "unknown post-processor 0x%04x", postProcessorId);
@@ -2307,7 +2380,9 @@ int noalloc_run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const P
     p->stats.upload_bytes += s.nd * (sizeof(DrawDesc) + sizeof(DrawUniforms));
 
     bool fuseDepth = ps.clearDepth && s.tg.scan == W;
-    bool fuseColour = ps.clearColour && p->devW == W && p->devH == H;
+    ColourTarget ct;
+    if ((rc = colour_target(p, c0.colourTarget, ct))) return rc;
+    bool fuseColour = ps.clearColour && ct.display && p->devW == W && p->devH == H;
     if (ps.clearDepth && !fuseDepth && (rc = fill_depth_plain(p, c0.depthTarget, ps.depthValue))) return rc;
     if (ps.clearColour && !fuseColour && (rc = fill_colour_plain(p, ps.colourValue))) return rc;
 
@@ -2354,9 +2429,10 @@ int noalloc_run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const P
     P.depthW = s.tg.w;
     P.depthH = s.tg.h;
     P.shadeList = s.anyColour ? (int2*)(base + L.shadeList) : nullptr;
-    P.colour = p->colour;
-    P.colourW = p->devW;
-    P.colourH = p->devH;
+    P.colourRow0 = ct.row0;
+    P.colourPitch = ct.pitch;
+    P.colourW = ct.w;
+    P.colourH = ct.h;
     P.clearDepth = fuseDepth;
     P.clearColour = fuseColour;
     P.anyColour = s.anyColour;

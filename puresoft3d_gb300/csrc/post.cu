@@ -9,8 +9,9 @@
 // it does nothing once an earlier pass of its launch has failed (the
 // failed frame is replayed whole).
 //
-// Layout: colour BGRA8 with memory row H-1-y holding pixel row y (the
-// display FBO is top-down), depth FP32 with row y at y * depthScan.
+// Layout: the colour target (FBO slot 0: the display, whose memory row
+// H-1-y holds pixel row y, or a texture, row y at y) as its first pixel
+// row and a signed row pitch; depth FP32 with row y at y * depthScan.
 #include "ps3d_internal.h"
 #include "device_common.cuh"
 
@@ -20,12 +21,13 @@ namespace ps3d {
 // (the paddb of the reference demo's post-processor, test2/testpost.cpp:9-43).
 // 16 bytes per thread (4 pixels, SIMD within a register); the ragged end of a
 // row, when the width is not a multiple of 4, by single pixels.
-__global__ void k_post_add8(uint32_t* colour, int width, int height, uint32_t add, const int* status, int seq)
+__global__ void k_post_add8(uint32_t* row0, int pitch, int width, int height, uint32_t add, const int* status,
+                            int seq)
 {
     if (pass_failed(status, seq)) return;
     const int y = blockIdx.y;
     const int quads = width >> 2;
-    uint32_t* row = colour + (size_t)y * width;
+    uint32_t* row = row0 + (ptrdiff_t)y * pitch;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < quads + (width & 3); q += gridDim.x * blockDim.x) {
         if (q < quads && (((uintptr_t)row & 15) == 0)) {
             uint4 v = ((uint4*)row)[q];
@@ -47,14 +49,14 @@ __global__ void k_post_add8(uint32_t* colour, int width, int height, uint32_t ad
 // PS3D_PP_FOG: linear depth fog.  t = (d - near) / (far - near) clamped to
 // [0, 1]; each of B, G, R becomes (unsigned char)(c + (f - c) * t) with the
 // fog colour f; alpha is kept.  IEEE operations in this order.
-__global__ void k_post_fog(uint32_t* colour, int width, int height, const float* depth, int depthScan, uint32_t fog,
-                           float nearD, float farD, const int* status, int seq)
+__global__ void k_post_fog(uint32_t* row0, int pitch, int width, int height, const float* depth, int depthScan,
+                           uint32_t fog, float nearD, float farD, const int* status, int seq)
 {
     if (pass_failed(status, seq)) return;
     const int y = blockIdx.y;
     const float range = fsub(farD, nearD);
     const float* drow = depth + (size_t)y * depthScan;
-    uint32_t* crow = colour + (size_t)(height - 1 - y) * width;
+    uint32_t* crow = row0 + (ptrdiff_t)y * pitch;
     for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < width; x += gridDim.x * blockDim.x) {
         float t = fdiv(fsub(drow[x], nearD), range);
         t = t > 0.0f ? t : 0.0f;  // NaN -> 0
@@ -72,22 +74,23 @@ __global__ void k_post_fog(uint32_t* colour, int width, int height, const float*
 
 static inline int ceil_div_post(int a, int b) { return (a + b - 1) / b; }
 
-void launch_post_add8(uint32_t* colour, int width, int height, uint32_t add, const int* status, int seq,
+void launch_post_add8(uint32_t* row0, int pitch, int width, int height, uint32_t add, const int* status, int seq,
                       cudaStream_t s, int& launches, Prof* pr)
 {
     pr->begin(K_POST, s);
     const int items = (width >> 2) + (width & 3);
-    k_post_add8<<<dim3(ceil_div_post(items, 128), height), 128, 0, s>>>(colour, width, height, add, status, seq);
+    k_post_add8<<<dim3(ceil_div_post(items, 128), height), 128, 0, s>>>(row0, pitch, width, height, add, status, seq);
     pr->end(s);
     launches++;
 }
 
-void launch_post_fog(uint32_t* colour, int width, int height, const float* depth, int depthScan, uint32_t fog,
-                     float nearD, float farD, const int* status, int seq, cudaStream_t s, int& launches, Prof* pr)
+void launch_post_fog(uint32_t* row0, int pitch, int width, int height, const float* depth, int depthScan,
+                     uint32_t fog, float nearD, float farD, const int* status, int seq, cudaStream_t s, int& launches,
+                     Prof* pr)
 {
     pr->begin(K_POST, s);
-    k_post_fog<<<dim3(ceil_div_post(width, 256), height), 256, 0, s>>>(colour, width, height, depth, depthScan, fog,
-                                                                       nearD, farD, status, seq);
+    k_post_fog<<<dim3(ceil_div_post(width, 256), height), 256, 0, s>>>(row0, pitch, width, height, depth, depthScan,
+                                                                       fog, nearD, farD, status, seq);
     pr->end(s);
     launches++;
 }

@@ -16,10 +16,16 @@ __device__ __forceinline__ void bin_range(const PassParams& P, int bin, int& sta
     end = r.x < r.y ? r.y : 0;
 }
 
-// The pass's clear colour at target pixel (x, y) (colour rows top-down).
+// The colour target's pixel (x, y).
+__device__ __forceinline__ uint32_t* colour_px(const PassParams& P, int x, int y)
+{
+    return P.colourRow0 + (ptrdiff_t)y * P.colourPitch + x;
+}
+
+// The pass's clear colour at target pixel (x, y).
 __device__ __forceinline__ void clear_colour_px(const PassParams& P, int x, int y)
 {
-    ((uint32_t*)P.colour)[(size_t)(P.colourH - 1 - y) * P.colourW + x] = P.colourClearValue;
+    *colour_px(P, x, y) = P.colourClearValue;
 }
 
 // True when no pixel kA..kB (steps from leftClamped) of a span can pass a

@@ -318,7 +318,7 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
             uint32_t col = P.colourClearValue;
             int x = x0 + c, y = y0 + r;
             if (!P.clearColour && r >= rowBeg && r < rowEnd && c < cols && x < P.colourW && y < P.colourH)
-                col = ((const uint32_t*)P.colour)[(size_t)(P.colourH - 1 - y) * P.colourW + x];
+                col = *colour_px(P, x, y);
             sCol[r * S + c] = col;
         }
     }
@@ -585,7 +585,7 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
             for (int i = tid; i < nr * cols; i += kRasterThreads) {
                 int r = rowBeg + i / cols, c = i - (r - rowBeg) * cols, x = x0 + c, y = y0 + r;
                 if (x < P.colourW && y < P.colourH)
-                    ((uint32_t*)P.colour)[(size_t)(P.colourH - 1 - y) * P.colourW + x] = sCol[r * S + c];
+                    *colour_px(P, x, y) = sCol[r * S + c];
             }
         covered = 0;  // nothing is left to shade
     } else if (P.anyColour || P.clearColour) {
@@ -650,7 +650,7 @@ template <int FPK>
 __device__ __forceinline__ void shade_entry(const PassParams& P, int2 e)
 {
     const int y = e.x / P.W, x = e.x - y * P.W, w = e.y;
-    uint32_t* dst = (uint32_t*)P.colour + (size_t)(P.colourH - 1 - y) * P.colourW + x;
+    uint32_t* dst = colour_px(P, x, y);
     TriRaster t;
     {
         const float4* src = (const float4*)(P.tris + w);

@@ -53,6 +53,7 @@ _SIGS = {
     "ps3d_vbo_detach": [_c_void_p, _c_int, _c_int],
     "ps3d_set_uniform": [_c_void_p, _c_int, _c_void_p, _c_size_t],
     "ps3d_set_depth": [_c_void_p, _c_int],
+    "ps3d_set_fbo": [_c_void_p, _c_int, _c_int],
     "ps3d_set_viewport": [_c_void_p, _c_int, _c_int],
     "ps3d_set_viewport_rect": [_c_void_p, _c_int, _c_int, _c_int, _c_int],
     "ps3d_enable": [_c_void_p, _c_int],
@@ -260,6 +261,11 @@ class PuresoftPipeline:
 
     def setDepth(self, idx=-1):
         self._check(self.lib.ps3d_set_depth(self.h, idx))
+
+    def setFBO(self, idx, texture=-1):
+        """setFBO(idx, fbo): a texture as FBO slot idx (-1: none; slot 0 then
+        the display).  Draws colour slot 0; clearColour clears the display."""
+        self._check(self.lib.ps3d_set_fbo(self.h, idx, texture))
 
     def setViewport(self, w, h):
         self._check(self.lib.ps3d_set_viewport(self.h, w, h))

@@ -21,6 +21,8 @@ def render(pipe, scene):
     out = {"colour": pipe.readColour(), "depth": pipe.readDepthTexture(scene.info["depth_texture"])}
     if "shadow_texture" in scene.info:
         out["shadow"] = pipe.readDepthTexture(scene.info["shadow_texture"])
+    for t in scene.info.get("read_textures", []):  # textures a scene renders into (setFBO)
+        out["tex%d" % t] = pipe.readTexture(t)
     return out
 
 

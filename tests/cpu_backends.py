@@ -39,6 +39,7 @@ _API = [
     ("vbo_attach", [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
     ("set_uniform", [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]),
     ("set_depth", [ctypes.c_int]),
+    ("set_fbo", [ctypes.c_int, ctypes.c_int]),
     ("set_viewport", [ctypes.c_int, ctypes.c_int]),
     ("enable", [ctypes.c_int]),
     ("disable", [ctypes.c_int]),
@@ -125,6 +126,9 @@ class _CPipeline:
 
     def setDepth(self, idx=-1):
         self._call("set_depth", idx)
+
+    def setFBO(self, idx, tex=-1):
+        self._call("set_fbo", idx, tex)
 
     def setViewport(self, w, h):
         self._call("set_viewport", w, h)

@@ -79,6 +79,8 @@ def render(pipe_cls, scene):
     out = {"colour": p.readColour(), "depth": p.readDepthTexture(scene.info["depth_texture"])}
     if "shadow_texture" in scene.info:
         out["shadow"] = p.readDepthTexture(scene.info["shadow_texture"])
+    for t in scene.info.get("read_textures", []):
+        out["tex%d" % t] = p.readTexture(t)
     p.close()
     return out
 
@@ -98,6 +100,10 @@ def main():
                "covered": int((out["depth"] < 1.0).sum())}
         if "shadow" in out:
             rec["shadow_sha"] = sha(out["shadow"])
+        for k in out:
+            if k.startswith("tex"):
+                rec[k + "_sha"] = sha(out[k])
+                rec[k] = out[k]
         if name.startswith("kat_"):
             rec["colour"] = out["colour"]
             rec["depth"] = out["depth"]

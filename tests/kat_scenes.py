@@ -196,6 +196,51 @@ def _post_scene(name, w, h, seed):
     return S.Scene(name, w, h, b.setup, b.frame, {"triangles": 300, "depth_texture": depth})
 
 
+def _setfbo_scene(name, w, h, seed):
+    """Render to texture through setFBO (pipeline.cpp:260-275): a soup drawn
+    into a 64x48 BGRA8 texture bound as FBO slot 0 (rows bottom-up, its
+    seeded contents where nothing is drawn), the demo's add and depth fog
+    post-processed on it (postProcess runs on slot 0, post.cpp:14), and a
+    blended soup over it; clearColour meanwhile clears the display only
+    (pipeline.cpp:340-343).  Then slot 0 back to the display and a second
+    soup drawn there sampling the texture.  Colour, depth and the texture
+    are compared."""
+    b = S._Builder()
+    rng = np.random.default_rng(seed)
+    src = b.texture(_alpha_texture(seed))
+    tw, th = 64, 48
+    target = b.texture(S.checker_noise_bgra(64, 8, rng, noise=40)[:th], wrap=True)
+    d1, d2 = b.empty_texture(tw, th), b.empty_texture(w, h)
+    m1, m2, m3 = (_tri_mesh(random_soup(120, seed + k)) for k in range(3))
+    prog = b.programme(S.VP_DEF01, S.IP_DEF01, S.FP_LIT1)
+    v1, v2, v3 = (b.vao(m, slots=(0, 3, 4)) for m in (m1, m2, m3))
+    eye = np.eye(4)
+    b.f("setDepth", d1)
+    b.f("clearDepth", 1.0)
+    b.f("setFBO", 0, target)
+    b.f("clearColour", 0xFF204060)  # the display, not the texture
+    b.f("setViewport", tw, th)
+    b.f("useProgramme", prog)
+    for slot in (3, 4, 5):
+        b.f("setUniform", slot, S.col_major(eye))
+    b.f("setUniform", 7, S.vec4(0.3, 0.5, 0.81))
+    b.f("setUniform", 8, S.vec4(0, 0, 2, 1))
+    b.f("setUniform", 9, np.array([src], dtype=np.int32))
+    b.f("drawVAO", v1)
+    b.f("postProcess", S.PP_ADD8, S.add8_params(30, 5, 200, 9))
+    b.f("postProcess", S.PP_FOG, S.fog_params(0xFF40C080, -0.3, 0.8))
+    b.f("enable", S.ALPHABLEND)
+    b.f("drawVAO", v2)
+    b.f("disable", S.ALPHABLEND)
+    b.f("setFBO", 0, -1)
+    b.f("setDepth", d2)
+    b.f("clearDepth", 1.0)
+    b.f("setViewport", w, h)
+    b.f("setUniform", 9, np.array([target], dtype=np.int32))
+    b.f("drawVAO", v3)
+    return S.Scene(name, w, h, b.setup, b.frame, {"triangles": 360, "depth_texture": d2, "read_textures": [target]})
+
+
 def _planet_scene(name, w, h, seed, fp, blend=False):
     """The reference demo's planet processors (test/testproc.cpp) with the
     projective 4-tap Poisson shadow lookup (samplrproj.cpp): a depth-only
@@ -434,6 +479,8 @@ def kat_scenes():
                                                                _rot(-2.6, 1.05, -0.5), 32, False, blend=True)))
     # the post-processing hook between passes
     out.append(("kat_post_add_fog_96x64", _post_scene("kat_post_add_fog", 96, 64, 22)))
+    # render to texture through setFBO, then sampling it
+    out.append(("kat_setfbo_rtt_96x64", _setfbo_scene("kat_setfbo_rtt", 96, 64, 28)))
     # the reference demo's planet processors with the projective shadow lookup
     out.append(("kat_def0_planet_earth_96x64", _planet_scene("kat_planet_earth", 96, 64, 23, S.FP_EARTH)))
     out.append(("kat_def0_planet_satellite_80x60", _planet_scene("kat_planet_satellite", 80, 60, 24, S.FP_SATELLITE)))

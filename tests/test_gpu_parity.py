@@ -34,6 +34,10 @@ def test_gpu_matches_oracle(name, scene, gpu_lib):
     # device's acosf / cosf where the reference build has glibc's
     if "viewer" not in name:
         assert sha(gpu["colour"]) == str(g["colour_sha"]), name + ": colour differs from the reference build"
+    for k in ora:
+        if k.startswith("tex"):  # a texture the scene rendered into through setFBO
+            assert np.array_equal(gpu[k], ora[k]), name + " " + k
+            assert sha(gpu[k]) == str(g[k + "_sha"]), name + " " + k
 
 
 @pytest.mark.gpu

@@ -35,6 +35,9 @@ def test_oracle_matches_golden(name, scene):
     assert sha(out["colour"]) == str(g["colour_sha"]), name
     if "shadow_sha" in g:
         assert sha(out["shadow"]) == str(g["shadow_sha"]), name
+    for k in out:
+        if k.startswith("tex"):  # a texture the scene rendered into
+            assert sha(out[k]) == str(g[k + "_sha"]), name + " " + k
     assert int((out["depth"] < 1.0).sum()) == int(g["covered"])
 
 
