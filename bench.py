@@ -75,13 +75,15 @@ CONFIGS = {
 }
 
 
-# DRAM bytes (read + write) of one raster launch on each workload at its
-# pinned schedule, from one ncu capture of the same kernel on the same
-# full-size workload (one-pass metrics dram__bytes_read.sum and
-# dram__bytes_write.sum, every raster launch of two immediate-path frames:
+# DRAM bytes (read + write) of one launch of a kernel class on each workload
+# at its pinned schedule, from one ncu capture of the same kernels on the
+# same full-size workload (one-pass metrics dram__bytes_read.sum and
+# dram__bytes_write.sum, every launch of two immediate-path frames:
 # bench.py --config cN --ncu-frames 2); averages over the launches that ran
-# to completion.
-RASTER_TRAFFIC = {"c1": 77696, "c2": 5204672, "c3": 113905024, "c4": 778335744}
+# to completion.  c4's are the immediate path's (one launch per frame over
+# the whole atlas), the same kernels as the batched pass.
+KERNEL_TRAFFIC = {"c1": {"raster": 77696}, "c2": {"raster": 5204672}, "c3": {"raster": 113905024},
+                  "c4": {"raster": 821472512}}
 
 
 def peaks():
@@ -425,7 +427,7 @@ def run_c4(args):
     plain_graph_ips = views / (statistics.median(pg_ms) / 1e3)
 
     roof = dominant_roofline(prof, prof_frames, batched, counts, tune["bin_width"],
-                             RASTER_TRAFFIC.get("c4") if views == 4096 else None)
+                             KERNEL_TRAFFIC.get("c4", {}) if views == 4096 else {})
     line = {
         "metric": "images/s", "value": round(ips, 2), "unit": "images/s", "n_gpus": WORLD,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4),
@@ -629,7 +631,9 @@ def kernel_bytes_per_frame(kind, scene, counts, bin_w):
 def dominant_roofline(prof, prof_frames, scene, counts, bin_w, traffic):
     """The roofline object for the kernel class with the largest event-timed
     share: achieved = its algorithmic bytes per launch / its mean launch
-    time, against the measured HBM copy bandwidth."""
+    time, against the measured HBM copy bandwidth; traffic = the captured
+    DRAM bytes per launch of that class (`traffic`: class -> bytes), when
+    captured."""
     dom = max(prof, key=lambda k: prof[k][1])
     n_launch, ms = prof[dom]
     avg_ms = ms / max(n_launch, 1)
@@ -641,7 +645,7 @@ def dominant_roofline(prof, prof_frames, scene, counts, bin_w, traffic):
             "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5) if achieved else None,
             "peak_source": peak_kind, "avg_launch_ms": round(avg_ms, 5),
             "bytes_per_launch": round(bytes_per_launch) if bytes_per_launch else None,
-            "traffic": traffic if dom == "raster" else None}
+            "traffic": traffic.get(dom)}
 
 
 def run_ours(args):
@@ -727,7 +731,7 @@ def run_ours(args):
 
     fps = aggregate(args.steps * K, total_ms / 1e3)
     fps_e2e = aggregate(args.steps * K, e2e_s)
-    roof = dominant_roofline(prof, prof_frames, scene, counts, tune["bin_width"], RASTER_TRAFFIC.get(args.config))
+    roof = dominant_roofline(prof, prof_frames, scene, counts, tune["bin_width"], KERNEL_TRAFFIC.get(args.config, {}))
     line = {
         "metric": "frames/s", "value": round(fps, 3), "unit": "frames/s", "n_gpus": WORLD,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4),

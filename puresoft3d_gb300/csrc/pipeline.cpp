@@ -804,6 +804,18 @@ int pass_fp(const DrawDesc* dd, size_t n)
     return fp < 0 ? 0 : fp;
 }
 
+int pass_vp(const DrawDesc* dd, size_t n)
+{
+    int vp = -1;
+    for (size_t i = 0; i < n; i++) {
+        const DrawDesc& d = dd[i];
+        if (!(d.flags & F_COLOUR)) continue;
+        if (vp == -1) vp = d.vp;
+        else if (vp != d.vp) return 0;
+    }
+    return vp < 0 ? 0 : vp;
+}
+
 void pass_descriptors(const std::vector<Command>& cmds, const Pass& ps, std::vector<DrawDesc>& dd,
                       std::vector<DrawUniforms>& uu, int& nTris, int& nvMax, bool& anyColour)
 {
@@ -915,6 +927,7 @@ int run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const Pass& ps,
     P.spanItems = spanItems;
     P.spans = spanItems ? x.spans : nullptr;
     P.passFp = pass_fp(dd.data(), dd.size());
+    P.passVp = pass_vp(dd.data(), dd.size());
     P.forward = forward;
     P.binsX = binsX;
     P.binsY = binsY;
@@ -2396,6 +2409,7 @@ int noalloc_run_pass(ps3d_pipeline* p, const std::vector<Command>& cmds, const P
     P.rowSplit = p->rowSplit;
     P.warpBins = p->warpBins;
     P.passFp = pass_fp(g_noallocDraws, (size_t)s.nd);
+    P.passVp = pass_vp(g_noallocDraws, (size_t)s.nd);
     P.spanItems = s.spanItems;
     P.spans = s.spanItems ? (SpanItem*)(base + L.spans) : nullptr;
     P.forward = s.forward;

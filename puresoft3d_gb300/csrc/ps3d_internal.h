@@ -129,6 +129,7 @@ struct PassParams {
     int spanItems;            // 1 = short triangles are binned as set-up span items (no forward passes)
     SpanItem* spans;          // span items, by emission index (capacity pairCap)
     int passFp;               // the fragment processor every colour draw of the pass uses, else 0
+    int passVp;               // the vertex processor every colour draw of the pass uses, else 0
     int forward;              // some draw blends or may discard: shade every passing fragment in order
     int nTris, nDraws;
     const DrawDesc* draws;

@@ -103,7 +103,7 @@ __device__ __forceinline__ void vary_begin(const TriRaster& t, const float* vary
 // Set-up with the vertex varyings computed here (a pass whose set-up
 // deferred them): the draw's vertex processor on the triangle's three
 // vertices, each product added in vertex order as above.
-template <int NV>
+template <int NV, int VPK>
 __device__ __forceinline__ void vary_begin_lazy(const DrawDesc& d, const DrawUniforms& U, int lt, const Span& s,
                                                 const SpanZ& z, VaryState<NV>& v, bool nstep = false)
 {
@@ -111,7 +111,7 @@ __device__ __forceinline__ void vary_begin_lazy(const DrawDesc& d, const DrawUni
 #pragma unroll 1
     for (int vtx = 0; vtx < 3; vtx++) {
         float a[kMaxVary];
-        vp_varyings(d, U, 3 * lt + vtx, a);
+        vp_varyings<VPK>(d, U, 3 * lt + vtx, a);
         const float cl = vtx == 0 ? z.cl[0] : (vtx == 1 ? z.cl[1] : z.cl[2]);
         const float cr = vtx == 0 ? z.cr[0] : (vtx == 1 ? z.cr[1] : z.cr[2]);
 #pragma unroll
@@ -146,14 +146,17 @@ template <int NV> __device__ __forceinline__ void vary_out(const VaryState<NV>& 
 }
 
 // Varyings of the shade-list fragment at x of triangle w (its record t):
-// from the stored vertex varyings, or computed from the vertices.
-template <int NV>
+// from the stored vertex varyings (LAZY = 0), or computed from the vertices
+// (a pass whose set-up deferred them; LAZY = the pass's vertex processor, -1
+// any).  Separate kernels, so that the stored-varyings ones keep their
+// registers.
+template <int NV, int LAZY>
 __device__ __forceinline__ void shade_varyings(const PassParams& P, const DrawDesc& d, const DrawUniforms& U, int w,
                                                const TriRaster& t, const Span& s, const SpanZ& z, int x, float out[NV],
                                                bool nstep = false)
 {
     VaryState<NV> v;
-    if (P.lazyVary) vary_begin_lazy<NV>(d, U, w - d.triBase, s, z, v, nstep);
+    if constexpr (LAZY != 0) vary_begin_lazy<NV, (LAZY > 0 ? LAZY : 0)>(d, U, w - d.triBase, s, z, v, nstep);
     else vary_begin<NV>(t, P.vary + (size_t)w * 3 * P.nvMax, P.nvMax, s, z, v, nstep);
     vary_advance<NV>(v, x);
     vary_out<NV>(v, out);
@@ -646,7 +649,7 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
 
 // FPK: the fragment processor when every draw of the pass uses the same
 // one (a kernel with only that shader's registers), else 0 (any).
-template <int FPK>
+template <int FPK, int LAZY>
 __device__ __forceinline__ void shade_entry(const PassParams& P, int2 e)
 {
     const int y = e.x / P.W, x = e.x - y * P.W, w = e.y;
@@ -670,25 +673,25 @@ __device__ __forceinline__ void shade_entry(const PassParams& P, int2 e)
     case FP_EARTH:
     case FP_SATELLITE: {
         float in[21];
-        shade_varyings<21>(P, d, U, w, t, s, z, xl, in, true);
+        shade_varyings<21, LAZY>(P, d, U, w, t, s, z, xl, in, true);
         bgra = shade_planet(U, in, (FPK ? FPK : d.fp) == FP_EARTH);
         break;
     }
     case FP_CLOUD: {
         float in[13];
-        shade_varyings<13>(P, d, U, w, t, s, z, xl, in);
+        shade_varyings<13, LAZY>(P, d, U, w, t, s, z, xl, in);
         bgra = shade_cloud(U, in);
         break;
     }
     case FP_DIFFUSEONLY: {
         float in[13];
-        shade_varyings<13>(P, d, U, w, t, s, z, xl, in);
+        shade_varyings<13, LAZY>(P, d, U, w, t, s, z, xl, in);
         bgra = shade_diffuse_only(U, in);
         break;
     }
     case FP_SINGLECOLOUR: {
         float in[11];
-        shade_varyings<11>(P, d, U, w, t, s, z, xl, in);
+        shade_varyings<11, LAZY>(P, d, U, w, t, s, z, xl, in);
         bgra = shade_single_colour(U, in);
         break;
     }
@@ -697,43 +700,43 @@ __device__ __forceinline__ void shade_entry(const PassParams& P, int2 e)
         break;
     case FP_DEF03: {
         float in[17];
-        shade_varyings<17>(P, d, U, w, t, s, z, xl, in);
+        shade_varyings<17, LAZY>(P, d, U, w, t, s, z, xl, in);
         bgra = shade_def03(U, in);
         break;
     }
     case FP_LIT2: {
         float in[16];
-        shade_varyings<16>(P, d, U, w, t, s, z, xl, in);
+        shade_varyings<16, LAZY>(P, d, U, w, t, s, z, xl, in);
         bgra = shade_lit2(U, in);
         break;
     }
     case FP_LIT1: {
         float in[9];
-        shade_varyings<9>(P, d, U, w, t, s, z, xl, in);
+        shade_varyings<9, LAZY>(P, d, U, w, t, s, z, xl, in);
         bgra = shade_lit1(U, in);
         break;
     }
     case FP_DEF02: {
         float in[11];
-        shade_varyings<11>(P, d, U, w, t, s, z, xl, in);
+        shade_varyings<11, LAZY>(P, d, U, w, t, s, z, xl, in);
         bgra = shade_def02(U, in);
         break;
     }
     case FP_DEF04: {
         float in[3];
-        shade_varyings<3>(P, d, U, w, t, s, z, xl, in);
+        shade_varyings<3, LAZY>(P, d, U, w, t, s, z, xl, in);
         bgra = shade_def04(U, in);
         break;
     }
     case FP_LIT3: {
         float in[9];
-        shade_varyings<9>(P, d, U, w, t, s, z, xl, in);
+        shade_varyings<9, LAZY>(P, d, U, w, t, s, z, xl, in);
         bgra = shade_lit3(U, in);
         break;
     }
     default: {  // FP_DEF01
         float in[9];
-        shade_varyings<9>(P, d, U, w, t, s, z, xl, in);
+        shade_varyings<9, LAZY>(P, d, U, w, t, s, z, xl, in);
         bgra = shade_def01(U, in);
         break;
     }
@@ -743,13 +746,13 @@ __device__ __forceinline__ void shade_entry(const PassParams& P, int2 e)
 
 // One thread per shade-list entry; the grid strides over the list, whose
 // length the raster kernel left in the slot status.
-template <int FPK>
-__global__ void __launch_bounds__(256) k_shade(PassParams P)
+template <int FPK, int LAZY>
+__global__ void __launch_bounds__(256, (LAZY != 0 && FPK != 0) ? 2 : 1) k_shade(PassParams P)
 {
     if (pass_failed(P.status, P.passSeq)) return;
     const int n = P.slotStatus[kSlotShade];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        shade_entry<FPK>(P, P.shadeList[i]);
+        shade_entry<FPK, LAZY>(P, P.shadeList[i]);
 }
 
 __global__ void k_fill_u32(uint32_t* base, int width, int height, int pitchElems, uint32_t v, const int* status,
@@ -830,26 +833,43 @@ void launch_raster(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
     launches++;
 }
 
+// The shade kernel for the pass's fragment processor (0: any) and its
+// varyings: stored by the set-up (LAZY = 0) or computed here (LAZY = the
+// vertex processor, for the pairs the built-in programmes use, else -1).
+template <int LAZY> static void (*shade_kernel(int fp))(PassParams)
+{
+    switch (fp) {
+    case FP_LIT1: return k_shade<FP_LIT1, LAZY>;
+    case FP_LIT2: return k_shade<FP_LIT2, LAZY>;
+    case FP_LIT3: return k_shade<FP_LIT3, LAZY>;
+    case FP_DEF01: return k_shade<FP_DEF01, LAZY>;
+    case FP_DEF03: return k_shade<FP_DEF03, LAZY>;
+    case FP_DEF02: return k_shade<FP_DEF02, LAZY>;
+    case FP_DEF04: return k_shade<FP_DEF04, LAZY>;
+    case FP_EARTH: return k_shade<FP_EARTH, LAZY>;
+    case FP_SATELLITE: return k_shade<FP_SATELLITE, LAZY>;
+    case FP_CLOUD: return k_shade<FP_CLOUD, LAZY>;
+    case FP_SINGLECOLOUR: return k_shade<FP_SINGLECOLOUR, LAZY>;
+    case FP_DIFFUSEONLY: return k_shade<FP_DIFFUSEONLY, LAZY>;
+    default: return k_shade<0, LAZY>;
+    }
+}
+
+static void (*lazy_shade_kernel(int fp, int vp))(PassParams)
+{
+    if (vp == VP_LIT2 && fp == FP_LIT2) return k_shade<FP_LIT2, VP_LIT2>;
+    if (vp == VP_DEF01 && fp == FP_LIT1) return k_shade<FP_LIT1, VP_DEF01>;
+    if (vp == VP_DEF01 && fp == FP_LIT3) return k_shade<FP_LIT3, VP_DEF01>;
+    if (vp == VP_DEF01 && fp == FP_DEF01) return k_shade<FP_DEF01, VP_DEF01>;
+    if (vp == VP_DEF03 && fp == FP_DEF03) return k_shade<FP_DEF03, VP_DEF03>;
+    return shade_kernel<-1>(fp);
+}
+
 void launch_shade(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
 {
     if (!P.anyColour || P.forward) return;  // a forward pass shaded in the raster
     // a grid that fills the GPU, striding over the shade list
-    void (*kern)(PassParams) = k_shade<0>;
-    switch (P.passFp) {
-    case FP_LIT1: kern = k_shade<FP_LIT1>; break;
-    case FP_LIT2: kern = k_shade<FP_LIT2>; break;
-    case FP_LIT3: kern = k_shade<FP_LIT3>; break;
-    case FP_DEF01: kern = k_shade<FP_DEF01>; break;
-    case FP_DEF03: kern = k_shade<FP_DEF03>; break;
-    case FP_DEF02: kern = k_shade<FP_DEF02>; break;
-    case FP_DEF04: kern = k_shade<FP_DEF04>; break;
-    case FP_EARTH: kern = k_shade<FP_EARTH>; break;
-    case FP_SATELLITE: kern = k_shade<FP_SATELLITE>; break;
-    case FP_CLOUD: kern = k_shade<FP_CLOUD>; break;
-    case FP_SINGLECOLOUR: kern = k_shade<FP_SINGLECOLOUR>; break;
-    case FP_DIFFUSEONLY: kern = k_shade<FP_DIFFUSEONLY>; break;
-    default: break;
-    }
+    void (*kern)(PassParams) = P.lazyVary ? lazy_shade_kernel(P.passFp, P.passVp) : shade_kernel<0>(P.passFp);
     long long need = ((long long)P.W * P.H + 255) / 256;
     int grid = (int)std::min<long long>(need, resident_blocks((const void*)kern, 256));
     pr->begin(K_SHADE, s);

@@ -69,11 +69,14 @@ __device__ __forceinline__ void vp_position(const DrawDesc& d, const DrawUniform
     }
 }
 
+// VPK: the vertex processor every draw using this code runs (a kernel
+// compiled for one keeps only its registers), 0 = the draw's own.
+template <int VPK = 0>
 __device__ __forceinline__ void vp_varyings(const DrawDesc& d, const DrawUniforms& U, int idx, float* vary)
 {
     float p[4];
     ld4(d.vbo[0] + (size_t)idx * d.stride[0], p);
-    switch (d.vp) {
+    switch (VPK ? VPK : d.vp) {
     case VP_DEF01: {  // tex1light1.cpp:22-41
         float wp[4], n[4], nrm[4];
         m4v4(wp, U.M, p);

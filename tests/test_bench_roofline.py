@@ -42,13 +42,13 @@ def test_dominant_roofline_uses_the_top_class_per_launch():
     counts = {"pairs": 4000, "triangles": 992, "shaded": 70000}
     # 10 profiled frames: raster 10 launches 2.0 ms in all, sort 10 launches 1.0 ms
     prof = {"raster": (10, 2.0), "sort": (10, 1.0), "setup": (10, 0.5), "bounds": (10, 0.1), "shade": (10, 0.2)}
-    r = bench.dominant_roofline(prof, 10, sc, counts, 16, 1234)
+    r = bench.dominant_roofline(prof, 10, sc, counts, 16, {"raster": 1234})
     per_launch = bench.algorithmic_bytes(sc, counts)["raster_per_frame"]
     assert r["kernel"] == "raster" and r["traffic"] == 1234
     assert r["bytes_per_launch"] == round(per_launch)
     assert abs(r["achieved"] - per_launch / 0.2e-3 / 1e9) < 0.01
     assert abs(r["frac"] - r["achieved"] / r["peak"]) < 1e-4
     prof["sort"] = (10, 3.0)
-    r = bench.dominant_roofline(prof, 10, sc, counts, 16, 1234)
+    r = bench.dominant_roofline(prof, 10, sc, counts, 16, {"raster": 1234})
     assert r["kernel"] == "sort" and r["traffic"] is None
     assert r["bytes_per_launch"] == 4000 * 16 * 2
