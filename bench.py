@@ -82,8 +82,9 @@ CONFIGS = {
 # bench.py --config cN --ncu-frames 2); averages over the launches that ran
 # to completion.  c4's are the immediate path's (one launch per frame over
 # the whole atlas), the same kernels as the batched pass.
-KERNEL_TRAFFIC = {"c1": {"raster": 77696}, "c2": {"raster": 5204672}, "c3": {"raster": 113905024},
-                  "c4": {"raster": 821472512}}
+KERNEL_TRAFFIC = {"c1": {"raster": 76928}, "c2": {"raster": 5205824},
+                  "c3": {"raster": 114627712, "shade": 348042496},
+                  "c4": {"raster": 809109760, "shade": 2099934720}}
 
 
 def peaks():

@@ -81,41 +81,58 @@ __global__ void __launch_bounds__(kWarpRasterThreads, MINB) k_raster_warp(PassPa
         }
         if (rowBeg >= rowEnd) continue;
         const bool myRow = lane >= rowBeg && lane < rowEnd;
-        float* gDepth = P.depth + (size_t)(y0 + lane) * P.depthScan + x0;
         const bool vec = vecDepth && cols == BW;
 
+        // Tile loads and stores run with the lanes along the bin's rows in
+        // row-major order (whole row segments per instruction, 16-byte
+        // accesses where the rows allow), not lane = row.
+        const int nPx = (rowEnd - rowBeg) * BW;
         if (start == end) {  // no triangle: the bin's clears only
-            if (myRow) {
-                if (P.clearDepth) {
-                    if (vec) {
-                        const float v = P.depthClearValue;
-#pragma unroll
-                        for (int c = 0; c < BW; c += 4) *(float4*)(gDepth + c) = make_float4(v, v, v, v);
-                    } else {
-                        for (int c = 0; c < cols; c++) gDepth[c] = P.depthClearValue;
+            if (P.clearDepth) {
+                if (vec) {
+                    const float v = P.depthClearValue;
+                    for (int i = lane; i < nPx / 4; i += 32) {
+                        const int r = rowBeg + (4 * i) / BW, c = (4 * i) % BW;
+                        *(float4*)(P.depth + (size_t)(y0 + r) * P.depthScan + x0 + c) = make_float4(v, v, v, v);
+                    }
+                } else {
+                    for (int i = lane; i < nPx; i += 32) {
+                        const int r = rowBeg + i / BW, c = i % BW;
+                        if (c < cols) P.depth[(size_t)(y0 + r) * P.depthScan + x0 + c] = P.depthClearValue;
                     }
                 }
-                if (P.clearColour)
-                    for (int c = 0; c < cols; c++) clear_colour_px(P, x0 + c, y0 + lane);
             }
+            if (P.clearColour)
+                for (int i = lane; i < nPx; i += 32) {
+                    const int r = rowBeg + i / BW, c = i % BW;
+                    if (c < cols) clear_colour_px(P, x0 + c, y0 + r);
+                }
             continue;
         }
 
-        // the bin's depth: lane = row (16-byte loads where the row allows)
-        float rmax = -INFINITY;
-        if (myRow && !P.clearDepth && vec) {
-#pragma unroll
-            for (int c = 0; c < BW; c += 4) {
-                const float4 d = *(const float4*)(gDepth + c);
-                dRow[c] = d.x;
-                dRow[c + 1] = d.y;
-                dRow[c + 2] = d.z;
-                dRow[c + 3] = d.w;
+        // the bin's depth: the slice's rows from the target (none when the
+        // pass clears depth), the clear value elsewhere
+        if (!P.clearDepth && vec) {
+            for (int i = lane; i < kBinH * BW / 4; i += 32) {
+                const int r = (4 * i) / BW, c = (4 * i) % BW;
+                float4 d = make_float4(P.depthClearValue, P.depthClearValue, P.depthClearValue, P.depthClearValue);
+                if (r >= rowBeg && r < rowEnd) d = *(const float4*)(P.depth + (size_t)(y0 + r) * P.depthScan + x0 + c);
+                float* t = T.depth + r * S + c;
+                t[0] = d.x;
+                t[1] = d.y;
+                t[2] = d.z;
+                t[3] = d.w;
             }
         } else {
-            for (int c = 0; c < BW; c++)
-                dRow[c] = (myRow && !P.clearDepth && c < cols) ? gDepth[c] : P.depthClearValue;
+            for (int i = lane; i < kBinH * BW; i += 32) {
+                const int r = i / BW, c = i % BW;
+                T.depth[r * S + c] = (!P.clearDepth && r >= rowBeg && r < rowEnd && c < cols)
+                                         ? P.depth[(size_t)(y0 + r) * P.depthScan + x0 + c]
+                                         : P.depthClearValue;
+            }
         }
+        __syncwarp();
+        float rmax = -INFINITY;
 #pragma unroll
         for (int c = 0; c < BW; c++) {
             wRow[c] = -1;
@@ -273,42 +290,46 @@ __global__ void __launch_bounds__(kWarpRasterThreads, MINB) k_raster_warp(PassPa
         }
         __syncwarp();
 
-        // ---- depth write-back (lane = row), then the shade list
-        int covered = 0;
-        if (myRow) {
-            if (vec) {
-#pragma unroll
-                for (int c = 0; c < BW; c += 4)
-                    *(float4*)(gDepth + c) = make_float4(dRow[c], dRow[c + 1], dRow[c + 2], dRow[c + 3]);
-            } else {
-                for (int c = 0; c < cols; c++) gDepth[c] = dRow[c];
+        // ---- depth write-back, then the shade list: row by row, each row's
+        // covered pixels left to right (one reservation per warp), and the
+        // clear colour of the uncovered pixels
+        if (vec) {
+            for (int i = lane; i < nPx / 4; i += 32) {
+                const int r = rowBeg + (4 * i) / BW, c = (4 * i) % BW;
+                const float* t = T.depth + r * S + c;
+                *(float4*)(P.depth + (size_t)(y0 + r) * P.depthScan + x0 + c) = make_float4(t[0], t[1], t[2], t[3]);
             }
-            for (int c = 0; c < cols; c++) covered += wRow[c] >= 0;
+        } else {
+            for (int i = lane; i < nPx; i += 32) {
+                const int r = rowBeg + i / BW, c = i % BW;
+                if (c < cols) P.depth[(size_t)(y0 + r) * P.depthScan + x0 + c] = T.depth[r * S + c];
+            }
         }
+        int covered = 0;
         if (P.anyColour || P.clearColour) {
-            // one reservation per warp in the shade list, then each lane's
-            // covered pixels in order; uncovered pixels get the clear colour
-            int incl = covered;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int v = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += v;
-            }
-            const int warpTotal = __shfl_sync(0xffffffffu, incl, 31);
             int listBase = 0;
-            if (lane == 0 && P.anyColour && warpTotal) listBase = atomicAdd(P.slotStatus + kSlotShade, warpTotal);
-            listBase = __shfl_sync(0xffffffffu, listBase, 0);
-            int pos = listBase + incl - covered;
-            if (myRow) {
-                const int y = y0 + lane;
-                for (int c = 0; c < cols; c++) {
-                    const int w = wRow[c];
-                    if (w >= 0) {
-                        if (P.anyColour) P.shadeList[pos++] = make_int2(y * P.W + x0 + c, w);
-                    } else if (P.clearColour) {
-                        clear_colour_px(P, x0 + c, y);
-                    }
+            if (P.anyColour) {
+                int total = 0;
+                for (int i = 0; i < nPx; i += 32) {
+                    const int q = i + lane, r = rowBeg + q / BW, c = q % BW;
+                    total += __popc(__ballot_sync(0xffffffffu, q < nPx && c < cols && T.win[r * S + c] >= 0));
                 }
+                if (lane == 0 && total) listBase = atomicAdd(P.slotStatus + kSlotShade, total);
+                listBase = __shfl_sync(0xffffffffu, listBase, 0);
+            }
+            const unsigned below = (1u << lane) - 1u;
+            for (int i = 0; i < nPx; i += 32) {
+                const int q = i + lane, r = rowBeg + q / BW, c = q % BW;
+                const bool in = q < nPx && c < cols;
+                const int w = in ? T.win[r * S + c] : -1;
+                const unsigned b = __ballot_sync(0xffffffffu, w >= 0);
+                if (w >= 0) {
+                    if (P.anyColour) P.shadeList[listBase + __popc(b & below)] = make_int2((y0 + r) * P.W + x0 + c, w);
+                    covered++;
+                } else if (in && P.clearColour) {
+                    clear_colour_px(P, x0 + c, y0 + r);
+                }
+                listBase += __popc(b);
             }
         }
         coveredAll += (unsigned long long)covered;
