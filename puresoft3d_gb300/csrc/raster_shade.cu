@@ -272,7 +272,7 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
     for (int iter = 0;; iter++) {
     if (listed && tid == 0) sItem = next_bin_item(P);
     __syncthreads();  // sItem is ready; the previous item's shared data are no longer read
-    const int item = listed ? sItem : (iter ? -1 : blockIdx.x);
+    const int item = listed ? sItem : (iter ? -1 : (int)blockIdx.x);
     __syncthreads();  // sItem is written again only after every thread has read it
     if (item < 0) break;
     const int bin = item & kItemBinMask, slice = (item >> kItemSliceShift) & 15;
