@@ -483,6 +483,7 @@ constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / 32;
 constexpr int kSortGroups = kSortChunk / kSortThreads;  // 32-key groups per warp
 constexpr unsigned kFlagCount = 1u << 30, kFlagPrefix = 2u << 30, kValueMask = (1u << 30) - 1;
+constexpr int kSortLookahead = 16;  // descriptors read per look-back round trip
 
 __global__ void __launch_bounds__(kSortThreads) k_onesweep(PassParams P, int pass, const int* __restrict__ inKey,
                                                            const int* __restrict__ inTri, int* __restrict__ outKey,
@@ -543,16 +544,19 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(PassParams P, int pas
         *mine = kFlagCount | (unsigned)count;
         int j = tile - 1, spins = 0;
         while (j >= 0) {
-            // four predecessors' descriptors per round trip, nearest first:
-            // counts are added until an inclusive prefix ends the walk; a
-            // descriptor not yet published is waited for (bounded)
-            unsigned v[4];
+            // kSortLookahead predecessors' descriptors per round trip,
+            // nearest first: counts are added until an inclusive prefix ends
+            // the walk; a descriptor not yet published is waited for
+            // (bounded).  The tiles of a pass are few and run together, so
+            // the walk's round trips set the pass's length.
+            unsigned v[kSortLookahead];
 #pragma unroll
-            for (int k = 0; k < 4; k++)
+            for (int k = 0; k < kSortLookahead; k++)
                 v[k] = j - k >= 0 ? *(volatile unsigned*)(desc + (size_t)(j - k) * kRadixDigits + d) : (unsigned)kFlagPrefix;
             int k = 0;
             bool stop = false, wait = false;
-            for (; k < 4; k++) {
+#pragma unroll
+            for (; k < kSortLookahead; k++) {
                 const unsigned f = v[k] & ~kValueMask;
                 if (f == 0u) {
                     wait = true;
