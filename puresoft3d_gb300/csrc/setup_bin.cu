@@ -315,20 +315,24 @@ __device__ __forceinline__ void emit_span_items(const PassParams& P, int t, long
     }
 }
 
-// Set-up, pair offsets and pair emission in one kernel.  Block b (numbered
-// by an atomic ticket, so that it only ever waits for blocks already
-// running) sets up triangles [b*128, b*128+128): each thread one triangle
-// (vertex processor, divide, cull, z-reject, row range, bin rectangle); the
-// varyings go out through shared memory so that the block's stores are
-// contiguous.  The block's pair counts are scanned in the block and its
-// global offset found by decoupled look-back over the earlier blocks
-// (64-bit descriptors: flag << 62 | value; each wait bounded), then every
-// triangle writes its (bin, triangle) pairs in triangle order, and the radix
-// sort's digit histograms are counted in shared memory.  The last block
-// knows the total: it records the pass's pair count and sort tiles, or the
-// overflow when the pairs do not fit (pairs past the capacity are never
-// written).  The header (tickets, histograms) and all descriptors are
-// zeroed by a memset before the kernel.
+// Set-up, pair offsets and pair emission in one kernel, over groups of
+// kSetupThreads triangles numbered by an atomic ticket (so a group's
+// predecessors are always held by running blocks).  A group is set up by one
+// block, a thread per triangle (vertex processor, divide, cull, z-reject,
+// row range, bin rectangle); its varyings go out through shared memory so
+// that the stores are contiguous; its pair counts are scanned in the block
+// and its total published as a look-back descriptor.  Its global offset is
+// then found by decoupled look-back over the earlier groups (64-bit
+// descriptors: flag << 62 | value; each wait bounded) and every triangle
+// writes its (bin, triangle) pairs in triangle order; the radix sort's digit
+// histograms are counted in shared memory.  The grid is persistent and
+// software-pipelined: a block looks back for its group and emits its pairs
+// only after it has set up its next group, so that the earlier groups have
+// had a group's set-up time to publish and the block's warps do not idle at
+// the look-back.  The holder of the last group records the pass's pair
+// count and sort tiles, or the overflow when the pairs do not fit (pairs past
+// the capacity are never written).  The header (tickets, histograms) and
+// all descriptors are zeroed by a memset before the kernel.
 constexpr int kLookbackSpins = 1 << 22;  // bounded waits: ~0.1 s and more, then the pass fails
 constexpr unsigned long long kDescAgg = 1ull << 62, kDescPrefix = 2ull << 62, kDescValue = (1ull << 62) - 1;
 
@@ -337,127 +341,160 @@ __global__ void __launch_bounds__(kSetupThreads, 8) k_setup_emit(PassParams P)
     extern __shared__ float sVary[];  // kSetupThreads * 3 * nvMax floats (dynamic: sized by the pass)
     __shared__ int sHist[kRadixMaxPasses][kRadixDigits];
     __shared__ int sWarp[kSetupThreads / 32];
-    __shared__ int sTicket, sPrefix;
+    __shared__ int sTicket, sPrefix, sPendTotal;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) sTicket = atomicAdd(P.radix + kTicketSetup, 1);
+    const int nGroups = (P.nTris + kSetupThreads - 1) / kSetupThreads;
     for (int i = tid; i < kRadixMaxPasses * kRadixDigits; i += kSetupThreads) (&sHist[0][0])[i] = 0;
-    __syncthreads();
-    const int b = sTicket;
-    const int first = b * kSetupThreads, t = first + tid;
-    int count = 0;
-    int4 rect = make_int4(0, -1, 0, -1);
-    bool itemized = false;
-    if (t < P.nTris) setup_triangle(P, t, sVary, count, rect, itemized);
-    if (b == 0 && tid == 0) P.slotStatus[kSlotShade] = 0;  // the shade list starts empty
-    if (b == 0 && tid < kItemBuckets + 1) P.slotStatus[kSlotBucket + tid] = 0;  // the raster's work list too
     if (P.radixPasses > 0) {  // every bin's (start, end) starts empty: the last radix pass fills them in
         const int nBins = P.binsX * P.binsY;
         for (int i = blockIdx.x * kSetupThreads + tid; i < nBins; i += gridDim.x * kSetupThreads)
             ((int2*)P.binStart)[i] = make_int2(INT_MAX, 0);
     }
+    volatile unsigned long long* desc = (volatile unsigned long long*)(P.radix + kRadixHdr);
 
-    // block scan of the pair counts
-    int inc = count;
+    // the group set up but not yet emitted: its number (-1 none; its total in
+    // sPendTotal) and this thread's offset in the group and bin rectangle
+    // (columns and rows as two 16-bit halves each)
+    int pend = -1, pendOff = 0, pendCols = -65536, pendRows = -65536;  // empty: 0 .. -1
+    bool pendItem = false;
+    for (;;) {
+        if (tid == 0) sTicket = atomicAdd(P.radix + kTicketSetup, 1);
+        __syncthreads();  // the ticket is ready; the previous group's shared data are no longer read
+        const int g = sTicket < nGroups ? sTicket : -1;
+        int count = 0, off = 0, total = 0;
+        int4 rect = make_int4(0, -1, 0, -1);
+        bool itemized = false;
+        const int first = g * kSetupThreads, t = first + tid;
+        if (g >= 0) {
+            if (t < P.nTris) setup_triangle(P, t, sVary, count, rect, itemized);
+            if (g == 0 && tid == 0) P.slotStatus[kSlotShade] = 0;  // the shade list starts empty
+            if (g == 0 && tid < kItemBuckets + 1) P.slotStatus[kSlotBucket + tid] = 0;  // the work list too
+            // block scan of the pair counts
+            int inc = count;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        int v = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += v;
-    }
-    if (lane == 31) sWarp[warp] = inc;
-    __syncthreads();
-    if (P.anyVary && !P.lazyVary) {
-        int n = min(kSetupThreads, P.nTris - first), nf = n * 3 * P.nvMax;
-        float* dst = P.vary + (size_t)first * 3 * P.nvMax;
-        for (int i = tid; i < nf; i += kSetupThreads) dst[i] = sVary[i];
-    }
-    int wbase = 0, blockTotal = 0;
-#pragma unroll
-    for (int w = 0; w < kSetupThreads / 32; w++) {
-        int v = sWarp[w];
-        if (w < warp) wbase += v;
-        blockTotal += v;
-    }
-    if (tid == 0) {  // publish this block's total first: later blocks' look-backs wait on it
-        volatile unsigned long long* desc = (volatile unsigned long long*)(P.radix + kRadixHdr);
-        desc[b] = (b == 0 ? kDescPrefix : kDescAgg) | (unsigned long long)blockTotal;
-    }
-    {
-        // the radix passes' digit histograms of this block's pairs: they need
-        // no offsets, so they are counted while warp 0 looks back (when the
-        // pairs overflow the room the pass fails and the counts go unused)
-        const int passes = P.radixPasses;
-        for (int by = rect.z; by <= rect.w; by++)
-            for (int bx = rect.x; bx <= rect.y; bx++) {
-                const int key = by * P.binsX + bx;
-                for (int ps = 0; ps < passes; ps++) atomicAdd(&sHist[ps][(key >> (8 * ps)) & 255], 1);
+            for (int o = 1; o < 32; o <<= 1) {
+                int v = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += v;
             }
-    }
-    if (warp == 0) {
-        // warp-wide look-back: 32 earlier blocks' descriptors per step, up to
-        // and including the nearest one that holds an inclusive prefix
-        volatile unsigned long long* desc = (volatile unsigned long long*)(P.radix + kRadixHdr);
-        long long prefix = 0;
-        if (b != 0) {
-            int top = b - 1, spins = 0;
-            while (true) {
-                const int idx = top - lane;
-                unsigned long long v = kDescPrefix | 0ull;  // before block 0: an empty prefix
-                if (idx >= 0) v = desc[idx];
-                const unsigned long long f = v & ~kDescValue;
-                const unsigned withPrefix = __ballot_sync(0xffffffffu, f == kDescPrefix);
-                const unsigned notReady = __ballot_sync(0xffffffffu, f == 0ull);
-                const int stop = withPrefix ? __ffs(withPrefix) - 1 : 31;   // lanes 0..stop are needed
-                const unsigned need = stop == 31 ? 0xffffffffu : ((2u << stop) - 1u);
-                if (notReady & need) {
-                    if (++spins > kLookbackSpins) {
-                        if (lane == 0) {
-                            atomicMin(P.status + kFirstFailed, P.passSeq);
-                            atomicOr(P.status, 2);
+            if (lane == 31) sWarp[warp] = inc;
+        }
+        __syncthreads();  // sWarp and the staged varyings are complete (and sTicket read)
+        if (g >= 0) {
+            if (P.anyVary && !P.lazyVary) {
+                int n = min(kSetupThreads, P.nTris - first), nf = n * 3 * P.nvMax;
+                float* dst = P.vary + (size_t)first * 3 * P.nvMax;
+                for (int i = tid; i < nf; i += kSetupThreads) dst[i] = sVary[i];
+            }
+            int wbase = 0;
+#pragma unroll
+            for (int w = 0; w < kSetupThreads / 32; w++) {
+                int v = sWarp[w];
+                if (w < warp) wbase += v;
+                total += v;
+            }
+            off = wbase;
+            {
+                int inc = count;  // this thread's exclusive offset in the group
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    int v = __shfl_up_sync(0xffffffffu, inc, o);
+                    if (lane >= o) inc += v;
+                }
+                off += inc - count;
+            }
+            if (tid == 0)  // publish the group's total: later groups' look-backs wait on it
+                desc[g] = (g == 0 ? kDescPrefix : kDescAgg) | (unsigned long long)total;
+            // the radix passes' digit histograms of the group's pairs: they
+            // need no offsets (when the pairs overflow the room the pass
+            // fails and the counts go unused)
+            const int passes = P.radixPasses;
+            for (int by = rect.z; by <= rect.w; by++)
+                for (int bx = rect.x; bx <= rect.y; bx++) {
+                    const int key = by * P.binsX + bx;
+                    for (int ps = 0; ps < passes; ps++) atomicAdd(&sHist[ps][(key >> (8 * ps)) & 255], 1);
+                }
+        }
+        if (pend >= 0) {
+            // the pending group: its offset by look-back, then its pairs
+            if (warp == 0) {
+                // warp-wide look-back: 32 earlier groups' descriptors per
+                // step, up to and including the nearest one that holds an
+                // inclusive prefix
+                long long prefix = 0;
+                if (pend != 0) {
+                    int top = pend - 1, spins = 0;
+                    while (true) {
+                        const int idx = top - lane;
+                        unsigned long long v = kDescPrefix | 0ull;  // before group 0: an empty prefix
+                        if (idx >= 0) v = desc[idx];
+                        const unsigned long long f = v & ~kDescValue;
+                        const unsigned withPrefix = __ballot_sync(0xffffffffu, f == kDescPrefix);
+                        const unsigned notReady = __ballot_sync(0xffffffffu, f == 0ull);
+                        const int stop = withPrefix ? __ffs(withPrefix) - 1 : 31;  // lanes 0..stop are needed
+                        const unsigned need = stop == 31 ? 0xffffffffu : ((2u << stop) - 1u);
+                        if (notReady & need) {
+                            if (++spins > kLookbackSpins) {
+                                if (lane == 0) {
+                                    atomicMin(P.status + kFirstFailed, P.passSeq);
+                                    atomicOr(P.status, 2);
+                                }
+                                break;
+                            }
+                            __nanosleep(32);
+                            continue;
                         }
-                        break;
-                    }
-                    __nanosleep(32);
-                    continue;
-                }
-                long long val = lane <= stop ? (long long)(v & kDescValue) : 0;
+                        long long val = lane <= stop ? (long long)(v & kDescValue) : 0;
 #pragma unroll
-                for (int o = 16; o; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
-                prefix += val;
-                if (withPrefix) break;
-                top -= 32;
-            }
-            if (lane == 0) desc[b] = kDescPrefix | (unsigned long long)(prefix + blockTotal);
-        }
-        if (lane == 0) {
-            sPrefix = (int)min(prefix, (long long)INT_MAX);
-            if (b == (int)gridDim.x - 1) {  // the last block: the pass's total
-                long long total = prefix + blockTotal;
-                if (total > P.pairCap) {
-                    P.slotStatus[kSlotTiles] = 0;
-                    P.slotStatus[kSlotTotal] = 0;
-                    atomicMax(P.status + 1, (int)min(total, (long long)INT_MAX));
-                    atomicMin(P.status + kFirstFailed, P.passSeq);
-                    atomicOr(P.status, 1);
-                } else {
-                    P.slotStatus[kSlotTotal] = (int)total;
-                    P.slotStatus[kSlotTiles] = (int)((total + kSortChunk - 1) / kSortChunk);
-                    atomicAdd((unsigned long long*)(P.status + 8), (unsigned long long)total);
-                    // one bin, no radix pass: its list is the pairs in emission order
-                    if (P.radixPasses == 0) ((int2*)P.binStart)[0] = make_int2(0, (int)total);
+                        for (int o = 16; o; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
+                        prefix += val;
+                        if (withPrefix) break;
+                        top -= 32;
+                    }
+                    if (lane == 0) desc[pend] = kDescPrefix | (unsigned long long)(prefix + sPendTotal);
+                }
+                if (lane == 0) {
+                    sPrefix = (int)min(prefix, (long long)INT_MAX);
+                    if (pend == nGroups - 1) {  // the last group: the pass's total
+                        long long all = prefix + sPendTotal;
+                        if (all > P.pairCap) {
+                            P.slotStatus[kSlotTiles] = 0;
+                            P.slotStatus[kSlotTotal] = 0;
+                            atomicMax(P.status + 1, (int)min(all, (long long)INT_MAX));
+                            atomicMin(P.status + kFirstFailed, P.passSeq);
+                            atomicOr(P.status, 1);
+                        } else {
+                            P.slotStatus[kSlotTotal] = (int)all;
+                            P.slotStatus[kSlotTiles] = (int)((all + kSortChunk - 1) / kSortChunk);
+                            atomicAdd((unsigned long long*)(P.status + 8), (unsigned long long)all);
+                            // one bin, no radix pass: its list is the pairs in emission order
+                            if (P.radixPasses == 0) ((int2*)P.binStart)[0] = make_int2(0, (int)all);
+                        }
+                    }
                 }
             }
+            __syncthreads();  // sPrefix is ready
+            const int pt = pend * kSetupThreads + tid;
+            long long o = (long long)sPrefix + pendOff;
+            if (pendItem) emit_span_items(P, pt, o, sHist);
+            const int bx0 = (short)(pendCols & 0xffff), bx1 = pendCols >> 16;
+            const int by0 = (short)(pendRows & 0xffff), by1 = pendRows >> 16;
+            for (int by = by0; by <= by1; by++)
+                for (int bx = bx0; bx <= bx1; bx++, o++) {
+                    if (o >= P.pairCap) continue;
+                    int key = by * P.binsX + bx;
+                    P.pairKey[o] = key;
+                    P.pairTri[o] = pt;
+                }
         }
+        if (g < 0) break;  // block-uniform: nothing is pending now
+        __syncthreads();  // sPendTotal and sPrefix were last read above
+        if (tid == 0) sPendTotal = total;
+        pend = g;
+        pendOff = off;
+        pendCols = (int)(((unsigned)rect.x & 0xffffu) | ((unsigned)rect.y << 16));
+        pendRows = (int)(((unsigned)rect.z & 0xffffu) | ((unsigned)rect.w << 16));
+        pendItem = itemized;
     }
-    __syncthreads();
-    long long o = (long long)sPrefix + wbase + inc - count;
-    if (itemized) emit_span_items(P, t, o, sHist);
-    for (int by = rect.z; by <= rect.w; by++)
-        for (int bx = rect.x; bx <= rect.y; bx++, o++) {
-            if (o >= P.pairCap) continue;
-            int key = by * P.binsX + bx;
-            P.pairKey[o] = key;
-            P.pairTri[o] = t;
-        }
     __syncthreads();
     for (int i = tid; i < P.radixPasses * kRadixDigits; i += kSetupThreads) {
         int v = (&sHist[0][0])[i];
@@ -677,7 +714,19 @@ int launch_setup(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
     pr->begin(K_SETUP, s);
     // nvMax <= kMaxVary: < 48 KB; none when the shade computes the varyings
     const size_t varyBytes = P.lazyVary ? 0 : (size_t)kSetupThreads * 3 * P.nvMax * sizeof(float);
-    k_setup_emit<<<ceil_div(P.nTris, kSetupThreads), kSetupThreads, varyBytes, s>>>(P);
+    // a persistent grid: at most the blocks that fit on the device at once
+    static int perSm[2] = {-1, -1}, sms = 0;  // resident blocks without / with staged varyings
+    const int slot = varyBytes ? 1 : 0;
+    if (perSm[slot] < 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm[slot], k_setup_emit, kSetupThreads,
+                                                      slot ? (size_t)kSetupThreads * 3 * kMaxVary * sizeof(float) : 0);
+        if (perSm[slot] < 1) perSm[slot] = 1;
+    }
+    const int groups = ceil_div(P.nTris, kSetupThreads);
+    k_setup_emit<<<std::max(1, std::min(groups, perSm[slot] * sms)), kSetupThreads, varyBytes, s>>>(P);
     pr->end(s);
     launches++;
     return 0;
