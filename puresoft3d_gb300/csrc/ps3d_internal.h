@@ -172,7 +172,7 @@ struct PassParams {
     int passSeq;              // recorded in status[3] when this pass overflows
 };
 
-constexpr int kSortChunk = 4096;   // pairs per sort tile
+constexpr int kSortChunk = 2048;   // pairs per sort tile
 constexpr int kFirstFailed = 3;    // status word: the first pass that overflowed or timed out
 constexpr int kNoPass = 0x7f7f7f7f; // its value when none did (a byte-wise memset)
 constexpr int kSlotTiles = 0, kSlotShade = 1, kSlotTotal = 2;  // slot status words: sort tiles, shade list, pairs

@@ -5,15 +5,17 @@
 //                 rasteriser's triangle set-up (reference drawvao.cpp:36-63,
 //                 vertthrd.cpp:14-65, rasterizer.cpp:73-234), the bin
 //                 rectangle the triangle's spans can touch, and -- after a
-//                 scan of the pair counts across blocks by decoupled
-//                 look-back -- its (bin, triangle) pairs in triangle order.
+//                 scan of the pair counts across groups of triangles by
+//                 decoupled look-back -- its (bin, triangle) pairs in
+//                 triangle order.
 //   k_onesweep    stable LSD radix passes over the pairs by bin, so that
 //                 each bin lists its triangles in submission order -- per
 //                 pixel the reference applies fragments in that order (its
 //                 per-row FIFO queues, drawvao.cpp:77-109), and the depth
 //                 test's epsilon makes the order observable
 //                 (fragthrd.cpp:227).
-//   k_bin_bounds  each bin's first position in the sorted list.
+//   k_bin_bounds  the raster's work list from each bin's range in the
+//                 sorted list (the last radix pass writes the ranges).
 #include <cuda_runtime.h>
 #include "vertex_stage.cuh"
 
@@ -507,7 +509,7 @@ __global__ void __launch_bounds__(kSetupThreads, 8) k_setup_emit(PassParams P)
 // and finds its per-digit prefix over earlier tiles by decoupled look-back).
 //
 // A tile is kSortChunk consecutive pairs; warp w of the block takes pairs
-// [w*512, (w+1)*512) of it in 16 groups of 32 and ranks each key among the
+// [w*256, (w+1)*256) of it in 8 groups of 32 and ranks each key among the
 // equal digits before it (__match_any_sync per group, a running per-warp
 // count per digit), so ranks follow input order and the sort is stable.
 // Tiles are numbered by an atomic ticket taken when the block starts, so a
