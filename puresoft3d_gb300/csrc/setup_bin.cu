@@ -50,17 +50,20 @@ __device__ __forceinline__ bool back_face(const float p[3][4])
 __device__ __forceinline__ int edge_code(int a, int b) { return a | (b << 2); }
 
 constexpr int kSetupThreads = 128;
+constexpr int kSetupDrawCache = 512;  // draws whose first triangles the set-up keeps in shared memory
 
 // itemized: the triangle's pairs are span items (one per row span and bin),
 // emitted by emit_span_items after the look-back; otherwise one pair per bin
 // of `rect`.
-__device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float* sVary, int& pairs, int4& rect,
-                                               bool& itemized)
+// sBase: the draws' first triangles in shared memory (null: read from the
+// draw table).
+__device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float* sVary, const int* sBase, int& pairs,
+                                               int4& rect, bool& itemized)
 {
     int lo = 0, hi = P.nDraws - 1;
     while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
-        if (P.draws[mid].triBase <= t) lo = mid;
+        if ((sBase ? sBase[mid] : P.draws[mid].triBase) <= t) lo = mid;
         else hi = mid - 1;
     }
     const DrawDesc& d = P.draws[lo];
@@ -344,9 +347,13 @@ __global__ void __launch_bounds__(kSetupThreads, 8) k_setup_emit(PassParams P)
     __shared__ int sHist[kRadixMaxPasses][kRadixDigits];
     __shared__ int sWarp[kSetupThreads / 32];
     __shared__ int sTicket, sPrefix, sPendTotal;
+    __shared__ int sDrawBase[kSetupDrawCache];  // the draws' first triangles, for the draw search
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nGroups = (P.nTris + kSetupThreads - 1) / kSetupThreads;
     for (int i = tid; i < kRadixMaxPasses * kRadixDigits; i += kSetupThreads) (&sHist[0][0])[i] = 0;
+    const int* drawBase = P.nDraws <= kSetupDrawCache ? sDrawBase : nullptr;
+    if (drawBase)
+        for (int i = tid; i < P.nDraws; i += kSetupThreads) sDrawBase[i] = P.draws[i].triBase;
     if (P.radixPasses > 0) {  // every bin's (start, end) starts empty: the last radix pass fills them in
         const int nBins = P.binsX * P.binsY;
         for (int i = blockIdx.x * kSetupThreads + tid; i < nBins; i += gridDim.x * kSetupThreads)
@@ -368,7 +375,7 @@ __global__ void __launch_bounds__(kSetupThreads, 8) k_setup_emit(PassParams P)
         bool itemized = false;
         const int first = g * kSetupThreads, t = first + tid;
         if (g >= 0) {
-            if (t < P.nTris) setup_triangle(P, t, sVary, count, rect, itemized);
+            if (t < P.nTris) setup_triangle(P, t, sVary, drawBase, count, rect, itemized);
             if (g == 0 && tid == 0) P.slotStatus[kSlotShade] = 0;  // the shade list starts empty
             if (g == 0 && tid < kItemBuckets + 1) P.slotStatus[kSlotBucket + tid] = 0;  // the work list too
             // block scan of the pair counts
