@@ -60,16 +60,36 @@ __device__ __forceinline__ bool span_occluded(const SpanZ& z, int kA, int kB, fl
     return lhs - slack >= -0.0001f;  // false for NaN
 }
 
-// The next work item of the pass's list (k_bin_bounds): the crowded bins'
-// row slices, then the other bins, then the empty ones; -1 when done.
-__device__ __forceinline__ int next_bin_item(const PassParams& P)
+// The work list's bucket ends (running sums of the counts k_bin_bounds left
+// in the slot status; fixed while the raster runs), written to sEnd by
+// thread 0 of the block; the caller synchronises before next_bin_item.
+__device__ __forceinline__ void load_item_buckets(const PassParams& P, int* sEnd)
 {
-    int i = atomicAdd(P.slotStatus + kSlotCursor, 1);
+    if (threadIdx.x == 0) {
+        int n[kItemBuckets];
+#pragma unroll
+        for (int b = 0; b < kItemBuckets; b++) n[b] = __ldcg(P.slotStatus + kSlotBucket + b);
+        int run = 0;
+#pragma unroll
+        for (int b = 0; b < kItemBuckets; b++) {
+            run += n[b];
+            sEnd[b] = run;
+        }
+    }
+}
+
+// The next work item of the pass's list (k_bin_bounds): the crowded bins'
+// row slices, then the other bins by size, then the empty ones; -1 when done.
+// sEnd: the bucket ends from load_item_buckets.
+__device__ __forceinline__ int next_bin_item(const PassParams& P, const int* sEnd)
+{
+    const int i = atomicAdd(P.slotStatus + kSlotCursor, 1);
     const int nBins = P.binsX * P.binsY;
+    int start = 0;
+#pragma unroll
     for (int b = 0; b < kItemBuckets; b++) {
-        const int n = *(volatile const int*)(P.slotStatus + kSlotBucket + b);
-        if (i < n) return P.binItems[bucket_base(b, nBins) + i];
-        i -= n;
+        if (i < sEnd[b]) return __ldcg(P.binItems + bucket_base(b, nBins) + (i - start));
+        start = sEnd[b];
     }
     return -1;
 }

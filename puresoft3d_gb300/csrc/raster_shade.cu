@@ -257,6 +257,9 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
     __shared__ float sQMax[4][kBinH];            // per quarter and row: an upper bound of its depths
     __shared__ int sListBase;
     __shared__ int sItem;
+    __shared__ int sItemEnd[kItemBuckets];
+    if (P.rowSplit > 1) load_item_buckets(P, sItemEnd);
+    __syncthreads();  // before any early return: every thread reaches it
     if (pass_failed(P.status, P.passSeq)) return;
 
     // One block per bin (P.rowSplit == 1), or a persistent grid whose blocks
@@ -270,7 +273,7 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
     const bool listed = P.rowSplit > 1;
     unsigned long long tested = 0, passed = 0, coveredAll = 0;
     for (int iter = 0;; iter++) {
-    if (listed && tid == 0) sItem = next_bin_item(P);
+    if (listed && tid == 0) sItem = next_bin_item(P, sItemEnd);
     __syncthreads();  // sItem is ready; the previous item's shared data are no longer read
     const int item = listed ? sItem : (iter ? -1 : (int)blockIdx.x);
     __syncthreads();  // sItem is written again only after every thread has read it

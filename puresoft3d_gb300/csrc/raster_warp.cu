@@ -52,6 +52,9 @@ __global__ void __launch_bounds__(kWarpRasterThreads, MINB) k_raster_warp(PassPa
 {
     constexpr int S = BW + 1;
     __shared__ WarpTile<BW> tiles[kWarpRasterWarps];
+    __shared__ int sItemEnd[kItemBuckets];
+    load_item_buckets(P, sItemEnd);
+    __syncthreads();  // before any early return: every thread reaches it
     if (pass_failed(P.status, P.passSeq)) return;
     const int lane = threadIdx.x & 31;
     WarpTile<BW>& T = tiles[threadIdx.x >> 5];
@@ -62,7 +65,7 @@ __global__ void __launch_bounds__(kWarpRasterThreads, MINB) k_raster_warp(PassPa
 
     for (;;) {
         int item = 0;
-        if (lane == 0) item = next_bin_item(P);
+        if (lane == 0) item = next_bin_item(P, sItemEnd);
         item = __shfl_sync(0xffffffffu, item, 0);
         if (item < 0) break;
         const int bin = item & kItemBinMask, slice = (item >> kItemSliceShift) & 15;

@@ -671,8 +671,8 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(PassParams P, int pas
 // The raster's work list, from each bin's (start, end) in the sorted list
 // (written by the last radix pass): a bin with n triangles becomes s =
 // min(rowSplit, the largest power of two <= n / kSliceTris) items (row
-// slices when s > 1), in buckets by s, crowded first; empty bins last (they
-// still clear their pixels).  Launched only for rasters that take work items
+// slices when s > 1), in buckets by s, crowded first (unsliced bins by their
+// triangle count); empty bins last (they still clear their pixels).  Launched only for rasters that take work items
 // (row split or one warp per bin); a raster with one block per bin reads the
 // ranges directly.
 __global__ void k_bin_bounds(PassParams P)
@@ -685,7 +685,10 @@ __global__ void k_bin_bounds(PassParams P)
     const int n = r.x < r.y ? r.y - r.x : 0;
     int lg = 0;
     while (lg < 3 && (1 << (lg + 1)) <= P.rowSplit && n >= (kSliceTris << (lg + 1))) lg++;
-    const int bucket = n == 0 ? 4 : 3 - lg;
+    // sliced bins by their slice count; unsliced ones with many triangles
+    // ahead of the rest (their buckets have room: one item per bin), so that
+    // the long items start first
+    const int bucket = n == 0 ? 4 : lg > 0 ? 3 - lg : (n >= 4 * kSliceTris ? 1 : (n >= kSliceTris ? 2 : 3));
     const int k = 1 << lg;
     const int at = atomicAdd(P.slotStatus + kSlotBucket + bucket, k);
     int* out = P.binItems + bucket_base(bucket, nBins) + at;
