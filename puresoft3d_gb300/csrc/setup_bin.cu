@@ -677,12 +677,16 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(PassParams P, int pas
 // ranges directly.
 __global__ void k_bin_bounds(PassParams P)
 {
-    if (pass_failed(P.status, P.passSeq)) return;
-    int b = blockIdx.x * blockDim.x + threadIdx.x;
-    int nBins = P.binsX * P.binsY;
-    if (b >= nBins) return;
-    const int2 r = P.slotStatus[kSlotTiles] ? ((const int2*)P.binStart)[b] : make_int2(0, 0);
-    const int n = r.x < r.y ? r.y - r.x : 0;
+    if (pass_failed(P.status, P.passSeq)) return;  // one load per warp: the warp leaves or stays whole
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nBins = P.binsX * P.binsY;
+    const bool valid = b < nBins;
+    const int lane = threadIdx.x & 31;
+    int n = 0;
+    if (valid) {
+        const int2 r = P.slotStatus[kSlotTiles] ? ((const int2*)P.binStart)[b] : make_int2(0, 0);
+        n = r.x < r.y ? r.y - r.x : 0;
+    }
     int lg = 0;
     while (lg < 3 && (1 << (lg + 1)) <= P.rowSplit && n >= (kSliceTris << (lg + 1))) lg++;
     // sliced bins by their slice count; unsliced ones with many triangles
@@ -690,7 +694,29 @@ __global__ void k_bin_bounds(PassParams P)
     // the long items start first
     const int bucket = n == 0 ? 4 : lg > 0 ? 3 - lg : (n >= 4 * kSliceTris ? 1 : (n >= kSliceTris ? 2 : 3));
     const int k = 1 << lg;
-    const int at = atomicAdd(P.slotStatus + kSlotBucket + bucket, k);
+    // one reservation per warp and bucket (thousands of bins on five
+    // counters would queue at them): the lanes' items in lane order
+    int at = 0;
+#pragma unroll
+    for (int bk = 0; bk < kItemBuckets; bk++) {
+        const bool mine = valid && bucket == bk;
+        const unsigned m = __ballot_sync(0xffffffffu, mine);
+        if (!m) continue;
+        const int v = mine ? k : 0;
+        int incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        const int leader = __ffs(m) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(P.slotStatus + kSlotBucket + bk, total);
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (mine) at = base + incl - v;
+    }
+    if (!valid) return;
     int* out = P.binItems + bucket_base(bucket, nBins) + at;
     for (int s = 0; s < k; s++) out[s] = b | (s << kItemSliceShift) | (lg << kItemLog2Shift);
 }
