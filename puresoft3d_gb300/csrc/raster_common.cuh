@@ -113,11 +113,13 @@ __device__ __forceinline__ void load_item(const PassParams& P, int v, float4 rec
 // columns [x0, x0 + cols): the row result (rasterizer.cpp:93-118) and the
 // span set-up (interp.cpp:26-80), whose state is at pixel k0 = leftClamped
 // (in target columns).  False when the row has no span.
+// kRegs: t is held in registers (vertex selects instead of indexed loads).
+template <bool kRegs = false>
 __device__ __forceinline__ bool triangle_span(const TriRaster& t, int yl, int lw, int ox, int x0, int cols, int& xs,
                                               int& xe, int& k0, int& sflags, SpanZ& z)
 {
     Span sp;
-    if (!span_row(t, yl, lw, sp)) return false;
+    if (!span_row<kRegs>(t, yl, lw, sp)) return false;
     xs = max(sp.leftClamped + ox, x0);
     xe = min(sp.rightClamped + ox, x0 + cols - 1);
     k0 = sp.leftClamped + ox;

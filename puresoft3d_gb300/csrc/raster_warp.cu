@@ -31,7 +31,8 @@ constexpr int kWarpRasterThreads = 32 * kWarpRasterWarps;
 
 // One warp's shared memory.
 template <int BW> struct __align__(16) WarpTile {
-    TriRaster tri[32];               // the chunk's triangles, one per lane
+    int item[32];                    // the chunk's items (triangle, or ~index of a span item); their
+                                     // records are read back from L1 where the set-up needs them
     float depth[kBinH * (BW + 1)];   // the bin's depth (odd row stride: lanes = rows hit distinct banks)
     int win[kBinH * (BW + 1)];       // last colour-writing fragment that passed, -1 none
     float z[32 * (BW + 1)];          // per span of the round: exact z at each of its bin columns
@@ -151,14 +152,12 @@ __global__ void __launch_bounds__(kWarpRasterThreads, MINB) k_raster_warp(PassPa
             int cnt = 0, r0 = 0;
             if (chunk + lane < end) {
                 const int v = P.sortedTri[chunk + lane];  // a triangle, or ~index of a span item
-                float4* dst = (float4*)(T.tri + lane);
                 float4 rec[4];
                 load_item(P, v, rec);
+                T.item[lane] = v;
                 if (v >= 0) {
-#pragma unroll
-                    for (int k = 0; k < 4; k++) dst[k] = rec[k];
                     T.tid[lane] = v;
-                    const TriRaster& tr = T.tri[lane];
+                    const TriRaster& tr = *reinterpret_cast<const TriRaster*>(rec);
                     const DrawDesc& dd = P.draws[tr.draw];
                     const int oy = dd.vpY;
                     T.ox[lane] = (short)dd.vpX;
@@ -168,9 +167,7 @@ __global__ void __launch_bounds__(kWarpRasterThreads, MINB) k_raster_warp(PassPa
                     const int r1 = min((int)tr.lastRow + oy - y0, rowEnd - 1);
                     if (r0 <= r1) cnt = r1 - r0 + 1;
                 } else {  // a span item: one row, set up already
-                    dst[0] = rec[0];
-                    dst[1] = rec[1];
-                    const SpanItem& si = *(const SpanItem*)(T.tri + lane);
+                    const SpanItem& si = *reinterpret_cast<const SpanItem*>(rec);
                     T.tid[lane] = si.tri;
                     T.lw[lane] = -1;
                     r0 = si.y - y0;
@@ -206,8 +203,10 @@ __global__ void __launch_bounds__(kWarpRasterThreads, MINB) k_raster_warp(PassPa
                     bool live;
                     int xs, xe, k0, sflags;
                     SpanZ z;
+                    float4 rec[4];  // the item's record, staged by this chunk: an L1 hit
+                    load_item(P, T.item[j], rec);
                     if (T.lw[j] < 0) {
-                        const SpanItem& si = *(const SpanItem*)(T.tri + j);
+                        const SpanItem& si = *reinterpret_cast<const SpanItem*>(rec);
                         live = true;
                         xs = k0 = si.xs;
                         xe = si.xe;
@@ -217,8 +216,8 @@ __global__ void __launch_bounds__(kWarpRasterThreads, MINB) k_raster_warp(PassPa
                         z.cf2Step = si.cf2Step;
                         z.pzStep = si.pzStep;
                     } else {
-                        live = triangle_span(T.tri[j], y0 + r - T.oy[j], T.lw[j], T.ox[j], x0, cols, xs, xe, k0, sflags,
-                                             z);
+                        live = triangle_span<true>(*reinterpret_cast<const TriRaster*>(rec), y0 + r - T.oy[j], T.lw[j],
+                                                   T.ox[j], x0, cols, xs, xe, k0, sflags, z);
                     }
                     if (live) {
                         if (xs <= xe) {
@@ -388,8 +387,8 @@ void launch_raster_warp(const PassParams& P, int nBins, cudaStream_t s)
         if (P.cullSpans) launch_one<8, 8, true>(P, nBins, s);
         else launch_one<8, 8, false>(P, nBins, s);
     } else {
-        if (P.cullSpans) launch_one<16, 5, true>(P, nBins, s);
-        else launch_one<16, 5, false>(P, nBins, s);
+        if (P.cullSpans) launch_one<16, 7, true>(P, nBins, s);
+        else launch_one<16, 7, false>(P, nBins, s);
     }
 }
 
