@@ -55,17 +55,43 @@ constexpr int kSetupDrawCache = 512;  // draws whose first triangles the set-up 
 // itemized: the triangle's pairs are span items (one per row span and bin),
 // emitted by emit_span_items after the look-back; otherwise one pair per bin
 // of `rect`.
-// sBase: the draws' first triangles in shared memory (null: read from the
-// draw table).
-__device__ __forceinline__ void setup_triangle(const PassParams& P, int t, float* sVary, const int* sBase, int& pairs,
+// The draw of triangle t (the last draw whose first triangle is <= t), for
+// every lane of a warp whose triangles are consecutive from `first` (t <
+// nTris for the lanes that use it).  sBase: the draws' first triangles in
+// shared memory -- a binary search there; null: the warp finds the draw of
+// `first` by a 32-way search over the draw table (probe loads per round, 3
+// rounds for 4096 draws), then each lane steps forward over the draws that
+// start at or before its triangle.
+__device__ __forceinline__ int draw_of(const PassParams& P, int t, int first, const int* sBase)
+{
+    const int lane = threadIdx.x & 31;
+    int lo = 0, hi = P.nDraws - 1;
+    if (sBase) {
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (sBase[mid] <= t) lo = mid;
+            else hi = mid - 1;
+        }
+        return lo;
+    }
+    while (lo < hi) {  // warp-uniform; draws[lo].triBase <= first throughout
+        const int n = hi - lo;
+        const int c = lo + (int)(((long long)n * (lane + 1) + 31) / 32);  // lo < c <= hi, nondecreasing in lane
+        const unsigned m = __ballot_sync(0xffffffffu, __ldg(&P.draws[c].triBase) <= first);
+        const int L = __popc(m);  // the candidates at or before `first` are lanes 0 .. L-1
+        const int cHi = __shfl_sync(0xffffffffu, c, L < 32 ? L : 31);
+        lo = L ? __shfl_sync(0xffffffffu, c, L - 1) : lo;
+        hi = L < 32 ? cHi - 1 : hi;
+        if (L == 32) lo = hi;
+    }
+    while (lo + 1 < P.nDraws && __ldg(&P.draws[lo + 1].triBase) <= t) lo++;
+    return lo;
+}
+
+__device__ __forceinline__ void setup_triangle(const PassParams& P, int t, int drawIdx, float* sVary, int& pairs,
                                                int4& rect, bool& itemized)
 {
-    int lo = 0, hi = P.nDraws - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if ((sBase ? sBase[mid] : P.draws[mid].triBase) <= t) lo = mid;
-        else hi = mid - 1;
-    }
+    const int lo = drawIdx;
     const DrawDesc& d = P.draws[lo];
     const DrawUniforms& U = P.unis[d.uni];
     int lt = t - d.triBase;
@@ -375,7 +401,8 @@ __global__ void __launch_bounds__(kSetupThreads, 8) k_setup_emit(PassParams P)
         bool itemized = false;
         const int first = g * kSetupThreads, t = first + tid;
         if (g >= 0) {
-            if (t < P.nTris) setup_triangle(P, t, sVary, drawBase, count, rect, itemized);
+            const int drawIdx = draw_of(P, min(t, P.nTris - 1), first + 32 * warp, drawBase);
+            if (t < P.nTris) setup_triangle(P, t, drawIdx, sVary, count, rect, itemized);
             if (g == 0 && tid == 0) P.slotStatus[kSlotShade] = 0;  // the shade list starts empty
             if (g == 0 && tid < kItemBuckets + 1) P.slotStatus[kSlotBucket + tid] = 0;  // the work list too
             // block scan of the pair counts
