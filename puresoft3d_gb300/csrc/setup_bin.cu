@@ -780,18 +780,19 @@ int launch_setup(const PassParams& P, cudaStream_t s, int& launches, Prof* pr)
     // nvMax <= kMaxVary: < 48 KB; none when the shade computes the varyings
     const size_t varyBytes = P.lazyVary ? 0 : (size_t)kSetupThreads * 3 * P.nvMax * sizeof(float);
     // a persistent grid: at most the blocks that fit on the device at once
-    static int perSm[2] = {-1, -1}, sms = 0;  // resident blocks without / with staged varyings
-    const int slot = varyBytes ? 1 : 0;
-    if (perSm[slot] < 0) {
-        int dev = 0;
+    // (by the pass's own staging size: resident blocks per SM cached per
+    // varying count)
+    static int perSm[kMaxVary + 1] = {}, sms = 0;
+    const int nvKey = P.lazyVary ? 0 : std::min(std::max(P.nvMax, 0), kMaxVary);
+    if (perSm[nvKey] <= 0) {
+        int dev = 0, n = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm[slot], k_setup_emit, kSetupThreads,
-                                                      slot ? (size_t)kSetupThreads * 3 * kMaxVary * sizeof(float) : 0);
-        if (perSm[slot] < 1) perSm[slot] = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_setup_emit, kSetupThreads, varyBytes);
+        perSm[nvKey] = n < 1 ? 1 : n;
     }
     const int groups = ceil_div(P.nTris, kSetupThreads);
-    k_setup_emit<<<std::max(1, std::min(groups, perSm[slot] * sms)), kSetupThreads, varyBytes, s>>>(P);
+    k_setup_emit<<<std::max(1, std::min(groups, perSm[nvKey] * sms)), kSetupThreads, varyBytes, s>>>(P);
     pr->end(s);
     launches++;
     return 0;
