@@ -3,8 +3,8 @@
  * path (CallMeZhou/Puresoft3D), used as the oracle.
  *
  * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the
- * CPU-baseline leg of bench.py load this library, and only as the checker
- * (or as the timed CPU baseline); the product never routes through it.
+ * CPU-baseline leg of bench.py load this library, only to check results
+ * against (or as the timed CPU baseline); the product never routes through it.
  *
  * The entry points mirror the reference's PuresoftPipeline API
  * (src/puresoft3d/pipeline.h:26-69) one for one, in C, with the same status

@@ -10,7 +10,7 @@
  *  - InterlockedIncrement/Decrement/Exchange on the ring-queue length
  *    (reference: rinque.h endPush/endPop);
  *  - the BMP header structs and _wfopen_s used by PuresoftFBO::saveAsBmpFile
- *    (reference: fbo.cpp), which this build never calls but must compile.
+ *    (reference: fbo.cpp), which the headless build never calls but must compile.
  * GetCurrentThread() returns a pseudo handle meaning "the calling thread", as
  * on Windows; GetThreadId() of it yields the caller's id.
  */
