@@ -286,7 +286,9 @@ int ps3d_clear_depth(ps3d_pipeline* p, float furthest);
 int ps3d_clear_colour(ps3d_pipeline* p, uint32_t bgra);
 /* PuresoftPipeline::drawVAO(vao, false) (drawvao.cpp:3-133): records the draw
  * with a snapshot of the programme, uniforms, behaviour, viewport and
- * targets.  Work is launched by ps3d_flush / ps3d_finish / a read-back. */
+ * targets.  Work is launched by ps3d_flush / ps3d_finish / a read-back.
+ * PS3D_ERR_RANGE for a depth target wider than 65535 or taller than 32767
+ * pixels. */
 int ps3d_draw(ps3d_pipeline* p, int vao);
 /* Launch recorded work on the stream without waiting. */
 int ps3d_flush(ps3d_pipeline* p);

@@ -1760,6 +1760,8 @@ int ps3d_draw(ps3d_pipeline* p, int vao)
     if ((rc = depth_target(p, p->depthTarget, tg))) return rc;
     if (tg.w < p->vpX + p->W || tg.h < p->vpY + p->H)
         return fail(PS3D_ERR_INVALID, "the viewport rectangle is not inside the depth target");
+    if (tg.w > 65535 || tg.h > 32767)  // the rasters' row numbers and shade-list pixels are 16-bit
+        return fail(PS3D_ERR_RANGE, "a depth target larger than 65535 x 32767 cannot be drawn into");
     if (d.flags & F_COLOUR) {
         ColourTarget ct;
         if ((rc = colour_target(p, c.colourTarget, ct))) return rc;

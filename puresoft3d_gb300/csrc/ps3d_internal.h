@@ -162,7 +162,7 @@ struct PassParams {
     float* depth;             // depth target (rows bottom-up)
     int depthScan;            // in floats
     int depthW, depthH;
-    int2* shadeList;          // per covered pixel: (y * W + x, last colour-writing fragment that passed)
+    int2* shadeList;          // per covered pixel: (y << 16 | x, last colour-writing fragment that passed)
     uint32_t* colourRow0;     // the colour target (FBO slot 0), BGRA8: pixel (x, y) at colourRow0[y * colourPitch + x]
     int colourPitch;          // in pixels; negative for the display, whose rows run top-down
     int colourW, colourH;

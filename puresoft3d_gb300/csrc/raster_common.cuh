@@ -22,6 +22,11 @@ __device__ __forceinline__ uint32_t* colour_px(const PassParams& P, int x, int y
     return P.colourRow0 + (ptrdiff_t)y * P.colourPitch + x;
 }
 
+// A shade-list entry's pixel: y in the high and x in the low 16 bits
+// (targets are at most 32767 pixels a side), so that the shade needs no
+// division to find them.
+__device__ __forceinline__ int shade_pixel(int x, int y) { return (y << 16) | x; }
+
 // The pass's clear colour at target pixel (x, y).
 __device__ __forceinline__ void clear_colour_px(const PassParams& P, int x, int y)
 {

@@ -621,7 +621,7 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
             int r = rowBeg + i / cols, c = i - (r - rowBeg) * cols;
             int w = sWin[r * S + c];
             if (w >= 0) {
-                if (P.anyColour) P.shadeList[pos++] = make_int2((y0 + r) * P.W + x0 + c, w);
+                if (P.anyColour) P.shadeList[pos++] = make_int2(shade_pixel(x0 + c, y0 + r), w);
             } else if (P.clearColour) {
                 clear_colour_px(P, x0 + c, y0 + r);
             }
@@ -655,7 +655,7 @@ __global__ void __launch_bounds__(kRasterThreads, MINB) k_raster(PassParams P)
 template <int FPK, int LAZY>
 __device__ __forceinline__ void shade_entry(const PassParams& P, int2 e)
 {
-    const int y = e.x / P.W, x = e.x - y * P.W, w = e.y;
+    const int y = e.x >> 16, x = e.x & 0xffff, w = e.y;
     uint32_t* dst = colour_px(P, x, y);
     TriRaster t;
     {

@@ -326,7 +326,7 @@ __global__ void __launch_bounds__(kWarpRasterThreads, MINB) k_raster_warp(PassPa
                 const int w = in ? T.win[r * S + c] : -1;
                 const unsigned b = __ballot_sync(0xffffffffu, w >= 0);
                 if (w >= 0) {
-                    if (P.anyColour) P.shadeList[listBase + __popc(b & below)] = make_int2((y0 + r) * P.W + x0 + c, w);
+                    if (P.anyColour) P.shadeList[listBase + __popc(b & below)] = make_int2(shade_pixel(x0 + c, y0 + r), w);
                     covered++;
                 } else if (in && P.clearColour) {
                     clear_colour_px(P, x0 + c, y0 + r);
