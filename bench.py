@@ -82,9 +82,9 @@ CONFIGS = {
 # bench.py --config cN --ncu-frames 2); averages over the launches that ran
 # to completion.  c4's are the immediate path's (one launch per frame over
 # the whole atlas), the same kernels as the batched pass.
-KERNEL_TRAFFIC = {"c1": {"raster": 70272, "shade": 748160}, "c2": {"raster": 5204992, "shade": 18389248},
-                  "c3": {"raster": 113262464, "shade": 343955072},
-                  "c4": {"raster": 811194624, "shade": 2107241984}}
+KERNEL_TRAFFIC = {"c1": {"raster": 70272, "shade": 747264}, "c2": {"raster": 5207872, "shade": 18389504},
+                  "c3": {"raster": 117440640, "shade": 339642240},
+                  "c4": {"raster": 825424640, "shade": 2104926976}}
 
 
 def peaks():
