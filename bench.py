@@ -83,7 +83,7 @@ CONFIGS = {
 # to completion.  c4's are the immediate path's (one launch per frame over
 # the whole atlas), the same kernels as the batched pass.
 KERNEL_TRAFFIC = {"c1": {"raster": 70272, "shade": 747264}, "c2": {"raster": 5207872, "shade": 18389504},
-                  "c3": {"raster": 117440640, "shade": 339642240},
+                  "c3": {"raster": 117094912, "shade": 338297984},
                   "c4": {"raster": 825424640, "shade": 2104926976}}
 
 

@@ -57,8 +57,8 @@ CANDIDATES = tuple((bw, occ, cull, split, 0) for bw in (8, 16, 32) for occ in (0
 PINNED = {
     "c1": (16, 0, 0, 1, 0, 0, 1),
     "c2": (8, 8, 0, 1, 0, 0, 1),
-    "c3": (16, 0, 1, 1, 1),
-    "c3s": (16, 0, 1, 1, 1),
+    "c3": (16, 0, 1, 4, 1),
+    "c3s": (16, 0, 1, 4, 1),
     "c4": (16, 0, 0, 1, 1),
 }
 
