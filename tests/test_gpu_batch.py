@@ -53,6 +53,35 @@ def test_atlas_tiles_equal_views_alone(gpu_lib):
 
 
 @pytest.mark.gpu
+def test_atlas_of_many_draws(gpu_lib):
+    """600 views of 32x32 in one pass: more draws than the set-up keeps in
+    shared memory, so each warp finds its triangles' draws by its search of
+    the draw table; every tile equals its view rendered alone."""
+    from puresoft3d_gb300 import scenes as S
+    from puresoft3d_gb300.pipeline import PuresoftPipeline
+    views, size = 600, 32
+    batched, plain = S.scene_c4(views=views, size=size, tex_size=32, tri_min=20, tri_max=300)
+    atlas = PuresoftPipeline(batched.width, batched.height)
+    S.replay_setup(batched, atlas)
+    S.replay_frame(batched, atlas)
+    colour = atlas.readColour().copy()
+    depth = atlas.readDepth()[:, :batched.width].copy()
+    alone = PuresoftPipeline(size, size)
+    S.replay_setup(plain, alone)
+    covered = 0
+    for v, (ox, oy) in enumerate(batched.info["origins"]):
+        S.replay_ops(plain.info["view_frames"][v], alone)
+        c = alone.readColour()
+        d = alone.readDepth()[:, :size]
+        assert np.array_equal(_tile_colour(colour, ox, oy, size), c), "view %d colour" % v
+        assert np.array_equal(_tile_depth(depth, ox, oy, size).view(np.uint32), d.view(np.uint32)), "view %d" % v
+        covered += int((d < 1.0).sum())
+    assert covered > views * 50, "views cover too little to test anything"
+    atlas.close()
+    alone.close()
+
+
+@pytest.mark.gpu
 def test_views_alone_match_oracle(gpu_lib):
     """Every view alone against the oracle: depth bit-exact, colour within
     1 LSB."""
