@@ -444,7 +444,9 @@ def run_c4(args):
         "batched_over_plain": {"immediate": round(ips / WORLD / plain_ips, 2),
                                "graph": round(ips / WORLD / plain_graph_ips, 2)},
         "gfrag_per_s": round(frags * ips / views / 1e9, 4),
+        "gshaded_per_s": round(counts["shaded"] * ips / views / 1e9, 4),
         "fragments_per_step": frags,
+        "shaded_per_step": counts["shaded"],
         "gpu_launches": launches_per_frame * args.steps * K,
         "e2e": {"value": round(WORLD * views * e2e_steps / e2e_s, 2), "unit": "images/s",
                 "mode": "steps back to back on two pipelines (double-buffered): each uploads its inputs and "
@@ -743,7 +745,9 @@ def run_ours(args):
                    "l2": "256 MB scrub before each timed frame",
                    "parallelism": "replicas" if WORLD > 1 else "single GPU", "schedule": tune},
         "gfrag_per_s": round(frags * fps / WORLD / 1e9 * WORLD, 4),
+        "gshaded_per_s": round(counts["shaded"] * fps / 1e9, 4),
         "fragments_per_frame": frags,
+        "shaded_per_frame": counts["shaded"],
         "gpu_launches": launches_per_frame * args.steps * K,
         "e2e": {"value": round(fps_e2e, 3), "unit": "frames/s", "h2d_bytes_per_step": cb.input_bytes() * K,
                 "d2h_bytes_per_step": scene.width * scene.height * 4 * K,
