@@ -441,3 +441,46 @@ def test_tiny_and_thin_triangles(gpu_lib, bin_w):
     st = g.stats()
     assert (st["fragments"], st["fragments_passed"]) == o.fragments()
     assert int((ref["depth"] < 1.0).sum()) > 500  # the scene covers something
+
+
+def _soup_clip(n, seed, back=False):
+    """n small triangles over the target at random depths, in clip space, all
+    wound to face the viewer (back: all away from it)."""
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(-0.95, 0.95, size=(n, 1, 2))
+    d = rng.uniform(-0.15, 0.15, size=(n, 3, 2))
+    z = rng.uniform(-0.9, 0.9, size=(n, 3, 1))
+    t = np.concatenate([c + d, z, np.ones((n, 3, 1))], axis=2)
+    e1, e2 = t[:, 1, :2] - t[:, 0, :2], t[:, 2, :2] - t[:, 1, :2]
+    cz = e1[:, 0] * e2[:, 1] - e1[:, 1] * e2[:, 0]  # z of cross(v1 - v0, v2 - v1)
+    flip = (cz < 0) != back
+    t[flip] = t[flip][:, ::-1]
+    return t.reshape(-1, 4)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [1, 2, 127, 128, 129, 255, 256, 257, 1000, 3000])
+def test_setup_group_boundaries(gpu_lib, n):
+    """The set-up takes triangles in ticketed groups of 128 and emits a
+    group's pairs after setting up its next group: triangle counts around the
+    group size (a partial last group, one group, a group and one triangle,
+    more groups than blocks at once) give the oracle's depth bit for bit, its
+    colour within 1 LSB and the same fragment counts; so does a pass whose
+    triangles all face away under culling (no pair at all)."""
+    import kat_scenes as K
+    from puresoft3d_gb300.pipeline import PuresoftPipeline
+    w, h = 96, 64
+    for culled in (False, True):
+        clip = _soup_clip(n, 100 + n, back=culled)  # culled: every triangle faces away, culling on
+        scene = K._scene("groups_%d_%d" % (n, culled), w, h, clip, lit=True,
+                         behavior_on=K.S.FACE_CULLING if culled else 0)
+        g = PuresoftPipeline(w, h)
+        g.setFragmentCounting(True)
+        out = render(g, scene)
+        o = OraclePipeline(w, h)
+        ref = render(o, scene)
+        assert_depth_exact(out["depth"], ref["depth"], scene.name)
+        assert colour_diff(out["colour"], ref["colour"])[0] <= COLOUR_TOL
+        st = g.stats()
+        assert (st["fragments"], st["fragments_passed"]) == o.fragments(), scene.name
+        g.close()
